@@ -1,0 +1,1171 @@
+/*
+ * rfo.cpp -- CPU oracle for the bit-parallel string scorers (TEST INFRASTRUCTURE ONLY).
+ *
+ * A restatement of rapidfuzz-cpp v3.3.3 (paths below are relative to that project):
+ *   - pattern-match vectors           rapidfuzz/details/PatternMatchVector.hpp:62-221
+ *   - Levenshtein (Hyyro 2003, band, Myers block, dispatch, weights)
+ *                                     rapidfuzz/distance/Levenshtein_impl.hpp:85-155, 259-322, 419-505,
+ *                                     641-905, 1056-1089
+ *   - LCSseq / Indel (Hyyro 2004)     rapidfuzz/distance/LCSseq_impl.hpp:205-403, Indel_impl.hpp:14-66
+ *   - OSA (Hyyro 2003 + transpositions) rapidfuzz/distance/OSA_impl.hpp:34-74, 176-273, OSA.hpp:253-267
+ *   - Jaro / Jaro-Winkler             rapidfuzz/distance/Jaro_impl.hpp:32-454, JaroWinkler_impl.hpp:9-71
+ *   - formula chains of the bases     rapidfuzz/details/distance.hpp:52-76, 120-133, 177-203, 240-262,
+ *                                     304-317, 359-369, 421-460, 500-512, 552-563; common.hpp:50-53
+ *   - Multi* batch scorers            Levenshtein.hpp:297-419, LCSseq.hpp:77-195, Indel.hpp:77-146,
+ *                                     OSA.hpp:113-230, Jaro.hpp:64-193, JaroWinkler.hpp:75-166
+ *   - fuzz::ratio                     rapidfuzz/fuzz_impl.hpp:22-47, fuzz.hpp:50-95
+ *   - naive DP oracles                rapidfuzz_reference/{Levenshtein,LCSseq,OSA,Jaro}.hpp
+ *
+ * Two shortcuts of the reference are replaced by the bit-parallel paths they shortcut:
+ * mbleven (Levenshtein cutoff < 4, LCS max_misses < 5) and common-affix stripping.  Both
+ * return the same value under the cutoff contract d <= c ? d : c+1 (resp. s >= c ? s : 0),
+ * which the tests check against the reference itself.
+ *
+ * Build with -ffp-contract=off: the double formulas must not be fused into FMAs.
+ */
+#include "rfo.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <thread>
+#include <vector>
+
+namespace {
+
+typedef uint64_t u64;
+typedef int64_t i64;
+
+inline int popc(u64 x) { return __builtin_popcountll(x); }
+inline int ctz(u64 x) { return __builtin_ctzll(x); }
+inline u64 blsi(u64 x) { return x & (0 - x); }
+inline u64 blsr(u64 x) { return x & (x - 1); }
+inline i64 absdiff(i64 a, i64 b) { return a > b ? a - b : b - a; }
+inline i64 ceil_div(i64 a, i64 d) { return a / d + (a % d != 0); }
+inline u64 ceil_div_u(u64 a, u64 d) { return a / d + (a % d != 0); }
+
+/* ------------------------------------------------------------------ strings */
+
+template <typename C>
+struct Str {
+    const C* p;
+    i64 n;
+    u64 operator[](i64 i) const { return (u64)p[i]; }
+};
+
+/* call f(Str<C1>, Str<C2>) with the code-unit types named by the widths */
+template <typename F>
+auto with_strs(const void* a, i64 la, int ca, const void* b, i64 lb, int cb, F f) -> decltype(
+    f(Str<uint8_t>{nullptr, 0}, Str<uint8_t>{nullptr, 0}))
+{
+#define RFO_B(CA, TA)                                                                   \
+    switch (cb) {                                                                       \
+    case 1: return f(Str<TA>{(const TA*)a, la}, Str<uint8_t>{(const uint8_t*)b, lb});   \
+    case 2: return f(Str<TA>{(const TA*)a, la}, Str<uint16_t>{(const uint16_t*)b, lb}); \
+    case 4: return f(Str<TA>{(const TA*)a, la}, Str<uint32_t>{(const uint32_t*)b, lb}); \
+    default: return f(Str<TA>{(const TA*)a, la}, Str<uint64_t>{(const uint64_t*)b, lb}); \
+    }
+    switch (ca) {
+    case 1: RFO_B(1, uint8_t)
+    case 2: RFO_B(2, uint16_t)
+    case 4: RFO_B(4, uint32_t)
+    default: RFO_B(8, uint64_t)
+    }
+#undef RFO_B
+}
+
+template <typename S1, typename S2>
+bool str_equal(const S1& a, const S2& b)
+{
+    if (a.n != b.n) return false;
+    for (i64 i = 0; i < a.n; ++i)
+        if (a[i] != b[i]) return false;
+    return true;
+}
+
+/* ------------------------------------------------------- pattern-match vectors
+ * PM[c] bit i (word i/64) is set when s1[i] == c.  Code units below 256 index a
+ * dense table; larger ones go through an open-addressing table (PatternMatchVector.hpp:62-221
+ * uses a 128-slot CPython-probing map per word for these; a linear-probing table
+ * holds the same sets). */
+struct PM {
+    i64 words = 0;
+    std::vector<u64> lo; /* [256][words] */
+    u64 cap = 0;         /* power of two, or 0 */
+    std::vector<u64> keys;
+    std::vector<u64> vals; /* [cap][words] */
+
+    static u64 slot_of(u64 c, u64 cap) { return (c * 0x9E3779B97F4A7C15ull) >> 20 & (cap - 1); }
+
+    template <typename S>
+    void build(const S& s)
+    {
+        words = ceil_div(s.n, 64);
+        lo.assign(256 * (size_t)std::max<i64>(words, 1), 0);
+        i64 hi = 0;
+        for (i64 i = 0; i < s.n; ++i)
+            hi += s[i] >= 256;
+        cap = 0;
+        if (hi) {
+            cap = 8;
+            while (cap < (u64)(2 * hi)) cap <<= 1;
+            keys.assign(cap, 0);
+            vals.assign(cap * (size_t)words, 0);
+        }
+        for (i64 i = 0; i < s.n; ++i) {
+            u64 c = s[i];
+            u64 bit = 1ull << (i % 64);
+            if (c < 256) {
+                lo[c * words + i / 64] |= bit;
+            }
+            else {
+                u64 k = slot_of(c, cap);
+                while (keys[k] != 0 && keys[k] != c) k = (k + 1) & (cap - 1);
+                keys[k] = c;
+                vals[k * words + i / 64] |= bit;
+            }
+        }
+    }
+
+    u64 get(i64 w, u64 c) const
+    {
+        if (c < 256) return lo[c * words + w];
+        if (!cap) return 0;
+        u64 k = slot_of(c, cap);
+        while (true) {
+            if (keys[k] == c) return vals[k * words + w];
+            if (keys[k] == 0) return 0;
+            k = (k + 1) & (cap - 1);
+        }
+    }
+};
+
+/* ================================================================ Levenshtein */
+
+/* single word, s1 length 1..64 (Levenshtein_impl.hpp:259-322) */
+template <typename S2>
+i64 lev_hyyro_word(const PM& pm, i64 m, const S2& t)
+{
+    u64 VP = ~0ull, VN = 0;
+    i64 dist = m;
+    const u64 top = 1ull << (m - 1);
+    for (i64 j = 0; j < t.n; ++j) {
+        u64 X = pm.get(0, t[j]);
+        u64 D0 = (((X & VP) + VP) ^ VP) | X | VN;
+        u64 HP = VN | ~(D0 | VP);
+        u64 HN = D0 & VP;
+        dist += (HP & top) != 0;
+        dist -= (HN & top) != 0;
+        HP = (HP << 1) | 1;
+        HN = HN << 1;
+        VP = HN | ~(D0 | HP);
+        VN = HP & D0;
+    }
+    return dist;
+}
+
+/* diagonal band of one word, 2*max+1 <= 64, s1 > 64 (Levenshtein_impl.hpp:419-505) */
+template <typename S2>
+i64 lev_small_band(const PM& pm, i64 m, const S2& t, i64 max)
+{
+    u64 VP = ~0ull << (64 - max - 1);
+    u64 VN = 0;
+    const i64 words = pm.words;
+    i64 dist = max;
+    const u64 diag = 1ull << 63;
+    u64 horiz = 1ull << 62;
+    i64 start = max + 1 - 64;
+    const i64 break_score = 2 * max + t.n - m;
+
+    auto pm_window = [&](u64 c) -> u64 {
+        if (start < 0) return pm.get(0, c) << (-start);
+        i64 w = start / 64, b = start % 64;
+        u64 x = pm.get(w, c) >> b;
+        if (w + 1 < words && b != 0) x |= pm.get(w + 1, c) << (64 - b);
+        return x;
+    };
+
+    i64 j = 0;
+    if (m > max) {
+        for (; j < m - max; ++j, ++start) {
+            u64 X = pm_window(t[j]);
+            u64 D0 = (((X & VP) + VP) ^ VP) | X | VN;
+            u64 HP = VN | ~(D0 | VP);
+            u64 HN = D0 & VP;
+            dist += (D0 & diag) == 0;
+            if (dist > break_score) return max + 1;
+            VP = HN | ~((D0 >> 1) | HP);
+            VN = (D0 >> 1) & HP;
+        }
+    }
+    for (; j < t.n; ++j, ++start) {
+        u64 X = pm_window(t[j]);
+        u64 D0 = (((X & VP) + VP) ^ VP) | X | VN;
+        u64 HP = VN | ~(D0 | VP);
+        u64 HN = D0 & VP;
+        dist += (HP & horiz) != 0;
+        dist -= (HN & horiz) != 0;
+        horiz >>= 1;
+        if (dist > break_score) return max + 1;
+        VP = HN | ~((D0 >> 1) | HP);
+        VN = (D0 >> 1) & HP;
+    }
+    return dist <= max ? dist : max + 1;
+}
+
+/* Myers/Hyyro multi-word with the Ukkonen band of the reference (Levenshtein_impl.hpp:641-850) */
+template <typename S2>
+i64 lev_block(const PM& pm, i64 m, const S2& t, i64 max)
+{
+    const i64 n = t.n;
+    if (max < absdiff(m, n)) return max + 1;
+    const i64 words = pm.words;
+    std::vector<u64> VP(words, ~0ull), VN(words, 0);
+    std::vector<i64> score(words);
+    const u64 last = 1ull << ((m - 1) % 64);
+    for (i64 w = 0; w < words - 1; ++w) score[w] = (w + 1) * 64;
+    score[words - 1] = m;
+
+    max = std::min(max, std::max(m, n));
+    i64 first = 0;
+    i64 lastb = std::min(words, ceil_div(std::min(max, (max + m - n) / 2) + 1, 64)) - 1;
+
+    auto row_of = [&](i64 w) -> i64 { return (w + 1 == words) ? m - 1 : (w + 1) * 64 - 1; };
+
+    for (i64 row = 0; row < n; ++row) {
+        const u64 c = t[row];
+        u64 hp_carry = 1, hn_carry = 0;
+        auto advance = [&](i64 w) -> i64 {
+            u64 X = pm.get(w, c) | hn_carry;
+            u64 vp = VP[w], vn = VN[w];
+            u64 D0 = (((X & vp) + vp) ^ vp) | X | vn;
+            u64 HP = vn | ~(D0 | vp);
+            u64 HN = D0 & vp;
+            u64 hp_in = hp_carry, hn_in = hn_carry;
+            if (w < words - 1) {
+                hp_carry = HP >> 63;
+                hn_carry = HN >> 63;
+            }
+            else {
+                hp_carry = (HP & last) != 0;
+                hn_carry = (HN & last) != 0;
+            }
+            HP = (HP << 1) | hp_in;
+            HN = (HN << 1) | hn_in;
+            VP[w] = HN | ~(D0 | HP);
+            VN[w] = HP & D0;
+            return (i64)hp_carry - (i64)hn_carry;
+        };
+
+        for (i64 w = first; w <= lastb; ++w) score[w] += advance(w);
+
+        max = std::min(max, score[lastb] + std::max(n - row - 1, m - (1 + lastb) * 64 + 2));
+
+        if (lastb + 1 < words) {
+            i64 cond = (max + 128 + row + m) - (score[lastb] + 2 + n);
+            if (row_of(lastb) < cond) {
+                ++lastb;
+                VP[lastb] = ~0ull;
+                VN[lastb] = 0;
+                i64 chars = (lastb + 1 == words) ? ((m - 1) % 64 + 1) : 64;
+                score[lastb] = score[lastb - 1] + chars - (i64)hp_carry + (i64)hn_carry;
+                score[lastb] += advance(lastb);
+            }
+        }
+        for (; lastb >= first; --lastb) {
+            bool c1 = score[lastb] < max + 64;
+            i64 cond = (max + 128 + row + m + 1) - (score[lastb] + 2 + n);
+            bool c2 = row_of(lastb) <= cond;
+            if (c1 && c2) break;
+        }
+        for (; first <= lastb; ++first) {
+            bool c1 = score[first] < max + 64;
+            i64 cond = (score[first] + m + row) - (max + n);
+            bool c2 = row_of(first) >= cond;
+            if (c1 && c2) break;
+        }
+        if (lastb < first) return max + 1;
+    }
+    i64 dist = score[words - 1];
+    return dist > max ? max + 1 : dist;
+}
+
+/* uniform Levenshtein with a cached pattern (Levenshtein_impl.hpp:852-905) */
+template <typename S1, typename S2>
+u64 lev_uniform_cached(const PM& pm, const S1& s1, const S2& s2, u64 cutoff, u64 hint)
+{
+    const i64 m = s1.n, n = s2.n;
+    cutoff = std::min<u64>(cutoff, (u64)std::max(m, n));
+    if (hint < 31) hint = 31;
+    if (cutoff == 0) return str_equal(s1, s2) ? 0 : 1;
+    if (cutoff < (u64)absdiff(m, n)) return cutoff + 1;
+    if (m == 0) return (u64)n <= cutoff ? (u64)n : cutoff + 1;
+    const i64 k = (i64)cutoff;
+    if (m < 65) {
+        i64 d = lev_hyyro_word(pm, m, s2);
+        return d <= k ? (u64)d : cutoff + 1;
+    }
+    if (cutoff >= 4) {
+        if (std::min<i64>(m, 2 * k + 1) <= 64) return (u64)lev_small_band(pm, m, s2, k);
+        while (hint < cutoff) {
+            i64 h = (i64)hint;
+            i64 s = std::min<i64>(m, 2 * h + 1) <= 64 ? lev_small_band(pm, m, s2, h) : lev_block(pm, m, s2, h);
+            if (s <= h) return (u64)s;
+            if (std::numeric_limits<u64>::max() / 2 < hint) break;
+            hint *= 2;
+        }
+    }
+    return (u64)lev_block(pm, m, s2, k);
+}
+
+/* LCS: Hyyro 2004 full (LCSseq_impl.hpp:205-260) and banded (:262-333) */
+template <typename S2>
+i64 lcs_full(const PM& pm, const S2& t)
+{
+    const i64 words = pm.words;
+    std::vector<u64> S(words, ~0ull);
+    for (i64 j = 0; j < t.n; ++j) {
+        const u64 c = t[j];
+        u64 carry = 0;
+        for (i64 w = 0; w < words; ++w) {
+            u64 M = pm.get(w, c);
+            u64 u = S[w] & M;
+            u64 x = S[w] + u;
+            u64 c1 = x < u;
+            u64 x2 = x + carry;
+            u64 c2 = x2 < carry;
+            carry = c1 | c2;
+            S[w] = x2 | (S[w] - u);
+        }
+    }
+    i64 sim = 0;
+    for (i64 w = 0; w < words; ++w) sim += popc(~S[w]);
+    return sim;
+}
+
+template <typename S2>
+i64 lcs_blockwise(const PM& pm, i64 m, const S2& t, i64 cutoff)
+{
+    const i64 words = pm.words;
+    std::vector<u64> S(words, ~0ull);
+    const i64 left = m - cutoff, right = t.n - cutoff;
+    i64 first = 0, last = std::min(words, ceil_div(left + 1, 64));
+    for (i64 row = 0; row < t.n; ++row) {
+        const u64 c = t[row];
+        u64 carry = 0;
+        for (i64 w = first; w < last; ++w) {
+            u64 M = pm.get(w, c);
+            u64 s = S[w];
+            u64 u = s & M;
+            u64 x = s + u;
+            u64 c1 = x < u;
+            u64 x2 = x + carry;
+            u64 c2 = x2 < carry;
+            carry = c1 | c2;
+            S[w] = x2 | (s - u);
+        }
+        if (row > right) first = (row - right) / 64;
+        if (row + 1 + left <= m) last = ceil_div(row + 1 + left, 64);
+    }
+    i64 sim = 0;
+    for (u64 s : S) sim += popc(~s);
+    return sim;
+}
+
+/* lcs_seq_similarity with a cached pattern (LCSseq_impl.hpp:335-403) */
+template <typename S1, typename S2>
+u64 lcs_cached(const PM& pm, const S1& s1, const S2& s2, u64 cutoff)
+{
+    const i64 m = s1.n, n = s2.n;
+    if (cutoff > (u64)m || cutoff > (u64)n) return 0;
+    const i64 c = (i64)cutoff;
+    const i64 max_misses = m + n - 2 * c;
+    if (max_misses == 0 || (max_misses == 1 && m == n)) return str_equal(s1, s2) ? (u64)m : 0;
+    if (max_misses < absdiff(m, n)) return 0;
+    if (m == 0) return 0;
+    /* max_misses < 5 goes through affix stripping + mbleven in the reference (exact under
+     * the cutoff); the unbanded run gives the same value.  The banded run is only taken
+     * where the reference takes it. */
+    const i64 full_band = (m - c) + 1 + (n - c);
+    const i64 fbw = std::min(pm.words, full_band / 64 + 2);
+    i64 sim = (max_misses >= 5 && fbw < pm.words) ? lcs_blockwise(pm, m, s2, c) : lcs_full(pm, s2);
+    return sim >= c ? (u64)sim : 0;
+}
+
+/* ======================================================================== OSA */
+
+template <typename S2>
+i64 osa_word(const PM& pm, i64 m, const S2& t)
+{
+    u64 VP = ~0ull, VN = 0, D0 = 0, PMold = 0;
+    i64 dist = m;
+    const u64 top = 1ull << (m - 1);
+    for (i64 j = 0; j < t.n; ++j) {
+        u64 X = pm.get(0, t[j]);
+        u64 TR = (((~D0) & X) << 1) & PMold;
+        D0 = (((X & VP) + VP) ^ VP) | X | VN;
+        D0 |= TR;
+        u64 HP = VN | ~(D0 | VP);
+        u64 HN = D0 & VP;
+        dist += (HP & top) != 0;
+        dist -= (HN & top) != 0;
+        HP = (HP << 1) | 1;
+        HN = HN << 1;
+        VP = HN | ~(D0 | HP);
+        VN = HP & D0;
+        PMold = X;
+    }
+    return dist;
+}
+
+template <typename S2>
+i64 osa_block(const PM& pm, i64 m, const S2& t)
+{
+    struct Row {
+        u64 VP = ~0ull, VN = 0, D0 = 0, PM = 0;
+    };
+    const i64 words = pm.words;
+    const u64 last = 1ull << ((m - 1) % 64);
+    i64 dist = m;
+    std::vector<Row> oldr(words + 1), newr(words + 1);
+    for (i64 j = 0; j < t.n; ++j) {
+        const u64 c = t[j];
+        u64 hp_carry = 1, hn_carry = 0;
+        for (i64 w = 0; w < words; ++w) {
+            u64 VN = oldr[w + 1].VN, VP = oldr[w + 1].VP, D0 = oldr[w + 1].D0;
+            u64 D0_prev_word = oldr[w].D0;
+            u64 PM_old = oldr[w + 1].PM;
+            u64 PM_prev_word = newr[w].PM;
+            u64 X = pm.get(w, c);
+            u64 TR = ((((~D0) & X) << 1) | (((~D0_prev_word) & PM_prev_word) >> 63)) & PM_old;
+            u64 Xc = X | hn_carry;
+            D0 = (((Xc & VP) + VP) ^ VP) | Xc | VN | TR;
+            u64 HP = VN | ~(D0 | VP);
+            u64 HN = D0 & VP;
+            if (w == words - 1) {
+                dist += (HP & last) != 0;
+                dist -= (HN & last) != 0;
+            }
+            u64 hp_in = hp_carry;
+            hp_carry = HP >> 63;
+            HP = (HP << 1) | hp_in;
+            u64 hn_in = hn_carry;
+            hn_carry = HN >> 63;
+            HN = (HN << 1) | hn_in;
+            newr[w + 1].VP = HN | ~(D0 | HP);
+            newr[w + 1].VN = HP & D0;
+            newr[w + 1].D0 = D0;
+            newr[w + 1].PM = X;
+        }
+        std::swap(newr, oldr);
+    }
+    return dist;
+}
+
+/* CachedOSA::_distance (OSA.hpp:253-267) */
+template <typename S1, typename S2>
+u64 osa_cached(const PM& pm, const S1& s1, const S2& s2, u64 cutoff)
+{
+    u64 res;
+    if (s1.n == 0) res = (u64)s2.n;
+    else if (s2.n == 0) res = (u64)s1.n;
+    else if (s1.n < 64) res = (u64)osa_word(pm, s1.n, s2);
+    else res = (u64)osa_block(pm, s1.n, s2);
+    return res <= cutoff ? res : cutoff + 1;
+}
+
+/* ======================================================================= Jaro */
+
+/* greedy flagging over words (Jaro_impl.hpp:94-315): every text character takes
+ * the first unflagged equal pattern character inside its window */
+template <typename S1, typename S2>
+void jaro_counts_pm(const PM& pm, const S1& P, const S2& T, i64* common, i64* transp)
+{
+    const i64 pl = P.n, tl = T.n;
+    *common = 0;
+    *transp = 0;
+    if (!pl || !tl) return;
+    i64 bound = std::max(pl, tl) / 2;
+    if (bound > 0) --bound;
+    const i64 pw = pm.words;
+    std::vector<u64> pflag(pw, 0), tflag(ceil_div(tl, 64), 0);
+    for (i64 j = 0; j < tl; ++j) {
+        i64 lo = j >= bound ? j - bound : 0;
+        i64 hi = std::min(j + bound, pl - 1);
+        if (lo > hi) continue;
+        const u64 c = T[j];
+        for (i64 w = lo / 64; w <= hi / 64; ++w) {
+            u64 mask = ~0ull;
+            if (w == lo / 64) mask &= ~0ull << (lo % 64);
+            if (w == hi / 64) mask &= (hi % 64 == 63) ? ~0ull : ((1ull << (hi % 64 + 1)) - 1);
+            u64 x = pm.get(w, c) & mask & ~pflag[w];
+            if (x) {
+                pflag[w] |= blsi(x);
+                tflag[j / 64] |= 1ull << (j % 64);
+                break;
+            }
+        }
+    }
+    i64 cc = 0;
+    for (u64 f : pflag) cc += popc(f);
+    *common = cc;
+    i64 pwi = 0;
+    u64 pf = pflag.empty() ? 0 : pflag[0];
+    i64 t = 0;
+    for (i64 tw = 0; tw < (i64)tflag.size(); ++tw) {
+        u64 tf = tflag[tw];
+        while (tf) {
+            while (!pf) pf = pflag[++pwi];
+            i64 j = tw * 64 + ctz(tf);
+            u64 bit = blsi(pf);
+            t += (pm.get(pwi, T[j]) & bit) == 0;
+            tf = blsr(tf);
+            pf ^= bit;
+        }
+    }
+    *transp = t;
+}
+
+double jaro_formula(i64 pl, i64 tl, i64 common, i64 transp)
+{
+    transp /= 2;
+    double sim = 0;
+    sim += (double)common / (double)pl;
+    sim += (double)common / (double)tl;
+    sim += ((double)common - (double)transp) / (double)common;
+    return sim / 3.0;
+}
+
+bool jaro_length_filter(i64 pl, i64 tl, double cutoff)
+{
+    if (!tl || !pl) return false;
+    double mn = (double)std::min(pl, tl);
+    double sim = mn / (double)pl + mn / (double)tl + 1.0;
+    sim /= 3.0;
+    return sim >= cutoff;
+}
+
+bool jaro_common_filter(i64 pl, i64 tl, i64 common, double cutoff)
+{
+    if (!common) return false;
+    double sim = 0;
+    sim += (double)common / (double)pl;
+    sim += (double)common / (double)tl;
+    sim += 1.0;
+    sim /= 3.0;
+    return sim >= cutoff;
+}
+
+/* jaro_similarity (Jaro_impl.hpp:409-454) with its filters, from exact counts */
+double jaro_from_counts(i64 pl, i64 tl, i64 common, i64 transp, double cutoff)
+{
+    if (cutoff > 1.0) return 0.0;
+    if (!pl && !tl) return 1.0;
+    if (!jaro_length_filter(pl, tl, cutoff)) return 0.0;
+    if (pl == 1 && tl == 1) return (double)(common == 1);
+    if (!jaro_common_filter(pl, tl, common, cutoff)) return 0.0;
+    double sim = jaro_formula(pl, tl, common, transp);
+    return sim >= cutoff ? sim : 0;
+}
+
+template <typename S1, typename S2>
+i64 common_prefix4(const S1& P, const S2& T)
+{
+    i64 mx = std::min<i64>(std::min(P.n, T.n), 4);
+    i64 k = 0;
+    for (; k < mx; ++k)
+        if (T[k] != P[k]) break;
+    return k;
+}
+
+/* jaro_winkler_similarity (JaroWinkler_impl.hpp:41-71) */
+template <typename JaroFn>
+double jw_chain(i64 prefix, double pw, double cutoff, JaroFn jaro)
+{
+    double jc = cutoff;
+    if (jc > 0.7) {
+        double ps = (double)prefix * pw;
+        if (ps >= 1.0) jc = 0.7;
+        else jc = std::max(0.7, (ps - jc) / (ps - 1.0));
+    }
+    double sim = jaro(jc);
+    if (sim > 0.7) {
+        sim += (double)prefix * pw * (1.0 - sim);
+        sim = std::min(sim, 1.0);
+    }
+    return sim >= cutoff ? sim : 0;
+}
+
+/* MultiJaro (jaro_similarity_simd, Jaro_impl.hpp:818-840, 666-709) from exact counts */
+double multi_jaro_from_counts(i64 pl, i64 tl, i64 common, i64 transp, double cutoff)
+{
+    if (cutoff > 1.0) return 0.0;
+    if (tl == 0) return pl ? 0.0 : 1.0;
+    if (!jaro_common_filter(pl, tl, common, cutoff)) return 0.0;
+    double sim = jaro_formula(pl, tl, common, transp);
+    return sim >= cutoff ? sim : 0;
+}
+
+/* MultiJaroWinkler::_similarity (JaroWinkler.hpp:123-145) */
+double multi_jw(double jaro_sim, i64 prefix, double pw, double cutoff)
+{
+    double s = jaro_sim;
+    if (s > 0.7) {
+        s += (double)prefix * pw * (1.0 - s);
+        s = std::min(s, 1.0);
+    }
+    if (s < cutoff) s = 0.0;
+    return s;
+}
+
+/* ============================================================ formula chains */
+
+inline double norm_sim_to_norm_dist(double c) { return std::min(1.0, 1.0 - c + 0.00001); }
+
+u64 lev_maximum(u64 l1, u64 l2, const rfo_params* w)
+{
+    u64 ins = (u64)w->insert_cost, del = (u64)w->delete_cost, rep = (u64)w->replace_cost;
+    u64 mx = l1 * del + l2 * ins;
+    if (l1 >= l2) mx = std::min(mx, l2 * rep + (l1 - l2) * del);
+    else mx = std::min(mx, l1 * rep + (l2 - l1) * ins);
+    return mx;
+}
+
+/* distance-type chain (DistanceBase / CachedDistanceBase, distance.hpp:52-76, 120-133,
+ * 240-262, 304-317); dist(c) is the metric's _distance under cutoff c */
+template <typename DistFn>
+void chain_dist(int op, u64 M, DistFn dist, u64 ci, double cf, i64* oi, double* of)
+{
+    auto ndist = [&](double c) {
+        u64 cd = (u64)std::ceil((double)M * c);
+        u64 d = dist(cd);
+        double nd = M != 0 ? (double)d / (double)M : 0.0;
+        return nd <= c ? nd : 1.0;
+    };
+    switch (op) {
+    case RFO_DISTANCE: *oi = (i64)dist(ci); break;
+    case RFO_SIMILARITY:
+        if (ci > M) *oi = 0;
+        else {
+            u64 s = M - dist(M - ci);
+            *oi = s >= ci ? (i64)s : 0;
+        }
+        break;
+    case RFO_NORM_DISTANCE: *of = ndist(cf); break;
+    default: {
+        double nd = ndist(norm_sim_to_norm_dist(cf));
+        double ns = 1.0 - nd;
+        *of = ns >= cf ? ns : 0.0;
+    }
+    }
+}
+
+/* similarity-type chain over integers (SimilarityBase / CachedSimilarityBase, distance.hpp:177-203,
+ * 359-369); sim(c) is _similarity under cutoff c */
+template <typename SimFn>
+void chain_sim(int op, u64 M, SimFn sim, u64 ci, double cf, i64* oi, double* of)
+{
+    auto dist = [&](u64 c) -> u64 {
+        u64 cs = M >= c ? M - c : 0;
+        u64 d = M - sim(cs);
+        return d <= c ? d : c + 1;
+    };
+    auto ndist = [&](double c) {
+        u64 cd = (u64)std::ceil((double)M * c);
+        u64 d = dist(cd);
+        double nd = M != 0 ? (double)d / (double)M : 0.0;
+        return nd <= c ? nd : 1.0;
+    };
+    switch (op) {
+    case RFO_DISTANCE: *oi = (i64)dist(ci); break;
+    case RFO_SIMILARITY: *oi = (i64)sim(ci); break;
+    case RFO_NORM_DISTANCE: *of = ndist(cf); break;
+    default: {
+        double nd = ndist(norm_sim_to_norm_dist(cf));
+        double ns = 1.0 - nd;
+        *of = ns >= cf ? ns : 0.0;
+    }
+    }
+}
+
+/* similarity-type chain over doubles with maximum 1.0 (Jaro / Jaro-Winkler) */
+template <typename SimFn>
+void chain_fsim(int op, SimFn sim, double cf, double* of)
+{
+    auto dist = [&](double c) -> double {
+        double cs = 1.0 >= c ? 1.0 - c : 0.0;
+        double d = 1.0 - sim(cs);
+        return d <= c ? d : 1.0;
+    };
+    auto ndist = [&](double c) {
+        double cd = std::ceil(1.0 * c);
+        double nd = dist(cd) / 1.0;
+        return nd <= c ? nd : 1.0;
+    };
+    switch (op) {
+    case RFO_DISTANCE: *of = dist(cf); break;
+    case RFO_SIMILARITY: *of = sim(cf); break;
+    case RFO_NORM_DISTANCE: *of = ndist(cf); break;
+    default: {
+        double nd = ndist(norm_sim_to_norm_dist(cf));
+        double ns = 1.0 - nd;
+        *of = ns >= cf ? ns : 0.0;
+    }
+    }
+}
+
+/* Multi* chains (MultiDistanceBase / MultiSimilarityBase / MultiNormalizedMetricBase,
+ * distance.hpp:421-460, 500-512, 552-563): exact values, cutoff applied after */
+void chain_multi_dist(int op, u64 M, u64 D, u64 ci, double cf, i64* oi, double* of)
+{
+    switch (op) {
+    case RFO_DISTANCE: *oi = (i64)(D <= ci ? D : ci + 1); break;
+    case RFO_SIMILARITY: {
+        u64 s = M - D;
+        *oi = s >= ci ? (i64)s : 0;
+        break;
+    }
+    case RFO_NORM_DISTANCE: {
+        double nd = M != 0 ? (double)D / (double)M : 0.0;
+        *of = nd <= cf ? nd : 1.0;
+        break;
+    }
+    default: {
+        double nd = M != 0 ? (double)D / (double)M : 0.0;
+        nd = nd <= 1.0 ? nd : 1.0;
+        double ns = 1.0 - nd;
+        *of = ns >= cf ? ns : 0.0;
+    }
+    }
+}
+
+void chain_multi_sim(int op, u64 M, u64 S, u64 ci, double cf, i64* oi, double* of)
+{
+    switch (op) {
+    case RFO_SIMILARITY: *oi = S >= ci ? (i64)S : 0; break;
+    case RFO_DISTANCE: {
+        u64 d = M - S;
+        *oi = (i64)(d <= ci ? d : ci + 1);
+        break;
+    }
+    case RFO_NORM_DISTANCE: {
+        u64 d = M - S;
+        double nd = M != 0 ? (double)d / (double)M : 0.0;
+        *of = nd <= cf ? nd : 1.0;
+        break;
+    }
+    default: {
+        u64 d = M - S;
+        double nd = M != 0 ? (double)d / (double)M : 0.0;
+        nd = nd <= 1.0 ? nd : 1.0;
+        double ns = 1.0 - nd;
+        *of = ns >= cf ? ns : 0.0;
+    }
+    }
+}
+
+/* sim_at(c) is the Multi scorer's _similarity under cutoff c */
+template <typename SimAt>
+void chain_multi_fsim(int op, SimAt sim_at, double cf, double* of)
+{
+    switch (op) {
+    case RFO_SIMILARITY: *of = sim_at(cf); break;
+    case RFO_DISTANCE: {
+        double d = 1.0 - sim_at(0.0);
+        *of = d <= cf ? d : 1.0;
+        break;
+    }
+    case RFO_NORM_DISTANCE: {
+        double d = 1.0 - sim_at(0.0);
+        d = d <= 1.0 ? d : 1.0;
+        *of = d <= cf ? d : 1.0;
+        break;
+    }
+    default: {
+        double d = 1.0 - sim_at(0.0);
+        d = d <= 1.0 ? d : 1.0;
+        double ns = 1.0 - d;
+        *of = ns >= cf ? ns : 0.0;
+    }
+    }
+}
+
+/* =============================================== exact values with a cached PM */
+
+template <typename S1, typename S2>
+u64 lev_weighted_cached(const PM& pm, const S1& s1, const S2& s2, const rfo_params* w, u64 cutoff, u64 hint);
+
+/* generalized Wagner-Fischer (Levenshtein_impl.hpp:85-155), affix stripped */
+template <typename S1, typename S2>
+u64 lev_generalized(const S1& s1in, const S2& s2in, const rfo_params* w, u64 max)
+{
+    const u64 ins = (u64)w->insert_cost, del = (u64)w->delete_cost, rep = (u64)w->replace_cost;
+    u64 min_edits = s1in.n > s2in.n ? (u64)(s1in.n - s2in.n) * del : (u64)(s2in.n - s1in.n) * ins;
+    if (min_edits > max) return max + 1;
+    i64 a0 = 0, a1 = s1in.n, b0 = 0, b1 = s2in.n;
+    while (a0 < a1 && b0 < b1 && s1in[a0] == s2in[b0]) ++a0, ++b0;
+    while (a0 < a1 && b0 < b1 && s1in[a1 - 1] == s2in[b1 - 1]) --a1, --b1;
+    const i64 m = a1 - a0;
+    std::vector<u64> cache(m + 1);
+    for (i64 i = 0; i <= m; ++i) cache[i] = (u64)i * del;
+    for (i64 j = b0; j < b1; ++j) {
+        u64 temp = cache[0];
+        cache[0] += ins;
+        for (i64 i = 0; i < m; ++i) {
+            if (s1in[a0 + i] != s2in[j]) temp = std::min({cache[i] + del, cache[i + 1] + ins, temp + rep});
+            std::swap(cache[i + 1], temp);
+        }
+    }
+    u64 d = cache[m];
+    return d <= max ? d : max + 1;
+}
+
+/* levenshtein_distance with weights (Levenshtein_impl.hpp:1056-1089; CachedLevenshtein
+ * Levenshtein.hpp:445-477 takes the same branches with the cached pattern) */
+template <typename S1, typename S2>
+u64 lev_weighted_cached(const PM& pm, const S1& s1, const S2& s2, const rfo_params* w, u64 cutoff, u64 hint)
+{
+    const u64 ins = (u64)w->insert_cost, del = (u64)w->delete_cost, rep = (u64)w->replace_cost;
+    if (ins == del) {
+        if (ins == 0) return 0;
+        if (ins == rep) {
+            u64 d = lev_uniform_cached(pm, s1, s2, ceil_div_u(cutoff, ins), ceil_div_u(hint, ins)) * ins;
+            return d <= cutoff ? d : cutoff + 1;
+        }
+        if (rep >= ins + del) {
+            u64 nc = ceil_div_u(cutoff, ins);
+            u64 M = (u64)(s1.n + s2.n);
+            u64 lcs_cut = (M / 2 >= nc) ? M / 2 - nc : 0;
+            u64 l = lcs_cached(pm, s1, s2, lcs_cut);
+            u64 di = M - 2 * l;
+            di = di <= nc ? di : nc + 1;
+            u64 d = di * ins;
+            return d <= cutoff ? d : cutoff + 1;
+        }
+    }
+    return lev_generalized(s1, s2, w, cutoff);
+}
+
+/* Indel::_distance via the cached LCS (Indel.hpp:170-179) */
+template <typename S1, typename S2>
+u64 indel_cached(const PM& pm, const S1& s1, const S2& s2, u64 cutoff)
+{
+    u64 M = (u64)(s1.n + s2.n);
+    u64 lcs_cut = (M / 2 >= cutoff) ? M / 2 - cutoff : 0;
+    u64 l = lcs_cached(pm, s1, s2, lcs_cut);
+    u64 d = M - 2 * l;
+    return d <= cutoff ? d : cutoff + 1;
+}
+
+/* one scorer call with a prebuilt pattern of s1 */
+template <typename S1, typename S2>
+int score_with_pm(int metric, int op, int form, const PM& pm, const S1& s1, const S2& s2, const rfo_params* p,
+                  u64 ci, double cf, i64* oi, double* of)
+{
+    const u64 l1 = (u64)s1.n, l2 = (u64)s2.n;
+    const u64 HINT = std::numeric_limits<u64>::max();
+    if (form == RFO_FORM_MULTI) {
+        switch (metric) {
+        case RFO_LEVENSHTEIN: {
+            if (p->delete_cost != 1 || p->insert_cost != 1 || p->replace_cost > 2) return -1;
+            u64 D = lev_uniform_cached(pm, s1, s2, HINT, HINT);
+            chain_multi_dist(op, lev_maximum(l1, l2, p), D, ci, cf, oi, of);
+            return 0;
+        }
+        case RFO_OSA: {
+            u64 D = osa_cached(pm, s1, s2, HINT);
+            chain_multi_dist(op, std::max(l1, l2), D, ci, cf, oi, of);
+            return 0;
+        }
+        case RFO_INDEL: {
+            u64 L = s1.n ? (u64)lcs_full(pm, s2) : 0;
+            chain_multi_dist(op, l1 + l2, l1 + l2 - 2 * L, ci, cf, oi, of);
+            return 0;
+        }
+        case RFO_LCSSEQ: {
+            u64 L = s1.n ? (u64)lcs_full(pm, s2) : 0;
+            chain_multi_sim(op, std::max(l1, l2), L, ci, cf, oi, of);
+            return 0;
+        }
+        case RFO_RATIO: {
+            if (op != RFO_SIMILARITY) return -1;
+            u64 L = s1.n ? (u64)lcs_full(pm, s2) : 0;
+            double r;
+            chain_multi_dist(RFO_NORM_SIMILARITY, l1 + l2, l1 + l2 - 2 * L, 0, cf / 100.0, oi, &r);
+            *of = r * 100.0;
+            return 0;
+        }
+        case RFO_JARO:
+        case RFO_JARO_WINKLER: {
+            i64 C, T;
+            jaro_counts_pm(pm, s1, s2, &C, &T);
+            i64 prefix = common_prefix4(s1, s2);
+            auto sim_at = [&](double c) {
+                if (metric == RFO_JARO) return multi_jaro_from_counts(s1.n, s2.n, C, T, c);
+                double js = multi_jaro_from_counts(s1.n, s2.n, C, T, std::min(0.7, c));
+                return multi_jw(js, prefix, p->prefix_weight, c);
+            };
+            chain_multi_fsim(op, sim_at, cf, of);
+            return 0;
+        }
+        }
+        return -1;
+    }
+
+    switch (metric) {
+    case RFO_LEVENSHTEIN: {
+        auto dist = [&](u64 c) { return lev_weighted_cached(pm, s1, s2, p, c, HINT); };
+        chain_dist(op, lev_maximum(l1, l2, p), dist, ci, cf, oi, of);
+        return 0;
+    }
+    case RFO_INDEL: {
+        auto dist = [&](u64 c) { return indel_cached(pm, s1, s2, c); };
+        chain_dist(op, l1 + l2, dist, ci, cf, oi, of);
+        return 0;
+    }
+    case RFO_OSA: {
+        auto dist = [&](u64 c) { return osa_cached(pm, s1, s2, c); };
+        chain_dist(op, std::max(l1, l2), dist, ci, cf, oi, of);
+        return 0;
+    }
+    case RFO_LCSSEQ: {
+        auto sim = [&](u64 c) { return lcs_cached(pm, s1, s2, c); };
+        chain_sim(op, std::max(l1, l2), sim, ci, cf, oi, of);
+        return 0;
+    }
+    case RFO_RATIO: {
+        if (op != RFO_SIMILARITY) return -1;
+        auto dist = [&](u64 c) { return indel_cached(pm, s1, s2, c); };
+        double r;
+        chain_dist(RFO_NORM_SIMILARITY, l1 + l2, dist, 0, cf / 100.0, oi, &r);
+        *of = r * 100.0;
+        return 0;
+    }
+    case RFO_JARO:
+    case RFO_JARO_WINKLER: {
+        i64 C = -1, T = 0;
+        auto jaro = [&](double c) {
+            if (c > 1.0) return 0.0;
+            if (!s1.n && !s2.n) return 1.0;
+            if (!jaro_length_filter(s1.n, s2.n, c)) return 0.0;
+            if (C < 0) jaro_counts_pm(pm, s1, s2, &C, &T);
+            return jaro_from_counts(s1.n, s2.n, C, T, c);
+        };
+        if (metric == RFO_JARO) {
+            chain_fsim(op, jaro, cf, of);
+        }
+        else {
+            i64 prefix = common_prefix4(s1, s2);
+            auto jw = [&](double c) { return jw_chain(prefix, p->prefix_weight, c, jaro); };
+            chain_fsim(op, jw, cf, of);
+        }
+        return 0;
+    }
+    }
+    return -1;
+}
+
+template <typename T>
+void store(void* out, int dtype, i64 idx, i64 vi, double vf, bool is_int)
+{
+    (void)sizeof(T);
+    if (dtype == 0) ((int32_t*)out)[idx] = (int32_t)vi;
+    else if (dtype == 1) ((int64_t*)out)[idx] = vi;
+    else ((double*)out)[idx] = is_int ? (double)vi : vf;
+}
+
+bool result_is_int(int metric, int op)
+{
+    if (metric == RFO_JARO || metric == RFO_JARO_WINKLER || metric == RFO_RATIO) return false;
+    return op == RFO_DISTANCE || op == RFO_SIMILARITY;
+}
+
+} // namespace
+
+/* ====================================================================== C ABI */
+
+extern "C" {
+
+int64_t rfo_levenshtein_exact(const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb, int64_t ins,
+                              int64_t del, int64_t rep)
+{
+    rfo_params p{ins, del, rep, 0.1};
+    return with_strs(a, la, ca, b, lb, cb, [&](auto s1, auto s2) -> i64 {
+        PM pm;
+        pm.build(s1);
+        const u64 H = std::numeric_limits<u64>::max() / 4;
+        return (i64)lev_weighted_cached(pm, s1, s2, &p, H, H);
+    });
+}
+
+int64_t rfo_lcs_exact(const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb)
+{
+    return with_strs(a, la, ca, b, lb, cb, [&](auto s1, auto s2) -> i64 {
+        if (!s1.n) return 0;
+        PM pm;
+        pm.build(s1);
+        return lcs_full(pm, s2);
+    });
+}
+
+int64_t rfo_osa_exact(const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb)
+{
+    return with_strs(a, la, ca, b, lb, cb, [&](auto s1, auto s2) -> i64 {
+        PM pm;
+        pm.build(s1);
+        return (i64)osa_cached(pm, s1, s2, std::numeric_limits<u64>::max() / 4);
+    });
+}
+
+void rfo_jaro_counts(const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb, int64_t* common,
+                     int64_t* transp)
+{
+    with_strs(a, la, ca, b, lb, cb, [&](auto s1, auto s2) -> int {
+        PM pm;
+        pm.build(s1);
+        jaro_counts_pm(pm, s1, s2, common, transp);
+        return 0;
+    });
+}
+
+/* rapidfuzz_reference/Levenshtein.hpp: full weighted DP matrix */
+int64_t rfo_dp_levenshtein(const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb, int64_t ins,
+                           int64_t del, int64_t rep)
+{
+    return with_strs(a, la, ca, b, lb, cb, [&](auto s1, auto s2) -> i64 {
+        std::vector<i64> prev(s1.n + 1), cur(s1.n + 1);
+        for (i64 i = 0; i <= s1.n; ++i) prev[i] = i * del;
+        for (i64 j = 1; j <= s2.n; ++j) {
+            cur[0] = j * ins;
+            for (i64 i = 1; i <= s1.n; ++i) {
+                i64 sub = prev[i - 1] + (s1[i - 1] == s2[j - 1] ? 0 : rep);
+                cur[i] = std::min({prev[i] + ins, cur[i - 1] + del, sub});
+            }
+            std::swap(prev, cur);
+        }
+        return prev[s1.n];
+    });
+}
+
+/* rapidfuzz_reference/LCSseq.hpp */
+int64_t rfo_dp_lcs(const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb)
+{
+    return with_strs(a, la, ca, b, lb, cb, [&](auto s1, auto s2) -> i64 {
+        std::vector<i64> prev(s2.n + 1, 0), cur(s2.n + 1, 0);
+        for (i64 i = 1; i <= s1.n; ++i) {
+            for (i64 j = 1; j <= s2.n; ++j)
+                cur[j] = s1[i - 1] == s2[j - 1] ? prev[j - 1] + 1 : std::max(prev[j], cur[j - 1]);
+            std::swap(prev, cur);
+        }
+        return prev[s2.n];
+    });
+}
+
+/* rapidfuzz_reference/OSA.hpp:13-52 */
+int64_t rfo_dp_osa(const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb)
+{
+    return with_strs(a, la, ca, b, lb, cb, [&](auto s1, auto s2) -> i64 {
+        const i64 n1 = s1.n, n2 = s2.n;
+        std::vector<i64> M((n1 + 1) * (n2 + 1));
+        auto at = [&](i64 i, i64 j) -> i64& { return M[i * (n2 + 1) + j]; };
+        for (i64 i = 0; i <= n1; ++i) at(i, 0) = i;
+        for (i64 j = 0; j <= n2; ++j) at(0, j) = j;
+        for (i64 i = 0; i < n1; ++i)
+            for (i64 j = 0; j < n2; ++j) {
+                i64 cost = s1[i] == s2[j] ? 0 : 1;
+                i64 v = std::min({at(i, j + 1) + 1, at(i + 1, j) + 1, at(i, j) + cost});
+                if (i > 0 && j > 0 && s1[i] == s2[j - 1] && s1[i - 1] == s2[j]) v = std::min(v, at(i - 1, j - 1) + cost);
+                at(i + 1, j + 1) = v;
+            }
+        return at(n1, n2);
+    });
+}
+
+/* rapidfuzz_reference/Jaro.hpp:11-66 (counts only) */
+void rfo_naive_jaro_counts(const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb, int64_t* common,
+                           int64_t* transp)
+{
+    with_strs(a, la, ca, b, lb, cb, [&](auto P, auto T) -> int {
+        *common = 0;
+        *transp = 0;
+        if (!P.n || !T.n) return 0;
+        std::vector<char> pf(P.n + 1, 0), tf(T.n + 1, 0);
+        i64 bound = std::max(P.n, T.n) / 2;
+        if (bound > 0) --bound;
+        i64 cc = 0;
+        for (i64 i = 0; i < T.n; ++i) {
+            i64 lo = i >= bound ? i - bound : 0;
+            i64 hi = std::min(i + bound, P.n - 1);
+            for (i64 j = lo; j <= hi; ++j)
+                if (!pf[j] && P[j] == T[i]) {
+                    tf[i] = pf[j] = 1;
+                    ++cc;
+                    break;
+                }
+        }
+        i64 t = 0, k = 0;
+        for (i64 i = 0; i < T.n; ++i) {
+            if (!tf[i]) continue;
+            i64 j = k;
+            for (; j < P.n; ++j)
+                if (pf[j]) {
+                    k = j + 1;
+                    break;
+                }
+            if (T[i] != P[j]) ++t;
+        }
+        *common = cc;
+        *transp = t;
+        return 0;
+    });
+}
+
+int rfo_score(int metric, int op, int form, const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb,
+              const rfo_params* p, uint64_t ci, double cf, int64_t* oi, double* of)
+{
+    return with_strs(a, la, ca, b, lb, cb, [&](auto s1, auto s2) -> int {
+        PM pm;
+        pm.build(s1);
+        return score_with_pm(metric, op, form, pm, s1, s2, p, ci, cf, oi, of);
+    });
+}
+
+int rfo_cdist(int metric, int op, const rfo_strings* q, const rfo_strings* c, const rfo_params* p, uint64_t ci,
+              double cf, int out_dtype, void* out, int nthreads)
+{
+    if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+    const bool is_int = result_is_int(metric, op);
+    const i64 nq = q->count, nc = c->count;
+    /* queries are split across threads; each thread builds a query's pattern once
+     * and scores every choice with it (the Cached* loop of the reference) */
+    std::vector<int> errs(nthreads, 0);
+    auto work = [&](int tid) {
+        for (i64 qi = tid; qi < nq; qi += nthreads) {
+            const char* qd = (const char*)q->data + q->offsets[qi] * q->char_width;
+            i64 ql = q->offsets[qi + 1] - q->offsets[qi];
+            int rc = with_strs(qd, ql, q->char_width, c->data, 0, c->char_width, [&](auto s1, auto s2base) -> int {
+                PM pm;
+                pm.build(s1);
+                for (i64 k = 0; k < nc; ++k) {
+                    decltype(s2base) s2{s2base.p + c->offsets[k], c->offsets[k + 1] - c->offsets[k]};
+                    i64 vi = 0;
+                    double vf = 0;
+                    if (score_with_pm(metric, op, RFO_FORM_CACHED, pm, s1, s2, p, ci, cf, &vi, &vf)) return -1;
+                    store<int>(out, out_dtype, qi * nc + k, vi, vf, is_int);
+                }
+                return 0;
+            });
+            if (rc) errs[tid] = rc;
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nthreads; ++t) th.emplace_back(work, t);
+    work(0);
+    for (auto& t : th) t.join();
+    for (int e : errs)
+        if (e) return e;
+    return 0;
+}
+
+} /* extern "C" */

@@ -1,0 +1,1138 @@
+/*
+ * rfg_core.cuh -- bit-parallel scorer cores and the reference's formula chains.
+ *
+ * Every device result of this library is "formula chain over an exact integer":
+ *   Levenshtein    exact (weighted) distance        rapidfuzz/distance/Levenshtein_impl.hpp:1056-1089
+ *   Indel/LCSseq   exact LCS length                 rapidfuzz/distance/LCSseq_impl.hpp:205-403
+ *   OSA            exact OSA distance               rapidfuzz/distance/OSA_impl.hpp:34-273
+ *   Jaro / JW      common chars + transpositions    rapidfuzz/distance/Jaro_impl.hpp:94-454
+ * The chains (distance <-> similarity <-> normalized, cutoff translation) follow
+ * rapidfuzz/details/distance.hpp literally, so integers are bit-exact and doubles are
+ * bit-identical: every double operation below is an explicit round-to-nearest
+ * operation (no FMA contraction on the device).
+ *
+ * A core may stop early once the value it computes is known to exceed the pruning bound
+ * K it was given; it then returns any value > K.  The chains only ever look at
+ * "d <= K ? d : K+1", so pruning never changes a result.
+ *
+ * Early stop bound (all distance-type cores): after column j of an m x n DP, every
+ * alignment path crosses column j at some row i and still needs |(m-i)-(n-j)| unit
+ * operations, so dist >= min_i D[i][j] + |(m-i)-(n-j)|.  Because neighbouring cells of
+ * a column differ by at most 1, that minimum sits at the row i* = m-n+j on the diagonal
+ * through (m, n) (clamped to row 0, where it equals n-m).  D[i*][j] is j plus the
+ * masked popcounts of the vertical-delta vectors, so the bound costs a few popcounts.
+ * The same identity gives the final distance: D[m][n] = n + popc(VP) - popc(VN) over the
+ * m pattern bits, so no per-character score tracking is needed.
+ *
+ * This header compiles for the device (nvcc) and, for the CPU self-checks of the
+ * algorithms, for the host as well.
+ */
+#pragma once
+#include <stdint.h>
+
+#ifdef __CUDACC__
+#define RFG_HD __host__ __device__ __forceinline__
+#else
+#define RFG_HD inline
+#endif
+
+namespace rfg {
+
+typedef uint64_t u64;
+typedef int64_t i64;
+typedef uint32_t u32;
+
+/* ---------------------------------------------------------------- bit helpers */
+
+RFG_HD int popc64(u64 x)
+{
+#ifdef __CUDA_ARCH__
+    return __popcll(x);
+#else
+    return __builtin_popcountll(x);
+#endif
+}
+
+RFG_HD int ctz64(u64 x)
+{
+#ifdef __CUDA_ARCH__
+    return __ffsll((long long)x) - 1;
+#else
+    return __builtin_ctzll(x);
+#endif
+}
+
+RFG_HD u64 blsi(u64 x) { return x & (0ull - x); }
+RFG_HD u64 blsr(u64 x) { return x & (x - 1); }
+/* bits [0, n), n in [0, 64] */
+RFG_HD u64 low_mask(int n) { return n >= 64 ? ~0ull : ((1ull << n) - 1); }
+/* bits [a, b] of a 64-bit word, clipped to [0, 63]; empty when b < a */
+RFG_HD u64 range_mask(int a, int b)
+{
+    if (a < 0) a = 0;
+    if (b > 63) b = 63;
+    if (b < a) return 0;
+    return low_mask(b + 1) & ~low_mask(a);
+}
+
+/* a + b + carry_in over 64 bits, carry out */
+RFG_HD u64 add_carry(u64 a, u64 b, u32 cin, u32* cout)
+{
+#ifdef __CUDA_ARCH__
+    u32 al = (u32)a, ah = (u32)(a >> 32), bl = (u32)b, bh = (u32)(b >> 32);
+    u32 rl, rh, c;
+    asm("add.cc.u32 %0, %4, %5;\n\t"
+        "addc.cc.u32 %1, %6, %7;\n\t"
+        "addc.u32 %2, 0, 0;\n\t"
+        : "=r"(rl), "=r"(rh), "=r"(c)
+        : "r"(0), "r"(al), "r"(bl), "r"(ah), "r"(bh));
+    /* add the incoming carry separately: (a+b) + cin can carry only when a+b == ~0 */
+    u64 r = ((u64)rh << 32) | rl;
+    u64 r2 = r + cin;
+    *cout = c | (u32)(r2 < r);
+    return r2;
+#else
+    u64 r = a + b;
+    u32 c1 = r < a;
+    u64 r2 = r + cin;
+    u32 c2 = r2 < r;
+    *cout = c1 | c2;
+    return r2;
+#endif
+}
+
+/* -------------------------------------------------------------- exact doubles */
+
+RFG_HD double dadd(double a, double b)
+{
+#ifdef __CUDA_ARCH__
+    return __dadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+RFG_HD double dsub(double a, double b)
+{
+#ifdef __CUDA_ARCH__
+    return __dsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+RFG_HD double dmul(double a, double b)
+{
+#ifdef __CUDA_ARCH__
+    return __dmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+RFG_HD double ddiv(double a, double b)
+{
+#ifdef __CUDA_ARCH__
+    return __ddiv_rn(a, b);
+#else
+    return a / b;
+#endif
+}
+RFG_HD double dceil(double x)
+{
+#ifdef __CUDA_ARCH__
+    return ceil(x);
+#else
+    return __builtin_ceil(x);
+#endif
+}
+/* std::min / std::max semantics (first argument kept on ties) */
+RFG_HD double dmin(double a, double b) { return (b < a) ? b : a; }
+RFG_HD double dmax(double a, double b) { return (a < b) ? b : a; }
+
+/* ----------------------------------------------------------- metric/op enums */
+
+enum Metric { LEVENSHTEIN = 0, INDEL = 1, LCSSEQ = 2, OSA = 3, JARO = 4, JARO_WINKLER = 5, RATIO = 6 };
+enum Op { DISTANCE = 0, SIMILARITY = 1, NORM_DISTANCE = 2, NORM_SIMILARITY = 3 };
+enum Form { FORM_FREE = 0, FORM_CACHED = 1, FORM_MULTI = 2 };
+
+/* bit-parallel core family a (metric, weights) pair runs on */
+enum Family { FAM_LEV = 0, FAM_LCS = 1, FAM_OSA = 2, FAM_JARO = 3, FAM_WF = 4, FAM_NONE = 5 };
+
+struct ScoreParams {
+    i64 ins, del, rep;     /* Levenshtein weights */
+    double prefix_weight;  /* Jaro-Winkler */
+};
+
+/* ======================================================== single-word cores
+ * PM: pattern-match table of s1 (pm(c) = bit i set when s1[i] == c), pattern length
+ * m in 1..64.  TXT: t[j] yields the j-th code unit of s2.  K: pruning bound. */
+
+/* Hyyro 2003 (Levenshtein_impl.hpp:259-322) */
+template <typename PMF, typename TXT>
+RFG_HD i64 lev_word(const PMF& pm, int m, const TXT& t, int n, i64 K)
+{
+    u64 VP = ~0ull, VN = 0;
+    const bool check = K < (i64)(m > n ? m : n);
+    for (int j = 0; j < n; ++j) {
+        const u64 X = pm(t[j]);
+        const u64 D0 = (((X & VP) + VP) ^ VP) | X | VN;
+        u64 HP = VN | ~(D0 | VP);
+        u64 HN = D0 & VP;
+        HP = (HP << 1) | 1;
+        HN = HN << 1;
+        VP = HN | ~(D0 | HP);
+        VN = HP & D0;
+        if (check && (j & 7) == 7) {
+            const int jj = j + 1, is = m - n + jj;
+            if (is >= 0) {
+                const u64 lm = low_mask(is);
+                const i64 lb = (i64)jj + popc64(VP & lm) - popc64(VN & lm);
+                if (lb > K) return K + 1;
+            }
+        }
+    }
+    const u64 mm = low_mask(m);
+    return (i64)n + popc64(VP & mm) - popc64(VN & mm);
+}
+
+/* Hyyro 2004 LCS (LCSseq_impl.hpp:205-260).  Kd bounds the Indel distance m+n-2*LCS;
+ * returns the exact LCS, or -1 once the Indel distance is known to exceed Kd. */
+template <typename PMF, typename TXT>
+RFG_HD i64 lcs_word(const PMF& pm, int m, const TXT& t, int n, i64 Kd)
+{
+    u64 S = ~0ull;
+    const bool check = Kd < (i64)(m + n);
+    for (int j = 0; j < n; ++j) {
+        const u64 X = pm(t[j]);
+        const u64 u = S & X;
+        S = (S + u) | (S - u);
+        if (check && (j & 7) == 7) {
+            const int jj = j + 1, is = m - n + jj;
+            if (is >= 0) {
+                const i64 lcs_is = popc64(~S & low_mask(is));
+                if ((i64)is + jj - 2 * lcs_is > Kd) return -1;
+            }
+        }
+    }
+    return popc64(~S & low_mask(m));
+}
+
+/* Hyyro 2003 with the transposition term (OSA_impl.hpp:34-74) */
+template <typename PMF, typename TXT>
+RFG_HD i64 osa_word(const PMF& pm, int m, const TXT& t, int n, i64 K)
+{
+    u64 VP = ~0ull, VN = 0, D0 = 0, PMold = 0;
+    const bool check = K < (i64)(m > n ? m : n);
+    for (int j = 0; j < n; ++j) {
+        const u64 X = pm(t[j]);
+        const u64 TR = (((~D0) & X) << 1) & PMold;
+        D0 = (((X & VP) + VP) ^ VP) | X | VN | TR;
+        u64 HP = VN | ~(D0 | VP);
+        u64 HN = D0 & VP;
+        HP = (HP << 1) | 1;
+        HN = HN << 1;
+        VP = HN | ~(D0 | HP);
+        VN = HP & D0;
+        PMold = X;
+        if (check && (j & 7) == 7) {
+            const int jj = j + 1, is = m - n + jj;
+            if (is >= 0) {
+                const u64 lm = low_mask(is);
+                const i64 lb = (i64)jj + popc64(VP & lm) - popc64(VN & lm);
+                if (lb > K) return K + 1;
+            }
+        }
+    }
+    const u64 mm = low_mask(m);
+    return (i64)n + popc64(VP & mm) - popc64(VN & mm);
+}
+
+/* Jaro flagging, P (= s1) 1..64 chars, effective text length <= 64
+ * (Jaro_impl.hpp:94-132, 258-276).  Returns common chars, transpositions (unhalved). */
+template <typename PMF, typename TXT>
+RFG_HD void jaro_word(const PMF& pm, int pl, const TXT& t, int tl, int* common, int* transp)
+{
+    int bound = (pl > tl ? pl : tl) / 2;
+    if (bound > 0) --bound;
+    int te = tl;
+    if (te > pl + bound) te = pl + bound; /* text beyond the last window never matches */
+    u64 pflag = 0, tflag = 0;
+    u64 bmask = low_mask(bound + 1);
+    int j = 0;
+    const int lead = bound < te ? bound : te;
+    for (; j < lead; ++j) {
+        const u64 x = pm(t[j]) & bmask & ~pflag;
+        pflag |= blsi(x);
+        tflag |= (u64)(x != 0) << j;
+        bmask = (bmask << 1) | 1;
+    }
+    for (; j < te; ++j) {
+        const u64 x = pm(t[j]) & bmask & ~pflag;
+        pflag |= blsi(x);
+        tflag |= (u64)(x != 0) << j;
+        bmask <<= 1;
+    }
+    *common = popc64(pflag);
+    int tr = 0;
+    while (tflag) {
+        const u64 pbit = blsi(pflag);
+        tr += (pm(t[ctz64(tflag)]) & pbit) == 0;
+        tflag = blsr(tflag);
+        pflag ^= pbit;
+    }
+    *transp = tr;
+}
+
+/* ========================================================= multi-word cores
+ * PMW: pm(c, w) = word w of the pattern-match vector of c.  W words in registers,
+ * pattern length m in (64*(W-1), 64*W] (smaller m works: the extra words stay zero). */
+
+/* Myers/Hyyro blocks (Levenshtein_impl.hpp:641-850 without the band) */
+template <int W, typename PMW, typename TXT>
+RFG_HD i64 lev_multi(const PMW& pm, int m, const TXT& t, int n, i64 K)
+{
+    u64 VP[W], VN[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        VP[w] = ~0ull;
+        VN[w] = 0;
+    }
+    const bool check = K < (i64)(m > n ? m : n);
+    for (int j = 0; j < n; ++j) {
+        const u64 c = t[j];
+        u64 hp_c = 1, hn_c = 0;
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            const u64 X = pm(c, w) | hn_c;
+            const u64 vp = VP[w], vn = VN[w];
+            const u64 D0 = (((X & vp) + vp) ^ vp) | X | vn;
+            u64 HP = vn | ~(D0 | vp);
+            u64 HN = D0 & vp;
+            const u64 hp_o = HP >> 63, hn_o = HN >> 63;
+            HP = (HP << 1) | hp_c;
+            HN = (HN << 1) | hn_c;
+            hp_c = hp_o;
+            hn_c = hn_o;
+            VP[w] = HN | ~(D0 | HP);
+            VN[w] = HP & D0;
+        }
+        if (check && (j & 7) == 7) {
+            const int jj = j + 1, is = m - n + jj;
+            if (is >= 0) {
+                i64 lb = jj;
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    const int b = is - 64 * w;
+                    const u64 lm = b <= 0 ? 0 : low_mask(b);
+                    lb += popc64(VP[w] & lm) - popc64(VN[w] & lm);
+                }
+                if (lb > K) return K + 1;
+            }
+        }
+    }
+    i64 d = n;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        const int b = m - 64 * w;
+        const u64 lm = b <= 0 ? 0 : low_mask(b);
+        d += popc64(VP[w] & lm) - popc64(VN[w] & lm);
+    }
+    return d;
+}
+
+/* Hyyro 2004 over words with the add carry chained (LCSseq_impl.hpp:205-260) */
+template <int W, typename PMW, typename TXT>
+RFG_HD i64 lcs_multi(const PMW& pm, int m, const TXT& t, int n, i64 Kd)
+{
+    u64 S[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) S[w] = ~0ull;
+    const bool check = Kd < (i64)(m + n);
+    for (int j = 0; j < n; ++j) {
+        const u64 c = t[j];
+        u32 carry = 0;
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            const u64 X = pm(c, w);
+            const u64 s = S[w];
+            const u64 u = s & X;
+            const u64 x = add_carry(s, u, carry, &carry);
+            S[w] = x | (s - u);
+        }
+        if (check && (j & 7) == 7) {
+            const int jj = j + 1, is = m - n + jj;
+            if (is >= 0) {
+                i64 lcs_is = 0;
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    const int b = is - 64 * w;
+                    lcs_is += popc64(~S[w] & (b <= 0 ? 0 : low_mask(b)));
+                }
+                if ((i64)is + jj - 2 * lcs_is > Kd) return -1;
+            }
+        }
+    }
+    i64 l = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        const int b = m - 64 * w;
+        l += popc64(~S[w] & (b <= 0 ? 0 : low_mask(b)));
+    }
+    return l;
+}
+
+/* OSA over words (OSA_impl.hpp:176-249): the transposition term of word w needs the
+ * previous column's D0 and the current column's match vector of word w-1 */
+template <int W, typename PMW, typename TXT>
+RFG_HD i64 osa_multi(const PMW& pm, int m, const TXT& t, int n, i64 K)
+{
+    u64 VP[W], VN[W], D0v[W], PMo[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        VP[w] = ~0ull;
+        VN[w] = 0;
+        D0v[w] = 0;
+        PMo[w] = 0;
+    }
+    const bool check = K < (i64)(m > n ? m : n);
+    for (int j = 0; j < n; ++j) {
+        const u64 c = t[j];
+        u64 hp_c = 1, hn_c = 0;
+        u64 d0_prev_word = 0; /* previous column's D0 of word w-1 */
+        u64 pm_prev_word = 0; /* this column's match vector of word w-1 */
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            const u64 X = pm(c, w);
+            const u64 vp = VP[w], vn = VN[w], d0_old = D0v[w];
+            const u64 TR = ((((~d0_old) & X) << 1) | (((~d0_prev_word) & pm_prev_word) >> 63)) & PMo[w];
+            const u64 Xc = X | hn_c;
+            const u64 D0 = (((Xc & vp) + vp) ^ vp) | Xc | vn | TR;
+            u64 HP = vn | ~(D0 | vp);
+            u64 HN = D0 & vp;
+            const u64 hp_o = HP >> 63, hn_o = HN >> 63;
+            HP = (HP << 1) | hp_c;
+            HN = (HN << 1) | hn_c;
+            hp_c = hp_o;
+            hn_c = hn_o;
+            VP[w] = HN | ~(D0 | HP);
+            VN[w] = HP & D0;
+            d0_prev_word = d0_old;
+            pm_prev_word = X;
+            D0v[w] = D0;
+            PMo[w] = X;
+        }
+        if (check && (j & 7) == 7) {
+            const int jj = j + 1, is = m - n + jj;
+            if (is >= 0) {
+                i64 lb = jj;
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    const int b = is - 64 * w;
+                    const u64 lm = b <= 0 ? 0 : low_mask(b);
+                    lb += popc64(VP[w] & lm) - popc64(VN[w] & lm);
+                }
+                if (lb > K) return K + 1;
+            }
+        }
+    }
+    i64 d = n;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        const int b = m - 64 * w;
+        const u64 lm = b <= 0 ? 0 : low_mask(b);
+        d += popc64(VP[w] & lm) - popc64(VN[w] & lm);
+    }
+    return d;
+}
+
+/* Banded Levenshtein over a diagonal window of 64*B bits, the multi-word form of
+ * levenshtein_hyrroe2003_small_band (Levenshtein_impl.hpp:419-505).  Requires
+ * 2K+1 <= 64*B and |m-n| <= K.  Window bit b of step j is pattern index
+ * K+1-64B+j+b; the window moves down one row per text character (the D0 >> 1 frame
+ * shift).  diag tracks D[K+j][j] on the lower band edge (rows past m are virtual rows
+ * without matches; they never feed rows <= m).  D[m-n+j][j] = diag minus the vertical
+ * deltas of a fixed bit range below the edge: the early-stop bound and, at j = n, the
+ * distance. */
+template <int B, typename PMW, typename TXT>
+RFG_HD i64 lev_band(const PMW& pm, int pw, int m, const TXT& t, int n, int K)
+{
+    const int NB = 64 * B;
+    u64 VP[B], VN[B], rmask[B];
+    /* initial column: rows 1..K+1 (bits NB-1-K .. NB-1) have vertical delta +1 */
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        VP[b] = range_mask(NB - 1 - K - 64 * b, NB - 1 - 64 * b);
+        VN[b] = 0;
+        rmask[b] = range_mask(NB - 1 - K + (m - n) - 64 * b, NB - 2 - 64 * b);
+    }
+    i64 diag = K;
+    int start = K + 1 - NB; /* pattern index of window bit 0 */
+    for (int j = 0; j < n; ++j, ++start) {
+        const u64 c = t[j];
+        /* window of match bits: pattern indices [start, start + NB) */
+        u64 X[B];
+        {
+            const int w0 = start >> 6; /* floor division */
+            const int sh = start & 63;
+            u64 prev = (w0 >= 0 && w0 < pw) ? pm(c, w0) : 0;
+#pragma unroll
+            for (int b = 0; b < B; ++b) {
+                const int wn = w0 + b + 1;
+                const u64 next = (wn >= 0 && wn < pw) ? pm(c, wn) : 0;
+                X[b] = sh ? ((prev >> sh) | (next << (64 - sh))) : prev;
+                prev = next;
+            }
+        }
+        u64 D0[B];
+        u32 carry = 0;
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const u64 sum = add_carry(X[b] & VP[b], VP[b], carry, &carry);
+            D0[b] = (sum ^ VP[b]) | X[b] | VN[b];
+        }
+        diag += (D0[B - 1] >> 63) == 0;
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const u64 HP = VN[b] | ~(D0[b] | VP[b]);
+            const u64 HN = D0[b] & VP[b];
+            const u64 hi = (b + 1 < B) ? D0[b + 1 < B ? b + 1 : b] : 0;
+            const u64 D0s = (D0[b] >> 1) | (hi << 63);
+            VP[b] = HN | ~(D0s | HP);
+            VN[b] = D0s & HP;
+        }
+        if ((j & 7) == 7 || j == n - 1) {
+            i64 v = diag;
+#pragma unroll
+            for (int b = 0; b < B; ++b) v -= popc64(VP[b] & rmask[b]) - popc64(VN[b] & rmask[b]);
+            if (j == n - 1) return v;
+            if (v > K) return (i64)K + 1;
+        }
+    }
+    return (i64)n; /* n == 0; callers never ask (|m-n| <= K < m) */
+}
+
+/* Jaro with P (= s1) of up to 64*W chars and an effective text of <= 64 chars:
+ * the greedy flagging of flag_similar_characters_block (Jaro_impl.hpp:134-256), with
+ * the window masks built per word, and the transposition count of
+ * count_transpositions_block (Jaro_impl.hpp:278-315). */
+template <int W, typename PMW, typename TXT>
+RFG_HD void jaro_multi(const PMW& pm, int pl, const TXT& t, int tl, int* common, int* transp)
+{
+    int bound = (pl > tl ? pl : tl) / 2;
+    if (bound > 0) --bound;
+    int te = tl;
+    if (te > pl + bound) te = pl + bound;
+    u64 pflag[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) pflag[w] = 0;
+    u64 tflag = 0;
+    for (int j = 0; j < te; ++j) {
+        const u64 c = t[j];
+        const int lo = j - bound, hi = j + bound;
+        bool found = false;
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            const u64 x = pm(c, w) & range_mask(lo - 64 * w, hi - 64 * w) & ~pflag[w];
+            if (!found && x) {
+                pflag[w] |= blsi(x);
+                found = true;
+            }
+        }
+        tflag |= (u64)found << j;
+    }
+    int cc = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) cc += popc64(pflag[w]);
+    *common = cc;
+    int tr = 0, pwi = 0;
+    while (tflag) {
+        /* next flagged pattern position, in order */
+        u64 pf = 0;
+#pragma unroll
+        for (int w = 0; w < W; ++w)
+            if (w == pwi) pf = pflag[w];
+        while (!pf) {
+            ++pwi;
+#pragma unroll
+            for (int w = 0; w < W; ++w)
+                if (w == pwi) pf = pflag[w];
+        }
+        const u64 pbit = blsi(pf);
+        tr += (pm(t[ctz64(tflag)], pwi) & pbit) == 0;
+        tflag = blsr(tflag);
+#pragma unroll
+        for (int w = 0; w < W; ++w)
+            if (w == pwi) pflag[w] ^= pbit;
+    }
+    *transp = tr;
+}
+
+/* ====================================================== formula chains
+ * plan_*: the cutoff the reference passes to the metric's _distance/_similarity for
+ *         (metric, op, form) -- the core's pruning bound is derived from it;
+ * finish_*: the reference's arithmetic from that call's result to the API result. */
+
+RFG_HD double norm_sim_to_norm_dist(double c) { return dmin(1.0, dadd(dsub(1.0, c), 0.00001)); } /* common.hpp:50-53 */
+
+RFG_HD u64 ceil_div_u(u64 a, u64 d) { return a / d + (u64)(a % d != 0); }
+
+/* (size_t)std::ceil((double)maximum * cutoff) */
+RFG_HD u64 ceil_cut(u64 maximum, double c) { return (u64)dceil(dmul((double)maximum, c)); }
+
+/* levenshtein_maximum (Levenshtein_impl.hpp:118-128) */
+RFG_HD u64 lev_maximum(u64 l1, u64 l2, const ScoreParams& p)
+{
+    const u64 ins = (u64)p.ins, del = (u64)p.del, rep = (u64)p.rep;
+    u64 mx = l1 * del + l2 * ins;
+    u64 alt = (l1 >= l2) ? l2 * rep + (l1 - l2) * del : l1 * rep + (l2 - l1) * ins;
+    return alt < mx ? alt : mx;
+}
+
+/* How a Levenshtein weight table maps onto a core (Levenshtein_impl.hpp:1061-1088) */
+enum LevMode { LEV_ZERO = 0, LEV_UNIFORM = 1, LEV_INDEL = 2, LEV_GENERAL = 3 };
+RFG_HD int lev_mode(const ScoreParams& p)
+{
+    if (p.ins == p.del) {
+        if (p.ins == 0) return LEV_ZERO;
+        if (p.ins == p.rep) return LEV_UNIFORM;
+        if (p.rep >= p.ins + p.del) return LEV_INDEL;
+    }
+    return LEV_GENERAL;
+}
+
+/* Family of the bit-parallel core that (metric, weights, form) needs */
+RFG_HD int metric_family(int metric, int form, const ScoreParams& p)
+{
+    switch (metric) {
+    case LEVENSHTEIN:
+        if (form == FORM_MULTI) return FAM_LEV; /* Multi ignores the replace weight (Levenshtein.hpp:391-398) */
+        switch (lev_mode(p)) {
+        case LEV_ZERO: return FAM_NONE;
+        case LEV_UNIFORM: return FAM_LEV;
+        case LEV_INDEL: return FAM_LCS;
+        default: return FAM_WF;
+        }
+    case INDEL:
+    case LCSSEQ:
+    case RATIO: return FAM_LCS;
+    case OSA: return FAM_OSA;
+    default: return FAM_JARO;
+    }
+}
+
+/* A pair's plan: which core bound to run with (native units of the core) */
+struct Plan {
+    int run;     /* 0: the result needs no core */
+    i64 K;       /* pruning bound: distance for LEV/OSA/WF, Indel distance for LCS */
+    u64 Kchain;  /* the cutoff of the chain's single _distance/_similarity call */
+    double jc;   /* Jaro cutoff (Jaro families) */
+    u64 lcs_min; /* LCS families: the _similarity cutoff */
+};
+
+RFG_HD i64 clamp_bound(u64 k) { return k > (u64)0x3fffffffffffffffull ? (i64)0x3fffffffffffffffll : (i64)k; }
+
+/* _distance cutoff of a distance-type chain (distance.hpp:52-64, 120-133, 240-262, 304-317) */
+RFG_HD bool dist_chain_cutoff(int op, u64 M, u64 ci, double cf, u64* K)
+{
+    switch (op) {
+    case DISTANCE: *K = ci; return true;
+    case SIMILARITY:
+        if (ci > M) return false;
+        *K = M - ci;
+        return true;
+    case NORM_DISTANCE: *K = ceil_cut(M, cf); return true;
+    default: *K = ceil_cut(M, norm_sim_to_norm_dist(cf)); return true;
+    }
+}
+
+/* finish of a distance-type chain given d = _distance(K) */
+RFG_HD void dist_chain_finish(int op, u64 M, u64 d, u64 ci, double cf, i64* oi, double* of)
+{
+    switch (op) {
+    case DISTANCE: *oi = (i64)d; return;
+    case SIMILARITY: {
+        const u64 s = M - d;
+        *oi = s >= ci ? (i64)s : 0;
+        return;
+    }
+    case NORM_DISTANCE: {
+        const double nd = M != 0 ? ddiv((double)d, (double)M) : 0.0;
+        *of = nd <= cf ? nd : 1.0;
+        return;
+    }
+    default: {
+        const double cs = norm_sim_to_norm_dist(cf);
+        double nd = M != 0 ? ddiv((double)d, (double)M) : 0.0;
+        nd = nd <= cs ? nd : 1.0;
+        const double ns = dsub(1.0, nd);
+        *of = ns >= cf ? ns : 0.0;
+    }
+    }
+}
+
+/* Multi* chains (distance.hpp:421-460, 500-512, 552-563) over exact values */
+RFG_HD void multi_dist_finish(int op, u64 M, u64 D, u64 ci, double cf, i64* oi, double* of)
+{
+    switch (op) {
+    case DISTANCE: *oi = (i64)(D <= ci ? D : ci + 1); return;
+    case SIMILARITY: {
+        const u64 s = M - D;
+        *oi = s >= ci ? (i64)s : 0;
+        return;
+    }
+    case NORM_DISTANCE: {
+        const double nd = M != 0 ? ddiv((double)D, (double)M) : 0.0;
+        *of = nd <= cf ? nd : 1.0;
+        return;
+    }
+    default: {
+        double nd = M != 0 ? ddiv((double)D, (double)M) : 0.0;
+        nd = nd <= 1.0 ? nd : 1.0;
+        const double ns = dsub(1.0, nd);
+        *of = ns >= cf ? ns : 0.0;
+    }
+    }
+}
+
+RFG_HD void multi_sim_finish(int op, u64 M, u64 S, u64 ci, double cf, i64* oi, double* of)
+{
+    switch (op) {
+    case SIMILARITY: *oi = S >= ci ? (i64)S : 0; return;
+    case DISTANCE: {
+        const u64 d = M - S;
+        *oi = (i64)(d <= ci ? d : ci + 1);
+        return;
+    }
+    default: multi_dist_finish(op, M, M - S, ci, cf, oi, of);
+    }
+}
+
+/* ------------------------------------------------------------------ Jaro */
+
+RFG_HD double jaro_formula(i64 pl, i64 tl, i64 common, i64 transp) /* Jaro_impl.hpp:32-42 */
+{
+    transp /= 2;
+    double sim = ddiv((double)common, (double)pl);
+    sim = dadd(sim, ddiv((double)common, (double)tl));
+    sim = dadd(sim, ddiv(dsub((double)common, (double)transp), (double)common));
+    return ddiv(sim, 3.0);
+}
+
+RFG_HD bool jaro_length_filter(i64 pl, i64 tl, double c) /* Jaro_impl.hpp:47-55 */
+{
+    if (!tl || !pl) return false;
+    const double mn = (double)(pl < tl ? pl : tl);
+    double sim = dadd(dadd(ddiv(mn, (double)pl), ddiv(mn, (double)tl)), 1.0);
+    sim = ddiv(sim, 3.0);
+    return sim >= c;
+}
+
+RFG_HD bool jaro_common_filter(i64 pl, i64 tl, i64 common, double c) /* Jaro_impl.hpp:60-71 */
+{
+    if (!common) return false;
+    double sim = ddiv((double)common, (double)pl);
+    sim = dadd(sim, ddiv((double)common, (double)tl));
+    sim = dadd(sim, 1.0);
+    sim = ddiv(sim, 3.0);
+    return sim >= c;
+}
+
+/* jaro_similarity (Jaro_impl.hpp:409-454) from exact counts; needs_counts() tells
+ * whether the counts are read at all */
+RFG_HD bool jaro_needs_counts(i64 pl, i64 tl, double c)
+{
+    if (c > 1.0) return false;
+    if (!pl && !tl) return false;
+    if (!jaro_length_filter(pl, tl, c)) return false;
+    return true;
+}
+
+RFG_HD double jaro_from_counts(i64 pl, i64 tl, i64 common, i64 transp, double c)
+{
+    if (c > 1.0) return 0.0;
+    if (!pl && !tl) return 1.0;
+    if (!jaro_length_filter(pl, tl, c)) return 0.0;
+    if (pl == 1 && tl == 1) return (double)(common == 1);
+    if (!jaro_common_filter(pl, tl, common, c)) return 0.0;
+    const double sim = jaro_formula(pl, tl, common, transp);
+    return sim >= c ? sim : 0;
+}
+
+/* jaro_winkler_similarity's cutoff for the inner Jaro (JaroWinkler_impl.hpp:54-62) */
+RFG_HD double jw_jaro_cutoff(i64 prefix, double pw, double c)
+{
+    double jc = c;
+    if (jc > 0.7) {
+        const double ps = dmul((double)prefix, pw);
+        if (ps >= 1.0) jc = 0.7;
+        else jc = dmax(0.7, ddiv(dsub(ps, jc), dsub(ps, 1.0)));
+    }
+    return jc;
+}
+
+/* the Winkler boost and final cutoff (JaroWinkler_impl.hpp:64-70) */
+RFG_HD double jw_finish(double sim, i64 prefix, double pw, double c)
+{
+    if (sim > 0.7) {
+        sim = dadd(sim, dmul(dmul((double)prefix, pw), dsub(1.0, sim)));
+        sim = dmin(sim, 1.0);
+    }
+    return sim >= c ? sim : 0;
+}
+
+/* MultiJaro (jaro_similarity_simd, Jaro_impl.hpp:818-840, 666-709) */
+RFG_HD double multi_jaro_from_counts(i64 pl, i64 tl, i64 common, i64 transp, double c)
+{
+    if (c > 1.0) return 0.0;
+    if (tl == 0) return pl ? 0.0 : 1.0;
+    if (!jaro_common_filter(pl, tl, common, c)) return 0.0;
+    const double sim = jaro_formula(pl, tl, common, transp);
+    return sim >= c ? sim : 0;
+}
+
+/* MultiJaroWinkler::_similarity (JaroWinkler.hpp:123-145) */
+RFG_HD double multi_jw(double s, i64 prefix, double pw, double c)
+{
+    if (s > 0.7) {
+        s = dadd(s, dmul(dmul((double)prefix, pw), dsub(1.0, s)));
+        s = dmin(s, 1.0);
+    }
+    if (s < c) s = 0.0;
+    return s;
+}
+
+/* the similarity cutoff that a double similarity-type chain passes on (maximum 1.0):
+ * SimilarityBase::_distance and the normalized bases (distance.hpp:52-76, 177-190) */
+RFG_HD double fsim_chain_cutoff(int op, double cf)
+{
+    switch (op) {
+    case SIMILARITY: return cf;
+    case DISTANCE: return 1.0 >= cf ? dsub(1.0, cf) : 0.0;
+    case NORM_DISTANCE: {
+        const double cd = dceil(dmul(1.0, cf));
+        return 1.0 >= cd ? dsub(1.0, cd) : 0.0;
+    }
+    default: {
+        const double cd = dceil(dmul(1.0, norm_sim_to_norm_dist(cf)));
+        return 1.0 >= cd ? dsub(1.0, cd) : 0.0;
+    }
+    }
+}
+
+RFG_HD double fsim_chain_finish(int op, double s, double cf)
+{
+    switch (op) {
+    case SIMILARITY: return s;
+    case DISTANCE: {
+        const double d = dsub(1.0, s);
+        return d <= cf ? d : 1.0;
+    }
+    case NORM_DISTANCE: {
+        const double cd = dceil(dmul(1.0, cf));
+        double d = dsub(1.0, s);
+        d = d <= cd ? d : 1.0;
+        const double nd = ddiv(d, 1.0);
+        return nd <= cf ? nd : 1.0;
+    }
+    default: {
+        const double c2 = norm_sim_to_norm_dist(cf);
+        const double cd = dceil(dmul(1.0, c2));
+        double d = dsub(1.0, s);
+        d = d <= cd ? d : 1.0;
+        double nd = ddiv(d, 1.0);
+        nd = nd <= c2 ? nd : 1.0;
+        const double ns = dsub(1.0, nd);
+        return ns >= cf ? ns : 0.0;
+    }
+    }
+}
+
+RFG_HD double multi_fsim_finish(int op, double s_at_cf, double s_at_0, double cf)
+{
+    switch (op) {
+    case SIMILARITY: return s_at_cf;
+    case DISTANCE: {
+        const double d = dsub(1.0, s_at_0);
+        return d <= cf ? d : 1.0;
+    }
+    case NORM_DISTANCE: {
+        double d = dsub(1.0, s_at_0);
+        d = d <= 1.0 ? d : 1.0;
+        return d <= cf ? d : 1.0;
+    }
+    default: {
+        double d = dsub(1.0, s_at_0);
+        d = d <= 1.0 ? d : 1.0;
+        const double ns = dsub(1.0, d);
+        return ns >= cf ? ns : 0.0;
+    }
+    }
+}
+
+/* ================================================= per-pair plan and finish
+ * Integer-valued metrics: the core result `raw` (a distance, or an LCS length, or -1
+ * for "pruned") is turned into the API result.  l1/l2 are the string lengths. */
+
+struct PairSpec {
+    int metric, op, form;
+    u64 l1, l2;
+    u64 ci;
+    double cf;
+    ScoreParams p;
+};
+
+/* plan for integer families; returns the plan (run == 0: no core needed) */
+RFG_HD Plan plan_int(const PairSpec& s)
+{
+    Plan pl;
+    pl.run = 1;
+    pl.K = 0;
+    pl.Kchain = 0;
+    pl.jc = 0;
+    pl.lcs_min = 0;
+    const u64 l1 = s.l1, l2 = s.l2;
+    const u64 BIG = ~0ull;
+    if (s.form == FORM_MULTI) {
+        /* exact values; only the distance op carries its cutoff into the core */
+        const u64 K = (s.op == DISTANCE && s.metric != LCSSEQ) ? s.ci : BIG;
+        if (s.metric == LEVENSHTEIN || s.metric == OSA) pl.K = clamp_bound(K);
+        else pl.K = clamp_bound(BIG); /* LCS families: exact LCS */
+        return pl;
+    }
+    switch (s.metric) {
+    case LEVENSHTEIN: {
+        const u64 M = lev_maximum(l1, l2, s.p);
+        u64 Kw;
+        if (!dist_chain_cutoff(s.op, M, s.ci, s.cf, &Kw)) {
+            pl.run = 0;
+            return pl;
+        }
+        pl.Kchain = Kw;
+        switch (lev_mode(s.p)) {
+        case LEV_ZERO: pl.run = 0; break;
+        case LEV_UNIFORM:
+        case LEV_INDEL: pl.K = clamp_bound(ceil_div_u(Kw, (u64)s.p.ins)); break;
+        default: pl.K = clamp_bound(Kw);
+        }
+        return pl;
+    }
+    case INDEL:
+    case RATIO: {
+        const u64 M = l1 + l2;
+        u64 K;
+        const int op = s.metric == RATIO ? NORM_SIMILARITY : s.op;
+        const double cf = s.metric == RATIO ? ddiv(s.cf, 100.0) : s.cf;
+        if (!dist_chain_cutoff(op, M, s.ci, cf, &K)) {
+            pl.run = 0;
+            return pl;
+        }
+        pl.Kchain = K;
+        pl.K = clamp_bound(K);
+        return pl;
+    }
+    case OSA: {
+        const u64 M = l1 > l2 ? l1 : l2;
+        u64 K;
+        if (!dist_chain_cutoff(s.op, M, s.ci, s.cf, &K)) {
+            pl.run = 0;
+            return pl;
+        }
+        pl.Kchain = K;
+        pl.K = clamp_bound(K);
+        return pl;
+    }
+    case LCSSEQ: {
+        const u64 M = l1 > l2 ? l1 : l2;
+        u64 cs;
+        switch (s.op) {
+        case SIMILARITY: cs = s.ci; break;
+        case DISTANCE: cs = M >= s.ci ? M - s.ci : 0; break;
+        case NORM_DISTANCE: {
+            const u64 Kd = ceil_cut(M, s.cf);
+            pl.Kchain = Kd;
+            cs = M >= Kd ? M - Kd : 0;
+            break;
+        }
+        default: {
+            const u64 Kd = ceil_cut(M, norm_sim_to_norm_dist(s.cf));
+            pl.Kchain = Kd;
+            cs = M >= Kd ? M - Kd : 0;
+        }
+        }
+        pl.lcs_min = cs;
+        if (cs > l1 || cs > l2) {
+            pl.run = 0; /* lcs_seq_similarity returns 0 (LCSseq_impl.hpp:382) */
+            return pl;
+        }
+        pl.K = (i64)(l1 + l2 - 2 * cs);
+        return pl;
+    }
+    }
+    pl.run = 0;
+    return pl;
+}
+
+/* Finish for integer families.  raw: LEV/OSA/WF -> distance (> K when pruned);
+ * LCS -> LCS length, or -1 when pruned.  Ignored when plan.run == 0. */
+RFG_HD void finish_int(const PairSpec& s, const Plan& pl, i64 raw, i64* oi, double* of)
+{
+    const u64 l1 = s.l1, l2 = s.l2;
+    if (s.form == FORM_MULTI) {
+        switch (s.metric) {
+        case LEVENSHTEIN: multi_dist_finish(s.op, lev_maximum(l1, l2, s.p), (u64)raw, s.ci, s.cf, oi, of); return;
+        case OSA: multi_dist_finish(s.op, l1 > l2 ? l1 : l2, (u64)raw, s.ci, s.cf, oi, of); return;
+        case INDEL: multi_dist_finish(s.op, l1 + l2, l1 + l2 - 2 * (u64)raw, s.ci, s.cf, oi, of); return;
+        case LCSSEQ: multi_sim_finish(s.op, l1 > l2 ? l1 : l2, (u64)raw, s.ci, s.cf, oi, of); return;
+        case RATIO: {
+            double r = 0;
+            multi_dist_finish(NORM_SIMILARITY, l1 + l2, l1 + l2 - 2 * (u64)raw, 0, ddiv(s.cf, 100.0), oi, &r);
+            *of = dmul(r, 100.0);
+            return;
+        }
+        }
+        return;
+    }
+    switch (s.metric) {
+    case LEVENSHTEIN: {
+        const u64 M = lev_maximum(l1, l2, s.p);
+        if (!pl.run && lev_mode(s.p) != LEV_ZERO) { /* similarity with cutoff above the maximum */
+            *oi = 0;
+            return;
+        }
+        const u64 Kw = pl.Kchain;
+        u64 d;
+        switch (lev_mode(s.p)) {
+        case LEV_ZERO: d = 0; break;
+        case LEV_UNIFORM: {
+            const u64 Kb = (u64)pl.K;
+            u64 b = (raw >= 0 && (u64)raw <= Kb) ? (u64)raw : Kb + 1;
+            d = b * (u64)s.p.ins;
+            d = d <= Kw ? d : Kw + 1;
+            break;
+        }
+        case LEV_INDEL: {
+            /* raw is an LCS length (or -1): indel distance = l1 + l2 - 2 lcs */
+            const u64 Kb = (u64)pl.K;
+            u64 b = raw >= 0 ? l1 + l2 - 2 * (u64)raw : Kb + 1;
+            b = b <= Kb ? b : Kb + 1;
+            d = b * (u64)s.p.ins;
+            d = d <= Kw ? d : Kw + 1;
+            break;
+        }
+        default: d = (u64)raw <= Kw ? (u64)raw : Kw + 1;
+        }
+        if (lev_mode(s.p) == LEV_ZERO) {
+            /* _distance returns 0 without a cutoff check; the chain still runs */
+            u64 K2;
+            if (!dist_chain_cutoff(s.op, M, s.ci, s.cf, &K2)) {
+                *oi = 0;
+                return;
+            }
+        }
+        dist_chain_finish(s.op, M, d, s.ci, s.cf, oi, of);
+        return;
+    }
+    case INDEL:
+    case RATIO: {
+        const u64 M = l1 + l2;
+        const int op = s.metric == RATIO ? NORM_SIMILARITY : s.op;
+        const double cf = s.metric == RATIO ? ddiv(s.cf, 100.0) : s.cf;
+        if (!pl.run) {
+            *oi = 0;
+            return;
+        }
+        const u64 K = pl.Kchain;
+        u64 d = raw >= 0 ? M - 2 * (u64)raw : K + 1;
+        d = d <= K ? d : K + 1;
+        double r = 0;
+        dist_chain_finish(op, M, d, s.ci, cf, oi, &r);
+        if (s.metric == RATIO) *of = dmul(r, 100.0);
+        else *of = r;
+        return;
+    }
+    case OSA: {
+        const u64 M = l1 > l2 ? l1 : l2;
+        if (!pl.run) {
+            *oi = 0;
+            return;
+        }
+        const u64 K = pl.Kchain;
+        const u64 d = (u64)raw <= K ? (u64)raw : K + 1;
+        dist_chain_finish(s.op, M, d, s.ci, s.cf, oi, of);
+        return;
+    }
+    case LCSSEQ: {
+        const u64 M = l1 > l2 ? l1 : l2;
+        const u64 cs = pl.lcs_min;
+        u64 sim = 0;
+        if (pl.run && raw >= 0 && (u64)raw >= cs) sim = (u64)raw;
+        switch (s.op) {
+        case SIMILARITY: *oi = (i64)sim; return;
+        case DISTANCE: {
+            const u64 d = M - sim;
+            *oi = (i64)(d <= s.ci ? d : s.ci + 1);
+            return;
+        }
+        case NORM_DISTANCE: {
+            const u64 Kd = pl.Kchain;
+            u64 d = M - sim;
+            d = d <= Kd ? d : Kd + 1;
+            const double nd = M != 0 ? ddiv((double)d, (double)M) : 0.0;
+            *of = nd <= s.cf ? nd : 1.0;
+            return;
+        }
+        default: {
+            const u64 Kd = pl.Kchain;
+            const double c2 = norm_sim_to_norm_dist(s.cf);
+            u64 d = M - sim;
+            d = d <= Kd ? d : Kd + 1;
+            double nd = M != 0 ? ddiv((double)d, (double)M) : 0.0;
+            nd = nd <= c2 ? nd : 1.0;
+            const double ns = dsub(1.0, nd);
+            *of = ns >= s.cf ? ns : 0.0;
+            return;
+        }
+        }
+    }
+    }
+}
+
+/* Jaro families.  prefix: common prefix (<= 4) of the two strings. */
+RFG_HD double jaro_cutoff_for(const PairSpec& s, i64 prefix)
+{
+    if (s.form == FORM_MULTI) return 0.0; /* Multi: counts are always read */
+    const double c = fsim_chain_cutoff(s.op, s.cf);
+    return s.metric == JARO ? c : jw_jaro_cutoff(prefix, s.p.prefix_weight, c);
+}
+
+RFG_HD bool jaro_pair_needs_counts(const PairSpec& s, i64 prefix)
+{
+    if (s.form == FORM_MULTI) return s.l2 != 0;
+    return jaro_needs_counts((i64)s.l1, (i64)s.l2, jaro_cutoff_for(s, prefix));
+}
+
+RFG_HD double finish_jaro(const PairSpec& s, i64 prefix, i64 common, i64 transp)
+{
+    const i64 pl = (i64)s.l1, tl = (i64)s.l2;
+    const double pw = s.p.prefix_weight;
+    if (s.form == FORM_MULTI) {
+        if (s.metric == JARO) {
+            const double a = multi_jaro_from_counts(pl, tl, common, transp, s.cf);
+            const double b = multi_jaro_from_counts(pl, tl, common, transp, 0.0);
+            return multi_fsim_finish(s.op, a, b, s.cf);
+        }
+        const double a = multi_jw(multi_jaro_from_counts(pl, tl, common, transp, dmin(0.7, s.cf)), prefix, pw, s.cf);
+        const double b = multi_jw(multi_jaro_from_counts(pl, tl, common, transp, dmin(0.7, 0.0)), prefix, pw, 0.0);
+        return multi_fsim_finish(s.op, a, b, s.cf);
+    }
+    const double c = fsim_chain_cutoff(s.op, s.cf);
+    double sim;
+    if (s.metric == JARO) {
+        sim = jaro_from_counts(pl, tl, common, transp, c);
+    }
+    else {
+        const double jc = jw_jaro_cutoff(prefix, pw, c);
+        sim = jw_finish(jaro_from_counts(pl, tl, common, transp, jc), prefix, pw, c);
+    }
+    return fsim_chain_finish(s.op, sim, s.cf);
+}
+
+} // namespace rfg
