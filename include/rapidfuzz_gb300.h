@@ -1,0 +1,171 @@
+/*
+ * rapidfuzz_gb300.h -- C ABI of the GB300 bit-parallel string scorers.
+ *
+ * One shared library (librapidfuzz_gb300.so) with plain pointers and sizes in every
+ * signature.  Each entry point replaces a rapidfuzz-cpp v3.3.3 interface (paths are
+ * relative to that project); the C++ mirror in rapidfuzz-cpp_gb300/include/rapidfuzz_gb300/
+ * binds these entry points behind the reference's own class and function names.
+ *
+ * Results are those of the reference on the same inputs: integers bit-exact, doubles
+ * bit-identical (the formula chains of rapidfuzz/details/distance.hpp are replayed on
+ * the device with round-to-nearest double operations).
+ *
+ * Errors: every call returns an rfg_status.  RFG_ERR_INVALID_ARGUMENT corresponds to
+ * the reference throwing std::invalid_argument, RFG_ERR_OUT_OF_RANGE to
+ * std::out_of_range; rfg_last_error() gives the message of the calling thread's last
+ * failure.  Nothing throws across the ABI.
+ *
+ * Strings are sequences of unsigned code units of 1, 2, 4 or 8 bytes.  Batches are
+ * packed code units plus count+1 int64 offsets (in code units).
+ *
+ * Threading: handles may be shared between host threads for const calls (score*);
+ * every call synchronises with its own stream before returning host results.
+ */
+#ifndef RAPIDFUZZ_GB300_H
+#define RAPIDFUZZ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RFG_ABI_VERSION 1
+
+typedef enum {
+    RFG_OK = 0,
+    RFG_ERR_INVALID_ARGUMENT = 1, /* std::invalid_argument in the reference */
+    RFG_ERR_OUT_OF_RANGE = 2,     /* std::out_of_range in the reference */
+    RFG_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+    RFG_ERR_OUT_OF_MEMORY = 4,    /* device or pinned host allocation failed */
+    RFG_ERR_NO_DEVICE = 5,        /* no CUDA device: the library has no CPU path */
+    RFG_ERR_DEVICE_CHECK = 6,     /* a kernel's own bounds/timeout check fired */
+    RFG_ERR_BUSY = 7              /* serving: admission refused (no slot / no memory) */
+} rfg_status;
+
+/* metrics (the scorer families of rapidfuzz/distance/ and fuzz::ratio) */
+typedef enum {
+    RFG_LEVENSHTEIN = 0,
+    RFG_INDEL = 1,
+    RFG_LCSSEQ = 2,
+    RFG_OSA = 3,
+    RFG_JARO = 4,
+    RFG_JARO_WINKLER = 5,
+    RFG_RATIO = 6 /* fuzz::ratio; only RFG_SIMILARITY */
+} rfg_metric;
+
+/* the four result kinds of every metric (rapidfuzz/details/distance.hpp) */
+typedef enum {
+    RFG_DISTANCE = 0,
+    RFG_SIMILARITY = 1,
+    RFG_NORMALIZED_DISTANCE = 2,
+    RFG_NORMALIZED_SIMILARITY = 3
+} rfg_op;
+
+/* which reference API the formula chain follows: the free functions, the Cached*
+ * scorers, or experimental::Multi* (whose chains differ in a few corner cases) */
+typedef enum { RFG_FORM_FREE = 0, RFG_FORM_CACHED = 1, RFG_FORM_MULTI = 2 } rfg_form;
+
+/* output element types */
+typedef enum { RFG_I32 = 0, RFG_I64 = 1, RFG_F64 = 2 } rfg_dtype;
+
+typedef struct {
+    int64_t insert_cost;  /* LevenshteinWeightTable (rapidfuzz/details/types.hpp:19-23) */
+    int64_t delete_cost;
+    int64_t replace_cost;
+    double prefix_weight; /* Jaro-Winkler, default 0.1 */
+} rfg_params;
+
+/* score_cutoff / score_hint of one call: the integer overloads (size_t) read *_i,
+ * the double overloads (normalized, Jaro, Jaro-Winkler, ratio) read *_f */
+typedef struct {
+    uint64_t cutoff_i;
+    double cutoff_f;
+    uint64_t hint_i;
+    double hint_f;
+} rfg_cutoff;
+
+typedef struct {
+    const void* data;       /* packed code units */
+    const int64_t* offsets; /* count+1 entries, code units */
+    int64_t count;
+    int32_t char_width;     /* 1, 2, 4 or 8 */
+} rfg_strings;
+
+/* flags of batch calls */
+#define RFG_DEVICE_INPUTS 1u  /* data/offsets of the batches are device pointers */
+#define RFG_DEVICE_OUTPUT 2u  /* out is a device pointer (no copy back) */
+
+typedef struct rfg_cached_s* rfg_cached;
+typedef struct rfg_multi_s* rfg_multi;
+typedef struct rfg_corpus_s* rfg_corpus;
+typedef struct rfg_server_s* rfg_server;
+
+/* ------------------------------------------------------------------ library */
+
+int rfg_abi_version(void);
+const char* rfg_last_error(void);
+/* device the library runs on (default 0); must precede the first other call */
+rfg_status rfg_set_device(int device);
+/* synchronise the library's streams (the calls below already do for host results) */
+rfg_status rfg_synchronize(void);
+
+/* ------------------------------------------------------- free functions (per call)
+ * levenshtein_distance / _similarity / _normalized_* (Levenshtein.hpp:140-265),
+ * indel_* (Indel.hpp:12-63), lcs_seq_* (LCSseq.hpp:12-63), osa_* (OSA.hpp:12-111),
+ * jaro_* (Jaro.hpp:12-61), jaro_winkler_* (JaroWinkler.hpp:11-73),
+ * fuzz::ratio (fuzz.hpp:44-48, fuzz_impl.hpp:28-32). */
+rfg_status rfg_score_i64(rfg_metric metric, rfg_op op, const void* s1, int64_t len1, int32_t width1,
+                         const void* s2, int64_t len2, int32_t width2, const rfg_params* params,
+                         uint64_t score_cutoff, uint64_t score_hint, int64_t* result);
+rfg_status rfg_score_f64(rfg_metric metric, rfg_op op, const void* s1, int64_t len1, int32_t width1,
+                         const void* s2, int64_t len2, int32_t width2, const rfg_params* params,
+                         double score_cutoff, double score_hint, double* result);
+
+/* ------------------------------------------------------------- cached scorers
+ * CachedLevenshtein (Levenshtein.hpp:421-482), CachedIndel (Indel.hpp:148-183),
+ * CachedLCSseq (LCSseq.hpp:197-226), CachedOSA (OSA.hpp:232-271), CachedJaro
+ * (Jaro.hpp:195-223), CachedJaroWinkler (JaroWinkler.hpp:168-199), fuzz::CachedRatio
+ * (fuzz.hpp:99-126).  create copies s1 to the device; calls are const and reentrant. */
+rfg_status rfg_cached_create(rfg_metric metric, const void* s1, int64_t len1, int32_t width1,
+                             const rfg_params* params, rfg_cached* out);
+rfg_status rfg_cached_destroy(rfg_cached scorer);
+/* one choice: Cached*::distance / similarity / normalized_* (distance.hpp:269-388) */
+rfg_status rfg_cached_score_i64(rfg_cached scorer, rfg_op op, const void* s2, int64_t len2, int32_t width2,
+                                uint64_t score_cutoff, uint64_t score_hint, int64_t* result);
+rfg_status rfg_cached_score_f64(rfg_cached scorer, rfg_op op, const void* s2, int64_t len2, int32_t width2,
+                                double score_cutoff, double score_hint, double* result);
+/* many choices in one launch (the README's scorer-over-choices loop, README.md:153-240):
+ * out[i] for choice i, out_dtype element type */
+rfg_status rfg_cached_score_many(rfg_cached scorer, rfg_op op, const rfg_strings* choices, rfg_cutoff cutoff,
+                                 rfg_dtype out_dtype, void* out, uint32_t flags);
+
+/* ---------------------------------------------------------------- all pairs
+ * cdist: out[q * ld + c] = scorer(queries[q]).op(choices[c]) for every pair, following
+ * the Cached* chain (form RFG_FORM_CACHED) or the free-function chain.  ld >= count of
+ * choices (0 means dense).  This is the batched persistent-kernel path. */
+rfg_status rfg_cdist(rfg_metric metric, rfg_op op, rfg_form form, const rfg_strings* queries,
+                     const rfg_strings* choices, const rfg_params* params, rfg_cutoff cutoff,
+                     rfg_dtype out_dtype, void* out, int64_t ld, uint32_t flags);
+
+/* ------------------------------------------------------- experimental::Multi*
+ * MultiLevenshtein (Levenshtein.hpp:297-419), MultiIndel (Indel.hpp:77-146),
+ * MultiLCSseq (LCSseq.hpp:77-195), MultiOSA (OSA.hpp:113-230), MultiJaro (Jaro.hpp:64-193),
+ * MultiJaroWinkler (JaroWinkler.hpp:75-166), fuzz::experimental::MultiRatio (fuzz.hpp:50-95).
+ * max_len is the MaxLen template argument (8, 16, 32 or 64). */
+rfg_status rfg_multi_create(rfg_metric metric, int32_t max_len, size_t count, const rfg_params* params,
+                            rfg_multi* out);
+rfg_status rfg_multi_destroy(rfg_multi scorer);
+rfg_status rfg_multi_insert(rfg_multi scorer, const void* s, int64_t len, int32_t width);
+rfg_status rfg_multi_result_count(rfg_multi scorer, size_t* out);
+rfg_status rfg_multi_score_i64(rfg_multi scorer, rfg_op op, int64_t* scores, size_t score_count, const void* s2,
+                               int64_t len2, int32_t width2, uint64_t score_cutoff);
+rfg_status rfg_multi_score_f64(rfg_multi scorer, rfg_op op, double* scores, size_t score_count, const void* s2,
+                               int64_t len2, int32_t width2, double score_cutoff);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RAPIDFUZZ_GB300_H */

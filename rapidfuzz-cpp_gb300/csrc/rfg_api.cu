@@ -1,0 +1,761 @@
+/*
+ * rfg_api.cu -- host runtime and C ABI of librapidfuzz_gb300.
+ *
+ * Every entry point ends in one engine: run_batch() scores a set of queries (the s1
+ * side, whose pattern tables are built on the device) against a set of choices (the
+ * s2 side).  Queries are classified by pattern words (1, 2, 4, 8 words in registers,
+ * or the any-length scratch kernel), each class is ordered longest first and cut
+ * into (query, choice-chunk) tiles that persistent CTAs pull from an atomic counter.
+ * The free functions and Cached* scorers are batches of one query; Multi* scorers are
+ * batches of many short queries against one choice; cdist is the general case.
+ *
+ * Device memory is taken from the stream-ordered pool (cudaMallocAsync) with a release
+ * threshold that keeps it cached between calls.  One library stream; calls from
+ * several host threads are serialised by a mutex.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "rapidfuzz_gb300.h"
+#include "rfg_device.cuh"
+#include "rfg_kernels.h"
+
+using namespace rfg;
+
+namespace {
+
+thread_local std::string g_err;
+
+rfg_status fail(rfg_status s, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return s;
+}
+
+#define RFG_CUDA(call)                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess) {                                                                    \
+            return fail(e_ == cudaErrorMemoryAllocation ? RFG_ERR_OUT_OF_MEMORY : RFG_ERR_CUDA,     \
+                        "%s failed: %s", #call, cudaGetErrorString(e_));                            \
+        }                                                                                           \
+    } while (0)
+
+#define RFG_TRY(expr)                        \
+    do {                                     \
+        rfg_status s_ = (expr);              \
+        if (s_ != RFG_OK) return s_;         \
+    } while (0)
+
+struct Ctx {
+    bool init = false;
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    std::recursive_mutex mu;
+    std::unordered_map<const void*, int> occ; /* (kernel) -> CTAs per SM at the default smem */
+};
+Ctx g;
+
+rfg_status ensure_ctx()
+{
+    if (g.init) return RFG_OK;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(RFG_ERR_NO_DEVICE, "no CUDA device available (%s); this library has no CPU path",
+                    cudaGetErrorString(e));
+    RFG_CUDA(cudaSetDevice(g.device));
+    RFG_CUDA(cudaDeviceGetAttribute(&g.sms, cudaDevAttrMultiProcessorCount, g.device));
+    RFG_CUDA(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+    cudaMemPool_t pool;
+    RFG_CUDA(cudaDeviceGetDefaultMemPool(&pool, g.device));
+    uint64_t thr = UINT64_MAX;
+    RFG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+    g.init = true;
+    return RFG_OK;
+}
+
+/* stream-ordered device allocation freed at scope exit */
+struct DBuf {
+    void* p = nullptr;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf()
+    {
+        if (p) cudaFreeAsync(p, g.stream);
+    }
+    rfg_status alloc(size_t bytes)
+    {
+        if (bytes == 0) bytes = 16;
+        cudaError_t e = cudaMallocAsync(&p, bytes, g.stream);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return fail(RFG_ERR_OUT_OF_MEMORY, "device allocation of %zu bytes failed: %s", bytes,
+                        cudaGetErrorString(e));
+        }
+        return RFG_OK;
+    }
+    template <typename T>
+    T* as() const
+    {
+        return static_cast<T*>(p);
+    }
+};
+
+inline bool valid_width(int w) { return w == 1 || w == 2 || w == 4 || w == 8; }
+
+inline u64 unit_at(const void* data, int width, int64_t i)
+{
+    switch (width) {
+    case 1: return ((const uint8_t*)data)[i];
+    case 2: return ((const uint16_t*)data)[i];
+    case 4: return ((const uint32_t*)data)[i];
+    default: return ((const uint64_t*)data)[i];
+    }
+}
+
+inline bool is_int_result(int metric, int op)
+{
+    if (metric == RFG_JARO || metric == RFG_JARO_WINKLER || metric == RFG_RATIO) return false;
+    return op == RFG_DISTANCE || op == RFG_SIMILARITY;
+}
+
+inline int next_pow2(int x)
+{
+    int p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+/* queries as the engine needs them: device strings plus host lengths and the number of
+ * code units >= 256 of each query (sizes the shared-memory hash table) */
+struct QuerySet {
+    KStrings dev{};
+    std::vector<int64_t> len;
+    std::vector<int32_t> wide;
+};
+
+rfg_status query_info_from_host(const void* data, const int64_t* off, int64_t n, int width, QuerySet* qs)
+{
+    qs->len.resize(n);
+    qs->wide.assign(n, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t a = off[i], b = off[i + 1];
+        if (a < 0 || b < a) return fail(RFG_ERR_INVALID_ARGUMENT, "offsets must be non-decreasing and >= 0");
+        if (b - a > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "strings longer than 2^31-1 code units");
+        qs->len[i] = b - a;
+        if (width > 1) {
+            int32_t w = 0;
+            for (int64_t k = a; k < b; ++k) w += unit_at(data, width, k) >= 256;
+            qs->wide[i] = w;
+        }
+    }
+    return RFG_OK;
+}
+
+/* copy a host batch to the device (data padded to 16 bytes) */
+rfg_status upload_strings(const rfg_strings* s, DBuf* data, DBuf* off, KStrings* out)
+{
+    const int64_t n = s->count;
+    const int64_t units = n > 0 ? s->offsets[n] : 0;
+    const size_t bytes = (size_t)units * s->char_width;
+    RFG_TRY(data->alloc(bytes + 16));
+    RFG_TRY(off->alloc((size_t)(n + 1) * 8));
+    if (bytes) RFG_CUDA(cudaMemcpyAsync(data->p, s->data, bytes, cudaMemcpyHostToDevice, g.stream));
+    RFG_CUDA(cudaMemcpyAsync(off->p, s->offsets, (size_t)(n + 1) * 8, cudaMemcpyHostToDevice, g.stream));
+    out->data = data->as<unsigned char>();
+    out->off = off->as<int64_t>();
+    out->n = n;
+    out->width = s->char_width;
+    return RFG_OK;
+}
+
+rfg_status check_strings(const rfg_strings* s, const char* what)
+{
+    if (!s) return fail(RFG_ERR_INVALID_ARGUMENT, "%s is NULL", what);
+    if (s->count < 0) return fail(RFG_ERR_INVALID_ARGUMENT, "%s: negative count", what);
+    if (!valid_width(s->char_width)) return fail(RFG_ERR_INVALID_ARGUMENT, "%s: char_width must be 1, 2, 4 or 8", what);
+    if (!s->offsets) return fail(RFG_ERR_INVALID_ARGUMENT, "%s: offsets is NULL", what);
+    return RFG_OK;
+}
+
+rfg_status check_metric_op(int metric, int op, int form)
+{
+    if (metric < RFG_LEVENSHTEIN || metric > RFG_RATIO) return fail(RFG_ERR_INVALID_ARGUMENT, "unknown metric %d", metric);
+    if (op < RFG_DISTANCE || op > RFG_NORMALIZED_SIMILARITY) return fail(RFG_ERR_INVALID_ARGUMENT, "unknown op %d", op);
+    if (form < RFG_FORM_FREE || form > RFG_FORM_MULTI) return fail(RFG_ERR_INVALID_ARGUMENT, "unknown form %d", form);
+    if (metric == RFG_RATIO && op != RFG_SIMILARITY)
+        return fail(RFG_ERR_INVALID_ARGUMENT, "fuzz::ratio only has a similarity");
+    return RFG_OK;
+}
+
+ScoreParams to_sp(const rfg_params* p)
+{
+    ScoreParams sp;
+    sp.ins = p ? p->insert_cost : 1;
+    sp.del = p ? p->delete_cost : 1;
+    sp.rep = p ? p->replace_cost : 1;
+    sp.prefix_weight = p ? p->prefix_weight : 0.1;
+    return sp;
+}
+
+rfg_status check_params(int metric, const ScoreParams& sp)
+{
+    if (metric == RFG_LEVENSHTEIN && (sp.ins < 0 || sp.del < 0 || sp.rep < 0))
+        return fail(RFG_ERR_INVALID_ARGUMENT, "Levenshtein weights must be >= 0");
+    return RFG_OK;
+}
+
+int occupancy(const void* fn, int block, size_t smem)
+{
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, block, smem) != cudaSuccess || nb < 1) nb = 1;
+    return nb;
+}
+
+/* size class of a query of m code units: pattern words held in registers, 0 = any-length kernel */
+inline int word_class(int64_t m)
+{
+    const int64_t w = (m + 63) / 64;
+    if (w <= 1) return 1;
+    if (w <= 2) return 2;
+    if (w <= 4) return 4;
+    if (w <= 8) return 8;
+    return 0;
+}
+
+struct BatchSpec {
+    int metric, op, form;
+    ScoreParams sp;
+    u64 ci;
+    double cf;
+    int out_dtype;
+    void* out; /* device */
+    int64_t ld;
+};
+
+int64_t g_tiles_target = 0; /* override of the tile-count target (autotuning) */
+
+/* Score every (query, choice) pair on the device, results to spec.out (device). */
+rfg_status run_batch(const QuerySet& q, const KStrings& c, const BatchSpec& spec)
+{
+    const int64_t nq = q.dev.n, nc = c.n;
+    if (nq == 0 || nc == 0) return RFG_OK;
+    const int fam = metric_family(spec.metric, spec.form, spec.sp);
+
+    /* classes: 1, 2, 4, 8 register words; index 4 = any length */
+    std::vector<int32_t> cls[5];
+    int64_t cls_maxlen[5] = {0, 0, 0, 0, 0};
+    int32_t cls_wide[5] = {0, 0, 0, 0, 0};
+    for (int64_t i = 0; i < nq; ++i) {
+        int k;
+        if (fam == FAM_WF || fam == FAM_NONE) k = 4;
+        else {
+            const int wc = word_class(q.len[i]);
+            k = wc == 1 ? 0 : wc == 2 ? 1 : wc == 4 ? 2 : wc == 8 ? 3 : 4;
+        }
+        cls[k].push_back((int32_t)i);
+        cls_maxlen[k] = std::max(cls_maxlen[k], q.len[i]);
+        cls_wide[k] = std::max(cls_wide[k], q.wide[i]);
+    }
+    size_t total = 0;
+    for (auto& v : cls) {
+        std::sort(v.begin(), v.end(), [&](int32_t a, int32_t b) {
+            return q.len[a] != q.len[b] ? q.len[a] > q.len[b] : a < b;
+        });
+        total += v.size();
+    }
+    std::vector<int32_t> qall;
+    qall.reserve(total);
+    size_t cls_off[5];
+    for (int k = 0; k < 5; ++k) {
+        cls_off[k] = qall.size();
+        qall.insert(qall.end(), cls[k].begin(), cls[k].end());
+    }
+    DBuf d_qlist, d_small;
+    RFG_TRY(d_qlist.alloc(qall.size() * 4));
+    RFG_TRY(d_small.alloc(16 * sizeof(int)));
+    RFG_CUDA(cudaMemcpyAsync(d_qlist.p, qall.data(), qall.size() * 4, cudaMemcpyHostToDevice, g.stream));
+    RFG_CUDA(cudaMemsetAsync(d_small.p, 0, 16 * sizeof(int), g.stream));
+    int* counters = d_small.as<int>();
+    int* err = counters + 15;
+
+    for (int k = 0; k < 5; ++k) {
+        if (cls[k].empty()) continue;
+        DBuf scratch; /* freed (stream-ordered) after this class's launch */
+        KParams a;
+        memset(&a, 0, sizeof a);
+        a.q = q.dev;
+        a.c = c;
+        a.qlist = d_qlist.as<int32_t>() + cls_off[k];
+        a.nq = (int32_t)cls[k].size();
+        a.counter = counters + k;
+        a.err = err;
+        a.metric = spec.metric;
+        a.op = spec.op;
+        a.form = spec.form;
+        a.sp = spec.sp;
+        a.ci = spec.ci;
+        a.cf = spec.cf;
+        a.out = spec.out;
+        a.out_dtype = spec.out_dtype;
+        a.ld = spec.ld;
+        a.hcap = (c.width > 1 && cls_wide[k] > 0) ? next_pow2(2 * cls_wide[k]) : 0;
+
+        const void* fn;
+        int block;
+        size_t smem = 0;
+        int per_sm;
+        if (k < 4) {
+            const int W = 1 << k;
+            switch (fam) {
+            case FAM_LEV: fn = tiles_kernel_lev(c.width, W); break;
+            case FAM_LCS: fn = tiles_kernel_lcs(c.width, W); break;
+            case FAM_OSA: fn = tiles_kernel_osa(c.width, W); break;
+            default: fn = tiles_kernel_jaro(c.width, W);
+            }
+            block = 256;
+            smem = tiles_smem_bytes(W, a.hcap);
+            if (smem > 48 * 1024) RFG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            per_sm = occupancy(fn, block, smem);
+        }
+        else {
+            fn = generic_kernel(fam == FAM_NONE ? FAM_WF : fam, c.width);
+            block = 128;
+            per_sm = 2;
+        }
+        /* tiles: enough to keep every SM busy and balanced, but each big enough to
+         * amortise the pattern build (longest queries first) */
+        const int64_t slots = (int64_t)g.sms * per_sm;
+        const int64_t target = g_tiles_target > 0 ? g_tiles_target : slots * 4;
+        int64_t chunk = (nc * a.nq + target - 1) / target;
+        chunk = std::max<int64_t>(chunk, block);
+        chunk = std::min<int64_t>(chunk, std::max<int64_t>(nc, 1));
+        chunk = (chunk + block - 1) / block * block;
+        a.chunk = chunk;
+        a.nchunks = (nc + chunk - 1) / chunk;
+        const int64_t ntiles = (int64_t)a.nq * a.nchunks;
+        if (ntiles > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "batch too large for one launch");
+        int64_t grid = std::min<int64_t>(ntiles, slots);
+        if (k == 4) {
+            /* any-length kernel: pattern table + per-thread state in global scratch */
+            const int wmax = (fam == FAM_WF || fam == FAM_NONE) ? 0 : (int)((cls_maxlen[k] + 63) / 64);
+            int64_t per_thread;
+            switch (fam) {
+            case FAM_LEV: per_thread = 2 * (int64_t)wmax; break;
+            case FAM_LCS: per_thread = wmax; break;
+            case FAM_OSA: per_thread = 4 * (int64_t)wmax; break;
+            case FAM_JARO: per_thread = 2 * (int64_t)wmax; break;
+            default: per_thread = cls_maxlen[k] + 1;
+            }
+            a.wmax = wmax;
+            a.scratch_per_thread = per_thread;
+            a.scratch_per_cta = (wmax ? (int64_t)(256 + a.hcap + 1) * wmax + a.hcap : 0) + (int64_t)block * per_thread;
+            RFG_TRY(scratch.alloc((size_t)grid * a.scratch_per_cta * 8));
+            a.scratch = scratch.as<u64>();
+        }
+        void* args[] = {&a};
+        RFG_CUDA(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(block), args, smem, g.stream));
+    }
+    int h_err = 0;
+    RFG_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, g.stream));
+    RFG_CUDA(cudaStreamSynchronize(g.stream));
+    if (h_err) return fail(RFG_ERR_DEVICE_CHECK, "device-side check failed (code %d)", h_err);
+    return RFG_OK;
+}
+
+size_t dtype_size(int dt) { return dt == RFG_I32 ? 4 : 8; }
+
+rfg_status check_dtype(int metric, int op, int dt)
+{
+    if (dt < RFG_I32 || dt > RFG_F64) return fail(RFG_ERR_INVALID_ARGUMENT, "unknown output dtype");
+    if (!is_int_result(metric, op) && dt != RFG_F64)
+        return fail(RFG_ERR_INVALID_ARGUMENT, "this metric/op returns doubles: use RFG_F64");
+    return RFG_OK;
+}
+
+/* cdist over host or device batches */
+rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const rfg_strings* C, const rfg_params* p,
+                      rfg_cutoff cut, int dt, void* out, int64_t ld, uint32_t flags)
+{
+    RFG_TRY(check_metric_op(metric, op, form));
+    RFG_TRY(check_strings(Q, "queries"));
+    RFG_TRY(check_strings(C, "choices"));
+    RFG_TRY(check_dtype(metric, op, dt));
+    const ScoreParams sp = to_sp(p);
+    RFG_TRY(check_params(metric, sp));
+    const int64_t nq = Q->count, nc = C->count;
+    if (ld == 0) ld = nc;
+    if (ld < nc) return fail(RFG_ERR_INVALID_ARGUMENT, "ld must be >= the number of choices");
+    if (!out && nq * nc) return fail(RFG_ERR_INVALID_ARGUMENT, "out is NULL");
+    RFG_TRY(ensure_ctx());
+
+    const bool dev_in = flags & RFG_DEVICE_INPUTS;
+    QuerySet qs;
+    DBuf qd, qo, cd, co, od;
+    KStrings ck;
+    if (dev_in) {
+        /* pattern tables need the query lengths and wide-unit counts on the host */
+        std::vector<int64_t> off(nq + 1);
+        RFG_CUDA(cudaMemcpyAsync(off.data(), Q->offsets, (nq + 1) * 8, cudaMemcpyDeviceToHost, g.stream));
+        RFG_CUDA(cudaStreamSynchronize(g.stream));
+        std::vector<unsigned char> qh;
+        if (Q->char_width > 1 && nq) {
+            qh.resize((size_t)off[nq] * Q->char_width);
+            RFG_CUDA(cudaMemcpyAsync(qh.data(), Q->data, qh.size(), cudaMemcpyDeviceToHost, g.stream));
+            RFG_CUDA(cudaStreamSynchronize(g.stream));
+        }
+        RFG_TRY(query_info_from_host(qh.data(), off.data(), nq, Q->char_width, &qs));
+        qs.dev = KStrings{(const unsigned char*)Q->data, Q->offsets, nq, Q->char_width};
+        ck = KStrings{(const unsigned char*)C->data, C->offsets, nc, C->char_width};
+    }
+    else {
+        if ((!Q->data && nq && Q->offsets[nq]) || (!C->data && nc && C->offsets[nc]))
+            return fail(RFG_ERR_INVALID_ARGUMENT, "string data is NULL");
+        RFG_TRY(query_info_from_host(Q->data, Q->offsets, nq, Q->char_width, &qs));
+        for (int64_t i = 0; i < nc; ++i)
+            if (C->offsets[i] < 0 || C->offsets[i + 1] < C->offsets[i] || C->offsets[i + 1] - C->offsets[i] > INT32_MAX)
+                return fail(RFG_ERR_INVALID_ARGUMENT, "choice offsets must be non-decreasing and >= 0");
+        RFG_TRY(upload_strings(Q, &qd, &qo, &qs.dev));
+        RFG_TRY(upload_strings(C, &cd, &co, &ck));
+    }
+    BatchSpec spec;
+    spec.metric = metric;
+    spec.op = op;
+    spec.form = form;
+    spec.sp = sp;
+    spec.ci = cut.cutoff_i;
+    spec.cf = cut.cutoff_f;
+    spec.out_dtype = dt;
+    spec.ld = ld;
+    const size_t esz = dtype_size(dt);
+    if (flags & RFG_DEVICE_OUTPUT) spec.out = out;
+    else {
+        RFG_TRY(od.alloc((size_t)nq * ld * esz));
+        spec.out = od.p;
+    }
+    RFG_TRY(run_batch(qs, ck, spec));
+    if (!(flags & RFG_DEVICE_OUTPUT) && nq * nc) {
+        RFG_CUDA(cudaMemcpy2DAsync(out, ld * esz, od.p, ld * esz, nc * esz, nq, cudaMemcpyDeviceToHost, g.stream));
+        RFG_CUDA(cudaStreamSynchronize(g.stream));
+    }
+    return RFG_OK;
+}
+
+/* one pair through the engine */
+rfg_status score_one(int metric, int op, int form, const void* s1, int64_t l1, int w1, const void* s2, int64_t l2,
+                     int w2, const rfg_params* p, rfg_cutoff cut, int dt, void* result)
+{
+    if (!valid_width(w1) || !valid_width(w2)) return fail(RFG_ERR_INVALID_ARGUMENT, "char width must be 1, 2, 4 or 8");
+    if (l1 < 0 || l2 < 0) return fail(RFG_ERR_INVALID_ARGUMENT, "negative length");
+    if ((!s1 && l1) || (!s2 && l2)) return fail(RFG_ERR_INVALID_ARGUMENT, "string data is NULL");
+    if (!result) return fail(RFG_ERR_INVALID_ARGUMENT, "result is NULL");
+    int64_t o1[2] = {0, l1}, o2[2] = {0, l2};
+    rfg_strings q{s1, o1, 1, w1}, c{s2, o2, 1, w2};
+    return cdist_impl(metric, op, form, &q, &c, p, cut, dt, result, 1, 0);
+}
+
+} // namespace
+
+/* ======================================================================== C ABI */
+
+struct rfg_cached_s {
+    int metric;
+    rfg_params params;
+    int width;
+    int64_t len;
+    std::vector<unsigned char> host; /* s1 (the reference's CachedX keeps a copy too) */
+    DBuf data, off;
+    QuerySet qs;
+};
+
+struct rfg_multi_s {
+    int metric;
+    int max_len;
+    size_t count;
+    rfg_params params;
+    std::vector<std::vector<u64>> strs; /* inserted strings, code units */
+    int width = 1;                      /* widest code unit seen */
+};
+
+extern "C" {
+
+int rfg_abi_version(void) { return RFG_ABI_VERSION; }
+
+const char* rfg_last_error(void) { return g_err.c_str(); }
+
+rfg_status rfg_set_device(int device)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (g.init && device != g.device) return fail(RFG_ERR_INVALID_ARGUMENT, "device already selected");
+    g.device = device;
+    return ensure_ctx();
+}
+
+rfg_status rfg_synchronize(void)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    RFG_TRY(ensure_ctx());
+    RFG_CUDA(cudaStreamSynchronize(g.stream));
+    return RFG_OK;
+}
+
+rfg_status rfg_score_i64(rfg_metric metric, rfg_op op, const void* s1, int64_t len1, int32_t width1, const void* s2,
+                         int64_t len2, int32_t width2, const rfg_params* params, uint64_t score_cutoff,
+                         uint64_t score_hint, int64_t* result)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (!is_int_result(metric, op)) return fail(RFG_ERR_INVALID_ARGUMENT, "this metric/op returns a double");
+    rfg_cutoff cut{score_cutoff, 0.0, score_hint, 0.0};
+    return score_one(metric, op, RFG_FORM_FREE, s1, len1, width1, s2, len2, width2, params, cut, RFG_I64, result);
+}
+
+rfg_status rfg_score_f64(rfg_metric metric, rfg_op op, const void* s1, int64_t len1, int32_t width1, const void* s2,
+                         int64_t len2, int32_t width2, const rfg_params* params, double score_cutoff, double score_hint,
+                         double* result)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (is_int_result(metric, op)) return fail(RFG_ERR_INVALID_ARGUMENT, "this metric/op returns an integer");
+    rfg_cutoff cut{0, score_cutoff, 0, score_hint};
+    return score_one(metric, op, RFG_FORM_FREE, s1, len1, width1, s2, len2, width2, params, cut, RFG_F64, result);
+}
+
+rfg_status rfg_cached_create(rfg_metric metric, const void* s1, int64_t len1, int32_t width1, const rfg_params* params,
+                             rfg_cached* out)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (!out) return fail(RFG_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    RFG_TRY(check_metric_op(metric, metric == RFG_RATIO ? RFG_SIMILARITY : RFG_DISTANCE, RFG_FORM_CACHED));
+    if (!valid_width(width1)) return fail(RFG_ERR_INVALID_ARGUMENT, "char width must be 1, 2, 4 or 8");
+    if (len1 < 0 || (!s1 && len1)) return fail(RFG_ERR_INVALID_ARGUMENT, "invalid s1");
+    RFG_TRY(check_params(metric, to_sp(params)));
+    RFG_TRY(ensure_ctx());
+    rfg_cached_s* h = new rfg_cached_s();
+    h->metric = metric;
+    const ScoreParams sp = to_sp(params);
+    h->params = rfg_params{sp.ins, sp.del, sp.rep, sp.prefix_weight};
+    h->width = width1;
+    h->len = len1;
+    h->host.assign((const unsigned char*)s1, (const unsigned char*)s1 + len1 * width1);
+    int64_t off[2] = {0, len1};
+    rfg_strings q{h->host.data(), off, 1, width1};
+    rfg_status st = query_info_from_host(h->host.data(), off, 1, width1, &h->qs);
+    if (st == RFG_OK) st = upload_strings(&q, &h->data, &h->off, &h->qs.dev);
+    if (st == RFG_OK && cudaStreamSynchronize(g.stream) != cudaSuccess) st = fail(RFG_ERR_CUDA, "upload failed");
+    if (st != RFG_OK) {
+        delete h;
+        return st;
+    }
+    *out = h;
+    return RFG_OK;
+}
+
+rfg_status rfg_cached_destroy(rfg_cached h)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    delete h;
+    return RFG_OK;
+}
+
+static rfg_status cached_many(rfg_cached h, int op, const rfg_strings* C, rfg_cutoff cut, int dt, void* out,
+                              uint32_t flags)
+{
+    if (!h) return fail(RFG_ERR_INVALID_ARGUMENT, "scorer is NULL");
+    RFG_TRY(check_metric_op(h->metric, op, RFG_FORM_CACHED));
+    RFG_TRY(check_strings(C, "choices"));
+    RFG_TRY(check_dtype(h->metric, op, dt));
+    RFG_TRY(ensure_ctx());
+    const int64_t nc = C->count;
+    DBuf cd, co, od;
+    KStrings ck;
+    if (flags & RFG_DEVICE_INPUTS) ck = KStrings{(const unsigned char*)C->data, C->offsets, nc, C->char_width};
+    else {
+        for (int64_t i = 0; i < nc; ++i)
+            if (C->offsets[i] < 0 || C->offsets[i + 1] < C->offsets[i])
+                return fail(RFG_ERR_INVALID_ARGUMENT, "choice offsets must be non-decreasing and >= 0");
+        RFG_TRY(upload_strings(C, &cd, &co, &ck));
+    }
+    BatchSpec spec;
+    spec.metric = h->metric;
+    spec.op = op;
+    spec.form = RFG_FORM_CACHED;
+    spec.sp = to_sp(&h->params);
+    spec.ci = cut.cutoff_i;
+    spec.cf = cut.cutoff_f;
+    spec.out_dtype = dt;
+    spec.ld = nc;
+    if (flags & RFG_DEVICE_OUTPUT) spec.out = out;
+    else {
+        RFG_TRY(od.alloc((size_t)nc * dtype_size(dt)));
+        spec.out = od.p;
+    }
+    RFG_TRY(run_batch(h->qs, ck, spec));
+    if (!(flags & RFG_DEVICE_OUTPUT) && nc) {
+        RFG_CUDA(cudaMemcpyAsync(out, od.p, (size_t)nc * dtype_size(dt), cudaMemcpyDeviceToHost, g.stream));
+        RFG_CUDA(cudaStreamSynchronize(g.stream));
+    }
+    return RFG_OK;
+}
+
+rfg_status rfg_cached_score_i64(rfg_cached h, rfg_op op, const void* s2, int64_t len2, int32_t width2,
+                                uint64_t score_cutoff, uint64_t score_hint, int64_t* result)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (!h) return fail(RFG_ERR_INVALID_ARGUMENT, "scorer is NULL");
+    if (!is_int_result(h->metric, op)) return fail(RFG_ERR_INVALID_ARGUMENT, "this metric/op returns a double");
+    if (!valid_width(width2) || len2 < 0 || (!s2 && len2) || !result) return fail(RFG_ERR_INVALID_ARGUMENT, "invalid s2");
+    int64_t off[2] = {0, len2};
+    rfg_strings c{s2, off, 1, width2};
+    return cached_many(h, op, &c, rfg_cutoff{score_cutoff, 0.0, score_hint, 0.0}, RFG_I64, result, 0);
+}
+
+rfg_status rfg_cached_score_f64(rfg_cached h, rfg_op op, const void* s2, int64_t len2, int32_t width2,
+                                double score_cutoff, double score_hint, double* result)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (!h) return fail(RFG_ERR_INVALID_ARGUMENT, "scorer is NULL");
+    if (is_int_result(h->metric, op)) return fail(RFG_ERR_INVALID_ARGUMENT, "this metric/op returns an integer");
+    if (!valid_width(width2) || len2 < 0 || (!s2 && len2) || !result) return fail(RFG_ERR_INVALID_ARGUMENT, "invalid s2");
+    int64_t off[2] = {0, len2};
+    rfg_strings c{s2, off, 1, width2};
+    return cached_many(h, op, &c, rfg_cutoff{0, score_cutoff, 0, score_hint}, RFG_F64, result, 0);
+}
+
+rfg_status rfg_cached_score_many(rfg_cached h, rfg_op op, const rfg_strings* choices, rfg_cutoff cutoff,
+                                 rfg_dtype out_dtype, void* out, uint32_t flags)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    return cached_many(h, op, choices, cutoff, out_dtype, out, flags);
+}
+
+rfg_status rfg_cdist(rfg_metric metric, rfg_op op, rfg_form form, const rfg_strings* queries,
+                     const rfg_strings* choices, const rfg_params* params, rfg_cutoff cutoff, rfg_dtype out_dtype,
+                     void* out, int64_t ld, uint32_t flags)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    return cdist_impl(metric, op, form, queries, choices, params, cutoff, out_dtype, out, ld, flags);
+}
+
+/* ---------------------------------------------------------------- Multi* */
+
+static size_t multi_vec_size(int max_len)
+{
+    /* AVX2 lanes of the reference build: 256 bits / lane width (Levenshtein.hpp:307-324) */
+    return max_len <= 8 ? 32 : max_len <= 16 ? 16 : max_len <= 32 ? 8 : 4;
+}
+
+static size_t multi_result_count(const rfg_multi_s* h)
+{
+    const size_t v = multi_vec_size(h->max_len);
+    return (h->count + v - 1) / v * v;
+}
+
+rfg_status rfg_multi_create(rfg_metric metric, int32_t max_len, size_t count, const rfg_params* params, rfg_multi* out)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (!out) return fail(RFG_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    RFG_TRY(check_metric_op(metric, metric == RFG_RATIO ? RFG_SIMILARITY : RFG_DISTANCE, RFG_FORM_MULTI));
+    if (max_len != 8 && max_len != 16 && max_len != 32 && max_len != 64)
+        return fail(RFG_ERR_INVALID_ARGUMENT, "MaxLen must be 8, 16, 32 or 64");
+    const ScoreParams sp = to_sp(params);
+    /* MultiLevenshtein only supports insert = delete = 1, replace <= 2 (Levenshtein.hpp:338-339) */
+    if (metric == RFG_LEVENSHTEIN && (sp.del != 1 || sp.ins != 1 || sp.rep > 2 || sp.rep < 0))
+        return fail(RFG_ERR_INVALID_ARGUMENT, "unsupported weights");
+    rfg_multi_s* h = new rfg_multi_s();
+    h->metric = metric;
+    h->max_len = max_len;
+    h->count = count;
+    h->params = rfg_params{sp.ins, sp.del, sp.rep, sp.prefix_weight};
+    *out = h;
+    return RFG_OK;
+}
+
+rfg_status rfg_multi_destroy(rfg_multi h)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    delete h;
+    return RFG_OK;
+}
+
+rfg_status rfg_multi_insert(rfg_multi h, const void* s, int64_t len, int32_t width)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (!h) return fail(RFG_ERR_INVALID_ARGUMENT, "scorer is NULL");
+    if (!valid_width(width) || len < 0 || (!s && len)) return fail(RFG_ERR_INVALID_ARGUMENT, "invalid string");
+    if (h->strs.size() >= h->count) return fail(RFG_ERR_INVALID_ARGUMENT, "out of bounds insert");
+    if (len > h->max_len) return fail(RFG_ERR_INVALID_ARGUMENT, "string longer than MaxLen");
+    std::vector<u64> v(len);
+    for (int64_t i = 0; i < len; ++i) v[i] = unit_at(s, width, i);
+    h->strs.push_back(std::move(v));
+    h->width = std::max(h->width, (int)width);
+    return RFG_OK;
+}
+
+rfg_status rfg_multi_result_count(rfg_multi h, size_t* out)
+{
+    if (!h || !out) return fail(RFG_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = multi_result_count(h);
+    return RFG_OK;
+}
+
+static rfg_status multi_score(rfg_multi h, int op, void* scores, size_t score_count, const void* s2, int64_t len2,
+                              int32_t width2, rfg_cutoff cut, int dt)
+{
+    if (!h) return fail(RFG_ERR_INVALID_ARGUMENT, "scorer is NULL");
+    RFG_TRY(check_metric_op(h->metric, op, RFG_FORM_MULTI));
+    if (!valid_width(width2) || len2 < 0 || (!s2 && len2)) return fail(RFG_ERR_INVALID_ARGUMENT, "invalid s2");
+    const size_t rc = multi_result_count(h);
+    if (score_count < rc) return fail(RFG_ERR_INVALID_ARGUMENT, "scores has to have >= result_count() elements");
+    if (!scores && rc) return fail(RFG_ERR_INVALID_ARGUMENT, "scores is NULL");
+    /* declared slots not inserted yet, and the padding up to result_count(), score as
+     * empty strings */
+    const int w = h->width;
+    std::vector<int64_t> off(rc + 1, 0);
+    for (size_t i = 0; i < rc; ++i) off[i + 1] = off[i] + (i < h->strs.size() ? (int64_t)h->strs[i].size() : 0);
+    std::vector<unsigned char> data((size_t)off[rc] * w + 8);
+    for (size_t i = 0; i < h->strs.size(); ++i)
+        for (size_t k = 0; k < h->strs[i].size(); ++k) {
+            const u64 v = h->strs[i][k];
+            unsigned char* dst = data.data() + (size_t)(off[i] + k) * w;
+            memcpy(dst, &v, w); /* little-endian: the low w bytes */
+        }
+    rfg_strings q{data.data(), off.data(), (int64_t)rc, w};
+    int64_t o2[2] = {0, len2};
+    rfg_strings c{s2, o2, 1, width2};
+    return cdist_impl(h->metric, op, RFG_FORM_MULTI, &q, &c, &h->params, cut, dt, scores, 1, 0);
+}
+
+rfg_status rfg_multi_score_i64(rfg_multi h, rfg_op op, int64_t* scores, size_t score_count, const void* s2,
+                               int64_t len2, int32_t width2, uint64_t score_cutoff)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (h && !is_int_result(h->metric, op)) return fail(RFG_ERR_INVALID_ARGUMENT, "this metric/op returns doubles");
+    return multi_score(h, op, scores, score_count, s2, len2, width2, rfg_cutoff{score_cutoff, 0.0, 0, 0.0}, RFG_I64);
+}
+
+rfg_status rfg_multi_score_f64(rfg_multi h, rfg_op op, double* scores, size_t score_count, const void* s2,
+                               int64_t len2, int32_t width2, double score_cutoff)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (h && is_int_result(h->metric, op)) return fail(RFG_ERR_INVALID_ARGUMENT, "this metric/op returns integers");
+    return multi_score(h, op, scores, score_count, s2, len2, width2, rfg_cutoff{0, score_cutoff, 0, 0.0}, RFG_F64);
+}
+
+} /* extern "C" */

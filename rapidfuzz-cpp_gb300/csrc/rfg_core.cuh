@@ -509,10 +509,38 @@ RFG_HD i64 lev_band(const PMW& pm, int pw, int m, const TXT& t, int n, int K)
     return (i64)n; /* n == 0; callers never ask (|m-n| <= K < m) */
 }
 
-/* Jaro with P (= s1) of up to 64*W chars and an effective text of <= 64 chars:
- * the greedy flagging of flag_similar_characters_block (Jaro_impl.hpp:134-256), with
- * the window masks built per word, and the transposition count of
- * count_transpositions_block (Jaro_impl.hpp:278-315). */
+/* Jaro with P (= s1) of up to 64*W chars and a text of any length: the greedy
+ * flagging of flag_similar_characters_block (Jaro_impl.hpp:134-256), with the window
+ * masks built per word, and the transposition count of count_transpositions_block
+ * (Jaro_impl.hpp:278-315), which pairs the k-th flagged text character with the k-th
+ * flagged pattern position.  Up to 64 relevant text characters the text flags live in
+ * one register; beyond that the flagging is run a second time and each newly flagged
+ * text character is compared on the fly, so no per-text storage is needed. */
+template <int W, typename PMW, typename TXT>
+RFG_HD bool jaro_flag_step(const PMW& pm, u64* pflag, u64 c, int lo, int hi)
+{
+    bool found = false;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        const u64 x = pm(c, w) & range_mask(lo - 64 * w, hi - 64 * w) & ~pflag[w];
+        if (!found && x) {
+            pflag[w] |= blsi(x);
+            found = true;
+        }
+    }
+    return found;
+}
+
+template <int W>
+RFG_HD u64 select_word(const u64* v, int idx)
+{
+    u64 r = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+        if (w == idx) r = v[w];
+    return r;
+}
+
 template <int W, typename PMW, typename TXT>
 RFG_HD void jaro_multi(const PMW& pm, int pl, const TXT& t, int tl, int* common, int* transp)
 {
@@ -525,44 +553,254 @@ RFG_HD void jaro_multi(const PMW& pm, int pl, const TXT& t, int tl, int* common,
     for (int w = 0; w < W; ++w) pflag[w] = 0;
     u64 tflag = 0;
     for (int j = 0; j < te; ++j) {
-        const u64 c = t[j];
-        const int lo = j - bound, hi = j + bound;
-        bool found = false;
-#pragma unroll
-        for (int w = 0; w < W; ++w) {
-            const u64 x = pm(c, w) & range_mask(lo - 64 * w, hi - 64 * w) & ~pflag[w];
-            if (!found && x) {
-                pflag[w] |= blsi(x);
-                found = true;
-            }
-        }
-        tflag |= (u64)found << j;
+        const bool f = jaro_flag_step<W, PMW, TXT>(pm, pflag, t[j], j - bound, j + bound);
+        if (j < 64) tflag |= (u64)f << j;
     }
     int cc = 0;
 #pragma unroll
     for (int w = 0; w < W; ++w) cc += popc64(pflag[w]);
     *common = cc;
     int tr = 0, pwi = 0;
-    while (tflag) {
-        /* next flagged pattern position, in order */
-        u64 pf = 0;
-#pragma unroll
-        for (int w = 0; w < W; ++w)
-            if (w == pwi) pf = pflag[w];
-        while (!pf) {
-            ++pwi;
-#pragma unroll
-            for (int w = 0; w < W; ++w)
-                if (w == pwi) pf = pflag[w];
+    u64 pf = select_word<W>(pflag, 0);
+    auto next_pbit = [&]() -> u64 {
+        while (!pf) pf = select_word<W>(pflag, ++pwi);
+        const u64 b = blsi(pf);
+        pf ^= b;
+        return b;
+    };
+    if (te <= 64) {
+        while (tflag) {
+            const u64 pbit = next_pbit();
+            tr += (pm(t[ctz64(tflag)], pwi) & pbit) == 0;
+            tflag = blsr(tflag);
         }
-        const u64 pbit = blsi(pf);
-        tr += (pm(t[ctz64(tflag)], pwi) & pbit) == 0;
-        tflag = blsr(tflag);
+    }
+    else {
+        u64 pflag2[W];
 #pragma unroll
-        for (int w = 0; w < W; ++w)
-            if (w == pwi) pflag[w] ^= pbit;
+        for (int w = 0; w < W; ++w) pflag2[w] = 0;
+        for (int j = 0; j < te; ++j) {
+            const u64 r = t[j];
+            if (jaro_flag_step<W, PMW, TXT>(pm, pflag2, r, j - bound, j + bound)) {
+                const u64 pbit = next_pbit();
+                tr += (pm(r, pwi) & pbit) == 0;
+            }
+        }
     }
     *transp = tr;
+}
+
+/* ======================================================= any-length cores
+ * Runtime word count W, state in caller-provided memory (global scratch on the
+ * device): the same recurrences as the register-resident cores above. */
+
+template <typename PMW, typename TXT>
+RFG_HD i64 lev_multi_rt(const PMW& pm, int W, int m, const TXT& t, int n, i64 K, u64* VP, u64* VN)
+{
+    for (int w = 0; w < W; ++w) {
+        VP[w] = ~0ull;
+        VN[w] = 0;
+    }
+    const bool check = K < (i64)(m > n ? m : n);
+    for (int j = 0; j < n; ++j) {
+        const u64 c = t[j];
+        u64 hp_c = 1, hn_c = 0;
+        for (int w = 0; w < W; ++w) {
+            const u64 X = pm(c, w) | hn_c;
+            const u64 vp = VP[w], vn = VN[w];
+            const u64 D0 = (((X & vp) + vp) ^ vp) | X | vn;
+            u64 HP = vn | ~(D0 | vp);
+            u64 HN = D0 & vp;
+            const u64 hp_o = HP >> 63, hn_o = HN >> 63;
+            HP = (HP << 1) | hp_c;
+            HN = (HN << 1) | hn_c;
+            hp_c = hp_o;
+            hn_c = hn_o;
+            VP[w] = HN | ~(D0 | HP);
+            VN[w] = HP & D0;
+        }
+        if (check && (j & 7) == 7) {
+            const int jj = j + 1, is = m - n + jj;
+            if (is >= 0) {
+                i64 lb = jj;
+                for (int w = 0; w * 64 < is; ++w) {
+                    const u64 lm = low_mask(is - 64 * w);
+                    lb += popc64(VP[w] & lm) - popc64(VN[w] & lm);
+                }
+                if (lb > K) return K + 1;
+            }
+        }
+    }
+    i64 d = n;
+    for (int w = 0; w * 64 < m; ++w) {
+        const u64 lm = low_mask(m - 64 * w);
+        d += popc64(VP[w] & lm) - popc64(VN[w] & lm);
+    }
+    return d;
+}
+
+template <typename PMW, typename TXT>
+RFG_HD i64 lcs_multi_rt(const PMW& pm, int W, int m, const TXT& t, int n, i64 Kd, u64* S)
+{
+    for (int w = 0; w < W; ++w) S[w] = ~0ull;
+    const bool check = Kd < (i64)(m + n);
+    for (int j = 0; j < n; ++j) {
+        const u64 c = t[j];
+        u32 carry = 0;
+        for (int w = 0; w < W; ++w) {
+            const u64 X = pm(c, w);
+            const u64 sv = S[w];
+            const u64 u = sv & X;
+            const u64 x = add_carry(sv, u, carry, &carry);
+            S[w] = x | (sv - u);
+        }
+        if (check && (j & 7) == 7) {
+            const int jj = j + 1, is = m - n + jj;
+            if (is >= 0) {
+                i64 l = 0;
+                for (int w = 0; w * 64 < is; ++w) l += popc64(~S[w] & low_mask(is - 64 * w));
+                if ((i64)is + jj - 2 * l > Kd) return -1;
+            }
+        }
+    }
+    i64 l = 0;
+    for (int w = 0; w * 64 < m; ++w) l += popc64(~S[w] & low_mask(m - 64 * w));
+    return l;
+}
+
+template <typename PMW, typename TXT>
+RFG_HD i64 osa_multi_rt(const PMW& pm, int W, int m, const TXT& t, int n, i64 K, u64* VP, u64* VN, u64* D0v,
+                        u64* PMo)
+{
+    for (int w = 0; w < W; ++w) {
+        VP[w] = ~0ull;
+        VN[w] = 0;
+        D0v[w] = 0;
+        PMo[w] = 0;
+    }
+    const bool check = K < (i64)(m > n ? m : n);
+    for (int j = 0; j < n; ++j) {
+        const u64 c = t[j];
+        u64 hp_c = 1, hn_c = 0, d0_prev_word = 0, pm_prev_word = 0;
+        for (int w = 0; w < W; ++w) {
+            const u64 X = pm(c, w);
+            const u64 vp = VP[w], vn = VN[w], d0_old = D0v[w];
+            const u64 TR = ((((~d0_old) & X) << 1) | (((~d0_prev_word) & pm_prev_word) >> 63)) & PMo[w];
+            const u64 Xc = X | hn_c;
+            const u64 D0 = (((Xc & vp) + vp) ^ vp) | Xc | vn | TR;
+            u64 HP = vn | ~(D0 | vp);
+            u64 HN = D0 & vp;
+            const u64 hp_o = HP >> 63, hn_o = HN >> 63;
+            HP = (HP << 1) | hp_c;
+            HN = (HN << 1) | hn_c;
+            hp_c = hp_o;
+            hn_c = hn_o;
+            VP[w] = HN | ~(D0 | HP);
+            VN[w] = HP & D0;
+            d0_prev_word = d0_old;
+            pm_prev_word = X;
+            D0v[w] = D0;
+            PMo[w] = X;
+        }
+        if (check && (j & 7) == 7) {
+            const int jj = j + 1, is = m - n + jj;
+            if (is >= 0) {
+                i64 lb = jj;
+                for (int w = 0; w * 64 < is; ++w) {
+                    const u64 lm = low_mask(is - 64 * w);
+                    lb += popc64(VP[w] & lm) - popc64(VN[w] & lm);
+                }
+                if (lb > K) return K + 1;
+            }
+        }
+    }
+    i64 d = n;
+    for (int w = 0; w * 64 < m; ++w) {
+        const u64 lm = low_mask(m - 64 * w);
+        d += popc64(VP[w] & lm) - popc64(VN[w] & lm);
+    }
+    return d;
+}
+
+/* Jaro with any pattern length: flags in caller memory (W words), two-pass
+ * transposition count (see jaro_multi) */
+template <typename PMW>
+RFG_HD bool jaro_flag_step_rt(const PMW& pm, int W, u64* pflag, u64 c, int lo, int hi)
+{
+    int w0 = lo < 0 ? 0 : lo >> 6;
+    const int w1 = hi >> 6;
+    for (int w = w0; w <= w1 && w < W; ++w) {
+        const u64 x = pm(c, w) & range_mask(lo - 64 * w, hi - 64 * w) & ~pflag[w];
+        if (x) {
+            pflag[w] |= blsi(x);
+            return true;
+        }
+    }
+    return false;
+}
+
+template <typename PMW, typename TXT>
+RFG_HD void jaro_multi_rt(const PMW& pm, int W, int pl, const TXT& t, int tl, int* common, int* transp, u64* pflag,
+                          u64* pflag2)
+{
+    int bound = (pl > tl ? pl : tl) / 2;
+    if (bound > 0) --bound;
+    int te = tl;
+    if (te > pl + bound) te = pl + bound;
+    for (int w = 0; w < W; ++w) {
+        pflag[w] = 0;
+        pflag2[w] = 0;
+    }
+    for (int j = 0; j < te; ++j) jaro_flag_step_rt(pm, W, pflag, t[j], j - bound, j + bound);
+    int cc = 0;
+    for (int w = 0; w < W; ++w) cc += popc64(pflag[w]);
+    *common = cc;
+    int tr = 0, pwi = 0;
+    u64 pf = W > 0 ? pflag[0] : 0;
+    for (int j = 0; j < te; ++j) {
+        const u64 r = t[j];
+        if (jaro_flag_step_rt(pm, W, pflag2, r, j - bound, j + bound)) {
+            while (!pf) pf = pflag[++pwi];
+            const u64 pbit = blsi(pf);
+            pf ^= pbit;
+            tr += (pm(r, pwi) & pbit) == 0;
+        }
+    }
+    *transp = tr;
+}
+
+/* generalized Wagner-Fischer (Levenshtein_impl.hpp:85-155): weighted distance,
+ * common affix stripped, `cache` holds m+1 entries; S1/S2 yield raw code units */
+template <typename S1, typename S2>
+RFG_HD u64 wf_distance(const S1& s1, int m, const S2& s2, int n, const ScoreParams& w, u64 max, u64* cache)
+{
+    const u64 ins = (u64)w.ins, del = (u64)w.del, rep = (u64)w.rep;
+    const u64 min_edits = m > n ? (u64)(m - n) * del : (u64)(n - m) * ins;
+    if (min_edits > max) return max + 1;
+    int a0 = 0, a1 = m, b0 = 0, b1 = n;
+    while (a0 < a1 && b0 < b1 && s1[a0] == s2[b0]) ++a0, ++b0;
+    while (a0 < a1 && b0 < b1 && s1[a1 - 1] == s2[b1 - 1]) --a1, --b1;
+    const int mm = a1 - a0;
+    for (int i = 0; i <= mm; ++i) cache[i] = (u64)i * del;
+    for (int j = b0; j < b1; ++j) {
+        const u64 cj = s2[j];
+        u64 temp = cache[0];
+        cache[0] += ins;
+        for (int i = 0; i < mm; ++i) {
+            if (s1[a0 + i] != cj) {
+                u64 v = cache[i] + del;
+                const u64 v2 = cache[i + 1] + ins;
+                const u64 v3 = temp + rep;
+                v = v2 < v ? v2 : v;
+                temp = v3 < v ? v3 : v;
+            }
+            const u64 nx = cache[i + 1];
+            cache[i + 1] = temp;
+            temp = nx;
+        }
+    }
+    const u64 d = cache[mm];
+    return d <= max ? d : max + 1;
 }
 
 /* ====================================================== formula chains

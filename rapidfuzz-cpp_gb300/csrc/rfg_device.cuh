@@ -1,0 +1,433 @@
+/*
+ * rfg_device.cuh -- the scoring kernels: one persistent CTA per SM slot pulls
+ * (query, choice-chunk) tiles from an atomic work counter, builds the query's
+ * pattern-match table in shared memory and scores the chunk one pair per thread.
+ *
+ * Shared-memory pattern table (the device form of BlockPatternMatchVector,
+ * rapidfuzz/details/PatternMatchVector.hpp:136-221): `rows` holds W words per row;
+ * rows 0..255 are code units below 256, rows 256..256+hcap-1 the slots of an
+ * open-addressing table for wider code units (keys in `keys`, 0 = empty, so the
+ * reference's CPython-style 128-slot map becomes a linear-probing table sized by the
+ * host to twice the query's wide code units), and the last row is all zero (code
+ * units the query does not contain).  Text characters are resolved to a row index
+ * once; the cores then read `rows[r * W + w]`.
+ */
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "rfg_core.cuh"
+
+namespace rfg {
+
+struct KStrings {
+    const unsigned char* data; /* packed code units */
+    const int64_t* off;        /* count+1 offsets in code units */
+    int64_t n;
+    int width;
+};
+
+struct KParams {
+    KStrings q, c;
+    const int32_t* qlist; /* queries of this launch (size class), longest first */
+    int32_t nq;
+    int64_t chunk;   /* choices per tile */
+    int64_t nchunks;
+    int* counter;    /* tile counter, zero before the launch */
+    int* err;        /* device-side check flag */
+    int metric, op, form;
+    ScoreParams sp;
+    u64 ci;
+    double cf;
+    void* out;
+    int out_dtype; /* 0 i32, 1 i64, 2 f64 */
+    int64_t ld;
+    int hcap;      /* hash slots for code units >= 256 (power of two, or 0) */
+    /* generic (scratch) kernels */
+    u64* scratch;
+    int64_t scratch_per_cta;    /* u64 words of the per-CTA pattern table region */
+    int64_t scratch_per_thread; /* u64 words of each thread's state */
+    int wmax;                   /* pattern words of the generic class */
+};
+
+/* ----------------------------------------------------------------- helpers */
+
+__device__ __forceinline__ u64 load_unit(const unsigned char* base, int width, int64_t i)
+{
+    switch (width) {
+    case 1: return __ldg(base + i);
+    case 2: return __ldg((const unsigned short*)base + i);
+    case 4: return __ldg((const unsigned int*)base + i);
+    default: return __ldg((const unsigned long long*)base + i);
+    }
+}
+
+__device__ __forceinline__ u32 hash_slot(u64 c, int hmask) { return (u32)((c * 0x9E3779B97F4A7C15ull) >> 32) & (u32)hmask; }
+
+/* row index of code unit c in a table with hcap hash slots */
+__device__ __forceinline__ int resolve_row(const u64* keys, int hcap, u64 c)
+{
+    if (c < 256) return (int)c;
+    if (!hcap) return 256;
+    u32 k = hash_slot(c, hcap - 1);
+    for (int probe = 0; probe < hcap; ++probe) {
+        const u64 key = keys[k];
+        if (key == c) return 256 + (int)k;
+        if (key == 0) break;
+        k = (k + 1) & (u32)(hcap - 1);
+    }
+    return 256 + hcap;
+}
+
+/* Build the pattern table of query string (base, m, width) into rows/keys.  Must be
+ * called by all threads of the CTA; ends with a barrier. */
+template <int W>
+__device__ void build_pm(u64* rows, u64* keys, int hcap, const unsigned char* base, int m, int width, int* err)
+{
+    const int nrows = 256 + hcap + 1;
+    for (int i = threadIdx.x; i < nrows * W; i += blockDim.x) rows[i] = 0;
+    for (int i = threadIdx.x; i < hcap; i += blockDim.x) keys[i] = 0;
+    __syncthreads();
+    if (hcap) {
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            const u64 c = load_unit(base, width, i);
+            if (c < 256) continue;
+            u32 k = hash_slot(c, hcap - 1);
+            int probe = 0;
+            for (; probe < hcap; ++probe) {
+                const u64 old = atomicCAS((unsigned long long*)&keys[k], 0ull, (unsigned long long)c);
+                if (old == 0 || old == c) break;
+                k = (k + 1) & (u32)(hcap - 1);
+            }
+            if (probe == hcap) atomicExch(err, 1); /* table sized too small by the host */
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const u64 c = load_unit(base, width, i);
+        const int r = resolve_row(keys, hcap, c);
+        if (r < 256 + hcap) atomicOr((unsigned long long*)&rows[r * W + (i >> 6)], 1ull << (i & 63));
+    }
+    __syncthreads();
+}
+
+/* pattern accessors over resolved rows */
+template <int W>
+struct PMRows {
+    const u64* rows;
+    __device__ __forceinline__ u64 operator()(u64 r) const { return rows[r * W]; }
+    __device__ __forceinline__ u64 operator()(u64 r, int w) const { return rows[r * W + w]; }
+};
+
+/* text accessor: yields the resolved row of s2[j] */
+template <typename CT, bool WIDE>
+struct TextRows {
+    const CT* p;
+    const u64* keys;
+    int hcap;
+    __device__ __forceinline__ u64 operator[](int j) const
+    {
+        const u64 c = (u64)__ldg(p + j);
+        if (!WIDE) return c;
+        return (u64)resolve_row(keys, hcap, c);
+    }
+};
+
+__device__ __forceinline__ void store_result(const KParams& a, int64_t q, int64_t c, i64 vi, double vf, bool is_int)
+{
+    const int64_t idx = q * a.ld + c;
+    switch (a.out_dtype) {
+    case 0: ((int32_t*)a.out)[idx] = (int32_t)vi; break;
+    case 1: ((int64_t*)a.out)[idx] = vi; break;
+    default: ((double*)a.out)[idx] = is_int ? (double)vi : vf;
+    }
+}
+
+__device__ __forceinline__ bool result_is_int(int metric, int op)
+{
+    if (metric == JARO || metric == JARO_WINKLER || metric == RATIO) return false;
+    return op == DISTANCE || op == SIMILARITY;
+}
+
+/* -------------------------------------------------------- integer families */
+
+template <int FAM, int W, typename PMF, typename TXT>
+__device__ __forceinline__ i64 run_int_core(const PMF& pm, int m, const TXT& t, int n, i64 K)
+{
+    if (FAM == FAM_LCS) {
+        if (m == 0 || n == 0) return 0;
+        if (K < (i64)(m > n ? m - n : n - m)) return -1; /* Indel distance >= |m-n| */
+        if (W == 1) return lcs_word(pm, m, t, n, K);
+        return lcs_multi<W>(pm, m, t, n, K);
+    }
+    if (m == 0) return n;
+    const i64 diff = m > n ? m - n : n - m;
+    if (K < diff) return K + 1; /* length filter (Levenshtein_impl.hpp:863) */
+    if (FAM == FAM_OSA) {
+        if (n == 0) return m;
+        if (W == 1) return osa_word(pm, m, t, n, K);
+        return osa_multi<W>(pm, m, t, n, K);
+    }
+    /* FAM_LEV */
+    if (n == 0) return m;
+    if (W == 1) return lev_word(pm, m, t, n, K);
+    /* a diagonal band narrower than the full pattern (Levenshtein_impl.hpp:876-897) */
+    if (K < m) {
+        const i64 band = 2 * K + 1;
+        if (W > 1 && band <= 64) return lev_band<1>(pm, W, m, t, n, (int)K);
+        if (W > 2 && band <= 128) return lev_band<2>(pm, W, m, t, n, (int)K);
+        if (W > 4 && band <= 256) return lev_band<4>(pm, W, m, t, n, (int)K);
+    }
+    return lev_multi<W>(pm, m, t, n, K);
+}
+
+/* one (query, choice) pair of an integer-valued or Jaro family */
+template <int FAM, int W, typename CT>
+__device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, const u64* keys, int64_t qi, int m,
+                                           const u64* qpre, int64_t ci)
+{
+    const int64_t o0 = a.c.off[ci], o1 = a.c.off[ci + 1];
+    const int n = (int)(o1 - o0);
+    const CT* s2 = (const CT*)a.c.data + o0;
+    PairSpec s;
+    s.metric = a.metric;
+    s.op = a.op;
+    s.form = a.form;
+    s.l1 = (u64)m;
+    s.l2 = (u64)n;
+    s.ci = a.ci;
+    s.cf = a.cf;
+    s.p = a.sp;
+    const PMRows<W> pm{rows};
+    const TextRows<CT, (sizeof(CT) > 1)> txt{s2, keys, a.hcap};
+    i64 vi = 0;
+    double vf = 0.0;
+    if (FAM == FAM_JARO) {
+        i64 prefix = 0;
+        const int mx = (m < n ? m : n) < 4 ? (m < n ? m : n) : 4;
+        for (; prefix < mx; ++prefix)
+            if ((u64)__ldg(s2 + prefix) != qpre[prefix]) break;
+        int common = 0, transp = 0;
+        if (m > 0 && n > 0 && jaro_pair_needs_counts(s, prefix)) {
+            if (W == 1) {
+                int bound = (m > n ? m : n) / 2;
+                if (bound > 0) --bound;
+                const int te = n < m + bound ? n : m + bound;
+                if (te <= 64) jaro_word(pm, m, txt, n, &common, &transp);
+                else jaro_multi<1>(pm, m, txt, n, &common, &transp);
+            }
+            else {
+                jaro_multi<W>(pm, m, txt, n, &common, &transp);
+            }
+        }
+        vf = finish_jaro(s, prefix, common, transp);
+        store_result(a, qi, ci, 0, vf, false);
+        return;
+    }
+    const Plan pl = plan_int(s);
+    i64 raw = 0;
+    if (pl.run) raw = run_int_core<FAM, W>(pm, m, txt, n, pl.K);
+    finish_int(s, pl, raw, &vi, &vf);
+    store_result(a, qi, ci, vi, vf, result_is_int(a.metric, a.op));
+}
+
+/* -------------------------------------------------------------- the kernel */
+
+template <int FAM, typename CT, int W>
+__global__ void __launch_bounds__(256) k_tiles(const KParams a)
+{
+    extern __shared__ u64 smem[];
+    const int nrows = 256 + a.hcap + 1;
+    u64* rows = smem;
+    u64* keys = smem + (size_t)nrows * W;
+    __shared__ int64_t s_tile;
+    __shared__ u64 s_qpre[4];
+    int64_t cur_q = -1;
+    int m = 0;
+    const int64_t ntiles = (int64_t)a.nq * a.nchunks;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(a.counter, 1);
+        __syncthreads();
+        const int64_t t = s_tile;
+        if (t >= ntiles) break;
+        const int64_t qi = a.qlist[t / a.nchunks];
+        const int64_t ch = t % a.nchunks;
+        if (qi != cur_q) {
+            const int64_t q0 = a.q.off[qi];
+            m = (int)(a.q.off[qi + 1] - q0);
+            const unsigned char* qb = a.q.data + q0 * a.q.width;
+            if (m > 64 * W) { /* the host classified this query into a smaller class */
+                if (threadIdx.x == 0) atomicExch(a.err, 2);
+                m = 64 * W;
+            }
+            build_pm<W>(rows, keys, a.hcap, qb, m, a.q.width, a.err);
+            if (threadIdx.x < 4) s_qpre[threadIdx.x] = (int)threadIdx.x < m ? load_unit(qb, a.q.width, threadIdx.x) : 0;
+            __syncthreads();
+            cur_q = qi;
+        }
+        const int64_t c0 = ch * a.chunk;
+        const int64_t c1 = c0 + a.chunk < a.c.n ? c0 + a.chunk : a.c.n;
+        for (int64_t ci = c0 + threadIdx.x; ci < c1; ci += blockDim.x)
+            score_pair<FAM, W, CT>(a, rows, keys, qi, m, s_qpre, ci);
+        __syncthreads();
+    }
+}
+
+/* --------------------------------------------- any-length kernel (scratch)
+ * Queries longer than 512 code units (and the weighted Wagner-Fischer family) run one
+ * pair per thread with their state in global scratch: per CTA a pattern table of
+ * (256 + hcap + 1) * wmax words plus hcap keys, then per thread scratch_per_thread
+ * words of recurrence state (VP/VN/..., Jaro flags, or the Wagner-Fischer row). */
+
+template <typename CT>
+struct RawText {
+    const CT* p;
+    __device__ __forceinline__ u64 operator[](int j) const { return (u64)__ldg(p + j); }
+};
+
+struct RawQuery {
+    const unsigned char* p;
+    int width;
+    __device__ __forceinline__ u64 operator[](int j) const { return load_unit(p, width, j); }
+};
+
+struct PMRowsRT {
+    const u64* rows;
+    int W;
+    __device__ __forceinline__ u64 operator()(u64 r, int w) const { return rows[r * W + w]; }
+};
+
+/* build_pm for a runtime word count, table in global memory */
+__device__ inline void build_pm_rt(u64* rows, u64* keys, int hcap, int W, const unsigned char* base, int m,
+                                   int width, int* err)
+{
+    const int64_t nrows = 256 + hcap + 1;
+    for (int64_t i = threadIdx.x; i < nrows * W; i += blockDim.x) rows[i] = 0;
+    for (int i = threadIdx.x; i < hcap; i += blockDim.x) keys[i] = 0;
+    __syncthreads();
+    if (hcap) {
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            const u64 c = load_unit(base, width, i);
+            if (c < 256) continue;
+            u32 k = hash_slot(c, hcap - 1);
+            int probe = 0;
+            for (; probe < hcap; ++probe) {
+                const u64 old = atomicCAS((unsigned long long*)&keys[k], 0ull, (unsigned long long)c);
+                if (old == 0 || old == c) break;
+                k = (k + 1) & (u32)(hcap - 1);
+            }
+            if (probe == hcap) atomicExch(err, 1);
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const u64 c = load_unit(base, width, i);
+        const int r = resolve_row(keys, hcap, c);
+        if (r < 256 + hcap) atomicOr((unsigned long long*)&rows[(int64_t)r * W + (i >> 6)], 1ull << (i & 63));
+    }
+    __syncthreads();
+}
+
+template <int FAM, typename CT>
+__device__ __forceinline__ void score_pair_generic(const KParams& a, const u64* rows, const u64* keys, int W,
+                                                   int64_t qi, int m, const unsigned char* qb, int64_t ci, u64* st)
+{
+    const int64_t o0 = a.c.off[ci], o1 = a.c.off[ci + 1];
+    const int n = (int)(o1 - o0);
+    const CT* s2 = (const CT*)a.c.data + o0;
+    PairSpec s;
+    s.metric = a.metric;
+    s.op = a.op;
+    s.form = a.form;
+    s.l1 = (u64)m;
+    s.l2 = (u64)n;
+    s.ci = a.ci;
+    s.cf = a.cf;
+    s.p = a.sp;
+    const PMRowsRT pm{rows, W};
+    const TextRows<CT, (sizeof(CT) > 1)> txt{s2, keys, a.hcap};
+    i64 vi = 0;
+    double vf = 0.0;
+    if (FAM == FAM_JARO) {
+        const RawQuery q{qb, a.q.width};
+        i64 prefix = 0;
+        const int mx = (m < n ? m : n) < 4 ? (m < n ? m : n) : 4;
+        for (; prefix < mx; ++prefix)
+            if ((u64)__ldg(s2 + prefix) != q[prefix]) break;
+        int common = 0, transp = 0;
+        if (m > 0 && n > 0 && jaro_pair_needs_counts(s, prefix))
+            jaro_multi_rt(pm, W, m, txt, n, &common, &transp, st, st + W);
+        vf = finish_jaro(s, prefix, common, transp);
+        store_result(a, qi, ci, 0, vf, false);
+        return;
+    }
+    const Plan pl = plan_int(s);
+    i64 raw = 0;
+    if (pl.run) {
+        const i64 K = pl.K;
+        const i64 diff = m > n ? m - n : n - m;
+        if (FAM == FAM_WF) {
+            const RawQuery q{qb, a.q.width};
+            const RawText<CT> t2{s2};
+            raw = (i64)wf_distance(q, m, t2, n, a.sp, (u64)K, st);
+        }
+        else if (FAM == FAM_LCS) {
+            if (m == 0 || n == 0) raw = 0;
+            else if (K < diff) raw = -1;
+            else raw = lcs_multi_rt(pm, W, m, txt, n, K, st);
+        }
+        else if (m == 0) raw = n;
+        else if (K < diff) raw = K + 1;
+        else if (n == 0) raw = m;
+        else if (FAM == FAM_OSA) raw = osa_multi_rt(pm, W, m, txt, n, K, st, st + W, st + 2 * W, st + 3 * W);
+        else raw = lev_multi_rt(pm, W, m, txt, n, K, st, st + W);
+    }
+    finish_int(s, pl, raw, &vi, &vf);
+    store_result(a, qi, ci, vi, vf, result_is_int(a.metric, a.op));
+}
+
+template <int FAM, typename CT>
+__global__ void __launch_bounds__(128) k_generic(const KParams a)
+{
+    const int W = a.wmax;
+    u64* region = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
+    u64* rows = region;
+    u64* keys = rows + (int64_t)(256 + a.hcap + 1) * W;
+    u64* st = region + (int64_t)(256 + a.hcap + 1) * W + a.hcap + (int64_t)threadIdx.x * a.scratch_per_thread;
+    __shared__ int64_t s_tile;
+    int64_t cur_q = -1;
+    int m = 0;
+    const unsigned char* qb = nullptr;
+    const int64_t ntiles = (int64_t)a.nq * a.nchunks;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(a.counter, 1);
+        __syncthreads();
+        const int64_t t = s_tile;
+        if (t >= ntiles) break;
+        const int64_t qi = a.qlist[t / a.nchunks];
+        const int64_t ch = t % a.nchunks;
+        if (qi != cur_q) {
+            const int64_t q0 = a.q.off[qi];
+            m = (int)(a.q.off[qi + 1] - q0);
+            qb = a.q.data + q0 * a.q.width;
+            if (FAM != FAM_WF) {
+                if (m > 64 * W) {
+                    if (threadIdx.x == 0) atomicExch(a.err, 2);
+                    m = 64 * W;
+                }
+                build_pm_rt(rows, keys, a.hcap, W, qb, m, a.q.width, a.err);
+            }
+            cur_q = qi;
+        }
+        const int64_t c0 = ch * a.chunk;
+        const int64_t c1 = c0 + a.chunk < a.c.n ? c0 + a.chunk : a.c.n;
+        for (int64_t ci = c0 + threadIdx.x; ci < c1; ci += blockDim.x)
+            score_pair_generic<FAM, CT>(a, rows, keys, W, qi, m, qb, ci, st);
+        __syncthreads();
+    }
+}
+
+/* shared memory of k_tiles<.., W> */
+inline size_t tiles_smem_bytes(int W, int hcap) { return ((size_t)(256 + hcap + 1) * W + (size_t)hcap) * 8; }
+
+} // namespace rfg

@@ -1,0 +1,30 @@
+/* k_tiles instantiations of the JARO core family */
+#include "rfg_device.cuh"
+#include "rfg_kernels.h"
+
+namespace rfg {
+
+template <typename CT>
+static const void* pick_jaro(int W)
+{
+    switch (W) {
+    case 1: return (const void*)&k_tiles<FAM_JARO, CT, 1>;
+    case 2: return (const void*)&k_tiles<FAM_JARO, CT, 2>;
+    case 4: return (const void*)&k_tiles<FAM_JARO, CT, 4>;
+    case 8: return (const void*)&k_tiles<FAM_JARO, CT, 8>;
+    }
+    return nullptr;
+}
+
+const void* tiles_kernel_jaro(int width, int W)
+{
+    switch (width) {
+    case 1: return pick_jaro<uint8_t>(W);
+    case 2: return pick_jaro<uint16_t>(W);
+    case 4: return pick_jaro<uint32_t>(W);
+    case 8: return pick_jaro<unsigned long long>(W);
+    }
+    return nullptr;
+}
+
+} // namespace rfg

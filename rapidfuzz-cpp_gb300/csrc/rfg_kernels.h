@@ -1,0 +1,14 @@
+/* rfg_kernels.h -- host-side lookup of the kernel instantiations (one translation
+ * unit per core family, compiled in parallel). */
+#pragma once
+#include <stdint.h>
+
+namespace rfg {
+/* k_tiles<FAM, CT, W>: width in {1,2,4,8}, W in {1,2,4,8}; nullptr when absent */
+const void* tiles_kernel_lev(int width, int W);
+const void* tiles_kernel_lcs(int width, int W);
+const void* tiles_kernel_osa(int width, int W);
+const void* tiles_kernel_jaro(int width, int W);
+/* k_generic<FAM, CT> */
+const void* generic_kernel(int fam, int width);
+} // namespace rfg

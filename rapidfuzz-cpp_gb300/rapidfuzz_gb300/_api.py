@@ -1,0 +1,123 @@
+"""The reference's function and class names over the generic entry points
+(rapidfuzz/distance/*.hpp, rapidfuzz/fuzz.hpp)."""
+from ._lib import (DISTANCE, SIMILARITY, NORMALIZED_DISTANCE, NORMALIZED_SIMILARITY, LEVENSHTEIN, INDEL, LCSSEQ,
+                   OSA, JARO, JARO_WINKLER, RATIO, Cached, Multi, score)
+
+__all__ = []
+
+
+def _free(metric, op, name, has_weights=False, has_pw=False):
+    def f(s1, s2, *args, score_cutoff=None, score_hint=None, weights=(1, 1, 1), prefix_weight=0.1):
+        a = list(args)
+        if has_weights and a:
+            weights = a.pop(0)
+        if has_pw and a:
+            prefix_weight = a.pop(0)
+        if a:
+            score_cutoff = a.pop(0)
+        if a:
+            score_hint = a.pop(0)
+        return score(metric, op, s1, s2, score_cutoff, score_hint, weights, prefix_weight)
+    f.__name__ = name
+    globals()[name] = f
+    __all__.append(name)
+
+
+for _metric, _prefix, _w, _pw in ((LEVENSHTEIN, "levenshtein", True, False), (INDEL, "indel", False, False),
+                                  (LCSSEQ, "lcs_seq", False, False), (OSA, "osa", False, False),
+                                  (JARO, "jaro", False, False), (JARO_WINKLER, "jaro_winkler", False, True)):
+    for _op, _suffix in ((DISTANCE, "distance"), (SIMILARITY, "similarity"),
+                         (NORMALIZED_DISTANCE, "normalized_distance"), (NORMALIZED_SIMILARITY, "normalized_similarity")):
+        _free(_metric, _op, "%s_%s" % (_prefix, _suffix), _w, _pw)
+
+
+def fuzz_ratio(s1, s2, score_cutoff=0.0):
+    return score(RATIO, SIMILARITY, s1, s2, score_cutoff)
+
+
+__all__.append("fuzz_ratio")
+
+
+class _CachedBase:
+    metric = None
+
+    def __init__(self, s1, *args, **kw):
+        self._c = Cached(self.metric, s1, *args, **kw)
+
+    def distance(self, s2, score_cutoff=None, score_hint=None):
+        return self._c.score(DISTANCE, s2, score_cutoff, score_hint)
+
+    def similarity(self, s2, score_cutoff=None, score_hint=None):
+        return self._c.score(SIMILARITY, s2, score_cutoff, score_hint)
+
+    def normalized_distance(self, s2, score_cutoff=None, score_hint=None):
+        return self._c.score(NORMALIZED_DISTANCE, s2, score_cutoff, score_hint)
+
+    def normalized_similarity(self, s2, score_cutoff=None, score_hint=None):
+        return self._c.score(NORMALIZED_SIMILARITY, s2, score_cutoff, score_hint)
+
+
+def _cached(name, metric):
+    cls = type(name, (_CachedBase,), {"metric": metric})
+    globals()[name] = cls
+    __all__.append(name)
+
+
+for _name, _metric in (("CachedLevenshtein", LEVENSHTEIN), ("CachedIndel", INDEL), ("CachedLCSseq", LCSSEQ),
+                       ("CachedOSA", OSA), ("CachedJaro", JARO), ("CachedJaroWinkler", JARO_WINKLER)):
+    _cached(_name, _metric)
+
+
+class CachedRatio:
+    def __init__(self, s1):
+        self._c = Cached(RATIO, s1)
+
+    def similarity(self, s2, score_cutoff=0.0, score_hint=0.0):
+        return self._c.score(SIMILARITY, s2, score_cutoff, score_hint)
+
+
+__all__.append("CachedRatio")
+
+
+class experimental:
+    """experimental::Multi* (max_len = the MaxLen template argument)"""
+
+    class _MultiBase:
+        metric = None
+
+        def __init__(self, max_len, count, *args, **kw):
+            self._m = Multi(self.metric, max_len, count, *args, **kw)
+
+        def insert(self, s):
+            self._m.insert(s)
+
+        def result_count(self):
+            return self._m.result_count()
+
+        def distance(self, s2, score_cutoff=None):
+            return self._m.score(DISTANCE, s2, score_cutoff)
+
+        def similarity(self, s2, score_cutoff=None):
+            return self._m.score(SIMILARITY, s2, score_cutoff)
+
+        def normalized_distance(self, s2, score_cutoff=None):
+            return self._m.score(NORMALIZED_DISTANCE, s2, score_cutoff)
+
+        def normalized_similarity(self, s2, score_cutoff=None):
+            return self._m.score(NORMALIZED_SIMILARITY, s2, score_cutoff)
+
+    MultiLevenshtein = type("MultiLevenshtein", (_MultiBase,), {"metric": LEVENSHTEIN})
+    MultiIndel = type("MultiIndel", (_MultiBase,), {"metric": INDEL})
+    MultiLCSseq = type("MultiLCSseq", (_MultiBase,), {"metric": LCSSEQ})
+    MultiOSA = type("MultiOSA", (_MultiBase,), {"metric": OSA})
+    MultiJaro = type("MultiJaro", (_MultiBase,), {"metric": JARO})
+    MultiJaroWinkler = type("MultiJaroWinkler", (_MultiBase,), {"metric": JARO_WINKLER})
+
+    class MultiRatio(_MultiBase):
+        metric = RATIO
+
+        def similarity(self, s2, score_cutoff=0.0):
+            return self._m.score(SIMILARITY, s2, score_cutoff)
+
+
+__all__.append("experimental")

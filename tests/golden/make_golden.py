@@ -1,0 +1,309 @@
+"""Generate tests/golden/*.json from the UNMODIFIED reference (oracle/_ref/librfref.so,
+built by `make -C oracle ref` from the rapidfuzz-cpp v3.3.3 headers).
+
+Three fixtures:
+  kat.json      the known-answer vectors of the reference's own test suite (each case cites
+                the test file:line it restates), with the value the reference computes here;
+  random.json   seeded random cases over every metric x op x API form x cutoff, char widths
+                1/2/4/8, lengths 0..300 (word, multi-word, banded and any-length paths);
+  multi.json    Multi* batches with several inserted strings.
+Doubles are stored with float.hex() so the comparison is bit-exact.
+
+Usage: python tests/golden/make_golden.py   (needs the reference checkout; run in the
+build container, the fixtures are committed).
+"""
+import ctypes
+import json
+import os
+import random
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+import numpy as np  # noqa: E402
+
+from oracle_lib import (DISTANCE, SIMILARITY, NORM_DISTANCE, NORM_SIMILARITY, LEVENSHTEIN, INDEL, LCSSEQ, OSA,  # noqa: E402
+                        JARO, JARO_WINKLER, RATIO, FREE, CACHED, MULTI, as_units, reference, result_is_int,
+                        score, make_params, pack_strings, strings_struct)
+
+OPS = (DISTANCE, SIMILARITY, NORM_DISTANCE, NORM_SIMILARITY)
+
+
+def enc(v):
+    return v if isinstance(v, int) else float(v).hex()
+
+
+def case(metric, op, form, s1, s2, cutoff=None, weights=(1, 1, 1), pw=0.1, w1=None, w2=None, cite=None):
+    a = as_units(s1, w1)
+    b = as_units(s2, w2)
+    ref = reference()
+    v = score(ref.rfref_score, metric, op, form, a, b, cutoff, weights, pw)
+    if v is None:
+        return None
+    d = {"metric": metric, "op": op, "form": form, "s1": [int(x) for x in a], "w1": a.itemsize,
+         "s2": [int(x) for x in b], "w2": b.itemsize, "cutoff": cutoff, "weights": list(weights), "pw": pw,
+         "expected": enc(v)}
+    if cite:
+        d["cite"] = cite
+    return d
+
+
+def mul(s, k):
+    return s * k
+
+
+def kat_cases():
+    """Known answers of the reference's tests (expected values re-derived by the reference)."""
+    out = []
+    T = "test/distance/tests-Levenshtein.cpp"
+    # empty / simple / weighted (tests-Levenshtein.cpp:98-141)
+    for s1, s2 in (("", ""), ("aaaa", ""), ("", "aaaa"), ("aaaa", "aaaa"), ("aaaa", "aaa"), ("abaa", "baaa"),
+                   ("aaaa", "aaab"), ("aaaa", "bbbb")):
+        for w in ((1, 1, 1), (1, 1, 2)):
+            out.append(case(LEVENSHTEIN, DISTANCE, FREE, s1, s2, None, w, cite=T + ":108-130"))
+            out.append(case(LEVENSHTEIN, NORM_SIMILARITY, FREE, s1, s2, None, w, cite=T + ":132-141"))
+            out.append(case(LEVENSHTEIN, DISTANCE, CACHED, s1, s2, None, w, cite=T + ":21-96"))
+    # mbleven cutoffs (tests-Levenshtein.cpp:143-179)
+    for a, b in (("South Korea", "North Korea"), ("aabc", "cccd")):
+        for w in ((1, 1, 1), (1, 1, 2)):
+            for c in (None, 0, 1, 2, 3, 4, 5, 6):
+                out.append(case(LEVENSHTEIN, DISTANCE, FREE, a, b, c, w, cite=T + ":143-179"))
+                out.append(case(LEVENSHTEIN, DISTANCE, CACHED, a, b, c, w, cite=T + ":143-179"))
+    # banded (tests-Levenshtein.cpp:181-232)
+    banded = [
+        ("kkkkbbbbfkkkkkkibfkkkafakkfekgkkkkkkkkkkbdbbddddddddddafkkkekkkhkk",
+         "khddddddddkkkkdgkdikkccccckcckkkekkkkdddddddddddafkkhckkkkkdckkkcc", (None, 31)),
+        ("ccddcddddddddddddddddddddddddddddddddddddddddddddddddddddaaaaaaaaaaa",
+         "aaaaaaaaaaaaaadddddddddbddddddddddddddddddddddddddddddddddbddddddddd", (None, 31)),
+        ("accccccccccaaaaaaaccccccccccccccccccccccccccccccacccccccccccccccccccccccccccccc"
+         "ccccccccccccccccccccaaaaaaaaaaaaacccccccccccccccccccccc",
+         "ccccccccccccccccccccccccccccccccccccccccccccccccccccccccccccccccccccccccccccccc"
+         "ccccccccccccccccccccccccccccccccccccbcccb", (None, 25)),
+        ("miiiiiiiiiiliiiiiiibghiiaaaaaaaaaaaaaaacccfccccedddaaaaaaaaaaaaaaaaaaaaaaaaaaaa"
+         "aaaaaaaaaaaaa",
+         "aaaaaaajaaaaaaaabghiiaaaaaaaaaaaaaaacccfccccedddaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaajjdim", (None, 27)),
+        ("lllllfllllllllllllllllllllllllllllllllllllllllllllllllglllllilldcaaaaaaaaaaaaaa"
+         "aaaaadbbllllllllllhllllllllllllllllllllllllllgl",
+         "aaaaaaaaaaaaaadbbllllllllllllllelllllllllllllllllllllllllllllllglllllilldcaaaaa"
+         "aaaaaaaaaaaaaadbbllllllllllllllellllllllllllllhlllllllllill", (None, 27, 28)),
+        ("llccacaaaaaaaaaccccccccccccccccddffaccccaccecccggggclallhcccccljif",
+         "bddcbllllllbcccccccccccccccccddffccccccccebcccggggclbllhcccccljifbddcccccc", (None, 27, 28)),
+    ]
+    for a, b, cuts in banded:
+        for c in cuts:
+            for form in (FREE, CACHED):
+                out.append(case(LEVENSHTEIN, DISTANCE, form, a, b, c, cite=T + ":181-232"))
+    # Indel (tests-Indel.cpp:204-286)
+    T = "test/distance/tests-Indel.cpp"
+    for op in OPS:
+        out.append(case(INDEL, op, FREE, "aaaa", "aaaa", cite=T + ":208-220"))
+        out.append(case(INDEL, op, FREE, "aaaa", "bbbb", cite=T + ":208-220"))
+    for a, b in (("South Korea", "North Korea"), ("aabc", "cccd")):
+        for c in (None, 0, 1, 2, 3, 4, 5, 6):
+            out.append(case(INDEL, DISTANCE, FREE, a, b, c, cite=T + ":222-247"))
+    out.append(case(INDEL, NORM_SIMILARITY, FREE, "001", "220", cite=T + ":249-256"))
+    out.append(case(INDEL, NORM_SIMILARITY, CACHED, "001", "220", cite=T + ":249-256"))
+    s1 = "ddccbccc"
+    s2 = ("aaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaa"
+          "aaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaccacccaccaaaaaaaa"
+          "daaaaaaaaccccaccccccaaaaaaaccccaaacccaccccadddaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaa"
+          "aaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaaccccccccacccaaaaaacccaaaaaacccacccaaaaaacccdccc"
+          "cccacccccccccccccccccccccccccccccccccccccccccccccccccccccccccccccddddddaaaaaaaa"
+          "aaaaaaaaaaaaaaaaaacacccaaaaaacccddddaaaaaaaaaaaaaaaaaaaaaaaaaaaaaccccaaaaaaaaaa"
+          "ccccccaadddaaaaaaaaaaaaaaaaaaaaaacaaaaaa")
+    for c in (None, 508, 507, 2**64 - 1):
+        out.append(case(INDEL, DISTANCE, FREE, s1, s2, c, cite=T + ":258-272"))
+    a = ("bbbdbbmbbbbbbbbbBbfbbbbbbbbbbbbbbbbbbbrbbbbbrbbbbbdbnbbbjbhbbbbbbbbbhbbbbbCbobb"
+         "bxbbbbbkbbbAbxbbwbbbtbcbbbbebbiblbbbbqbbbbbbpbbbbbbubbbkbbDbbbhbkbCbbgbbrbbbbbb"
+         "bbbbbkbyvbbsbAbbbbz")
+    b = "jaaagaaqyaaaanrCfwaaxaeahtaaaCzaaaspaaBkvaaaaqDaacndaaeolwiaaauaaaaaaamA"
+    out.append(case(INDEL, DISTANCE, FREE, a, b, cite=T + ":274-283"))
+    # LCSseq (tests-LCSseq.cpp:148-204)
+    T = "test/distance/tests-LCSseq.cpp"
+    for op in OPS:
+        out.append(case(LCSSEQ, op, FREE, "aaaa", "aaaa", cite=T + ":152-164"))
+        out.append(case(LCSSEQ, op, FREE, "aaaa", "bbbb", cite=T + ":152-164"))
+    for a, b in (("South Korea", "North Korea"), ("aabc", "cccd")):
+        for c in (None, 0, 1, 2, 3, 4, 9, 10):
+            out.append(case(LCSSEQ, SIMILARITY, FREE, a, b, c, cite=T + ":166-196"))
+            out.append(case(LCSSEQ, DISTANCE, FREE, a, b, c, cite=T + ":166-196"))
+    out.append(case(LCSSEQ, SIMILARITY, CACHED, "001", "220", cite=T + ":198-204"))
+    # OSA (tests-OSA.cpp:55-97)
+    T = "test/distance/tests-OSA.cpp"
+    for a, b, c in (("", "", None), ("aaaa", "", None), ("", "aaaa", None), ("aaaa", "", 1), ("", "aaaa", 1),
+                    ("CA", "ABC", None), ("CA", "AC", None)):
+        out.append(case(OSA, DISTANCE, FREE, a, b, c, cite=T + ":59-86"))
+        out.append(case(OSA, DISTANCE, CACHED, a, b, c, cite=T + ":59-86"))
+    filler = "a" * 64
+    out.append(case(OSA, DISTANCE, FREE, "a" + filler + "CA" + filler + "a", "b" + filler + "AC" + filler + "b",
+                    cite=T + ":88-96"))
+    out.append(case(OSA, DISTANCE, CACHED, "a" + filler + "CA" + filler + "a", "b" + filler + "AC" + filler + "b",
+                    cite=T + ":88-96"))
+    # Jaro / Jaro-Winkler names x names x cutoffs (tests-Jaro.cpp:160-170, tests-JaroWinkler.cpp:128-174)
+    names = ["james", "robert", "john", "michael", "william", "david", "joseph", "thomas", "charles", "mary",
+             "patricia", "jennifer", "linda", "elizabeth", "barbara", "susan", "jessica", "sarah", "karen", ""]
+    cuts = (0.1, 0.5, 0.7, 0.8, 0.9, 1.0, 1.1)
+    rng = random.Random(7)
+    for metric, T in ((JARO, "test/distance/tests-Jaro.cpp:160-170"),
+                      (JARO_WINKLER, "test/distance/tests-JaroWinkler.cpp:128-174")):
+        for n1 in names:
+            for n2 in names:
+                c = rng.choice(cuts)
+                out.append(case(metric, SIMILARITY, FREE, n1, n2, c, cite=T))
+                out.append(case(metric, DISTANCE, CACHED, n1, n2, round(1.0 - c, 10), cite=T))
+    # edge lengths (tests-Jaro.cpp:172-231, tests-JaroWinkler.cpp:177-216)
+    edge = [("", ""), ("0", "0"), ("00", "00"), ("0", "00"), ("0" * 65, "0" * 65), ("0" * 64, "0" * 65),
+            ("0" * 63, "0" * 65), ("000000001", "0000010"), ("01234567", "0" * 170 + "7654321" + "0" * 200),
+            ("01", "1111100000"),
+            ("1" + "0" * 62 + "20", "0" * 65),
+            ("0" * 14 + "1" + "0" * 24 + "1" + "0" * 25, "0" * 78 + "1"),
+            ("0" * 65, "01" + "0" * 126)]
+    for metric, T in ((JARO, "test/distance/tests-Jaro.cpp:172-231"),
+                      (JARO_WINKLER, "test/distance/tests-JaroWinkler.cpp:177-216")):
+        for a, b in edge:
+            for form in (FREE, CACHED):
+                out.append(case(metric, SIMILARITY, form, a, b, cite=T))
+                out.append(case(metric, SIMILARITY, form, b, a, cite=T))
+    # MultiJaro fuzz regression (tests-Jaro.cpp:233-256): covered in multi.json
+    # fuzz::ratio (test/tests-fuzz.cpp:52-74)
+    T = "test/tests-fuzz.cpp:52-74"
+    fz = ["new york mets", "new YORK mets", "the wonderful new york mets", "new york mets vs atlanta braves",
+          "atlanta braves vs new york mets", "new york mets - atlanta braves", "new york city mets - atlanta braves",
+          "{", "{a", "a{", "{b", "test"]
+    for a in fz:
+        for b in fz:
+            out.append(case(RATIO, SIMILARITY, FREE, a, b, cite=T))
+            out.append(case(RATIO, SIMILARITY, CACHED, a, b, 85.0, cite=T))
+    return [c for c in out if c is not None]
+
+
+def rand_str(rng, alpha, lo, hi):
+    return [rng.choice(alpha) for _ in range(rng.randint(lo, hi))]
+
+
+def mutate(rng, s, alpha, k):
+    s = list(s)
+    for _ in range(k):
+        op = rng.randint(0, 3)
+        if op == 0 and s:
+            s[rng.randrange(len(s))] = rng.choice(alpha)
+        elif op == 1:
+            s.insert(rng.randint(0, len(s)), rng.choice(alpha))
+        elif op == 2 and s:
+            del s[rng.randrange(len(s))]
+        elif op == 3 and len(s) > 1:
+            i = rng.randrange(len(s) - 1)
+            s[i], s[i + 1] = s[i + 1], s[i]
+    return s
+
+
+ALPHABETS = [[65, 67, 71, 84], list(range(97, 123)), [97, 98], list(range(0, 256)), [97, 98, 300, 70000],
+             [1000, 1001, 1002], [0x41, 0xC0, 0xC9, 0xFF, 0x20], [2**40 + 1, 2**40 + 2, 5]]
+
+
+def random_cases(n, seed=1):
+    rng = random.Random(seed)
+    out = []
+    while len(out) < n:
+        alpha = rng.choice(ALPHABETS)
+        maxlen = rng.choice([4, 8, 16, 40, 63, 64, 65, 100, 128, 129, 200, 300])
+        s1 = rand_str(rng, alpha, 0, maxlen)
+        s2 = mutate(rng, s1, alpha, rng.randint(0, 12)) if rng.random() < 0.6 else rand_str(rng, alpha, 0, maxlen)
+        if rng.random() < 0.5:
+            s1, s2 = s2, s1
+        mx1, mx2 = max(s1 + [0]), max(s2 + [0])
+        w1 = 8 if mx1 >= 2**32 else (4 if mx1 >= 65536 else rng.choice([1, 2, 4, 8]) if mx1 < 256 else rng.choice([2, 4]) if mx1 < 65536 else 4)
+        w2 = 8 if mx2 >= 2**32 else (4 if mx2 >= 65536 else rng.choice([1, 2, 4, 8]) if mx2 < 256 else rng.choice([2, 4]) if mx2 < 65536 else 4)
+        metric = rng.randrange(7)
+        op = SIMILARITY if metric == RATIO else rng.randrange(4)
+        form = rng.choice([FREE, CACHED, MULTI])
+        if form == MULTI and len(s1) > 64:
+            form = CACHED
+        weights = (1, 1, 1)
+        if metric == LEVENSHTEIN:
+            weights = rng.choice([(1, 1, 1), (1, 1, 1), (1, 1, 2), (2, 2, 2), (1, 2, 3), (3, 1, 1), (2, 2, 5),
+                                  (0, 0, 1), (1, 1, 0)])
+            if form == MULTI and weights not in ((1, 1, 1), (1, 1, 2), (1, 1, 0)):
+                weights = (1, 1, 1)
+        if result_is_int(metric, op):
+            cutoff = rng.choice([None, 0, 1, 2, 3, 4, 5, 8, 10, 31, 32, 40, 64, 100, 1000])
+        else:
+            cutoff = rng.choice([None, 0.0, 0.1, 0.5, 0.7, 0.8, 0.85, 0.9, 0.95, 1.0, 1.1])
+            if metric == RATIO and cutoff is not None:
+                cutoff = cutoff * 100
+        pw = rng.choice([0.1, 0.1, 0.25])
+        c = case(metric, op, form, s1, s2, cutoff, weights, pw, w1, w2)
+        if c is not None:
+            out.append(c)
+    return out
+
+
+def multi_cases(seed=3):
+    """Multi* batches (8-bit code units; the reference driver's Multi entry takes bytes)."""
+    ref = reference()
+    rng = random.Random(seed)
+    out = []
+
+    def run(metric, op, max_len, strs, s2, cutoff, weights=(1, 1, 1), pw=0.1, cite=None):
+        data, offsets, width = pack_strings([as_units(bytes(s)) for s in strs], 1)
+        st = strings_struct(data, offsets, width)
+        b = as_units(bytes(s2))
+        n = len(strs)
+        oi = np.zeros(max(n, 1), dtype=np.int64)
+        of = np.zeros(max(n, 1), dtype=np.float64)
+        rc = ctypes.c_int64()
+        p = make_params(weights, pw)
+        is_int = result_is_int(metric, op)
+        ci = (2**63 - 1 if op == DISTANCE else 0) if (cutoff is None or not is_int) else int(cutoff)
+        cf = (1.0 if op in (DISTANCE, NORM_DISTANCE) and metric != RATIO else 0.0) if (cutoff is None or is_int) \
+            else float(cutoff)
+        r = ref.rfref_multi(metric, op, max_len, ctypes.byref(st), b.ctypes.data if b.size else None, b.size, 1,
+                            ctypes.byref(p), ci, cf, oi.ctypes.data, of.ctypes.data, ctypes.byref(rc))
+        if r != 0:
+            return
+        vals = [int(v) for v in oi[:n]] if is_int else [float(v).hex() for v in of[:n]]
+        d = {"metric": metric, "op": op, "max_len": max_len, "strs": [list(s) for s in strs], "s2": list(s2),
+             "cutoff": cutoff, "weights": list(weights), "pw": pw, "result_count": rc.value, "expected": vals}
+        if cite:
+            d["cite"] = cite
+        out.append(d)
+
+    # MultiJaro fuzz regression (tests-Jaro.cpp:233-256)
+    s2 = b"01" * 133
+    run(JARO, SIMILARITY, 8, [b"10010010"] * 32 + [b"00100100"], s2, 0.0, cite="test/distance/tests-Jaro.cpp:233-256")
+    # SIMD wraparound (tests-LCSseq.cpp:207-244)
+    for k in (256, 300, 512):
+        run(LCSSEQ, DISTANCE, 8, [b"a", b"b", b"aa", b"bb"], b"b" * k, None,
+            cite="test/distance/tests-LCSseq.cpp:207-244")
+    for _ in range(120):
+        metric = rng.randrange(7)
+        op = SIMILARITY if metric == RATIO else rng.randrange(4)
+        max_len = rng.choice([8, 16, 32, 64])
+        alpha = rng.choice([[65, 67, 71, 84], list(range(97, 123)), [97, 98]])
+        count = rng.randint(1, 70)
+        base = rand_str(rng, alpha, 0, max_len)
+        strs = [bytes(mutate(rng, base, alpha, rng.randint(0, 4))[:max_len]) if rng.random() < 0.5
+                else bytes(rand_str(rng, alpha, 0, max_len)) for _ in range(count)]
+        s2 = bytes(mutate(rng, base, alpha, rng.randint(0, 6)) if rng.random() < 0.6 else rand_str(rng, alpha, 0, 90))
+        weights = rng.choice([(1, 1, 1), (1, 1, 2)]) if metric == LEVENSHTEIN else (1, 1, 1)
+        if result_is_int(metric, op):
+            cutoff = rng.choice([None, 0, 2, 5, 10])
+        else:
+            cutoff = rng.choice([None, 0.0, 0.5, 0.8, 0.9, 1.0])
+            if metric == RATIO and cutoff is not None:
+                cutoff *= 100
+        run(metric, op, max_len, strs, s2, cutoff, weights, rng.choice([0.1, 0.2]))
+    return out
+
+
+def main():
+    if reference() is None:
+        sys.exit("oracle/_ref/librfref.so is missing: run `make -C oracle ref` where the reference checkout exists")
+    for name, cases in (("kat.json", kat_cases()), ("random.json", random_cases(4000)), ("multi.json", multi_cases())):
+        with open(os.path.join(HERE, name), "w") as f:
+            json.dump(cases, f, separators=(",", ":"))
+        print(name, len(cases))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,173 @@
+"""Parity of the CUDA path with the reference: every result bit-exact (integers) or
+bit-identical (doubles) -- tolerance 0.  Calls go through the C ABI."""
+import random
+
+import numpy as np
+import pytest
+
+import golden_lib as G
+from oracle_lib import oracle, oracle_cdist, score as oscore, FREE, CACHED, MULTI
+
+pytestmark = pytest.mark.gpu
+
+import rapidfuzz_gb300 as R  # noqa: E402
+
+
+def gpu_score(c, a, b):
+    m, op, form = c["metric"], c["op"], c["form"]
+    w, pw, cut = tuple(c["weights"]), c["pw"], c["cutoff"]
+    if form == FREE:
+        return R.score(m, op, a, b, cut, None, w, pw)
+    if form == CACHED:
+        return R.Cached(m, a, w, pw).score(op, b, cut)
+    ml = 8 if a.size <= 8 else 16 if a.size <= 16 else 32 if a.size <= 32 else 64
+    mu = R.Multi(m, ml, 1, w, pw)
+    mu.insert(a)
+    v = mu.score(op, b, cut)[0]
+    return int(v) if R._lib.result_is_int(m, op) else float(v)
+
+
+@pytest.mark.parametrize("fixture", ["kat.json", "random.json"])
+def test_fixtures_per_call(fixture):
+    bad = []
+    for c in G.load(fixture):
+        a, b = G.arrays(c)
+        v = gpu_score(c, a, b)
+        if not G.same(v, G.dec(c["expected"])):
+            bad.append((c.get("cite"), c["metric"], c["op"], c["form"], c["cutoff"], len(a), len(b), v,
+                        G.dec(c["expected"])))
+    assert not bad, "%d mismatches: %r" % (len(bad), bad[:5])
+
+
+def test_multi_batches():
+    for c in G.load("multi.json"):
+        mu = R.Multi(c["metric"], c["max_len"], len(c["strs"]), tuple(c["weights"]), c["pw"])
+        for s in c["strs"]:
+            mu.insert(bytes(s))
+        assert mu.result_count() == c["result_count"]
+        out = mu.score(c["op"], bytes(c["s2"]), c["cutoff"])
+        for i, exp in enumerate(c["expected"]):
+            v = out[i].item()
+            assert G.same(v, G.dec(exp)), (c.get("cite"), c["metric"], c["op"], i, v, exp)
+
+
+def _rand(rng, alpha, lo, hi):
+    return [rng.choice(alpha) for _ in range(rng.randint(lo, hi))]
+
+
+def _mut(rng, s, alpha, k):
+    s = list(s)
+    for _ in range(k):
+        op = rng.randint(0, 3)
+        if op == 0 and s:
+            s[rng.randrange(len(s))] = rng.choice(alpha)
+        elif op == 1:
+            s.insert(rng.randint(0, len(s)), rng.choice(alpha))
+        elif op == 2 and s:
+            del s[rng.randrange(len(s))]
+        elif op == 3 and len(s) > 1:
+            i = rng.randrange(len(s) - 1)
+            s[i], s[i + 1] = s[i + 1], s[i]
+    return s
+
+
+def _batch(rng, alpha, n, lo, hi, width, base=None):
+    out = []
+    for _ in range(n):
+        if base and rng.random() < 0.4:
+            out.append(_mut(rng, rng.choice(base), alpha, rng.randint(0, 8)))
+        else:
+            out.append(_rand(rng, alpha, lo, hi))
+    return R.pack_strings([np.array(s, dtype={1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}[width])
+                           for s in out], width), out
+
+
+CASES = [
+    # metric, op, cutoff
+    (R.LEVENSHTEIN, R.DISTANCE, None), (R.LEVENSHTEIN, R.DISTANCE, 8), (R.LEVENSHTEIN, R.SIMILARITY, 20),
+    (R.LEVENSHTEIN, R.NORMALIZED_SIMILARITY, 0.7), (R.LEVENSHTEIN, R.NORMALIZED_DISTANCE, 0.2),
+    (R.INDEL, R.DISTANCE, 8), (R.INDEL, R.NORMALIZED_SIMILARITY, 0.6), (R.LCSSEQ, R.SIMILARITY, 10),
+    (R.LCSSEQ, R.DISTANCE, 12), (R.OSA, R.DISTANCE, 8), (R.OSA, R.NORMALIZED_SIMILARITY, 0.5),
+    (R.JARO, R.SIMILARITY, 0.7), (R.JARO_WINKLER, R.SIMILARITY, 0.85), (R.JARO_WINKLER, R.NORMALIZED_DISTANCE, 0.3),
+    (R.RATIO, R.SIMILARITY, 85.0), (R.RATIO, R.SIMILARITY, 0.0),
+]
+
+
+@pytest.mark.parametrize("metric,op,cut", CASES)
+@pytest.mark.parametrize("shape", ["short", "multiword", "mixed", "wide"])
+def test_cdist_matches_oracle(metric, op, cut, shape):
+    rng = random.Random(hash((metric, op, shape)) & 0xffff)
+    if shape == "short":
+        alpha, qlo, qhi, clo, chi, w = list(range(97, 123)), 0, 64, 0, 80, 1
+    elif shape == "multiword":
+        alpha, qlo, qhi, clo, chi, w = [65, 67, 71, 84], 65, 512, 50, 600, 1
+    elif shape == "mixed":
+        alpha, qlo, qhi, clo, chi, w = [97, 98, 99], 0, 700, 0, 700, 1
+    else:
+        alpha, qlo, qhi, clo, chi, w = [0x41, 0xC0, 0xFF, 0x20, 300, 70000, 1000], 0, 140, 0, 140, 4
+    (qd, qo, qw), qs = _batch(rng, alpha, 23, qlo, qhi, w)
+    (cd, co, cw), _ = _batch(rng, alpha, 57, clo, chi, w, base=qs)
+    weights = (1, 1, 1)
+    got = R.cdist(metric, op, (qd, qo, qw), (cd, co, cw), cut, weights)
+    exp = oracle_cdist(metric, op, (qd, qo, qw), (cd, co, cw), cut, weights)
+    assert got.dtype == exp.dtype
+    bad = np.argwhere(got.view(np.int64) != exp.view(np.int64)) if got.dtype == np.float64 else np.argwhere(got != exp)
+    assert bad.size == 0, "mismatch at %r: got %r exp %r" % (bad[0], got[tuple(bad[0])], exp[tuple(bad[0])])
+
+
+@pytest.mark.parametrize("weights", [(1, 1, 1), (1, 1, 2), (2, 2, 2), (1, 2, 3), (3, 1, 1), (0, 0, 5)])
+def test_cdist_weighted_levenshtein(weights):
+    rng = random.Random(sum(weights))
+    (qd, qo, qw), qs = _batch(rng, list(range(97, 110)), 9, 0, 150, 1)
+    (cd, co, cw), _ = _batch(rng, list(range(97, 110)), 17, 0, 150, 1, base=qs)
+    for op, cut in ((R.DISTANCE, None), (R.DISTANCE, 9), (R.SIMILARITY, 30), (R.NORMALIZED_SIMILARITY, 0.6)):
+        got = R.cdist(R.LEVENSHTEIN, op, (qd, qo, qw), (cd, co, cw), cut, weights)
+        exp = oracle_cdist(R.LEVENSHTEIN, op, (qd, qo, qw), (cd, co, cw), cut, weights)
+        assert np.array_equal(got.view(np.int64), exp.view(np.int64)), (weights, op, cut)
+
+
+def test_cdist_int32_output_and_ld():
+    rng = random.Random(3)
+    (qd, qo, qw), qs = _batch(rng, list(range(97, 123)), 11, 16, 64, 1)
+    (cd, co, cw), _ = _batch(rng, list(range(97, 123)), 31, 16, 64, 1, base=qs)
+    out = np.full((11, 40), -7, dtype=np.int32)
+    R.cdist(R.OSA, R.DISTANCE, (qd, qo, qw), (cd, co, cw), 8, out_dtype=R.I32, out=out, ld=40)
+    exp = oracle_cdist(R.OSA, R.DISTANCE, (qd, qo, qw), (cd, co, cw), 8, out_dtype=0)
+    assert np.array_equal(out[:, :31], exp)
+    assert (out[:, 31:] == -7).all()
+
+
+def test_empty_batches_and_strings():
+    assert R.cdist(R.LEVENSHTEIN, R.DISTANCE, [], ["abc"]).shape == (0, 1)
+    assert R.cdist(R.LEVENSHTEIN, R.DISTANCE, ["abc"], []).shape == (1, 0)
+    m = R.cdist(R.JARO_WINKLER, R.SIMILARITY, ["", "a", ""], ["", "a", "b"])
+    o = oracle()
+    for i, q in enumerate(["", "a", ""]):
+        for j, c in enumerate(["", "a", "b"]):
+            assert G.same(m[i, j].item(), oscore(o.rfo_score, R.JARO_WINKLER, R.SIMILARITY, CACHED, q, c))
+
+
+def test_cached_score_many():
+    rng = random.Random(8)
+    q = bytes(_rand(rng, b"acgt", 100, 100))
+    cs = [bytes(_mut(rng, q, b"acgt", rng.randint(0, 30))) for _ in range(300)]
+    sc = R.Cached(R.LEVENSHTEIN, q)
+    got = sc.score_many(R.DISTANCE, cs, 10)
+    o = oracle()
+    for j, c in enumerate(cs):
+        assert got[j] == oscore(o.rfo_score, R.LEVENSHTEIN, R.DISTANCE, CACHED, q, c, 10)
+
+
+def test_long_strings_any_length_kernel():
+    """pattern > 512 code units: the any-length (scratch) kernel"""
+    rng = random.Random(21)
+    alpha = b"acgt"
+    q = bytes(_rand(rng, alpha, 3000, 3000))
+    cs = [bytes(_mut(rng, q, alpha, k)) for k in (0, 5, 50, 400)] + [bytes(_rand(rng, alpha, 2500, 3500))]
+    o = oracle()
+    for metric, op, cut in ((R.LEVENSHTEIN, R.DISTANCE, None), (R.LEVENSHTEIN, R.DISTANCE, 60),
+                            (R.INDEL, R.DISTANCE, None), (R.OSA, R.DISTANCE, None), (R.LCSSEQ, R.SIMILARITY, 2000),
+                            (R.JARO_WINKLER, R.SIMILARITY, 0.0), (R.JARO, R.SIMILARITY, 0.6)):
+        got = R.cdist(metric, op, [q], cs, cut)
+        for j, c in enumerate(cs):
+            assert G.same(got[0, j].item(), oscore(o.rfo_score, metric, op, CACHED, q, c, cut)), (metric, op, j)
