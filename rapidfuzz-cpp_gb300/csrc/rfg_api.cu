@@ -315,7 +315,8 @@ rfg_status run_batch(const QuerySet& q, const KStrings& c, const BatchSpec& spec
         a.out = spec.out;
         a.out_dtype = spec.out_dtype;
         a.ld = spec.ld;
-        a.hcap = (c.width > 1 && cls_wide[k] > 0) ? next_pow2(2 * cls_wide[k]) : 0;
+        const bool needs_table = fam != FAM_WF && fam != FAM_NONE;
+        a.hcap = (needs_table && c.width > 1 && cls_wide[k] > 0) ? next_pow2(2 * cls_wide[k]) : 0;
 
         const void* fn;
         int block;
