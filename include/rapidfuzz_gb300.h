@@ -149,6 +149,29 @@ rfg_status rfg_cdist(rfg_metric metric, rfg_op op, rfg_form form, const rfg_stri
                      const rfg_strings* choices, const rfg_params* params, rfg_cutoff cutoff,
                      rfg_dtype out_dtype, void* out, int64_t ld, uint32_t flags);
 
+/* ------------------------------------------------------------ prepared batches
+ * The batched path of cdist with the host work done once: create() classifies the
+ * queries, orders the tiles and places every buffer on the device; launch() only
+ * enqueues the kernels on the given stream (no allocation, no host synchronisation),
+ * so it can be timed with events, relaunched, or captured in a CUDA graph
+ * (RFG_LAUNCH_GRAPH captures on the first call and replays afterwards).  out must be
+ * device memory.  check() waits for the stream and reports the kernels' own checks.
+ * tune() times block size x tile count on this batch and keeps the fastest.
+ * (No reference counterpart: this is the persistent-kernel form of the reference's
+ * "scorer over all choices" loop, README.md:153-240.) */
+typedef struct rfg_batch_s* rfg_batch;
+#define RFG_LAUNCH_GRAPH 1u
+
+rfg_status rfg_batch_create(rfg_metric metric, rfg_op op, rfg_form form, const rfg_strings* queries,
+                            const rfg_strings* choices, const rfg_params* params, rfg_cutoff cutoff,
+                            rfg_dtype out_dtype, void* out, int64_t ld, uint32_t flags, rfg_batch* batch);
+rfg_status rfg_batch_launch(rfg_batch batch, void* cuda_stream, uint32_t launch_flags);
+rfg_status rfg_batch_check(rfg_batch batch, void* cuda_stream);
+rfg_status rfg_batch_tune(rfg_batch batch, void* cuda_stream, int32_t* best_block, int64_t* best_tiles);
+rfg_status rfg_batch_destroy(rfg_batch batch);
+/* the library's own stream (the synchronous entry points run on it) */
+rfg_status rfg_get_stream(void** cuda_stream);
+
 /* ------------------------------------------------------- experimental::Multi*
  * MultiLevenshtein (Levenshtein.hpp:297-419), MultiIndel (Indel.hpp:77-146),
  * MultiLCSseq (LCSseq.hpp:77-195), MultiOSA (OSA.hpp:113-230), MultiJaro (Jaro.hpp:64-193),

@@ -12,6 +12,7 @@ CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIB_DIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIB_DIR, "librapidfuzz_gb300.so")
+PEAK_LIB = os.path.join(LIB_DIR, "librfg_peak.so")  # INT32 issue-rate microbenchmark (bench roofline)
 
 SOURCES = ["rfg_api.cu", "rfg_k_lev.cu", "rfg_k_lcs.cu", "rfg_k_osa.cu", "rfg_k_jaro.cu", "rfg_k_generic.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -41,7 +42,7 @@ def _compile(src):
 
 def build(force=False, verbose=False):
     """Compile the library if any source is newer than it; returns the .so path."""
-    if not force and os.path.exists(LIB):
+    if not force and os.path.exists(LIB) and os.path.exists(PEAK_LIB):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in _deps()):
             return LIB
@@ -55,6 +56,10 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    r = subprocess.run([nvcc()] + ARCH + ["-O3", "-Xcompiler", "-fPIC", "-shared", "-o", PEAK_LIB,
+                                          os.path.join(CSRC, "rfg_peak.cu")], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("peak benchmark build failed:\n%s%s" % (r.stdout, r.stderr))
     if verbose:
         print("built", LIB)
     return LIB

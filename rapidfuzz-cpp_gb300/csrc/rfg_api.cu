@@ -250,11 +250,33 @@ struct BatchSpec {
 };
 
 int64_t g_tiles_target = 0; /* override of the tile-count target (autotuning) */
+int g_block_override = 0;   /* override of the tile kernels' block size (autotuning) */
 
-/* Score every (query, choice) pair on the device, results to spec.out (device). */
-rfg_status run_batch(const QuerySet& q, const KStrings& c, const BatchSpec& spec)
+/* A prepared batch: everything a launch needs is on the device, so enqueue() only
+ * resets the tile counters and launches the kernels (no host work, no allocation,
+ * no synchronisation) -- relaunchable and capturable in a CUDA graph. */
+struct LaunchRec {
+    const void* fn;
+    unsigned grid;
+    int block;
+    size_t smem;
+    KParams a;
+};
+
+struct Prepared {
+    std::vector<LaunchRec> launches;
+    DBuf qlist, small, scratch[1];
+    int* counters = nullptr;
+    int* err = nullptr;
+    int64_t scratch_words = 0;
+};
+
+rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& spec, Prepared* pb)
 {
     const int64_t nq = q.dev.n, nc = c.n;
+    RFG_TRY(pb->small.alloc(16 * sizeof(int)));
+    pb->counters = pb->small.as<int>();
+    pb->err = pb->counters + 15;
     if (nq == 0 || nc == 0) return RFG_OK;
     const int fam = metric_family(spec.metric, spec.form, spec.sp);
 
@@ -287,25 +309,19 @@ rfg_status run_batch(const QuerySet& q, const KStrings& c, const BatchSpec& spec
         cls_off[k] = qall.size();
         qall.insert(qall.end(), cls[k].begin(), cls[k].end());
     }
-    DBuf d_qlist, d_small;
-    RFG_TRY(d_qlist.alloc(qall.size() * 4));
-    RFG_TRY(d_small.alloc(16 * sizeof(int)));
-    RFG_CUDA(cudaMemcpyAsync(d_qlist.p, qall.data(), qall.size() * 4, cudaMemcpyHostToDevice, g.stream));
-    RFG_CUDA(cudaMemsetAsync(d_small.p, 0, 16 * sizeof(int), g.stream));
-    int* counters = d_small.as<int>();
-    int* err = counters + 15;
+    RFG_TRY(pb->qlist.alloc(qall.size() * 4));
+    RFG_CUDA(cudaMemcpyAsync(pb->qlist.p, qall.data(), qall.size() * 4, cudaMemcpyHostToDevice, g.stream));
 
     for (int k = 0; k < 5; ++k) {
         if (cls[k].empty()) continue;
-        DBuf scratch; /* freed (stream-ordered) after this class's launch */
         KParams a;
         memset(&a, 0, sizeof a);
         a.q = q.dev;
         a.c = c;
-        a.qlist = d_qlist.as<int32_t>() + cls_off[k];
+        a.qlist = pb->qlist.as<int32_t>() + cls_off[k];
         a.nq = (int32_t)cls[k].size();
-        a.counter = counters + k;
-        a.err = err;
+        a.counter = pb->counters + k;
+        a.err = pb->err;
         a.metric = spec.metric;
         a.op = spec.op;
         a.form = spec.form;
@@ -330,7 +346,7 @@ rfg_status run_batch(const QuerySet& q, const KStrings& c, const BatchSpec& spec
             case FAM_OSA: fn = tiles_kernel_osa(c.width, W); break;
             default: fn = tiles_kernel_jaro(c.width, W);
             }
-            block = 256;
+            block = g_block_override > 0 ? g_block_override : 256;
             smem = tiles_smem_bytes(W, a.hcap);
             if (smem > 48 * 1024) RFG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             per_sm = occupancy(fn, block, smem);
@@ -352,7 +368,7 @@ rfg_status run_batch(const QuerySet& q, const KStrings& c, const BatchSpec& spec
         a.nchunks = (nc + chunk - 1) / chunk;
         const int64_t ntiles = (int64_t)a.nq * a.nchunks;
         if (ntiles > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "batch too large for one launch");
-        int64_t grid = std::min<int64_t>(ntiles, slots);
+        const int64_t grid = std::min<int64_t>(ntiles, slots);
         if (k == 4) {
             /* any-length kernel: pattern table + per-thread state in global scratch */
             const int wmax = (fam == FAM_WF || fam == FAM_NONE) ? 0 : (int)((cls_maxlen[k] + 63) / 64);
@@ -367,17 +383,42 @@ rfg_status run_batch(const QuerySet& q, const KStrings& c, const BatchSpec& spec
             a.wmax = wmax;
             a.scratch_per_thread = per_thread;
             a.scratch_per_cta = (wmax ? (int64_t)(256 + a.hcap + 1) * wmax + a.hcap : 0) + (int64_t)block * per_thread;
-            RFG_TRY(scratch.alloc((size_t)grid * a.scratch_per_cta * 8));
-            a.scratch = scratch.as<u64>();
+            RFG_TRY(pb->scratch[0].alloc((size_t)grid * a.scratch_per_cta * 8));
+            pb->scratch_words = grid * a.scratch_per_cta;
+            a.scratch = pb->scratch[0].as<u64>();
         }
-        void* args[] = {&a};
-        RFG_CUDA(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(block), args, smem, g.stream));
+        pb->launches.push_back(LaunchRec{fn, (unsigned)grid, block, smem, a});
     }
+    return RFG_OK;
+}
+
+rfg_status enqueue_batch(const Prepared& pb, cudaStream_t st)
+{
+    RFG_CUDA(cudaMemsetAsync(pb.counters, 0, 16 * sizeof(int), st));
+    for (const LaunchRec& L : pb.launches) {
+        KParams a = L.a;
+        void* args[] = {&a};
+        RFG_CUDA(cudaLaunchKernel(L.fn, dim3(L.grid), dim3(L.block), args, L.smem, st));
+    }
+    return RFG_OK;
+}
+
+rfg_status check_batch(const Prepared& pb, cudaStream_t st)
+{
     int h_err = 0;
-    RFG_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, g.stream));
-    RFG_CUDA(cudaStreamSynchronize(g.stream));
+    RFG_CUDA(cudaMemcpyAsync(&h_err, pb.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RFG_CUDA(cudaStreamSynchronize(st));
     if (h_err) return fail(RFG_ERR_DEVICE_CHECK, "device-side check failed (code %d)", h_err);
     return RFG_OK;
+}
+
+/* Score every (query, choice) pair on the device, results to spec.out (device). */
+rfg_status run_batch(const QuerySet& q, const KStrings& c, const BatchSpec& spec)
+{
+    Prepared pb;
+    RFG_TRY(prepare_batch(q, c, spec, &pb));
+    RFG_TRY(enqueue_batch(pb, g.stream));
+    return check_batch(pb, g.stream);
 }
 
 size_t dtype_size(int dt) { return dt == RFG_I32 ? 4 : 8; }
@@ -483,6 +524,22 @@ struct rfg_cached_s {
     std::vector<unsigned char> host; /* s1 (the reference's CachedX keeps a copy too) */
     DBuf data, off;
     QuerySet qs;
+};
+
+struct rfg_batch_s {
+    QuerySet qs;
+    KStrings ck{};
+    DBuf qd, qo, cd, co;
+    BatchSpec spec{};
+    Prepared* pb = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int block = 0;
+    int64_t tiles = 0;
+    ~rfg_batch_s()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+        delete pb;
+    }
 };
 
 struct rfg_multi_s {
@@ -757,6 +814,182 @@ rfg_status rfg_multi_score_f64(rfg_multi h, rfg_op op, double* scores, size_t sc
     std::lock_guard<std::recursive_mutex> lk(g.mu);
     if (h && is_int_result(h->metric, op)) return fail(RFG_ERR_INVALID_ARGUMENT, "this metric/op returns integers");
     return multi_score(h, op, scores, score_count, s2, len2, width2, rfg_cutoff{0, score_cutoff, 0, 0.0}, RFG_F64);
+}
+
+/* --------------------------------------------------------- prepared batches */
+
+static rfg_status batch_reprepare(rfg_batch b, int block, int64_t tiles)
+{
+    const int ob = g_block_override;
+    const int64_t ot = g_tiles_target;
+    g_block_override = block;
+    g_tiles_target = tiles;
+    Prepared* np = new Prepared();
+    rfg_status st = prepare_batch(b->qs, b->ck, b->spec, np);
+    g_block_override = ob;
+    g_tiles_target = ot;
+    if (st == RFG_OK && cudaStreamSynchronize(g.stream) != cudaSuccess) st = fail(RFG_ERR_CUDA, "prepare failed");
+    if (st != RFG_OK) {
+        delete np;
+        return st;
+    }
+    delete b->pb;
+    b->pb = np;
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    b->block = block;
+    b->tiles = tiles;
+    return RFG_OK;
+}
+
+rfg_status rfg_batch_create(rfg_metric metric, rfg_op op, rfg_form form, const rfg_strings* Q, const rfg_strings* C,
+                            const rfg_params* p, rfg_cutoff cut, rfg_dtype dt, void* out, int64_t ld, uint32_t flags,
+                            rfg_batch* outb)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (!outb) return fail(RFG_ERR_INVALID_ARGUMENT, "batch is NULL");
+    *outb = nullptr;
+    RFG_TRY(check_metric_op(metric, op, form));
+    RFG_TRY(check_strings(Q, "queries"));
+    RFG_TRY(check_strings(C, "choices"));
+    RFG_TRY(check_dtype(metric, op, dt));
+    const ScoreParams sp = to_sp(p);
+    RFG_TRY(check_params(metric, sp));
+    if (!out) return fail(RFG_ERR_INVALID_ARGUMENT, "out (device memory) is NULL");
+    const int64_t nq = Q->count, nc = C->count;
+    if (ld == 0) ld = nc;
+    if (ld < nc) return fail(RFG_ERR_INVALID_ARGUMENT, "ld must be >= the number of choices");
+    RFG_TRY(ensure_ctx());
+    rfg_batch b = new rfg_batch_s();
+    rfg_status st = RFG_OK;
+    if (flags & RFG_DEVICE_INPUTS) {
+        std::vector<int64_t> off(nq + 1);
+        std::vector<unsigned char> qh;
+        if (cudaMemcpy(off.data(), Q->offsets, (nq + 1) * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = fail(RFG_ERR_CUDA, "reading query offsets failed");
+        if (st == RFG_OK && Q->char_width > 1 && nq) {
+            qh.resize((size_t)off[nq] * Q->char_width);
+            if (cudaMemcpy(qh.data(), Q->data, qh.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+                st = fail(RFG_ERR_CUDA, "reading queries failed");
+        }
+        if (st == RFG_OK) st = query_info_from_host(qh.data(), off.data(), nq, Q->char_width, &b->qs);
+        b->qs.dev = KStrings{(const unsigned char*)Q->data, Q->offsets, nq, Q->char_width};
+        b->ck = KStrings{(const unsigned char*)C->data, C->offsets, nc, C->char_width};
+    }
+    else {
+        st = query_info_from_host(Q->data, Q->offsets, nq, Q->char_width, &b->qs);
+        if (st == RFG_OK) st = upload_strings(Q, &b->qd, &b->qo, &b->qs.dev);
+        if (st == RFG_OK) st = upload_strings(C, &b->cd, &b->co, &b->ck);
+    }
+    b->spec.metric = metric;
+    b->spec.op = op;
+    b->spec.form = form;
+    b->spec.sp = sp;
+    b->spec.ci = cut.cutoff_i;
+    b->spec.cf = cut.cutoff_f;
+    b->spec.out_dtype = dt;
+    b->spec.out = out;
+    b->spec.ld = ld;
+    if (st == RFG_OK) st = batch_reprepare(b, 0, 0);
+    if (st != RFG_OK) {
+        delete b;
+        return st;
+    }
+    *outb = b;
+    return RFG_OK;
+}
+
+rfg_status rfg_batch_launch(rfg_batch b, void* stream, uint32_t launch_flags)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (!b) return fail(RFG_ERR_INVALID_ARGUMENT, "batch is NULL");
+    cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+    if (!(launch_flags & RFG_LAUNCH_GRAPH)) return enqueue_batch(*b->pb, st);
+    if (!b->graph) {
+        cudaGraph_t graph;
+        RFG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        rfg_status s = enqueue_batch(*b->pb, st);
+        cudaError_t e = cudaStreamEndCapture(st, &graph);
+        if (s != RFG_OK) return s;
+        if (e != cudaSuccess) return fail(RFG_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&b->graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            b->graph = nullptr;
+            return fail(RFG_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+        }
+    }
+    RFG_CUDA(cudaGraphLaunch(b->graph, st));
+    return RFG_OK;
+}
+
+rfg_status rfg_batch_check(rfg_batch b, void* stream)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (!b) return fail(RFG_ERR_INVALID_ARGUMENT, "batch is NULL");
+    return check_batch(*b->pb, stream ? (cudaStream_t)stream : g.stream);
+}
+
+rfg_status rfg_batch_tune(rfg_batch b, void* stream, int32_t* best_block, int64_t* best_tiles)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (!b) return fail(RFG_ERR_INVALID_ARGUMENT, "batch is NULL");
+    cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+    cudaEvent_t e0, e1;
+    RFG_CUDA(cudaEventCreate(&e0));
+    RFG_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bb = 256;
+    int64_t bt = 0;
+    const int blocks[] = {128, 256};
+    const int mults[] = {2, 4, 8, 16, 32};
+    for (int blk : blocks) {
+        for (int mu : mults) {
+            const int64_t tiles = (int64_t)g.sms * mu * (256 / blk) * 2;
+            RFG_TRY(batch_reprepare(b, blk, tiles));
+            float times[3];
+            for (int r = 0; r < 3; ++r) {
+                RFG_CUDA(cudaEventRecord(e0, st));
+                RFG_TRY(enqueue_batch(*b->pb, st));
+                RFG_CUDA(cudaEventRecord(e1, st));
+                RFG_CUDA(cudaEventSynchronize(e1));
+                RFG_CUDA(cudaEventElapsedTime(&times[r], e0, e1));
+            }
+            std::sort(times, times + 3);
+            if (times[1] < best) {
+                best = times[1];
+                bb = blk;
+                bt = tiles;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    RFG_TRY(batch_reprepare(b, bb, bt));
+    RFG_TRY(check_batch(*b->pb, st));
+    if (best_block) *best_block = bb;
+    if (best_tiles) *best_tiles = bt;
+    return RFG_OK;
+}
+
+rfg_status rfg_batch_destroy(rfg_batch b)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (!b) return RFG_OK;
+    cudaDeviceSynchronize();
+    delete b;
+    return RFG_OK;
+}
+
+rfg_status rfg_get_stream(void** stream)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (!stream) return fail(RFG_ERR_INVALID_ARGUMENT, "stream is NULL");
+    RFG_TRY(ensure_ctx());
+    *stream = (void*)g.stream;
+    return RFG_OK;
 }
 
 } /* extern "C" */

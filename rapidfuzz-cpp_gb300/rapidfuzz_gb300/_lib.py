@@ -77,6 +77,13 @@ def lib():
             "rfg_multi_result_count": ([vp, P(ctypes.c_size_t)], ctypes.c_int),
             "rfg_multi_score_i64": ([vp, ctypes.c_int, P(i64), ctypes.c_size_t, vp, i64, i32, u64], ctypes.c_int),
             "rfg_multi_score_f64": ([vp, ctypes.c_int, P(f64), ctypes.c_size_t, vp, i64, i32, f64], ctypes.c_int),
+            "rfg_batch_create": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, P(Strings), P(Strings), P(Params), Cutoff,
+                                  ctypes.c_int, vp, i64, ctypes.c_uint32, P(vp)], ctypes.c_int),
+            "rfg_batch_launch": ([vp, vp, ctypes.c_uint32], ctypes.c_int),
+            "rfg_batch_check": ([vp, vp], ctypes.c_int),
+            "rfg_batch_tune": ([vp, vp, P(i32), P(i64)], ctypes.c_int),
+            "rfg_batch_destroy": ([vp], ctypes.c_int),
+            "rfg_get_stream": ([P(vp)], ctypes.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -272,3 +279,50 @@ def _batch(b):
     s = Strings(data.ctypes.data, offsets.ctypes.data, offsets.size - 1, width)
     s._keep = (data, offsets)
     return s
+
+
+LAUNCH_GRAPH = 1
+
+
+class Batch:
+    """A prepared cdist (rfg_batch_*): launch() only enqueues kernels on a stream."""
+
+    def __init__(self, metric, op, queries, choices, out_ptr, score_cutoff=None, weights=(1, 1, 1),
+                 prefix_weight=0.1, out_dtype=None, form=FORM_CACHED, flags=0, ld=0):
+        self._h = ctypes.c_void_p()
+        q, ch = _batch(queries), _batch(choices)
+        self._keep = (q, ch)
+        is_int = result_is_int(metric, op)
+        if out_dtype is None:
+            out_dtype = I64 if is_int else F64
+        c = _default_cutoff(metric, op) if score_cutoff is None else score_cutoff
+        cut = Cutoff(int(c) if is_int else 0, 0.0 if is_int else float(c), 0, 0.0)
+        p = make_params(weights, prefix_weight)
+        check(lib().rfg_batch_create(metric, op, form, ctypes.byref(q), ctypes.byref(ch), ctypes.byref(p), cut,
+                                     out_dtype, out_ptr, ld, flags, ctypes.byref(self._h)))
+
+    def launch(self, stream=0, graph=True):
+        check(lib().rfg_batch_launch(self._h, stream, LAUNCH_GRAPH if graph else 0))
+
+    def check(self, stream=0):
+        check(lib().rfg_batch_check(self._h, stream))
+
+    def tune(self, stream=0):
+        b, t = ctypes.c_int32(), ctypes.c_int64()
+        check(lib().rfg_batch_tune(self._h, stream, ctypes.byref(b), ctypes.byref(t)))
+        return b.value, t.value
+
+    def close(self):
+        if self._h and self._h.value:
+            lib().rfg_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        if _lib is not None:
+            self.close()
+
+
+def library_stream():
+    s = ctypes.c_void_p()
+    check(lib().rfg_get_stream(ctypes.byref(s)))
+    return s.value or 0
