@@ -172,6 +172,22 @@ rfg_status rfg_batch_destroy(rfg_batch batch);
 /* the library's own stream (the synchronous entry points run on it) */
 rfg_status rfg_get_stream(void** cuda_stream);
 
+/* ------------------------------------------------------ no-allocation cdist
+ * rfg_cdist_noalloc has no counterpart in the reference.  It is for callers that may
+ * not allocate device memory (inside another framework's memory manager, in a process
+ * whose device memory is reserved up front, or in a service that must not grow after
+ * start-up) and already hold their strings and result buffer on the device: queries,
+ * choices and out are device pointers, and the call allocates nothing.  Its scratch is a
+ * fixed 32 MiB array in the library's device image, shared by every call on a device
+ * and held by every GPU that loads the library until exit.  The first call on a device
+ * looks up that array's address (make it before any stream capture); calls that
+ * overlap on the GPU race on the array and must be serialised.  max_query_len bounds
+ * the query lengths (at most 4096 code units); larger values, or a query longer than
+ * the bound, return RFG_ERR_INVALID_ARGUMENT.  Runs on cuda_stream and waits for it. */
+rfg_status rfg_cdist_noalloc(rfg_metric metric, rfg_op op, rfg_form form, const rfg_strings* queries,
+                             const rfg_strings* choices, int64_t max_query_len, const rfg_params* params,
+                             rfg_cutoff cutoff, rfg_dtype out_dtype, void* out, int64_t ld, void* cuda_stream);
+
 /* ------------------------------------------------------- experimental::Multi*
  * MultiLevenshtein (Levenshtein.hpp:297-419), MultiIndel (Indel.hpp:77-146),
  * MultiLCSseq (LCSseq.hpp:77-195), MultiOSA (OSA.hpp:113-230), MultiJaro (Jaro.hpp:64-193),

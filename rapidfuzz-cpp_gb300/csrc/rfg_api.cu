@@ -514,6 +514,15 @@ rfg_status score_one(int metric, int op, int form, const void* s1, int64_t l1, i
 
 } // namespace
 
+namespace rfg {
+/* error message of the calling thread, set from other translation units */
+rfg_status set_last_error(rfg_status s, const char* msg)
+{
+    g_err = msg;
+    return s;
+}
+} // namespace rfg
+
 /* ======================================================================== C ABI */
 
 struct rfg_cached_s {

@@ -84,6 +84,8 @@ def lib():
             "rfg_batch_tune": ([vp, vp, P(i32), P(i64)], ctypes.c_int),
             "rfg_batch_destroy": ([vp], ctypes.c_int),
             "rfg_get_stream": ([P(vp)], ctypes.c_int),
+            "rfg_cdist_noalloc": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, P(Strings), P(Strings), i64, P(Params),
+                                   Cutoff, ctypes.c_int, vp, i64, vp], ctypes.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
