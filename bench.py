@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape (fixed launch list)")
     ap.add_argument("--nq", type=int, default=4096)
     ap.add_argument("--nc", type=int, default=4096)
     return ap.parse_args()
@@ -212,7 +213,8 @@ def main():
     for (name, m), o in zip(metrics, outs):
         b = R.Batch(m, R.DISTANCE, (qd.data_ptr(), qo.data_ptr(), 1, nq), (cd.data_ptr(), co.data_ptr(), 1, nc),
                     o.data_ptr(), CUTOFF, out_dtype=R.I32, flags=R.DEVICE_INPUTS)
-        b.tune(stream.cuda_stream)
+        if not args.no_tune:
+            b.tune(stream.cuda_stream)
         batches.append((name, b))
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
 

@@ -265,13 +265,62 @@ struct LaunchRec {
 
 struct Prepared {
     std::vector<LaunchRec> launches;
-    DBuf qlist, small, scratch[1];
+    DBuf qlist, small, scratch[1], perm;
     int* counters = nullptr;
     int* err = nullptr;
     int64_t scratch_words = 0;
 };
 
-rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& spec, Prepared* pb)
+/* Host-side choice offsets (for the length order of each chunk): read from the device
+ * when the batch lives there. */
+rfg_status choice_lengths(const KStrings& c, const int64_t* host_off, std::vector<int32_t>* len)
+{
+    const int64_t nc = c.n;
+    std::vector<int64_t> tmp;
+    if (!host_off) {
+        tmp.resize(nc + 1);
+        RFG_CUDA(cudaMemcpyAsync(tmp.data(), c.off, (nc + 1) * 8, cudaMemcpyDeviceToHost, g.stream));
+        RFG_CUDA(cudaStreamSynchronize(g.stream));
+        host_off = tmp.data();
+    }
+    len->resize(nc);
+    for (int64_t i = 0; i < nc; ++i) {
+        const int64_t l = host_off[i + 1] - host_off[i];
+        (*len)[i] = (int32_t)(l < 0 ? 0 : l > INT32_MAX ? INT32_MAX : l);
+    }
+    return RFG_OK;
+}
+
+/* stable counting sort of each chunk's positions by choice length */
+void chunk_length_order(const std::vector<int32_t>& len, int64_t chunk, std::vector<int32_t>* perm)
+{
+    const int64_t nc = (int64_t)len.size();
+    perm->resize(nc);
+    std::vector<int64_t> count;
+    for (int64_t c0 = 0; c0 < nc; c0 += chunk) {
+        const int64_t c1 = std::min(nc, c0 + chunk);
+        int32_t lo = INT32_MAX, hi = 0;
+        for (int64_t i = c0; i < c1; ++i) {
+            lo = std::min(lo, len[i]);
+            hi = std::max(hi, len[i]);
+        }
+        const int64_t range = (int64_t)hi - lo + 1;
+        if (range > 4 * (c1 - c0) + 1024) { /* wide length range: comparison sort */
+            std::vector<int32_t> idx(c1 - c0);
+            for (int64_t i = c0; i < c1; ++i) idx[i - c0] = (int32_t)i;
+            std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) { return len[a] < len[b]; });
+            std::copy(idx.begin(), idx.end(), perm->begin() + c0);
+            continue;
+        }
+        count.assign(range + 1, 0);
+        for (int64_t i = c0; i < c1; ++i) ++count[len[i] - lo + 1];
+        for (int64_t k = 1; k <= range; ++k) count[k] += count[k - 1];
+        for (int64_t i = c0; i < c1; ++i) (*perm)[c0 + count[len[i] - lo]++] = (int32_t)i;
+    }
+}
+
+rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& spec, Prepared* pb,
+                         const int64_t* host_choice_off = nullptr)
 {
     const int64_t nq = q.dev.n, nc = c.n;
     RFG_TRY(pb->small.alloc(16 * sizeof(int)));
@@ -311,6 +360,20 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
     }
     RFG_TRY(pb->qlist.alloc(qall.size() * 4));
     RFG_CUDA(cudaMemcpyAsync(pb->qlist.p, qall.data(), qall.size() * 4, cudaMemcpyHostToDevice, g.stream));
+
+    /* one chunking of the choices for every class, each chunk visited in length order */
+    const int64_t target_all = g_tiles_target > 0 ? g_tiles_target : (int64_t)g.sms * 32;
+    const int blk = g_block_override > 0 ? g_block_override : 256;
+    int64_t chunk = (nc * nq + target_all - 1) / target_all;
+    chunk = std::max<int64_t>(chunk, blk);
+    chunk = std::min<int64_t>(chunk, std::max<int64_t>(nc, 1));
+    chunk = (chunk + blk - 1) / blk * blk;
+    std::vector<int32_t> clen, perm;
+    RFG_TRY(choice_lengths(c, host_choice_off, &clen));
+    chunk_length_order(clen, chunk, &perm);
+    RFG_TRY(pb->perm.alloc((size_t)nc * 4));
+    RFG_CUDA(cudaMemcpyAsync(pb->perm.p, perm.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, g.stream));
+    RFG_CUDA(cudaStreamSynchronize(g.stream)); /* perm / qall are host temporaries */
 
     for (int k = 0; k < 5; ++k) {
         if (cls[k].empty()) continue;
@@ -356,15 +419,10 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             block = 128;
             per_sm = 2;
         }
-        /* tiles: enough to keep every SM busy and balanced, but each big enough to
-         * amortise the pattern build (longest queries first) */
+        /* tiles: (query, chunk), longest queries first; persistent CTAs fill every SM */
         const int64_t slots = (int64_t)g.sms * per_sm;
-        const int64_t target = g_tiles_target > 0 ? g_tiles_target : slots * 4;
-        int64_t chunk = (nc * a.nq + target - 1) / target;
-        chunk = std::max<int64_t>(chunk, block);
-        chunk = std::min<int64_t>(chunk, std::max<int64_t>(nc, 1));
-        chunk = (chunk + block - 1) / block * block;
         a.chunk = chunk;
+        a.perm = pb->perm.as<int32_t>();
         a.nchunks = (nc + chunk - 1) / chunk;
         const int64_t ntiles = (int64_t)a.nq * a.nchunks;
         if (ntiles > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "batch too large for one launch");
@@ -413,10 +471,11 @@ rfg_status check_batch(const Prepared& pb, cudaStream_t st)
 }
 
 /* Score every (query, choice) pair on the device, results to spec.out (device). */
-rfg_status run_batch(const QuerySet& q, const KStrings& c, const BatchSpec& spec)
+rfg_status run_batch(const QuerySet& q, const KStrings& c, const BatchSpec& spec,
+                     const int64_t* host_choice_off = nullptr)
 {
     Prepared pb;
-    RFG_TRY(prepare_batch(q, c, spec, &pb));
+    RFG_TRY(prepare_batch(q, c, spec, &pb, host_choice_off));
     RFG_TRY(enqueue_batch(pb, g.stream));
     return check_batch(pb, g.stream);
 }
@@ -491,7 +550,7 @@ rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const 
         RFG_TRY(od.alloc((size_t)nq * ld * esz));
         spec.out = od.p;
     }
-    RFG_TRY(run_batch(qs, ck, spec));
+    RFG_TRY(run_batch(qs, ck, spec, dev_in ? nullptr : C->offsets));
     if (!(flags & RFG_DEVICE_OUTPUT) && nq * nc) {
         RFG_CUDA(cudaMemcpy2DAsync(out, ld * esz, od.p, ld * esz, nc * esz, nq, cudaMemcpyDeviceToHost, g.stream));
         RFG_CUDA(cudaStreamSynchronize(g.stream));
@@ -672,7 +731,7 @@ static rfg_status cached_many(rfg_cached h, int op, const rfg_strings* C, rfg_cu
         RFG_TRY(od.alloc((size_t)nc * dtype_size(dt)));
         spec.out = od.p;
     }
-    RFG_TRY(run_batch(h->qs, ck, spec));
+    RFG_TRY(run_batch(h->qs, ck, spec, (flags & RFG_DEVICE_INPUTS) ? nullptr : C->offsets));
     if (!(flags & RFG_DEVICE_OUTPUT) && nc) {
         RFG_CUDA(cudaMemcpyAsync(out, od.p, (size_t)nc * dtype_size(dt), cudaMemcpyDeviceToHost, g.stream));
         RFG_CUDA(cudaStreamSynchronize(g.stream));

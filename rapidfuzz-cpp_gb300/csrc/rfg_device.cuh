@@ -43,6 +43,7 @@ struct KParams {
     int out_dtype; /* 0 i32, 1 i64, 2 f64 */
     int64_t ld;
     int hcap;      /* hash slots for code units >= 256 (power of two, or 0) */
+    const int32_t* perm; /* choice order within each chunk (length-sorted), or nullptr */
     /* generic (scratch) kernels */
     u64* scratch;
     int64_t scratch_per_cta;    /* u64 words of the per-CTA pattern table region */
@@ -267,8 +268,11 @@ __global__ void __launch_bounds__(256) k_tiles(const KParams a)
         }
         const int64_t c0 = ch * a.chunk;
         const int64_t c1 = c0 + a.chunk < a.c.n ? c0 + a.chunk : a.c.n;
-        for (int64_t ci = c0 + threadIdx.x; ci < c1; ci += blockDim.x)
-            score_pair<FAM, W, CT>(a, rows, keys, qi, m, s_qpre, ci);
+        /* positions of a chunk are visited in length order, so the threads of a warp get
+         * pairs of similar work and pairs decided by the length filter cluster into
+         * whole warps */
+        for (int64_t p = c0 + threadIdx.x; p < c1; p += blockDim.x)
+            score_pair<FAM, W, CT>(a, rows, keys, qi, m, s_qpre, a.perm ? (int64_t)__ldg(a.perm + p) : p);
         __syncthreads();
     }
 }
@@ -421,8 +425,8 @@ __global__ void __launch_bounds__(128) k_generic(const KParams a)
         }
         const int64_t c0 = ch * a.chunk;
         const int64_t c1 = c0 + a.chunk < a.c.n ? c0 + a.chunk : a.c.n;
-        for (int64_t ci = c0 + threadIdx.x; ci < c1; ci += blockDim.x)
-            score_pair_generic<FAM, CT>(a, rows, keys, W, qi, m, qb, ci, st);
+        for (int64_t p = c0 + threadIdx.x; p < c1; p += blockDim.x)
+            score_pair_generic<FAM, CT>(a, rows, keys, W, qi, m, qb, a.perm ? (int64_t)__ldg(a.perm + p) : p, st);
         __syncthreads();
     }
 }

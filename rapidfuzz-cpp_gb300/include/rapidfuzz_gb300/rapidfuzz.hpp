@@ -1,0 +1,661 @@
+/*
+ * rapidfuzz_gb300/rapidfuzz.hpp -- the rapidfuzz-cpp API over the GB300 library.
+ *
+ * Same names, overloads, defaults and exceptions as rapidfuzz-cpp v3.3.3 (paths relative
+ * to that project), in namespace rapidfuzz_gb300; a caller switches with
+ *     namespace rapidfuzz = rapidfuzz_gb300;
+ * and links librapidfuzz_gb300.so.  Every call runs on the GPU through the C ABI in
+ * rapidfuzz_gb300.h; results are the reference's (integers bit-exact, doubles
+ * bit-identical).
+ *
+ *   free functions   rapidfuzz/distance/{Levenshtein,Indel,LCSseq,OSA,Jaro,JaroWinkler}.hpp
+ *   Cached* scorers  same files (CachedLevenshtein Levenshtein.hpp:421-482, ...)
+ *   Multi* scorers   experimental::Multi*<MaxLen> (Levenshtein.hpp:297-419, ...)
+ *   fuzz::ratio      rapidfuzz/fuzz.hpp:44-126
+ * Exceptions: std::invalid_argument where the reference throws it; std::runtime_error
+ * for device failures (the reference has none).
+ */
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <iterator>
+#include <limits>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "rapidfuzz_gb300.h"
+
+namespace rapidfuzz_gb300 {
+
+/* rapidfuzz/details/types.hpp:19-23 */
+struct LevenshteinWeightTable {
+    size_t insert_cost;
+    size_t delete_cost;
+    size_t replace_cost;
+};
+
+namespace detail {
+
+inline void throw_on(rfg_status s)
+{
+    if (s == RFG_OK) return;
+    const char* msg = rfg_last_error();
+    if (s == RFG_ERR_INVALID_ARGUMENT) throw std::invalid_argument(msg);
+    if (s == RFG_ERR_OUT_OF_RANGE) throw std::out_of_range(msg);
+    throw std::runtime_error(std::string("rapidfuzz_gb300: ") + msg);
+}
+
+/* a string as unsigned code units: contiguous storage is referenced, anything else copied */
+template <typename T>
+struct Units {
+    const void* data = nullptr;
+    int64_t len = 0;
+    int32_t width = 1;
+    std::vector<typename std::make_unsigned<T>::type> copy;
+};
+
+template <typename T>
+struct is_unit : std::integral_constant<bool, std::is_integral<T>::value && !std::is_same<T, bool>::value &&
+                                                  (sizeof(T) == 1 || sizeof(T) == 2 || sizeof(T) == 4 ||
+                                                   sizeof(T) == 8)> {};
+
+/* iterator overloads only take part for iterator types (no clash with Sentence + weights) */
+template <typename T, typename = void>
+struct is_iter : std::false_type {};
+template <typename T>
+struct is_iter<T, decltype(void(std::declval<typename std::iterator_traits<T>::iterator_category>()))>
+    : std::true_type {};
+template <typename T>
+using if_iter = typename std::enable_if<is_iter<T>::value, int>::type;
+template <typename T>
+using if_not_array = typename std::enable_if<!std::is_array<T>::value && !std::is_pointer<T>::value, int>::type;
+
+template <typename InputIt>
+Units<typename std::iterator_traits<InputIt>::value_type> units(InputIt first, InputIt last)
+{
+    using T = typename std::iterator_traits<InputIt>::value_type;
+    static_assert(is_unit<T>::value, "code units must be integral types of 1, 2, 4 or 8 bytes");
+    Units<T> u;
+    for (; first != last; ++first) u.copy.push_back(static_cast<typename std::make_unsigned<T>::type>(*first));
+    u.data = u.copy.data();
+    u.len = (int64_t)u.copy.size();
+    u.width = (int32_t)sizeof(T);
+    return u;
+}
+
+template <typename Sentence, if_not_array<Sentence> = 0>
+auto units(const Sentence& s) -> Units<typename std::decay<decltype(*std::begin(s))>::type>
+{
+    using T = typename std::decay<decltype(*std::begin(s))>::type;
+    static_assert(is_unit<T>::value, "code units must be integral types of 1, 2, 4 or 8 bytes");
+    Units<T> u;
+    const auto n = std::distance(std::begin(s), std::end(s));
+    if (n > 0 && std::is_pointer<decltype(&*std::begin(s))>::value &&
+        &*std::begin(s) + (n - 1) == &*std::prev(std::end(s))) {
+        u.data = static_cast<const void*>(&*std::begin(s));
+        u.len = (int64_t)n;
+    }
+    else {
+        for (const auto& ch : s) u.copy.push_back(static_cast<typename std::make_unsigned<T>::type>(ch));
+        u.data = u.copy.data();
+        u.len = (int64_t)u.copy.size();
+    }
+    u.width = (int32_t)sizeof(T);
+    return u;
+}
+
+/* NUL-terminated strings and string literals: the characters before the first NUL */
+template <typename CharT>
+Units<CharT> units(const CharT* s)
+{
+    Units<CharT> u;
+    int64_t n = 0;
+    while (s[n] != 0) ++n;
+    u.data = s;
+    u.len = n;
+    u.width = (int32_t)sizeof(CharT);
+    return u;
+}
+
+
+inline rfg_params lev_params(LevenshteinWeightTable w)
+{
+    return rfg_params{(int64_t)w.insert_cost, (int64_t)w.delete_cost, (int64_t)w.replace_cost, 0.1};
+}
+
+inline rfg_params jw_params(double pw) { return rfg_params{1, 1, 1, pw}; }
+
+template <typename U1, typename U2>
+size_t score_i(rfg_metric m, rfg_op op, const U1& a, const U2& b, const rfg_params& p, size_t cutoff, size_t hint)
+{
+    int64_t r = 0;
+    throw_on(rfg_score_i64(m, op, a.data, a.len, a.width, b.data, b.len, b.width, &p, cutoff, hint, &r));
+    return (size_t)r;
+}
+
+template <typename U1, typename U2>
+double score_f(rfg_metric m, rfg_op op, const U1& a, const U2& b, const rfg_params& p, double cutoff, double hint)
+{
+    double r = 0;
+    throw_on(rfg_score_f64(m, op, a.data, a.len, a.width, b.data, b.len, b.width, &p, cutoff, hint, &r));
+    return r;
+}
+
+/* the integer defaults of the reference: distance cutoff SIZE_MAX, similarity 0 */
+constexpr size_t SIZE_MAX_ = std::numeric_limits<size_t>::max();
+
+} // namespace detail
+
+/* -------------------------------------------------------------- free functions */
+
+#define RFG_FREE_INT(NAME, METRIC, OP, DEFCUT)                                                                 \
+    template <typename Sentence1, typename Sentence2>                                                          \
+    size_t NAME(const Sentence1& s1, const Sentence2& s2, size_t score_cutoff = DEFCUT)                        \
+    {                                                                                                          \
+        return detail::score_i(METRIC, OP, detail::units(s1), detail::units(s2), rfg_params{1, 1, 1, 0.1},     \
+                               score_cutoff, score_cutoff);                                                    \
+    }                                                                                                          \
+    template <typename InputIt1, typename InputIt2, detail::if_iter<InputIt1> = 0>                              \
+    size_t NAME(InputIt1 first1, InputIt1 last1, InputIt2 first2, InputIt2 last2, size_t score_cutoff = DEFCUT) \
+    {                                                                                                          \
+        return detail::score_i(METRIC, OP, detail::units(first1, last1), detail::units(first2, last2),         \
+                               rfg_params{1, 1, 1, 0.1}, score_cutoff, score_cutoff);                          \
+    }
+
+#define RFG_FREE_DBL(NAME, METRIC, OP, DEFCUT)                                                                 \
+    template <typename Sentence1, typename Sentence2>                                                          \
+    double NAME(const Sentence1& s1, const Sentence2& s2, double score_cutoff = DEFCUT)                        \
+    {                                                                                                          \
+        return detail::score_f(METRIC, OP, detail::units(s1), detail::units(s2), rfg_params{1, 1, 1, 0.1},     \
+                               score_cutoff, score_cutoff);                                                    \
+    }                                                                                                          \
+    template <typename InputIt1, typename InputIt2, detail::if_iter<InputIt1> = 0>                              \
+    double NAME(InputIt1 first1, InputIt1 last1, InputIt2 first2, InputIt2 last2, double score_cutoff = DEFCUT) \
+    {                                                                                                          \
+        return detail::score_f(METRIC, OP, detail::units(first1, last1), detail::units(first2, last2),         \
+                               rfg_params{1, 1, 1, 0.1}, score_cutoff, score_cutoff);                          \
+    }
+
+/* Indel.hpp:12-63, LCSseq.hpp:12-63, OSA.hpp:12-111, Jaro.hpp:12-61 */
+RFG_FREE_INT(indel_distance, RFG_INDEL, RFG_DISTANCE, detail::SIZE_MAX_)
+RFG_FREE_INT(indel_similarity, RFG_INDEL, RFG_SIMILARITY, 0)
+RFG_FREE_DBL(indel_normalized_distance, RFG_INDEL, RFG_NORMALIZED_DISTANCE, 1.0)
+RFG_FREE_DBL(indel_normalized_similarity, RFG_INDEL, RFG_NORMALIZED_SIMILARITY, 0.0)
+RFG_FREE_INT(lcs_seq_distance, RFG_LCSSEQ, RFG_DISTANCE, detail::SIZE_MAX_)
+RFG_FREE_INT(lcs_seq_similarity, RFG_LCSSEQ, RFG_SIMILARITY, 0)
+RFG_FREE_DBL(lcs_seq_normalized_distance, RFG_LCSSEQ, RFG_NORMALIZED_DISTANCE, 1.0)
+RFG_FREE_DBL(lcs_seq_normalized_similarity, RFG_LCSSEQ, RFG_NORMALIZED_SIMILARITY, 0.0)
+RFG_FREE_INT(osa_distance, RFG_OSA, RFG_DISTANCE, detail::SIZE_MAX_)
+RFG_FREE_INT(osa_similarity, RFG_OSA, RFG_SIMILARITY, 0)
+RFG_FREE_DBL(osa_normalized_distance, RFG_OSA, RFG_NORMALIZED_DISTANCE, 1.0)
+RFG_FREE_DBL(osa_normalized_similarity, RFG_OSA, RFG_NORMALIZED_SIMILARITY, 0.0)
+RFG_FREE_DBL(jaro_distance, RFG_JARO, RFG_DISTANCE, 1.0)
+RFG_FREE_DBL(jaro_similarity, RFG_JARO, RFG_SIMILARITY, 0.0)
+RFG_FREE_DBL(jaro_normalized_distance, RFG_JARO, RFG_NORMALIZED_DISTANCE, 1.0)
+RFG_FREE_DBL(jaro_normalized_similarity, RFG_JARO, RFG_NORMALIZED_SIMILARITY, 0.0)
+
+#undef RFG_FREE_INT
+#undef RFG_FREE_DBL
+
+/* Levenshtein.hpp:140-265: weights, score_cutoff, score_hint */
+template <typename Sentence1, typename Sentence2>
+size_t levenshtein_distance(const Sentence1& s1, const Sentence2& s2, LevenshteinWeightTable weights = {1, 1, 1},
+                            size_t score_cutoff = detail::SIZE_MAX_, size_t score_hint = detail::SIZE_MAX_)
+{
+    return detail::score_i(RFG_LEVENSHTEIN, RFG_DISTANCE, detail::units(s1), detail::units(s2),
+                           detail::lev_params(weights), score_cutoff, score_hint);
+}
+template <typename InputIt1, typename InputIt2, detail::if_iter<InputIt1> = 0>
+size_t levenshtein_distance(InputIt1 first1, InputIt1 last1, InputIt2 first2, InputIt2 last2,
+                            LevenshteinWeightTable weights = {1, 1, 1}, size_t score_cutoff = detail::SIZE_MAX_,
+                            size_t score_hint = detail::SIZE_MAX_)
+{
+    return detail::score_i(RFG_LEVENSHTEIN, RFG_DISTANCE, detail::units(first1, last1), detail::units(first2, last2),
+                           detail::lev_params(weights), score_cutoff, score_hint);
+}
+template <typename Sentence1, typename Sentence2>
+size_t levenshtein_similarity(const Sentence1& s1, const Sentence2& s2, LevenshteinWeightTable weights = {1, 1, 1},
+                              size_t score_cutoff = 0, size_t score_hint = 0)
+{
+    return detail::score_i(RFG_LEVENSHTEIN, RFG_SIMILARITY, detail::units(s1), detail::units(s2),
+                           detail::lev_params(weights), score_cutoff, score_hint);
+}
+template <typename Sentence1, typename Sentence2>
+double levenshtein_normalized_distance(const Sentence1& s1, const Sentence2& s2,
+                                       LevenshteinWeightTable weights = {1, 1, 1}, double score_cutoff = 1.0,
+                                       double score_hint = 1.0)
+{
+    return detail::score_f(RFG_LEVENSHTEIN, RFG_NORMALIZED_DISTANCE, detail::units(s1), detail::units(s2),
+                           detail::lev_params(weights), score_cutoff, score_hint);
+}
+template <typename Sentence1, typename Sentence2>
+double levenshtein_normalized_similarity(const Sentence1& s1, const Sentence2& s2,
+                                         LevenshteinWeightTable weights = {1, 1, 1}, double score_cutoff = 0.0,
+                                         double score_hint = 0.0)
+{
+    return detail::score_f(RFG_LEVENSHTEIN, RFG_NORMALIZED_SIMILARITY, detail::units(s1), detail::units(s2),
+                           detail::lev_params(weights), score_cutoff, score_hint);
+}
+
+/* JaroWinkler.hpp:11-73: prefix_weight, score_cutoff */
+#define RFG_JW(NAME, OP, DEFCUT)                                                                               \
+    template <typename Sentence1, typename Sentence2>                                                          \
+    double NAME(const Sentence1& s1, const Sentence2& s2, double prefix_weight = 0.1, double score_cutoff = DEFCUT) \
+    {                                                                                                          \
+        return detail::score_f(RFG_JARO_WINKLER, OP, detail::units(s1), detail::units(s2),                     \
+                               detail::jw_params(prefix_weight), score_cutoff, score_cutoff);                  \
+    }
+RFG_JW(jaro_winkler_distance, RFG_DISTANCE, 1.0)
+RFG_JW(jaro_winkler_similarity, RFG_SIMILARITY, 0.0)
+RFG_JW(jaro_winkler_normalized_distance, RFG_NORMALIZED_DISTANCE, 1.0)
+RFG_JW(jaro_winkler_normalized_similarity, RFG_NORMALIZED_SIMILARITY, 0.0)
+#undef RFG_JW
+
+/* ------------------------------------------------------------------ Cached* */
+
+namespace detail {
+
+/* CachedDistanceBase / CachedSimilarityBase / CachedNormalizedMetricBase (distance.hpp:210-388) */
+class CachedScorer {
+public:
+    CachedScorer(const CachedScorer&) = delete;
+    CachedScorer& operator=(const CachedScorer&) = delete;
+    ~CachedScorer()
+    {
+        if (h_) rfg_cached_destroy(h_);
+    }
+
+protected:
+    template <typename U>
+    CachedScorer(rfg_metric m, const U& s1, const rfg_params& p) : metric_(m)
+    {
+        throw_on(rfg_cached_create(m, s1.data, s1.len, s1.width, &p, &h_));
+    }
+    template <typename U>
+    size_t cached_i(rfg_op op, const U& s2, size_t cutoff, size_t hint) const
+    {
+        int64_t r = 0;
+        throw_on(rfg_cached_score_i64(h_, op, s2.data, s2.len, s2.width, cutoff, hint, &r));
+        return (size_t)r;
+    }
+    template <typename U>
+    double cached_f(rfg_op op, const U& s2, double cutoff, double hint) const
+    {
+        double r = 0;
+        throw_on(rfg_cached_score_f64(h_, op, s2.data, s2.len, s2.width, cutoff, hint, &r));
+        return r;
+    }
+    rfg_metric metric_;
+    rfg_cached h_ = nullptr;
+};
+
+/* integer-valued metrics: distance/similarity as size_t, normalized as double */
+class CachedIntScorer : public CachedScorer {
+public:
+    template <typename Sentence2>
+    size_t distance(const Sentence2& s2, size_t score_cutoff = SIZE_MAX_default(), size_t score_hint = SIZE_MAX_default()) const
+    {
+        return cached_i(RFG_DISTANCE, units(s2), score_cutoff, score_hint);
+    }
+    template <typename InputIt2, rapidfuzz_gb300::detail::if_iter<InputIt2> = 0>
+    size_t distance(InputIt2 first2, InputIt2 last2, size_t score_cutoff = SIZE_MAX_default(),
+                    size_t score_hint = SIZE_MAX_default()) const
+    {
+        return cached_i(RFG_DISTANCE, units(first2, last2), score_cutoff, score_hint);
+    }
+    template <typename Sentence2>
+    size_t similarity(const Sentence2& s2, size_t score_cutoff = 0, size_t score_hint = 0) const
+    {
+        return cached_i(RFG_SIMILARITY, units(s2), score_cutoff, score_hint);
+    }
+    template <typename InputIt2, rapidfuzz_gb300::detail::if_iter<InputIt2> = 0>
+    size_t similarity(InputIt2 first2, InputIt2 last2, size_t score_cutoff = 0, size_t score_hint = 0) const
+    {
+        return cached_i(RFG_SIMILARITY, units(first2, last2), score_cutoff, score_hint);
+    }
+    template <typename Sentence2>
+    double normalized_distance(const Sentence2& s2, double score_cutoff = 1.0, double score_hint = 1.0) const
+    {
+        return cached_f(RFG_NORMALIZED_DISTANCE, units(s2), score_cutoff, score_hint);
+    }
+    template <typename Sentence2>
+    double normalized_similarity(const Sentence2& s2, double score_cutoff = 0.0, double score_hint = 0.0) const
+    {
+        return cached_f(RFG_NORMALIZED_SIMILARITY, units(s2), score_cutoff, score_hint);
+    }
+
+protected:
+    /* WorstDistance of the Cached* bases: INT64_MAX (Levenshtein.hpp:422-423) */
+    static constexpr size_t SIZE_MAX_default() { return (size_t)std::numeric_limits<int64_t>::max(); }
+    template <typename U>
+    CachedIntScorer(rfg_metric m, const U& s1, const rfg_params& p) : CachedScorer(m, s1, p)
+    {}
+};
+
+/* double-valued metrics (Jaro, Jaro-Winkler) */
+class CachedDblScorer : public CachedScorer {
+public:
+    template <typename Sentence2>
+    double distance(const Sentence2& s2, double score_cutoff = 1.0, double score_hint = 1.0) const
+    {
+        return cached_f(RFG_DISTANCE, units(s2), score_cutoff, score_hint);
+    }
+    template <typename Sentence2>
+    double similarity(const Sentence2& s2, double score_cutoff = 0.0, double score_hint = 0.0) const
+    {
+        return cached_f(RFG_SIMILARITY, units(s2), score_cutoff, score_hint);
+    }
+    template <typename InputIt2, rapidfuzz_gb300::detail::if_iter<InputIt2> = 0>
+    double similarity(InputIt2 first2, InputIt2 last2, double score_cutoff = 0.0, double score_hint = 0.0) const
+    {
+        return cached_f(RFG_SIMILARITY, units(first2, last2), score_cutoff, score_hint);
+    }
+    template <typename Sentence2>
+    double normalized_distance(const Sentence2& s2, double score_cutoff = 1.0, double score_hint = 1.0) const
+    {
+        return cached_f(RFG_NORMALIZED_DISTANCE, units(s2), score_cutoff, score_hint);
+    }
+    template <typename Sentence2>
+    double normalized_similarity(const Sentence2& s2, double score_cutoff = 0.0, double score_hint = 0.0) const
+    {
+        return cached_f(RFG_NORMALIZED_SIMILARITY, units(s2), score_cutoff, score_hint);
+    }
+
+protected:
+    template <typename U>
+    CachedDblScorer(rfg_metric m, const U& s1, const rfg_params& p) : CachedScorer(m, s1, p)
+    {}
+};
+
+} // namespace detail
+
+template <typename CharT1>
+struct CachedLevenshtein : detail::CachedIntScorer {
+    template <typename Sentence1>
+    explicit CachedLevenshtein(const Sentence1& s1, LevenshteinWeightTable w = {1, 1, 1})
+        : CachedIntScorer(RFG_LEVENSHTEIN, detail::units(s1), detail::lev_params(w))
+    {}
+    template <typename InputIt1, rapidfuzz_gb300::detail::if_iter<InputIt1> = 0>
+    CachedLevenshtein(InputIt1 first1, InputIt1 last1, LevenshteinWeightTable w = {1, 1, 1})
+        : CachedIntScorer(RFG_LEVENSHTEIN, detail::units(first1, last1), detail::lev_params(w))
+    {}
+};
+
+#define RFG_CACHED_INT(NAME, METRIC)                                                                           \
+    template <typename CharT1>                                                                                 \
+    struct NAME : detail::CachedIntScorer {                                                                    \
+        template <typename Sentence1>                                                                          \
+        explicit NAME(const Sentence1& s1) : CachedIntScorer(METRIC, detail::units(s1), rfg_params{1, 1, 1, 0.1}) \
+        {}                                                                                                     \
+        template <typename InputIt1, rapidfuzz_gb300::detail::if_iter<InputIt1> = 0>                           \
+        NAME(InputIt1 first1, InputIt1 last1)                                                                  \
+            : CachedIntScorer(METRIC, detail::units(first1, last1), rfg_params{1, 1, 1, 0.1})                  \
+        {}                                                                                                     \
+    };
+RFG_CACHED_INT(CachedIndel, RFG_INDEL)
+RFG_CACHED_INT(CachedLCSseq, RFG_LCSSEQ)
+RFG_CACHED_INT(CachedOSA, RFG_OSA)
+#undef RFG_CACHED_INT
+
+template <typename CharT1>
+struct CachedJaro : detail::CachedDblScorer {
+    template <typename Sentence1>
+    explicit CachedJaro(const Sentence1& s1) : CachedDblScorer(RFG_JARO, detail::units(s1), rfg_params{1, 1, 1, 0.1})
+    {}
+    template <typename InputIt1, rapidfuzz_gb300::detail::if_iter<InputIt1> = 0>
+    CachedJaro(InputIt1 first1, InputIt1 last1)
+        : CachedDblScorer(RFG_JARO, detail::units(first1, last1), rfg_params{1, 1, 1, 0.1})
+    {}
+};
+
+template <typename CharT1>
+struct CachedJaroWinkler : detail::CachedDblScorer {
+    template <typename Sentence1>
+    explicit CachedJaroWinkler(const Sentence1& s1, double prefix_weight = 0.1)
+        : CachedDblScorer(RFG_JARO_WINKLER, detail::units(s1), detail::jw_params(prefix_weight))
+    {}
+    template <typename InputIt1, rapidfuzz_gb300::detail::if_iter<InputIt1> = 0>
+    CachedJaroWinkler(InputIt1 first1, InputIt1 last1, double prefix_weight = 0.1)
+        : CachedDblScorer(RFG_JARO_WINKLER, detail::units(first1, last1), detail::jw_params(prefix_weight))
+    {}
+};
+
+#if __cplusplus >= 201703L
+/* C++17 deduction guides, as in the reference */
+template <typename Sentence1>
+explicit CachedLevenshtein(const Sentence1&, LevenshteinWeightTable = {1, 1, 1})
+    -> CachedLevenshtein<typename std::decay<decltype(*std::begin(std::declval<Sentence1>()))>::type>;
+template <typename Sentence1>
+explicit CachedIndel(const Sentence1&) -> CachedIndel<typename std::decay<decltype(*std::begin(std::declval<Sentence1>()))>::type>;
+template <typename Sentence1>
+explicit CachedLCSseq(const Sentence1&) -> CachedLCSseq<typename std::decay<decltype(*std::begin(std::declval<Sentence1>()))>::type>;
+template <typename Sentence1>
+explicit CachedOSA(const Sentence1&) -> CachedOSA<typename std::decay<decltype(*std::begin(std::declval<Sentence1>()))>::type>;
+template <typename Sentence1>
+explicit CachedJaro(const Sentence1&) -> CachedJaro<typename std::decay<decltype(*std::begin(std::declval<Sentence1>()))>::type>;
+template <typename Sentence1>
+explicit CachedJaroWinkler(const Sentence1&, double = 0.1)
+    -> CachedJaroWinkler<typename std::decay<decltype(*std::begin(std::declval<Sentence1>()))>::type>;
+#endif
+
+/* --------------------------------------------------------------------- fuzz */
+
+namespace fuzz {
+
+/* fuzz.hpp:44-48 */
+template <typename Sentence1, typename Sentence2>
+double ratio(const Sentence1& s1, const Sentence2& s2, double score_cutoff = 0)
+{
+    return detail::score_f(RFG_RATIO, RFG_SIMILARITY, detail::units(s1), detail::units(s2), rfg_params{1, 1, 1, 0.1},
+                           score_cutoff, score_cutoff);
+}
+template <typename InputIt1, typename InputIt2, detail::if_iter<InputIt1> = 0>
+double ratio(InputIt1 first1, InputIt1 last1, InputIt2 first2, InputIt2 last2, double score_cutoff = 0)
+{
+    return detail::score_f(RFG_RATIO, RFG_SIMILARITY, detail::units(first1, last1), detail::units(first2, last2),
+                           rfg_params{1, 1, 1, 0.1}, score_cutoff, score_cutoff);
+}
+
+/* fuzz.hpp:99-126 */
+template <typename CharT1>
+struct CachedRatio : rapidfuzz_gb300::detail::CachedScorer {
+    template <typename Sentence1>
+    CachedRatio(const Sentence1& s1)
+        : CachedScorer(RFG_RATIO, rapidfuzz_gb300::detail::units(s1), rfg_params{1, 1, 1, 0.1})
+    {}
+    template <typename InputIt1, rapidfuzz_gb300::detail::if_iter<InputIt1> = 0>
+    CachedRatio(InputIt1 first1, InputIt1 last1)
+        : CachedScorer(RFG_RATIO, rapidfuzz_gb300::detail::units(first1, last1), rfg_params{1, 1, 1, 0.1})
+    {}
+    template <typename Sentence2>
+    double similarity(const Sentence2& s2, double score_cutoff = 0.0, double score_hint = 0.0) const
+    {
+        return cached_f(RFG_SIMILARITY, rapidfuzz_gb300::detail::units(s2), score_cutoff, score_hint);
+    }
+    template <typename InputIt2, rapidfuzz_gb300::detail::if_iter<InputIt2> = 0>
+    double similarity(InputIt2 first2, InputIt2 last2, double score_cutoff = 0.0, double score_hint = 0.0) const
+    {
+        return cached_f(RFG_SIMILARITY, rapidfuzz_gb300::detail::units(first2, last2), score_cutoff, score_hint);
+    }
+};
+
+} // namespace fuzz
+
+/* ---------------------------------------------------------------- Multi* */
+
+namespace experimental {
+
+namespace detail_multi {
+
+template <rfg_metric M, int MaxLen, bool IntResult>
+class MultiScorer {
+public:
+    static_assert(MaxLen == 8 || MaxLen == 16 || MaxLen == 32 || MaxLen == 64, "expected MaxLen in 8/16/32/64");
+    MultiScorer(const MultiScorer&) = delete;
+    MultiScorer& operator=(const MultiScorer&) = delete;
+    ~MultiScorer()
+    {
+        if (h_) rfg_multi_destroy(h_);
+    }
+    size_t result_count() const
+    {
+        size_t n = 0;
+        rapidfuzz_gb300::detail::throw_on(rfg_multi_result_count(h_, &n));
+        return n;
+    }
+    template <typename Sentence1>
+    void insert(const Sentence1& s1)
+    {
+        auto u = rapidfuzz_gb300::detail::units(s1);
+        rapidfuzz_gb300::detail::throw_on(rfg_multi_insert(h_, u.data, u.len, u.width));
+    }
+    template <typename InputIt1, rapidfuzz_gb300::detail::if_iter<InputIt1> = 0>
+    void insert(InputIt1 first1, InputIt1 last1)
+    {
+        auto u = rapidfuzz_gb300::detail::units(first1, last1);
+        rapidfuzz_gb300::detail::throw_on(rfg_multi_insert(h_, u.data, u.len, u.width));
+    }
+
+protected:
+    MultiScorer(size_t count, const rfg_params& p)
+    {
+        rapidfuzz_gb300::detail::throw_on(rfg_multi_create(M, MaxLen, count, &p, &h_));
+    }
+    template <typename Sentence2>
+    void run_i(rfg_op op, size_t* scores, size_t n, const Sentence2& s2, size_t cutoff) const
+    {
+        static_assert(sizeof(size_t) == sizeof(int64_t), "64-bit size_t expected");
+        auto u = rapidfuzz_gb300::detail::units(s2);
+        rapidfuzz_gb300::detail::throw_on(
+            rfg_multi_score_i64(h_, op, reinterpret_cast<int64_t*>(scores), n, u.data, u.len, u.width, cutoff));
+    }
+    template <typename Sentence2>
+    void run_f(rfg_op op, double* scores, size_t n, const Sentence2& s2, double cutoff) const
+    {
+        auto u = rapidfuzz_gb300::detail::units(s2);
+        rapidfuzz_gb300::detail::throw_on(rfg_multi_score_f64(h_, op, scores, n, u.data, u.len, u.width, cutoff));
+    }
+    rfg_multi h_ = nullptr;
+};
+
+/* MultiDistanceBase / MultiSimilarityBase (distance.hpp:390-582) over size_t scores */
+template <rfg_metric M, int MaxLen>
+class MultiIntScorer : public MultiScorer<M, MaxLen, true> {
+public:
+    template <typename Sentence2>
+    void distance(size_t* scores, size_t score_count, const Sentence2& s2,
+                  size_t score_cutoff = (size_t)std::numeric_limits<int64_t>::max()) const
+    {
+        this->run_i(RFG_DISTANCE, scores, score_count, s2, score_cutoff);
+    }
+    template <typename Sentence2>
+    void similarity(size_t* scores, size_t score_count, const Sentence2& s2, size_t score_cutoff = 0) const
+    {
+        this->run_i(RFG_SIMILARITY, scores, score_count, s2, score_cutoff);
+    }
+    template <typename Sentence2>
+    void normalized_distance(double* scores, size_t score_count, const Sentence2& s2, double score_cutoff = 1.0) const
+    {
+        this->run_f(RFG_NORMALIZED_DISTANCE, scores, score_count, s2, score_cutoff);
+    }
+    template <typename Sentence2>
+    void normalized_similarity(double* scores, size_t score_count, const Sentence2& s2,
+                               double score_cutoff = 0.0) const
+    {
+        this->run_f(RFG_NORMALIZED_SIMILARITY, scores, score_count, s2, score_cutoff);
+    }
+
+protected:
+    MultiIntScorer(size_t count, const rfg_params& p) : MultiScorer<M, MaxLen, true>(count, p)
+    {}
+};
+
+template <rfg_metric M, int MaxLen>
+class MultiDblScorer : public MultiScorer<M, MaxLen, false> {
+public:
+    template <typename Sentence2>
+    void distance(double* scores, size_t score_count, const Sentence2& s2, double score_cutoff = 1.0) const
+    {
+        this->run_f(RFG_DISTANCE, scores, score_count, s2, score_cutoff);
+    }
+    template <typename Sentence2>
+    void similarity(double* scores, size_t score_count, const Sentence2& s2, double score_cutoff = 0.0) const
+    {
+        this->run_f(RFG_SIMILARITY, scores, score_count, s2, score_cutoff);
+    }
+    template <typename Sentence2>
+    void normalized_distance(double* scores, size_t score_count, const Sentence2& s2, double score_cutoff = 1.0) const
+    {
+        this->run_f(RFG_NORMALIZED_DISTANCE, scores, score_count, s2, score_cutoff);
+    }
+    template <typename Sentence2>
+    void normalized_similarity(double* scores, size_t score_count, const Sentence2& s2,
+                               double score_cutoff = 0.0) const
+    {
+        this->run_f(RFG_NORMALIZED_SIMILARITY, scores, score_count, s2, score_cutoff);
+    }
+
+protected:
+    MultiDblScorer(size_t count, const rfg_params& p) : MultiScorer<M, MaxLen, false>(count, p)
+    {}
+};
+
+} // namespace detail_multi
+
+template <int MaxLen>
+struct MultiLevenshtein : detail_multi::MultiIntScorer<RFG_LEVENSHTEIN, MaxLen> {
+    MultiLevenshtein(size_t count, LevenshteinWeightTable w = {1, 1, 1})
+        : detail_multi::MultiIntScorer<RFG_LEVENSHTEIN, MaxLen>(count, rapidfuzz_gb300::detail::lev_params(w))
+    {}
+};
+template <int MaxLen>
+struct MultiIndel : detail_multi::MultiIntScorer<RFG_INDEL, MaxLen> {
+    MultiIndel(size_t count) : detail_multi::MultiIntScorer<RFG_INDEL, MaxLen>(count, rfg_params{1, 1, 1, 0.1})
+    {}
+};
+template <int MaxLen>
+struct MultiLCSseq : detail_multi::MultiIntScorer<RFG_LCSSEQ, MaxLen> {
+    MultiLCSseq(size_t count) : detail_multi::MultiIntScorer<RFG_LCSSEQ, MaxLen>(count, rfg_params{1, 1, 1, 0.1})
+    {}
+};
+template <int MaxLen>
+struct MultiOSA : detail_multi::MultiIntScorer<RFG_OSA, MaxLen> {
+    MultiOSA(size_t count) : detail_multi::MultiIntScorer<RFG_OSA, MaxLen>(count, rfg_params{1, 1, 1, 0.1})
+    {}
+};
+template <int MaxLen>
+struct MultiJaro : detail_multi::MultiDblScorer<RFG_JARO, MaxLen> {
+    MultiJaro(size_t count) : detail_multi::MultiDblScorer<RFG_JARO, MaxLen>(count, rfg_params{1, 1, 1, 0.1})
+    {}
+};
+template <int MaxLen>
+struct MultiJaroWinkler : detail_multi::MultiDblScorer<RFG_JARO_WINKLER, MaxLen> {
+    MultiJaroWinkler(size_t count, double prefix_weight = 0.1)
+        : detail_multi::MultiDblScorer<RFG_JARO_WINKLER, MaxLen>(count, rapidfuzz_gb300::detail::jw_params(prefix_weight))
+    {}
+};
+
+} // namespace experimental
+
+namespace fuzz {
+namespace experimental {
+/* fuzz.hpp:50-95 */
+template <int MaxLen>
+struct MultiRatio : rapidfuzz_gb300::experimental::detail_multi::MultiScorer<RFG_RATIO, MaxLen, false> {
+    MultiRatio(size_t count)
+        : rapidfuzz_gb300::experimental::detail_multi::MultiScorer<RFG_RATIO, MaxLen, false>(count,
+                                                                                           rfg_params{1, 1, 1, 0.1})
+    {}
+    template <typename Sentence2>
+    void similarity(double* scores, size_t score_count, const Sentence2& s2, double score_cutoff = 0) const
+    {
+        this->run_f(RFG_SIMILARITY, scores, score_count, s2, score_cutoff);
+    }
+};
+} // namespace experimental
+} // namespace fuzz
+
+} // namespace rapidfuzz_gb300
