@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape (fixed launch list)")
     ap.add_argument("--nq", type=int, default=4096)
     ap.add_argument("--nc", type=int, default=4096)
+    ap.add_argument("--workload", default="cdist", choices=["cdist", "cfg1", "cfg3", "cfg4"],
+                    help="cdist: 4096x4096 Zipf a-z Lev/Indel/OSA (the headline); cfg1: 1 x 100k DNA per-call "
+                         "vs batched; cfg3: 256 x 65536 long DNA banded; cfg4: 1024 x 1M uint32 JW + ratio")
     return ap.parse_args()
 
 
@@ -183,6 +186,9 @@ def int_peak_ops():
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.workload != "cdist":
+        import bench_configs
+        return bench_configs.run(args, rank, world, local)
     if args.impl == "reference":
         return run_reference(args, rank, world)
 

@@ -1,0 +1,195 @@
+"""The other benchmark configurations of bench.py (--workload cfg1 | cfg3 | cfg4); each
+prints one JSON line like the headline workload.
+
+cfg1  Levenshtein (no cutoff), 1 query x 100,000 DNA choices len U[8,64], int64: the
+      batched launch (prepared batch, device-resident) against the plain per-call path
+      (rfg_cached_score_i64, one H2D + launch + D2H per choice, timed on a sample) and the
+      CPU port (Cached* loop, all host threads).
+cfg3  Levenshtein normalized_distance with score_cutoff 0.1 (cutoff = 10 % of the longer
+      string), 256 x 65,536 DNA strings, lengths log-normal(300, 0.6) in [100, 2000], each
+      choice unrelated or a query mutated at 1-15 %: multi-word and banded kernels.
+cfg4  Jaro-Winkler (prefix_weight 0.1, cutoff 0.85) and fuzz::ratio (cutoff 85) over uint32
+      code-point token strings, 1,024 x 1,000,000, dense float64 outputs kept on the device.
+"""
+import json
+import os
+import time
+
+import numpy as np
+
+import bench as B
+
+METRIC = B.METRIC_NAME
+
+
+def _timed_batches(torch, batches, stream, steps, warmup, flush):
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            for b in batches:
+                b.launch(stream.cuda_stream, graph=True)
+        for b in batches:
+            b.check(stream.cuda_stream)
+    torch.cuda.synchronize()
+    clocks = B.ClockSampler()
+    clocks.start()
+    time.sleep(0.3)
+    per = [0.0] * len(batches)
+    total = 0.0
+    with torch.cuda.stream(stream):
+        for _ in range(steps):
+            flush.zero_()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in batches]
+            for (e0, e1), b in zip(ev, batches):
+                e0.record(stream)
+                b.launch(stream.cuda_stream, graph=True)
+                e1.record(stream)
+            stream.synchronize()
+            for i, (e0, e1) in enumerate(ev):
+                per[i] += e0.elapsed_time(e1)
+            total += ev[0][0].elapsed_time(ev[-1][1])
+    torch.cuda.synchronize()
+    return total / 1e3, [p / steps for p in per], clocks.stop(torch.cuda.current_device())
+
+
+def _dev(torch, batch, dev):
+    d, o, w = batch
+    td = torch.from_numpy(np.ascontiguousarray(d)).to(dev)
+    to = torch.from_numpy(np.ascontiguousarray(o)).to(dev)
+    return (td.data_ptr(), to.data_ptr(), w, o.size - 1), (td, to)
+
+
+def _cells(q, c):
+    ql = np.diff(q[1]).astype(np.float64)
+    cl = np.diff(c[1]).astype(np.float64)
+    return float(ql.sum()) * float(cl.sum())
+
+
+def run(args, rank, world, local):
+    import torch
+    import rapidfuzz_gb300 as R
+    from rapidfuzz_gb300 import workloads as WL
+    from oracle_lib import oracle_cdist
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    steps, warmup = args.steps, args.warmup
+    line = {"metric": METRIC, "unit": "GCUPS", "n_gpus": 1, "steps": steps, "warmup": warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic (seeded)"}
+    if args.workload == "cfg1":
+        q = WL.dna_uniform(seed=11, n=1)
+        c = WL.dna_uniform(seed=12, n=100000)
+        nq, nc = 1, 100000
+        cells = _cells(q, c)
+        qd, kq = _dev(torch, q, dev)
+        cd, kc = _dev(torch, c, dev)
+        out = torch.empty((nq, nc), dtype=torch.int64, device=dev)
+        b = R.Batch(R.LEVENSHTEIN, R.DISTANCE, qd, cd, out.data_ptr(), None, out_dtype=R.I64, flags=R.DEVICE_INPUTS)
+        b.tune(stream.cuda_stream)
+        t, per, clk = _timed_batches(torch, [b], stream, steps, warmup, flush)
+        batched_pairs = nc * steps / t
+        exp = oracle_cdist(R.LEVENSHTEIN, R.DISTANCE, q, c)
+        assert np.array_equal(out.cpu().numpy(), exp), "cfg1 parity"
+        # plain per-call GPU path: one Cached* call per choice
+        qs = q[0][:q[1][1]]
+        sc = R.Cached(R.LEVENSHTEIN, qs)
+        strs = [c[0][c[1][i]:c[1][i + 1]] for i in range(2000)]
+        for s2 in strs[:50]:
+            sc.score(R.DISTANCE, s2)
+        t0 = time.perf_counter()
+        vals = [sc.score(R.DISTANCE, s2) for s2 in strs]
+        tp = time.perf_counter() - t0
+        assert vals == exp[0, :2000].tolist()
+        percall_pairs = len(strs) / tp
+        # e2e of the batched path from host buffers (Cached scorer over all choices)
+        for _ in range(2):
+            sc.score_many(R.DISTANCE, c)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            sc.score_many(R.DISTANCE, c)
+        te = time.perf_counter() - t0
+        tc0 = time.perf_counter()
+        oracle_cdist(R.LEVENSHTEIN, R.DISTANCE, q, c)
+        tc = time.perf_counter() - tc0
+        tc1 = time.perf_counter()
+        oracle_cdist(R.LEVENSHTEIN, R.DISTANCE, q, c, nthreads=1)
+        tc1 = time.perf_counter() - tc1
+        line.update({"value": cells * steps / t / 1e9, "ms_per_step": t / steps * 1e3, "dtype": "u64",
+                     "config": {"workload": "cfg1: Levenshtein, 1 query x 100,000 DNA len U[8,64], no cutoff, int64",
+                                "pairs_per_s_batched": batched_pairs, "pairs_per_s_per_call_gpu": percall_pairs,
+                                "batched_over_per_call": batched_pairs / percall_pairs,
+                                "per_call_us": tp / len(strs) * 1e6,
+                                "cpu_pairs_per_s_all_cores": nc / tc, "cpu_pairs_per_s_1_core": nc / tc1},
+                     "e2e": {"value": cells * steps / te / 1e9, "unit": "GCUPS",
+                             "h2d_bytes_per_step": int(c[0].nbytes + c[1].nbytes), "d2h_bytes_per_step": nc * 8,
+                             "pairs_per_s": nc * steps / te},
+                     "cpu_baseline": {"value": cells / tc / 1e9, "unit": "GCUPS", "cores": os.cpu_count(),
+                                      "kind": "port", "sample": "the full 1 x 100k workload"},
+                     "gpu_launches": steps, "clocks": clk})
+    elif args.workload == "cfg3":
+        q, c = WL.dna_lognormal(seed=13, nq=256, nc=65536)
+        nq, nc = 256, 65536
+        cells = _cells(q, c)
+        qd, kq = _dev(torch, q, dev)
+        cd, kc = _dev(torch, c, dev)
+        out = torch.empty((nq, nc), dtype=torch.float64, device=dev)
+        b = R.Batch(R.LEVENSHTEIN, R.NORMALIZED_DISTANCE, qd, cd, out.data_ptr(), 0.1, out_dtype=R.F64,
+                    flags=R.DEVICE_INPUTS)
+        b.tune(stream.cuda_stream)
+        t, per, clk = _timed_batches(torch, [b], stream, steps, warmup, flush)
+        rows = [0, 100, 255]
+        exp = oracle_cdist(R.LEVENSHTEIN, R.NORMALIZED_DISTANCE,
+                           (np.concatenate([q[0][q[1][r]:q[1][r + 1]] for r in rows]),
+                            np.concatenate([[0], np.cumsum([q[1][r + 1] - q[1][r] for r in rows])]).astype(np.int64),
+                            1), c, 0.1)
+        assert np.array_equal(out[rows].cpu().numpy().view(np.int64), exp.view(np.int64)), "cfg3 parity"
+        tc0 = time.perf_counter()
+        sub = 16
+        qsub = (q[0][:q[1][sub]], q[1][:sub + 1].copy(), 1)
+        oracle_cdist(R.LEVENSHTEIN, R.NORMALIZED_DISTANCE, qsub, c, 0.1)
+        tc = time.perf_counter() - tc0
+        line.update({"value": cells * steps / t / 1e9, "ms_per_step": t / steps * 1e3, "dtype": "u64",
+                     "config": {"workload": "cfg3: Levenshtein normalized_distance cutoff 0.1, 256 x 65,536 DNA "
+                                            "lognormal(300,0.6) in [100,2000], half mutated 1-15%",
+                                "pairs_per_s": nq * nc * steps / t},
+                     "cpu_baseline": {"value": _cells(qsub, c) / tc / 1e9, "unit": "GCUPS", "cores": os.cpu_count(),
+                                      "kind": "port", "sample": "16 of the 256 queries x all 65,536 choices"},
+                     "e2e": None, "gpu_launches": steps, "clocks": clk})
+    else:
+        (q, ql) = WL.tokens_u32(seed=14, n=1024)
+        (c, _) = WL.tokens_u32(seed=15, n=1000000, derive_from=ql, derive_frac=0.05)
+        nq, nc = 1024, 1000000
+        cells = _cells(q, c)
+        qd, kq = _dev(torch, q, dev)
+        cd, kc = _dev(torch, c, dev)
+        outs = [torch.empty((nq, nc), dtype=torch.float64, device=dev) for _ in range(2)]
+        bs = [R.Batch(R.JARO_WINKLER, R.SIMILARITY, qd, cd, outs[0].data_ptr(), 0.85, out_dtype=R.F64,
+                      flags=R.DEVICE_INPUTS),
+              R.Batch(R.RATIO, R.SIMILARITY, qd, cd, outs[1].data_ptr(), 85.0, out_dtype=R.F64,
+                      flags=R.DEVICE_INPUTS)]
+        for b in bs:
+            b.tune(stream.cuda_stream)
+        t, per, clk = _timed_batches(torch, bs, stream, steps, warmup, flush)
+        rows = [0, 511, 1023]
+        qrows = (np.concatenate([q[0][q[1][r]:q[1][r + 1]] for r in rows]),
+                 np.concatenate([[0], np.cumsum([q[1][r + 1] - q[1][r] for r in rows])]).astype(np.int64), 4)
+        for m, cut, o in ((R.JARO_WINKLER, 0.85, outs[0]), (R.RATIO, 85.0, outs[1])):
+            exp = oracle_cdist(m, R.SIMILARITY, qrows, c, cut)
+            assert np.array_equal(o[rows].cpu().numpy().view(np.int64), exp.view(np.int64)), "cfg4 parity"
+        tc0 = time.perf_counter()
+        sub = 4
+        qsub = (q[0][:q[1][sub]], q[1][:sub + 1].copy(), 4)
+        for m, cut in ((R.JARO_WINKLER, 0.85), (R.RATIO, 85.0)):
+            oracle_cdist(m, R.SIMILARITY, qsub, c, cut)
+        tc = time.perf_counter() - tc0
+        line.update({"value": 2 * cells * steps / t / 1e9, "ms_per_step": t / steps * 1e3, "dtype": "u64+f64",
+                     "config": {"workload": "cfg4: Jaro-Winkler 0.85 + fuzz::ratio 85, 1,024 x 1,000,000 uint32 "
+                                            "token strings, dense float64 out (on device)",
+                                "pairs_per_s": 2 * nq * nc * steps / t,
+                                "per_kernel_ms": {"jaro_winkler": per[0], "ratio": per[1]},
+                                "out_bytes_per_step": 2 * nq * nc * 8},
+                     "cpu_baseline": {"value": 2 * _cells(qsub, c) / tc / 1e9, "unit": "GCUPS",
+                                      "cores": os.cpu_count(), "kind": "port",
+                                      "sample": "4 of the 1,024 queries x all 1,000,000 choices"},
+                     "e2e": None, "gpu_launches": 2 * steps, "clocks": clk})
+    print(json.dumps(line), flush=True)

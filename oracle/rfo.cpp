@@ -26,6 +26,7 @@
 #include "rfo.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -1137,17 +1138,24 @@ int rfo_cdist(int metric, int op, const rfo_strings* q, const rfo_strings* c, co
     if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
     const bool is_int = result_is_int(metric, op);
     const i64 nq = q->count, nc = c->count;
-    /* queries are split across threads; each thread builds a query's pattern once
-     * and scores every choice with it (the Cached* loop of the reference) */
+    /* work items are (query, block of choices); each item builds the query's pattern
+     * once and scores the block with it (the Cached* loop of the reference) */
+    const i64 CB = 2048;
+    const i64 nblk = (nc + CB - 1) / CB;
+    const i64 items = nq * nblk;
     std::vector<int> errs(nthreads, 0);
+    std::atomic<i64> next(0);
     auto work = [&](int tid) {
-        for (i64 qi = tid; qi < nq; qi += nthreads) {
+        for (;;) {
+            const i64 it = next.fetch_add(1);
+            if (it >= items) break;
+            const i64 qi = it / nblk, b0 = (it % nblk) * CB, b1 = std::min(nc, b0 + CB);
             const char* qd = (const char*)q->data + q->offsets[qi] * q->char_width;
             i64 ql = q->offsets[qi + 1] - q->offsets[qi];
             int rc = with_strs(qd, ql, q->char_width, c->data, 0, c->char_width, [&](auto s1, auto s2base) -> int {
                 PM pm;
                 pm.build(s1);
-                for (i64 k = 0; k < nc; ++k) {
+                for (i64 k = b0; k < b1; ++k) {
                     decltype(s2base) s2{s2base.p + c->offsets[k], c->offsets[k + 1] - c->offsets[k]};
                     i64 vi = 0;
                     double vf = 0;
