@@ -172,6 +172,23 @@ rfg_status rfg_batch_destroy(rfg_batch batch);
 /* the library's own stream (the synchronous entry points run on it) */
 rfg_status rfg_get_stream(void** cuda_stream);
 
+/* ------------------------------------------------------------------ extract
+ * A corpus keeps a choice list on the device (with its length order precomputed) for
+ * repeated extract calls.  rfg_extract returns, per query, the best `limit` (1..32)
+ * choices whose score passes score_cutoff -- score >= cutoff for similarity ops,
+ * <= cutoff for distance ops -- best first: the README's extract/extractOne loops over
+ * a Cached* scorer (README.md:153-214).  Ties go to the lower choice index, or with
+ * tie_last_wins to the later one, as the README's extractOne (`score >= best_score`)
+ * does.  out_index/out_score hold count*limit entries (-1 / unspecified past
+ * out_count[q]); scores are doubles (integer results convert exactly).  Tiles publish
+ * their limit-th best so later tiles score under a tightened cutoff, the device form of
+ * extractOne passing its running best as score_cutoff. */
+rfg_status rfg_corpus_create(const rfg_strings* choices, uint32_t flags, rfg_corpus* corpus);
+rfg_status rfg_corpus_destroy(rfg_corpus corpus);
+rfg_status rfg_extract(rfg_corpus corpus, rfg_metric metric, rfg_op op, const rfg_strings* queries,
+                       const rfg_params* params, rfg_cutoff cutoff, int32_t limit, int32_t tie_last_wins,
+                       int64_t* out_index, double* out_score, int32_t* out_count, uint32_t flags);
+
 /* ------------------------------------------------------ no-allocation cdist
  * rfg_cdist_noalloc has no counterpart in the reference.  It is for callers that may
  * not allocate device memory (inside another framework's memory manager, in a process

@@ -92,12 +92,13 @@ rfg_status ensure_ctx()
 /* stream-ordered device allocation freed at scope exit */
 struct DBuf {
     void* p = nullptr;
+    cudaStream_t free_on = nullptr; /* stream of the last use (nullptr: the library stream) */
     DBuf() = default;
     DBuf(const DBuf&) = delete;
     DBuf& operator=(const DBuf&) = delete;
     ~DBuf()
     {
-        if (p) cudaFreeAsync(p, g.stream);
+        if (p) cudaFreeAsync(p, free_on ? free_on : g.stream);
     }
     rfg_status alloc(size_t bytes)
     {
@@ -247,7 +248,18 @@ struct BatchSpec {
     int out_dtype;
     void* out; /* device */
     int64_t ld;
+    /* extract epilogue (topk > 0): candidates per (query, chunk) instead of out */
+    int topk = 0;
+    int tie_last = 0;
+    u64* thr = nullptr;
+    u64* cand_key = nullptr;
+    int64_t* cand_idx = nullptr;
+    /* a corpus brings its own chunking and length order */
+    const int32_t* fixed_perm = nullptr;
+    int64_t fixed_chunk = 0;
 };
+
+inline bool better_high_of(int op) { return op == RFG_SIMILARITY || op == RFG_NORMALIZED_SIMILARITY; }
 
 int64_t g_tiles_target = 0; /* override of the tile-count target (autotuning) */
 int g_block_override = 0;   /* override of the tile kernels' block size (autotuning) */
@@ -269,6 +281,11 @@ struct Prepared {
     int* counters = nullptr;
     int* err = nullptr;
     int64_t scratch_words = 0;
+    int64_t chunk = 0, nchunks = 0;
+    void free_on(cudaStream_t st)
+    {
+        qlist.free_on = small.free_on = scratch[0].free_on = perm.free_on = st;
+    }
 };
 
 /* Host-side choice offsets (for the length order of each chunk): read from the device
@@ -362,18 +379,31 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
     RFG_CUDA(cudaMemcpyAsync(pb->qlist.p, qall.data(), qall.size() * 4, cudaMemcpyHostToDevice, g.stream));
 
     /* one chunking of the choices for every class, each chunk visited in length order */
-    const int64_t target_all = g_tiles_target > 0 ? g_tiles_target : (int64_t)g.sms * 32;
-    const int blk = g_block_override > 0 ? g_block_override : 256;
-    int64_t chunk = (nc * nq + target_all - 1) / target_all;
-    chunk = std::max<int64_t>(chunk, blk);
-    chunk = std::min<int64_t>(chunk, std::max<int64_t>(nc, 1));
-    chunk = (chunk + blk - 1) / blk * blk;
-    std::vector<int32_t> clen, perm;
-    RFG_TRY(choice_lengths(c, host_choice_off, &clen));
-    chunk_length_order(clen, chunk, &perm);
-    RFG_TRY(pb->perm.alloc((size_t)nc * 4));
-    RFG_CUDA(cudaMemcpyAsync(pb->perm.p, perm.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, g.stream));
-    RFG_CUDA(cudaStreamSynchronize(g.stream)); /* perm / qall are host temporaries */
+    int64_t chunk;
+    const int32_t* dperm;
+    if (spec.fixed_perm) {
+        chunk = spec.fixed_chunk;
+        dperm = spec.fixed_perm;
+        RFG_CUDA(cudaStreamSynchronize(g.stream)); /* qall is a host temporary */
+    }
+    else {
+        const int64_t target_all = g_tiles_target > 0 ? g_tiles_target : (int64_t)g.sms * 32;
+        const int blk = g_block_override > 0 ? g_block_override : 256;
+        chunk = (nc * nq + target_all - 1) / target_all;
+        chunk = std::max<int64_t>(chunk, blk);
+        chunk = std::min<int64_t>(chunk, std::max<int64_t>(nc, 1));
+        chunk = (chunk + blk - 1) / blk * blk;
+        std::vector<int32_t> clen, perm;
+        RFG_TRY(choice_lengths(c, host_choice_off, &clen));
+        chunk_length_order(clen, chunk, &perm);
+        RFG_TRY(pb->perm.alloc((size_t)nc * 4));
+        RFG_CUDA(cudaMemcpyAsync(pb->perm.p, perm.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, g.stream));
+        RFG_CUDA(cudaStreamSynchronize(g.stream)); /* perm / qall are host temporaries */
+        dperm = pb->perm.as<int32_t>();
+    }
+    pb->chunk = chunk;
+    pb->nchunks = (nc + chunk - 1) / chunk;
+    const bool topk = spec.topk > 0;
 
     for (int k = 0; k < 5; ++k) {
         if (cls[k].empty()) continue;
@@ -404,10 +434,10 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         if (k < 4) {
             const int W = 1 << k;
             switch (fam) {
-            case FAM_LEV: fn = tiles_kernel_lev(c.width, W); break;
-            case FAM_LCS: fn = tiles_kernel_lcs(c.width, W); break;
-            case FAM_OSA: fn = tiles_kernel_osa(c.width, W); break;
-            default: fn = tiles_kernel_jaro(c.width, W);
+            case FAM_LEV: fn = tiles_kernel_lev(c.width, W, topk); break;
+            case FAM_LCS: fn = tiles_kernel_lcs(c.width, W, topk); break;
+            case FAM_OSA: fn = tiles_kernel_osa(c.width, W, topk); break;
+            default: fn = tiles_kernel_jaro(c.width, W, topk);
             }
             block = g_block_override > 0 ? g_block_override : 256;
             smem = tiles_smem_bytes(W, a.hcap);
@@ -415,14 +445,20 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             per_sm = occupancy(fn, block, smem);
         }
         else {
-            fn = generic_kernel(fam == FAM_NONE ? FAM_WF : fam, c.width);
+            fn = generic_kernel(fam == FAM_NONE ? FAM_WF : fam, c.width, topk);
             block = 128;
             per_sm = 2;
         }
         /* tiles: (query, chunk), longest queries first; persistent CTAs fill every SM */
         const int64_t slots = (int64_t)g.sms * per_sm;
         a.chunk = chunk;
-        a.perm = pb->perm.as<int32_t>();
+        a.perm = dperm;
+        a.topk = spec.topk;
+        a.tie_last = spec.tie_last;
+        a.better_high = better_high_of(spec.op);
+        a.thr = spec.thr;
+        a.cand_key = spec.cand_key;
+        a.cand_idx = spec.cand_idx;
         a.nchunks = (nc + chunk - 1) / chunk;
         const int64_t ntiles = (int64_t)a.nq * a.nchunks;
         if (ntiles > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "batch too large for one launch");
@@ -608,6 +644,13 @@ struct rfg_batch_s {
         if (graph) cudaGraphExecDestroy(graph);
         delete pb;
     }
+};
+
+struct rfg_corpus_s {
+    DBuf data, off, perm;
+    KStrings dev{};
+    int64_t chunk = 0;
+    int64_t count = 0;
 };
 
 struct rfg_multi_s {
@@ -882,6 +925,176 @@ rfg_status rfg_multi_score_f64(rfg_multi h, rfg_op op, double* scores, size_t sc
     std::lock_guard<std::recursive_mutex> lk(g.mu);
     if (h && is_int_result(h->metric, op)) return fail(RFG_ERR_INVALID_ARGUMENT, "this metric/op returns integers");
     return multi_score(h, op, scores, score_count, s2, len2, width2, rfg_cutoff{0, score_cutoff, 0, 0.0}, RFG_F64);
+}
+
+/* ----------------------------------------------------------------- extract */
+
+namespace rfg {
+/* Device buffers of one in-flight extract (freed on its stream once it is done). */
+struct ExtractJob {
+    Prepared pb;
+    DBuf thr, ckey, cidx, oidx, oscore, ocount;
+    int64_t nq = 0;
+    int k = 0;
+    void free_on(cudaStream_t st)
+    {
+        pb.free_on(st);
+        thr.free_on = ckey.free_on = cidx.free_on = oidx.free_on = oscore.free_on = ocount.free_on = st;
+    }
+};
+
+/* Enqueue extract/extractOne of the queries against a corpus on stream st: the tile
+ * kernels keep each tile's best `k`, a merge kernel keeps each query's best `k`. */
+rfg_status extract_enqueue(rfg_corpus c, const QuerySet& q, int metric, int op, const ScoreParams& sp,
+                           rfg_cutoff cut, int k, int tie_last, cudaStream_t st, ExtractJob* job)
+{
+    const int64_t nq = q.dev.n;
+    job->nq = nq;
+    job->k = k;
+    if (nq == 0) return RFG_OK;
+    const int64_t nchunks = c->count ? (c->count + c->chunk - 1) / c->chunk : 0;
+    RFG_TRY(job->oidx.alloc((size_t)nq * k * 8));
+    RFG_TRY(job->oscore.alloc((size_t)nq * k * 8));
+    RFG_TRY(job->ocount.alloc((size_t)nq * 4));
+    RFG_CUDA(cudaMemsetAsync(job->oidx.p, 0xff, (size_t)nq * k * 8, g.stream));
+    RFG_CUDA(cudaMemsetAsync(job->ocount.p, 0, (size_t)nq * 4, g.stream));
+    if (nchunks == 0) return RFG_OK;
+    RFG_TRY(job->thr.alloc((size_t)nq * 8));
+    RFG_TRY(job->ckey.alloc((size_t)nq * nchunks * k * 8));
+    RFG_TRY(job->cidx.alloc((size_t)nq * nchunks * k * 8));
+    RFG_CUDA(cudaMemsetAsync(job->thr.p, 0, (size_t)nq * 8, g.stream));
+    BatchSpec spec;
+    spec.metric = metric;
+    spec.op = op;
+    spec.form = RFG_FORM_CACHED;
+    spec.sp = sp;
+    spec.ci = cut.cutoff_i;
+    spec.cf = cut.cutoff_f;
+    spec.out_dtype = RFG_F64;
+    spec.out = nullptr;
+    spec.ld = 0;
+    spec.topk = k;
+    spec.tie_last = tie_last;
+    spec.thr = job->thr.as<u64>();
+    spec.cand_key = job->ckey.as<u64>();
+    spec.cand_idx = job->cidx.as<int64_t>();
+    spec.fixed_perm = c->perm.as<int32_t>();
+    spec.fixed_chunk = c->chunk;
+    RFG_TRY(prepare_batch(q, c->dev, spec, &job->pb)); /* synchronises the library stream */
+    RFG_TRY(enqueue_batch(job->pb, st));
+    const int is_int = is_int_result(metric, op);
+    const int bh = better_high_of(op);
+    void* args[] = {&job->ckey.p, &job->cidx.p, (void*)&nchunks, &k, &tie_last, (void*)&bh, (void*)&is_int,
+                    &job->oidx.p, &job->oscore.p, &job->ocount.p};
+    RFG_CUDA(cudaLaunchKernel(topk_merge_kernel(), dim3((unsigned)nq), dim3(256), args, 0, st));
+    job->free_on(st);
+    return RFG_OK;
+}
+} // namespace rfg
+
+rfg_status rfg_corpus_create(const rfg_strings* C, uint32_t flags, rfg_corpus* out)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (!out) return fail(RFG_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    RFG_TRY(check_strings(C, "choices"));
+    RFG_TRY(ensure_ctx());
+    rfg_corpus c = new rfg_corpus_s();
+    const int64_t nc = C->count;
+    rfg_status st = RFG_OK;
+    std::vector<int64_t> hoff;
+    const int64_t* off = C->offsets;
+    if (flags & RFG_DEVICE_INPUTS) {
+        hoff.resize(nc + 1);
+        if (cudaMemcpy(hoff.data(), C->offsets, (nc + 1) * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = fail(RFG_ERR_CUDA, "reading choice offsets failed");
+        off = hoff.data();
+        /* the corpus keeps its own copy: callers may free theirs */
+        if (st == RFG_OK) st = c->data.alloc((size_t)off[nc] * C->char_width + 16);
+        if (st == RFG_OK) st = c->off.alloc((size_t)(nc + 1) * 8);
+        if (st == RFG_OK && off[nc])
+            if (cudaMemcpyAsync(c->data.p, C->data, (size_t)off[nc] * C->char_width, cudaMemcpyDeviceToDevice,
+                                g.stream) != cudaSuccess)
+                st = fail(RFG_ERR_CUDA, "copying the corpus failed");
+        if (st == RFG_OK &&
+            cudaMemcpyAsync(c->off.p, C->offsets, (nc + 1) * 8, cudaMemcpyDeviceToDevice, g.stream) != cudaSuccess)
+            st = fail(RFG_ERR_CUDA, "copying the corpus failed");
+        c->dev = KStrings{c->data.as<unsigned char>(), c->off.as<int64_t>(), nc, C->char_width};
+    }
+    else {
+        for (int64_t i = 0; i < nc && st == RFG_OK; ++i)
+            if (off[i] < 0 || off[i + 1] < off[i]) st = fail(RFG_ERR_INVALID_ARGUMENT, "offsets must be non-decreasing");
+        if (st == RFG_OK) st = upload_strings(C, &c->data, &c->off, &c->dev);
+    }
+    c->count = nc;
+    c->chunk = 4096;
+    if (st == RFG_OK && nc) {
+        std::vector<int32_t> len(nc), perm;
+        for (int64_t i = 0; i < nc; ++i) len[i] = (int32_t)std::min<int64_t>(off[i + 1] - off[i], INT32_MAX);
+        chunk_length_order(len, c->chunk, &perm);
+        st = c->perm.alloc((size_t)nc * 4);
+        if (st == RFG_OK &&
+            cudaMemcpyAsync(c->perm.p, perm.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, g.stream) != cudaSuccess)
+            st = fail(RFG_ERR_CUDA, "uploading the corpus order failed");
+        if (st == RFG_OK && cudaStreamSynchronize(g.stream) != cudaSuccess) st = fail(RFG_ERR_CUDA, "corpus upload failed");
+    }
+    if (st != RFG_OK) {
+        delete c;
+        return st;
+    }
+    *out = c;
+    return RFG_OK;
+}
+
+rfg_status rfg_corpus_destroy(rfg_corpus c)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (c) cudaDeviceSynchronize();
+    delete c;
+    return RFG_OK;
+}
+
+rfg_status rfg_extract(rfg_corpus c, rfg_metric metric, rfg_op op, const rfg_strings* Q, const rfg_params* p,
+                       rfg_cutoff cut, int32_t limit, int32_t tie_last_wins, int64_t* out_index, double* out_score,
+                       int32_t* out_count, uint32_t flags)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (!c) return fail(RFG_ERR_INVALID_ARGUMENT, "corpus is NULL");
+    RFG_TRY(check_metric_op(metric, op, RFG_FORM_CACHED));
+    RFG_TRY(check_strings(Q, "queries"));
+    if (limit < 1 || limit > RFG_MAX_TOPK) return fail(RFG_ERR_INVALID_ARGUMENT, "limit must be in [1, 32]");
+    if (!out_index || !out_score || !out_count) return fail(RFG_ERR_INVALID_ARGUMENT, "NULL output");
+    const ScoreParams sp = to_sp(p);
+    RFG_TRY(check_params(metric, sp));
+    RFG_TRY(ensure_ctx());
+    QuerySet qs;
+    DBuf qd, qo;
+    const int64_t nq = Q->count;
+    if (flags & RFG_DEVICE_INPUTS) {
+        std::vector<int64_t> off(nq + 1);
+        RFG_CUDA(cudaMemcpy(off.data(), Q->offsets, (nq + 1) * 8, cudaMemcpyDeviceToHost));
+        std::vector<unsigned char> qh;
+        if (Q->char_width > 1 && nq) {
+            qh.resize((size_t)off[nq] * Q->char_width);
+            RFG_CUDA(cudaMemcpy(qh.data(), Q->data, qh.size(), cudaMemcpyDeviceToHost));
+        }
+        RFG_TRY(query_info_from_host(qh.data(), off.data(), nq, Q->char_width, &qs));
+        qs.dev = KStrings{(const unsigned char*)Q->data, Q->offsets, nq, Q->char_width};
+    }
+    else {
+        RFG_TRY(query_info_from_host(Q->data, Q->offsets, nq, Q->char_width, &qs));
+        RFG_TRY(upload_strings(Q, &qd, &qo, &qs.dev));
+    }
+    ExtractJob job;
+    RFG_TRY(extract_enqueue(c, qs, metric, op, sp, cut, limit, tie_last_wins ? 1 : 0, g.stream, &job));
+    job.free_on(nullptr);
+    if (nq) {
+        const cudaMemcpyKind kind = (flags & RFG_DEVICE_OUTPUT) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        RFG_CUDA(cudaMemcpyAsync(out_index, job.oidx.p, (size_t)nq * limit * 8, kind, g.stream));
+        RFG_CUDA(cudaMemcpyAsync(out_score, job.oscore.p, (size_t)nq * limit * 8, kind, g.stream));
+        RFG_CUDA(cudaMemcpyAsync(out_count, job.ocount.p, (size_t)nq * 4, kind, g.stream));
+    }
+    return check_batch(job.pb, g.stream);
 }
 
 /* --------------------------------------------------------- prepared batches */

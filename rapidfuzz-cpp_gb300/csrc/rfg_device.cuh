@@ -44,6 +44,17 @@ struct KParams {
     int64_t ld;
     int hcap;      /* hash slots for code units >= 256 (power of two, or 0) */
     const int32_t* perm; /* choice order within each chunk (length-sorted), or nullptr */
+    /* extract epilogue (topk > 0): instead of a dense matrix, every (query, chunk) tile
+     * keeps its best topk results in cand_key/cand_idx[(q * nchunks + chunk) * topk + r];
+     * keys order results best-first: the score's bits for similarity ops, their
+     * complement for distance ops.  thr[q] is the running threshold key of query q
+     * (raised by every tile that fills its topk), used to tighten the cutoff. */
+    int topk;
+    int tie_last;    /* equal scores: the later choice wins (extractOne) instead of the earlier */
+    int better_high; /* 1: larger scores are better (similarity ops) */
+    u64* thr;
+    u64* cand_key;
+    int64_t* cand_idx;
     /* generic (scratch) kernels */
     u64* scratch;
     int64_t scratch_per_cta;    /* u64 words of the per-CTA pattern table region */
@@ -150,6 +161,145 @@ __device__ __forceinline__ bool result_is_int(int metric, int op)
     return op == DISTANCE || op == SIMILARITY;
 }
 
+/* ------------------------------------------------------- extract epilogue */
+
+#define RFG_MAX_TOPK 32
+
+/* per-thread list of the best results so far (extract kernels only) */
+template <bool TOPK>
+struct TopList {
+    int n;
+};
+template <>
+struct TopList<true> {
+    u64 key[RFG_MAX_TOPK];
+    int64_t idx[RFG_MAX_TOPK];
+    int n;
+};
+
+__device__ __forceinline__ bool cand_better(u64 ka, int64_t ia, u64 kb, int64_t ib, int tie_last)
+{
+    if (ia < 0) return false;
+    if (ib < 0) return true;
+    if (ka != kb) return ka > kb;
+    return tie_last ? ia > ib : ia < ib;
+}
+
+__device__ __forceinline__ void top_insert(TopList<true>& tl, int k, u64 key, int64_t idx, int tie_last)
+{
+    if (tl.n == k && !cand_better(key, idx, tl.key[k - 1], tl.idx[k - 1], tie_last)) return;
+    int pos = tl.n < k ? tl.n : k - 1;
+    while (pos > 0 && cand_better(key, idx, tl.key[pos - 1], tl.idx[pos - 1], tie_last)) {
+        tl.key[pos] = tl.key[pos - 1];
+        tl.idx[pos] = tl.idx[pos - 1];
+        --pos;
+    }
+    tl.key[pos] = key;
+    tl.idx[pos] = idx;
+    if (tl.n < k) ++tl.n;
+}
+
+__device__ __forceinline__ u64 score_key(bool is_int, i64 vi, double vf, int better_high)
+{
+    const u64 raw = is_int ? (u64)vi : (u64)__double_as_longlong(vf);
+    return better_high ? raw : ~raw;
+}
+
+/* the cutoff of one pair, tightened by the query's running threshold */
+__device__ __forceinline__ void tightened_cutoff(const KParams& a, int64_t qi, bool is_int, u64* ci, double* cf)
+{
+    *ci = a.ci;
+    *cf = a.cf;
+    if (a.topk <= 0 || !a.thr) return;
+    const u64 key = *(volatile const u64*)(a.thr + qi);
+    if (key == 0) return;
+    const u64 raw = a.better_high ? key : ~key;
+    if (is_int) *ci = a.better_high ? (raw > a.ci ? raw : a.ci) : (raw < a.ci ? raw : a.ci);
+    else {
+        const double v = __longlong_as_double((long long)raw);
+        *cf = a.better_high ? (v > a.cf ? v : a.cf) : (v < a.cf ? v : a.cf);
+    }
+}
+
+/* a result passes the (tightened) cutoff: the reference's extract keeps score >= cutoff
+ * for similarities and score <= cutoff for distances */
+__device__ __forceinline__ bool passes(bool is_int, int better_high, i64 vi, double vf, u64 ci, double cf)
+{
+    if (is_int) return better_high ? (u64)vi >= ci : (u64)vi <= ci;
+    return better_high ? vf >= cf : vf <= cf;
+}
+
+/* Block-wide selection of the tile's best results into the candidate arrays; all
+ * threads call it; tl is consumed. */
+static __device__ void flush_topk(const KParams& a, int64_t qi, int64_t ch, TopList<true>& tl)
+{
+    __shared__ u64 s_key[32];
+    __shared__ int64_t s_idx[32];
+    __shared__ int64_t s_win;
+    const int k = a.topk;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    int head = 0;
+    const int64_t base = (qi * a.nchunks + ch) * k;
+    u64 last_key = 0;
+    int filled = 0;
+    for (int r = 0; r < k; ++r) {
+        u64 bk = head < tl.n ? tl.key[head] : 0;
+        int64_t bi = head < tl.n ? tl.idx[head] : -1;
+        for (int o = 16; o > 0; o >>= 1) {
+            const u64 ok = __shfl_down_sync(0xffffffffu, bk, o);
+            const int64_t oi = __shfl_down_sync(0xffffffffu, bi, o);
+            if (cand_better(ok, oi, bk, bi, a.tie_last)) {
+                bk = ok;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            s_key[warp] = bk;
+            s_idx[warp] = bi;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            u64 wk = s_key[0];
+            int64_t wi = s_idx[0];
+            for (int w = 1; w < nw; ++w)
+                if (cand_better(s_key[w], s_idx[w], wk, wi, a.tie_last)) {
+                    wk = s_key[w];
+                    wi = s_idx[w];
+                }
+            a.cand_key[base + r] = wk;
+            a.cand_idx[base + r] = wi;
+            s_win = wi;
+            if (wi >= 0) {
+                last_key = wk;
+                ++filled;
+            }
+        }
+        __syncthreads();
+        const int64_t win = s_win;
+        if (win >= 0 && head < tl.n && tl.idx[head] == win) ++head;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && filled == k && a.thr) atomicMax((unsigned long long*)(a.thr + qi), last_key);
+    tl.n = 0;
+}
+
+/* dense store, or the extract list */
+__device__ __forceinline__ void emit(const KParams& a, int64_t qi, int64_t ci, i64 vi, double vf, bool is_int,
+                                     u64 cut_i, double cut_f, TopList<false>* tl)
+{
+    (void)cut_i;
+    (void)cut_f;
+    (void)tl;
+    store_result(a, qi, ci, vi, vf, is_int);
+}
+
+__device__ __forceinline__ void emit(const KParams& a, int64_t qi, int64_t ci, i64 vi, double vf, bool is_int,
+                                     u64 cut_i, double cut_f, TopList<true>* tl)
+{
+    if (passes(is_int, a.better_high, vi, vf, cut_i, cut_f))
+        top_insert(*tl, a.topk, score_key(is_int, vi, vf, a.better_high), ci, a.tie_last);
+}
+
 /* -------------------------------------------------------- integer families */
 
 template <int FAM, int W, typename PMF, typename TXT>
@@ -183,9 +333,9 @@ __device__ __forceinline__ i64 run_int_core(const PMF& pm, int m, const TXT& t, 
 }
 
 /* one (query, choice) pair of an integer-valued or Jaro family */
-template <int FAM, int W, typename CT>
+template <int FAM, int W, typename CT, bool TOPK>
 __device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, const u64* keys, int64_t qi, int m,
-                                           const u64* qpre, int64_t ci)
+                                           const u64* qpre, int64_t ci, TopList<TOPK>* tl)
 {
     const int64_t o0 = a.c.off[ci], o1 = a.c.off[ci + 1];
     const int n = (int)(o1 - o0);
@@ -196,8 +346,10 @@ __device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, co
     s.form = a.form;
     s.l1 = (u64)m;
     s.l2 = (u64)n;
+    const bool is_int = result_is_int(a.metric, a.op);
     s.ci = a.ci;
     s.cf = a.cf;
+    if (TOPK) tightened_cutoff(a, qi, is_int, &s.ci, &s.cf);
     s.p = a.sp;
     const PMRows<W> pm{rows};
     const TextRows<CT, (sizeof(CT) > 1)> txt{s2, keys, a.hcap};
@@ -222,19 +374,19 @@ __device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, co
             }
         }
         vf = finish_jaro(s, prefix, common, transp);
-        store_result(a, qi, ci, 0, vf, false);
+        emit(a, qi, ci, 0, vf, false, s.ci, s.cf, tl);
         return;
     }
     const Plan pl = plan_int(s);
     i64 raw = 0;
     if (pl.run) raw = run_int_core<FAM, W>(pm, m, txt, n, pl.K);
     finish_int(s, pl, raw, &vi, &vf);
-    store_result(a, qi, ci, vi, vf, result_is_int(a.metric, a.op));
+    emit(a, qi, ci, vi, vf, is_int, s.ci, s.cf, tl);
 }
 
 /* -------------------------------------------------------------- the kernel */
 
-template <int FAM, typename CT, int W>
+template <int FAM, typename CT, int W, bool TOPK = false>
 __global__ void __launch_bounds__(256) k_tiles(const KParams a)
 {
     extern __shared__ u64 smem[];
@@ -245,6 +397,8 @@ __global__ void __launch_bounds__(256) k_tiles(const KParams a)
     __shared__ u64 s_qpre[4];
     int64_t cur_q = -1;
     int m = 0;
+    TopList<TOPK> tl;
+    tl.n = 0;
     const int64_t ntiles = (int64_t)a.nq * a.nchunks;
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(a.counter, 1);
@@ -272,7 +426,8 @@ __global__ void __launch_bounds__(256) k_tiles(const KParams a)
          * pairs of similar work and pairs decided by the length filter cluster into
          * whole warps */
         for (int64_t p = c0 + threadIdx.x; p < c1; p += blockDim.x)
-            score_pair<FAM, W, CT>(a, rows, keys, qi, m, s_qpre, a.perm ? (int64_t)__ldg(a.perm + p) : p);
+            score_pair<FAM, W, CT, TOPK>(a, rows, keys, qi, m, s_qpre, a.perm ? (int64_t)__ldg(a.perm + p) : p, &tl);
+        if constexpr (TOPK) flush_topk(a, qi, ch, tl);
         __syncthreads();
     }
 }
@@ -332,9 +487,10 @@ __device__ inline void build_pm_rt(u64* rows, u64* keys, int hcap, int W, const 
     __syncthreads();
 }
 
-template <int FAM, typename CT>
+template <int FAM, typename CT, bool TOPK = false>
 __device__ __forceinline__ void score_pair_generic(const KParams& a, const u64* rows, const u64* keys, int W,
-                                                   int64_t qi, int m, const unsigned char* qb, int64_t ci, u64* st)
+                                                   int64_t qi, int m, const unsigned char* qb, int64_t ci, u64* st,
+                                                   TopList<TOPK>* tl = nullptr)
 {
     const int64_t o0 = a.c.off[ci], o1 = a.c.off[ci + 1];
     const int n = (int)(o1 - o0);
@@ -345,8 +501,10 @@ __device__ __forceinline__ void score_pair_generic(const KParams& a, const u64* 
     s.form = a.form;
     s.l1 = (u64)m;
     s.l2 = (u64)n;
+    const bool is_int = result_is_int(a.metric, a.op);
     s.ci = a.ci;
     s.cf = a.cf;
+    if (TOPK) tightened_cutoff(a, qi, is_int, &s.ci, &s.cf);
     s.p = a.sp;
     const PMRowsRT pm{rows, W};
     const TextRows<CT, (sizeof(CT) > 1)> txt{s2, keys, a.hcap};
@@ -362,7 +520,7 @@ __device__ __forceinline__ void score_pair_generic(const KParams& a, const u64* 
         if (m > 0 && n > 0 && jaro_pair_needs_counts(s, prefix))
             jaro_multi_rt(pm, W, m, txt, n, &common, &transp, st, st + W);
         vf = finish_jaro(s, prefix, common, transp);
-        store_result(a, qi, ci, 0, vf, false);
+        emit(a, qi, ci, 0, vf, false, s.ci, s.cf, tl);
         return;
     }
     const Plan pl = plan_int(s);
@@ -387,10 +545,10 @@ __device__ __forceinline__ void score_pair_generic(const KParams& a, const u64* 
         else raw = lev_multi_rt(pm, W, m, txt, n, K, st, st + W);
     }
     finish_int(s, pl, raw, &vi, &vf);
-    store_result(a, qi, ci, vi, vf, result_is_int(a.metric, a.op));
+    emit(a, qi, ci, vi, vf, is_int, s.ci, s.cf, tl);
 }
 
-template <int FAM, typename CT>
+template <int FAM, typename CT, bool TOPK = false>
 __global__ void __launch_bounds__(128) k_generic(const KParams a)
 {
     const int W = a.wmax;
@@ -402,6 +560,8 @@ __global__ void __launch_bounds__(128) k_generic(const KParams a)
     int64_t cur_q = -1;
     int m = 0;
     const unsigned char* qb = nullptr;
+    TopList<TOPK> tl;
+    tl.n = 0;
     const int64_t ntiles = (int64_t)a.nq * a.nchunks;
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(a.counter, 1);
@@ -426,9 +586,76 @@ __global__ void __launch_bounds__(128) k_generic(const KParams a)
         const int64_t c0 = ch * a.chunk;
         const int64_t c1 = c0 + a.chunk < a.c.n ? c0 + a.chunk : a.c.n;
         for (int64_t p = c0 + threadIdx.x; p < c1; p += blockDim.x)
-            score_pair_generic<FAM, CT>(a, rows, keys, W, qi, m, qb, a.perm ? (int64_t)__ldg(a.perm + p) : p, st);
+            score_pair_generic<FAM, CT, TOPK>(a, rows, keys, W, qi, m, qb, a.perm ? (int64_t)__ldg(a.perm + p) : p,
+                                              st, &tl);
+        if constexpr (TOPK) flush_topk(a, qi, ch, tl);
         __syncthreads();
     }
+}
+
+/* Per query: the best topk of all its tiles' candidates, best first; scores as doubles
+ * (integer results convert exactly).  One CTA per query. */
+static __global__ void __launch_bounds__(256) k_topk_merge(const u64* cand_key, const int64_t* cand_idx, int64_t nchunks,
+                                                     int k, int tie_last, int better_high, int is_int,
+                                                     int64_t* out_idx, double* out_score, int32_t* out_count)
+{
+    __shared__ u64 s_key[32];
+    __shared__ int64_t s_idx[32];
+    __shared__ int64_t s_win;
+    __shared__ u64 s_wkey;
+    const int64_t q = blockIdx.x;
+    const int64_t n = nchunks * k;
+    const u64* ck = cand_key + q * n;
+    const int64_t* ci = cand_idx + q * n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    int count = 0;
+    for (int r = 0; r < k; ++r) {
+        u64 bk = 0;
+        int64_t bi = -1;
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
+            if (cand_better(ck[i], ci[i], bk, bi, tie_last)) {
+                bk = ck[i];
+                bi = ci[i];
+            }
+        for (int o = 16; o > 0; o >>= 1) {
+            const u64 ok = __shfl_down_sync(0xffffffffu, bk, o);
+            const int64_t oi = __shfl_down_sync(0xffffffffu, bi, o);
+            if (cand_better(ok, oi, bk, bi, tie_last)) {
+                bk = ok;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            s_key[warp] = bk;
+            s_idx[warp] = bi;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            u64 wk = s_key[0];
+            int64_t wi = s_idx[0];
+            for (int w = 1; w < nw; ++w)
+                if (cand_better(s_key[w], s_idx[w], wk, wi, tie_last)) {
+                    wk = s_key[w];
+                    wi = s_idx[w];
+                }
+            s_win = wi;
+            s_wkey = wk;
+        }
+        __syncthreads();
+        const int64_t win = s_win;
+        if (win < 0) break;
+        /* remove the winner (its choice index is unique within the query) */
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
+            if (ci[i] == win) ((int64_t*)ci)[i] = -1;
+        if (threadIdx.x == 0) {
+            const u64 raw = better_high ? s_wkey : ~s_wkey;
+            out_idx[q * k + r] = win;
+            out_score[q * k + r] = is_int ? (double)(int64_t)raw : __longlong_as_double((long long)raw);
+        }
+        ++count;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out_count[q] = count;
 }
 
 /* shared memory of k_tiles<.., W> */

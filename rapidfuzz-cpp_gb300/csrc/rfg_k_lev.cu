@@ -5,24 +5,24 @@
 namespace rfg {
 
 template <typename CT>
-static const void* pick_lev(int W)
+static const void* pick_lev(int W, bool topk)
 {
     switch (W) {
-    case 1: return (const void*)&k_tiles<FAM_LEV, CT, 1>;
-    case 2: return (const void*)&k_tiles<FAM_LEV, CT, 2>;
-    case 4: return (const void*)&k_tiles<FAM_LEV, CT, 4>;
-    case 8: return (const void*)&k_tiles<FAM_LEV, CT, 8>;
+    case 1: return topk ? (const void*)&k_tiles<FAM_LEV, CT, 1, true> : (const void*)&k_tiles<FAM_LEV, CT, 1>;
+    case 2: return topk ? (const void*)&k_tiles<FAM_LEV, CT, 2, true> : (const void*)&k_tiles<FAM_LEV, CT, 2>;
+    case 4: return topk ? (const void*)&k_tiles<FAM_LEV, CT, 4, true> : (const void*)&k_tiles<FAM_LEV, CT, 4>;
+    case 8: return topk ? (const void*)&k_tiles<FAM_LEV, CT, 8, true> : (const void*)&k_tiles<FAM_LEV, CT, 8>;
     }
     return nullptr;
 }
 
-const void* tiles_kernel_lev(int width, int W)
+const void* tiles_kernel_lev(int width, int W, bool topk)
 {
     switch (width) {
-    case 1: return pick_lev<uint8_t>(W);
-    case 2: return pick_lev<uint16_t>(W);
-    case 4: return pick_lev<uint32_t>(W);
-    case 8: return pick_lev<unsigned long long>(W);
+    case 1: return pick_lev<uint8_t>(W, topk);
+    case 2: return pick_lev<uint16_t>(W, topk);
+    case 4: return pick_lev<uint32_t>(W, topk);
+    case 8: return pick_lev<unsigned long long>(W, topk);
     }
     return nullptr;
 }

@@ -4,11 +4,13 @@
 #include <stdint.h>
 
 namespace rfg {
-/* k_tiles<FAM, CT, W>: width in {1,2,4,8}, W in {1,2,4,8}; nullptr when absent */
-const void* tiles_kernel_lev(int width, int W);
-const void* tiles_kernel_lcs(int width, int W);
-const void* tiles_kernel_osa(int width, int W);
-const void* tiles_kernel_jaro(int width, int W);
-/* k_generic<FAM, CT> */
-const void* generic_kernel(int fam, int width);
+/* k_tiles<FAM, CT, W, TOPK>: width in {1,2,4,8}, W in {1,2,4,8}; nullptr when absent */
+const void* tiles_kernel_lev(int width, int W, bool topk);
+const void* tiles_kernel_lcs(int width, int W, bool topk);
+const void* tiles_kernel_osa(int width, int W, bool topk);
+const void* tiles_kernel_jaro(int width, int W, bool topk);
+/* k_generic<FAM, CT, TOPK> */
+const void* generic_kernel(int fam, int width, bool topk);
+/* k_topk_merge */
+const void* topk_merge_kernel();
 } // namespace rfg

@@ -84,6 +84,10 @@ def lib():
             "rfg_batch_tune": ([vp, vp, P(i32), P(i64)], ctypes.c_int),
             "rfg_batch_destroy": ([vp], ctypes.c_int),
             "rfg_get_stream": ([P(vp)], ctypes.c_int),
+            "rfg_corpus_create": ([P(Strings), ctypes.c_uint32, P(vp)], ctypes.c_int),
+            "rfg_corpus_destroy": ([vp], ctypes.c_int),
+            "rfg_extract": ([vp, ctypes.c_int, ctypes.c_int, P(Strings), P(Params), Cutoff, i32, i32, vp, vp, vp,
+                             ctypes.c_uint32], ctypes.c_int),
             "rfg_cdist_noalloc": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, P(Strings), P(Strings), i64, P(Params),
                                    Cutoff, ctypes.c_int, vp, i64, vp], ctypes.c_int),
         }
@@ -328,3 +332,37 @@ def library_stream():
     s = ctypes.c_void_p()
     check(lib().rfg_get_stream(ctypes.byref(s)))
     return s.value or 0
+
+
+class Corpus:
+    """A device-resident choice list for repeated extract calls (rfg_corpus_*)."""
+
+    def __init__(self, choices, flags=0):
+        self._h = ctypes.c_void_p()
+        self._b = _batch(choices)
+        self.count = self._b.count
+        check(lib().rfg_corpus_create(ctypes.byref(self._b), flags, ctypes.byref(self._h)))
+
+    def extract(self, metric, op, queries, limit=5, score_cutoff=None, tie_last=False, weights=(1, 1, 1),
+                prefix_weight=0.1):
+        """-> (index int64 [nq, limit], score float64 [nq, limit], count int32 [nq]), best first"""
+        q = _batch(queries)
+        is_int = result_is_int(metric, op)
+        c = _default_cutoff(metric, op) if score_cutoff is None else score_cutoff
+        cut = Cutoff(int(c) if is_int else 0, 0.0 if is_int else float(c), 0, 0.0)
+        idx = np.full((q.count, limit), -1, dtype=np.int64)
+        sc = np.zeros((q.count, limit), dtype=np.float64)
+        cnt = np.zeros(q.count, dtype=np.int32)
+        p = make_params(weights, prefix_weight)
+        check(lib().rfg_extract(self._h, metric, op, ctypes.byref(q), ctypes.byref(p), cut, limit, int(tie_last),
+                                idx.ctypes.data, sc.ctypes.data, cnt.ctypes.data, 0))
+        return idx, sc, cnt
+
+    def close(self):
+        if self._h and self._h.value:
+            lib().rfg_corpus_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        if _lib is not None:
+            self.close()
