@@ -189,6 +189,45 @@ rfg_status rfg_extract(rfg_corpus corpus, rfg_metric metric, rfg_op op, const rf
                        const rfg_params* params, rfg_cutoff cutoff, int32_t limit, int32_t tie_last_wins,
                        int64_t* out_index, double* out_score, int32_t* out_count, uint32_t flags);
 
+/* ------------------------------------------------------------------ serving
+ * A continuous-batching extract service over device-resident corpora (no reference
+ * counterpart; the serving form of the README's extract loops, README.md:153-214).
+ * submit() queues a request and returns at once; a loop thread groups queued requests
+ * with the same spec (corpus, metric, op, params, cutoff, limit, tie rule, width) into
+ * batches of up to max_batch and admits a batch whenever one of max_inflight stream
+ * slots is free and its device-memory estimate fits max_device_bytes (0: 80 % of the
+ * free device memory at create); batches run concurrently.  wait() blocks until the
+ * request's result is in its out_* buffers (limit entries; out_count set) and reports
+ * the submit-to-completion latency.  Results equal rfg_extract of the request alone. */
+typedef struct {
+    int32_t max_inflight;
+    int32_t max_batch;
+    int64_t max_device_bytes;
+} rfg_server_config;
+
+typedef struct {
+    int32_t corpus; /* index into the server's corpora */
+    rfg_metric metric;
+    rfg_op op;
+    rfg_params params;
+    rfg_cutoff cutoff;
+    int32_t limit;          /* 1..32: 1 with tie_last_wins = extractOne */
+    int32_t tie_last_wins;
+    const void* query;      /* copied at submit */
+    int64_t query_len;
+    int32_t query_width;
+    int64_t* out_index;     /* caller buffers, filled on completion */
+    double* out_score;
+    int32_t* out_count;
+} rfg_request;
+
+rfg_status rfg_server_create(const rfg_corpus* corpora, int32_t ncorpora, const rfg_server_config* config,
+                             rfg_server* server);
+rfg_status rfg_server_submit(rfg_server server, const rfg_request* request, uint64_t* ticket);
+rfg_status rfg_server_wait(rfg_server server, uint64_t ticket, double timeout_s, double* latency_ms);
+rfg_status rfg_server_stats(rfg_server server, int64_t* completed, int64_t* batches, int64_t* batched_requests);
+rfg_status rfg_server_destroy(rfg_server server);
+
 /* ------------------------------------------------------ no-allocation cdist
  * rfg_cdist_noalloc has no counterpart in the reference.  It is for callers that may
  * not allocate device memory (inside another framework's memory manager, in a process

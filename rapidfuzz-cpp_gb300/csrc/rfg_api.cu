@@ -929,6 +929,8 @@ rfg_status rfg_multi_score_f64(rfg_multi h, rfg_op op, double* scores, size_t sc
 
 /* ----------------------------------------------------------------- extract */
 
+} /* extern "C" */
+
 namespace rfg {
 /* Device buffers of one in-flight extract (freed on its stream once it is done). */
 struct ExtractJob {
@@ -991,6 +993,55 @@ rfg_status extract_enqueue(rfg_corpus c, const QuerySet& q, int metric, int op, 
     return RFG_OK;
 }
 } // namespace rfg
+
+namespace rfg {
+/* the serving loop's view of extract (rfg_server.cu) */
+struct ServerJob {
+    ExtractJob ej;
+    DBuf qd, qo;
+    QuerySet qs;
+};
+
+int64_t corpus_chunks(rfg_corpus c) { return c->count ? (c->count + c->chunk - 1) / c->chunk : 0; }
+
+rfg_status server_extract_enqueue(rfg_corpus c, const unsigned char* qdata, const int64_t* qoff, int64_t nq,
+                                  int width, int metric, int op, const rfg_params* p, rfg_cutoff cut, int k,
+                                  int tie_last, cudaStream_t st, void** job, int64_t* est_bytes)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    RFG_TRY(ensure_ctx());
+    ServerJob* j = new ServerJob();
+    *job = j;
+    *est_bytes = 0;
+    rfg_strings q{qdata, qoff, nq, width};
+    RFG_TRY(query_info_from_host(qdata, qoff, nq, width, &j->qs));
+    RFG_TRY(upload_strings(&q, &j->qd, &j->qo, &j->qs.dev));
+    const ScoreParams sp = to_sp(p);
+    RFG_TRY(check_params(metric, sp));
+    RFG_TRY(extract_enqueue(c, j->qs, metric, op, sp, cut, k, tie_last, st, &j->ej));
+    j->qd.free_on = j->qo.free_on = st;
+    return RFG_OK;
+}
+
+rfg_status server_extract_results(void* job, int64_t* idx, double* score, int32_t* count, cudaStream_t st)
+{
+    ServerJob* j = (ServerJob*)job;
+    const int64_t nq = j->ej.nq, k = j->ej.k;
+    if (!nq) return RFG_OK;
+    RFG_CUDA(cudaMemcpyAsync(idx, j->ej.oidx.p, (size_t)nq * k * 8, cudaMemcpyDeviceToHost, st));
+    RFG_CUDA(cudaMemcpyAsync(score, j->ej.oscore.p, (size_t)nq * k * 8, cudaMemcpyDeviceToHost, st));
+    RFG_CUDA(cudaMemcpyAsync(count, j->ej.ocount.p, (size_t)nq * 4, cudaMemcpyDeviceToHost, st));
+    return RFG_OK;
+}
+
+void server_extract_free(void* job)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    delete (ServerJob*)job;
+}
+} // namespace rfg
+
+extern "C" {
 
 rfg_status rfg_corpus_create(const rfg_strings* C, uint32_t flags, rfg_corpus* out)
 {

@@ -405,8 +405,10 @@ __global__ void __launch_bounds__(256) k_tiles(const KParams a)
         __syncthreads();
         const int64_t t = s_tile;
         if (t >= ntiles) break;
-        const int64_t qi = a.qlist[t / a.nchunks];
-        const int64_t ch = t % a.nchunks;
+        /* extract batches sweep the corpus chunk-major (every query of the batch scores a
+         * chunk while it is in L2); dense batches go query-major (coalesced rows) */
+        const int64_t qi = TOPK ? a.qlist[t % a.nq] : a.qlist[t / a.nchunks];
+        const int64_t ch = TOPK ? t / a.nq : t % a.nchunks;
         if (qi != cur_q) {
             const int64_t q0 = a.q.off[qi];
             m = (int)(a.q.off[qi + 1] - q0);
@@ -568,8 +570,8 @@ __global__ void __launch_bounds__(128) k_generic(const KParams a)
         __syncthreads();
         const int64_t t = s_tile;
         if (t >= ntiles) break;
-        const int64_t qi = a.qlist[t / a.nchunks];
-        const int64_t ch = t % a.nchunks;
+        const int64_t qi = TOPK ? a.qlist[t % a.nq] : a.qlist[t / a.nchunks];
+        const int64_t ch = TOPK ? t / a.nq : t % a.nchunks;
         if (qi != cur_q) {
             const int64_t q0 = a.q.off[qi];
             m = (int)(a.q.off[qi + 1] - q0);

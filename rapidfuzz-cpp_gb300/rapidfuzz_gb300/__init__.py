@@ -9,5 +9,5 @@ from ._lib import (DISTANCE, SIMILARITY, NORMALIZED_DISTANCE, NORMALIZED_SIMILAR
                    LEVENSHTEIN, INDEL, LCSSEQ, OSA, JARO, JARO_WINKLER, RATIO,
                    FORM_FREE, FORM_CACHED, FORM_MULTI, I32, I64, F64,
                    DEVICE_INPUTS, DEVICE_OUTPUT, RapidfuzzError, lib, lib_path,
-                   as_units, pack_strings, score, Cached, Multi, cdist, Batch, library_stream, Corpus)
+                   as_units, pack_strings, score, Cached, Multi, cdist, Batch, library_stream, Corpus, Server)
 from ._api import *  # noqa: F401,F403

@@ -42,6 +42,17 @@ class Strings(ctypes.Structure):
                 ("count", ctypes.c_int64), ("char_width", ctypes.c_int32)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("max_inflight", ctypes.c_int32), ("max_batch", ctypes.c_int32), ("max_device_bytes", ctypes.c_int64)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("corpus", ctypes.c_int32), ("metric", ctypes.c_int), ("op", ctypes.c_int), ("params", Params),
+                ("cutoff", Cutoff), ("limit", ctypes.c_int32), ("tie_last_wins", ctypes.c_int32),
+                ("query", ctypes.c_void_p), ("query_len", ctypes.c_int64), ("query_width", ctypes.c_int32),
+                ("out_index", ctypes.c_void_p), ("out_score", ctypes.c_void_p), ("out_count", ctypes.c_void_p)]
+
+
 _lib = None
 
 
@@ -88,6 +99,11 @@ def lib():
             "rfg_corpus_destroy": ([vp], ctypes.c_int),
             "rfg_extract": ([vp, ctypes.c_int, ctypes.c_int, P(Strings), P(Params), Cutoff, i32, i32, vp, vp, vp,
                              ctypes.c_uint32], ctypes.c_int),
+            "rfg_server_create": ([P(vp), i32, P(ServerConfig), P(vp)], ctypes.c_int),
+            "rfg_server_submit": ([vp, P(Request), P(ctypes.c_uint64)], ctypes.c_int),
+            "rfg_server_wait": ([vp, ctypes.c_uint64, ctypes.c_double, P(ctypes.c_double)], ctypes.c_int),
+            "rfg_server_stats": ([vp, P(i64), P(i64), P(i64)], ctypes.c_int),
+            "rfg_server_destroy": ([vp], ctypes.c_int),
             "rfg_cdist_noalloc": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, P(Strings), P(Strings), i64, P(Params),
                                    Cutoff, ctypes.c_int, vp, i64, vp], ctypes.c_int),
         }
@@ -361,6 +377,56 @@ class Corpus:
     def close(self):
         if self._h and self._h.value:
             lib().rfg_corpus_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        if _lib is not None:
+            self.close()
+
+
+class Server:
+    """Continuous-batching extract service (rfg_server_*)."""
+
+    def __init__(self, corpora, max_inflight=4, max_batch=64, max_device_bytes=0):
+        self._corpora = list(corpora)
+        arr = (ctypes.c_void_p * len(self._corpora))(*[c._h.value for c in self._corpora])
+        cfg = ServerConfig(max_inflight, max_batch, max_device_bytes)
+        self._h = ctypes.c_void_p()
+        check(lib().rfg_server_create(arr, len(self._corpora), ctypes.byref(cfg), ctypes.byref(self._h)))
+        self._pending = {}
+
+    def submit(self, corpus, metric, op, query, limit=1, score_cutoff=None, tie_last=None, weights=(1, 1, 1),
+               prefix_weight=0.1):
+        q = as_units(query)
+        is_int = result_is_int(metric, op)
+        c = _default_cutoff(metric, op) if score_cutoff is None else score_cutoff
+        idx = np.full(limit, -1, dtype=np.int64)
+        sc = np.zeros(limit, dtype=np.float64)
+        cnt = np.zeros(1, dtype=np.int32)
+        r = Request(corpus, metric, op, make_params(weights, prefix_weight),
+                    Cutoff(int(c) if is_int else 0, 0.0 if is_int else float(c), 0, 0.0), limit,
+                    int(limit == 1 if tie_last is None else tie_last), q.ctypes.data if q.size else None, q.size,
+                    q.itemsize, idx.ctypes.data, sc.ctypes.data, cnt.ctypes.data)
+        t = ctypes.c_uint64()
+        check(lib().rfg_server_submit(self._h, ctypes.byref(r), ctypes.byref(t)))
+        self._pending[t.value] = (idx, sc, cnt)
+        return t.value
+
+    def wait(self, ticket, timeout=600.0):
+        lat = ctypes.c_double()
+        check(lib().rfg_server_wait(self._h, ticket, timeout, ctypes.byref(lat)))
+        idx, sc, cnt = self._pending.pop(ticket)
+        n = int(cnt[0])
+        return idx[:n], sc[:n], lat.value
+
+    def stats(self):
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        check(lib().rfg_server_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"completed": a.value, "batches": b.value, "batched_requests": c.value}
+
+    def close(self):
+        if self._h and self._h.value:
+            lib().rfg_server_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):
