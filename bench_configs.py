@@ -10,6 +10,12 @@ cfg3  Levenshtein normalized_distance with score_cutoff 0.1 (cutoff = 10 % of th
       choice unrelated or a query mutated at 1-15 %: multi-word and banded kernels.
 cfg4  Jaro-Winkler (prefix_weight 0.1, cutoff 0.85) and fuzz::ratio (cutoff 85) over uint32
       code-point token strings, 1,024 x 1,000,000, dense float64 outputs kept on the device.
+cfg5  serving: device-resident corpora of 10,000,000 DNA strings (len U[10,200]) and
+      1,000,000 uint32 token strings; Poisson arrivals (--rate req/s for --duration s), each
+      an extractOne (limit 1) or top-10 extract of one query of length U[5,500] with a metric
+      drawn from {Levenshtein, Indel, OSA} (DNA corpus) or Jaro-Winkler (token corpus);
+      continuous batching (rfg_server); p50/p99 submit-to-result latency and pairs/s, beside
+      the same requests run one at a time (rfg_extract).
 """
 import json
 import os
@@ -155,6 +161,8 @@ def run(args, rank, world, local):
                      "cpu_baseline": {"value": _cells(qsub, c) / tc / 1e9, "unit": "GCUPS", "cores": os.cpu_count(),
                                       "kind": "port", "sample": "16 of the 256 queries x all 65,536 choices"},
                      "e2e": None, "gpu_launches": steps, "clocks": clk})
+    elif args.workload == "cfg5":
+        return run_serving(args, R, WL)
     else:
         (q, ql) = WL.tokens_u32(seed=14, n=1024)
         (c, _) = WL.tokens_u32(seed=15, n=1000000, derive_from=ql, derive_frac=0.05)
@@ -192,4 +200,89 @@ def run(args, rank, world, local):
                                       "cores": os.cpu_count(), "kind": "port",
                                       "sample": "4 of the 1,024 queries x all 1,000,000 choices"},
                      "e2e": None, "gpu_launches": 2 * steps, "clocks": clk})
+    print(json.dumps(line), flush=True)
+
+
+def run_serving(args, R, WL):
+    import threading
+    t0 = time.perf_counter()
+    dna = WL.dna_corpus_fast(seed=31, n=args.corpus)
+    tok = WL.tokens_u32_fast(seed=32, n=1_000_000)
+    corpora = [R.Corpus(dna), R.Corpus(tok)]
+    t_setup = time.perf_counter() - t0
+    rng = np.random.default_rng(33)
+    acgt = np.frombuffer(b"ACGT", dtype=np.uint8)
+    alpha = np.array(WL.TOKEN_ALPHABET + [0x20], dtype=np.uint32)
+    kinds = [(0, R.LEVENSHTEIN, R.DISTANCE), (0, R.INDEL, R.DISTANCE), (0, R.OSA, R.DISTANCE),
+             (1, R.JARO_WINKLER, R.SIMILARITY)]
+
+    def make_request():
+        c, m, op = kinds[int(rng.integers(0, 4))]
+        n = int(rng.integers(5, 501))
+        q = acgt[rng.integers(0, 4, size=n)] if c == 0 else alpha[rng.integers(0, len(alpha), size=n)]
+        limit = 1 if rng.random() < 0.5 else 10
+        return c, m, op, q, limit
+
+    # the same kinds of requests one at a time through rfg_extract
+    alone = {}
+    for kind in range(4):
+        c, m, op = kinds[kind]
+        ts = []
+        for rep in range(4):
+            n = int(rng.integers(5, 501))
+            q = acgt[rng.integers(0, 4, size=n)] if c == 0 else alpha[rng.integers(0, len(alpha), size=n)]
+            qb = R.pack_strings([q], q.itemsize)
+            a = time.perf_counter()
+            corpora[c].extract(m, op, qb, 10, None, False)
+            ts.append(time.perf_counter() - a)
+        alone[kind] = float(np.median(ts[1:]))
+    sizes = [corpora[0].count, corpora[1].count]
+
+    n_req = int(args.rate * args.duration)
+    gaps = rng.exponential(1.0 / args.rate, size=n_req)
+    arrivals = np.cumsum(gaps)
+    reqs = [make_request() for _ in range(n_req)]
+    server = R.Server(corpora, max_inflight=4, max_batch=64)
+    tickets = [None] * n_req
+    clocks = B.ClockSampler()
+    clocks.start()
+    start = time.perf_counter()
+
+    def submitter():
+        for i, (c, m, op, q, limit) in enumerate(reqs):
+            delay = start + arrivals[i] - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            tickets[i] = server.submit(c, m, op, q, limit, None, limit == 1)
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    th.join()
+    t_submitted = time.perf_counter() - start
+    lat = []
+    for t in tickets:
+        _, _, ms = server.wait(t, timeout=3600)
+        lat.append(ms)
+    wall = time.perf_counter() - start
+    clk = clocks.stop(0)
+    st = server.stats()
+    server.close()
+    lat = np.array(lat)
+    pairs = float(sum(sizes[c] for c, *_ in reqs))
+    pairs_alone = float(np.mean([sizes[kinds[k][0]] / alone[k] for k in range(4)]))
+    line = {"metric": METRIC, "value": pairs / wall, "unit": "pairs/s", "n_gpus": 1, "steps": n_req, "warmup": 0,
+            "ms_per_step": wall / n_req * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64+f64", "data": "synthetic (seeded dna_corpus_fast, tokens_u32_fast)",
+            "config": {"workload": "cfg5: serving, %d DNA (len U[10,200]) + 1,000,000 uint32 token strings, "
+                                   "Poisson %.0f req/s for %.1f s, extractOne/top-10, Lev/Indel/OSA/JW, "
+                                   "query len U[5,500]" % (args.corpus, args.rate, args.duration),
+                       "requests": n_req, "p50_ms": float(np.percentile(lat, 50)),
+                       "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
+                       "completed_per_s": n_req / wall, "offered_per_s": args.rate,
+                       "arrivals_span_s": float(arrivals[-1]), "submit_span_s": t_submitted,
+                       "batches": st["batches"], "mean_batch": st["batched_requests"] / max(st["batches"], 1),
+                       "alone_ms": {"levenshtein": alone[0] * 1e3, "indel": alone[1] * 1e3, "osa": alone[2] * 1e3,
+                                    "jaro_winkler": alone[3] * 1e3},
+                       "pairs_per_s_one_at_a_time": pairs_alone, "setup_s": t_setup},
+            "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": clk}
     print(json.dumps(line), flush=True)

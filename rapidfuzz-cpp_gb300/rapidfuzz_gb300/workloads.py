@@ -120,3 +120,41 @@ def tokens_u32(seed=0, n=1000, derive_from=None, derive_frac=0.0):
         out.append(s)
     d, o = _pack(out, np.uint32)
     return (d, o, 4), out
+
+
+def dna_corpus_fast(seed=0, n=10_000_000, lo=10, hi=200):
+    """n uint8 DNA strings, lengths U[lo, hi] (vectorised; ~1 GB at the serving size)"""
+    rng = np.random.default_rng(seed)
+    lens = rng.integers(lo, hi + 1, size=n)
+    off = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(lens, out=off[1:])
+    codes = np.frombuffer(b"ACGT", dtype=np.uint8)
+    data = codes[rng.integers(0, 4, size=int(off[-1]), dtype=np.uint8)]
+    return data, off, 1
+
+
+def tokens_u32_fast(seed=0, n=1_000_000):
+    """n uint32 strings of 1-4 space-joined tokens of 3-12 code points from TOKEN_ALPHABET"""
+    rng = np.random.default_rng(seed)
+    ntok = rng.integers(1, 5, size=n)
+    tot = int(ntok.sum())
+    tlen = rng.integers(3, 13, size=tot)
+    owner = np.repeat(np.arange(n), ntok)
+    slen = np.bincount(owner, weights=tlen, minlength=n).astype(np.int64) + (ntok - 1)
+    off = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(slen, out=off[1:])
+    alpha = np.array(TOKEN_ALPHABET, dtype=np.uint32)
+    data = alpha[rng.integers(0, len(alpha), size=int(off[-1]))]
+    # a space after every token except the last of its string
+    tok_end = np.cumsum(tlen + 1) - 1  # position of the separator in a space-after-every-token layout
+    first_tok = np.zeros(n, dtype=np.int64)
+    np.cumsum(ntok[:-1], out=first_tok[1:])
+    is_last = np.zeros(tot, dtype=bool)
+    is_last[first_tok + ntok - 1] = True
+    # separator position inside its string = (start of the string in the all-separators layout)
+    start_all = np.zeros(tot, dtype=np.int64)
+    np.cumsum((tlen + 1)[:-1], out=start_all[1:])
+    str_start_all = start_all[first_tok][owner]
+    sep_pos = off[owner] + (tok_end - str_start_all)
+    data[sep_pos[~is_last]] = 0x20
+    return data, off, 4
