@@ -257,6 +257,8 @@ struct BatchSpec {
     /* a corpus brings its own chunking and length order */
     const int32_t* fixed_perm = nullptr;
     int64_t fixed_chunk = 0;
+    const int32_t* chunk_lmin = nullptr;
+    const int32_t* chunk_lmax = nullptr;
 };
 
 inline bool better_high_of(int op) { return op == RFG_SIMILARITY || op == RFG_NORMALIZED_SIMILARITY; }
@@ -459,6 +461,8 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         a.thr = spec.thr;
         a.cand_key = spec.cand_key;
         a.cand_idx = spec.cand_idx;
+        a.chunk_lmin = spec.chunk_lmin;
+        a.chunk_lmax = spec.chunk_lmax;
         a.nchunks = (nc + chunk - 1) / chunk;
         const int64_t ntiles = (int64_t)a.nq * a.nchunks;
         if (ntiles > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "batch too large for one launch");
@@ -647,7 +651,7 @@ struct rfg_batch_s {
 };
 
 struct rfg_corpus_s {
-    DBuf data, off, perm;
+    DBuf data, off, perm, lmin, lmax;
     KStrings dev{};
     int64_t chunk = 0;
     int64_t count = 0;
@@ -982,6 +986,8 @@ rfg_status extract_enqueue(rfg_corpus c, const QuerySet& q, int metric, int op, 
     spec.cand_idx = job->cidx.as<int64_t>();
     spec.fixed_perm = c->perm.as<int32_t>();
     spec.fixed_chunk = c->chunk;
+    spec.chunk_lmin = c->lmin.as<int32_t>();
+    spec.chunk_lmax = c->lmax.as<int32_t>();
     RFG_TRY(prepare_batch(q, c->dev, spec, &job->pb)); /* synchronises the library stream */
     RFG_TRY(enqueue_batch(job->pb, st));
     const int is_int = is_int_result(metric, op);
@@ -1080,12 +1086,24 @@ rfg_status rfg_corpus_create(const rfg_strings* C, uint32_t flags, rfg_corpus* o
     c->count = nc;
     c->chunk = 4096;
     if (st == RFG_OK && nc) {
+        /* one global length order: chunks then hold narrow length ranges that extract
+         * tiles can test against the running threshold */
         std::vector<int32_t> len(nc), perm;
         for (int64_t i = 0; i < nc; ++i) len[i] = (int32_t)std::min<int64_t>(off[i + 1] - off[i], INT32_MAX);
-        chunk_length_order(len, c->chunk, &perm);
+        chunk_length_order(len, nc, &perm);
+        const int64_t nch = (nc + c->chunk - 1) / c->chunk;
+        std::vector<int32_t> lmin(nch), lmax(nch);
+        for (int64_t k = 0; k < nch; ++k) {
+            lmin[k] = len[perm[k * c->chunk]];
+            lmax[k] = len[perm[std::min(nc, (k + 1) * c->chunk) - 1]];
+        }
         st = c->perm.alloc((size_t)nc * 4);
+        if (st == RFG_OK) st = c->lmin.alloc((size_t)nch * 4);
+        if (st == RFG_OK) st = c->lmax.alloc((size_t)nch * 4);
         if (st == RFG_OK &&
-            cudaMemcpyAsync(c->perm.p, perm.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, g.stream) != cudaSuccess)
+            (cudaMemcpyAsync(c->perm.p, perm.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, g.stream) != cudaSuccess ||
+             cudaMemcpyAsync(c->lmin.p, lmin.data(), (size_t)nch * 4, cudaMemcpyHostToDevice, g.stream) != cudaSuccess ||
+             cudaMemcpyAsync(c->lmax.p, lmax.data(), (size_t)nch * 4, cudaMemcpyHostToDevice, g.stream) != cudaSuccess))
             st = fail(RFG_ERR_CUDA, "uploading the corpus order failed");
         if (st == RFG_OK && cudaStreamSynchronize(g.stream) != cudaSuccess) st = fail(RFG_ERR_CUDA, "corpus upload failed");
     }

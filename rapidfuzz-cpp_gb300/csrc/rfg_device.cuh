@@ -50,6 +50,11 @@ struct KParams {
      * complement for distance ops.  thr[q] is the running threshold key of query q
      * (raised by every tile that fills its topk), used to tighten the cutoff. */
     int topk;
+    /* corpus with a global length order: per-chunk length range; extract tiles then visit
+     * each query's chunks from its own length outwards and skip chunks whose lengths all
+     * fail the running threshold */
+    const int32_t* chunk_lmin;
+    const int32_t* chunk_lmax;
     int tie_last;    /* equal scores: the later choice wins (extractOne) instead of the earlier */
     int better_high; /* 1: larger scores are better (similarity ops) */
     u64* thr;
@@ -283,6 +288,49 @@ static __device__ void flush_topk(const KParams& a, int64_t qi, int64_t ch, TopL
     tl.n = 0;
 }
 
+/* chunk visited at step r of a query whose own length falls in chunk c0: c0, c0+1,
+ * c0-1, c0+2, ... (then one-sided once a side is exhausted) */
+__device__ __forceinline__ int64_t center_out(int64_t c0, int64_t r, int64_t nchunks)
+{
+    const int64_t below = c0, above = nchunks - 1 - c0;
+    const int64_t m2 = below < above ? below : above;
+    if (r == 0) return c0;
+    if (r <= 2 * m2) {
+        const int64_t k = (r + 1) / 2;
+        return (r & 1) ? c0 + k : c0 - k;
+    }
+    const int64_t t = r - 2 * m2;
+    return below > above ? c0 - (m2 + t) : c0 + (m2 + t);
+}
+
+/* first chunk whose length range reaches m (chunks are in ascending length order) */
+__device__ __forceinline__ int64_t chunk_of_length(const int32_t* lmax, int64_t nchunks, int m)
+{
+    int64_t lo = 0, hi = nchunks - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) / 2;
+        if (lmax[mid] < m) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+/* An extract tile can be skipped when no pair of it can pass the running threshold:
+ * distance ops of the unit-cost families, where every distance is >= |m - n|. */
+__device__ __forceinline__ bool tile_hopeless(const KParams& a, int64_t qi, int m, int64_t ch)
+{
+    if (!a.chunk_lmin || a.op != DISTANCE) return false;
+    const bool unit = a.metric == INDEL || a.metric == LCSSEQ || a.metric == OSA ||
+                      (a.metric == LEVENSHTEIN && a.sp.ins == 1 && a.sp.del == 1 && a.sp.rep == 1);
+    if (!unit) return false;
+    u64 K;
+    double unused;
+    tightened_cutoff(a, qi, true, &K, &unused);
+    const int64_t lo = a.chunk_lmin[ch], hi = a.chunk_lmax[ch];
+    if (K >= (u64)0x7fffffff) return false;
+    return hi < (int64_t)m - (int64_t)K || lo > (int64_t)m + (int64_t)K;
+}
+
 /* dense store, or the extract list */
 __device__ __forceinline__ void emit(const KParams& a, int64_t qi, int64_t ci, i64 vi, double vf, bool is_int,
                                      u64 cut_i, double cut_f, TopList<false>* tl)
@@ -408,7 +456,11 @@ __global__ void __launch_bounds__(256) k_tiles(const KParams a)
         /* extract batches sweep the corpus chunk-major (every query of the batch scores a
          * chunk while it is in L2); dense batches go query-major (coalesced rows) */
         const int64_t qi = TOPK ? a.qlist[t % a.nq] : a.qlist[t / a.nchunks];
-        const int64_t ch = TOPK ? t / a.nq : t % a.nchunks;
+        int64_t ch = TOPK ? t / a.nq : t % a.nchunks;
+        if (TOPK && a.chunk_lmin) {
+            const int ql = (int)(a.q.off[qi + 1] - a.q.off[qi]);
+            ch = center_out(chunk_of_length(a.chunk_lmax, a.nchunks, ql), ch, a.nchunks);
+        }
         if (qi != cur_q) {
             const int64_t q0 = a.q.off[qi];
             m = (int)(a.q.off[qi + 1] - q0);
@@ -427,8 +479,11 @@ __global__ void __launch_bounds__(256) k_tiles(const KParams a)
         /* positions of a chunk are visited in length order, so the threads of a warp get
          * pairs of similar work and pairs decided by the length filter cluster into
          * whole warps */
-        for (int64_t p = c0 + threadIdx.x; p < c1; p += blockDim.x)
-            score_pair<FAM, W, CT, TOPK>(a, rows, keys, qi, m, s_qpre, a.perm ? (int64_t)__ldg(a.perm + p) : p, &tl);
+        const bool skip = TOPK && tile_hopeless(a, qi, m, ch);
+        if (!skip)
+            for (int64_t p = c0 + threadIdx.x; p < c1; p += blockDim.x)
+                score_pair<FAM, W, CT, TOPK>(a, rows, keys, qi, m, s_qpre, a.perm ? (int64_t)__ldg(a.perm + p) : p,
+                                             &tl);
         if constexpr (TOPK) flush_topk(a, qi, ch, tl);
         __syncthreads();
     }
@@ -571,7 +626,11 @@ __global__ void __launch_bounds__(128) k_generic(const KParams a)
         const int64_t t = s_tile;
         if (t >= ntiles) break;
         const int64_t qi = TOPK ? a.qlist[t % a.nq] : a.qlist[t / a.nchunks];
-        const int64_t ch = TOPK ? t / a.nq : t % a.nchunks;
+        int64_t ch = TOPK ? t / a.nq : t % a.nchunks;
+        if (TOPK && a.chunk_lmin) {
+            const int ql = (int)(a.q.off[qi + 1] - a.q.off[qi]);
+            ch = center_out(chunk_of_length(a.chunk_lmax, a.nchunks, ql), ch, a.nchunks);
+        }
         if (qi != cur_q) {
             const int64_t q0 = a.q.off[qi];
             m = (int)(a.q.off[qi + 1] - q0);
@@ -587,9 +646,11 @@ __global__ void __launch_bounds__(128) k_generic(const KParams a)
         }
         const int64_t c0 = ch * a.chunk;
         const int64_t c1 = c0 + a.chunk < a.c.n ? c0 + a.chunk : a.c.n;
-        for (int64_t p = c0 + threadIdx.x; p < c1; p += blockDim.x)
-            score_pair_generic<FAM, CT, TOPK>(a, rows, keys, W, qi, m, qb, a.perm ? (int64_t)__ldg(a.perm + p) : p,
-                                              st, &tl);
+        const bool skip = TOPK && tile_hopeless(a, qi, m, ch);
+        if (!skip)
+            for (int64_t p = c0 + threadIdx.x; p < c1; p += blockDim.x)
+                score_pair_generic<FAM, CT, TOPK>(a, rows, keys, W, qi, m, qb,
+                                                  a.perm ? (int64_t)__ldg(a.perm + p) : p, st, &tl);
         if constexpr (TOPK) flush_topk(a, qi, ch, tl);
         __syncthreads();
     }
