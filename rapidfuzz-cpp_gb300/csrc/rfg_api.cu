@@ -382,6 +382,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
 
     /* one chunking of the choices for every class, each chunk visited in length order */
     int64_t chunk;
+    int64_t host_max_choice_len = 0;
     const int32_t* dperm;
     if (spec.fixed_perm) {
         chunk = spec.fixed_chunk;
@@ -397,6 +398,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         chunk = (chunk + blk - 1) / blk * blk;
         std::vector<int32_t> clen, perm;
         RFG_TRY(choice_lengths(c, host_choice_off, &clen));
+        for (int32_t l : clen) host_max_choice_len = std::max<int64_t>(host_max_choice_len, l);
         chunk_length_order(clen, chunk, &perm);
         RFG_TRY(pb->perm.alloc((size_t)nc * 4));
         RFG_CUDA(cudaMemcpyAsync(pb->perm.p, perm.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, g.stream));
@@ -406,6 +408,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
     pb->chunk = chunk;
     pb->nchunks = (nc + chunk - 1) / chunk;
     const bool topk = spec.topk > 0;
+    const int64_t max_choice_len = spec.fixed_perm ? RFG_JT_MAXT : host_max_choice_len;
 
     for (int k = 0; k < 5; ++k) {
         if (cls[k].empty()) continue;
@@ -449,7 +452,16 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         else {
             fn = generic_kernel(fam == FAM_NONE ? FAM_WF : fam, c.width, topk);
             block = 128;
-            per_sm = 2;
+            const int wmax = (fam == FAM_WF || fam == FAM_NONE) ? 0 : (int)((cls_maxlen[k] + 63) / 64);
+            const size_t table = wmax ? ((size_t)(256 + a.hcap + 1) * wmax + a.hcap) * 8 : 0;
+            if (table > 0 && table <= 100 * 1024) {
+                /* pattern table in shared memory; per-thread state stays in scratch */
+                a.pm_smem = 1;
+                smem = table;
+                if (smem > 48 * 1024)
+                    RFG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            }
+            per_sm = std::min(occupancy(fn, block, smem), 8);
         }
         /* tiles: (query, chunk), longest queries first; persistent CTAs fill every SM */
         const int64_t slots = (int64_t)g.sms * per_sm;
@@ -463,6 +475,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         a.cand_idx = spec.cand_idx;
         a.chunk_lmin = spec.chunk_lmin;
         a.chunk_lmax = spec.chunk_lmax;
+        a.tab_t = (int)std::min<int64_t>(RFG_JT_MAXT, max_choice_len);
         a.nchunks = (nc + chunk - 1) / chunk;
         const int64_t ntiles = (int64_t)a.nq * a.nchunks;
         if (ntiles > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "batch too large for one launch");
@@ -480,7 +493,8 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             }
             a.wmax = wmax;
             a.scratch_per_thread = per_thread;
-            a.scratch_per_cta = (wmax ? (int64_t)(256 + a.hcap + 1) * wmax + a.hcap : 0) + (int64_t)block * per_thread;
+            a.scratch_per_cta = (wmax && !a.pm_smem ? (int64_t)(256 + a.hcap + 1) * wmax + a.hcap : 0) +
+                                (int64_t)block * per_thread;
             RFG_TRY(pb->scratch[0].alloc((size_t)grid * a.scratch_per_cta * 8));
             pb->scratch_words = grid * a.scratch_per_cta;
             a.scratch = pb->scratch[0].as<u64>();

@@ -881,9 +881,17 @@ RFG_HD bool dist_chain_cutoff(int op, u64 M, u64 ci, double cf, u64* K)
     }
 }
 
-/* finish of a distance-type chain given d = _distance(K) */
-RFG_HD void dist_chain_finish(int op, u64 M, u64 d, u64 ci, double cf, i64* oi, double* of)
+/* finish of a distance-type chain given d = _distance(K), K the chain's cutoff.
+ * A pruned pair of a normalized op has d = K + 1 with K = ceil(M * c): then
+ * (K+1)/M >= c(1 - 2^-53) + 1/M exceeds c by far more than one rounding step (M < 2^33,
+ * c <= 2), so the reference returns exactly 1.0 (normalized distance) or 0.0
+ * (normalized similarity) -- taken here without the double division. */
+RFG_HD void dist_chain_finish(int op, u64 M, u64 d, u64 ci, double cf, i64* oi, double* of, u64 Kc = ~0ull)
 {
+    if (op >= NORM_DISTANCE && M != 0 && Kc != ~0ull && d > Kc && cf <= 2.0 && cf >= -2.0) {
+        *of = op == NORM_DISTANCE ? 1.0 : 0.0;
+        return;
+    }
     switch (op) {
     case DISTANCE: *oi = (i64)d; return;
     case SIMILARITY: {
@@ -1115,7 +1123,30 @@ struct PairSpec {
     u64 ci;
     double cf;
     ScoreParams p;
+    u64 kd_pre = ~0ull; /* precomputed chain cutoff of a normalized op (chain_kd), or ~0 */
 };
+
+/* The internal distance cutoff of a normalized op's chain for (l1, l2): ceil(M * c)
+ * with M the metric's maximum and c the cutoff the chain hands down.  Depends only on the
+ * lengths, so kernels tabulate it per query.  ~0 for ops without one. */
+RFG_HD u64 chain_kd(const PairSpec& s)
+{
+    if (s.form == FORM_MULTI) return ~0ull;
+    const int op = s.metric == RATIO ? NORM_SIMILARITY : s.op;
+    if (op != NORM_DISTANCE && op != NORM_SIMILARITY) return ~0ull;
+    const double cf = s.metric == RATIO ? ddiv(s.cf, 100.0) : s.cf;
+    const double c = op == NORM_DISTANCE ? cf : norm_sim_to_norm_dist(cf);
+    u64 M;
+    switch (s.metric) {
+    case LEVENSHTEIN: M = lev_maximum(s.l1, s.l2, s.p); break;
+    case INDEL:
+    case RATIO: M = s.l1 + s.l2; break;
+    case OSA:
+    case LCSSEQ: M = s.l1 > s.l2 ? s.l1 : s.l2; break;
+    default: return ~0ull;
+    }
+    return ceil_cut(M, c);
+}
 
 /* plan for integer families; returns the plan (run == 0: no core needed) */
 RFG_HD Plan plan_int(const PairSpec& s)
@@ -1139,7 +1170,8 @@ RFG_HD Plan plan_int(const PairSpec& s)
     case LEVENSHTEIN: {
         const u64 M = lev_maximum(l1, l2, s.p);
         u64 Kw;
-        if (!dist_chain_cutoff(s.op, M, s.ci, s.cf, &Kw)) {
+        if (s.kd_pre != ~0ull && s.op >= NORM_DISTANCE) Kw = s.kd_pre;
+        else if (!dist_chain_cutoff(s.op, M, s.ci, s.cf, &Kw)) {
             pl.run = 0;
             return pl;
         }
@@ -1157,8 +1189,8 @@ RFG_HD Plan plan_int(const PairSpec& s)
         const u64 M = l1 + l2;
         u64 K;
         const int op = s.metric == RATIO ? NORM_SIMILARITY : s.op;
-        const double cf = s.metric == RATIO ? ddiv(s.cf, 100.0) : s.cf;
-        if (!dist_chain_cutoff(op, M, s.ci, cf, &K)) {
+        if (s.kd_pre != ~0ull && op >= NORM_DISTANCE) K = s.kd_pre;
+        else if (!dist_chain_cutoff(op, M, s.ci, s.metric == RATIO ? ddiv(s.cf, 100.0) : s.cf, &K)) {
             pl.run = 0;
             return pl;
         }
@@ -1169,7 +1201,8 @@ RFG_HD Plan plan_int(const PairSpec& s)
     case OSA: {
         const u64 M = l1 > l2 ? l1 : l2;
         u64 K;
-        if (!dist_chain_cutoff(s.op, M, s.ci, s.cf, &K)) {
+        if (s.kd_pre != ~0ull && s.op >= NORM_DISTANCE) K = s.kd_pre;
+        else if (!dist_chain_cutoff(s.op, M, s.ci, s.cf, &K)) {
             pl.run = 0;
             return pl;
         }
@@ -1184,13 +1217,13 @@ RFG_HD Plan plan_int(const PairSpec& s)
         case SIMILARITY: cs = s.ci; break;
         case DISTANCE: cs = M >= s.ci ? M - s.ci : 0; break;
         case NORM_DISTANCE: {
-            const u64 Kd = ceil_cut(M, s.cf);
+            const u64 Kd = s.kd_pre != ~0ull ? s.kd_pre : ceil_cut(M, s.cf);
             pl.Kchain = Kd;
             cs = M >= Kd ? M - Kd : 0;
             break;
         }
         default: {
-            const u64 Kd = ceil_cut(M, norm_sim_to_norm_dist(s.cf));
+            const u64 Kd = s.kd_pre != ~0ull ? s.kd_pre : ceil_cut(M, norm_sim_to_norm_dist(s.cf));
             pl.Kchain = Kd;
             cs = M >= Kd ? M - Kd : 0;
         }
@@ -1265,7 +1298,7 @@ RFG_HD void finish_int(const PairSpec& s, const Plan& pl, i64 raw, i64* oi, doub
                 return;
             }
         }
-        dist_chain_finish(s.op, M, d, s.ci, s.cf, oi, of);
+        dist_chain_finish(s.op, M, d, s.ci, s.cf, oi, of, lev_mode(s.p) == LEV_ZERO ? ~0ull : Kw);
         return;
     }
     case INDEL:
@@ -1281,8 +1314,8 @@ RFG_HD void finish_int(const PairSpec& s, const Plan& pl, i64 raw, i64* oi, doub
         u64 d = raw >= 0 ? M - 2 * (u64)raw : K + 1;
         d = d <= K ? d : K + 1;
         double r = 0;
-        dist_chain_finish(op, M, d, s.ci, cf, oi, &r);
-        if (s.metric == RATIO) *of = dmul(r, 100.0);
+        dist_chain_finish(op, M, d, s.ci, cf, oi, &r, K);
+        if (s.metric == RATIO) *of = r == 0.0 ? 0.0 : dmul(r, 100.0);
         else *of = r;
         return;
     }
@@ -1294,7 +1327,7 @@ RFG_HD void finish_int(const PairSpec& s, const Plan& pl, i64 raw, i64* oi, doub
         }
         const u64 K = pl.Kchain;
         const u64 d = (u64)raw <= K ? (u64)raw : K + 1;
-        dist_chain_finish(s.op, M, d, s.ci, s.cf, oi, of);
+        dist_chain_finish(s.op, M, d, s.ci, s.cf, oi, of, K);
         return;
     }
     case LCSSEQ: {
@@ -1313,6 +1346,10 @@ RFG_HD void finish_int(const PairSpec& s, const Plan& pl, i64 raw, i64* oi, doub
             const u64 Kd = pl.Kchain;
             u64 d = M - sim;
             d = d <= Kd ? d : Kd + 1;
+            if (d > Kd && M != 0 && s.cf <= 2.0 && s.cf >= -2.0) { /* see dist_chain_finish */
+                *of = 1.0;
+                return;
+            }
             const double nd = M != 0 ? ddiv((double)d, (double)M) : 0.0;
             *of = nd <= s.cf ? nd : 1.0;
             return;
@@ -1322,6 +1359,10 @@ RFG_HD void finish_int(const PairSpec& s, const Plan& pl, i64 raw, i64* oi, doub
             const double c2 = norm_sim_to_norm_dist(s.cf);
             u64 d = M - sim;
             d = d <= Kd ? d : Kd + 1;
+            if (d > Kd && M != 0 && s.cf <= 2.0 && s.cf >= -2.0) {
+                *of = 0.0;
+                return;
+            }
             double nd = M != 0 ? ddiv((double)d, (double)M) : 0.0;
             nd = nd <= c2 ? nd : 1.0;
             const double ns = dsub(1.0, nd);
@@ -1345,6 +1386,64 @@ RFG_HD bool jaro_pair_needs_counts(const PairSpec& s, i64 prefix)
 {
     if (s.form == FORM_MULTI) return s.l2 != 0;
     return jaro_needs_counts((i64)s.l1, (i64)s.l2, jaro_cutoff_for(s, prefix));
+}
+
+/* Per-query tables of the Jaro chains (free / Cached forms): everything that depends
+ * only on the common prefix (0..4) and the text length.  minc[p][tl] is 0 when the
+ * reference never reads the counts (its early exits), else the smallest common-character
+ * count passing jaro_common_filter (the filter is monotone in the count), 0xffff when
+ * none does.  jc[p]: the cutoff the inner Jaro runs with; v0[p]: its value when the
+ * counts are not read.  With them a pair needs doubles only when it can pass. */
+#define RFG_JT_MAXT 256
+struct JaroTab {
+    double jc[5];
+    unsigned short minc[5][RFG_JT_MAXT + 1];
+};
+
+RFG_HD double jaro_tab_cutoff(const PairSpec& s, int prefix)
+{
+    const double c = fsim_chain_cutoff(s.op, s.cf);
+    return s.metric == JARO ? c : jw_jaro_cutoff(prefix, s.p.prefix_weight, c);
+}
+
+/* entry (prefix, tl) for a query of length pl; s carries metric, op, cutoff, weight */
+RFG_HD unsigned short jaro_tab_minc(const PairSpec& s, i64 pl, int prefix, i64 tl)
+{
+    const double c = jaro_tab_cutoff(s, prefix);
+    if (!jaro_needs_counts(pl, tl, c)) return 0;
+    const i64 cmax = pl < tl ? pl : tl;
+    i64 lo = 1, hi = cmax + 1; /* first passing count in [1, cmax], or cmax + 1 */
+    while (lo < hi) {
+        const i64 mid = (lo + hi) / 2;
+        if (jaro_common_filter(pl, tl, mid, c)) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo > cmax ? (unsigned short)0xffff : (unsigned short)(lo > 0xfffe ? 0xfffe : lo);
+}
+
+/* jaro_from_counts with the table: identical values */
+RFG_HD double jaro_from_counts_tab(i64 pl, i64 tl, i64 common, i64 transp, double c, unsigned short minc)
+{
+    if (minc == 0) return c > 1.0 ? 0.0 : ((pl == 0 && tl == 0) ? 1.0 : 0.0);
+    if (pl == 1 && tl == 1) return (double)(common == 1);
+    if (common < (i64)minc) return 0.0;
+    const double sim = jaro_formula(pl, tl, common, transp);
+    return sim >= c ? sim : 0;
+}
+
+RFG_HD double finish_jaro_tab(const PairSpec& s, const JaroTab& t, i64 prefix, i64 common, i64 transp)
+{
+    const i64 pl = (i64)s.l1, tl = (i64)s.l2;
+    const double jc = t.jc[prefix];
+    const double sim_j = jaro_from_counts_tab(pl, tl, common, transp, jc, t.minc[prefix][tl]);
+    const double sim = s.metric == JARO ? sim_j : jw_finish(sim_j, prefix, s.p.prefix_weight, fsim_chain_cutoff(s.op, s.cf));
+    if (s.op == SIMILARITY) return sim;
+    return fsim_chain_finish(s.op, sim, s.cf);
+}
+
+RFG_HD void jaro_tab_head(JaroTab& t, const PairSpec& s)
+{
+    for (int p = 0; p < 5; ++p) t.jc[p] = jaro_tab_cutoff(s, p);
 }
 
 RFG_HD double finish_jaro(const PairSpec& s, i64 prefix, i64 common, i64 transp)

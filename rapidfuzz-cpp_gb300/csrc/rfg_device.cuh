@@ -43,6 +43,7 @@ struct KParams {
     int out_dtype; /* 0 i32, 1 i64, 2 f64 */
     int64_t ld;
     int hcap;      /* hash slots for code units >= 256 (power of two, or 0) */
+    int tab_t;     /* per-query length tables cover text lengths 0..tab_t (<= RFG_JT_MAXT) */
     const int32_t* perm; /* choice order within each chunk (length-sorted), or nullptr */
     /* extract epilogue (topk > 0): instead of a dense matrix, every (query, chunk) tile
      * keeps its best topk results in cand_key/cand_idx[(q * nchunks + chunk) * topk + r];
@@ -65,6 +66,7 @@ struct KParams {
     int64_t scratch_per_cta;    /* u64 words of the per-CTA pattern table region */
     int64_t scratch_per_thread; /* u64 words of each thread's state */
     int wmax;                   /* pattern words of the generic class */
+    int pm_smem;                /* 1: the generic pattern table lives in dynamic shared memory */
 };
 
 /* ----------------------------------------------------------------- helpers */
@@ -381,9 +383,52 @@ __device__ __forceinline__ i64 run_int_core(const PMF& pm, int m, const TXT& t, 
 }
 
 /* one (query, choice) pair of an integer-valued or Jaro family */
+/* per-query length tables (see JaroTab / chain_kd) */
+union LenTab {
+    JaroTab jt;
+    u64 kd[RFG_JT_MAXT + 1];
+};
+
+__device__ __forceinline__ bool uses_jaro_tab(const KParams& a) { return a.form != FORM_MULTI && a.tab_t >= 0; }
+__device__ __forceinline__ bool uses_kd_tab(const KParams& a)
+{
+    const int op = a.metric == RATIO ? NORM_SIMILARITY : a.op;
+    return a.form != FORM_MULTI && a.tab_t >= 0 && op >= NORM_DISTANCE;
+}
+
+/* build the tables of query length m; all threads; ends with a barrier */
+template <int FAM>
+__device__ __noinline__ void build_len_tab(const KParams& a, int m, LenTab& t)
+{
+    PairSpec s;
+    s.metric = a.metric;
+    s.op = a.op;
+    s.form = a.form;
+    s.l1 = (u64)m;
+    s.ci = a.ci;
+    s.cf = a.cf;
+    s.p = a.sp;
+    if (FAM == FAM_JARO) {
+        if (!uses_jaro_tab(a)) return;
+        if (threadIdx.x == 0) jaro_tab_head(t.jt, s);
+        for (int i = threadIdx.x; i < 5 * (a.tab_t + 1); i += blockDim.x) {
+            const int p = i / (a.tab_t + 1), tl = i % (a.tab_t + 1);
+            t.jt.minc[p][tl] = jaro_tab_minc(s, m, p, tl);
+        }
+    }
+    else {
+        if (!uses_kd_tab(a)) return;
+        for (int tl = threadIdx.x; tl <= a.tab_t; tl += blockDim.x) {
+            s.l2 = (u64)tl;
+            t.kd[tl] = chain_kd(s);
+        }
+    }
+    __syncthreads();
+}
+
 template <int FAM, int W, typename CT, bool TOPK>
 __device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, const u64* keys, int64_t qi, int m,
-                                           const u64* qpre, int64_t ci, TopList<TOPK>* tl)
+                                           const u64* qpre, int64_t ci, TopList<TOPK>* tl, const LenTab& lt)
 {
     const int64_t o0 = a.c.off[ci], o1 = a.c.off[ci + 1];
     const int n = (int)(o1 - o0);
@@ -409,6 +454,26 @@ __device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, co
         for (; prefix < mx; ++prefix)
             if ((u64)__ldg(s2 + prefix) != qpre[prefix]) break;
         int common = 0, transp = 0;
+        if (uses_jaro_tab(a) && n <= a.tab_t && !TOPK) {
+            /* the table decides which pairs need counts and whether they can pass */
+            const unsigned short mc = lt.jt.minc[prefix][n];
+            const int cmax = m < n ? m : n;
+            if (mc != 0 && ((mc != 0xffff && cmax >= (int)mc) || (m == 1 && n == 1))) {
+                if (W == 1) {
+                    int bound = (m > n ? m : n) / 2;
+                    if (bound > 0) --bound;
+                    const int te = n < m + bound ? n : m + bound;
+                    if (te <= 64) jaro_word(pm, m, txt, n, &common, &transp);
+                    else jaro_multi<1>(pm, m, txt, n, &common, &transp);
+                }
+                else {
+                    jaro_multi<W>(pm, m, txt, n, &common, &transp);
+                }
+            }
+            vf = finish_jaro_tab(s, lt.jt, prefix, common, transp);
+            emit(a, qi, ci, 0, vf, false, s.ci, s.cf, tl);
+            return;
+        }
         if (m > 0 && n > 0 && jaro_pair_needs_counts(s, prefix)) {
             if (W == 1) {
                 int bound = (m > n ? m : n) / 2;
@@ -425,6 +490,7 @@ __device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, co
         emit(a, qi, ci, 0, vf, false, s.ci, s.cf, tl);
         return;
     }
+    if (!TOPK && n <= a.tab_t && uses_kd_tab(a)) s.kd_pre = lt.kd[n];
     const Plan pl = plan_int(s);
     i64 raw = 0;
     if (pl.run) raw = run_int_core<FAM, W>(pm, m, txt, n, pl.K);
@@ -443,6 +509,7 @@ __global__ void __launch_bounds__(256) k_tiles(const KParams a)
     u64* keys = smem + (size_t)nrows * W;
     __shared__ int64_t s_tile;
     __shared__ u64 s_qpre[4];
+    __shared__ LenTab s_lt;
     int64_t cur_q = -1;
     int m = 0;
     TopList<TOPK> tl;
@@ -471,6 +538,7 @@ __global__ void __launch_bounds__(256) k_tiles(const KParams a)
             }
             build_pm<W>(rows, keys, a.hcap, qb, m, a.q.width, a.err);
             if (threadIdx.x < 4) s_qpre[threadIdx.x] = (int)threadIdx.x < m ? load_unit(qb, a.q.width, threadIdx.x) : 0;
+            if (!TOPK) build_len_tab<FAM>(a, m, s_lt);
             __syncthreads();
             cur_q = qi;
         }
@@ -483,7 +551,7 @@ __global__ void __launch_bounds__(256) k_tiles(const KParams a)
         if (!skip)
             for (int64_t p = c0 + threadIdx.x; p < c1; p += blockDim.x)
                 score_pair<FAM, W, CT, TOPK>(a, rows, keys, qi, m, s_qpre, a.perm ? (int64_t)__ldg(a.perm + p) : p,
-                                             &tl);
+                                             &tl, s_lt);
         if constexpr (TOPK) flush_topk(a, qi, ch, tl);
         __syncthreads();
     }
@@ -599,6 +667,10 @@ __device__ __forceinline__ void score_pair_generic(const KParams& a, const u64* 
         else if (K < diff) raw = K + 1;
         else if (n == 0) raw = m;
         else if (FAM == FAM_OSA) raw = osa_multi_rt(pm, W, m, txt, n, K, st, st + W, st + 2 * W, st + 3 * W);
+        else if (K < m && 2 * K + 1 <= 64) raw = lev_band<1>(pm, W, m, txt, n, (int)K);
+        else if (K < m && 2 * K + 1 <= 128) raw = lev_band<2>(pm, W, m, txt, n, (int)K);
+        else if (K < m && 2 * K + 1 <= 256) raw = lev_band<4>(pm, W, m, txt, n, (int)K);
+        else if (K < m && 2 * K + 1 <= 512) raw = lev_band<8>(pm, W, m, txt, n, (int)K);
         else raw = lev_multi_rt(pm, W, m, txt, n, K, st, st + W);
     }
     finish_int(s, pl, raw, &vi, &vf);
@@ -606,13 +678,15 @@ __device__ __forceinline__ void score_pair_generic(const KParams& a, const u64* 
 }
 
 template <int FAM, typename CT, bool TOPK = false>
-__global__ void __launch_bounds__(128) k_generic(const KParams a)
+__global__ void __launch_bounds__(256) k_generic(const KParams a)
 {
+    extern __shared__ u64 gsm[];
     const int W = a.wmax;
+    const int64_t table = (int64_t)(256 + a.hcap + 1) * W + a.hcap;
     u64* region = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
-    u64* rows = region;
+    u64* rows = a.pm_smem ? gsm : region;
     u64* keys = rows + (int64_t)(256 + a.hcap + 1) * W;
-    u64* st = region + (int64_t)(256 + a.hcap + 1) * W + a.hcap + (int64_t)threadIdx.x * a.scratch_per_thread;
+    u64* st = region + (a.pm_smem ? 0 : table) + (int64_t)threadIdx.x * a.scratch_per_thread;
     __shared__ int64_t s_tile;
     int64_t cur_q = -1;
     int m = 0;
