@@ -38,6 +38,7 @@ sys.path.insert(0, os.path.join(ROOT, "rapidfuzz-cpp_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 METRIC_NAME = "GCUPS & pairs/s, batched vs per-call, 1 GB300, bit-exact; extract p50/p99 ms"
+DRAM_BYTES_PER_LAUNCH = {"levenshtein": 35292672, "indel": 35352320, "osa": 26712320}
 OPS_PER_WORD_STEP = {"levenshtein": 23, "indel": 8, "osa": 29}
 CUTOFF = 8
 
@@ -203,6 +204,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     import rapidfuzz_gb300 as R
+    from rapidfuzz_gb300 import sharding
     R.lib().rfg_set_device(local)
 
     q, c = workload(rank, args.nq, args.nc)
@@ -275,13 +277,7 @@ def main():
             total_ms += ev[0][0].elapsed_time(ev[-1][1])
     torch.cuda.synchronize()
     clk = clocks.stop(local)
-    t_local = total_ms / 1e3
-    if dist is not None:
-        tt = torch.tensor([t_local], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    else:
-        t_max = t_local
+    t_max = sharding.max_over_ranks(total_ms / 1e3, device=dev)
     for _, b in batches:
         b.check(stream.cuda_stream)
 
@@ -294,13 +290,9 @@ def main():
     alg_ops = req_steps * OPS_PER_WORD_STEP[dom]
     peak = int_peak_ops()
     achieved = alg_ops / (dom_ms * 1e-3)
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tf):
-        try:
-            traffic = json.load(open(tf)).get(dom)
-        except Exception:
-            traffic = None
+    # dram__bytes_read.sum + dram__bytes_write.sum per launch of the default launch shape,
+    # from one ncu capture of this workload (profiles/k_tiles_cdist4096_full.md)
+    traffic = DRAM_BYTES_PER_LAUNCH.get(dom) if args.nq == 4096 and args.nc == 4096 else None
 
     # e2e through the public C ABI with pinned host buffers
     e2e = None
@@ -320,13 +312,7 @@ def main():
         for _ in range(args.steps):
             for (name, m), o in zip(metrics, ho):
                 R.cdist(m, R.DISTANCE, qh, ch, CUTOFF, out_dtype=R.I32, out=o)
-        te = time.perf_counter() - t0
-        if dist is not None:
-            tt = torch.tensor([te], device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            te = float(tt.item())
-        for (name, m), o in zip(metrics, outs):
-            pass
+        te = sharding.max_over_ranks(time.perf_counter() - t0, device=dev)
         h2d = 3 * (q[0].nbytes + q[1].nbytes + c[0].nbytes + c[1].nbytes)
         d2h = 3 * nq * nc * 4
         e2e = {"value": cells * 3 * args.steps * world / te / 1e9, "unit": "GCUPS", "h2d_bytes_per_step": h2d,
