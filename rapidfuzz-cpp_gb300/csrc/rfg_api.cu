@@ -264,6 +264,7 @@ struct BatchSpec {
 inline bool better_high_of(int op) { return op == RFG_SIMILARITY || op == RFG_NORMALIZED_SIMILARITY; }
 
 int64_t g_tiles_target = 0; /* override of the tile-count target (autotuning) */
+int g_stage_mode = 1;       /* dense tiles stage their results in shared memory (autotuning) */
 int g_block_override = 0;   /* override of the tile kernels' block size (autotuning) */
 
 /* A prepared batch: everything a launch needs is on the device, so enqueue() only
@@ -383,6 +384,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
     /* one chunking of the choices for every class, each chunk visited in length order */
     int64_t chunk;
     int64_t host_max_choice_len = 0;
+    int64_t stage = 0; /* staged window of the dense tiles (elements), 0 = direct stores */
     const int32_t* dperm;
     if (spec.fixed_perm) {
         chunk = spec.fixed_chunk;
@@ -396,10 +398,16 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         chunk = std::max<int64_t>(chunk, blk);
         chunk = std::min<int64_t>(chunk, std::max<int64_t>(nc, 1));
         chunk = (chunk + blk - 1) / blk * blk;
+        if (spec.topk == 0 && g_stage_mode != 0) {
+            /* windows of up to 32 KB of results, each its own length-sorted run */
+            const int64_t cap = spec.out_dtype == RFG_I32 ? 8192 : 4096;
+            if (chunk > cap) chunk = (chunk + cap - 1) / cap * cap;
+            stage = std::min(chunk, cap);
+        }
         std::vector<int32_t> clen, perm;
         RFG_TRY(choice_lengths(c, host_choice_off, &clen));
         for (int32_t l : clen) host_max_choice_len = std::max<int64_t>(host_max_choice_len, l);
-        chunk_length_order(clen, chunk, &perm);
+        chunk_length_order(clen, stage ? stage : chunk, &perm);
         RFG_TRY(pb->perm.alloc((size_t)nc * 4));
         RFG_CUDA(cudaMemcpyAsync(pb->perm.p, perm.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, g.stream));
         RFG_CUDA(cudaStreamSynchronize(g.stream)); /* perm / qall are host temporaries */
@@ -446,6 +454,10 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             }
             block = g_block_override > 0 ? g_block_override : 256;
             smem = tiles_smem_bytes(W, a.hcap);
+            if (stage) {
+                a.stage = stage;
+                smem += (size_t)stage * (spec.out_dtype == RFG_I32 ? 4 : 8);
+            }
             if (smem > 48 * 1024) RFG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             per_sm = occupancy(fn, block, smem);
         }
@@ -1182,16 +1194,19 @@ rfg_status rfg_extract(rfg_corpus c, rfg_metric metric, rfg_op op, const rfg_str
 
 /* --------------------------------------------------------- prepared batches */
 
-static rfg_status batch_reprepare(rfg_batch b, int block, int64_t tiles)
+static rfg_status batch_reprepare(rfg_batch b, int block, int64_t tiles, int stage = 1)
 {
     const int ob = g_block_override;
     const int64_t ot = g_tiles_target;
+    const int os = g_stage_mode;
     g_block_override = block;
     g_tiles_target = tiles;
+    g_stage_mode = stage;
     Prepared* np = new Prepared();
     rfg_status st = prepare_batch(b->qs, b->ck, b->spec, np);
     g_block_override = ob;
     g_tiles_target = ot;
+    g_stage_mode = os;
     if (st == RFG_OK && cudaStreamSynchronize(g.stream) != cudaSuccess) st = fail(RFG_ERR_CUDA, "prepare failed");
     if (st != RFG_OK) {
         delete np;
@@ -1305,14 +1320,15 @@ rfg_status rfg_batch_tune(rfg_batch b, void* stream, int32_t* best_block, int64_
     RFG_CUDA(cudaEventCreate(&e0));
     RFG_CUDA(cudaEventCreate(&e1));
     float best = 1e30f;
-    int bb = 256;
+    int bb = 256, bs = 1;
     int64_t bt = 0;
     const int blocks[] = {128, 256};
     const int mults[] = {2, 4, 8, 16, 32};
+    for (int stage = 1; stage >= 0; --stage)
     for (int blk : blocks) {
         for (int mu : mults) {
             const int64_t tiles = (int64_t)g.sms * mu * (256 / blk) * 2;
-            RFG_TRY(batch_reprepare(b, blk, tiles));
+            RFG_TRY(batch_reprepare(b, blk, tiles, stage));
             float times[3];
             for (int r = 0; r < 3; ++r) {
                 RFG_CUDA(cudaEventRecord(e0, st));
@@ -1326,12 +1342,13 @@ rfg_status rfg_batch_tune(rfg_batch b, void* stream, int32_t* best_block, int64_
                 best = times[1];
                 bb = blk;
                 bt = tiles;
+                bs = stage;
             }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    RFG_TRY(batch_reprepare(b, bb, bt));
+    RFG_TRY(batch_reprepare(b, bb, bt, bs));
     RFG_TRY(check_batch(*b->pb, st));
     if (best_block) *best_block = bb;
     if (best_tiles) *best_tiles = bt;

@@ -32,8 +32,12 @@
 
 #ifdef __CUDACC__
 #define RFG_HD __host__ __device__ __forceinline__
+/* double-precision tails of the chains: kept out of line so the integer launches never
+ * evaluate them speculatively (the FP64 pipe is a small fraction of the INT32 rate) */
+#define RFG_COLD static __host__ __device__ __noinline__
 #else
 #define RFG_HD inline
+#define RFG_COLD static inline
 #endif
 
 namespace rfg {
@@ -103,6 +107,20 @@ RFG_HD u64 add_carry(u64 a, u64 b, u32 cin, u32* cout)
 
 /* -------------------------------------------------------------- exact doubles */
 
+/* |x| <= lim for lim >= 0 on the bit patterns (no FP64 instruction; NaN compares false):
+ * non-negative doubles order like their bit patterns */
+RFG_HD bool abs_le_bits(double x, double lim)
+{
+#ifdef __CUDA_ARCH__
+    const u64 bx = (u64)__double_as_longlong(x), bl = (u64)__double_as_longlong(lim);
+#else
+    u64 bx, bl;
+    __builtin_memcpy(&bx, &x, 8);
+    __builtin_memcpy(&bl, &lim, 8);
+#endif
+    return (bx & 0x7fffffffffffffffull) <= bl;
+}
+
 RFG_HD double dadd(double a, double b)
 {
 #ifdef __CUDA_ARCH__
@@ -165,23 +183,45 @@ struct ScoreParams {
  * PM: pattern-match table of s1 (pm(c) = bit i set when s1[i] == c), pattern length
  * m in 1..64.  TXT: t[j] yields the j-th code unit of s2.  K: pruning bound. */
 
+/* The single-word cores fetch the text eight characters at a time: the eight loads and
+ * pattern-row lookups are independent of each other and of the recurrence, so their
+ * latencies overlap.  The lower-bound check runs every 8th character. */
+#ifndef RFG_FETCH
+#define RFG_FETCH 8
+#endif
+
+template <typename PMF, typename TXT>
+RFG_HD void fetch_block(const PMF& pm, const TXT& t, int j0, int n, u64 (&X)[RFG_FETCH])
+{
+#pragma unroll
+    for (int k = 0; k < RFG_FETCH; ++k) X[k] = j0 + k < n ? pm(t[j0 + k]) : 0;
+}
+
 /* Hyyro 2003 (Levenshtein_impl.hpp:259-322) */
 template <typename PMF, typename TXT>
 RFG_HD i64 lev_word(const PMF& pm, int m, const TXT& t, int n, i64 K)
 {
     u64 VP = ~0ull, VN = 0;
     const bool check = K < (i64)(m > n ? m : n);
-    for (int j = 0; j < n; ++j) {
-        const u64 X = pm(t[j]);
-        const u64 D0 = (((X & VP) + VP) ^ VP) | X | VN;
-        u64 HP = VN | ~(D0 | VP);
-        u64 HN = D0 & VP;
-        HP = (HP << 1) | 1;
-        HN = HN << 1;
-        VP = HN | ~(D0 | HP);
-        VN = HP & D0;
-        if (check && (j & 7) == 7) {
-            const int jj = j + 1, is = m - n + jj;
+    for (int j0 = 0; j0 < n; j0 += RFG_FETCH) {
+        u64 Xb[RFG_FETCH];
+        fetch_block(pm, t, j0, n, Xb);
+        const int kn = n - j0 < RFG_FETCH ? n - j0 : RFG_FETCH;
+#pragma unroll
+        for (int k = 0; k < RFG_FETCH; ++k) {
+            if (k < kn) {
+                const u64 X = Xb[k];
+                const u64 D0 = (((X & VP) + VP) ^ VP) | X | VN;
+                u64 HP = VN | ~(D0 | VP);
+                u64 HN = D0 & VP;
+                HP = (HP << 1) | 1;
+                HN = HN << 1;
+                VP = HN | ~(D0 | HP);
+                VN = HP & D0;
+            }
+        }
+        if (check && kn == RFG_FETCH && ((j0 + RFG_FETCH) & 7) == 0) {
+            const int jj = j0 + RFG_FETCH, is = m - n + jj;
             if (is >= 0) {
                 const u64 lm = low_mask(is);
                 const i64 lb = (i64)jj + popc64(VP & lm) - popc64(VN & lm);
@@ -200,12 +240,19 @@ RFG_HD i64 lcs_word(const PMF& pm, int m, const TXT& t, int n, i64 Kd)
 {
     u64 S = ~0ull;
     const bool check = Kd < (i64)(m + n);
-    for (int j = 0; j < n; ++j) {
-        const u64 X = pm(t[j]);
-        const u64 u = S & X;
-        S = (S + u) | (S - u);
-        if (check && (j & 7) == 7) {
-            const int jj = j + 1, is = m - n + jj;
+    for (int j0 = 0; j0 < n; j0 += RFG_FETCH) {
+        u64 Xb[RFG_FETCH];
+        fetch_block(pm, t, j0, n, Xb);
+        const int kn = n - j0 < RFG_FETCH ? n - j0 : RFG_FETCH;
+#pragma unroll
+        for (int k = 0; k < RFG_FETCH; ++k) {
+            if (k < kn) {
+                const u64 u = S & Xb[k];
+                S = (S + u) | (S - u);
+            }
+        }
+        if (check && kn == RFG_FETCH && ((j0 + RFG_FETCH) & 7) == 0) {
+            const int jj = j0 + RFG_FETCH, is = m - n + jj;
             if (is >= 0) {
                 const i64 lcs_is = popc64(~S & low_mask(is));
                 if ((i64)is + jj - 2 * lcs_is > Kd) return -1;
@@ -221,19 +268,27 @@ RFG_HD i64 osa_word(const PMF& pm, int m, const TXT& t, int n, i64 K)
 {
     u64 VP = ~0ull, VN = 0, D0 = 0, PMold = 0;
     const bool check = K < (i64)(m > n ? m : n);
-    for (int j = 0; j < n; ++j) {
-        const u64 X = pm(t[j]);
-        const u64 TR = (((~D0) & X) << 1) & PMold;
-        D0 = (((X & VP) + VP) ^ VP) | X | VN | TR;
-        u64 HP = VN | ~(D0 | VP);
-        u64 HN = D0 & VP;
-        HP = (HP << 1) | 1;
-        HN = HN << 1;
-        VP = HN | ~(D0 | HP);
-        VN = HP & D0;
-        PMold = X;
-        if (check && (j & 7) == 7) {
-            const int jj = j + 1, is = m - n + jj;
+    for (int j0 = 0; j0 < n; j0 += RFG_FETCH) {
+        u64 Xb[RFG_FETCH];
+        fetch_block(pm, t, j0, n, Xb);
+        const int kn = n - j0 < RFG_FETCH ? n - j0 : RFG_FETCH;
+#pragma unroll
+        for (int k = 0; k < RFG_FETCH; ++k) {
+            if (k < kn) {
+                const u64 X = Xb[k];
+                const u64 TR = (((~D0) & X) << 1) & PMold;
+                D0 = (((X & VP) + VP) ^ VP) | X | VN | TR;
+                u64 HP = VN | ~(D0 | VP);
+                u64 HN = D0 & VP;
+                HP = (HP << 1) | 1;
+                HN = HN << 1;
+                VP = HN | ~(D0 | HP);
+                VN = HP & D0;
+                PMold = X;
+            }
+        }
+        if (check && kn == RFG_FETCH && ((j0 + RFG_FETCH) & 7) == 0) {
+            const int jj = j0 + RFG_FETCH, is = m - n + jj;
             if (is >= 0) {
                 const u64 lm = low_mask(is);
                 const i64 lb = (i64)jj + popc64(VP & lm) - popc64(VN & lm);
@@ -248,7 +303,7 @@ RFG_HD i64 osa_word(const PMF& pm, int m, const TXT& t, int n, i64 K)
 /* Jaro flagging, P (= s1) 1..64 chars, effective text length <= 64
  * (Jaro_impl.hpp:94-132, 258-276).  Returns common chars, transpositions (unhalved). */
 template <typename PMF, typename TXT>
-RFG_HD void jaro_word(const PMF& pm, int pl, const TXT& t, int tl, int* common, int* transp)
+RFG_HD void jaro_word(const PMF& pm, int pl, const TXT& t, int tl, int* common, int* transp, int need = 0)
 {
     int bound = (pl > tl ? pl : tl) / 2;
     if (bound > 0) --bound;
@@ -269,8 +324,19 @@ RFG_HD void jaro_word(const PMF& pm, int pl, const TXT& t, int tl, int* common, 
         pflag |= blsi(x);
         tflag |= (u64)(x != 0) << j;
         bmask <<= 1;
+        /* each remaining text character adds at most one common character: a caller
+         * that only needs to know whether `need` is reached stops here */
+        if ((j & 7) == 7 && popc64(pflag) + (te - 1 - j) < need) {
+            *common = 0;
+            *transp = 0;
+            return;
+        }
     }
     *common = popc64(pflag);
+    if (*common < need) {
+        *transp = 0;
+        return;
+    }
     int tr = 0;
     while (tflag) {
         const u64 pbit = blsi(pflag);
@@ -867,6 +933,14 @@ struct Plan {
 
 RFG_HD i64 clamp_bound(u64 k) { return k > (u64)0x3fffffffffffffffull ? (i64)0x3fffffffffffffffll : (i64)k; }
 
+/* integer cutoff of a normalized op: ceil(M * c_nd) (distance.hpp:52-76); ratio: the
+ * cutoff arrives in percent (fuzz_impl.hpp:28-32) */
+RFG_COLD u64 norm_cut(int op, u64 M, double cf, int ratio)
+{
+    if (ratio) cf = ddiv(cf, 100.0);
+    return op == NORM_DISTANCE ? ceil_cut(M, cf) : ceil_cut(M, norm_sim_to_norm_dist(cf));
+}
+
 /* _distance cutoff of a distance-type chain (distance.hpp:52-64, 120-133, 240-262, 304-317) */
 RFG_HD bool dist_chain_cutoff(int op, u64 M, u64 ci, double cf, u64* K)
 {
@@ -876,8 +950,7 @@ RFG_HD bool dist_chain_cutoff(int op, u64 M, u64 ci, double cf, u64* K)
         if (ci > M) return false;
         *K = M - ci;
         return true;
-    case NORM_DISTANCE: *K = ceil_cut(M, cf); return true;
-    default: *K = ceil_cut(M, norm_sim_to_norm_dist(cf)); return true;
+    default: *K = norm_cut(op, M, cf, 0); return true;
     }
 }
 
@@ -886,32 +959,43 @@ RFG_HD bool dist_chain_cutoff(int op, u64 M, u64 ci, double cf, u64* K)
  * (K+1)/M >= c(1 - 2^-53) + 1/M exceeds c by far more than one rounding step (M < 2^33,
  * c <= 2), so the reference returns exactly 1.0 (normalized distance) or 0.0
  * (normalized similarity) -- taken here without the double division. */
+RFG_COLD double norm_finish(int op, u64 M, u64 d, double cf, u64 Kc)
+{
+    if (M != 0 && Kc != ~0ull && d > Kc && cf <= 2.0 && cf >= -2.0) return op == NORM_DISTANCE ? 1.0 : 0.0;
+    if (op == NORM_DISTANCE) {
+        const double nd = M != 0 ? ddiv((double)d, (double)M) : 0.0;
+        return nd <= cf ? nd : 1.0;
+    }
+    const double cs = norm_sim_to_norm_dist(cf);
+    double nd = M != 0 ? ddiv((double)d, (double)M) : 0.0;
+    nd = nd <= cs ? nd : 1.0;
+    const double ns = dsub(1.0, nd);
+    return ns >= cf ? ns : 0.0;
+}
+
 RFG_HD void dist_chain_finish(int op, u64 M, u64 d, u64 ci, double cf, i64* oi, double* of, u64 Kc = ~0ull)
 {
-    if (op >= NORM_DISTANCE && M != 0 && Kc != ~0ull && d > Kc && cf <= 2.0 && cf >= -2.0) {
-        *of = op == NORM_DISTANCE ? 1.0 : 0.0;
+    if (op == DISTANCE) {
+        *oi = (i64)d;
         return;
     }
-    switch (op) {
-    case DISTANCE: *oi = (i64)d; return;
-    case SIMILARITY: {
+    if (op == SIMILARITY) {
         const u64 s = M - d;
         *oi = s >= ci ? (i64)s : 0;
         return;
     }
-    case NORM_DISTANCE: {
-        const double nd = M != 0 ? ddiv((double)d, (double)M) : 0.0;
-        *of = nd <= cf ? nd : 1.0;
+    if (M != 0 && Kc != ~0ull && d > Kc && abs_le_bits(cf, 2.0)) {
+        *of = op == NORM_DISTANCE ? 1.0 : 0.0; /* the shortcut of norm_finish, integer tests only */
         return;
     }
-    default: {
-        const double cs = norm_sim_to_norm_dist(cf);
-        double nd = M != 0 ? ddiv((double)d, (double)M) : 0.0;
-        nd = nd <= cs ? nd : 1.0;
-        const double ns = dsub(1.0, nd);
-        *of = ns >= cf ? ns : 0.0;
-    }
-    }
+    *of = norm_finish(op, M, d, cf, Kc);
+}
+
+/* fuzz::ratio = indel_normalized_similarity(s1, s2, c / 100) * 100 (fuzz_impl.hpp:28-32) */
+RFG_COLD double ratio_finish(u64 M, u64 d, double cf_percent, u64 Kc)
+{
+    const double r = norm_finish(NORM_SIMILARITY, M, d, ddiv(cf_percent, 100.0), Kc);
+    return r == 0.0 ? 0.0 : dmul(r, 100.0);
 }
 
 /* Multi* chains (distance.hpp:421-460, 500-512, 552-563) over exact values */
@@ -1190,7 +1274,8 @@ RFG_HD Plan plan_int(const PairSpec& s)
         u64 K;
         const int op = s.metric == RATIO ? NORM_SIMILARITY : s.op;
         if (s.kd_pre != ~0ull && op >= NORM_DISTANCE) K = s.kd_pre;
-        else if (!dist_chain_cutoff(op, M, s.ci, s.metric == RATIO ? ddiv(s.cf, 100.0) : s.cf, &K)) {
+        else if (op >= NORM_DISTANCE) K = norm_cut(op, M, s.cf, s.metric == RATIO);
+        else if (!dist_chain_cutoff(op, M, s.ci, s.cf, &K)) {
             pl.run = 0;
             return pl;
         }
@@ -1217,13 +1302,13 @@ RFG_HD Plan plan_int(const PairSpec& s)
         case SIMILARITY: cs = s.ci; break;
         case DISTANCE: cs = M >= s.ci ? M - s.ci : 0; break;
         case NORM_DISTANCE: {
-            const u64 Kd = s.kd_pre != ~0ull ? s.kd_pre : ceil_cut(M, s.cf);
+            const u64 Kd = s.kd_pre != ~0ull ? s.kd_pre : norm_cut(NORM_DISTANCE, M, s.cf, 0);
             pl.Kchain = Kd;
             cs = M >= Kd ? M - Kd : 0;
             break;
         }
         default: {
-            const u64 Kd = s.kd_pre != ~0ull ? s.kd_pre : ceil_cut(M, norm_sim_to_norm_dist(s.cf));
+            const u64 Kd = s.kd_pre != ~0ull ? s.kd_pre : norm_cut(NORM_SIMILARITY, M, s.cf, 0);
             pl.Kchain = Kd;
             cs = M >= Kd ? M - Kd : 0;
         }
@@ -1304,8 +1389,6 @@ RFG_HD void finish_int(const PairSpec& s, const Plan& pl, i64 raw, i64* oi, doub
     case INDEL:
     case RATIO: {
         const u64 M = l1 + l2;
-        const int op = s.metric == RATIO ? NORM_SIMILARITY : s.op;
-        const double cf = s.metric == RATIO ? ddiv(s.cf, 100.0) : s.cf;
         if (!pl.run) {
             *oi = 0;
             return;
@@ -1313,10 +1396,9 @@ RFG_HD void finish_int(const PairSpec& s, const Plan& pl, i64 raw, i64* oi, doub
         const u64 K = pl.Kchain;
         u64 d = raw >= 0 ? M - 2 * (u64)raw : K + 1;
         d = d <= K ? d : K + 1;
-        double r = 0;
-        dist_chain_finish(op, M, d, s.ci, cf, oi, &r, K);
-        if (s.metric == RATIO) *of = r == 0.0 ? 0.0 : dmul(r, 100.0);
-        else *of = r;
+        if (s.metric == RATIO) /* |c| <= 200 percent implies c / 100 <= 2: ratio_finish's shortcut, inline */
+            *of = (M != 0 && d > K && abs_le_bits(s.cf, 200.0)) ? 0.0 : ratio_finish(M, d, s.cf, K);
+        else dist_chain_finish(s.op, M, d, s.ci, s.cf, oi, of, K);
         return;
     }
     case OSA: {
@@ -1397,6 +1479,7 @@ RFG_HD bool jaro_pair_needs_counts(const PairSpec& s, i64 prefix)
 #define RFG_JT_MAXT 256
 struct JaroTab {
     double jc[5];
+    double vfail[5]; /* the API result of a pair whose count stays below minc */
     unsigned short minc[5][RFG_JT_MAXT + 1];
 };
 
@@ -1443,7 +1526,12 @@ RFG_HD double finish_jaro_tab(const PairSpec& s, const JaroTab& t, i64 prefix, i
 
 RFG_HD void jaro_tab_head(JaroTab& t, const PairSpec& s)
 {
-    for (int p = 0; p < 5; ++p) t.jc[p] = jaro_tab_cutoff(s, p);
+    for (int p = 0; p < 5; ++p) {
+        t.jc[p] = jaro_tab_cutoff(s, p);
+        /* finish_jaro_tab with the inner Jaro at 0.0 (jaro_from_counts_tab's value below minc) */
+        const double sim = s.metric == JARO ? 0.0 : jw_finish(0.0, p, s.p.prefix_weight, fsim_chain_cutoff(s.op, s.cf));
+        t.vfail[p] = s.op == SIMILARITY ? sim : fsim_chain_finish(s.op, sim, s.cf);
+    }
 }
 
 RFG_HD double finish_jaro(const PairSpec& s, i64 prefix, i64 common, i64 transp)

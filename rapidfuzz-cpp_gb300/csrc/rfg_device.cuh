@@ -67,6 +67,10 @@ struct KParams {
     int64_t scratch_per_thread; /* u64 words of each thread's state */
     int wmax;                   /* pattern words of the generic class */
     int pm_smem;                /* 1: the generic pattern table lives in dynamic shared memory */
+    /* dense tiles: results of each window of `stage` choice positions (one length-sorted
+     * run of the permutation) gather in shared memory and leave as coalesced row
+     * segments; 0 = store each result where it belongs */
+    int64_t stage;
 };
 
 /* ----------------------------------------------------------------- helpers */
@@ -152,13 +156,15 @@ struct TextRows {
     }
 };
 
+static __device__ __noinline__ double int_result_as_double(i64 v) { return (double)v; }
+
 __device__ __forceinline__ void store_result(const KParams& a, int64_t q, int64_t c, i64 vi, double vf, bool is_int)
 {
     const int64_t idx = q * a.ld + c;
     switch (a.out_dtype) {
     case 0: ((int32_t*)a.out)[idx] = (int32_t)vi; break;
     case 1: ((int64_t*)a.out)[idx] = vi; break;
-    default: ((double*)a.out)[idx] = is_int ? (double)vi : vf;
+    default: ((double*)a.out)[idx] = is_int ? int_result_as_double(vi) : vf;
     }
 }
 
@@ -335,16 +341,42 @@ __device__ __forceinline__ bool tile_hopeless(const KParams& a, int64_t qi, int 
 
 /* dense store, or the extract list */
 __device__ __forceinline__ void emit(const KParams& a, int64_t qi, int64_t ci, i64 vi, double vf, bool is_int,
-                                     u64 cut_i, double cut_f, TopList<false>* tl)
+                                     u64 cut_i, double cut_f, TopList<false>* tl, unsigned char* stage = nullptr,
+                                     int64_t s0 = 0)
 {
     (void)cut_i;
     (void)cut_f;
     (void)tl;
+    if (stage) {
+        const int64_t i = ci - s0;
+        switch (a.out_dtype) {
+        case 0: ((int32_t*)stage)[i] = (int32_t)vi; break;
+        case 1: ((int64_t*)stage)[i] = vi; break;
+        default: ((double*)stage)[i] = is_int ? int_result_as_double(vi) : vf;
+        }
+        return;
+    }
     store_result(a, qi, ci, vi, vf, is_int);
 }
 
+/* one window's staged results to out[qi][s0, s1), consecutive threads on consecutive
+ * elements */
+__device__ __forceinline__ void flush_stage(const KParams& a, const unsigned char* stage, int64_t qi, int64_t s0,
+                                            int64_t s1)
+{
+    const int64_t n = s1 - s0, base = qi * a.ld + s0;
+    if (a.out_dtype == 0) {
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) ((int32_t*)a.out)[base + i] = ((const int32_t*)stage)[i];
+    }
+    else {
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
+            ((unsigned long long*)a.out)[base + i] = ((const unsigned long long*)stage)[i];
+    }
+}
+
 __device__ __forceinline__ void emit(const KParams& a, int64_t qi, int64_t ci, i64 vi, double vf, bool is_int,
-                                     u64 cut_i, double cut_f, TopList<true>* tl)
+                                     u64 cut_i, double cut_f, TopList<true>* tl, unsigned char* = nullptr,
+                                     int64_t = 0)
 {
     if (passes(is_int, a.better_high, vi, vf, cut_i, cut_f))
         top_insert(*tl, a.topk, score_key(is_int, vi, vf, a.better_high), ci, a.tie_last);
@@ -428,7 +460,8 @@ __device__ __noinline__ void build_len_tab(const KParams& a, int m, LenTab& t)
 
 template <int FAM, int W, typename CT, bool TOPK>
 __device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, const u64* keys, int64_t qi, int m,
-                                           const u64* qpre, int64_t ci, TopList<TOPK>* tl, const LenTab& lt)
+                                           const u64* qpre, int64_t ci, TopList<TOPK>* tl, const LenTab& lt,
+                                           unsigned char* stage, int64_t s0)
 {
     const int64_t o0 = a.c.off[ci], o1 = a.c.off[ci + 1];
     const int n = (int)(o1 - o0);
@@ -455,23 +488,28 @@ __device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, co
             if ((u64)__ldg(s2 + prefix) != qpre[prefix]) break;
         int common = 0, transp = 0;
         if (uses_jaro_tab(a) && n <= a.tab_t && !TOPK) {
-            /* the table decides which pairs need counts and whether they can pass */
+            /* the table decides which pairs need counts and whether they can pass; a pair
+             * whose common count stays below minc takes the precomputed failing value */
             const unsigned short mc = lt.jt.minc[prefix][n];
             const int cmax = m < n ? m : n;
-            if (mc != 0 && ((mc != 0xffff && cmax >= (int)mc) || (m == 1 && n == 1))) {
+            const bool one = m == 1 && n == 1;
+            bool fail = mc != 0 && !one && (mc == 0xffff || cmax < (int)mc);
+            if (mc != 0 && !fail) {
+                const int need = one ? 0 : (int)mc;
                 if (W == 1) {
                     int bound = (m > n ? m : n) / 2;
                     if (bound > 0) --bound;
                     const int te = n < m + bound ? n : m + bound;
-                    if (te <= 64) jaro_word(pm, m, txt, n, &common, &transp);
+                    if (te <= 64) jaro_word(pm, m, txt, n, &common, &transp, need);
                     else jaro_multi<1>(pm, m, txt, n, &common, &transp);
                 }
                 else {
                     jaro_multi<W>(pm, m, txt, n, &common, &transp);
                 }
+                fail = common < need;
             }
-            vf = finish_jaro_tab(s, lt.jt, prefix, common, transp);
-            emit(a, qi, ci, 0, vf, false, s.ci, s.cf, tl);
+            vf = fail ? lt.jt.vfail[prefix] : finish_jaro_tab(s, lt.jt, prefix, common, transp);
+            emit(a, qi, ci, 0, vf, false, s.ci, s.cf, tl, stage, s0);
             return;
         }
         if (m > 0 && n > 0 && jaro_pair_needs_counts(s, prefix)) {
@@ -487,7 +525,7 @@ __device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, co
             }
         }
         vf = finish_jaro(s, prefix, common, transp);
-        emit(a, qi, ci, 0, vf, false, s.ci, s.cf, tl);
+        emit(a, qi, ci, 0, vf, false, s.ci, s.cf, tl, stage, s0);
         return;
     }
     if (!TOPK && n <= a.tab_t && uses_kd_tab(a)) s.kd_pre = lt.kd[n];
@@ -495,7 +533,7 @@ __device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, co
     i64 raw = 0;
     if (pl.run) raw = run_int_core<FAM, W>(pm, m, txt, n, pl.K);
     finish_int(s, pl, raw, &vi, &vf);
-    emit(a, qi, ci, vi, vf, is_int, s.ci, s.cf, tl);
+    emit(a, qi, ci, vi, vf, is_int, s.ci, s.cf, tl, stage, s0);
 }
 
 /* -------------------------------------------------------------- the kernel */
@@ -548,10 +586,19 @@ __global__ void __launch_bounds__(256) k_tiles(const KParams a)
          * pairs of similar work and pairs decided by the length filter cluster into
          * whole warps */
         const bool skip = TOPK && tile_hopeless(a, qi, m, ch);
-        if (!skip)
-            for (int64_t p = c0 + threadIdx.x; p < c1; p += blockDim.x)
+        unsigned char* stage = (!TOPK && a.stage) ? (unsigned char*)(keys + a.hcap) : nullptr;
+        const int64_t win = stage ? a.stage : c1 - c0;
+        for (int64_t s0 = c0; s0 < c1 && !skip; s0 += win) {
+            const int64_t s1 = s0 + win < c1 ? s0 + win : c1;
+            for (int64_t p = s0 + threadIdx.x; p < s1; p += blockDim.x)
                 score_pair<FAM, W, CT, TOPK>(a, rows, keys, qi, m, s_qpre, a.perm ? (int64_t)__ldg(a.perm + p) : p,
-                                             &tl, s_lt);
+                                             &tl, s_lt, stage, s0);
+            if (stage) {
+                __syncthreads();
+                flush_stage(a, stage, qi, s0, s1);
+                __syncthreads();
+            }
+        }
         if constexpr (TOPK) flush_topk(a, qi, ch, tl);
         __syncthreads();
     }
