@@ -19,7 +19,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -60,11 +62,16 @@ rfg_status fail(rfg_status s, const char* fmt, ...)
         if (s_ != RFG_OK) return s_;         \
     } while (0)
 
+#define RFG_COUNTERS 64
+#define RFG_MAX_ROW_BLOCKS 12
+
 struct Ctx {
     bool init = false;
     int device = 0;
     int sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy = nullptr; /* device-to-host result copies overlapping the next row block */
+    cudaEvent_t blk_ev[RFG_MAX_ROW_BLOCKS] = {};
     std::recursive_mutex mu;
     std::unordered_map<const void*, int> occ; /* (kernel) -> CTAs per SM at the default smem */
 };
@@ -81,6 +88,8 @@ rfg_status ensure_ctx()
     RFG_CUDA(cudaSetDevice(g.device));
     RFG_CUDA(cudaDeviceGetAttribute(&g.sms, cudaDevAttrMultiProcessorCount, g.device));
     RFG_CUDA(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+    RFG_CUDA(cudaStreamCreateWithFlags(&g.copy, cudaStreamNonBlocking));
+    for (auto& e : g.blk_ev) RFG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     cudaMemPool_t pool;
     RFG_CUDA(cudaDeviceGetDefaultMemPool(&pool, g.device));
     uint64_t thr = UINT64_MAX;
@@ -224,8 +233,13 @@ rfg_status check_params(int metric, const ScoreParams& sp)
 
 int occupancy(const void* fn, int block, size_t smem)
 {
+    static std::map<std::tuple<const void*, int, size_t>, int> cache;
+    const auto key = std::make_tuple(fn, block, smem);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, block, smem) != cudaSuccess || nb < 1) nb = 1;
+    cache[key] = nb;
     return nb;
 }
 
@@ -259,6 +273,8 @@ struct BatchSpec {
     int64_t fixed_chunk = 0;
     const int32_t* chunk_lmin = nullptr;
     const int32_t* chunk_lmax = nullptr;
+    /* split the queries into this many contiguous row blocks (host-output pipelining) */
+    int row_blocks = 1;
 };
 
 inline bool better_high_of(int op) { return op == RFG_SIMILARITY || op == RFG_NORMALIZED_SIMILARITY; }
@@ -276,6 +292,7 @@ struct LaunchRec {
     int block;
     size_t smem;
     KParams a;
+    int rblock; /* row block (a contiguous range of queries) the launch belongs to */
 };
 
 struct Prepared {
@@ -285,6 +302,22 @@ struct Prepared {
     int* err = nullptr;
     int64_t scratch_words = 0;
     int64_t chunk = 0, nchunks = 0;
+    /* query rows of each row block; a host-output cdist copies block b while block b+1
+     * computes */
+    std::vector<std::pair<int64_t, int64_t>> rows;
+    /* the class launches of one batch are independent: launches 1.. run on side streams
+     * forked from and joined back into the caller's stream (graph capture records the
+     * same fork/join as parallel branches) */
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> ev; /* [0] fork, [1..] joins */
+    Prepared() = default;
+    Prepared(const Prepared&) = delete;
+    Prepared& operator=(const Prepared&) = delete;
+    ~Prepared()
+    {
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+        for (cudaStream_t s : side) cudaStreamDestroy(s);
+    }
     void free_on(cudaStream_t st)
     {
         qlist.free_on = small.free_on = scratch[0].free_on = perm.free_on = st;
@@ -339,44 +372,72 @@ void chunk_length_order(const std::vector<int32_t>& len, int64_t chunk, std::vec
     }
 }
 
+/* query indices (ascending) -> longest first, ties in index order; counting sort when the
+ * length range is small */
+void sort_by_length_desc(std::vector<int32_t>* v, const std::vector<int64_t>& len)
+{
+    const size_t n = v->size();
+    if (n < 2) return;
+    int64_t lo = INT64_MAX, hi = 0;
+    for (int32_t i : *v) {
+        lo = std::min(lo, len[i]);
+        hi = std::max(hi, len[i]);
+    }
+    if (hi - lo > (int64_t)(4 * n + 1024)) {
+        std::stable_sort(v->begin(), v->end(), [&](int32_t a, int32_t b) { return len[a] > len[b]; });
+        return;
+    }
+    std::vector<int32_t> count(hi - lo + 2, 0), out(n);
+    for (int32_t i : *v) ++count[hi - len[i] + 1];
+    for (size_t k = 1; k < count.size(); ++k) count[k] += count[k - 1];
+    for (int32_t i : *v) out[count[hi - len[i]]++] = i;
+    v->swap(out);
+}
+
 rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& spec, Prepared* pb,
                          const int64_t* host_choice_off = nullptr)
 {
     const int64_t nq = q.dev.n, nc = c.n;
-    RFG_TRY(pb->small.alloc(16 * sizeof(int)));
+    RFG_TRY(pb->small.alloc(RFG_COUNTERS * sizeof(int)));
     pb->counters = pb->small.as<int>();
-    pb->err = pb->counters + 15;
+    pb->err = pb->counters + RFG_COUNTERS - 1;
     if (nq == 0 || nc == 0) return RFG_OK;
     const int fam = metric_family(spec.metric, spec.form, spec.sp);
 
-    /* classes: 1, 2, 4, 8 register words; index 4 = any length */
-    std::vector<int32_t> cls[5];
-    int64_t cls_maxlen[5] = {0, 0, 0, 0, 0};
-    int32_t cls_wide[5] = {0, 0, 0, 0, 0};
-    for (int64_t i = 0; i < nq; ++i) {
-        int k;
-        if (fam == FAM_WF || fam == FAM_NONE) k = 4;
-        else {
-            const int wc = word_class(q.len[i]);
-            k = wc == 1 ? 0 : wc == 2 ? 1 : wc == 4 ? 2 : wc == 8 ? 3 : 4;
+    /* row blocks: contiguous query ranges, each with its own launches */
+    const int64_t R = std::max<int64_t>(1, std::min<int64_t>({(int64_t)spec.row_blocks, RFG_MAX_ROW_BLOCKS, nq}));
+    const int64_t rb = (nq + R - 1) / R;
+    for (int64_t b = 0; b < R; ++b) pb->rows.emplace_back(b * rb, std::min(nq, (b + 1) * rb));
+    const int64_t nblk = (int64_t)pb->rows.size();
+
+    /* classes: 1, 2, 4, 8 register words; index 4 = any length; one set per row block */
+    std::vector<std::vector<int32_t>> cls(nblk * 5);
+    std::vector<int64_t> cls_maxlen(nblk * 5, 0);
+    std::vector<int32_t> cls_wide(nblk * 5, 0);
+    for (int64_t b = 0; b < nblk; ++b)
+        for (int64_t i = pb->rows[b].first; i < pb->rows[b].second; ++i) {
+            int k;
+            if (fam == FAM_WF || fam == FAM_NONE) k = 4;
+            else {
+                const int wc = word_class(q.len[i]);
+                k = wc == 1 ? 0 : wc == 2 ? 1 : wc == 4 ? 2 : wc == 8 ? 3 : 4;
+            }
+            const int64_t bk = b * 5 + k;
+            cls[bk].push_back((int32_t)i);
+            cls_maxlen[bk] = std::max(cls_maxlen[bk], q.len[i]);
+            cls_wide[bk] = std::max(cls_wide[bk], q.wide[i]);
         }
-        cls[k].push_back((int32_t)i);
-        cls_maxlen[k] = std::max(cls_maxlen[k], q.len[i]);
-        cls_wide[k] = std::max(cls_wide[k], q.wide[i]);
-    }
     size_t total = 0;
     for (auto& v : cls) {
-        std::sort(v.begin(), v.end(), [&](int32_t a, int32_t b) {
-            return q.len[a] != q.len[b] ? q.len[a] > q.len[b] : a < b;
-        });
+        sort_by_length_desc(&v, q.len);
         total += v.size();
     }
     std::vector<int32_t> qall;
     qall.reserve(total);
-    size_t cls_off[5];
-    for (int k = 0; k < 5; ++k) {
-        cls_off[k] = qall.size();
-        qall.insert(qall.end(), cls[k].begin(), cls[k].end());
+    std::vector<size_t> cls_off(nblk * 5);
+    for (int64_t bk = 0; bk < nblk * 5; ++bk) {
+        cls_off[bk] = qall.size();
+        qall.insert(qall.end(), cls[bk].begin(), cls[bk].end());
     }
     RFG_TRY(pb->qlist.alloc(qall.size() * 4));
     RFG_CUDA(cudaMemcpyAsync(pb->qlist.p, qall.data(), qall.size() * 4, cudaMemcpyHostToDevice, g.stream));
@@ -389,12 +450,11 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
     if (spec.fixed_perm) {
         chunk = spec.fixed_chunk;
         dperm = spec.fixed_perm;
-        RFG_CUDA(cudaStreamSynchronize(g.stream)); /* qall is a host temporary */
     }
     else {
         const int64_t target_all = g_tiles_target > 0 ? g_tiles_target : (int64_t)g.sms * 32;
         const int blk = g_block_override > 0 ? g_block_override : 256;
-        chunk = (nc * nq + target_all - 1) / target_all;
+        chunk = (nc * rb + target_all - 1) / target_all;
         chunk = std::max<int64_t>(chunk, blk);
         chunk = std::min<int64_t>(chunk, std::max<int64_t>(nc, 1));
         chunk = (chunk + blk - 1) / blk * blk;
@@ -410,7 +470,8 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         chunk_length_order(clen, stage ? stage : chunk, &perm);
         RFG_TRY(pb->perm.alloc((size_t)nc * 4));
         RFG_CUDA(cudaMemcpyAsync(pb->perm.p, perm.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, g.stream));
-        RFG_CUDA(cudaStreamSynchronize(g.stream)); /* perm / qall are host temporaries */
+        /* qall and perm are host temporaries: an asynchronous copy from pageable memory
+         * returns once the source has been staged, so they may go out of scope */
         dperm = pb->perm.as<int32_t>();
     }
     pb->chunk = chunk;
@@ -418,15 +479,18 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
     const bool topk = spec.topk > 0;
     const int64_t max_choice_len = spec.fixed_perm ? RFG_JT_MAXT : host_max_choice_len;
 
-    for (int k = 0; k < 5; ++k) {
-        if (cls[k].empty()) continue;
+    std::vector<size_t> generic_recs;
+    size_t scratch_bytes = 0;
+    for (int64_t bk = 0; bk < nblk * 5; ++bk) {
+        const int k = (int)(bk % 5);
+        if (cls[bk].empty()) continue;
         KParams a;
         memset(&a, 0, sizeof a);
         a.q = q.dev;
         a.c = c;
-        a.qlist = pb->qlist.as<int32_t>() + cls_off[k];
-        a.nq = (int32_t)cls[k].size();
-        a.counter = pb->counters + k;
+        a.qlist = pb->qlist.as<int32_t>() + cls_off[bk];
+        a.nq = (int32_t)cls[bk].size();
+        a.counter = pb->counters + bk;
         a.err = pb->err;
         a.metric = spec.metric;
         a.op = spec.op;
@@ -438,7 +502,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         a.out_dtype = spec.out_dtype;
         a.ld = spec.ld;
         const bool needs_table = fam != FAM_WF && fam != FAM_NONE;
-        a.hcap = (needs_table && c.width > 1 && cls_wide[k] > 0) ? next_pow2(2 * cls_wide[k]) : 0;
+        a.hcap = (needs_table && c.width > 1 && cls_wide[bk] > 0) ? next_pow2(2 * cls_wide[bk]) : 0;
 
         const void* fn;
         int block;
@@ -464,7 +528,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         else {
             fn = generic_kernel(fam == FAM_NONE ? FAM_WF : fam, c.width, topk);
             block = 128;
-            const int wmax = (fam == FAM_WF || fam == FAM_NONE) ? 0 : (int)((cls_maxlen[k] + 63) / 64);
+            const int wmax = (fam == FAM_WF || fam == FAM_NONE) ? 0 : (int)((cls_maxlen[bk] + 63) / 64);
             const size_t table = wmax ? ((size_t)(256 + a.hcap + 1) * wmax + a.hcap) * 8 : 0;
             if (table > 0 && table <= 100 * 1024) {
                 /* pattern table in shared memory; per-thread state stays in scratch */
@@ -477,7 +541,17 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         }
         /* tiles: (query, chunk), longest queries first; persistent CTAs fill every SM */
         const int64_t slots = (int64_t)g.sms * per_sm;
-        a.chunk = chunk;
+        int64_t cchunk = chunk;
+        if (k == 4 && !topk) {
+            /* the any-length class has few, heavy queries: smaller tiles so that every
+             * resident CTA gets work (no locality is needed here: results go straight out) */
+            const int64_t want = slots * 4;
+            int64_t cc = ((int64_t)cls[bk].size() * nc + want - 1) / want;
+            cc = std::max<int64_t>(cc, block);
+            cc = (cc + block - 1) / block * block;
+            cchunk = std::min(chunk, cc);
+        }
+        a.chunk = cchunk;
         a.perm = dperm;
         a.topk = spec.topk;
         a.tie_last = spec.tie_last;
@@ -488,42 +562,79 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         a.chunk_lmin = spec.chunk_lmin;
         a.chunk_lmax = spec.chunk_lmax;
         a.tab_t = (int)std::min<int64_t>(RFG_JT_MAXT, max_choice_len);
-        a.nchunks = (nc + chunk - 1) / chunk;
+        a.nchunks = (nc + cchunk - 1) / cchunk;
         const int64_t ntiles = (int64_t)a.nq * a.nchunks;
         if (ntiles > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "batch too large for one launch");
         const int64_t grid = std::min<int64_t>(ntiles, slots);
         if (k == 4) {
             /* any-length kernel: pattern table + per-thread state in global scratch */
-            const int wmax = (fam == FAM_WF || fam == FAM_NONE) ? 0 : (int)((cls_maxlen[k] + 63) / 64);
+            const int wmax = (fam == FAM_WF || fam == FAM_NONE) ? 0 : (int)((cls_maxlen[bk] + 63) / 64);
             int64_t per_thread;
             switch (fam) {
             case FAM_LEV: per_thread = 2 * (int64_t)wmax; break;
             case FAM_LCS: per_thread = wmax; break;
             case FAM_OSA: per_thread = 4 * (int64_t)wmax; break;
             case FAM_JARO: per_thread = 2 * (int64_t)wmax; break;
-            default: per_thread = cls_maxlen[k] + 1;
+            default: per_thread = cls_maxlen[bk] + 1;
             }
             a.wmax = wmax;
             a.scratch_per_thread = per_thread;
             a.scratch_per_cta = (wmax && !a.pm_smem ? (int64_t)(256 + a.hcap + 1) * wmax + a.hcap : 0) +
                                 (int64_t)block * per_thread;
-            RFG_TRY(pb->scratch[0].alloc((size_t)grid * a.scratch_per_cta * 8));
-            pb->scratch_words = grid * a.scratch_per_cta;
-            a.scratch = pb->scratch[0].as<u64>();
+            /* row blocks run one after another: their any-length launches share one region */
+            scratch_bytes = std::max(scratch_bytes, (size_t)grid * a.scratch_per_cta * 8);
+            generic_recs.push_back(pb->launches.size());
         }
-        pb->launches.push_back(LaunchRec{fn, (unsigned)grid, block, smem, a});
+        pb->launches.push_back(LaunchRec{fn, (unsigned)grid, block, smem, a, (int)(bk / 5)});
+    }
+    if (!generic_recs.empty()) {
+        RFG_TRY(pb->scratch[0].alloc(scratch_bytes));
+        pb->scratch_words = (int64_t)(scratch_bytes / 8);
+        for (size_t i : generic_recs) pb->launches[i].a.scratch = pb->scratch[0].as<u64>();
     }
     return RFG_OK;
 }
 
-rfg_status enqueue_batch(const Prepared& pb, cudaStream_t st)
+/* the launches of row block b, forked over side streams and joined back into st */
+rfg_status enqueue_block(Prepared& pb, int b, cudaStream_t st)
 {
-    RFG_CUDA(cudaMemsetAsync(pb.counters, 0, 16 * sizeof(int), st));
-    for (const LaunchRec& L : pb.launches) {
+    std::vector<const LaunchRec*> ls;
+    for (const LaunchRec& L : pb.launches)
+        if (L.rblock == b) ls.push_back(&L);
+    const size_t nl = ls.size();
+    if (nl > 1 && pb.side.size() < nl - 1) {
+        while (pb.side.size() < nl - 1) {
+            cudaStream_t x;
+            RFG_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+            pb.side.push_back(x);
+        }
+        while (pb.ev.size() < nl) {
+            cudaEvent_t e;
+            RFG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            pb.ev.push_back(e);
+        }
+    }
+    if (nl > 1) RFG_CUDA(cudaEventRecord(pb.ev[0], st));
+    for (size_t i = 0; i < nl; ++i) {
+        const LaunchRec& L = *ls[i];
+        cudaStream_t s = st;
+        if (i > 0) {
+            s = pb.side[i - 1];
+            RFG_CUDA(cudaStreamWaitEvent(s, pb.ev[0], 0));
+        }
         KParams a = L.a;
         void* args[] = {&a};
-        RFG_CUDA(cudaLaunchKernel(L.fn, dim3(L.grid), dim3(L.block), args, L.smem, st));
+        RFG_CUDA(cudaLaunchKernel(L.fn, dim3(L.grid), dim3(L.block), args, L.smem, s));
+        if (i > 0) RFG_CUDA(cudaEventRecord(pb.ev[i], s));
     }
+    for (size_t i = 1; i < nl; ++i) RFG_CUDA(cudaStreamWaitEvent(st, pb.ev[i], 0));
+    return RFG_OK;
+}
+
+rfg_status enqueue_batch(Prepared& pb, cudaStream_t st)
+{
+    RFG_CUDA(cudaMemsetAsync(pb.counters, 0, RFG_COUNTERS * sizeof(int), st));
+    for (size_t b = 0; b < std::max<size_t>(pb.rows.size(), 1); ++b) RFG_TRY(enqueue_block(pb, (int)b, st));
     return RFG_OK;
 }
 
@@ -611,17 +722,33 @@ rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const 
     spec.out_dtype = dt;
     spec.ld = ld;
     const size_t esz = dtype_size(dt);
-    if (flags & RFG_DEVICE_OUTPUT) spec.out = out;
-    else {
-        RFG_TRY(od.alloc((size_t)nq * ld * esz));
-        spec.out = od.p;
+    if (flags & RFG_DEVICE_OUTPUT) {
+        spec.out = out;
+        return run_batch(qs, ck, spec, dev_in ? nullptr : C->offsets);
     }
-    RFG_TRY(run_batch(qs, ck, spec, dev_in ? nullptr : C->offsets));
-    if (!(flags & RFG_DEVICE_OUTPUT) && nq * nc) {
-        RFG_CUDA(cudaMemcpy2DAsync(out, ld * esz, od.p, ld * esz, nc * esz, nq, cudaMemcpyDeviceToHost, g.stream));
-        RFG_CUDA(cudaStreamSynchronize(g.stream));
+    RFG_TRY(od.alloc((size_t)nq * ld * esz));
+    spec.out = od.p;
+    /* host results: row blocks of about 16 MB, block b copied out while b+1 computes */
+    const size_t bytes = (size_t)nq * ld * esz;
+    spec.row_blocks = (int)std::min<size_t>(8, std::max<size_t>(1, bytes / (16u << 20)));
+    Prepared pb;
+    struct CopyJoin { /* the copies end before od and pb are released, on every path */
+        ~CopyJoin() { cudaStreamSynchronize(g.copy); }
+    } join;
+    RFG_TRY(prepare_batch(qs, ck, spec, &pb, dev_in ? nullptr : C->offsets));
+    RFG_CUDA(cudaMemsetAsync(pb.counters, 0, RFG_COUNTERS * sizeof(int), g.stream));
+    for (size_t b = 0; b < pb.rows.size(); ++b) {
+        RFG_TRY(enqueue_block(pb, (int)b, g.stream));
+        const int64_t r0 = pb.rows[b].first, r1 = pb.rows[b].second;
+        if (r1 <= r0 || nc == 0) continue;
+        RFG_CUDA(cudaEventRecord(g.blk_ev[b], g.stream));
+        RFG_CUDA(cudaStreamWaitEvent(g.copy, g.blk_ev[b], 0));
+        RFG_CUDA(cudaMemcpy2DAsync((char*)out + (size_t)r0 * ld * esz, ld * esz,
+                                   (const char*)od.p + (size_t)r0 * ld * esz, ld * esz, nc * esz, r1 - r0,
+                                   cudaMemcpyDeviceToHost, g.copy));
     }
-    return RFG_OK;
+    RFG_CUDA(cudaStreamSynchronize(g.copy));
+    return check_batch(pb, g.stream);
 }
 
 /* one pair through the engine */

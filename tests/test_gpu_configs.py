@@ -75,3 +75,19 @@ def test_config4_shape_tokens_u32():
         exp = oracle_cdist(m, R.SIMILARITY, q, c, cut)
         assert _same(got, exp), m
     assert (got >= 0).all()
+
+
+def test_host_output_row_blocks_match_oracle():
+    """Host results larger than 32 MB leave in row blocks copied while the next block
+    computes; rows on both sides of every block boundary must equal the oracle"""
+    q, c = WL.cdist_zipf(seed=9, nq=4096, nc=2200)
+    got = R.cdist(R.LEVENSHTEIN, R.DISTANCE, q, c, 8, out_dtype=R.I32)          # 36 MB: 2 blocks
+    rows = [0, 1, 2047, 2048, 2049, 4095]
+    exp = oracle_cdist(R.LEVENSHTEIN, R.DISTANCE, _rows(q, rows), c, 8, out_dtype=0)
+    assert _same(got[rows], exp)
+    got = R.cdist(R.INDEL, R.NORMALIZED_SIMILARITY, q, c, 0.7)                    # 72 MB float64: 4 blocks
+    rows = [0, 1023, 1024, 2047, 2048, 3071, 3072, 4095]
+    exp = oracle_cdist(R.INDEL, R.NORMALIZED_SIMILARITY, _rows(q, rows), c, 0.7)
+    assert _same(got[rows], exp)
+    dev = R.cdist(R.INDEL, R.NORMALIZED_SIMILARITY, _rows(q, rows), c, 0.7)
+    assert _same(dev, exp)
