@@ -13,6 +13,7 @@ OBJ = os.path.join(PKG, "_build")
 LIB_DIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIB_DIR, "librapidfuzz_gb300.so")
 PEAK_LIB = os.path.join(LIB_DIR, "librfg_peak.so")  # INT32 issue-rate microbenchmark (bench roofline)
+COUNT_LIB = os.path.join(LIB_DIR, "librfg_count.so")  # executed word steps of the kernels (bench roofline)
 
 SOURCES = ["rfg_api.cu", "rfg_k_lev.cu", "rfg_k_lcs.cu", "rfg_k_osa.cu", "rfg_k_jaro.cu", "rfg_k_generic.cu", "rfg_noalloc.cu", "rfg_server.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -42,7 +43,7 @@ def _compile(src):
 
 def build(force=False, verbose=False):
     """Compile the library if any source is newer than it; returns the .so path."""
-    if not force and os.path.exists(LIB) and os.path.exists(PEAK_LIB):
+    if not force and all(os.path.exists(x) for x in (LIB, PEAK_LIB, COUNT_LIB)):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in _deps()):
             return LIB
@@ -60,6 +61,11 @@ def build(force=False, verbose=False):
                                           os.path.join(CSRC, "rfg_peak.cu")], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("peak benchmark build failed:\n%s%s" % (r.stdout, r.stderr))
+    cxx = shutil.which("g++") or "g++"
+    r = subprocess.run([cxx, "-O3", "-std=c++17", "-fPIC", "-shared", "-pthread", "-ffp-contract=off", "-I" + CSRC,
+                        "-o", COUNT_LIB, os.path.join(CSRC, "rfg_count.cpp")], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("work counter build failed:\n%s%s" % (r.stdout, r.stderr))
     if verbose:
         print("built", LIB)
     return LIB

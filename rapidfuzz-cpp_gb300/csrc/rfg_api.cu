@@ -72,6 +72,7 @@ struct Ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t copy = nullptr; /* device-to-host result copies overlapping the next row block */
     cudaEvent_t blk_ev[RFG_MAX_ROW_BLOCKS] = {};
+    cudaEvent_t prep_ev = nullptr; /* end of a preparation on `stream`, for launches on other streams */
     std::recursive_mutex mu;
     std::unordered_map<const void*, int> occ; /* (kernel) -> CTAs per SM at the default smem */
 };
@@ -90,6 +91,7 @@ rfg_status ensure_ctx()
     RFG_CUDA(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
     RFG_CUDA(cudaStreamCreateWithFlags(&g.copy, cudaStreamNonBlocking));
     for (auto& e : g.blk_ev) RFG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    RFG_CUDA(cudaEventCreateWithFlags(&g.prep_ev, cudaEventDisableTiming));
     cudaMemPool_t pool;
     RFG_CUDA(cudaDeviceGetDefaultMemPool(&pool, g.device));
     uint64_t thr = UINT64_MAX;
@@ -562,6 +564,13 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         a.chunk_lmin = spec.chunk_lmin;
         a.chunk_lmax = spec.chunk_lmax;
         a.tab_t = (int)std::min<int64_t>(RFG_JT_MAXT, max_choice_len);
+        if (spec.form != RFG_FORM_MULTI && spec.op == RFG_DISTANCE &&
+            ((spec.metric == RFG_LEVENSHTEIN && fam == FAM_LEV && spec.sp.ins == 1 && spec.sp.del == 1 &&
+              spec.sp.rep == 1) ||
+             spec.metric == RFG_INDEL || spec.metric == RFG_OSA)) {
+            a.fast = 1;
+            a.fast_k = clamp_bound(spec.ci);
+        }
         a.nchunks = (nc + cchunk - 1) / cchunk;
         const int64_t ntiles = (int64_t)a.nq * a.nchunks;
         if (ntiles > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "batch too large for one launch");
@@ -1141,7 +1150,12 @@ rfg_status extract_enqueue(rfg_corpus c, const QuerySet& q, int metric, int op, 
     spec.fixed_chunk = c->chunk;
     spec.chunk_lmin = c->lmin.as<int32_t>();
     spec.chunk_lmax = c->lmax.as<int32_t>();
-    RFG_TRY(prepare_batch(q, c->dev, spec, &job->pb)); /* synchronises the library stream */
+    RFG_TRY(prepare_batch(q, c->dev, spec, &job->pb));
+    if (st != g.stream) {
+        /* uploads, resets and the tile lists were enqueued on the library stream */
+        RFG_CUDA(cudaEventRecord(g.prep_ev, g.stream));
+        RFG_CUDA(cudaStreamWaitEvent(st, g.prep_ev, 0));
+    }
     RFG_TRY(enqueue_batch(job->pb, st));
     const int is_int = is_int_result(metric, op);
     const int bh = better_high_of(op);

@@ -1263,7 +1263,7 @@ RFG_HD Plan plan_int(const PairSpec& s)
         switch (lev_mode(s.p)) {
         case LEV_ZERO: pl.run = 0; break;
         case LEV_UNIFORM:
-        case LEV_INDEL: pl.K = clamp_bound(ceil_div_u(Kw, (u64)s.p.ins)); break;
+        case LEV_INDEL: pl.K = clamp_bound(s.p.ins == 1 ? Kw : ceil_div_u(Kw, (u64)s.p.ins)); break;
         default: pl.K = clamp_bound(Kw);
         }
         return pl;

@@ -71,6 +71,10 @@ struct KParams {
      * run of the permutation) gather in shared memory and leave as coalesced row
      * segments; 0 = store each result where it belongs */
     int64_t stage;
+    /* 1: distance with unit weights (Levenshtein 1/1/1, Indel, OSA; free or cached form):
+     * the whole chain is d <= K ? d : K + 1 with K = fast_k (the cutoff clamped to 2^62-1) */
+    int fast;
+    i64 fast_k;
 };
 
 /* ----------------------------------------------------------------- helpers */
@@ -528,6 +532,14 @@ __device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, co
         emit(a, qi, ci, 0, vf, false, s.ci, s.cf, tl, stage, s0);
         return;
     }
+    if (!TOPK && a.fast) {
+        const i64 K = a.fast_k;
+        const i64 raw = run_int_core<FAM, W>(pm, m, txt, n, K);
+        i64 d = raw;
+        if (FAM == FAM_LCS) d = raw >= 0 ? (i64)m + n - 2 * raw : K + 1;
+        emit(a, qi, ci, d <= K ? d : K + 1, 0.0, true, s.ci, s.cf, tl, stage, s0);
+        return;
+    }
     if (!TOPK && n <= a.tab_t && uses_kd_tab(a)) s.kd_pre = lt.kd[n];
     const Plan pl = plan_int(s);
     i64 raw = 0;
@@ -538,8 +550,28 @@ __device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, co
 
 /* -------------------------------------------------------------- the kernel */
 
+/* resident 256-thread CTAs per SM the register allocation must allow, per word class:
+ * the single-word kernels are latency bound and gain from a fifth CTA; the wide classes
+ * keep their state in registers */
+#ifndef RFG_MINB_W1
+#define RFG_MINB_W1 5
+#endif
+#ifndef RFG_MINB_W2
+#define RFG_MINB_W2 4
+#endif
+#ifndef RFG_MINB_W4
+#define RFG_MINB_W4 2
+#endif
+#ifndef RFG_MINB_W8
+#define RFG_MINB_W8 1
+#endif
+constexpr int tiles_min_blocks(int W)
+{
+    return W == 1 ? RFG_MINB_W1 : W == 2 ? RFG_MINB_W2 : W == 4 ? RFG_MINB_W4 : RFG_MINB_W8;
+}
+
 template <int FAM, typename CT, int W, bool TOPK = false>
-__global__ void __launch_bounds__(256) k_tiles(const KParams a)
+__global__ void __launch_bounds__(256, tiles_min_blocks(W)) k_tiles(const KParams a)
 {
     extern __shared__ u64 smem[];
     const int nrows = 256 + a.hcap + 1;
