@@ -299,7 +299,7 @@ struct LaunchRec {
 
 struct Prepared {
     std::vector<LaunchRec> launches;
-    DBuf qlist, small, scratch[1], perm;
+    DBuf qlist, small, scratch[1], perm, poff, plen;
     int* counters = nullptr;
     int* err = nullptr;
     int64_t scratch_words = 0;
@@ -322,21 +322,21 @@ struct Prepared {
     }
     void free_on(cudaStream_t st)
     {
-        qlist.free_on = small.free_on = scratch[0].free_on = perm.free_on = st;
+        qlist.free_on = small.free_on = scratch[0].free_on = perm.free_on = poff.free_on = plen.free_on = st;
     }
 };
 
 /* Host-side choice offsets (for the length order of each chunk): read from the device
  * when the batch lives there. */
-rfg_status choice_lengths(const KStrings& c, const int64_t* host_off, std::vector<int32_t>* len)
+rfg_status choice_lengths(const KStrings& c, const int64_t* host_off, std::vector<int32_t>* len,
+                          std::vector<int64_t>* tmp)
 {
     const int64_t nc = c.n;
-    std::vector<int64_t> tmp;
     if (!host_off) {
-        tmp.resize(nc + 1);
-        RFG_CUDA(cudaMemcpyAsync(tmp.data(), c.off, (nc + 1) * 8, cudaMemcpyDeviceToHost, g.stream));
+        tmp->resize(nc + 1);
+        RFG_CUDA(cudaMemcpyAsync(tmp->data(), c.off, (nc + 1) * 8, cudaMemcpyDeviceToHost, g.stream));
         RFG_CUDA(cudaStreamSynchronize(g.stream));
-        host_off = tmp.data();
+        host_off = tmp->data();
     }
     len->resize(nc);
     for (int64_t i = 0; i < nc; ++i) {
@@ -467,11 +467,26 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             stage = std::min(chunk, cap);
         }
         std::vector<int32_t> clen, perm;
-        RFG_TRY(choice_lengths(c, host_choice_off, &clen));
+        std::vector<int64_t> off_tmp;
+        RFG_TRY(choice_lengths(c, host_choice_off, &clen, &off_tmp));
+        const int64_t* hoff = host_choice_off ? host_choice_off : off_tmp.data();
         for (int32_t l : clen) host_max_choice_len = std::max<int64_t>(host_max_choice_len, l);
         chunk_length_order(clen, stage ? stage : chunk, &perm);
         RFG_TRY(pb->perm.alloc((size_t)nc * 4));
         RFG_CUDA(cudaMemcpyAsync(pb->perm.p, perm.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, g.stream));
+        if (spec.topk == 0) {
+            /* offsets and lengths in visiting order */
+            std::vector<int64_t> po(nc);
+            std::vector<int32_t> pl(nc);
+            for (int64_t i = 0; i < nc; ++i) {
+                po[i] = hoff[perm[i]];
+                pl[i] = clen[perm[i]];
+            }
+            RFG_TRY(pb->poff.alloc((size_t)nc * 8));
+            RFG_TRY(pb->plen.alloc((size_t)nc * 4));
+            RFG_CUDA(cudaMemcpyAsync(pb->poff.p, po.data(), (size_t)nc * 8, cudaMemcpyHostToDevice, g.stream));
+            RFG_CUDA(cudaMemcpyAsync(pb->plen.p, pl.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, g.stream));
+        }
         /* qall and perm are host temporaries: an asynchronous copy from pageable memory
          * returns once the source has been staged, so they may go out of scope */
         dperm = pb->perm.as<int32_t>();
@@ -564,6 +579,10 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         a.chunk_lmin = spec.chunk_lmin;
         a.chunk_lmax = spec.chunk_lmax;
         a.tab_t = (int)std::min<int64_t>(RFG_JT_MAXT, max_choice_len);
+        if (pb->poff.p) {
+            a.poff = pb->poff.as<int64_t>();
+            a.plen = pb->plen.as<int32_t>();
+        }
         if (spec.form != RFG_FORM_MULTI && spec.op == RFG_DISTANCE &&
             ((spec.metric == RFG_LEVENSHTEIN && fam == FAM_LEV && spec.sp.ins == 1 && spec.sp.del == 1 &&
               spec.sp.rep == 1) ||

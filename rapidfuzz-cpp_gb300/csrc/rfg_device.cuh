@@ -75,6 +75,10 @@ struct KParams {
      * the whole chain is d <= K ? d : K + 1 with K = fast_k (the cutoff clamped to 2^62-1) */
     int fast;
     i64 fast_k;
+    /* per visiting position p: start offset and length of choice perm[p] (coalesced
+     * loads that do not wait for perm); null when the batch brings its own order */
+    const int64_t* poff;
+    const int32_t* plen;
 };
 
 /* ----------------------------------------------------------------- helpers */
@@ -464,11 +468,9 @@ __device__ __noinline__ void build_len_tab(const KParams& a, int m, LenTab& t)
 
 template <int FAM, int W, typename CT, bool TOPK>
 __device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, const u64* keys, int64_t qi, int m,
-                                           const u64* qpre, int64_t ci, TopList<TOPK>* tl, const LenTab& lt,
-                                           unsigned char* stage, int64_t s0)
+                                           const u64* qpre, int64_t ci, int64_t o0, int n, TopList<TOPK>* tl,
+                                           const LenTab& lt, unsigned char* stage, int64_t s0)
 {
-    const int64_t o0 = a.c.off[ci], o1 = a.c.off[ci + 1];
-    const int n = (int)(o1 - o0);
     const CT* s2 = (const CT*)a.c.data + o0;
     PairSpec s;
     s.metric = a.metric;
@@ -622,9 +624,36 @@ __global__ void __launch_bounds__(256, tiles_min_blocks(W)) k_tiles(const KParam
         const int64_t win = stage ? a.stage : c1 - c0;
         for (int64_t s0 = c0; s0 < c1 && !skip; s0 += win) {
             const int64_t s1 = s0 + win < c1 ? s0 + win : c1;
-            for (int64_t p = s0 + threadIdx.x; p < s1; p += blockDim.x)
-                score_pair<FAM, W, CT, TOPK>(a, rows, keys, qi, m, s_qpre, a.perm ? (int64_t)__ldg(a.perm + p) : p,
-                                             &tl, s_lt, stage, s0);
+            if (!TOPK && a.poff) {
+                /* the next position's (choice, offset, length) load while this pair runs */
+                int64_t p = s0 + threadIdx.x;
+                int64_t ci_n = 0, o_n = 0;
+                int n_n = 0;
+                if (p < s1) {
+                    ci_n = __ldg(a.perm + p);
+                    o_n = __ldg(a.poff + p);
+                    n_n = __ldg(a.plen + p);
+                }
+                for (; p < s1; p += blockDim.x) {
+                    const int64_t ci = ci_n, o0 = o_n;
+                    const int n = n_n;
+                    const int64_t pn = p + blockDim.x;
+                    if (pn < s1) {
+                        ci_n = __ldg(a.perm + pn);
+                        o_n = __ldg(a.poff + pn);
+                        n_n = __ldg(a.plen + pn);
+                    }
+                    score_pair<FAM, W, CT, TOPK>(a, rows, keys, qi, m, s_qpre, ci, o0, n, &tl, s_lt, stage, s0);
+                }
+            }
+            else {
+                for (int64_t p = s0 + threadIdx.x; p < s1; p += blockDim.x) {
+                    const int64_t ci = a.perm ? (int64_t)__ldg(a.perm + p) : p;
+                    const int64_t o0 = a.c.off[ci];
+                    score_pair<FAM, W, CT, TOPK>(a, rows, keys, qi, m, s_qpre, ci, o0, (int)(a.c.off[ci + 1] - o0), &tl,
+                                                 s_lt, stage, s0);
+                }
+            }
             if (stage) {
                 __syncthreads();
                 flush_stage(a, stage, qi, s0, s1);
