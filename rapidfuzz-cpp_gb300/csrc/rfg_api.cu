@@ -283,6 +283,7 @@ inline bool better_high_of(int op) { return op == RFG_SIMILARITY || op == RFG_NO
 
 int64_t g_tiles_target = 0; /* override of the tile-count target (autotuning) */
 int g_stage_mode = 1;       /* dense tiles stage their results in shared memory (autotuning) */
+int g_mq_mode = 1;          /* one-word unit-weight distances take several queries per thread (autotuning) */
 int g_block_override = 0;   /* override of the tile kernels' block size (autotuning) */
 
 /* A prepared batch: everything a launch needs is on the device, so enqueue() only
@@ -448,6 +449,12 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
     int64_t chunk;
     int64_t host_max_choice_len = 0;
     int64_t stage = 0; /* staged window of the dense tiles (elements), 0 = direct stores */
+    /* unit-weight distance: the chain is d <= K ? d : K + 1 (fast path of the tile kernels) */
+    const bool fast_ok = spec.form != RFG_FORM_MULTI && spec.op == RFG_DISTANCE &&
+                         ((spec.metric == RFG_LEVENSHTEIN && fam == FAM_LEV && spec.sp.ins == 1 &&
+                           spec.sp.del == 1 && spec.sp.rep == 1) ||
+                          spec.metric == RFG_INDEL || spec.metric == RFG_OSA);
+    const bool mq_ok = fast_ok && spec.topk == 0 && !spec.fixed_perm && g_stage_mode != 0 && g_mq_mode != 0;
     const int32_t* dperm;
     if (spec.fixed_perm) {
         chunk = spec.fixed_chunk;
@@ -461,8 +468,9 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         chunk = std::min<int64_t>(chunk, std::max<int64_t>(nc, 1));
         chunk = (chunk + blk - 1) / blk * blk;
         if (spec.topk == 0 && g_stage_mode != 0) {
-            /* windows of up to 32 KB of results, each its own length-sorted run */
-            const int64_t cap = spec.out_dtype == RFG_I32 ? 8192 : 4096;
+            /* windows of up to 32 KB of results, each its own length-sorted run (a
+             * quarter of that per query row in the several-queries kernel) */
+            const int64_t cap = (spec.out_dtype == RFG_I32 ? 8192 : 4096) / (mq_ok ? RFG_MQ : 1);
             if (chunk > cap) chunk = (chunk + cap - 1) / cap * cap;
             stage = std::min(chunk, cap);
         }
@@ -525,7 +533,20 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         int block;
         size_t smem = 0;
         int per_sm;
-        if (k < 4) {
+        const bool use_mq = k == 0 && mq_ok && a.hcap == 0 && stage > 0;
+        if (use_mq) {
+            switch (fam) {
+            case FAM_LEV: fn = tiles_mq_kernel_lev(c.width); break;
+            case FAM_LCS: fn = tiles_mq_kernel_lcs(c.width); break;
+            default: fn = tiles_mq_kernel_osa(c.width);
+            }
+            block = g_block_override > 0 ? g_block_override : 256;
+            a.stage = stage;
+            smem = tiles_mq_smem_bytes(stage, spec.out_dtype);
+            if (smem > 48 * 1024) RFG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            per_sm = occupancy(fn, block, smem);
+        }
+        else if (k < 4) {
             const int W = 1 << k;
             switch (fam) {
             case FAM_LEV: fn = tiles_kernel_lev(c.width, W, topk); break;
@@ -583,15 +604,12 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             a.poff = pb->poff.as<int64_t>();
             a.plen = pb->plen.as<int32_t>();
         }
-        if (spec.form != RFG_FORM_MULTI && spec.op == RFG_DISTANCE &&
-            ((spec.metric == RFG_LEVENSHTEIN && fam == FAM_LEV && spec.sp.ins == 1 && spec.sp.del == 1 &&
-              spec.sp.rep == 1) ||
-             spec.metric == RFG_INDEL || spec.metric == RFG_OSA)) {
+        if (fast_ok) {
             a.fast = 1;
             a.fast_k = clamp_bound(spec.ci);
         }
         a.nchunks = (nc + cchunk - 1) / cchunk;
-        const int64_t ntiles = (int64_t)a.nq * a.nchunks;
+        const int64_t ntiles = (use_mq ? ((int64_t)a.nq + RFG_MQ - 1) / RFG_MQ : (int64_t)a.nq) * a.nchunks;
         if (ntiles > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "batch too large for one launch");
         const int64_t grid = std::min<int64_t>(ntiles, slots);
         if (k == 4) {

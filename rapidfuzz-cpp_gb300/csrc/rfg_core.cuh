@@ -300,6 +300,103 @@ RFG_HD i64 osa_word(const PMF& pm, int m, const TXT& t, int n, i64 K)
     return (i64)n + popc64(VP & mm) - popc64(VN & mm);
 }
 
+/* Q one-word patterns against one text, sharing each fetched block of text units:
+ * for pattern q (q < qn) the unit-weight distance chain d <= K ? d : K + 1 of
+ * Levenshtein / OSA (lev_word / osa_word) or Indel (lcs_word, d = m + n - 2 LCS),
+ * with the same length filter, empty-string rules and lower-bound exits as those cores
+ * behind the tile kernel's fast path, so every d equals the single-pair result.
+ * pm(q, c): pattern-match word of pattern q for text unit c; m[q] <= 64. */
+template <int FAM, int Q, typename PMQ, typename TXT>
+RFG_HD void group_word_dist(const PMQ& pm, const int* m, int qn, const TXT& t, int n, i64 K, i64* d)
+{
+    u64 A[Q], B[Q], D0[Q], PO[Q]; /* Lev / OSA: VP, VN, D0, previous X; Indel: S in A */
+    unsigned live = 0, chk = 0;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        A[q] = ~0ull;
+        B[q] = D0[q] = PO[q] = 0;
+        d[q] = 0;
+        if (q >= qn) continue;
+        const int mq = m[q];
+        const i64 diff = mq > n ? mq - n : n - mq;
+        if (FAM == FAM_LCS) {
+            if (mq == 0 || n == 0) d[q] = (i64)mq + n;
+            else if (K < diff) d[q] = K + 1;
+            else {
+                live |= 1u << q;
+                if (K < (i64)mq + n) chk |= 1u << q;
+            }
+        }
+        else {
+            if (mq == 0) d[q] = n;
+            else if (K < diff) d[q] = K + 1;
+            else if (n == 0) d[q] = mq;
+            else {
+                live |= 1u << q;
+                if (K < (i64)(mq > n ? mq : n)) chk |= 1u << q;
+            }
+        }
+    }
+    for (int j0 = 0; j0 < n && live; j0 += RFG_FETCH) {
+        u64 c[RFG_FETCH];
+#pragma unroll
+        for (int k = 0; k < RFG_FETCH; ++k) c[k] = j0 + k < n ? t[j0 + k] : 0;
+        const int kn = n - j0 < RFG_FETCH ? n - j0 : RFG_FETCH;
+        const bool at_check = kn == RFG_FETCH && ((j0 + RFG_FETCH) & 7) == 0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            if (!((live >> q) & 1u)) continue;
+#pragma unroll
+            for (int k = 0; k < RFG_FETCH; ++k) {
+                if (k < kn) {
+                    const u64 X = pm(q, c[k]);
+                    if (FAM == FAM_LCS) {
+                        const u64 u = A[q] & X;
+                        A[q] = (A[q] + u) | (A[q] - u);
+                    }
+                    else {
+                        const u64 VP = A[q], VN = B[q];
+                        u64 D = (((X & VP) + VP) ^ VP) | X | VN;
+                        if (FAM == FAM_OSA) {
+                            D |= (((~D0[q]) & X) << 1) & PO[q];
+                            D0[q] = D;
+                            PO[q] = X;
+                        }
+                        u64 HP = VN | ~(D | VP);
+                        u64 HN = D & VP;
+                        HP = (HP << 1) | 1;
+                        HN = HN << 1;
+                        A[q] = HN | ~(D | HP);
+                        B[q] = HP & D;
+                    }
+                }
+            }
+            if (at_check && ((chk >> q) & 1u)) {
+                const int jj = j0 + RFG_FETCH, is = m[q] - n + jj;
+                if (is >= 0) {
+                    const u64 lm = low_mask(is);
+                    const bool out = FAM == FAM_LCS
+                                         ? (i64)is + jj - 2 * (i64)popc64(~A[q] & lm) > K
+                                         : (i64)jj + popc64(A[q] & lm) - popc64(B[q] & lm) > K;
+                    if (out) {
+                        d[q] = K + 1;
+                        live &= ~(1u << q);
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if ((live >> q) & 1u) {
+            const u64 mm = low_mask(m[q]);
+            d[q] = FAM == FAM_LCS ? (i64)m[q] + n - 2 * (i64)popc64(~A[q] & mm)
+                                  : (i64)n + popc64(A[q] & mm) - popc64(B[q] & mm);
+        }
+        d[q] = d[q] <= K ? d[q] : K + 1;
+    }
+}
+
 /* Jaro flagging, P (= s1) 1..64 chars, effective text length <= 64
  * (Jaro_impl.hpp:94-132, 258-276).  Returns common chars, transpositions (unhalved). */
 template <typename PMF, typename TXT>

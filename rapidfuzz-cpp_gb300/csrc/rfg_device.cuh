@@ -838,6 +838,148 @@ __global__ void __launch_bounds__(256) k_generic(const KParams a)
     }
 }
 
+/* ------------------------------------------- several queries per thread
+ * Unit-weight distances of one-word patterns whose code units are all below 256:
+ * a tile is (RFG_MQ consecutive queries of the class, chunk); every thread fetches a
+ * choice's text once per block of characters and advances the recurrences of all the
+ * tile's queries on it (group_word_dist), so text loads, per-choice bookkeeping and
+ * the loop overhead are shared by RFG_MQ pairs and the independent recurrences overlap.
+ * Results leave through the staged windows (a.stage positions per query row). */
+#define RFG_MQ 4
+#ifndef RFG_MINB_MQ
+#define RFG_MINB_MQ 4
+#endif
+
+struct MQRows {
+    const u64* rows;
+    __device__ __forceinline__ u64 operator()(int q, u64 c) const { return rows[q * 257 + c]; }
+};
+
+template <typename CT>
+struct MQText {
+    const CT* p;
+    __device__ __forceinline__ u64 operator[](int j) const
+    {
+        const u64 c = (u64)__ldg(p + j);
+        return c < 256 ? c : 256; /* units the patterns lack: the zero row */
+    }
+};
+
+template <int FAM, typename CT>
+__global__ void __launch_bounds__(256, RFG_MINB_MQ) k_tiles_mq(const KParams a)
+{
+    extern __shared__ u64 smem[];
+    u64* rows = smem;
+    unsigned char* stage = (unsigned char*)(smem + RFG_MQ * 257);
+    __shared__ int64_t s_tile;
+    __shared__ int64_t s_q[RFG_MQ];
+    __shared__ int s_m[RFG_MQ];
+    const int64_t ngroups = ((int64_t)a.nq + RFG_MQ - 1) / RFG_MQ;
+    const int64_t ntiles = ngroups * a.nchunks;
+    const i64 K = a.fast_k;
+    int64_t cur_g = -1;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(a.counter, 1);
+        __syncthreads();
+        const int64_t t = s_tile;
+        if (t >= ntiles) break;
+        const int64_t gi = t / a.nchunks, ch = t % a.nchunks;
+        if (gi != cur_g) {
+            for (int i = threadIdx.x; i < RFG_MQ * 257; i += blockDim.x) rows[i] = 0;
+            if (threadIdx.x < RFG_MQ) {
+                const int64_t k = gi * RFG_MQ + threadIdx.x;
+                int64_t qi = -1;
+                int m = 0;
+                if (k < a.nq) {
+                    qi = a.qlist[k];
+                    m = (int)(a.q.off[qi + 1] - a.q.off[qi]);
+                    if (m > 64) { /* the host classified this query into a smaller class */
+                        atomicExch(a.err, 2);
+                        m = 64;
+                    }
+                }
+                s_q[threadIdx.x] = qi;
+                s_m[threadIdx.x] = m;
+            }
+            __syncthreads();
+            for (int q = 0; q < RFG_MQ; ++q) {
+                if (s_q[q] < 0) continue;
+                const unsigned char* qb = a.q.data + a.q.off[s_q[q]] * a.q.width;
+                for (int i = threadIdx.x; i < s_m[q]; i += blockDim.x) {
+                    const u64 c = load_unit(qb, a.q.width, i);
+                    /* a unit >= 256 here means one-byte choices, which never hold it */
+                    if (c < 256) atomicOr((unsigned long long*)&rows[q * 257 + c], 1ull << i);
+                }
+            }
+            __syncthreads();
+            cur_g = gi;
+        }
+        int m[RFG_MQ];
+        int qn = 0;
+#pragma unroll
+        for (int q = 0; q < RFG_MQ; ++q) {
+            m[q] = s_m[q];
+            if (s_q[q] >= 0) qn = q + 1;
+        }
+        const MQRows pm{rows};
+        const int64_t c0 = ch * a.chunk;
+        const int64_t c1 = c0 + a.chunk < a.c.n ? c0 + a.chunk : a.c.n;
+        for (int64_t s0 = c0; s0 < c1; s0 += a.stage) {
+            const int64_t s1 = s0 + a.stage < c1 ? s0 + a.stage : c1;
+            int64_t p = s0 + threadIdx.x;
+            int64_t ci_n = 0, o_n = 0;
+            int n_n = 0;
+            if (p < s1) {
+                ci_n = __ldg(a.perm + p);
+                o_n = __ldg(a.poff + p);
+                n_n = __ldg(a.plen + p);
+            }
+            for (; p < s1; p += blockDim.x) {
+                const int64_t ci = ci_n, o0 = o_n;
+                const int n = n_n;
+                const int64_t pn = p + blockDim.x;
+                if (pn < s1) {
+                    ci_n = __ldg(a.perm + pn);
+                    o_n = __ldg(a.poff + pn);
+                    n_n = __ldg(a.plen + pn);
+                }
+                i64 d[RFG_MQ];
+                group_word_dist<FAM, RFG_MQ>(pm, m, qn, MQText<CT>{(const CT*)a.c.data + o0}, n, K, d);
+                const int64_t i = ci - s0;
+#pragma unroll
+                for (int q = 0; q < RFG_MQ; ++q) {
+                    if (q >= qn) break;
+                    const int64_t at = (int64_t)q * a.stage + i;
+                    switch (a.out_dtype) {
+                    case 0: ((int32_t*)stage)[at] = (int32_t)d[q]; break;
+                    case 1: ((int64_t*)stage)[at] = d[q]; break;
+                    default: ((double*)stage)[at] = int_result_as_double(d[q]);
+                    }
+                }
+            }
+            __syncthreads();
+            for (int q = 0; q < qn; ++q) {
+                const int64_t base = s_q[q] * a.ld + s0, nn = s1 - s0;
+                if (a.out_dtype == 0) {
+                    const int32_t* src = (const int32_t*)stage + (int64_t)q * a.stage;
+                    for (int64_t i = threadIdx.x; i < nn; i += blockDim.x) ((int32_t*)a.out)[base + i] = src[i];
+                }
+                else {
+                    const unsigned long long* src = (const unsigned long long*)stage + (int64_t)q * a.stage;
+                    for (int64_t i = threadIdx.x; i < nn; i += blockDim.x)
+                        ((unsigned long long*)a.out)[base + i] = src[i];
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+inline size_t tiles_mq_smem_bytes(int64_t stage, int out_dtype)
+{
+    return (size_t)RFG_MQ * 257 * 8 + (size_t)RFG_MQ * stage * (out_dtype == 0 ? 4 : 8);
+}
+
 /* Per query: the best topk of all its tiles' candidates, best first; scores as doubles
  * (integer results convert exactly).  One CTA per query. */
 static __global__ void __launch_bounds__(256) k_topk_merge(const u64* cand_key, const int64_t* cand_idx, int64_t nchunks,

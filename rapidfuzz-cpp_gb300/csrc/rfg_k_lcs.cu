@@ -27,4 +27,15 @@ const void* tiles_kernel_lcs(int width, int W, bool topk)
     return nullptr;
 }
 
+const void* tiles_mq_kernel_lcs(int width)
+{
+    switch (width) {
+    case 1: return (const void*)&k_tiles_mq<FAM_LCS, uint8_t>;
+    case 2: return (const void*)&k_tiles_mq<FAM_LCS, uint16_t>;
+    case 4: return (const void*)&k_tiles_mq<FAM_LCS, uint32_t>;
+    case 8: return (const void*)&k_tiles_mq<FAM_LCS, unsigned long long>;
+    }
+    return nullptr;
+}
+
 } // namespace rfg

@@ -27,4 +27,15 @@ const void* tiles_kernel_lev(int width, int W, bool topk)
     return nullptr;
 }
 
+const void* tiles_mq_kernel_lev(int width)
+{
+    switch (width) {
+    case 1: return (const void*)&k_tiles_mq<FAM_LEV, uint8_t>;
+    case 2: return (const void*)&k_tiles_mq<FAM_LEV, uint16_t>;
+    case 4: return (const void*)&k_tiles_mq<FAM_LEV, uint32_t>;
+    case 8: return (const void*)&k_tiles_mq<FAM_LEV, unsigned long long>;
+    }
+    return nullptr;
+}
+
 } // namespace rfg

@@ -9,6 +9,10 @@ const void* tiles_kernel_lev(int width, int W, bool topk);
 const void* tiles_kernel_lcs(int width, int W, bool topk);
 const void* tiles_kernel_osa(int width, int W, bool topk);
 const void* tiles_kernel_jaro(int width, int W, bool topk);
+/* k_tiles_mq<FAM, CT> (unit-weight distances, several queries per thread) */
+const void* tiles_mq_kernel_lev(int width);
+const void* tiles_mq_kernel_lcs(int width);
+const void* tiles_mq_kernel_osa(int width);
 /* k_generic<FAM, CT, TOPK> */
 const void* generic_kernel(int fam, int width, bool topk);
 /* k_topk_merge */

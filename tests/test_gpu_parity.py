@@ -171,3 +171,26 @@ def test_long_strings_any_length_kernel():
         got = R.cdist(metric, op, [q], cs, cut)
         for j, c in enumerate(cs):
             assert G.same(got[0, j].item(), oscore(o.rfo_score, metric, op, CACHED, q, c, cut)), (metric, op, j)
+
+
+@pytest.mark.parametrize("metric", [R.LEVENSHTEIN, R.INDEL, R.OSA])
+@pytest.mark.parametrize("width", [1, 2, 4])
+def test_cdist_several_queries_per_thread(metric, width):
+    """One-word unit-weight distances run several queries per thread: partial query
+    groups, empty strings, choices holding code units the queries lack (>= 256), every
+    output type"""
+    rng = random.Random(1000 + metric * 10 + width)
+    qalpha = list(range(97, 105))
+    calpha = qalpha + ([300, 4000] if width > 1 else [200, 250])
+    for nq in (1, 3, 4, 6, 9):
+        qs = [_rand(rng, qalpha, 0, 64) for _ in range(nq)] + [[]]
+        cs = [_mut(rng, rng.choice(qs), calpha, rng.randint(0, 6)) if rng.random() < 0.5 else _rand(rng, calpha, 0, 70)
+              for _ in range(300)] + [[]]
+        dt = {1: np.uint8, 2: np.uint16, 4: np.uint32}[width]
+        q = R.pack_strings([np.array(s, dtype=dt) for s in qs], width)
+        c = R.pack_strings([np.array(s, dtype=dt) for s in cs], width)
+        for cut in (None, 0, 3, 8, 64):
+            exp = oracle_cdist(metric, R.DISTANCE, q, c, cut)
+            for out_dtype in (R.I32, R.I64):
+                got = R.cdist(metric, R.DISTANCE, q, c, cut, out_dtype=out_dtype)
+                assert np.array_equal(got.astype(np.int64), exp), (nq, cut, out_dtype)
