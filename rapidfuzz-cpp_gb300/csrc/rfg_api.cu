@@ -233,6 +233,20 @@ rfg_status check_params(int metric, const ScoreParams& sp)
     return RFG_OK;
 }
 
+/* launches whose static plus dynamic shared memory passes 48 KB need the opt-in */
+rfg_status allow_dynamic_smem(const void* fn, size_t smem)
+{
+    static std::map<const void*, size_t> granted;
+    auto it = granted.find(fn);
+    if (it != granted.end() && it->second >= smem) return RFG_OK;
+    cudaFuncAttributes fa;
+    RFG_CUDA(cudaFuncGetAttributes(&fa, fn));
+    if (fa.sharedSizeBytes + smem > 48 * 1024)
+        RFG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    granted[fn] = smem;
+    return RFG_OK;
+}
+
 int occupancy(const void* fn, int block, size_t smem)
 {
     static std::map<std::tuple<const void*, int, size_t>, int> cache;
@@ -454,7 +468,15 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
                          ((spec.metric == RFG_LEVENSHTEIN && fam == FAM_LEV && spec.sp.ins == 1 &&
                            spec.sp.del == 1 && spec.sp.rep == 1) ||
                           spec.metric == RFG_INDEL || spec.metric == RFG_OSA);
-    const bool mq_ok = fast_ok && spec.topk == 0 && !spec.fixed_perm && g_stage_mode != 0 && g_mq_mode != 0;
+    /* the normalized chains of the same unit-weight metrics (integer cutoff tabulated) */
+    const bool norm_ok = spec.form != RFG_FORM_MULTI &&
+                         (spec.op == RFG_NORMALIZED_DISTANCE || spec.op == RFG_NORMALIZED_SIMILARITY ||
+                          spec.metric == RFG_RATIO) &&
+                         ((spec.metric == RFG_LEVENSHTEIN && fam == FAM_LEV && spec.sp.ins == 1 &&
+                           spec.sp.del == 1 && spec.sp.rep == 1) ||
+                          spec.metric == RFG_INDEL || spec.metric == RFG_RATIO || spec.metric == RFG_OSA);
+    const bool mq_ok =
+        (fast_ok || norm_ok) && spec.topk == 0 && !spec.fixed_perm && g_stage_mode != 0 && g_mq_mode != 0;
     const int32_t* dperm;
     if (spec.fixed_perm) {
         chunk = spec.fixed_chunk;
@@ -536,14 +558,15 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         const bool use_mq = k == 0 && mq_ok && a.hcap == 0 && stage > 0;
         if (use_mq) {
             switch (fam) {
-            case FAM_LEV: fn = tiles_mq_kernel_lev(c.width); break;
-            case FAM_LCS: fn = tiles_mq_kernel_lcs(c.width); break;
-            default: fn = tiles_mq_kernel_osa(c.width);
+            case FAM_LEV: fn = tiles_mq_kernel_lev(c.width, !fast_ok); break;
+            case FAM_LCS: fn = tiles_mq_kernel_lcs(c.width, !fast_ok); break;
+            default: fn = tiles_mq_kernel_osa(c.width, !fast_ok);
             }
             block = g_block_override > 0 ? g_block_override : 256;
             a.stage = stage;
-            smem = tiles_mq_smem_bytes(stage, spec.out_dtype);
-            if (smem > 48 * 1024) RFG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            smem = tiles_mq_smem_bytes(stage, spec.out_dtype,
+                                       fast_ok ? 0 : (int)std::min<int64_t>(RFG_JT_MAXT, max_choice_len) + 1);
+            RFG_TRY(allow_dynamic_smem(fn, smem));
             per_sm = occupancy(fn, block, smem);
         }
         else if (k < 4) {
@@ -560,7 +583,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
                 a.stage = stage;
                 smem += (size_t)stage * (spec.out_dtype == RFG_I32 ? 4 : 8);
             }
-            if (smem > 48 * 1024) RFG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            RFG_TRY(allow_dynamic_smem(fn, smem));
             per_sm = occupancy(fn, block, smem);
         }
         else {
@@ -572,8 +595,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
                 /* pattern table in shared memory; per-thread state stays in scratch */
                 a.pm_smem = 1;
                 smem = table;
-                if (smem > 48 * 1024)
-                    RFG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                RFG_TRY(allow_dynamic_smem(fn, smem));
             }
             per_sm = std::min(occupancy(fn, block, smem), 8);
         }

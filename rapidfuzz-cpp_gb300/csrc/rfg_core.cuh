@@ -301,13 +301,13 @@ RFG_HD i64 osa_word(const PMF& pm, int m, const TXT& t, int n, i64 K)
 }
 
 /* Q one-word patterns against one text, sharing each fetched block of text units:
- * for pattern q (q < qn) the unit-weight distance chain d <= K ? d : K + 1 of
+ * for pattern q (q < qn) the unit-weight distance chain d <= K[q] ? d : K[q] + 1 of
  * Levenshtein / OSA (lev_word / osa_word) or Indel (lcs_word, d = m + n - 2 LCS),
  * with the same length filter, empty-string rules and lower-bound exits as those cores
  * behind the tile kernel's fast path, so every d equals the single-pair result.
  * pm(q, c): pattern-match word of pattern q for text unit c; m[q] <= 64. */
 template <int FAM, int Q, typename PMQ, typename TXT>
-RFG_HD void group_word_dist(const PMQ& pm, const int* m, int qn, const TXT& t, int n, i64 K, i64* d)
+RFG_HD void group_word_dist(const PMQ& pm, const int* m, int qn, const TXT& t, int n, const i64* Kq, i64* d)
 {
     u64 A[Q], B[Q], D0[Q], PO[Q]; /* Lev / OSA: VP, VN, D0, previous X; Indel: S in A */
     unsigned live = 0, chk = 0;
@@ -318,6 +318,7 @@ RFG_HD void group_word_dist(const PMQ& pm, const int* m, int qn, const TXT& t, i
         d[q] = 0;
         if (q >= qn) continue;
         const int mq = m[q];
+        const i64 K = Kq[q];
         const i64 diff = mq > n ? mq - n : n - mq;
         if (FAM == FAM_LCS) {
             if (mq == 0 || n == 0) d[q] = (i64)mq + n;
@@ -372,6 +373,7 @@ RFG_HD void group_word_dist(const PMQ& pm, const int* m, int qn, const TXT& t, i
                 }
             }
             if (at_check && ((chk >> q) & 1u)) {
+                const i64 K = Kq[q];
                 const int jj = j0 + RFG_FETCH, is = m[q] - n + jj;
                 if (is >= 0) {
                     const u64 lm = low_mask(is);
@@ -393,7 +395,7 @@ RFG_HD void group_word_dist(const PMQ& pm, const int* m, int qn, const TXT& t, i
             d[q] = FAM == FAM_LCS ? (i64)m[q] + n - 2 * (i64)popc64(~A[q] & mm)
                                   : (i64)n + popc64(A[q] & mm) - popc64(B[q] & mm);
         }
-        d[q] = d[q] <= K ? d[q] : K + 1;
+        d[q] = d[q] <= Kq[q] ? d[q] : Kq[q] + 1;
     }
 }
 

@@ -839,7 +839,8 @@ __global__ void __launch_bounds__(256) k_generic(const KParams a)
 }
 
 /* ------------------------------------------- several queries per thread
- * Unit-weight distances of one-word patterns whose code units are all below 256:
+ * Unit-weight distances of one-word patterns whose code units are all below 256
+ * (distance, or the normalized chains with the integer cutoff from per-query tables):
  * a tile is (RFG_MQ consecutive queries of the class, chunk); every thread fetches a
  * choice's text once per block of characters and advances the recurrences of all the
  * tile's queries on it (group_word_dist), so text loads, per-choice bookkeeping and
@@ -848,6 +849,9 @@ __global__ void __launch_bounds__(256) k_generic(const KParams a)
 #define RFG_MQ 4
 #ifndef RFG_MINB_MQ
 #define RFG_MINB_MQ 4
+#endif
+#ifndef RFG_MINB_MQ_OSA
+#define RFG_MINB_MQ_OSA 3 /* four OSA states (VP, VN, D0, previous X) per query */
 #endif
 
 struct MQRows {
@@ -865,12 +869,15 @@ struct MQText {
     }
 };
 
-template <int FAM, typename CT>
-__global__ void __launch_bounds__(256, RFG_MINB_MQ) k_tiles_mq(const KParams a)
+template <int FAM, typename CT, bool NORM>
+__global__ void __launch_bounds__(256, FAM == FAM_OSA ? RFG_MINB_MQ_OSA : RFG_MINB_MQ) k_tiles_mq(const KParams a)
 {
     extern __shared__ u64 smem[];
     u64* rows = smem;
-    unsigned char* stage = (unsigned char*)(smem + RFG_MQ * 257);
+    /* normalized ops (NORM): chain_kd per (query, text length 0..tab_t) */
+    const int tn = NORM ? a.tab_t + 1 : 0;
+    u64* kdt = smem + RFG_MQ * 257;
+    unsigned char* stage = (unsigned char*)(kdt + RFG_MQ * tn);
     __shared__ int64_t s_tile;
     __shared__ int64_t s_q[RFG_MQ];
     __shared__ int s_m[RFG_MQ];
@@ -902,6 +909,20 @@ __global__ void __launch_bounds__(256, RFG_MINB_MQ) k_tiles_mq(const KParams a)
                 s_m[threadIdx.x] = m;
             }
             __syncthreads();
+            if (NORM) {
+                PairSpec sp;
+                sp.metric = a.metric;
+                sp.op = a.op;
+                sp.form = a.form;
+                sp.ci = a.ci;
+                sp.cf = a.cf;
+                sp.p = a.sp;
+                for (int i = threadIdx.x; i < RFG_MQ * tn; i += blockDim.x) {
+                    sp.l1 = (u64)s_m[i / tn];
+                    sp.l2 = (u64)(i % tn);
+                    kdt[i] = chain_kd(sp);
+                }
+            }
             for (int q = 0; q < RFG_MQ; ++q) {
                 if (s_q[q] < 0) continue;
                 const unsigned char* qb = a.q.data + a.q.off[s_q[q]] * a.q.width;
@@ -943,17 +964,53 @@ __global__ void __launch_bounds__(256, RFG_MINB_MQ) k_tiles_mq(const KParams a)
                     o_n = __ldg(a.poff + pn);
                     n_n = __ldg(a.plen + pn);
                 }
-                i64 d[RFG_MQ];
-                group_word_dist<FAM, RFG_MQ>(pm, m, qn, MQText<CT>{(const CT*)a.c.data + o0}, n, K, d);
+                i64 d[RFG_MQ], Kq[RFG_MQ];
+#pragma unroll
+                for (int q = 0; q < RFG_MQ; ++q) {
+                    if (!NORM) Kq[q] = K;
+                    else {
+                        u64 kd;
+                        if (n <= a.tab_t) kd = kdt[q * tn + n];
+                        else {
+                            PairSpec sp;
+                            sp.metric = a.metric;
+                            sp.op = a.op;
+                            sp.form = a.form;
+                            sp.ci = a.ci;
+                            sp.cf = a.cf;
+                            sp.p = a.sp;
+                            sp.l1 = (u64)m[q];
+                            sp.l2 = (u64)n;
+                            kd = chain_kd(sp);
+                        }
+                        Kq[q] = clamp_bound(kd);
+                    }
+                }
+                group_word_dist<FAM, RFG_MQ>(pm, m, qn, MQText<CT>{(const CT*)a.c.data + o0}, n, Kq, d);
                 const int64_t i = ci - s0;
 #pragma unroll
                 for (int q = 0; q < RFG_MQ; ++q) {
                     if (q >= qn) break;
                     const int64_t at = (int64_t)q * a.stage + i;
-                    switch (a.out_dtype) {
-                    case 0: ((int32_t*)stage)[at] = (int32_t)d[q]; break;
-                    case 1: ((int64_t*)stage)[at] = d[q]; break;
-                    default: ((double*)stage)[at] = int_result_as_double(d[q]);
+                    if (!NORM) {
+                        switch (a.out_dtype) {
+                        case 0: ((int32_t*)stage)[at] = (int32_t)d[q]; break;
+                        case 1: ((int64_t*)stage)[at] = d[q]; break;
+                        default: ((double*)stage)[at] = int_result_as_double(d[q]);
+                        }
+                    }
+                    else {
+                        /* the normalized chain over d with its integer cutoff Kq (finish_int) */
+                        const u64 M = FAM == FAM_LCS ? (u64)m[q] + n : (u64)(m[q] > n ? m[q] : n);
+                        const u64 Kc = (u64)Kq[q], du = (u64)d[q];
+                        double vf = 0.0;
+                        if (a.metric == RATIO)
+                            vf = (M != 0 && du > Kc && abs_le_bits(a.cf, 200.0)) ? 0.0 : ratio_finish(M, du, a.cf, Kc);
+                        else {
+                            i64 vi = 0;
+                            dist_chain_finish(a.op, M, du, a.ci, a.cf, &vi, &vf, Kc);
+                        }
+                        ((double*)stage)[at] = vf;
                     }
                 }
             }
@@ -975,9 +1032,9 @@ __global__ void __launch_bounds__(256, RFG_MINB_MQ) k_tiles_mq(const KParams a)
     }
 }
 
-inline size_t tiles_mq_smem_bytes(int64_t stage, int out_dtype)
+inline size_t tiles_mq_smem_bytes(int64_t stage, int out_dtype, int kd_len)
 {
-    return (size_t)RFG_MQ * 257 * 8 + (size_t)RFG_MQ * stage * (out_dtype == 0 ? 4 : 8);
+    return ((size_t)RFG_MQ * 257 + (size_t)RFG_MQ * kd_len) * 8 + (size_t)RFG_MQ * stage * (out_dtype == 0 ? 4 : 8);
 }
 
 /* Per query: the best topk of all its tiles' candidates, best first; scores as doubles

@@ -27,13 +27,15 @@ const void* tiles_kernel_lev(int width, int W, bool topk)
     return nullptr;
 }
 
-const void* tiles_mq_kernel_lev(int width)
+const void* tiles_mq_kernel_lev(int width, bool norm)
 {
     switch (width) {
-    case 1: return (const void*)&k_tiles_mq<FAM_LEV, uint8_t>;
-    case 2: return (const void*)&k_tiles_mq<FAM_LEV, uint16_t>;
-    case 4: return (const void*)&k_tiles_mq<FAM_LEV, uint32_t>;
-    case 8: return (const void*)&k_tiles_mq<FAM_LEV, unsigned long long>;
+    case 1: return norm ? (const void*)&k_tiles_mq<FAM_LEV, uint8_t, true> : (const void*)&k_tiles_mq<FAM_LEV, uint8_t, false>;
+    case 2: return norm ? (const void*)&k_tiles_mq<FAM_LEV, uint16_t, true> : (const void*)&k_tiles_mq<FAM_LEV, uint16_t, false>;
+    case 4: return norm ? (const void*)&k_tiles_mq<FAM_LEV, uint32_t, true> : (const void*)&k_tiles_mq<FAM_LEV, uint32_t, false>;
+    case 8:
+        return norm ? (const void*)&k_tiles_mq<FAM_LEV, unsigned long long, true>
+                    : (const void*)&k_tiles_mq<FAM_LEV, unsigned long long, false>;
     }
     return nullptr;
 }

@@ -9,10 +9,11 @@ const void* tiles_kernel_lev(int width, int W, bool topk);
 const void* tiles_kernel_lcs(int width, int W, bool topk);
 const void* tiles_kernel_osa(int width, int W, bool topk);
 const void* tiles_kernel_jaro(int width, int W, bool topk);
-/* k_tiles_mq<FAM, CT> (unit-weight distances, several queries per thread) */
-const void* tiles_mq_kernel_lev(int width);
-const void* tiles_mq_kernel_lcs(int width);
-const void* tiles_mq_kernel_osa(int width);
+/* k_tiles_mq<FAM, CT, NORM> (unit-weight distances or their normalized chains, several
+ * queries per thread) */
+const void* tiles_mq_kernel_lev(int width, bool norm);
+const void* tiles_mq_kernel_lcs(int width, bool norm);
+const void* tiles_mq_kernel_osa(int width, bool norm);
 /* k_generic<FAM, CT, TOPK> */
 const void* generic_kernel(int fam, int width, bool topk);
 /* k_topk_merge */
