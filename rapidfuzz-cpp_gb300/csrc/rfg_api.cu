@@ -314,7 +314,9 @@ struct LaunchRec {
 
 struct Prepared {
     std::vector<LaunchRec> launches;
-    DBuf qlist, small, scratch[1], perm, poff, plen;
+    DBuf qlist, small, scratch[1], perm, poff, plen, jtab;
+    bool has_pre = false; /* pre.a / grid: the per-query table pass before the row blocks */
+    KParams pre;
     int* counters = nullptr;
     int* err = nullptr;
     int64_t scratch_words = 0;
@@ -337,7 +339,8 @@ struct Prepared {
     }
     void free_on(cudaStream_t st)
     {
-        qlist.free_on = small.free_on = scratch[0].free_on = perm.free_on = poff.free_on = plen.free_on = st;
+        qlist.free_on = small.free_on = scratch[0].free_on = perm.free_on = poff.free_on = plen.free_on =
+            jtab.free_on = st;
     }
 };
 
@@ -622,6 +625,14 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         a.chunk_lmin = spec.chunk_lmin;
         a.chunk_lmax = spec.chunk_lmax;
         a.tab_t = (int)std::min<int64_t>(RFG_JT_MAXT, max_choice_len);
+        if (fam == FAM_JARO && !topk && spec.form != RFG_FORM_MULTI && k < 4) {
+            if (!pb->jtab.p) {
+                RFG_TRY(pb->jtab.alloc((size_t)nq * sizeof(JaroTab)));
+                pb->pre = a;
+                pb->has_pre = true;
+            }
+            a.jtab = pb->jtab.as<JaroTab>();
+        }
         if (pb->poff.p) {
             a.poff = pb->poff.as<int64_t>();
             a.plen = pb->plen.as<int32_t>();
@@ -699,9 +710,21 @@ rfg_status enqueue_block(Prepared& pb, int b, cudaStream_t st)
     return RFG_OK;
 }
 
+/* the per-query table pass that the row blocks read */
+rfg_status enqueue_pre(Prepared& pb, cudaStream_t st)
+{
+    if (!pb.has_pre || pb.pre.q.n == 0) return RFG_OK;
+    KParams a = pb.pre;
+    JaroTab* out = pb.jtab.as<JaroTab>();
+    void* args[] = {&a, &out};
+    RFG_CUDA(cudaLaunchKernel(jaro_tables_kernel(), dim3((unsigned)a.q.n), dim3(256), args, 0, st));
+    return RFG_OK;
+}
+
 rfg_status enqueue_batch(Prepared& pb, cudaStream_t st)
 {
     RFG_CUDA(cudaMemsetAsync(pb.counters, 0, RFG_COUNTERS * sizeof(int), st));
+    RFG_TRY(enqueue_pre(pb, st));
     for (size_t b = 0; b < std::max<size_t>(pb.rows.size(), 1); ++b) RFG_TRY(enqueue_block(pb, (int)b, st));
     return RFG_OK;
 }
@@ -805,6 +828,7 @@ rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const 
     } join;
     RFG_TRY(prepare_batch(qs, ck, spec, &pb, dev_in ? nullptr : C->offsets));
     RFG_CUDA(cudaMemsetAsync(pb.counters, 0, RFG_COUNTERS * sizeof(int), g.stream));
+    RFG_TRY(enqueue_pre(pb, g.stream));
     for (size_t b = 0; b < pb.rows.size(); ++b) {
         RFG_TRY(enqueue_block(pb, (int)b, g.stream));
         const int64_t r0 = pb.rows[b].first, r1 = pb.rows[b].second;

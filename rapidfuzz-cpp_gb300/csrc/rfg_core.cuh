@@ -410,25 +410,28 @@ RFG_HD void jaro_word(const PMF& pm, int pl, const TXT& t, int tl, int* common, 
     if (te > pl + bound) te = pl + bound; /* text beyond the last window never matches */
     u64 pflag = 0, tflag = 0;
     u64 bmask = low_mask(bound + 1);
-    int j = 0;
     const int lead = bound < te ? bound : te;
-    for (; j < lead; ++j) {
-        const u64 x = pm(t[j]) & bmask & ~pflag;
-        pflag |= blsi(x);
-        tflag |= (u64)(x != 0) << j;
-        bmask = (bmask << 1) | 1;
-    }
-    for (; j < te; ++j) {
-        const u64 x = pm(t[j]) & bmask & ~pflag;
-        pflag |= blsi(x);
-        tflag |= (u64)(x != 0) << j;
-        bmask <<= 1;
-        /* each remaining text character adds at most one common character: a caller
-         * that only needs to know whether `need` is reached stops here */
-        if ((j & 7) == 7 && popc64(pflag) + (te - 1 - j) < need) {
-            *common = 0;
-            *transp = 0;
-            return;
+    /* text units fetched RFG_FETCH at a time (independent loads), as in the edit cores */
+    for (int j0 = 0; j0 < te; j0 += RFG_FETCH) {
+        u64 X[RFG_FETCH];
+#pragma unroll
+        for (int k = 0; k < RFG_FETCH; ++k) X[k] = j0 + k < te ? pm(t[j0 + k]) : 0;
+#pragma unroll
+        for (int k = 0; k < RFG_FETCH; ++k) {
+            const int j = j0 + k;
+            if (j < te) {
+                const u64 x = X[k] & bmask & ~pflag;
+                pflag |= blsi(x);
+                tflag |= (u64)(x != 0) << j;
+                bmask = j < lead ? (bmask << 1) | 1 : bmask << 1;
+                /* each remaining text character adds at most one common character: a
+                 * caller that only needs to know whether `need` is reached stops here */
+                if ((j & 3) == 3 && popc64(pflag) + (te - 1 - j) < need) {
+                    *common = 0;
+                    *transp = 0;
+                    return;
+                }
+            }
         }
     }
     *common = popc64(pflag);

@@ -75,6 +75,9 @@ struct KParams {
      * the whole chain is d <= K ? d : K + 1 with K = fast_k (the cutoff clamped to 2^62-1) */
     int fast;
     i64 fast_k;
+    /* Jaro / Jaro-Winkler: every query's JaroTab, filled by k_jaro_tables before the
+     * tile kernels (null: the tile kernel builds it) */
+    const JaroTab* jtab;
     /* per visiting position p: start offset and length of choice perm[p] (coalesced
      * loads that do not wait for perm); null when the batch brings its own order */
     const int64_t* poff;
@@ -550,13 +553,30 @@ __device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, co
     emit(a, qi, ci, vi, vf, is_int, s.ci, s.cf, tl, stage, s0);
 }
 
+/* visiting position p: its choice, the choice's start offset and length */
+struct PosMeta {
+    int64_t ci, o;
+    int n;
+};
+
+__device__ __forceinline__ PosMeta load_pos(const KParams& a, int64_t p)
+{
+    return PosMeta{(int64_t)__ldg(a.perm + p), __ldg(a.poff + p), __ldg(a.plen + p)};
+}
+
+/* pull the first 128-byte line of a non-empty choice into L1 (no register waits on it) */
+__device__ __forceinline__ void prefetch_text(const KParams& a, const PosMeta& m)
+{
+    if (m.n > 0) asm volatile("prefetch.global.L1 [%0];" ::"l"(a.c.data + m.o * a.c.width));
+}
+
 /* -------------------------------------------------------------- the kernel */
 
 /* resident 256-thread CTAs per SM the register allocation must allow, per word class:
  * the single-word kernels are latency bound and gain from a fifth CTA; the wide classes
  * keep their state in registers */
 #ifndef RFG_MINB_W1
-#define RFG_MINB_W1 5
+#define RFG_MINB_W1 4
 #endif
 #ifndef RFG_MINB_W2
 #define RFG_MINB_W2 4
@@ -610,7 +630,16 @@ __global__ void __launch_bounds__(256, tiles_min_blocks(W)) k_tiles(const KParam
             }
             build_pm<W>(rows, keys, a.hcap, qb, m, a.q.width, a.err);
             if (threadIdx.x < 4) s_qpre[threadIdx.x] = (int)threadIdx.x < m ? load_unit(qb, a.q.width, threadIdx.x) : 0;
-            if (!TOPK) build_len_tab<FAM>(a, m, s_lt);
+            if (!TOPK) {
+                if (FAM == FAM_JARO && a.jtab && uses_jaro_tab(a)) {
+                    /* copy the precomputed table (the doubles and the minc rows) */
+                    const u64* src = (const u64*)(a.jtab + qi);
+                    u64* dst = (u64*)&s_lt.jt;
+                    for (int i = threadIdx.x; i < (int)(sizeof(JaroTab) / 8); i += blockDim.x) dst[i] = __ldg(src + i);
+                    __syncthreads();
+                }
+                else build_len_tab<FAM>(a, m, s_lt);
+            }
             __syncthreads();
             cur_q = qi;
         }
@@ -625,25 +654,20 @@ __global__ void __launch_bounds__(256, tiles_min_blocks(W)) k_tiles(const KParam
         for (int64_t s0 = c0; s0 < c1 && !skip; s0 += win) {
             const int64_t s1 = s0 + win < c1 ? s0 + win : c1;
             if (!TOPK && a.poff) {
-                /* the next position's (choice, offset, length) load while this pair runs */
+                /* two positions ahead: (choice, offset, length) two iterations early, the
+                 * text's first line pulled into L1 one iteration early */
+                const int64_t bd = blockDim.x;
                 int64_t p = s0 + threadIdx.x;
-                int64_t ci_n = 0, o_n = 0;
-                int n_n = 0;
-                if (p < s1) {
-                    ci_n = __ldg(a.perm + p);
-                    o_n = __ldg(a.poff + p);
-                    n_n = __ldg(a.plen + p);
-                }
-                for (; p < s1; p += blockDim.x) {
-                    const int64_t ci = ci_n, o0 = o_n;
-                    const int n = n_n;
-                    const int64_t pn = p + blockDim.x;
-                    if (pn < s1) {
-                        ci_n = __ldg(a.perm + pn);
-                        o_n = __ldg(a.poff + pn);
-                        n_n = __ldg(a.plen + pn);
-                    }
-                    score_pair<FAM, W, CT, TOPK>(a, rows, keys, qi, m, s_qpre, ci, o0, n, &tl, s_lt, stage, s0);
+                PosMeta cur{0, 0, 0}, nxt{0, 0, 0};
+                if (p < s1) cur = load_pos(a, p);
+                if (p + bd < s1) nxt = load_pos(a, p + bd);
+                if (p < s1) prefetch_text(a, cur);
+                for (; p < s1; p += bd) {
+                    const PosMeta m0 = cur;
+                    cur = nxt;
+                    if (p + 2 * bd < s1) nxt = load_pos(a, p + 2 * bd);
+                    if (p + bd < s1) prefetch_text(a, cur);
+                    score_pair<FAM, W, CT, TOPK>(a, rows, keys, qi, m, s_qpre, m0.ci, m0.o, m0.n, &tl, s_lt, stage, s0);
                 }
             }
             else {
@@ -1039,6 +1063,29 @@ inline size_t tiles_mq_smem_bytes(int64_t stage, int out_dtype, int kd_len)
 
 /* Per query: the best topk of all its tiles' candidates, best first; scores as doubles
  * (integer results convert exactly).  One CTA per query. */
+/* One CTA per query: its JaroTab over text lengths 0..tab_t (the double-precision
+ * filters once per query instead of once per tile). */
+static __global__ void __launch_bounds__(256) k_jaro_tables(const KParams a, JaroTab* out)
+{
+    const int64_t qi = blockIdx.x;
+    if (qi >= a.q.n) return;
+    const int m = (int)(a.q.off[qi + 1] - a.q.off[qi]);
+    PairSpec s;
+    s.metric = a.metric;
+    s.op = a.op;
+    s.form = a.form;
+    s.l1 = (u64)m;
+    s.ci = a.ci;
+    s.cf = a.cf;
+    s.p = a.sp;
+    JaroTab& t = out[qi];
+    if (threadIdx.x == 0) jaro_tab_head(t, s);
+    for (int i = threadIdx.x; i < 5 * (a.tab_t + 1); i += blockDim.x) {
+        const int p = i / (a.tab_t + 1), tl = i % (a.tab_t + 1);
+        t.minc[p][tl] = jaro_tab_minc(s, m, p, tl);
+    }
+}
+
 static __global__ void __launch_bounds__(256) k_topk_merge(const u64* cand_key, const int64_t* cand_idx, int64_t nchunks,
                                                      int k, int tie_last, int better_high, int is_int,
                                                      int64_t* out_idx, double* out_score, int32_t* out_count)

@@ -30,4 +30,6 @@ const void* generic_kernel(int fam, int width, bool topk)
 
 const void* topk_merge_kernel() { return (const void*)&k_topk_merge; }
 
+const void* jaro_tables_kernel() { return (const void*)&k_jaro_tables; }
+
 } // namespace rfg

@@ -18,4 +18,6 @@ const void* tiles_mq_kernel_osa(int width, bool norm);
 const void* generic_kernel(int fam, int width, bool topk);
 /* k_topk_merge */
 const void* topk_merge_kernel();
+/* k_jaro_tables (per-query JaroTab pre-pass) */
+const void* jaro_tables_kernel();
 } // namespace rfg
