@@ -38,7 +38,9 @@ sys.path.insert(0, os.path.join(ROOT, "rapidfuzz-cpp_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 METRIC_NAME = "GCUPS & pairs/s, batched vs per-call, 1 GB300, bit-exact; extract p50/p99 ms"
-DRAM_BYTES_PER_LAUNCH = {"levenshtein": 35292672, "indel": 35352320, "osa": 26712320}
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the several-queries kernels
+# (k_tiles_mq) on this workload, default launch shape (profiles/k_tiles_mq_cdist4096_full.md)
+DRAM_BYTES_PER_LAUNCH = {"levenshtein": 8301312, "indel": 8237824, "osa": 7320576}
 OPS_PER_WORD_STEP = {"levenshtein": 23, "indel": 8, "osa": 29}
 CUTOFF = 8
 
@@ -305,9 +307,10 @@ def main():
     alg_ops = (exec_steps[dom] if exec_steps[dom] is not None else req_steps) * OPS_PER_WORD_STEP[dom]
     peak = int_peak_ops()
     achieved = alg_ops / (dom_ms * 1e-3)
-    # dram__bytes_read.sum + dram__bytes_write.sum per launch of the default launch shape,
-    # from one ncu capture of this workload (profiles/k_tiles_cdist4096_full.md)
-    traffic = DRAM_BYTES_PER_LAUNCH.get(dom) if args.nq == 4096 and args.nc == 4096 else None
+    kern = dict((name, b.kernels()) for name, b in batches)
+    dom_kernel = ";".join(kern[dom])
+    traffic = (DRAM_BYTES_PER_LAUNCH.get(dom) if args.nq == 4096 and args.nc == 4096 and "k_tiles_mq" in dom_kernel
+               else None)
 
     # e2e through the public C ABI with pinned host buffers
     e2e = None
@@ -353,7 +356,7 @@ def main():
                            "required_word_steps_per_metric": req_steps,
                            "executed_word_steps": exec_steps, "pairs_passing_length_filter": pairs_pass},
                 "roofline": {"bound": "int32", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "Tops/s",
-                             "frac": achieved / peak, "traffic": traffic, "kernel": "k_tiles<%s,u8,W=1>" % dom,
+                             "frac": achieved / peak, "traffic": traffic, "kernel": dom_kernel,
                              "peak_source": "measured: LOP3/IADD3/SHF issue-rate microbenchmark (librfg_peak.so)",
                              "ops_per_word_step": OPS_PER_WORD_STEP[dom]},
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * args.steps, "clocks": clk}

@@ -169,6 +169,9 @@ rfg_status rfg_batch_launch(rfg_batch batch, void* cuda_stream, uint32_t launch_
 rfg_status rfg_batch_check(rfg_batch batch, void* cuda_stream);
 rfg_status rfg_batch_tune(rfg_batch batch, void* cuda_stream, int32_t* best_block, int64_t* best_tiles);
 rfg_status rfg_batch_destroy(rfg_batch batch);
+/* the kernels one launch of the batch runs (as the toolchain names them), separated by
+ * ';' into names[0..cap), NUL-terminated; for profiling and logs */
+rfg_status rfg_batch_kernels(rfg_batch batch, char* names, size_t cap);
 /* the library's own stream (the synchronous entry points run on it) */
 rfg_status rfg_get_stream(void** cuda_stream);
 

@@ -1588,6 +1588,24 @@ rfg_status rfg_batch_destroy(rfg_batch b)
     return RFG_OK;
 }
 
+rfg_status rfg_batch_kernels(rfg_batch b, char* names, size_t cap)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (!b || !names || cap == 0) return fail(RFG_ERR_INVALID_ARGUMENT, "batch or buffer is NULL");
+    std::string all;
+    auto add = [&](const void* fn) {
+        const char* nm = nullptr;
+        if (cudaFuncGetName(&nm, fn) != cudaSuccess || !nm) nm = "?";
+        if (!all.empty()) all += ';';
+        all += nm;
+    };
+    if (b->pb->has_pre) add(jaro_tables_kernel());
+    for (const LaunchRec& L : b->pb->launches) add(L.fn);
+    if (all.size() + 1 > cap) return fail(RFG_ERR_INVALID_ARGUMENT, "buffer too small (%zu bytes needed)", all.size() + 1);
+    memcpy(names, all.c_str(), all.size() + 1);
+    return RFG_OK;
+}
+
 rfg_status rfg_get_stream(void** stream)
 {
     std::lock_guard<std::recursive_mutex> lk(g.mu);

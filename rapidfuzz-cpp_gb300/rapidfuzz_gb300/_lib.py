@@ -94,6 +94,7 @@ def lib():
             "rfg_batch_check": ([vp, vp], ctypes.c_int),
             "rfg_batch_tune": ([vp, vp, P(i32), P(i64)], ctypes.c_int),
             "rfg_batch_destroy": ([vp], ctypes.c_int),
+            "rfg_batch_kernels": ([vp, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
             "rfg_get_stream": ([P(vp)], ctypes.c_int),
             "rfg_corpus_create": ([P(Strings), ctypes.c_uint32, P(vp)], ctypes.c_int),
             "rfg_corpus_destroy": ([vp], ctypes.c_int),
@@ -333,6 +334,12 @@ class Batch:
         b, t = ctypes.c_int32(), ctypes.c_int64()
         check(lib().rfg_batch_tune(self._h, stream, ctypes.byref(b), ctypes.byref(t)))
         return b.value, t.value
+
+    def kernels(self):
+        """names of the kernels one launch runs"""
+        buf = ctypes.create_string_buffer(4096)
+        check(lib().rfg_batch_kernels(self._h, buf, len(buf)))
+        return [k for k in buf.value.decode().split(";") if k]
 
     def close(self):
         if self._h and self._h.value:
