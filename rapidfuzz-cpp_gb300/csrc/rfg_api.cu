@@ -843,6 +843,112 @@ rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const 
     return check_batch(pb, g.stream);
 }
 
+/* One pair in one round trip (the per-call path of the free functions and the cached
+ * scorers): both strings, their offsets, the tile list and the zeroed counter and check
+ * flag leave in one copy from pinned staging memory, one CTA of the any-length kernel
+ * scores the pair, and the check flag and the result return in one copy.  Staging and
+ * scratch are allocated once per context; calls are serialised by the library lock. */
+struct PairPath {
+    bool init = false;
+    unsigned char* h = nullptr; /* pinned */
+    unsigned char* d = nullptr;
+    u64* scratch = nullptr;
+};
+PairPath g_pair;
+constexpr size_t kPairStage = 64 * 1024, kPairHead = 128, kPairScratchWords = 128 * 1024;
+constexpr int64_t kPairMaxLen1 = 1024;
+
+rfg_status pair_path_init()
+{
+    if (g_pair.init) return RFG_OK;
+    RFG_CUDA(cudaHostAlloc((void**)&g_pair.h, kPairStage, cudaHostAllocDefault));
+    RFG_CUDA(cudaMalloc((void**)&g_pair.d, kPairStage));
+    RFG_CUDA(cudaMalloc((void**)&g_pair.scratch, kPairScratchWords * 8));
+    g_pair.init = true;
+    return RFG_OK;
+}
+
+/* RFG_OK with *done = false: the pair does not fit the one-trip layout (the caller takes
+ * the batch path) */
+rfg_status score_pair_trip(int metric, int op, int form, const void* s1, int64_t l1, int w1, const void* s2,
+                           int64_t l2, int w2, const ScoreParams& sp, rfg_cutoff cut, int dt, void* result,
+                           bool* done)
+{
+    *done = false;
+    const size_t b1 = (size_t)l1 * w1, b2 = (size_t)l2 * w2;
+    const size_t o1 = kPairHead, o2 = (o1 + b1 + 15) / 16 * 16;
+    if (l1 > kPairMaxLen1 || o2 + b2 + 16 > kPairStage) return RFG_OK;
+    const int fam = metric_family(metric, form, sp);
+    QuerySet qs;
+    const int64_t qo[2] = {0, l1};
+    RFG_TRY(query_info_from_host(s1, qo, 1, w1, &qs));
+    const int hcap = (fam != FAM_WF && fam != FAM_NONE && w2 > 1 && qs.wide[0] > 0) ? next_pow2(2 * qs.wide[0]) : 0;
+    const int wmax = (fam == FAM_WF || fam == FAM_NONE) ? 0 : (int)std::max<int64_t>(1, (l1 + 63) / 64);
+    int64_t per_thread;
+    switch (fam) {
+    case FAM_LEV: per_thread = 2 * (int64_t)wmax; break;
+    case FAM_LCS: per_thread = wmax; break;
+    case FAM_OSA: per_thread = 4 * (int64_t)wmax; break;
+    case FAM_JARO: per_thread = 2 * (int64_t)wmax; break;
+    default: per_thread = l1 + 1;
+    }
+    const int block = 128;
+    const int64_t table = wmax ? (int64_t)(256 + hcap + 1) * wmax + hcap : 0;
+    if (table + block * per_thread > (int64_t)kPairScratchWords) return RFG_OK;
+    RFG_TRY(pair_path_init());
+
+    unsigned char* h = g_pair.h;
+    unsigned char* d = g_pair.d;
+    int64_t* hoff = (int64_t*)h;
+    hoff[0] = 0;
+    hoff[1] = l1;
+    hoff[2] = 0;
+    hoff[3] = l2;
+    ((int32_t*)(h + 32))[0] = 0; /* qlist */
+    ((int32_t*)(h + 36))[0] = 0; /* tile counter */
+    ((int32_t*)(h + 40))[0] = 0; /* check flag */
+    if (b1) memcpy(h + o1, s1, b1);
+    if (b2) memcpy(h + o2, s2, b2);
+    RFG_CUDA(cudaMemcpyAsync(d, h, o2 + b2, cudaMemcpyHostToDevice, g.stream));
+
+    KParams a;
+    memset(&a, 0, sizeof a);
+    a.q = KStrings{d + o1, (const int64_t*)d, 1, w1};
+    a.c = KStrings{d + o2, (const int64_t*)(d + 16), 1, w2};
+    a.qlist = (const int32_t*)(d + 32);
+    a.nq = 1;
+    a.chunk = 1;
+    a.nchunks = 1;
+    a.counter = (int*)(d + 36);
+    a.err = (int*)(d + 40);
+    a.metric = metric;
+    a.op = op;
+    a.form = form;
+    a.sp = sp;
+    a.ci = cut.cutoff_i;
+    a.cf = cut.cutoff_f;
+    a.out = d + 48;
+    a.out_dtype = dt;
+    a.ld = 1;
+    a.hcap = hcap;
+    a.tab_t = -1;
+    a.better_high = better_high_of(op);
+    a.wmax = wmax;
+    a.scratch = g_pair.scratch;
+    a.scratch_per_thread = per_thread;
+    a.scratch_per_cta = table + block * per_thread;
+    const void* fn = generic_kernel(fam == FAM_NONE ? FAM_WF : fam, w2, false);
+    void* args[] = {&a};
+    RFG_CUDA(cudaLaunchKernel(fn, dim3(1), dim3(block), args, 0, g.stream));
+    RFG_CUDA(cudaMemcpyAsync(h + 40, d + 40, 16, cudaMemcpyDeviceToHost, g.stream));
+    RFG_CUDA(cudaStreamSynchronize(g.stream));
+    const int err = ((int32_t*)(h + 40))[0];
+    if (err) return fail(RFG_ERR_DEVICE_CHECK, "device-side check failed (code %d)", err);
+    memcpy(result, h + 48, 8);
+    *done = true;
+    return RFG_OK;
+}
+
 /* one pair through the engine */
 rfg_status score_one(int metric, int op, int form, const void* s1, int64_t l1, int w1, const void* s2, int64_t l2,
                      int w2, const rfg_params* p, rfg_cutoff cut, int dt, void* result)
@@ -851,6 +957,14 @@ rfg_status score_one(int metric, int op, int form, const void* s1, int64_t l1, i
     if (l1 < 0 || l2 < 0) return fail(RFG_ERR_INVALID_ARGUMENT, "negative length");
     if ((!s1 && l1) || (!s2 && l2)) return fail(RFG_ERR_INVALID_ARGUMENT, "string data is NULL");
     if (!result) return fail(RFG_ERR_INVALID_ARGUMENT, "result is NULL");
+    RFG_TRY(check_metric_op(metric, op, form));
+    RFG_TRY(check_dtype(metric, op, dt));
+    const ScoreParams sp = to_sp(p);
+    RFG_TRY(check_params(metric, sp));
+    RFG_TRY(ensure_ctx());
+    bool done = false;
+    RFG_TRY(score_pair_trip(metric, op, form, s1, l1, w1, s2, l2, w2, sp, cut, dt, result, &done));
+    if (done) return RFG_OK;
     int64_t o1[2] = {0, l1}, o2[2] = {0, l2};
     rfg_strings q{s1, o1, 1, w1}, c{s2, o2, 1, w2};
     return cdist_impl(metric, op, form, &q, &c, p, cut, dt, result, 1, 0);
@@ -1038,6 +1152,12 @@ rfg_status rfg_cached_score_i64(rfg_cached h, rfg_op op, const void* s2, int64_t
     if (!h) return fail(RFG_ERR_INVALID_ARGUMENT, "scorer is NULL");
     if (!is_int_result(h->metric, op)) return fail(RFG_ERR_INVALID_ARGUMENT, "this metric/op returns a double");
     if (!valid_width(width2) || len2 < 0 || (!s2 && len2) || !result) return fail(RFG_ERR_INVALID_ARGUMENT, "invalid s2");
+    RFG_TRY(check_metric_op(h->metric, op, RFG_FORM_CACHED));
+    RFG_TRY(ensure_ctx());
+    bool done = false;
+    RFG_TRY(score_pair_trip(h->metric, op, RFG_FORM_CACHED, h->host.data(), h->len, h->width, s2, len2, width2,
+                            to_sp(&h->params), rfg_cutoff{score_cutoff, 0.0, score_hint, 0.0}, RFG_I64, result, &done));
+    if (done) return RFG_OK;
     int64_t off[2] = {0, len2};
     rfg_strings c{s2, off, 1, width2};
     return cached_many(h, op, &c, rfg_cutoff{score_cutoff, 0.0, score_hint, 0.0}, RFG_I64, result, 0);
@@ -1050,6 +1170,12 @@ rfg_status rfg_cached_score_f64(rfg_cached h, rfg_op op, const void* s2, int64_t
     if (!h) return fail(RFG_ERR_INVALID_ARGUMENT, "scorer is NULL");
     if (is_int_result(h->metric, op)) return fail(RFG_ERR_INVALID_ARGUMENT, "this metric/op returns an integer");
     if (!valid_width(width2) || len2 < 0 || (!s2 && len2) || !result) return fail(RFG_ERR_INVALID_ARGUMENT, "invalid s2");
+    RFG_TRY(check_metric_op(h->metric, op, RFG_FORM_CACHED));
+    RFG_TRY(ensure_ctx());
+    bool done = false;
+    RFG_TRY(score_pair_trip(h->metric, op, RFG_FORM_CACHED, h->host.data(), h->len, h->width, s2, len2, width2,
+                            to_sp(&h->params), rfg_cutoff{0, score_cutoff, 0, score_hint}, RFG_F64, result, &done));
+    if (done) return RFG_OK;
     int64_t off[2] = {0, len2};
     rfg_strings c{s2, off, 1, width2};
     return cached_many(h, op, &c, rfg_cutoff{0, score_cutoff, 0, score_hint}, RFG_F64, result, 0);
