@@ -478,8 +478,9 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
                          ((spec.metric == RFG_LEVENSHTEIN && fam == FAM_LEV && spec.sp.ins == 1 &&
                            spec.sp.del == 1 && spec.sp.rep == 1) ||
                           spec.metric == RFG_INDEL || spec.metric == RFG_RATIO || spec.metric == RFG_OSA);
-    const bool mq_ok =
-        (fast_ok || norm_ok) && spec.topk == 0 && !spec.fixed_perm && g_stage_mode != 0 && g_mq_mode != 0;
+    const bool jaro_ok = fam == FAM_JARO && spec.form != RFG_FORM_MULTI;
+    const bool mq_ok = (fast_ok || norm_ok || jaro_ok) && spec.topk == 0 && !spec.fixed_perm && g_stage_mode != 0 &&
+                       g_mq_mode != 0;
     const int32_t* dperm;
     if (spec.fixed_perm) {
         chunk = spec.fixed_chunk;
@@ -559,7 +560,15 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         size_t smem = 0;
         int per_sm;
         const bool use_mq = k == 0 && mq_ok && a.hcap == 0 && stage > 0;
-        if (use_mq) {
+        if (use_mq && fam == FAM_JARO) {
+            fn = tiles_mq_kernel_jaro(c.width);
+            block = g_block_override > 0 ? g_block_override : 256;
+            a.stage = stage;
+            smem = tiles_mq_jaro_smem_bytes(stage);
+            RFG_TRY(allow_dynamic_smem(fn, smem));
+            per_sm = occupancy(fn, block, smem);
+        }
+        else if (use_mq) {
             switch (fam) {
             case FAM_LEV: fn = tiles_mq_kernel_lev(c.width, !fast_ok); break;
             case FAM_LCS: fn = tiles_mq_kernel_lcs(c.width, !fast_ok); break;

@@ -449,6 +449,70 @@ RFG_HD void jaro_word(const PMF& pm, int pl, const TXT& t, int tl, int* common, 
     *transp = tr;
 }
 
+/* Jaro flagging of Q one-word patterns against one text, sharing each fetched block of
+ * text units.  For every pattern q in `active`: the common and (unhalved)
+ * transposition counts of jaro_word(pm_q, pl[q], t, tl, need[q]) -- a pattern whose
+ * count can no longer reach need[q] stops early with both counts 0, and one that ends
+ * below need[q] skips the transpositions.  Every active pattern
+ * must have its effective text end (jaro_bounds) at or below 64. */
+template <int Q, typename PMQ, typename TXT>
+RFG_HD void group_jaro_word(const PMQ& pm, const int* pl, unsigned active, const TXT& t, int tl, const int* need,
+                            int* common, int* transp)
+{
+    u64 pflag[Q], tflag[Q], bmask[Q];
+    int te[Q], lead[Q];
+    unsigned live = active;
+    int temax = 0;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        pflag[q] = tflag[q] = bmask[q] = 0;
+        te[q] = lead[q] = 0;
+        common[q] = transp[q] = 0;
+        if (!((active >> q) & 1u)) continue;
+        int bound = (pl[q] > tl ? pl[q] : tl) / 2;
+        if (bound > 0) --bound;
+        te[q] = tl < pl[q] + bound ? tl : pl[q] + bound;
+        bmask[q] = low_mask(bound + 1);
+        lead[q] = bound < te[q] ? bound : te[q];
+        temax = te[q] > temax ? te[q] : temax;
+    }
+    for (int j0 = 0; j0 < temax && live; j0 += RFG_FETCH) {
+        u64 c[RFG_FETCH];
+#pragma unroll
+        for (int k = 0; k < RFG_FETCH; ++k) c[k] = j0 + k < temax ? t[j0 + k] : 0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            if (!((live >> q) & 1u)) continue;
+#pragma unroll
+            for (int k = 0; k < RFG_FETCH; ++k) {
+                const int j = j0 + k;
+                if (j < te[q]) {
+                    const u64 x = pm(q, c[k]) & bmask[q] & ~pflag[q];
+                    pflag[q] |= blsi(x);
+                    tflag[q] |= (u64)(x != 0) << j;
+                    bmask[q] = j < lead[q] ? (bmask[q] << 1) | 1 : bmask[q] << 1;
+                    if ((j & 3) == 3 && popc64(pflag[q]) + (te[q] - 1 - j) < need[q]) live &= ~(1u << q);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if (!((live >> q) & 1u)) continue;
+        common[q] = popc64(pflag[q]);
+        if (common[q] < need[q]) continue;
+        int tr = 0;
+        u64 pf = pflag[q], tf = tflag[q];
+        while (tf) {
+            const u64 pbit = blsi(pf);
+            tr += (pm(q, t[ctz64(tf)]) & pbit) == 0;
+            tf = blsr(tf);
+            pf ^= pbit;
+        }
+        transp[q] = tr;
+    }
+}
+
 /* ========================================================= multi-word cores
  * PMW: pm(c, w) = word w of the pattern-match vector of c.  W words in registers,
  * pattern length m in (64*(W-1), 64*W] (smaller m works: the extra words stay zero). */

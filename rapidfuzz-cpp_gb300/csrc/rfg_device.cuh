@@ -1056,6 +1056,196 @@ __global__ void __launch_bounds__(256, FAM == FAM_OSA ? RFG_MINB_MQ_OSA : RFG_MI
     }
 }
 
+/* Jaro / Jaro-Winkler over one-word patterns with code units below 256, four queries
+ * per thread: the per-query tables come from k_jaro_tables, the flagging of the four
+ * patterns shares the text fetch (group_jaro_word); a pair outside the tables or with an
+ * effective text end above 64 takes the one-query cores. */
+#ifndef RFG_MINB_MQJ
+#define RFG_MINB_MQJ 3
+#endif
+
+struct MQRow1 {
+    const u64* rows;
+    __device__ __forceinline__ u64 operator()(u64 c) const { return rows[c]; }
+    __device__ __forceinline__ u64 operator()(u64 c, int) const { return rows[c]; }
+};
+
+template <typename CT>
+__global__ void __launch_bounds__(256, RFG_MINB_MQJ) k_tiles_mq_jaro(const KParams a)
+{
+    extern __shared__ u64 smem[];
+    u64* rows = smem;
+    JaroTab* jt = (JaroTab*)(smem + RFG_MQ * 257);
+    unsigned char* stage = (unsigned char*)(jt + RFG_MQ);
+    __shared__ int64_t s_tile;
+    __shared__ int64_t s_q[RFG_MQ];
+    __shared__ int s_m[RFG_MQ];
+    __shared__ u64 s_pre[RFG_MQ][4];
+    const int64_t ngroups = ((int64_t)a.nq + RFG_MQ - 1) / RFG_MQ;
+    const int64_t ntiles = ngroups * a.nchunks;
+    const int tw = (int)(sizeof(JaroTab) / 8);
+    int64_t cur_g = -1;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(a.counter, 1);
+        __syncthreads();
+        const int64_t t = s_tile;
+        if (t >= ntiles) break;
+        const int64_t gi = t / a.nchunks, ch = t % a.nchunks;
+        if (gi != cur_g) {
+            for (int i = threadIdx.x; i < RFG_MQ * 257; i += blockDim.x) rows[i] = 0;
+            if (threadIdx.x < RFG_MQ) {
+                const int64_t k = gi * RFG_MQ + threadIdx.x;
+                int64_t qi = -1;
+                int m = 0;
+                if (k < a.nq) {
+                    qi = a.qlist[k];
+                    m = (int)(a.q.off[qi + 1] - a.q.off[qi]);
+                    if (m > 64) { /* the host classified this query into a smaller class */
+                        atomicExch(a.err, 2);
+                        m = 64;
+                    }
+                }
+                s_q[threadIdx.x] = qi;
+                s_m[threadIdx.x] = m;
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < RFG_MQ * tw; i += blockDim.x) {
+                const int q = i / tw;
+                if (s_q[q] >= 0) ((u64*)(jt + q))[i % tw] = __ldg((const u64*)(a.jtab + s_q[q]) + i % tw);
+            }
+            for (int q = 0; q < RFG_MQ; ++q) {
+                if (s_q[q] < 0) continue;
+                const unsigned char* qb = a.q.data + a.q.off[s_q[q]] * a.q.width;
+                for (int i = threadIdx.x; i < s_m[q]; i += blockDim.x) {
+                    const u64 c = load_unit(qb, a.q.width, i);
+                    /* a unit >= 256 here means one-byte choices, which never hold it */
+                    if (c < 256) atomicOr((unsigned long long*)&rows[q * 257 + c], 1ull << i);
+                }
+                if (threadIdx.x < 4) s_pre[q][threadIdx.x] = (int)threadIdx.x < s_m[q] ? load_unit(qb, a.q.width, threadIdx.x) : 0;
+            }
+            __syncthreads();
+            cur_g = gi;
+        }
+        int m[RFG_MQ];
+        int qn = 0;
+#pragma unroll
+        for (int q = 0; q < RFG_MQ; ++q) {
+            m[q] = s_m[q];
+            if (s_q[q] >= 0) qn = q + 1;
+        }
+        const MQRows pm{rows};
+        const int64_t c0 = ch * a.chunk;
+        const int64_t c1 = c0 + a.chunk < a.c.n ? c0 + a.chunk : a.c.n;
+        for (int64_t s0 = c0; s0 < c1; s0 += a.stage) {
+            const int64_t s1 = s0 + a.stage < c1 ? s0 + a.stage : c1;
+            const int64_t bd = blockDim.x;
+            int64_t p = s0 + threadIdx.x;
+            PosMeta cur{0, 0, 0}, nxt{0, 0, 0};
+            if (p < s1) cur = load_pos(a, p);
+            if (p + bd < s1) nxt = load_pos(a, p + bd);
+            for (; p < s1; p += bd) {
+                const PosMeta pos = cur;
+                cur = nxt;
+                if (p + 2 * bd < s1) nxt = load_pos(a, p + 2 * bd);
+                if (p + bd < s1) prefetch_text(a, cur);
+                const int n = pos.n;
+                const CT* s2 = (const CT*)a.c.data + pos.o;
+                const MQText<CT> txt{s2};
+                u64 t4[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) t4[k] = k < n ? (u64)__ldg(s2 + k) : ~0ull;
+                PairSpec sp;
+                sp.metric = a.metric;
+                sp.op = a.op;
+                sp.form = a.form;
+                sp.ci = a.ci;
+                sp.cf = a.cf;
+                sp.p = a.sp;
+                sp.l2 = (u64)n;
+                int prefix[RFG_MQ], need[RFG_MQ], C[RFG_MQ], Tr[RFG_MQ];
+                double vf[RFG_MQ];
+                unsigned active = 0, decided = 0;
+#pragma unroll
+                for (int q = 0; q < RFG_MQ; ++q) {
+                    prefix[q] = 0;
+                    need[q] = 0;
+                    vf[q] = 0.0;
+                    if (q >= qn) continue;
+                    const int mx = (m[q] < n ? m[q] : n) < 4 ? (m[q] < n ? m[q] : n) : 4;
+                    int pr = 0;
+                    for (; pr < mx; ++pr)
+                        if (t4[pr] != s_pre[q][pr]) break;
+                    prefix[q] = pr;
+                    sp.l1 = (u64)m[q];
+                    int bound = (m[q] > n ? m[q] : n) / 2;
+                    if (bound > 0) --bound;
+                    const int te = n < m[q] + bound ? n : m[q] + bound;
+                    if (n <= a.tab_t) {
+                        const unsigned short mc = jt[q].minc[pr][n];
+                        const int cmax = m[q] < n ? m[q] : n;
+                        const bool one = m[q] == 1 && n == 1;
+                        const bool fail = mc != 0 && !one && (mc == 0xffff || cmax < (int)mc);
+                        if (fail) {
+                            vf[q] = jt[q].vfail[pr];
+                            decided |= 1u << q;
+                        }
+                        else if (mc == 0) {
+                            vf[q] = finish_jaro_tab(sp, jt[q], pr, 0, 0);
+                            decided |= 1u << q;
+                        }
+                        else if (te <= 64) {
+                            need[q] = one ? 0 : (int)mc;
+                            active |= 1u << q;
+                        }
+                        else {
+                            int c = 0, tr = 0;
+                            jaro_multi<1>(MQRow1{rows + q * 257}, m[q], txt, n, &c, &tr);
+                            vf[q] = c < (one ? 0 : (int)mc) ? jt[q].vfail[pr] : finish_jaro_tab(sp, jt[q], pr, c, tr);
+                            decided |= 1u << q;
+                        }
+                    }
+                    else {
+                        /* outside the tables: the reference's filters pair by pair */
+                        int c = 0, tr = 0;
+                        if (m[q] > 0 && n > 0 && jaro_pair_needs_counts(sp, pr)) {
+                            if (te <= 64) jaro_word(MQRow1{rows + q * 257}, m[q], txt, n, &c, &tr);
+                            else jaro_multi<1>(MQRow1{rows + q * 257}, m[q], txt, n, &c, &tr);
+                        }
+                        vf[q] = finish_jaro(sp, pr, c, tr);
+                        decided |= 1u << q;
+                    }
+                }
+                if (active) {
+                    group_jaro_word<RFG_MQ>(pm, m, active, txt, n, need, C, Tr);
+#pragma unroll
+                    for (int q = 0; q < RFG_MQ; ++q) {
+                        if (!((active >> q) & 1u)) continue;
+                        sp.l1 = (u64)m[q];
+                        vf[q] = C[q] < need[q] ? jt[q].vfail[prefix[q]] : finish_jaro_tab(sp, jt[q], prefix[q], C[q], Tr[q]);
+                    }
+                }
+                (void)decided;
+                const int64_t i = pos.ci - s0;
+#pragma unroll
+                for (int q = 0; q < RFG_MQ; ++q)
+                    if (q < qn) ((double*)stage)[(int64_t)q * a.stage + i] = vf[q];
+            }
+            __syncthreads();
+            for (int q = 0; q < qn; ++q) {
+                const int64_t base = s_q[q] * a.ld + s0, nn = s1 - s0;
+                const unsigned long long* src = (const unsigned long long*)stage + (int64_t)q * a.stage;
+                for (int64_t i = threadIdx.x; i < nn; i += blockDim.x) ((unsigned long long*)a.out)[base + i] = src[i];
+            }
+            __syncthreads();
+        }
+    }
+}
+
+inline size_t tiles_mq_jaro_smem_bytes(int64_t stage)
+{
+    return (size_t)RFG_MQ * 257 * 8 + (size_t)RFG_MQ * sizeof(JaroTab) + (size_t)RFG_MQ * stage * 8;
+}
+
 inline size_t tiles_mq_smem_bytes(int64_t stage, int out_dtype, int kd_len)
 {
     return ((size_t)RFG_MQ * 257 + (size_t)RFG_MQ * kd_len) * 8 + (size_t)RFG_MQ * stage * (out_dtype == 0 ? 4 : 8);

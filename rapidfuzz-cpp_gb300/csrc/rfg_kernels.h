@@ -14,6 +14,8 @@ const void* tiles_kernel_jaro(int width, int W, bool topk);
 const void* tiles_mq_kernel_lev(int width, bool norm);
 const void* tiles_mq_kernel_lcs(int width, bool norm);
 const void* tiles_mq_kernel_osa(int width, bool norm);
+/* k_tiles_mq_jaro<CT> (Jaro / Jaro-Winkler, several queries per thread) */
+const void* tiles_mq_kernel_jaro(int width);
 /* k_generic<FAM, CT, TOPK> */
 const void* generic_kernel(int fam, int width, bool topk);
 /* k_topk_merge */
