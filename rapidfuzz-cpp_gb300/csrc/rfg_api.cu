@@ -559,7 +559,12 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         int block;
         size_t smem = 0;
         int per_sm;
-        const bool use_mq = k == 0 && mq_ok && a.hcap == 0 && stage > 0;
+        /* a class with too few (query, chunk) tiles to fill the GPU takes smaller tiles
+         * with direct stores (a staged window must cover whole sorted runs) */
+        const int64_t nchunks_full = (nc + chunk - 1) / chunk;
+        const bool small_class =
+            k < 4 && !topk && (int64_t)cls[bk].size() * nchunks_full < (int64_t)g.sms * 8 && chunk > 256;
+        const bool use_mq = k == 0 && mq_ok && a.hcap == 0 && stage > 0 && !small_class;
         if (use_mq && fam == FAM_JARO) {
             fn = tiles_mq_kernel_jaro(c.width);
             block = g_block_override > 0 ? g_block_override : 256;
@@ -591,7 +596,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             }
             block = g_block_override > 0 ? g_block_override : 256;
             smem = tiles_smem_bytes(W, a.hcap);
-            if (stage) {
+            if (stage && !small_class) {
                 a.stage = stage;
                 smem += (size_t)stage * (spec.out_dtype == RFG_I32 ? 4 : 8);
             }
@@ -614,6 +619,12 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         /* tiles: (query, chunk), longest queries first; persistent CTAs fill every SM */
         const int64_t slots = (int64_t)g.sms * per_sm;
         int64_t cchunk = chunk;
+        if (small_class) {
+            const int64_t want = slots * 4;
+            int64_t cc = ((int64_t)cls[bk].size() * nc + want - 1) / want;
+            cc = std::max<int64_t>(cc, block);
+            cchunk = std::min(chunk, (cc + block - 1) / block * block);
+        }
         if (k == 4 && !topk) {
             /* the any-length class has few, heavy queries: smaller tiles so that every
              * resident CTA gets work (no locality is needed here: results go straight out) */

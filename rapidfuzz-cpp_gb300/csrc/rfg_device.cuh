@@ -517,6 +517,9 @@ __device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, co
                 }
                 fail = common < need;
             }
+            /* counts never read (mc == 0) give the inner Jaro 0.0 unless both strings are
+             * empty: the failing value as well */
+            if (mc == 0 && !(m == 0 && n == 0)) fail = true;
             vf = fail ? lt.jt.vfail[prefix] : finish_jaro_tab(s, lt.jt, prefix, common, transp);
             emit(a, qi, ci, 0, vf, false, s.ci, s.cf, tl, stage, s0);
             return;
@@ -1190,7 +1193,8 @@ __global__ void __launch_bounds__(256, RFG_MINB_MQJ) k_tiles_mq_jaro(const KPara
                             decided |= 1u << q;
                         }
                         else if (mc == 0) {
-                            vf[q] = finish_jaro_tab(sp, jt[q], pr, 0, 0);
+                            /* counts never read: 0.0 inside (the failing value) unless both empty */
+                            vf[q] = (m[q] == 0 && n == 0) ? finish_jaro_tab(sp, jt[q], pr, 0, 0) : jt[q].vfail[pr];
                             decided |= 1u << q;
                         }
                         else if (te <= 64) {
