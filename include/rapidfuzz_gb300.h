@@ -52,7 +52,9 @@ typedef enum {
     RFG_OSA = 3,
     RFG_JARO = 4,
     RFG_JARO_WINKLER = 5,
-    RFG_RATIO = 6 /* fuzz::ratio; only RFG_SIMILARITY */
+    RFG_RATIO = 6,        /* fuzz::ratio; only RFG_SIMILARITY */
+    RFG_PARTIAL_RATIO = 7 /* fuzz::partial_ratio / CachedPartialRatio (fuzz.hpp:128-183,
+                             fuzz_impl.hpp:49-293); only RFG_SIMILARITY, no Multi form */
 } rfg_metric;
 
 /* the four result kinds of every metric (rapidfuzz/details/distance.hpp) */

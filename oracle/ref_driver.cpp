@@ -166,6 +166,10 @@ int score(int metric, int op, int form, const void* a, int64_t la, const void* b
             if (op != RFO_SIMILARITY) return -1;
             *of = fuzz::ratio(s1, s2, cf);
             return 0;
+        case RFO_PARTIAL_RATIO:
+            if (op != RFO_SIMILARITY) return -1;
+            *of = fuzz::partial_ratio(s1, s2, cf);
+            return 0;
         }
         return -1;
     }
@@ -217,6 +221,12 @@ int score(int metric, int op, int form, const void* a, int64_t la, const void* b
     case RFO_RATIO: {
         if (op != RFO_SIMILARITY) return -1;
         fuzz::CachedRatio<C1> sc(s1);
+        *of = sc.similarity(s2, cf);
+        return 0;
+    }
+    case RFO_PARTIAL_RATIO: {
+        if (op != RFO_SIMILARITY) return -1;
+        fuzz::CachedPartialRatio<C1> sc(s1);
         *of = sc.similarity(s2, cf);
         return 0;
     }

@@ -935,6 +935,11 @@ int score_with_pm(int metric, int op, int form, const PM& pm, const S1& s1, cons
         chain_sim(op, std::max(l1, l2), sim, ci, cf, oi, of);
         return 0;
     }
+    case RFO_PARTIAL_RATIO: {
+        if (op != RFO_SIMILARITY) return -1;
+        *of = partial_ratio_score(s1, s2, cf);
+        return 0;
+    }
     case RFO_RATIO: {
         if (op != RFO_SIMILARITY) return -1;
         auto dist = [&](u64 c) { return indel_cached(pm, s1, s2, c); };
@@ -967,6 +972,119 @@ int score_with_pm(int metric, int op, int form, const PM& pm, const S1& s1, cons
     return -1;
 }
 
+/* ------------------------------------------------------------- partial_ratio
+ * fuzz::partial_ratio / CachedPartialRatio::similarity (fuzz_impl.hpp:49-293): the best
+ * fuzz::ratio of the shorter string against every window of its length in the longer
+ * one (searched by bisection with a distance bound, fuzz_impl.hpp:82-149), and against
+ * the shorter prefixes and suffixes of the longer string whose edge unit occurs in the
+ * shorter (fuzz_impl.hpp:151-175); equal lengths also try the other direction
+ * (fuzz_impl.hpp:215-224). */
+
+/* CachedRatio::similarity (fuzz_impl.hpp:43-47) of needle against sub */
+template <typename S1, typename S2>
+double ratio_with_pm(const PM& pm, const S1& needle, const S2& sub, double cutoff)
+{
+    auto dist = [&](u64 c) { return indel_cached(pm, needle, sub, c); };
+    double r = 0;
+    i64 oi = 0;
+    chain_dist(RFO_NORM_SIMILARITY, (u64)needle.n + (u64)sub.n, dist, 0, cutoff / 100.0, &oi, &r);
+    return r * 100.0;
+}
+
+template <typename S1, typename S2>
+bool char_in(const S1& s, u64 c)
+{
+    for (i64 i = 0; i < s.n; ++i)
+        if (s[i] == c) return true;
+    return false;
+}
+
+/* partial_ratio_impl: s1 no longer than s2, both non-empty */
+template <typename S1, typename S2>
+double partial_impl(const S1& s1, const S2& s2, double cutoff)
+{
+    PM pm;
+    pm.build(s1);
+    const i64 len1 = s1.n, len2 = s2.n;
+    double res = 0.0;
+    if (len2 > len1) {
+        const u64 maximum = (u64)len1 * 2;
+        const double ncs = norm_sim_to_norm_dist(cutoff / 100);
+        u64 cutoff_dist = (u64)std::ceil((double)maximum * ncs);
+        u64 best = std::numeric_limits<u64>::max();
+        const u64 NONE = std::numeric_limits<u64>::max();
+        std::vector<u64> scores((size_t)(len2 - len1), NONE);
+        std::vector<std::pair<i64, i64>> windows = {{0, len2 - len1 - 1}}, next;
+        auto eval = [&](i64 pos) -> bool { /* true: a perfect window */
+            if (scores[(size_t)pos] != NONE) return false;
+            S2 sub{s2.p + pos, len1};
+            scores[(size_t)pos] = indel_cached(pm, s1, sub, NONE);
+            if (scores[(size_t)pos] < cutoff_dist) {
+                cutoff_dist = best = scores[(size_t)pos];
+                if (best == 0) return true;
+            }
+            return false;
+        };
+        while (!windows.empty()) {
+            for (const auto& w : windows) {
+                if (eval(w.first)) return 100.0;
+                if (eval(w.second)) return 100.0;
+                const u64 cell_diff = (u64)(w.second - w.first);
+                if (cell_diff == 1) continue;
+                const u64 a = scores[(size_t)w.first], b = scores[(size_t)w.second];
+                const u64 known = a > b ? a - b : b - a;
+                const u64 max_imp = (cell_diff - known / 2) / 2 * 2;
+                const i64 min_score = (i64)std::min(a, b) - (i64)max_imp;
+                if (min_score < (i64)cutoff_dist) {
+                    const i64 center = (i64)(cell_diff / 2);
+                    next.emplace_back(w.first, w.first + center);
+                    next.emplace_back(w.first + center, w.second);
+                }
+            }
+            std::swap(windows, next);
+            next.clear();
+        }
+        double score = 1.0 - (double)best / (double)maximum;
+        score *= 100;
+        if (score >= cutoff) cutoff = res = score;
+    }
+    for (i64 i = 1; i < len1; ++i) {
+        S2 sub{s2.p, i};
+        if (!char_in<S1, S2>(s1, sub[i - 1])) continue;
+        const double r = ratio_with_pm(pm, s1, sub, cutoff);
+        if (r > res) {
+            cutoff = res = r;
+            if (res == 100.0) return res;
+        }
+    }
+    for (i64 i = len2 - len1; i < len2; ++i) {
+        S2 sub{s2.p + i, len2 - i};
+        if (!char_in<S1, S2>(s1, sub[0])) continue;
+        const double r = ratio_with_pm(pm, s1, sub, cutoff);
+        if (r > res) {
+            cutoff = res = r;
+            if (res == 100.0) return res;
+        }
+    }
+    return res;
+}
+
+/* partial_ratio_alignment(...).score (fuzz_impl.hpp:194-227) */
+template <typename S1, typename S2>
+double partial_ratio_score(const S1& s1, const S2& s2, double cutoff)
+{
+    if (s1.n > s2.n) return partial_ratio_score(s2, s1, cutoff);
+    if (cutoff > 100) return 0.0;
+    if (!s1.n || !s2.n) return (double)(s1.n == s2.n) * 100.0;
+    const double score = partial_impl(s1, s2, cutoff);
+    if (score != 100 && s1.n == s2.n) {
+        cutoff = std::max(cutoff, score);
+        const double score2 = partial_impl(s2, s1, cutoff);
+        if (score2 > score) return score2;
+    }
+    return score;
+}
+
 template <typename T>
 void store(void* out, int dtype, i64 idx, i64 vi, double vf, bool is_int)
 {
@@ -978,7 +1096,8 @@ void store(void* out, int dtype, i64 idx, i64 vi, double vf, bool is_int)
 
 bool result_is_int(int metric, int op)
 {
-    if (metric == RFO_JARO || metric == RFO_JARO_WINKLER || metric == RFO_RATIO) return false;
+    if (metric == RFO_JARO || metric == RFO_JARO_WINKLER || metric == RFO_RATIO || metric == RFO_PARTIAL_RATIO)
+        return false;
     return op == RFO_DISTANCE || op == RFO_SIMILARITY;
 }
 

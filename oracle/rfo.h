@@ -31,7 +31,8 @@ enum {
     RFO_OSA = 3,
     RFO_JARO = 4,
     RFO_JARO_WINKLER = 5,
-    RFO_RATIO = 6
+    RFO_RATIO = 6,
+    RFO_PARTIAL_RATIO = 7
 };
 
 /* operations */

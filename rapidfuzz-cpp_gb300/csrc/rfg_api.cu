@@ -143,9 +143,14 @@ inline u64 unit_at(const void* data, int width, int64_t i)
 
 inline bool is_int_result(int metric, int op)
 {
-    if (metric == RFG_JARO || metric == RFG_JARO_WINKLER || metric == RFG_RATIO) return false;
+    if (metric == RFG_JARO || metric == RFG_JARO_WINKLER || metric == RFG_RATIO || metric == RFG_PARTIAL_RATIO)
+        return false;
     return op == RFG_DISTANCE || op == RFG_SIMILARITY;
 }
+
+/* per-thread scratch of the partial_ratio pairs: W + 1 LCS state words, then 5L + 2
+ * 32-bit slots for the window search over a haystack of up to L units */
+inline int64_t partial_scratch_words(int W, int64_t L) { return (int64_t)W + 1 + (5 * L + 2 + 1) / 2; }
 
 inline int next_pow2(int x)
 {
@@ -208,11 +213,16 @@ rfg_status check_strings(const rfg_strings* s, const char* what)
 
 rfg_status check_metric_op(int metric, int op, int form)
 {
-    if (metric < RFG_LEVENSHTEIN || metric > RFG_RATIO) return fail(RFG_ERR_INVALID_ARGUMENT, "unknown metric %d", metric);
+    if (metric < RFG_LEVENSHTEIN || metric > RFG_PARTIAL_RATIO)
+        return fail(RFG_ERR_INVALID_ARGUMENT, "unknown metric %d", metric);
     if (op < RFG_DISTANCE || op > RFG_NORMALIZED_SIMILARITY) return fail(RFG_ERR_INVALID_ARGUMENT, "unknown op %d", op);
     if (form < RFG_FORM_FREE || form > RFG_FORM_MULTI) return fail(RFG_ERR_INVALID_ARGUMENT, "unknown form %d", form);
     if (metric == RFG_RATIO && op != RFG_SIMILARITY)
         return fail(RFG_ERR_INVALID_ARGUMENT, "fuzz::ratio only has a similarity");
+    if (metric == RFG_PARTIAL_RATIO && op != RFG_SIMILARITY)
+        return fail(RFG_ERR_INVALID_ARGUMENT, "fuzz::partial_ratio only has a similarity");
+    if (metric == RFG_PARTIAL_RATIO && form == RFG_FORM_MULTI)
+        return fail(RFG_ERR_INVALID_ARGUMENT, "fuzz::partial_ratio has no experimental::Multi form");
     return RFG_OK;
 }
 
@@ -289,6 +299,7 @@ struct BatchSpec {
     int64_t fixed_chunk = 0;
     const int32_t* chunk_lmin = nullptr;
     const int32_t* chunk_lmax = nullptr;
+    int64_t fixed_maxlen = 0; /* the corpus's longest string */
     /* split the queries into this many contiguous row blocks (host-output pipelining) */
     int row_blocks = 1;
 };
@@ -437,7 +448,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
     for (int64_t b = 0; b < nblk; ++b)
         for (int64_t i = pb->rows[b].first; i < pb->rows[b].second; ++i) {
             int k;
-            if (fam == FAM_WF || fam == FAM_NONE) k = 4;
+            if (fam == FAM_WF || fam == FAM_NONE || fam == FAM_PARTIAL) k = 4;
             else {
                 const int wc = word_class(q.len[i]);
                 k = wc == 1 ? 0 : wc == 2 ? 1 : wc == 4 ? 2 : wc == 8 ? 3 : 4;
@@ -674,6 +685,10 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             case FAM_LCS: per_thread = wmax; break;
             case FAM_OSA: per_thread = 4 * (int64_t)wmax; break;
             case FAM_JARO: per_thread = 2 * (int64_t)wmax; break;
+            case FAM_PARTIAL:
+                per_thread = partial_scratch_words(
+                    wmax, std::max<int64_t>(cls_maxlen[bk], spec.fixed_perm ? spec.fixed_maxlen : max_choice_len));
+                break;
             default: per_thread = cls_maxlen[bk] + 1;
             }
             a.wmax = wmax;
@@ -910,6 +925,7 @@ rfg_status score_pair_trip(int metric, int op, int form, const void* s1, int64_t
     case FAM_LCS: per_thread = wmax; break;
     case FAM_OSA: per_thread = 4 * (int64_t)wmax; break;
     case FAM_JARO: per_thread = 2 * (int64_t)wmax; break;
+    case FAM_PARTIAL: per_thread = partial_scratch_words(wmax, std::max(l1, l2)); break;
     default: per_thread = l1 + 1;
     }
     const int block = 128;
@@ -1034,6 +1050,7 @@ struct rfg_corpus_s {
     KStrings dev{};
     int64_t chunk = 0;
     int64_t count = 0;
+    int64_t maxlen = 0; /* longest string */
 };
 
 struct rfg_multi_s {
@@ -1093,7 +1110,8 @@ rfg_status rfg_cached_create(rfg_metric metric, const void* s1, int64_t len1, in
     std::lock_guard<std::recursive_mutex> lk(g.mu);
     if (!out) return fail(RFG_ERR_INVALID_ARGUMENT, "out is NULL");
     *out = nullptr;
-    RFG_TRY(check_metric_op(metric, metric == RFG_RATIO ? RFG_SIMILARITY : RFG_DISTANCE, RFG_FORM_CACHED));
+    const bool sim_only = metric == RFG_RATIO || metric == RFG_PARTIAL_RATIO;
+    RFG_TRY(check_metric_op(metric, sim_only ? RFG_SIMILARITY : RFG_DISTANCE, RFG_FORM_CACHED));
     if (!valid_width(width1)) return fail(RFG_ERR_INVALID_ARGUMENT, "char width must be 1, 2, 4 or 8");
     if (len1 < 0 || (!s1 && len1)) return fail(RFG_ERR_INVALID_ARGUMENT, "invalid s1");
     RFG_TRY(check_params(metric, to_sp(params)));
@@ -1379,6 +1397,7 @@ rfg_status extract_enqueue(rfg_corpus c, const QuerySet& q, int metric, int op, 
     spec.fixed_chunk = c->chunk;
     spec.chunk_lmin = c->lmin.as<int32_t>();
     spec.chunk_lmax = c->lmax.as<int32_t>();
+    spec.fixed_maxlen = c->maxlen;
     RFG_TRY(prepare_batch(q, c->dev, spec, &job->pb));
     if (st != g.stream) {
         /* uploads, resets and the tile lists were enqueued on the library stream */
@@ -1485,7 +1504,10 @@ rfg_status rfg_corpus_create(const rfg_strings* C, uint32_t flags, rfg_corpus* o
         /* one global length order: chunks then hold narrow length ranges that extract
          * tiles can test against the running threshold */
         std::vector<int32_t> len(nc), perm;
-        for (int64_t i = 0; i < nc; ++i) len[i] = (int32_t)std::min<int64_t>(off[i + 1] - off[i], INT32_MAX);
+        for (int64_t i = 0; i < nc; ++i) {
+            len[i] = (int32_t)std::min<int64_t>(off[i + 1] - off[i], INT32_MAX);
+            c->maxlen = std::max<int64_t>(c->maxlen, len[i]);
+        }
         chunk_length_order(len, nc, &perm);
         const int64_t nch = (nc + c->chunk - 1) / c->chunk;
         std::vector<int32_t> lmin(nch), lmax(nch);

@@ -167,12 +167,12 @@ RFG_HD double dmax(double a, double b) { return (a < b) ? b : a; }
 
 /* ----------------------------------------------------------- metric/op enums */
 
-enum Metric { LEVENSHTEIN = 0, INDEL = 1, LCSSEQ = 2, OSA = 3, JARO = 4, JARO_WINKLER = 5, RATIO = 6 };
+enum Metric { LEVENSHTEIN = 0, INDEL = 1, LCSSEQ = 2, OSA = 3, JARO = 4, JARO_WINKLER = 5, RATIO = 6, PARTIAL_RATIO = 7 };
 enum Op { DISTANCE = 0, SIMILARITY = 1, NORM_DISTANCE = 2, NORM_SIMILARITY = 3 };
 enum Form { FORM_FREE = 0, FORM_CACHED = 1, FORM_MULTI = 2 };
 
 /* bit-parallel core family a (metric, weights) pair runs on */
-enum Family { FAM_LEV = 0, FAM_LCS = 1, FAM_OSA = 2, FAM_JARO = 3, FAM_WF = 4, FAM_NONE = 5 };
+enum Family { FAM_LEV = 0, FAM_LCS = 1, FAM_OSA = 2, FAM_JARO = 3, FAM_WF = 4, FAM_NONE = 5, FAM_PARTIAL = 6 };
 
 struct ScoreParams {
     i64 ins, del, rep;     /* Levenshtein weights */
@@ -1084,6 +1084,7 @@ RFG_HD int metric_family(int metric, int form, const ScoreParams& p)
     case LCSSEQ:
     case RATIO: return FAM_LCS;
     case OSA: return FAM_OSA;
+    case PARTIAL_RATIO: return FAM_PARTIAL;
     default: return FAM_JARO;
     }
 }
@@ -1634,6 +1635,164 @@ RFG_HD bool jaro_pair_needs_counts(const PairSpec& s, i64 prefix)
 {
     if (s.form == FORM_MULTI) return s.l2 != 0;
     return jaro_needs_counts((i64)s.l1, (i64)s.l2, jaro_cutoff_for(s, prefix));
+}
+
+/* ---------------------------------------------------------- partial_ratio
+ * fuzz::partial_ratio / CachedPartialRatio::similarity (fuzz_impl.hpp:49-293) for a
+ * query q (pattern table pm, W words) and a choice c, both given as resolved rows.
+ * Every LCS runs on the query's table: against windows of the choice directly, and
+ * with the query in the haystack role through a shifted view of the table (the table
+ * of q[a, a+L) is bits a..a+L-1 of q's table), so no per-pair table is built.
+ * Scratch: st holds W + 1 state words; work holds 5 * |m - n| + 2 32-bit slots. */
+
+/* pattern table of q[a, a + L) from q's table */
+template <typename PMW>
+struct PMShift {
+    const PMW* pm;
+    int W, a, L;
+    RFG_HD u64 operator()(u64 c, int w) const
+    {
+        const int bit = a + 64 * w, w0 = bit >> 6, sh = bit & 63;
+        u64 x = w0 < W ? (*pm)(c, w0) >> sh : 0;
+        if (sh && w0 + 1 < W) x |= (*pm)(c, w0 + 1) << (64 - sh);
+        const int rem = L - 64 * w;
+        return rem >= 64 ? x : x & low_mask(rem < 0 ? 0 : rem);
+    }
+};
+
+/* text rows t[a, a + L) */
+template <typename TXT>
+struct TextSlice {
+    const TXT* t;
+    int a;
+    RFG_HD u64 operator[](int j) const { return (*t)[a + j]; }
+};
+
+/* CachedRatio::similarity from an exact LCS (fuzz_impl.hpp:43-47 over the Indel chain) */
+RFG_HD double ratio_from_lcs(u64 l1, u64 l2, u64 lcs, double cutoff)
+{
+    const u64 M = l1 + l2;
+    const u64 K = norm_cut(NORM_SIMILARITY, M, cutoff, 1);
+    u64 d = M - 2 * lcs;
+    d = d <= K ? d : K + 1;
+    return (M != 0 && d > K && abs_le_bits(cutoff, 200.0)) ? 0.0 : ratio_finish(M, d, cutoff, K);
+}
+
+/* partial_ratio_impl with needle = q (QN = true: q shorter or equal) or needle = c */
+template <bool QN, typename PMW, typename TXT>
+RFG_HD double partial_impl_dev(const PMW& pm, int W, int m, const TXT& c, int n, double cutoff, u64* st, u32* work)
+{
+    const int len1 = QN ? m : n, len2 = QN ? n : m;
+    double res = 0.0;
+    /* LCS of the needle against haystack[a, a + L) */
+    auto lcs_at = [&](int a, int L) -> u64 {
+        if (QN) {
+            const TextSlice<TXT> sub{&c, a};
+            return m ? (u64)lcs_multi_rt(pm, W, m, sub, L, (i64)1 << 62, st) : 0;
+        }
+        const PMShift<PMW> pq{&pm, W, a, L};
+        return L ? (u64)lcs_multi_rt(pq, (L + 63) / 64, L, c, n, (i64)1 << 62, st) : 0;
+    };
+    /* does the needle hold the haystack unit at position i */
+    auto needle_has = [&](int i) -> bool {
+        if (QN) {
+            const u64 r = c[i];
+            for (int w = 0; w < W; ++w)
+                if (pm(r, w)) return true;
+            return false;
+        }
+        /* the haystack is q: q[i] occurs in c when some c[j] has bit i in q's table */
+        const int bit = i;
+        for (int j = 0; j < n; ++j) {
+            const u64 r = c[j];
+            if ((pm(r, bit >> 6) >> (bit & 63)) & 1u) return true;
+        }
+        return false;
+    };
+    if (len2 > len1) {
+        const u64 maximum = (u64)len1 * 2;
+        u64 cutoff_dist = ceil_cut(maximum, norm_sim_to_norm_dist(ddiv(cutoff, 100.0)));
+        u64 best = ~0ull;
+        const int L = len2 - len1;
+        const u32 NONE = 0xffffffffu;
+        u32* scores = work;
+        u32* wa = work + L;          /* windows of this level: pairs */
+        u32* wb = work + 3 * L + 1;  /* windows of the next level */
+        for (int i = 0; i < L; ++i) scores[i] = NONE;
+        int na = 1, nb = 0;
+        wa[0] = 0;
+        wa[1] = (u32)(L - 1);
+        while (na) {
+            for (int k = 0; k < na; ++k) {
+                const int first = (int)wa[2 * k], second = (int)wa[2 * k + 1];
+                for (int e = 0; e < 2; ++e) {
+                    const int pos = e ? second : first;
+                    if (scores[pos] != NONE) continue;
+                    const u64 lcs = lcs_at(pos, len1);
+                    scores[pos] = (u32)(2 * (u64)len1 - 2 * lcs);
+                    if ((u64)scores[pos] < cutoff_dist) {
+                        cutoff_dist = best = scores[pos];
+                        if (best == 0) return 100.0;
+                    }
+                }
+                const u64 cell_diff = (u64)(second - first);
+                if (cell_diff == 1) continue;
+                const u64 sa = scores[first], sb = scores[second];
+                const u64 known = sa > sb ? sa - sb : sb - sa;
+                const u64 max_imp = (cell_diff - known / 2) / 2 * 2;
+                const i64 min_score = (i64)(sa < sb ? sa : sb) - (i64)max_imp;
+                if (min_score < (i64)cutoff_dist) {
+                    const int center = (int)(cell_diff / 2);
+                    wb[2 * nb] = (u32)first;
+                    wb[2 * nb + 1] = (u32)(first + center);
+                    wb[2 * nb + 2] = (u32)(first + center);
+                    wb[2 * nb + 3] = (u32)second;
+                    nb += 2;
+                }
+            }
+            u32* tmp = wa;
+            wa = wb;
+            wb = tmp;
+            na = nb;
+            nb = 0;
+        }
+        double score = dsub(1.0, ddiv((double)best, (double)maximum));
+        score = dmul(score, 100.0);
+        if (score >= cutoff) cutoff = res = score;
+    }
+    for (int i = 1; i < len1; ++i) {
+        if (!needle_has(i - 1)) continue;
+        const double r = ratio_from_lcs((u64)len1, (u64)i, lcs_at(0, i), cutoff);
+        if (r > res) {
+            cutoff = res = r;
+            if (res == 100.0) return res;
+        }
+    }
+    for (int i = len2 - len1; i < len2; ++i) {
+        if (!needle_has(i)) continue;
+        const double r = ratio_from_lcs((u64)len1, (u64)(len2 - i), lcs_at(i, len2 - i), cutoff);
+        if (r > res) {
+            cutoff = res = r;
+            if (res == 100.0) return res;
+        }
+    }
+    return res;
+}
+
+/* partial_ratio_alignment(q, c, cutoff).score (fuzz_impl.hpp:194-227) */
+template <typename PMW, typename TXT>
+RFG_HD double partial_ratio_dev(const PMW& pm, int W, int m, const TXT& c, int n, double cutoff, u64* st, u32* work)
+{
+    if (cutoff > 100) return 0.0;
+    if (!m || !n) return (double)(m == n) * 100.0;
+    if (m > n) return partial_impl_dev<false>(pm, W, m, c, n, cutoff, st, work);
+    const double score = partial_impl_dev<true>(pm, W, m, c, n, cutoff, st, work);
+    if (score != 100 && m == n) {
+        cutoff = dmax(cutoff, score);
+        const double score2 = partial_impl_dev<false>(pm, W, m, c, n, cutoff, st, work);
+        if (score2 > score) return score2;
+    }
+    return score;
 }
 
 /* Per-query tables of the Jaro chains (free / Cached forms): everything that depends

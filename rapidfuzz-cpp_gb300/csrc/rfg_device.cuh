@@ -181,7 +181,7 @@ __device__ __forceinline__ void store_result(const KParams& a, int64_t q, int64_
 
 __device__ __forceinline__ bool result_is_int(int metric, int op)
 {
-    if (metric == JARO || metric == JARO_WINKLER || metric == RATIO) return false;
+    if (metric == JARO || metric == JARO_WINKLER || metric == RATIO || metric == PARTIAL_RATIO) return false;
     return op == DISTANCE || op == SIMILARITY;
 }
 
@@ -770,6 +770,12 @@ __device__ __forceinline__ void score_pair_generic(const KParams& a, const u64* 
     const TextRows<CT, (sizeof(CT) > 1)> txt{s2, keys, a.hcap};
     i64 vi = 0;
     double vf = 0.0;
+    if (FAM == FAM_PARTIAL) {
+        /* fuzz::partial_ratio: W + 1 state words, then the window bookkeeping */
+        vf = partial_ratio_dev(pm, W, m, txt, n, s.cf, st, (u32*)(st + W + 1));
+        emit(a, qi, ci, 0, vf, false, s.ci, s.cf, tl);
+        return;
+    }
     if (FAM == FAM_JARO) {
         const RawQuery q{qb, a.q.width};
         i64 prefix = 0;

@@ -13,6 +13,7 @@ static const void* pick_generic(int fam)
     case FAM_OSA: return (const void*)&k_generic<FAM_OSA, CT, TOPK>;
     case FAM_JARO: return (const void*)&k_generic<FAM_JARO, CT, TOPK>;
     case FAM_WF: return (const void*)&k_generic<FAM_WF, CT, TOPK>;
+    case FAM_PARTIAL: return (const void*)&k_generic<FAM_PARTIAL, CT, TOPK>;
     }
     return nullptr;
 }

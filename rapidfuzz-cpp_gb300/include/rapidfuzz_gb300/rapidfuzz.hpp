@@ -482,6 +482,43 @@ struct CachedRatio : rapidfuzz_gb300::detail::CachedScorer {
     }
 };
 
+/* fuzz.hpp:128-147 (partial_ratio, fuzz_impl.hpp:194-239) */
+template <typename Sentence1, typename Sentence2>
+double partial_ratio(const Sentence1& s1, const Sentence2& s2, double score_cutoff = 0)
+{
+    return detail::score_f(RFG_PARTIAL_RATIO, RFG_SIMILARITY, detail::units(s1), detail::units(s2),
+                           rfg_params{1, 1, 1, 0.1}, score_cutoff, score_cutoff);
+}
+template <typename InputIt1, typename InputIt2, detail::if_iter<InputIt1> = 0>
+double partial_ratio(InputIt1 first1, InputIt1 last1, InputIt2 first2, InputIt2 last2, double score_cutoff = 0)
+{
+    return detail::score_f(RFG_PARTIAL_RATIO, RFG_SIMILARITY, detail::units(first1, last1),
+                           detail::units(first2, last2), rfg_params{1, 1, 1, 0.1}, score_cutoff, score_cutoff);
+}
+
+/* fuzz.hpp:158-183 (CachedPartialRatio, fuzz_impl.hpp:241-283) */
+template <typename CharT1>
+struct CachedPartialRatio : rapidfuzz_gb300::detail::CachedScorer {
+    template <typename Sentence1>
+    CachedPartialRatio(const Sentence1& s1)
+        : CachedScorer(RFG_PARTIAL_RATIO, rapidfuzz_gb300::detail::units(s1), rfg_params{1, 1, 1, 0.1})
+    {}
+    template <typename InputIt1, rapidfuzz_gb300::detail::if_iter<InputIt1> = 0>
+    CachedPartialRatio(InputIt1 first1, InputIt1 last1)
+        : CachedScorer(RFG_PARTIAL_RATIO, rapidfuzz_gb300::detail::units(first1, last1), rfg_params{1, 1, 1, 0.1})
+    {}
+    template <typename Sentence2>
+    double similarity(const Sentence2& s2, double score_cutoff = 0.0, double score_hint = 0.0) const
+    {
+        return cached_f(RFG_SIMILARITY, rapidfuzz_gb300::detail::units(s2), score_cutoff, score_hint);
+    }
+    template <typename InputIt2, rapidfuzz_gb300::detail::if_iter<InputIt2> = 0>
+    double similarity(InputIt2 first2, InputIt2 last2, double score_cutoff = 0.0, double score_hint = 0.0) const
+    {
+        return cached_f(RFG_SIMILARITY, rapidfuzz_gb300::detail::units(first2, last2), score_cutoff, score_hint);
+    }
+};
+
 } // namespace fuzz
 
 /* ---------------------------------------------------------------- Multi* */

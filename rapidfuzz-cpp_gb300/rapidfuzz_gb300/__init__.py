@@ -6,7 +6,7 @@ batched all-pairs path.  Strings are str, bytes, or numpy arrays of unsigned cod
 There is no CPU fallback: importing fails when the CUDA library has not been built.
 """
 from ._lib import (DISTANCE, SIMILARITY, NORMALIZED_DISTANCE, NORMALIZED_SIMILARITY,  # noqa: F401
-                   LEVENSHTEIN, INDEL, LCSSEQ, OSA, JARO, JARO_WINKLER, RATIO,
+                   LEVENSHTEIN, INDEL, LCSSEQ, OSA, JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO,
                    FORM_FREE, FORM_CACHED, FORM_MULTI, I32, I64, F64,
                    DEVICE_INPUTS, DEVICE_OUTPUT, RapidfuzzError, lib, lib_path,
                    as_units, pack_strings, score, Cached, Multi, cdist, Batch, library_stream, Corpus, Server)

@@ -1,7 +1,7 @@
 """The reference's function and class names over the generic entry points
 (rapidfuzz/distance/*.hpp, rapidfuzz/fuzz.hpp)."""
 from ._lib import (DISTANCE, SIMILARITY, NORMALIZED_DISTANCE, NORMALIZED_SIMILARITY, LEVENSHTEIN, INDEL, LCSSEQ,
-                   OSA, JARO, JARO_WINKLER, RATIO, Cached, Multi, score)
+                   OSA, JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO, Cached, Multi, score)
 
 __all__ = []
 
@@ -36,6 +36,14 @@ def fuzz_ratio(s1, s2, score_cutoff=0.0):
 
 
 __all__.append("fuzz_ratio")
+
+
+def fuzz_partial_ratio(s1, s2, score_cutoff=0.0):
+    """fuzz::partial_ratio (fuzz_impl.hpp:194-239)"""
+    return score(PARTIAL_RATIO, SIMILARITY, s1, s2, score_cutoff)
+
+
+__all__.append("fuzz_partial_ratio")
 
 
 class _CachedBase:
@@ -77,6 +85,19 @@ class CachedRatio:
 
 
 __all__.append("CachedRatio")
+
+
+class CachedPartialRatio:
+    """fuzz::CachedPartialRatio (fuzz_impl.hpp:241-283)"""
+
+    def __init__(self, s1):
+        self._c = Cached(PARTIAL_RATIO, s1)
+
+    def similarity(self, s2, score_cutoff=0.0, score_hint=0.0):
+        return self._c.score(SIMILARITY, s2, score_cutoff, score_hint)
+
+
+__all__.append("CachedPartialRatio")
 
 
 class experimental:

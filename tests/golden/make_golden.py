@@ -6,7 +6,9 @@ Three fixtures:
                 the test file:line it restates), with the value the reference computes here;
   random.json   seeded random cases over every metric x op x API form x cutoff, char widths
                 1/2/4/8, lengths 0..300 (word, multi-word, banded and any-length paths);
-  multi.json    Multi* batches with several inserted strings.
+  multi.json    Multi* batches with several inserted strings;
+  partial.json  fuzz::partial_ratio / CachedPartialRatio: the reference fuzz tests' inputs and
+                seeded random pairs.
 Doubles are stored with float.hex() so the comparison is bit-exact.
 
 Usage: python tests/golden/make_golden.py   (needs the reference checkout; run in the
@@ -23,10 +25,11 @@ sys.path.insert(0, os.path.dirname(HERE))
 import numpy as np  # noqa: E402
 
 from oracle_lib import (DISTANCE, SIMILARITY, NORM_DISTANCE, NORM_SIMILARITY, LEVENSHTEIN, INDEL, LCSSEQ, OSA,  # noqa: E402
-                        JARO, JARO_WINKLER, RATIO, FREE, CACHED, MULTI, as_units, reference, result_is_int,
+                        JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO, FREE, CACHED, MULTI, as_units, reference, result_is_int,
                         score, make_params, pack_strings, strings_struct)
 
 OPS = (DISTANCE, SIMILARITY, NORM_DISTANCE, NORM_SIMILARITY)
+REF_ROOT = os.environ.get("RFG_REFERENCE", "/root/reference")  # the reference checkout (build container)
 
 
 def enc(v):
@@ -296,10 +299,74 @@ def multi_cases(seed=3):
     return out
 
 
+def fuzz_test_literals():
+    """the string literals of test/tests-fuzz.cpp (adjacent literals joined as C++ does)"""
+    import re
+    text = open(os.path.join(REF_ROOT, "test", "tests-fuzz.cpp"), encoding="utf-8").read()
+    lits, cur, last_end = [], None, -1
+    for mt in re.finditer(r'"((?:[^"\\]|\\.)*)"', text):
+        gap = text[last_end:mt.start()] if last_end >= 0 else "x"
+        val = bytes(mt.group(1), "utf-8").decode("unicode_escape")
+        if cur is not None and gap.strip() == "":
+            cur += val
+        else:
+            if cur is not None:
+                lits.append(cur)
+            cur = val
+        last_end = mt.end()
+    if cur is not None:
+        lits.append(cur)
+    seen, out = set(), []
+    for x in lits:
+        if x not in seen and "::" not in x and "%" not in x:
+            seen.add(x)
+            out.append(x)
+    return out
+
+
+def partial_cases(seed=11):
+    """fuzz::partial_ratio / CachedPartialRatio: the inputs of the reference's fuzz tests
+    (test/tests-fuzz.cpp, its partial_ratio sections and issue regressions) paired
+    with each other, then seeded random pairs (needle lengths 0..130, haystacks 0..300,
+    every char width, cutoffs 0..101)."""
+    T = "test/tests-fuzz.cpp"
+    lits = fuzz_test_literals()
+    out = []
+    for i, a in enumerate(lits):
+        for b in (lits[i], lits[(i + 1) % len(lits)], lits[(i + 3) % len(lits)]):
+            out.append(case(PARTIAL_RATIO, SIMILARITY, FREE, a, b, cite=T))
+            out.append(case(PARTIAL_RATIO, SIMILARITY, CACHED, b, a, 50.0, cite=T))
+    rng = random.Random(seed)
+    while len(out) < 3000:
+        alpha = rng.choice(ALPHABETS)
+        n1 = rng.choice([0, 1, 2, 3, 5, 8, 16, 31, 40, 63, 64, 65, 100, 130])
+        n2 = rng.choice([0, 1, 4, 16, 40, 64, 65, 100, 200, 300])
+        s1 = rand_str(rng, alpha, 0, n1)
+        if rng.random() < 0.5 and len(s1) < 300:
+            s2 = rand_str(rng, alpha, 0, n2)
+            at = rng.randint(0, len(s2))
+            s2 = s2[:at] + mutate(rng, s1, alpha, rng.randint(0, 4)) + s2[at:]
+        else:
+            s2 = rand_str(rng, alpha, 0, n2)
+        if rng.random() < 0.3:
+            s1, s2 = s2, s1
+        mx1, mx2 = max(s1 + [0]), max(s2 + [0])
+        w1 = 8 if mx1 >= 2**32 else (4 if mx1 >= 65536 else rng.choice([1, 2, 4]) if mx1 < 256 else 2 if mx1 < 65536 else 4)
+        w2 = 8 if mx2 >= 2**32 else (4 if mx2 >= 65536 else rng.choice([1, 2, 4]) if mx2 < 256 else 2 if mx2 < 65536 else 4)
+        cutoff = rng.choice([None, 0.0, 30.0, 50.0, 70.0, 85.0, 95.0, 100.0, 101.0])
+        c = case(PARTIAL_RATIO, SIMILARITY, rng.choice([FREE, CACHED]), s1, s2, cutoff, w1=w1, w2=w2)
+        if c is not None:
+            out.append(c)
+    return [c for c in out if c is not None]
+
+
 def main():
     if reference() is None:
         sys.exit("oracle/_ref/librfref.so is missing: run `make -C oracle ref` where the reference checkout exists")
-    for name, cases in (("kat.json", kat_cases()), ("random.json", random_cases(4000)), ("multi.json", multi_cases())):
+    which = sys.argv[1:] or ["kat.json", "random.json", "multi.json", "partial.json"]
+    gens = {"kat.json": kat_cases, "random.json": lambda: random_cases(4000), "multi.json": multi_cases,
+            "partial.json": partial_cases}
+    for name, cases in ((n, gens[n]()) for n in which):
         with open(os.path.join(HERE, name), "w") as f:
             json.dump(cases, f, separators=(",", ":"))
         print(name, len(cases))

@@ -10,7 +10,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 
-LEVENSHTEIN, INDEL, LCSSEQ, OSA, JARO, JARO_WINKLER, RATIO = range(7)
+LEVENSHTEIN, INDEL, LCSSEQ, OSA, JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO = range(8)
 DISTANCE, SIMILARITY, NORM_DISTANCE, NORM_SIMILARITY = range(4)
 FREE, CACHED, MULTI = range(3)
 METRIC_NAMES = ["levenshtein", "indel", "lcsseq", "osa", "jaro", "jaro_winkler", "ratio"]
@@ -27,7 +27,7 @@ class Strings(ctypes.Structure):
 
 
 def result_is_int(metric, op):
-    if metric in (JARO, JARO_WINKLER, RATIO):
+    if metric in (JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO):
         return False
     return op in (DISTANCE, SIMILARITY)
 
@@ -129,7 +129,7 @@ def score(lib_fn, metric, op, form, s1, s2, cutoff=None, weights=(1, 1, 1), pref
     else:
         ci = 0
         if cutoff is None:
-            cf = 1.0 if op in (DISTANCE, NORM_DISTANCE) and metric not in (RATIO,) else 0.0
+            cf = 1.0 if op in (DISTANCE, NORM_DISTANCE) and metric not in (RATIO, PARTIAL_RATIO) else 0.0
         else:
             cf = float(cutoff)
     oi = ctypes.c_int64(0)

@@ -31,7 +31,8 @@ def _strings(rng, n, alpha, lo, hi, base=None):
 
 CASES = [(R.LEVENSHTEIN, R.DISTANCE, None), (R.LEVENSHTEIN, R.DISTANCE, 12), (R.INDEL, R.NORMALIZED_SIMILARITY, 0.6),
          (R.OSA, R.SIMILARITY, 5), (R.LCSSEQ, R.SIMILARITY, None), (R.JARO_WINKLER, R.SIMILARITY, 0.0),
-         (R.JARO_WINKLER, R.SIMILARITY, 0.85), (R.RATIO, R.SIMILARITY, 50.0), (R.JARO, R.NORMALIZED_DISTANCE, 0.3)]
+         (R.JARO_WINKLER, R.SIMILARITY, 0.85), (R.RATIO, R.SIMILARITY, 50.0), (R.JARO, R.NORMALIZED_DISTANCE, 0.3),
+         (R.PARTIAL_RATIO, R.SIMILARITY, 60.0)]
 
 
 @pytest.mark.parametrize("metric,op,cut", CASES)

@@ -27,7 +27,7 @@ def gpu_score(c, a, b):
     return int(v) if R._lib.result_is_int(m, op) else float(v)
 
 
-@pytest.mark.parametrize("fixture", ["kat.json", "random.json"])
+@pytest.mark.parametrize("fixture", ["kat.json", "random.json", "partial.json"])
 def test_fixtures_per_call(fixture):
     bad = []
     for c in G.load(fixture):
@@ -194,3 +194,47 @@ def test_cdist_several_queries_per_thread(metric, width):
             for out_dtype in (R.I32, R.I64):
                 got = R.cdist(metric, R.DISTANCE, q, c, cut, out_dtype=out_dtype)
                 assert np.array_equal(got.astype(np.int64), exp), (nq, cut, out_dtype)
+
+
+@pytest.mark.parametrize("shape", ["short", "long", "wide"])
+def test_cdist_partial_ratio_matches_oracle(shape):
+    """fuzz::partial_ratio over batches: needles shorter, longer and equal to the
+    haystacks, embedded near-copies, several cutoffs, the CachedPartialRatio form"""
+    rng = random.Random({"short": 31, "long": 32, "wide": 33}[shape])
+    if shape == "short":
+        alpha, qlo, qhi, clo, chi, w = list(range(97, 103)), 0, 20, 0, 60, 1
+    elif shape == "long":
+        alpha, qlo, qhi, clo, chi, w = [65, 67, 71, 84], 30, 150, 0, 260, 1
+    else:
+        alpha, qlo, qhi, clo, chi, w = [0x41, 0xC0, 300, 70000, 0x20], 0, 40, 0, 90, 4
+    qs = [_rand(rng, alpha, qlo, qhi) for _ in range(13)] + [[]]
+    cs = []
+    for _ in range(61):
+        r = rng.random()
+        if r < 0.4 and qs:
+            base = rng.choice(qs)
+            pre, post = _rand(rng, alpha, 0, 20), _rand(rng, alpha, 0, 20)
+            cs.append(pre + _mut(rng, base, alpha, rng.randint(0, 3)) + post)
+        elif r < 0.5:
+            cs.append(list(rng.choice(qs)))
+        else:
+            cs.append(_rand(rng, alpha, clo, chi))
+    cs.append([])
+    dt = {1: np.uint8, 4: np.uint32}[w]
+    q = R.pack_strings([np.array(s, dtype=dt) for s in qs], w)
+    c = R.pack_strings([np.array(s, dtype=dt) for s in cs], w)
+    for cut in (0.0, 50.0, 80.0, 100.0, 100.5):
+        got = R.cdist(R.PARTIAL_RATIO, R.SIMILARITY, q, c, cut)
+        exp = oracle_cdist(R.PARTIAL_RATIO, R.SIMILARITY, q, c, cut)
+        bad = np.argwhere(got.view(np.int64) != exp.view(np.int64))
+        assert bad.size == 0, "cut %r mismatch at %r: got %r exp %r" % (cut, bad[0], got[tuple(bad[0])],
+                                                                        exp[tuple(bad[0])])
+
+
+def test_partial_ratio_api_names():
+    """the reference's names: fuzz::partial_ratio and CachedPartialRatio"""
+    o = oracle()
+    for a, b in (("001", "220222"), ("physics 2 vid", "study physics physics 2 video"), ("", ""), ("abc", "")):
+        exp = oscore(o.rfo_score, R.PARTIAL_RATIO, R.SIMILARITY, FREE, a.encode(), b.encode(), 0.0)
+        assert G.same(R.fuzz_partial_ratio(a, b), exp)
+        assert G.same(R.CachedPartialRatio(a).similarity(b), exp)
