@@ -10,6 +10,8 @@ cfg3  Levenshtein normalized_distance with score_cutoff 0.1 (cutoff = 10 % of th
       choice unrelated or a query mutated at 1-15 %: multi-word and banded kernels.
 cfg4  Jaro-Winkler (prefix_weight 0.1, cutoff 0.85) and fuzz::ratio (cutoff 85) over uint32
       code-point token strings, 1,024 x 1,000,000, dense float64 outputs kept on the device.
+partial  fuzz::partial_ratio (cutoff 80) of 256 token queries against 200,000 token strings
+      (uint32, as in cfg4), dense float64 out on the device (the first widening of the path).
 cfg5  serving: device-resident corpora of 10,000,000 DNA strings (len U[10,200]) and
       1,000,000 uint32 token strings; Poisson arrivals (--rate req/s for --duration s), each
       an extractOne (limit 1) or top-10 extract of one query of length U[5,500] with a metric
@@ -164,6 +166,37 @@ def run(args, rank, world, local):
                      "e2e": None, "gpu_launches": steps, "clocks": clk})
     elif args.workload == "cfg5":
         return run_serving(args, R, WL)
+    elif args.workload == "partial":
+        nq = 256
+        nc = args.nc if args.nc != 4096 else 200000
+        (q, ql) = WL.tokens_u32(seed=41, n=nq)
+        c = WL.tokens_u32_fast(seed=42, n=nc)
+        cells = _cells(q, c)
+        qd, kq = _dev(torch, q, dev)
+        cd, kc = _dev(torch, c, dev)
+        out = torch.empty((nq, nc), dtype=torch.float64, device=dev)
+        b = R.Batch(R.PARTIAL_RATIO, R.SIMILARITY, qd, cd, out.data_ptr(), 80.0, out_dtype=R.F64,
+                    flags=R.DEVICE_INPUTS)
+        if not args.no_tune:
+            b.tune(stream.cuda_stream)
+        t, per, clk = _timed_batches(torch, [b], stream, steps, warmup, flush)
+        rows = [0, 127, 255]
+        qrows = (np.concatenate([q[0][q[1][r]:q[1][r + 1]] for r in rows]),
+                 np.concatenate([[0], np.cumsum([q[1][r + 1] - q[1][r] for r in rows])]).astype(np.int64), 4)
+        exp = oracle_cdist(R.PARTIAL_RATIO, R.SIMILARITY, qrows, c, 80.0)
+        assert np.array_equal(out[rows].cpu().numpy().view(np.int64), exp.view(np.int64)), "partial parity"
+        sub = 4
+        qsub = (q[0][:q[1][sub]], q[1][:sub + 1].copy(), 4)
+        tc0 = time.perf_counter()
+        oracle_cdist(R.PARTIAL_RATIO, R.SIMILARITY, qsub, c, 80.0)
+        tc = time.perf_counter() - tc0
+        line.update({"value": nq * nc * steps / t, "unit": "pairs/s", "ms_per_step": t / steps * 1e3, "dtype": "f64",
+                     "config": {"workload": "fuzz::partial_ratio cutoff 80, 256 x %d uint32 token strings "
+                                            "(1-4 tokens of 3-12 units), dense float64 out (on device)" % nc,
+                                "gcups": cells * steps / t / 1e9, "per_kernel_ms": {"partial_ratio": per[0]}},
+                     "cpu_baseline": {"value": sub * nc / tc, "unit": "pairs/s", "cores": os.cpu_count(),
+                                      "kind": "port", "sample": "4 of the 256 queries x all %d choices" % nc},
+                     "e2e": None, "gpu_launches": steps, "clocks": clk})
     else:
         nq = 1024
         nc = args.nc if args.nc != 4096 else 1000000

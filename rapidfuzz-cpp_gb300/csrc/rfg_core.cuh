@@ -1660,6 +1660,81 @@ struct PMShift {
     }
 };
 
+/* bits [a, a + 64) of row c of a W-word table (zero outside it) */
+template <typename PMW>
+RFG_HD u64 pm_bits(const PMW& pm, int W, u64 c, int a)
+{
+    if (a <= -64 || a >= 64 * W) return 0;
+    if (a < 0) return pm(c, 0) << (-a);
+    const int w0 = a >> 6, sh = a & 63;
+    u64 x = pm(c, w0) >> sh;
+    if (sh && w0 + 1 < W) x |= pm(c, w0 + 1) << (64 - sh);
+    return x;
+}
+
+RFG_HD u64 bitrev64(u64 x)
+{
+#ifdef __CUDA_ARCH__
+    return __brevll(x);
+#else
+    x = ((x >> 1) & 0x5555555555555555ull) | ((x & 0x5555555555555555ull) << 1);
+    x = ((x >> 2) & 0x3333333333333333ull) | ((x & 0x3333333333333333ull) << 2);
+    x = ((x >> 4) & 0x0F0F0F0F0F0F0F0Full) | ((x & 0x0F0F0F0F0F0F0F0Full) << 4);
+    x = ((x >> 8) & 0x00FF00FF00FF00FFull) | ((x & 0x00FF00FF00FF00FFull) << 8);
+    x = ((x >> 16) & 0x0000FFFF0000FFFFull) | ((x & 0x0000FFFF0000FFFFull) << 16);
+    return (x >> 32) | (x << 32);
+#endif
+}
+
+/* pattern table of the reversed pattern q[m-1], ..., q[0] from q's table */
+template <typename PMW>
+struct PMRev {
+    const PMW* pm;
+    int W, m;
+    RFG_HD u64 operator()(u64 c, int w) const
+    {
+        /* reversed bits 64w .. 64w+63 are q's bits m-1-64w down to m-64-64w */
+        const u64 r = bitrev64(pm_bits(*pm, W, c, m - 64 - 64 * w));
+        const int rem = m - 64 * w;
+        return rem >= 64 ? r : r & low_mask(rem < 0 ? 0 : rem);
+    }
+};
+
+/* text rows read backwards: t[len-1], t[len-2], ... */
+template <typename TXT>
+struct RevText {
+    const TXT* t;
+    int len;
+    RFG_HD u64 operator[](int j) const { return (*t)[len - 1 - j]; }
+};
+
+/* Hyyro's LCS bit vector over the first T units of t (S: W words); after(j) runs after
+ * unit j.  LCS(pattern[0, i), text so far) = lcs_count(S, W, i). */
+template <typename PMW, typename TXT, typename F>
+RFG_HD void lcs_stream(const PMW& pm, int W, const TXT& t, int T, u64* S, F after)
+{
+    for (int w = 0; w < W; ++w) S[w] = ~0ull;
+    for (int j = 0; j < T; ++j) {
+        const u64 c = t[j];
+        u32 carry = 0;
+        for (int w = 0; w < W; ++w) {
+            const u64 X = pm(c, w);
+            const u64 sv = S[w];
+            const u64 u = sv & X;
+            const u64 x = add_carry(sv, u, carry, &carry);
+            S[w] = x | (sv - u);
+        }
+        after(j);
+    }
+}
+
+RFG_HD u64 lcs_count(const u64* S, int W, int i)
+{
+    u64 l = 0;
+    for (int w = 0; w < W && 64 * w < i; ++w) l += popc64(~S[w] & low_mask(i - 64 * w));
+    return l;
+}
+
 /* text rows t[a, a + L) */
 template <typename TXT>
 struct TextSlice {
@@ -1760,17 +1835,36 @@ RFG_HD double partial_impl_dev(const PMW& pm, int W, int m, const TXT& c, int n,
         score = dmul(score, 100.0);
         if (score >= cutoff) cutoff = res = score;
     }
+    /* prefixes and suffixes of the haystack shorter than the needle: every LCS of one
+     * family comes from a single bit-vector pass (text prefixes are the pass's steps,
+     * pattern prefixes the final vector's low bits; suffixes are prefixes of the reversed
+     * strings), kept in lbuf[length] -- the window search no longer needs work */
+    u32* lbuf = work;
+    const PMRev<PMW> pr{&pm, W, m};
+    const RevText<TXT> rc{&c, n};
+    if (QN) {
+        if (len1 > 1) lcs_stream(pm, W, c, len1 - 1, st, [&](int j) { lbuf[j + 1] = (u32)lcs_count(st, W, m); });
+    }
+    else {
+        lcs_stream(pm, W, c, n, st, [](int) {});
+        for (int i = 1; i < len1; ++i) lbuf[i] = (u32)lcs_count(st, W, i);
+    }
     for (int i = 1; i < len1; ++i) {
         if (!needle_has(i - 1)) continue;
-        const double r = ratio_from_lcs((u64)len1, (u64)i, lcs_at(0, i), cutoff);
+        const double r = ratio_from_lcs((u64)len1, (u64)i, lbuf[i], cutoff);
         if (r > res) {
             cutoff = res = r;
             if (res == 100.0) return res;
         }
     }
+    if (QN) lcs_stream(pr, W, rc, len1, st, [&](int k) { lbuf[k + 1] = (u32)lcs_count(st, W, m); });
+    else {
+        lcs_stream(pr, W, rc, n, st, [](int) {});
+        for (int L = 1; L <= len1; ++L) lbuf[L] = (u32)lcs_count(st, W, L);
+    }
     for (int i = len2 - len1; i < len2; ++i) {
         if (!needle_has(i)) continue;
-        const double r = ratio_from_lcs((u64)len1, (u64)(len2 - i), lcs_at(i, len2 - i), cutoff);
+        const double r = ratio_from_lcs((u64)len1, (u64)(len2 - i), lbuf[len2 - i], cutoff);
         if (r > res) {
             cutoff = res = r;
             if (res == 100.0) return res;
