@@ -507,7 +507,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         if (spec.topk == 0 && g_stage_mode != 0) {
             /* windows of up to 32 KB of results, each its own length-sorted run (a
              * quarter of that per query row in the several-queries kernel) */
-            const int64_t cap = (spec.out_dtype == RFG_I32 ? 8192 : 4096) / (mq_ok ? RFG_MQ : 1);
+            const int64_t cap = (spec.out_dtype == RFG_I32 ? 8192 : 4096) / (mq_ok ? mq_queries(fam) : 1);
             if (chunk > cap) chunk = (chunk + cap - 1) / cap * cap;
             stage = std::min(chunk, cap);
         }
@@ -580,7 +580,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             fn = tiles_mq_kernel_jaro(c.width);
             block = g_block_override > 0 ? g_block_override : 256;
             a.stage = stage;
-            smem = tiles_mq_jaro_smem_bytes(stage);
+            smem = tiles_mq_jaro_smem_bytes(stage, mq_queries(fam));
             RFG_TRY(allow_dynamic_smem(fn, smem));
             per_sm = occupancy(fn, block, smem);
         }
@@ -593,7 +593,8 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             block = g_block_override > 0 ? g_block_override : 256;
             a.stage = stage;
             smem = tiles_mq_smem_bytes(stage, spec.out_dtype,
-                                       fast_ok ? 0 : (int)std::min<int64_t>(RFG_JT_MAXT, max_choice_len) + 1);
+                                       fast_ok ? 0 : (int)std::min<int64_t>(RFG_JT_MAXT, max_choice_len) + 1,
+                                       mq_queries(fam));
             RFG_TRY(allow_dynamic_smem(fn, smem));
             per_sm = occupancy(fn, block, smem);
         }
@@ -673,7 +674,8 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             a.fast_k = clamp_bound(spec.ci);
         }
         a.nchunks = (nc + cchunk - 1) / cchunk;
-        const int64_t ntiles = (use_mq ? ((int64_t)a.nq + RFG_MQ - 1) / RFG_MQ : (int64_t)a.nq) * a.nchunks;
+        const int64_t mqq = mq_queries(fam);
+        const int64_t ntiles = (use_mq ? ((int64_t)a.nq + mqq - 1) / mqq : (int64_t)a.nq) * a.nchunks;
         if (ntiles > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "batch too large for one launch");
         const int64_t grid = std::min<int64_t>(ntiles, slots);
         if (k == 4) {

@@ -874,12 +874,12 @@ __global__ void __launch_bounds__(256) k_generic(const KParams a)
 /* ------------------------------------------- several queries per thread
  * Unit-weight distances of one-word patterns whose code units are all below 256
  * (distance, or the normalized chains with the integer cutoff from per-query tables):
- * a tile is (RFG_MQ consecutive queries of the class, chunk); every thread fetches a
+ * a tile is (Q consecutive queries of the class, chunk); every thread fetches a
  * choice's text once per block of characters and advances the recurrences of all the
  * tile's queries on it (group_word_dist), so text loads, per-choice bookkeeping and
- * the loop overhead are shared by RFG_MQ pairs and the independent recurrences overlap.
+ * the loop overhead are shared by Q pairs and the independent recurrences overlap.
+ * Q per family (mq_queries): two for Levenshtein, OSA and Jaro, four for Indel / ratio.
  * Results leave through the staged windows (a.stage positions per query row). */
-#define RFG_MQ 4
 #ifndef RFG_MINB_MQ
 #define RFG_MINB_MQ 4
 #endif
@@ -902,19 +902,19 @@ struct MQText {
     }
 };
 
-template <int FAM, typename CT, bool NORM>
+template <int FAM, typename CT, bool NORM, int Q>
 __global__ void __launch_bounds__(256, FAM == FAM_OSA ? RFG_MINB_MQ_OSA : RFG_MINB_MQ) k_tiles_mq(const KParams a)
 {
     extern __shared__ u64 smem[];
     u64* rows = smem;
     /* normalized ops (NORM): chain_kd per (query, text length 0..tab_t) */
     const int tn = NORM ? a.tab_t + 1 : 0;
-    u64* kdt = smem + RFG_MQ * 257;
-    unsigned char* stage = (unsigned char*)(kdt + RFG_MQ * tn);
+    u64* kdt = smem + Q * 257;
+    unsigned char* stage = (unsigned char*)(kdt + Q * tn);
     __shared__ int64_t s_tile;
-    __shared__ int64_t s_q[RFG_MQ];
-    __shared__ int s_m[RFG_MQ];
-    const int64_t ngroups = ((int64_t)a.nq + RFG_MQ - 1) / RFG_MQ;
+    __shared__ int64_t s_q[Q];
+    __shared__ int s_m[Q];
+    const int64_t ngroups = ((int64_t)a.nq + Q - 1) / Q;
     const int64_t ntiles = ngroups * a.nchunks;
     const i64 K = a.fast_k;
     int64_t cur_g = -1;
@@ -925,9 +925,9 @@ __global__ void __launch_bounds__(256, FAM == FAM_OSA ? RFG_MINB_MQ_OSA : RFG_MI
         if (t >= ntiles) break;
         const int64_t gi = t / a.nchunks, ch = t % a.nchunks;
         if (gi != cur_g) {
-            for (int i = threadIdx.x; i < RFG_MQ * 257; i += blockDim.x) rows[i] = 0;
-            if (threadIdx.x < RFG_MQ) {
-                const int64_t k = gi * RFG_MQ + threadIdx.x;
+            for (int i = threadIdx.x; i < Q * 257; i += blockDim.x) rows[i] = 0;
+            if (threadIdx.x < Q) {
+                const int64_t k = gi * Q + threadIdx.x;
                 int64_t qi = -1;
                 int m = 0;
                 if (k < a.nq) {
@@ -950,13 +950,13 @@ __global__ void __launch_bounds__(256, FAM == FAM_OSA ? RFG_MINB_MQ_OSA : RFG_MI
                 sp.ci = a.ci;
                 sp.cf = a.cf;
                 sp.p = a.sp;
-                for (int i = threadIdx.x; i < RFG_MQ * tn; i += blockDim.x) {
+                for (int i = threadIdx.x; i < Q * tn; i += blockDim.x) {
                     sp.l1 = (u64)s_m[i / tn];
                     sp.l2 = (u64)(i % tn);
                     kdt[i] = chain_kd(sp);
                 }
             }
-            for (int q = 0; q < RFG_MQ; ++q) {
+            for (int q = 0; q < Q; ++q) {
                 if (s_q[q] < 0) continue;
                 const unsigned char* qb = a.q.data + a.q.off[s_q[q]] * a.q.width;
                 for (int i = threadIdx.x; i < s_m[q]; i += blockDim.x) {
@@ -968,10 +968,10 @@ __global__ void __launch_bounds__(256, FAM == FAM_OSA ? RFG_MINB_MQ_OSA : RFG_MI
             __syncthreads();
             cur_g = gi;
         }
-        int m[RFG_MQ];
+        int m[Q];
         int qn = 0;
 #pragma unroll
-        for (int q = 0; q < RFG_MQ; ++q) {
+        for (int q = 0; q < Q; ++q) {
             m[q] = s_m[q];
             if (s_q[q] >= 0) qn = q + 1;
         }
@@ -997,9 +997,9 @@ __global__ void __launch_bounds__(256, FAM == FAM_OSA ? RFG_MINB_MQ_OSA : RFG_MI
                     o_n = __ldg(a.poff + pn);
                     n_n = __ldg(a.plen + pn);
                 }
-                i64 d[RFG_MQ], Kq[RFG_MQ];
+                i64 d[Q], Kq[Q];
 #pragma unroll
-                for (int q = 0; q < RFG_MQ; ++q) {
+                for (int q = 0; q < Q; ++q) {
                     if (!NORM) Kq[q] = K;
                     else {
                         u64 kd;
@@ -1019,10 +1019,10 @@ __global__ void __launch_bounds__(256, FAM == FAM_OSA ? RFG_MINB_MQ_OSA : RFG_MI
                         Kq[q] = clamp_bound(kd);
                     }
                 }
-                group_word_dist<FAM, RFG_MQ>(pm, m, qn, MQText<CT>{(const CT*)a.c.data + o0}, n, Kq, d);
+                group_word_dist<FAM, Q>(pm, m, qn, MQText<CT>{(const CT*)a.c.data + o0}, n, Kq, d);
                 const int64_t i = ci - s0;
 #pragma unroll
-                for (int q = 0; q < RFG_MQ; ++q) {
+                for (int q = 0; q < Q; ++q) {
                     if (q >= qn) break;
                     const int64_t at = (int64_t)q * a.stage + i;
                     if (!NORM) {
@@ -1079,18 +1079,18 @@ struct MQRow1 {
     __device__ __forceinline__ u64 operator()(u64 c, int) const { return rows[c]; }
 };
 
-template <typename CT>
+template <typename CT, int Q>
 __global__ void __launch_bounds__(256, RFG_MINB_MQJ) k_tiles_mq_jaro(const KParams a)
 {
     extern __shared__ u64 smem[];
     u64* rows = smem;
-    JaroTab* jt = (JaroTab*)(smem + RFG_MQ * 257);
-    unsigned char* stage = (unsigned char*)(jt + RFG_MQ);
+    JaroTab* jt = (JaroTab*)(smem + Q * 257);
+    unsigned char* stage = (unsigned char*)(jt + Q);
     __shared__ int64_t s_tile;
-    __shared__ int64_t s_q[RFG_MQ];
-    __shared__ int s_m[RFG_MQ];
-    __shared__ u64 s_pre[RFG_MQ][4];
-    const int64_t ngroups = ((int64_t)a.nq + RFG_MQ - 1) / RFG_MQ;
+    __shared__ int64_t s_q[Q];
+    __shared__ int s_m[Q];
+    __shared__ u64 s_pre[Q][4];
+    const int64_t ngroups = ((int64_t)a.nq + Q - 1) / Q;
     const int64_t ntiles = ngroups * a.nchunks;
     const int tw = (int)(sizeof(JaroTab) / 8);
     int64_t cur_g = -1;
@@ -1101,9 +1101,9 @@ __global__ void __launch_bounds__(256, RFG_MINB_MQJ) k_tiles_mq_jaro(const KPara
         if (t >= ntiles) break;
         const int64_t gi = t / a.nchunks, ch = t % a.nchunks;
         if (gi != cur_g) {
-            for (int i = threadIdx.x; i < RFG_MQ * 257; i += blockDim.x) rows[i] = 0;
-            if (threadIdx.x < RFG_MQ) {
-                const int64_t k = gi * RFG_MQ + threadIdx.x;
+            for (int i = threadIdx.x; i < Q * 257; i += blockDim.x) rows[i] = 0;
+            if (threadIdx.x < Q) {
+                const int64_t k = gi * Q + threadIdx.x;
                 int64_t qi = -1;
                 int m = 0;
                 if (k < a.nq) {
@@ -1118,11 +1118,11 @@ __global__ void __launch_bounds__(256, RFG_MINB_MQJ) k_tiles_mq_jaro(const KPara
                 s_m[threadIdx.x] = m;
             }
             __syncthreads();
-            for (int i = threadIdx.x; i < RFG_MQ * tw; i += blockDim.x) {
+            for (int i = threadIdx.x; i < Q * tw; i += blockDim.x) {
                 const int q = i / tw;
                 if (s_q[q] >= 0) ((u64*)(jt + q))[i % tw] = __ldg((const u64*)(a.jtab + s_q[q]) + i % tw);
             }
-            for (int q = 0; q < RFG_MQ; ++q) {
+            for (int q = 0; q < Q; ++q) {
                 if (s_q[q] < 0) continue;
                 const unsigned char* qb = a.q.data + a.q.off[s_q[q]] * a.q.width;
                 for (int i = threadIdx.x; i < s_m[q]; i += blockDim.x) {
@@ -1135,10 +1135,10 @@ __global__ void __launch_bounds__(256, RFG_MINB_MQJ) k_tiles_mq_jaro(const KPara
             __syncthreads();
             cur_g = gi;
         }
-        int m[RFG_MQ];
+        int m[Q];
         int qn = 0;
 #pragma unroll
-        for (int q = 0; q < RFG_MQ; ++q) {
+        for (int q = 0; q < Q; ++q) {
             m[q] = s_m[q];
             if (s_q[q] >= 0) qn = q + 1;
         }
@@ -1171,11 +1171,11 @@ __global__ void __launch_bounds__(256, RFG_MINB_MQJ) k_tiles_mq_jaro(const KPara
                 sp.cf = a.cf;
                 sp.p = a.sp;
                 sp.l2 = (u64)n;
-                int prefix[RFG_MQ], need[RFG_MQ], C[RFG_MQ], Tr[RFG_MQ];
-                double vf[RFG_MQ];
+                int prefix[Q], need[Q], C[Q], Tr[Q];
+                double vf[Q];
                 unsigned active = 0, decided = 0;
 #pragma unroll
-                for (int q = 0; q < RFG_MQ; ++q) {
+                for (int q = 0; q < Q; ++q) {
                     prefix[q] = 0;
                     need[q] = 0;
                     vf[q] = 0.0;
@@ -1226,9 +1226,9 @@ __global__ void __launch_bounds__(256, RFG_MINB_MQJ) k_tiles_mq_jaro(const KPara
                     }
                 }
                 if (active) {
-                    group_jaro_word<RFG_MQ>(pm, m, active, txt, n, need, C, Tr);
+                    group_jaro_word<Q>(pm, m, active, txt, n, need, C, Tr);
 #pragma unroll
-                    for (int q = 0; q < RFG_MQ; ++q) {
+                    for (int q = 0; q < Q; ++q) {
                         if (!((active >> q) & 1u)) continue;
                         sp.l1 = (u64)m[q];
                         vf[q] = C[q] < need[q] ? jt[q].vfail[prefix[q]] : finish_jaro_tab(sp, jt[q], prefix[q], C[q], Tr[q]);
@@ -1237,7 +1237,7 @@ __global__ void __launch_bounds__(256, RFG_MINB_MQJ) k_tiles_mq_jaro(const KPara
                 (void)decided;
                 const int64_t i = pos.ci - s0;
 #pragma unroll
-                for (int q = 0; q < RFG_MQ; ++q)
+                for (int q = 0; q < Q; ++q)
                     if (q < qn) ((double*)stage)[(int64_t)q * a.stage + i] = vf[q];
             }
             __syncthreads();
@@ -1251,14 +1251,14 @@ __global__ void __launch_bounds__(256, RFG_MINB_MQJ) k_tiles_mq_jaro(const KPara
     }
 }
 
-inline size_t tiles_mq_jaro_smem_bytes(int64_t stage)
+inline size_t tiles_mq_jaro_smem_bytes(int64_t stage, int Q)
 {
-    return (size_t)RFG_MQ * 257 * 8 + (size_t)RFG_MQ * sizeof(JaroTab) + (size_t)RFG_MQ * stage * 8;
+    return (size_t)Q * 257 * 8 + (size_t)Q * sizeof(JaroTab) + (size_t)Q * stage * 8;
 }
 
-inline size_t tiles_mq_smem_bytes(int64_t stage, int out_dtype, int kd_len)
+inline size_t tiles_mq_smem_bytes(int64_t stage, int out_dtype, int kd_len, int Q)
 {
-    return ((size_t)RFG_MQ * 257 + (size_t)RFG_MQ * kd_len) * 8 + (size_t)RFG_MQ * stage * (out_dtype == 0 ? 4 : 8);
+    return ((size_t)Q * 257 + (size_t)Q * kd_len) * 8 + (size_t)Q * stage * (out_dtype == 0 ? 4 : 8);
 }
 
 /* Per query: the best topk of all its tiles' candidates, best first; scores as doubles

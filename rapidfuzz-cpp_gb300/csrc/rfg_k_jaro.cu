@@ -30,10 +30,10 @@ const void* tiles_kernel_jaro(int width, int W, bool topk)
 const void* tiles_mq_kernel_jaro(int width)
 {
     switch (width) {
-    case 1: return (const void*)&k_tiles_mq_jaro<uint8_t>;
-    case 2: return (const void*)&k_tiles_mq_jaro<uint16_t>;
-    case 4: return (const void*)&k_tiles_mq_jaro<uint32_t>;
-    case 8: return (const void*)&k_tiles_mq_jaro<unsigned long long>;
+    case 1: return (const void*)&k_tiles_mq_jaro<uint8_t, 2>;
+    case 2: return (const void*)&k_tiles_mq_jaro<uint16_t, 2>;
+    case 4: return (const void*)&k_tiles_mq_jaro<uint32_t, 2>;
+    case 8: return (const void*)&k_tiles_mq_jaro<unsigned long long, 2>;
     }
     return nullptr;
 }

@@ -30,12 +30,18 @@ const void* tiles_kernel_lcs(int width, int W, bool topk)
 const void* tiles_mq_kernel_lcs(int width, bool norm)
 {
     switch (width) {
-    case 1: return norm ? (const void*)&k_tiles_mq<FAM_LCS, uint8_t, true> : (const void*)&k_tiles_mq<FAM_LCS, uint8_t, false>;
-    case 2: return norm ? (const void*)&k_tiles_mq<FAM_LCS, uint16_t, true> : (const void*)&k_tiles_mq<FAM_LCS, uint16_t, false>;
-    case 4: return norm ? (const void*)&k_tiles_mq<FAM_LCS, uint32_t, true> : (const void*)&k_tiles_mq<FAM_LCS, uint32_t, false>;
+    case 1:
+        return norm ? (const void*)&k_tiles_mq<FAM_LCS, uint8_t, true, 4>
+                    : (const void*)&k_tiles_mq<FAM_LCS, uint8_t, false, 4>;
+    case 2:
+        return norm ? (const void*)&k_tiles_mq<FAM_LCS, uint16_t, true, 4>
+                    : (const void*)&k_tiles_mq<FAM_LCS, uint16_t, false, 4>;
+    case 4:
+        return norm ? (const void*)&k_tiles_mq<FAM_LCS, uint32_t, true, 4>
+                    : (const void*)&k_tiles_mq<FAM_LCS, uint32_t, false, 4>;
     case 8:
-        return norm ? (const void*)&k_tiles_mq<FAM_LCS, unsigned long long, true>
-                    : (const void*)&k_tiles_mq<FAM_LCS, unsigned long long, false>;
+        return norm ? (const void*)&k_tiles_mq<FAM_LCS, unsigned long long, true, 4>
+                    : (const void*)&k_tiles_mq<FAM_LCS, unsigned long long, false, 4>;
     }
     return nullptr;
 }

@@ -30,12 +30,18 @@ const void* tiles_kernel_osa(int width, int W, bool topk)
 const void* tiles_mq_kernel_osa(int width, bool norm)
 {
     switch (width) {
-    case 1: return norm ? (const void*)&k_tiles_mq<FAM_OSA, uint8_t, true> : (const void*)&k_tiles_mq<FAM_OSA, uint8_t, false>;
-    case 2: return norm ? (const void*)&k_tiles_mq<FAM_OSA, uint16_t, true> : (const void*)&k_tiles_mq<FAM_OSA, uint16_t, false>;
-    case 4: return norm ? (const void*)&k_tiles_mq<FAM_OSA, uint32_t, true> : (const void*)&k_tiles_mq<FAM_OSA, uint32_t, false>;
+    case 1:
+        return norm ? (const void*)&k_tiles_mq<FAM_OSA, uint8_t, true, 2>
+                    : (const void*)&k_tiles_mq<FAM_OSA, uint8_t, false, 2>;
+    case 2:
+        return norm ? (const void*)&k_tiles_mq<FAM_OSA, uint16_t, true, 2>
+                    : (const void*)&k_tiles_mq<FAM_OSA, uint16_t, false, 2>;
+    case 4:
+        return norm ? (const void*)&k_tiles_mq<FAM_OSA, uint32_t, true, 2>
+                    : (const void*)&k_tiles_mq<FAM_OSA, uint32_t, false, 2>;
     case 8:
-        return norm ? (const void*)&k_tiles_mq<FAM_OSA, unsigned long long, true>
-                    : (const void*)&k_tiles_mq<FAM_OSA, unsigned long long, false>;
+        return norm ? (const void*)&k_tiles_mq<FAM_OSA, unsigned long long, true, 2>
+                    : (const void*)&k_tiles_mq<FAM_OSA, unsigned long long, false, 2>;
     }
     return nullptr;
 }
