@@ -1743,6 +1743,17 @@ struct TextSlice {
     RFG_HD u64 operator[](int j) const { return (*t)[a + j]; }
 };
 
+/* a * b >= c * d over 128-bit products */
+RFG_HD bool prod_ge(u64 a, u64 b, u64 c, u64 d)
+{
+#ifdef __CUDA_ARCH__
+    const u64 h1 = __umul64hi(a, b), h2 = __umul64hi(c, d);
+    return h1 != h2 ? h1 > h2 : a * b >= c * d;
+#else
+    return (unsigned __int128)a * b >= (unsigned __int128)c * d;
+#endif
+}
+
 /* CachedRatio::similarity from an exact LCS (fuzz_impl.hpp:43-47 over the Indel chain) */
 RFG_HD double ratio_from_lcs(u64 l1, u64 l2, u64 lcs, double cutoff)
 {
@@ -1759,6 +1770,7 @@ RFG_HD double partial_impl_dev(const PMW& pm, int W, int m, const TXT& c, int n,
 {
     const int len1 = QN ? m : n, len2 = QN ? n : m;
     double res = 0.0;
+    u64 bd = 1, bM = 1; /* res = 0 as the fraction 1 / 1 */
     /* LCS of the needle against haystack[a, a + L) */
     auto lcs_at = [&](int a, int L) -> u64 {
         if (QN) {
@@ -1833,8 +1845,39 @@ RFG_HD double partial_impl_dev(const PMW& pm, int W, int m, const TXT& c, int n,
         }
         double score = dsub(1.0, ddiv((double)best, (double)maximum));
         score = dmul(score, 100.0);
-        if (score >= cutoff) cutoff = res = score;
+        if (score >= cutoff) {
+            cutoff = res = score;
+            bd = best;
+            bM = maximum;
+        }
     }
+    /* res is f(bd, bM) with f(d, M) = (1 - d / M) * 100 in correctly rounded steps, which
+     * never increases with d / M: a candidate with d * bM >= bd * M cannot beat res, so
+     * only the others pay the double-precision chain (a negative res, possible only
+     * under a negative cutoff, turns the test off) */
+    const bool pf = res >= 0.0;
+    /* the cutoff side: the chain prunes d > ceil(M * c_nd) to 0; with cfix >= c_nd * 2^32,
+     * floor(M * cfix / 2^32) + 2 bounds that integer cutoff from above */
+    u64 cfix = 0;
+    auto set_cfix = [&]() {
+        const double cnd = norm_sim_to_norm_dist(ddiv(cutoff, 100.0));
+        cfix = cnd >= 2.0 ? ~0ull : (u64)dceil(dmul(cnd, 4294967296.0)) + 1;
+    };
+    set_cfix();
+    auto may_beat = [&](u64 L2, u64 lcs) {
+        if (!pf) return true;
+        const u64 M = (u64)len1 + L2, d = M - 2 * lcs;
+        if (cfix != ~0ull) {
+#ifdef __CUDA_ARCH__
+            const u64 hi = __umul64hi(M, cfix), lo = M * cfix;
+            const u64 kup = ((hi << 32) | (lo >> 32)) + 2;
+#else
+            const u64 kup = (u64)(((unsigned __int128)M * cfix) >> 32) + 2;
+#endif
+            if (d > kup) return false;
+        }
+        return !prod_ge(d, bM, bd, M);
+    };
     /* prefixes and suffixes of the haystack shorter than the needle: every LCS of one
      * family comes from a single bit-vector pass (text prefixes are the pass's steps,
      * pattern prefixes the final vector's low bits; suffixes are prefixes of the reversed
@@ -1850,11 +1893,14 @@ RFG_HD double partial_impl_dev(const PMW& pm, int W, int m, const TXT& c, int n,
         for (int i = 1; i < len1; ++i) lbuf[i] = (u32)lcs_count(st, W, i);
     }
     for (int i = 1; i < len1; ++i) {
-        if (!needle_has(i - 1)) continue;
+        if (!needle_has(i - 1) || !may_beat((u64)i, lbuf[i])) continue;
         const double r = ratio_from_lcs((u64)len1, (u64)i, lbuf[i], cutoff);
         if (r > res) {
             cutoff = res = r;
+            bM = (u64)len1 + i;
+            bd = bM - 2 * (u64)lbuf[i];
             if (res == 100.0) return res;
+            set_cfix();
         }
     }
     if (QN) lcs_stream(pr, W, rc, len1, st, [&](int k) { lbuf[k + 1] = (u32)lcs_count(st, W, m); });
@@ -1863,11 +1909,14 @@ RFG_HD double partial_impl_dev(const PMW& pm, int W, int m, const TXT& c, int n,
         for (int L = 1; L <= len1; ++L) lbuf[L] = (u32)lcs_count(st, W, L);
     }
     for (int i = len2 - len1; i < len2; ++i) {
-        if (!needle_has(i)) continue;
+        if (!needle_has(i) || !may_beat((u64)(len2 - i), lbuf[len2 - i])) continue;
         const double r = ratio_from_lcs((u64)len1, (u64)(len2 - i), lbuf[len2 - i], cutoff);
         if (r > res) {
             cutoff = res = r;
+            bM = (u64)len1 + (len2 - i);
+            bd = bM - 2 * (u64)lbuf[len2 - i];
             if (res == 100.0) return res;
+            set_cfix();
         }
     }
     return res;

@@ -93,6 +93,10 @@ int main()
     CHECK(std::fabs(rapidfuzz::fuzz::ratio(std::string("new york mets"), std::string("new york mets")) - 100) < 1e-6);
     rapidfuzz::fuzz::CachedRatio<char> cr(std::string("new york mets"));
     CHECK(std::fabs(cr.similarity(std::string("the wonderful new york mets")) - 65) < 1);
+    // fuzz::partial_ratio (tests-fuzz.cpp:154-158)
+    CHECK(std::fabs(rapidfuzz::fuzz::partial_ratio(std::string("001"), std::string("220222")) - 33.3333333) < 1e-6);
+    rapidfuzz::fuzz::CachedPartialRatio<char> cpr(std::string("physics 2 vid"));
+    CHECK(cpr.similarity(std::string("study physics physics 2 video")) == 100.0);
     // Multi* (Levenshtein.hpp:297-419) and its errors
     rapidfuzz::experimental::MultiLevenshtein<16> ml(3);
     ml.insert(std::string("kitten"));
@@ -149,6 +153,8 @@ int main()
         CHECK(same(rapidfuzz::jaro_similarity(s1, s2, cf), of(RFO_JARO, RFO_SIMILARITY, 0, s1, s2, cf)));
         CHECK(same(rapidfuzz::jaro_winkler_distance(s1, s2, 0.1, cf), of(RFO_JARO_WINKLER, RFO_DISTANCE, 0, s1, s2, cf)));
         CHECK(same(rapidfuzz::fuzz::ratio(s1, s2, cf * 100), of(RFO_RATIO, RFO_SIMILARITY, 0, s1, s2, cf * 100)));
+        CHECK(same(rapidfuzz::fuzz::partial_ratio(s1, s2, cf * 100),
+                   of(RFO_PARTIAL_RATIO, RFO_SIMILARITY, 0, s1, s2, cf * 100)));
         rapidfuzz::CachedOSA<char> co(s1);
         CHECK(same(co.normalized_similarity(s2, cf), of(RFO_OSA, RFO_NORM_SIMILARITY, 1, s1, s2, cf)));
     }
