@@ -540,8 +540,9 @@ __device__ __forceinline__ void score_pair(const KParams& a, const u64* rows, co
         emit(a, qi, ci, 0, vf, false, s.ci, s.cf, tl, stage, s0);
         return;
     }
-    if (!TOPK && a.fast) {
-        const i64 K = a.fast_k;
+    if (a.fast) {
+        /* extract: the cutoff tightened by the query's running threshold (s.ci) */
+        const i64 K = TOPK ? clamp_bound(s.ci) : a.fast_k;
         const i64 raw = run_int_core<FAM, W>(pm, m, txt, n, K);
         i64 d = raw;
         if (FAM == FAM_LCS) d = raw >= 0 ? (i64)m + n - 2 * raw : K + 1;
