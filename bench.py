@@ -39,7 +39,7 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 METRIC_NAME = "GCUPS & pairs/s, batched vs per-call, 1 GB300, bit-exact; extract p50/p99 ms"
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the several-queries kernels
-# (k_tiles_mq) on this workload, default launch shape (profiles/k_tiles_mq_cdist4096_full.md)
+# (k_tiles_mq) on this workload, default launch shape (one ncu --set full capture)
 DRAM_BYTES_PER_LAUNCH = {"levenshtein": 7950592, "indel": 8178688, "osa": 7104768}
 OPS_PER_WORD_STEP = {"levenshtein": 23, "indel": 8, "osa": 29}
 CUTOFF = 8
