@@ -53,8 +53,17 @@ typedef enum {
     RFG_JARO = 4,
     RFG_JARO_WINKLER = 5,
     RFG_RATIO = 6,        /* fuzz::ratio; only RFG_SIMILARITY */
-    RFG_PARTIAL_RATIO = 7 /* fuzz::partial_ratio / CachedPartialRatio (fuzz.hpp:128-183,
-                             fuzz_impl.hpp:49-293); only RFG_SIMILARITY, no Multi form */
+    RFG_PARTIAL_RATIO = 7, /* fuzz::partial_ratio / CachedPartialRatio (fuzz.hpp:128-183,
+                              fuzz_impl.hpp:49-293); only RFG_SIMILARITY, no Multi form */
+    /* token scorers over the ratio / partial_ratio engine: both strings are split on
+     * whitespace, the tokens sorted by code unit (compared unsigned) and joined with
+     * U+0020 on the host (fuzz.hpp:203-373, fuzz_impl.hpp:297-366); QRatio is ratio with
+     * 0 where either string is empty (fuzz.hpp:692-804, fuzz_impl.hpp:891-929).  Only
+     * RFG_SIMILARITY and RFG_F64, through rfg_score_f64, rfg_cached_*, rfg_cdist and (token
+     * sort and QRatio) rfg_multi_*; not on a corpus, a batch or the no-allocation entry. */
+    RFG_TOKEN_SORT_RATIO = 8,
+    RFG_PARTIAL_TOKEN_SORT_RATIO = 9,
+    RFG_QRATIO = 10
 } rfg_metric;
 
 /* the four result kinds of every metric (rapidfuzz/details/distance.hpp) */

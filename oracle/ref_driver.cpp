@@ -170,6 +170,18 @@ int score(int metric, int op, int form, const void* a, int64_t la, const void* b
             if (op != RFO_SIMILARITY) return -1;
             *of = fuzz::partial_ratio(s1, s2, cf);
             return 0;
+        case RFO_TOKEN_SORT_RATIO:
+            if (op != RFO_SIMILARITY) return -1;
+            *of = fuzz::token_sort_ratio(s1, s2, cf);
+            return 0;
+        case RFO_PARTIAL_TOKEN_SORT_RATIO:
+            if (op != RFO_SIMILARITY) return -1;
+            *of = fuzz::partial_token_sort_ratio(s1, s2, cf);
+            return 0;
+        case RFO_QRATIO:
+            if (op != RFO_SIMILARITY) return -1;
+            *of = fuzz::QRatio(s1, s2, cf);
+            return 0;
         }
         return -1;
     }
@@ -227,6 +239,24 @@ int score(int metric, int op, int form, const void* a, int64_t la, const void* b
     case RFO_PARTIAL_RATIO: {
         if (op != RFO_SIMILARITY) return -1;
         fuzz::CachedPartialRatio<C1> sc(s1);
+        *of = sc.similarity(s2, cf);
+        return 0;
+    }
+    case RFO_TOKEN_SORT_RATIO: {
+        if (op != RFO_SIMILARITY) return -1;
+        fuzz::CachedTokenSortRatio<C1> sc(s1);
+        *of = sc.similarity(s2, cf);
+        return 0;
+    }
+    case RFO_PARTIAL_TOKEN_SORT_RATIO: {
+        if (op != RFO_SIMILARITY) return -1;
+        fuzz::CachedPartialTokenSortRatio<C1> sc(s1);
+        *of = sc.similarity(s2, cf);
+        return 0;
+    }
+    case RFO_QRATIO: {
+        if (op != RFO_SIMILARITY) return -1;
+        fuzz::CachedQRatio<C1> sc(s1);
         *of = sc.similarity(s2, cf);
         return 0;
     }
@@ -307,6 +337,16 @@ extern "C" int rfref_multi(int metric, int op, int max_len, const rfo_strings* i
         }
         return 0;
     };
+    /* the fuzz Multi scorers: similarity only */
+    auto fuzz_go = [&](auto& sc) {
+        for (auto& x : strs) sc.insert(x);
+        *result_count = (int64_t)sc.result_count();
+        if (!of) return 0;
+        std::vector<double> r(sc.result_count());
+        sc.similarity(r.data(), r.size(), s2, cf);
+        for (size_t i = 0; i < strs.size(); ++i) of[i] = r[i];
+        return 0;
+    };
     try {
 #define RF_MULTI_CASE(ML)                                                                                      \
     case ML:                                                                                                   \
@@ -338,13 +378,15 @@ extern "C" int rfref_multi(int metric, int op, int max_len, const rfo_strings* i
         }                                                                                                      \
         case RFO_RATIO: {                                                                                      \
             rapidfuzz::fuzz::experimental::MultiRatio<ML> s(strs.size());                                      \
-            for (auto& x : strs) s.insert(x);                                                                  \
-            *result_count = (int64_t)s.result_count();                                                         \
-            if (!of) return 0;                                                                                 \
-            std::vector<double> r(s.result_count());                                                           \
-            s.similarity(r.data(), r.size(), s2, cf);                                                          \
-            for (size_t i = 0; i < strs.size(); ++i) of[i] = r[i];                                             \
-            return 0;                                                                                          \
+            return fuzz_go(s);                                                                                 \
+        }                                                                                                      \
+        case RFO_TOKEN_SORT_RATIO: {                                                                           \
+            rapidfuzz::fuzz::experimental::MultiTokenSortRatio<ML> s(strs.size());                             \
+            return fuzz_go(s);                                                                                 \
+        }                                                                                                      \
+        case RFO_QRATIO: {                                                                                     \
+            rapidfuzz::fuzz::experimental::MultiQRatio<ML> s(strs.size());                                     \
+            return fuzz_go(s);                                                                                 \
         }                                                                                                      \
         }                                                                                                      \
         return -1;

@@ -897,6 +897,12 @@ int score_with_pm(int metric, int op, int form, const PM& pm, const S1& s1, cons
             *of = r * 100.0;
             return 0;
         }
+        case RFO_TOKEN_SORT_RATIO:
+        case RFO_QRATIO: {
+            if (op != RFO_SIMILARITY) return -1;
+            *of = token_multi(metric, s1, s2, cf);
+            return 0;
+        }
         case RFO_JARO:
         case RFO_JARO_WINKLER: {
             i64 C, T;
@@ -938,6 +944,13 @@ int score_with_pm(int metric, int op, int form, const PM& pm, const S1& s1, cons
     case RFO_PARTIAL_RATIO: {
         if (op != RFO_SIMILARITY) return -1;
         *of = partial_ratio_score(s1, s2, cf);
+        return 0;
+    }
+    case RFO_TOKEN_SORT_RATIO:
+    case RFO_PARTIAL_TOKEN_SORT_RATIO:
+    case RFO_QRATIO: {
+        if (op != RFO_SIMILARITY) return -1;
+        *of = token_scorer(metric, s1, s2, cf);
         return 0;
     }
     case RFO_RATIO: {
@@ -1085,6 +1098,97 @@ double partial_ratio_score(const S1& s1, const S2& s2, double cutoff)
     return score;
 }
 
+/* ------------------------------------------------ token_sort_ratio, QRatio
+ * token_sort_ratio / partial_token_sort_ratio (fuzz_impl.hpp:294-360): ratio /
+ * partial_ratio of both strings after sorted_split(...).join() (common_impl.hpp:162-180,
+ * SplittedSentenceView.hpp:71-85): split on whitespace, drop empty tokens, sort the
+ * tokens lexicographically by code unit, join with U+0020.  Whitespace follows the
+ * code-unit size (common_impl.hpp:85-152): one-byte units know the ASCII set only.
+ * QRatio (fuzz_impl.hpp:887-931): 0 when either string is empty, else ratio. */
+bool unit_is_space(u64 c, bool one_byte)
+{
+    switch (c) {
+    case 0x09: case 0x0A: case 0x0B: case 0x0C: case 0x0D: case 0x1C: case 0x1D: case 0x1E: case 0x1F:
+    case 0x20: return true;
+    }
+    if (one_byte) return false;
+    switch (c) {
+    case 0x85: case 0xA0: case 0x1680: case 0x2000: case 0x2001: case 0x2002: case 0x2003: case 0x2004:
+    case 0x2005: case 0x2006: case 0x2007: case 0x2008: case 0x2009: case 0x200A: case 0x2028: case 0x2029:
+    case 0x202F: case 0x205F: case 0x3000: return true;
+    }
+    return false;
+}
+
+template <typename S>
+std::vector<u64> sorted_join(const S& s, bool one_byte)
+{
+    std::vector<std::vector<u64>> toks;
+    std::vector<u64> cur;
+    for (i64 i = 0; i <= s.n; ++i) {
+        if (i == s.n || unit_is_space(s[i], one_byte)) {
+            if (!cur.empty()) toks.push_back(cur);
+            cur.clear();
+        }
+        else cur.push_back(s[i]);
+    }
+    std::sort(toks.begin(), toks.end());
+    std::vector<u64> out;
+    for (size_t k = 0; k < toks.size(); ++k) {
+        if (k) out.push_back(0x20);
+        out.insert(out.end(), toks[k].begin(), toks[k].end());
+    }
+    return out;
+}
+
+/* fuzz::ratio (fuzz_impl.hpp:28-32) */
+template <typename S1, typename S2>
+double ratio_plain(const S1& a, const S2& b, double cutoff)
+{
+    PM pm;
+    pm.build(a);
+    return ratio_with_pm(pm, a, b, cutoff);
+}
+
+template <typename S1, typename S2>
+double token_scorer(int metric, const S1& s1, const S2& s2, double cutoff)
+{
+    if (metric == RFO_QRATIO) {
+        if (!s1.n || !s2.n) return 0.0;
+        return ratio_plain(s1, s2, cutoff);
+    }
+    if (cutoff > 100) return 0.0;
+    const std::vector<u64> a = sorted_join(s1, sizeof(s1.p[0]) == 1), b = sorted_join(s2, sizeof(s2.p[0]) == 1);
+    const Str<u64> sa{a.data(), (i64)a.size()}, sb{b.data(), (i64)b.size()};
+    if (metric == RFO_TOKEN_SORT_RATIO) return ratio_plain(sa, sb, cutoff);
+    return partial_ratio_score(sa, sb, cutoff);
+}
+
+/* MultiRatio's chain for one inserted string (fuzz.hpp:50-95 over MultiIndel) */
+template <typename S1, typename S2>
+double multi_ratio(const S1& a, const S2& b, double cutoff)
+{
+    PM pm;
+    pm.build(a);
+    const u64 L = a.n ? (u64)lcs_full(pm, b) : 0, M = (u64)(a.n + b.n);
+    double r;
+    chain_multi_dist(RFO_NORM_SIMILARITY, M, M - 2 * L, 0, cutoff / 100.0, nullptr, &r);
+    return r * 100.0;
+}
+
+/* MultiTokenSortRatio (fuzz.hpp:236-278): MultiRatio over the sorted-split joins;
+ * MultiQRatio (fuzz.hpp:719-774): 0 when either string is empty, else MultiRatio */
+template <typename S1, typename S2>
+double token_multi(int metric, const S1& s1, const S2& s2, double cutoff)
+{
+    if (metric == RFO_QRATIO) {
+        if (!s1.n || !s2.n) return 0.0;
+        return multi_ratio(s1, s2, cutoff);
+    }
+    const std::vector<u64> a = sorted_join(s1, sizeof(s1.p[0]) == 1), b = sorted_join(s2, sizeof(s2.p[0]) == 1);
+    return multi_ratio(Str<u64>{a.data(), (i64)a.size()}, Str<u64>{b.data(), (i64)b.size()}, cutoff);
+}
+
 template <typename T>
 void store(void* out, int dtype, i64 idx, i64 vi, double vf, bool is_int)
 {
@@ -1096,8 +1200,7 @@ void store(void* out, int dtype, i64 idx, i64 vi, double vf, bool is_int)
 
 bool result_is_int(int metric, int op)
 {
-    if (metric == RFO_JARO || metric == RFO_JARO_WINKLER || metric == RFO_RATIO || metric == RFO_PARTIAL_RATIO)
-        return false;
+    if (metric == RFO_JARO || metric == RFO_JARO_WINKLER || metric >= RFO_RATIO) return false;
     return op == RFO_DISTANCE || op == RFO_SIMILARITY;
 }
 

@@ -32,7 +32,10 @@ enum {
     RFO_JARO = 4,
     RFO_JARO_WINKLER = 5,
     RFO_RATIO = 6,
-    RFO_PARTIAL_RATIO = 7
+    RFO_PARTIAL_RATIO = 7,
+    RFO_TOKEN_SORT_RATIO = 8,
+    RFO_PARTIAL_TOKEN_SORT_RATIO = 9,
+    RFO_QRATIO = 10
 };
 
 /* operations */

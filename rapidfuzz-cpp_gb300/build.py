@@ -15,7 +15,8 @@ LIB = os.path.join(LIB_DIR, "librapidfuzz_gb300.so")
 PEAK_LIB = os.path.join(LIB_DIR, "librfg_peak.so")  # INT32 issue-rate microbenchmark (bench roofline)
 COUNT_LIB = os.path.join(LIB_DIR, "librfg_count.so")  # executed word steps of the kernels (bench roofline)
 
-SOURCES = ["rfg_api.cu", "rfg_k_lev.cu", "rfg_k_lcs.cu", "rfg_k_osa.cu", "rfg_k_jaro.cu", "rfg_k_generic.cu", "rfg_noalloc.cu", "rfg_server.cu"]
+SOURCES = ["rfg_api.cu", "rfg_k_lev.cu", "rfg_k_lcs.cu", "rfg_k_osa.cu", "rfg_k_jaro.cu", "rfg_k_generic.cu", "rfg_noalloc.cu", "rfg_server.cu",
+           "rfg_token.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
          "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
@@ -33,7 +34,7 @@ def _deps():
 
 
 def _compile(src):
-    obj = os.path.join(OBJ, src.replace(".cu", ".o"))
+    obj = os.path.join(OBJ, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc()] + ARCH + FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -29,6 +29,7 @@
 #include "rapidfuzz_gb300.h"
 #include "rfg_device.cuh"
 #include "rfg_kernels.h"
+#include "rfg_token.h"
 
 using namespace rfg;
 
@@ -143,8 +144,7 @@ inline u64 unit_at(const void* data, int width, int64_t i)
 
 inline bool is_int_result(int metric, int op)
 {
-    if (metric == RFG_JARO || metric == RFG_JARO_WINKLER || metric == RFG_RATIO || metric == RFG_PARTIAL_RATIO)
-        return false;
+    if (metric == RFG_JARO || metric == RFG_JARO_WINKLER || metric >= RFG_RATIO) return false;
     return op == RFG_DISTANCE || op == RFG_SIMILARITY;
 }
 
@@ -211,8 +211,17 @@ rfg_status check_strings(const rfg_strings* s, const char* what)
     return RFG_OK;
 }
 
+/* token_sort_ratio, partial_token_sort_ratio and QRatio: a host front end over the
+ * ratio / partial_ratio engine */
+inline bool is_token_metric(int metric) { return metric >= RFG_TOKEN_SORT_RATIO && metric <= RFG_QRATIO; }
+inline int token_base(int metric) { return metric == RFG_PARTIAL_TOKEN_SORT_RATIO ? RFG_PARTIAL_RATIO : RFG_RATIO; }
+
+/* the metrics the engine scores directly (every entry point) */
 rfg_status check_metric_op(int metric, int op, int form)
 {
+    if (is_token_metric(metric))
+        return fail(RFG_ERR_INVALID_ARGUMENT, "the token scorers take rfg_score_f64, rfg_cached_*, rfg_multi_* and "
+                                              "rfg_cdist only");
     if (metric < RFG_LEVENSHTEIN || metric > RFG_PARTIAL_RATIO)
         return fail(RFG_ERR_INVALID_ARGUMENT, "unknown metric %d", metric);
     if (op < RFG_DISTANCE || op > RFG_NORMALIZED_SIMILARITY) return fail(RFG_ERR_INVALID_ARGUMENT, "unknown op %d", op);
@@ -223,6 +232,20 @@ rfg_status check_metric_op(int metric, int op, int form)
         return fail(RFG_ERR_INVALID_ARGUMENT, "fuzz::partial_ratio only has a similarity");
     if (metric == RFG_PARTIAL_RATIO && form == RFG_FORM_MULTI)
         return fail(RFG_ERR_INVALID_ARGUMENT, "fuzz::partial_ratio has no experimental::Multi form");
+    return RFG_OK;
+}
+
+
+/* check_metric_op for the entry points that take the token scorers too */
+rfg_status check_any_metric_op(int metric, int op, int form)
+{
+    if (!is_token_metric(metric)) return check_metric_op(metric, op, form);
+    if (op < RFG_DISTANCE || op > RFG_NORMALIZED_SIMILARITY) return fail(RFG_ERR_INVALID_ARGUMENT, "unknown op %d", op);
+    if (form < RFG_FORM_FREE || form > RFG_FORM_MULTI) return fail(RFG_ERR_INVALID_ARGUMENT, "unknown form %d", form);
+    if (op != RFG_SIMILARITY)
+        return fail(RFG_ERR_INVALID_ARGUMENT, "token_sort_ratio, partial_token_sort_ratio and QRatio only have a similarity");
+    if (metric == RFG_PARTIAL_TOKEN_SORT_RATIO && form == RFG_FORM_MULTI)
+        return fail(RFG_ERR_INVALID_ARGUMENT, "fuzz::partial_token_sort_ratio has no experimental::Multi form");
     return RFG_OK;
 }
 
@@ -795,10 +818,16 @@ rfg_status check_dtype(int metric, int op, int dt)
     return RFG_OK;
 }
 
+rfg_status token_cdist(int metric, int op, int form, const rfg_strings* Q, bool q_dev, const rfg_strings* C,
+                       bool c_dev, const rfg_params* p, rfg_cutoff cut, int dt, void* out, int64_t ld, bool dev_out);
+
 /* cdist over host or device batches */
 rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const rfg_strings* C, const rfg_params* p,
                       rfg_cutoff cut, int dt, void* out, int64_t ld, uint32_t flags)
 {
+    if (is_token_metric(metric))
+        return token_cdist(metric, op, form, Q, flags & RFG_DEVICE_INPUTS, C, flags & RFG_DEVICE_INPUTS, p, cut, dt, out,
+                           ld, flags & RFG_DEVICE_OUTPUT);
     RFG_TRY(check_metric_op(metric, op, form));
     RFG_TRY(check_strings(Q, "queries"));
     RFG_TRY(check_strings(C, "choices"));
@@ -878,6 +907,104 @@ rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const 
     }
     RFG_CUDA(cudaStreamSynchronize(g.copy));
     return check_batch(pb, g.stream);
+}
+
+/* a host copy of a batch (the token front end downloads device batches) */
+struct HostStrings {
+    std::vector<unsigned char> data;
+    std::vector<int64_t> off;
+};
+
+rfg_status check_offsets(const int64_t* off, int64_t n, const char* what)
+{
+    for (int64_t i = 0; i < n; ++i)
+        if (off[i] < 0 || off[i + 1] < off[i] || off[i + 1] - off[i] > INT32_MAX)
+            return fail(RFG_ERR_INVALID_ARGUMENT, "%s: offsets must be non-decreasing and >= 0", what);
+    return RFG_OK;
+}
+
+rfg_status download_strings(const rfg_strings* s, HostStrings* h, const char* what)
+{
+    const int64_t n = s->count;
+    h->off.assign((size_t)n + 1, 0);
+    RFG_CUDA(cudaMemcpyAsync(h->off.data(), s->offsets, (size_t)(n + 1) * 8, cudaMemcpyDeviceToHost, g.stream));
+    RFG_CUDA(cudaStreamSynchronize(g.stream));
+    RFG_TRY(check_offsets(h->off.data(), n, what));
+    const size_t bytes = n ? (size_t)h->off[n] * s->char_width : 0;
+    h->data.assign(bytes + 16, 0);
+    if (bytes) {
+        RFG_CUDA(cudaMemcpyAsync(h->data.data(), s->data, bytes, cudaMemcpyDeviceToHost, g.stream));
+        RFG_CUDA(cudaStreamSynchronize(g.stream));
+    }
+    return RFG_OK;
+}
+
+/* token_sort_ratio / partial_token_sort_ratio (fuzz_impl.hpp:294-360): the engine's ratio /
+ * partial_ratio over sorted_split(s).join() of every string, made on the host threads
+ * (rfg_token.cpp); the reference's `score_cutoff > 100` early exit is the engine's own
+ * result there.  QRatio (fuzz_impl.hpp:887-931): ratio, then 0 wherever the query or the
+ * choice is empty (ratio only gives a non-zero there when both are). */
+rfg_status token_cdist(int metric, int op, int form, const rfg_strings* Q, bool q_dev, const rfg_strings* C,
+                       bool c_dev, const rfg_params* p, rfg_cutoff cut, int dt, void* out, int64_t ld, bool dev_out)
+{
+    RFG_TRY(check_any_metric_op(metric, op, form));
+    RFG_TRY(check_strings(Q, "queries"));
+    RFG_TRY(check_strings(C, "choices"));
+    RFG_TRY(check_dtype(metric, op, dt));
+    const int64_t nq = Q->count, nc = C->count;
+    if (ld == 0) ld = nc;
+    if (ld < nc) return fail(RFG_ERR_INVALID_ARGUMENT, "ld must be >= the number of choices");
+    if (!out && nq * nc) return fail(RFG_ERR_INVALID_ARGUMENT, "out is NULL");
+    RFG_TRY(ensure_ctx());
+    HostStrings hq, hc, jq, jc;
+    rfg_strings q = *Q, c = *C;
+    if (q_dev) {
+        RFG_TRY(download_strings(Q, &hq, "queries"));
+        q.data = hq.data.data();
+        q.offsets = hq.off.data();
+    }
+    if (c_dev) {
+        RFG_TRY(download_strings(C, &hc, "choices"));
+        c.data = hc.data.data();
+        c.offsets = hc.off.data();
+    }
+    RFG_TRY(check_offsets(q.offsets, nq, "queries"));
+    RFG_TRY(check_offsets(c.offsets, nc, "choices"));
+    if ((!q.data && nq && q.offsets[nq] > q.offsets[0]) || (!c.data && nc && c.offsets[nc] > c.offsets[0]))
+        return fail(RFG_ERR_INVALID_ARGUMENT, "string data is NULL");
+    if (metric != RFG_QRATIO) {
+        token_sort_join_set(q.data, q.offsets, nq, q.char_width, &jq.data, &jq.off);
+        token_sort_join_set(c.data, c.offsets, nc, c.char_width, &jc.data, &jc.off);
+        q.data = jq.data.data();
+        q.offsets = jq.off.data();
+        c.data = jc.data.data();
+        c.offsets = jc.off.data();
+    }
+    RFG_TRY(cdist_impl(token_base(metric), op, form, &q, &c, p, cut, dt, out, ld, dev_out ? RFG_DEVICE_OUTPUT : 0));
+    if (metric != RFG_QRATIO) return RFG_OK;
+    std::vector<int64_t> lists; /* empty query rows, then empty choice columns */
+    for (int64_t i = 0; i < nq; ++i)
+        if (q.offsets[i + 1] == q.offsets[i]) lists.push_back(i);
+    const int64_t nr = (int64_t)lists.size();
+    for (int64_t j = 0; j < nc; ++j)
+        if (c.offsets[j + 1] == c.offsets[j]) lists.push_back(j);
+    const int64_t ncol = (int64_t)lists.size() - nr;
+    if (!nr || !ncol) return RFG_OK;
+    if (!dev_out) {
+        for (int64_t a = 0; a < nr; ++a)
+            for (int64_t b = 0; b < ncol; ++b) ((double*)out)[lists[a] * ld + lists[nr + b]] = 0.0;
+        return RFG_OK;
+    }
+    DBuf d;
+    RFG_TRY(d.alloc(lists.size() * 8));
+    RFG_CUDA(cudaMemcpyAsync(d.p, lists.data(), lists.size() * 8, cudaMemcpyHostToDevice, g.stream));
+    double* o = (double*)out;
+    const int64_t* rows = d.as<int64_t>();
+    const int64_t* cols = rows + nr;
+    void* args[] = {&o, &ld, &rows, (void*)&nr, &cols, (void*)&ncol};
+    const int64_t blocks = std::min<int64_t>((nr * ncol + 255) / 256, 152 * 16);
+    RFG_CUDA(cudaLaunchKernel(zero_pairs_kernel(), dim3((unsigned)blocks), dim3(256), args, 0, g.stream));
+    return RFG_OK;
 }
 
 /* One pair in one round trip (the per-call path of the free functions and the cached
@@ -995,11 +1122,25 @@ rfg_status score_one(int metric, int op, int form, const void* s1, int64_t l1, i
     if (l1 < 0 || l2 < 0) return fail(RFG_ERR_INVALID_ARGUMENT, "negative length");
     if ((!s1 && l1) || (!s2 && l2)) return fail(RFG_ERR_INVALID_ARGUMENT, "string data is NULL");
     if (!result) return fail(RFG_ERR_INVALID_ARGUMENT, "result is NULL");
-    RFG_TRY(check_metric_op(metric, op, form));
+    RFG_TRY(check_any_metric_op(metric, op, form));
     RFG_TRY(check_dtype(metric, op, dt));
     const ScoreParams sp = to_sp(p);
     RFG_TRY(check_params(metric, sp));
     RFG_TRY(ensure_ctx());
+    std::vector<unsigned char> j1, j2;
+    if (is_token_metric(metric)) { /* the front end of token_cdist, for one pair */
+        if (metric == RFG_QRATIO && (!l1 || !l2)) {
+            *(double*)result = 0.0;
+            return RFG_OK;
+        }
+        if (metric != RFG_QRATIO) {
+            l1 = token_sort_join(s1, l1, w1, &j1);
+            l2 = token_sort_join(s2, l2, w2, &j2);
+            s1 = j1.data();
+            s2 = j2.data();
+        }
+        metric = token_base(metric);
+    }
     bool done = false;
     RFG_TRY(score_pair_trip(metric, op, form, s1, l1, w1, s2, l2, w2, sp, cut, dt, result, &done));
     if (done) return RFG_OK;
@@ -1112,8 +1253,8 @@ rfg_status rfg_cached_create(rfg_metric metric, const void* s1, int64_t len1, in
     std::lock_guard<std::recursive_mutex> lk(g.mu);
     if (!out) return fail(RFG_ERR_INVALID_ARGUMENT, "out is NULL");
     *out = nullptr;
-    const bool sim_only = metric == RFG_RATIO || metric == RFG_PARTIAL_RATIO;
-    RFG_TRY(check_metric_op(metric, sim_only ? RFG_SIMILARITY : RFG_DISTANCE, RFG_FORM_CACHED));
+    const bool sim_only = metric == RFG_RATIO || metric == RFG_PARTIAL_RATIO || is_token_metric(metric);
+    RFG_TRY(check_any_metric_op(metric, sim_only ? RFG_SIMILARITY : RFG_DISTANCE, RFG_FORM_CACHED));
     if (!valid_width(width1)) return fail(RFG_ERR_INVALID_ARGUMENT, "char width must be 1, 2, 4 or 8");
     if (len1 < 0 || (!s1 && len1)) return fail(RFG_ERR_INVALID_ARGUMENT, "invalid s1");
     RFG_TRY(check_params(metric, to_sp(params)));
@@ -1125,6 +1266,11 @@ rfg_status rfg_cached_create(rfg_metric metric, const void* s1, int64_t len1, in
     h->width = width1;
     h->len = len1;
     h->host.assign((const unsigned char*)s1, (const unsigned char*)s1 + len1 * width1);
+    if (is_token_metric(metric) && metric != RFG_QRATIO) { /* the sorted-split join, as CachedTokenSortRatio keeps */
+        std::vector<unsigned char> j;
+        len1 = h->len = token_sort_join(s1, len1, width1, &j);
+        h->host.assign(j.begin(), j.begin() + len1 * width1);
+    }
     int64_t off[2] = {0, len1};
     rfg_strings q{h->host.data(), off, 1, width1};
     rfg_status st = query_info_from_host(h->host.data(), off, 1, width1, &h->qs);
@@ -1149,6 +1295,12 @@ static rfg_status cached_many(rfg_cached h, int op, const rfg_strings* C, rfg_cu
                               uint32_t flags)
 {
     if (!h) return fail(RFG_ERR_INVALID_ARGUMENT, "scorer is NULL");
+    if (is_token_metric(h->metric)) {
+        int64_t qo[2] = {0, h->len};
+        rfg_strings q{h->host.data(), qo, 1, h->width};
+        return token_cdist(h->metric, op, RFG_FORM_CACHED, &q, false, C, flags & RFG_DEVICE_INPUTS, &h->params, cut, dt,
+                           out, C ? C->count : 0, flags & RFG_DEVICE_OUTPUT);
+    }
     RFG_TRY(check_metric_op(h->metric, op, RFG_FORM_CACHED));
     RFG_TRY(check_strings(C, "choices"));
     RFG_TRY(check_dtype(h->metric, op, dt));
@@ -1210,10 +1362,25 @@ rfg_status rfg_cached_score_f64(rfg_cached h, rfg_op op, const void* s2, int64_t
     if (!h) return fail(RFG_ERR_INVALID_ARGUMENT, "scorer is NULL");
     if (is_int_result(h->metric, op)) return fail(RFG_ERR_INVALID_ARGUMENT, "this metric/op returns an integer");
     if (!valid_width(width2) || len2 < 0 || (!s2 && len2) || !result) return fail(RFG_ERR_INVALID_ARGUMENT, "invalid s2");
-    RFG_TRY(check_metric_op(h->metric, op, RFG_FORM_CACHED));
+    RFG_TRY(check_any_metric_op(h->metric, op, RFG_FORM_CACHED));
     RFG_TRY(ensure_ctx());
+    int metric = h->metric;
+    const void* t2 = s2;
+    int64_t n2 = len2;
+    std::vector<unsigned char> j2;
+    if (is_token_metric(metric)) { /* CachedTokenSortRatio / CachedPartialTokenSortRatio / CachedQRatio */
+        if (metric == RFG_QRATIO && (!h->len || !len2)) {
+            *result = 0.0;
+            return RFG_OK;
+        }
+        if (metric != RFG_QRATIO) {
+            n2 = token_sort_join(s2, len2, width2, &j2);
+            t2 = j2.data();
+        }
+        metric = token_base(metric);
+    }
     bool done = false;
-    RFG_TRY(score_pair_trip(h->metric, op, RFG_FORM_CACHED, h->host.data(), h->len, h->width, s2, len2, width2,
+    RFG_TRY(score_pair_trip(metric, op, RFG_FORM_CACHED, h->host.data(), h->len, h->width, t2, n2, width2,
                             to_sp(&h->params), rfg_cutoff{0, score_cutoff, 0, score_hint}, RFG_F64, result, &done));
     if (done) return RFG_OK;
     int64_t off[2] = {0, len2};
@@ -1255,7 +1422,8 @@ rfg_status rfg_multi_create(rfg_metric metric, int32_t max_len, size_t count, co
     std::lock_guard<std::recursive_mutex> lk(g.mu);
     if (!out) return fail(RFG_ERR_INVALID_ARGUMENT, "out is NULL");
     *out = nullptr;
-    RFG_TRY(check_metric_op(metric, metric == RFG_RATIO ? RFG_SIMILARITY : RFG_DISTANCE, RFG_FORM_MULTI));
+    const bool sim_only = metric == RFG_RATIO || is_token_metric(metric);
+    RFG_TRY(check_any_metric_op(metric, sim_only ? RFG_SIMILARITY : RFG_DISTANCE, RFG_FORM_MULTI));
     if (max_len != 8 && max_len != 16 && max_len != 32 && max_len != 64)
         return fail(RFG_ERR_INVALID_ARGUMENT, "MaxLen must be 8, 16, 32 or 64");
     const ScoreParams sp = to_sp(params);
@@ -1284,6 +1452,11 @@ rfg_status rfg_multi_insert(rfg_multi h, const void* s, int64_t len, int32_t wid
     if (!h) return fail(RFG_ERR_INVALID_ARGUMENT, "scorer is NULL");
     if (!valid_width(width) || len < 0 || (!s && len)) return fail(RFG_ERR_INVALID_ARGUMENT, "invalid string");
     if (h->strs.size() >= h->count) return fail(RFG_ERR_INVALID_ARGUMENT, "out of bounds insert");
+    std::vector<unsigned char> j;
+    if (h->metric == RFG_TOKEN_SORT_RATIO) { /* MultiTokenSortRatio inserts the sorted-split join */
+        len = token_sort_join(s, len, width, &j);
+        s = j.data();
+    }
     if (len > h->max_len) return fail(RFG_ERR_INVALID_ARGUMENT, "string longer than MaxLen");
     std::vector<u64> v(len);
     for (int64_t i = 0; i < len; ++i) v[i] = unit_at(s, width, i);
@@ -1303,11 +1476,15 @@ static rfg_status multi_score(rfg_multi h, int op, void* scores, size_t score_co
                               int32_t width2, rfg_cutoff cut, int dt)
 {
     if (!h) return fail(RFG_ERR_INVALID_ARGUMENT, "scorer is NULL");
-    RFG_TRY(check_metric_op(h->metric, op, RFG_FORM_MULTI));
+    RFG_TRY(check_any_metric_op(h->metric, op, RFG_FORM_MULTI));
     if (!valid_width(width2) || len2 < 0 || (!s2 && len2)) return fail(RFG_ERR_INVALID_ARGUMENT, "invalid s2");
     const size_t rc = multi_result_count(h);
     if (score_count < rc) return fail(RFG_ERR_INVALID_ARGUMENT, "scores has to have >= result_count() elements");
     if (!scores && rc) return fail(RFG_ERR_INVALID_ARGUMENT, "scores is NULL");
+    if (h->metric == RFG_QRATIO && !len2) { /* MultiQRatio: the inserted strings score 0 (fuzz.hpp:752-767) */
+        for (size_t i = 0; i < h->strs.size(); ++i) ((double*)scores)[i] = 0.0;
+        return RFG_OK;
+    }
     /* declared slots not inserted yet, and the padding up to result_count(), score as
      * empty strings */
     const int w = h->width;

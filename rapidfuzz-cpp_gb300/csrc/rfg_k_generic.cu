@@ -33,4 +33,17 @@ const void* topk_merge_kernel() { return (const void*)&k_topk_merge; }
 
 const void* jaro_tables_kernel() { return (const void*)&k_jaro_tables; }
 
+/* QRatio's empty-string rule (fuzz_impl.hpp:887-931) on a device result matrix: the
+ * entries (rows[i], cols[j]) are set to 0 (ratio gives 100 where both strings are
+ * empty).  Grid-stride over nr * ncol entries. */
+__global__ void k_zero_pairs(double* out, int64_t ld, const int64_t* rows, int64_t nr, const int64_t* cols,
+                             int64_t ncol)
+{
+    const int64_t total = nr * ncol;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x)
+        out[rows[t / ncol] * ld + cols[t % ncol]] = 0.0;
+}
+
+const void* zero_pairs_kernel() { return (const void*)&k_zero_pairs; }
+
 } // namespace rfg

@@ -11,7 +11,10 @@
  *   free functions   rapidfuzz/distance/{Levenshtein,Indel,LCSseq,OSA,Jaro,JaroWinkler}.hpp
  *   Cached* scorers  same files (CachedLevenshtein Levenshtein.hpp:421-482, ...)
  *   Multi* scorers   experimental::Multi*<MaxLen> (Levenshtein.hpp:297-419, ...)
- *   fuzz::ratio      rapidfuzz/fuzz.hpp:44-126
+ *   fuzz::ratio      rapidfuzz/fuzz.hpp:44-126 (and CachedRatio, experimental::MultiRatio)
+ *   fuzz::partial_ratio, token_sort_ratio, partial_token_sort_ratio, QRatio
+ *                    rapidfuzz/fuzz.hpp:128-373, 692-804 (Cached*, MultiTokenSortRatio,
+ *                    MultiQRatio)
  * Exceptions: std::invalid_argument where the reference throws it; std::runtime_error
  * for device failures (the reference has none).
  */
@@ -519,6 +522,72 @@ struct CachedPartialRatio : rapidfuzz_gb300::detail::CachedScorer {
     }
 };
 
+/* token_sort_ratio (fuzz.hpp:203-234, fuzz_impl.hpp:297-311), partial_token_sort_ratio
+ * (fuzz.hpp:313-341, fuzz_impl.hpp:334-349), QRatio (fuzz.hpp:692-717,
+ * fuzz_impl.hpp:891-909).  Tokens compare as unsigned code units (for `char` strings this
+ * is the reference's order where `char` is unsigned). */
+#define RFG_FUZZ_FREE(NAME, METRIC)                                                                                \
+    template <typename Sentence1, typename Sentence2>                                                              \
+    double NAME(const Sentence1& s1, const Sentence2& s2, double score_cutoff = 0)                                 \
+    {                                                                                                              \
+        return detail::score_f(METRIC, RFG_SIMILARITY, detail::units(s1), detail::units(s2),                       \
+                               rfg_params{1, 1, 1, 0.1}, score_cutoff, score_cutoff);                              \
+    }                                                                                                              \
+    template <typename InputIt1, typename InputIt2, detail::if_iter<InputIt1> = 0>                                 \
+    double NAME(InputIt1 first1, InputIt1 last1, InputIt2 first2, InputIt2 last2, double score_cutoff = 0)         \
+    {                                                                                                              \
+        return detail::score_f(METRIC, RFG_SIMILARITY, detail::units(first1, last1), detail::units(first2, last2), \
+                               rfg_params{1, 1, 1, 0.1}, score_cutoff, score_cutoff);                              \
+    }
+RFG_FUZZ_FREE(token_sort_ratio, RFG_TOKEN_SORT_RATIO)
+RFG_FUZZ_FREE(partial_token_sort_ratio, RFG_PARTIAL_TOKEN_SORT_RATIO)
+RFG_FUZZ_FREE(QRatio, RFG_QRATIO)
+#undef RFG_FUZZ_FREE
+
+/* CachedTokenSortRatio (fuzz.hpp:282-305), CachedPartialTokenSortRatio (fuzz.hpp:342-366),
+ * CachedQRatio (fuzz.hpp:776-797): s1 (its sorted-split join for the token sorts) lives
+ * on the device */
+#define RFG_FUZZ_CACHED(NAME, METRIC)                                                                              \
+    template <typename CharT1>                                                                                     \
+    struct NAME : rapidfuzz_gb300::detail::CachedScorer {                                                          \
+        template <typename Sentence1>                                                                              \
+        explicit NAME(const Sentence1& s1)                                                                         \
+            : CachedScorer(METRIC, rapidfuzz_gb300::detail::units(s1), rfg_params{1, 1, 1, 0.1})                   \
+        {}                                                                                                         \
+        template <typename InputIt1, rapidfuzz_gb300::detail::if_iter<InputIt1> = 0>                              \
+        NAME(InputIt1 first1, InputIt1 last1)                                                                      \
+            : CachedScorer(METRIC, rapidfuzz_gb300::detail::units(first1, last1), rfg_params{1, 1, 1, 0.1})        \
+        {}                                                                                                         \
+        template <typename Sentence2>                                                                              \
+        double similarity(const Sentence2& s2, double score_cutoff = 0.0, double score_hint = 0.0) const           \
+        {                                                                                                          \
+            return cached_f(RFG_SIMILARITY, rapidfuzz_gb300::detail::units(s2), score_cutoff, score_hint);         \
+        }                                                                                                          \
+        template <typename InputIt2, rapidfuzz_gb300::detail::if_iter<InputIt2> = 0>                              \
+        double similarity(InputIt2 first2, InputIt2 last2, double score_cutoff = 0.0,                              \
+                          double score_hint = 0.0) const                                                           \
+        {                                                                                                          \
+            return cached_f(RFG_SIMILARITY, rapidfuzz_gb300::detail::units(first2, last2), score_cutoff,           \
+                            score_hint);                                                                           \
+        }                                                                                                          \
+    };
+RFG_FUZZ_CACHED(CachedTokenSortRatio, RFG_TOKEN_SORT_RATIO)
+RFG_FUZZ_CACHED(CachedPartialTokenSortRatio, RFG_PARTIAL_TOKEN_SORT_RATIO)
+RFG_FUZZ_CACHED(CachedQRatio, RFG_QRATIO)
+#undef RFG_FUZZ_CACHED
+
+#if __cplusplus >= 201703L
+template <typename Sentence1>
+explicit CachedTokenSortRatio(const Sentence1&)
+    -> CachedTokenSortRatio<typename std::decay<decltype(*std::begin(std::declval<Sentence1>()))>::type>;
+template <typename Sentence1>
+explicit CachedPartialTokenSortRatio(const Sentence1&)
+    -> CachedPartialTokenSortRatio<typename std::decay<decltype(*std::begin(std::declval<Sentence1>()))>::type>;
+template <typename Sentence1>
+explicit CachedQRatio(const Sentence1&)
+    -> CachedQRatio<typename std::decay<decltype(*std::begin(std::declval<Sentence1>()))>::type>;
+#endif
+
 } // namespace fuzz
 
 /* ---------------------------------------------------------------- Multi* */
@@ -685,6 +754,35 @@ struct MultiRatio : rapidfuzz_gb300::experimental::detail_multi::MultiScorer<RFG
     MultiRatio(size_t count)
         : rapidfuzz_gb300::experimental::detail_multi::MultiScorer<RFG_RATIO, MaxLen, false>(count,
                                                                                            rfg_params{1, 1, 1, 0.1})
+    {}
+    template <typename Sentence2>
+    void similarity(double* scores, size_t score_count, const Sentence2& s2, double score_cutoff = 0) const
+    {
+        this->run_f(RFG_SIMILARITY, scores, score_count, s2, score_cutoff);
+    }
+};
+
+/* fuzz.hpp:236-278 (insert keeps the sorted-split join) */
+template <int MaxLen>
+struct MultiTokenSortRatio
+    : rapidfuzz_gb300::experimental::detail_multi::MultiScorer<RFG_TOKEN_SORT_RATIO, MaxLen, false> {
+    MultiTokenSortRatio(size_t count)
+        : rapidfuzz_gb300::experimental::detail_multi::MultiScorer<RFG_TOKEN_SORT_RATIO, MaxLen, false>(
+              count, rfg_params{1, 1, 1, 0.1})
+    {}
+    template <typename Sentence2>
+    void similarity(double* scores, size_t score_count, const Sentence2& s2, double score_cutoff = 0) const
+    {
+        this->run_f(RFG_SIMILARITY, scores, score_count, s2, score_cutoff);
+    }
+};
+
+/* fuzz.hpp:719-774 */
+template <int MaxLen>
+struct MultiQRatio : rapidfuzz_gb300::experimental::detail_multi::MultiScorer<RFG_QRATIO, MaxLen, false> {
+    MultiQRatio(size_t count)
+        : rapidfuzz_gb300::experimental::detail_multi::MultiScorer<RFG_QRATIO, MaxLen, false>(count,
+                                                                                            rfg_params{1, 1, 1, 0.1})
     {}
     template <typename Sentence2>
     void similarity(double* scores, size_t score_count, const Sentence2& s2, double score_cutoff = 0) const

@@ -1,7 +1,8 @@
 """The reference's function and class names over the generic entry points
 (rapidfuzz/distance/*.hpp, rapidfuzz/fuzz.hpp)."""
 from ._lib import (DISTANCE, SIMILARITY, NORMALIZED_DISTANCE, NORMALIZED_SIMILARITY, LEVENSHTEIN, INDEL, LCSSEQ,
-                   OSA, JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO, Cached, Multi, score)
+                   OSA, JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO, TOKEN_SORT_RATIO, PARTIAL_TOKEN_SORT_RATIO,
+                   QRATIO, Cached, Multi, score)
 
 __all__ = []
 
@@ -44,6 +45,24 @@ def fuzz_partial_ratio(s1, s2, score_cutoff=0.0):
 
 
 __all__.append("fuzz_partial_ratio")
+
+
+def fuzz_token_sort_ratio(s1, s2, score_cutoff=0.0):
+    """fuzz::token_sort_ratio (fuzz_impl.hpp:297-311)"""
+    return score(TOKEN_SORT_RATIO, SIMILARITY, s1, s2, score_cutoff)
+
+
+def fuzz_partial_token_sort_ratio(s1, s2, score_cutoff=0.0):
+    """fuzz::partial_token_sort_ratio (fuzz_impl.hpp:334-349)"""
+    return score(PARTIAL_TOKEN_SORT_RATIO, SIMILARITY, s1, s2, score_cutoff)
+
+
+def fuzz_QRatio(s1, s2, score_cutoff=0.0):
+    """fuzz::QRatio (fuzz_impl.hpp:891-909)"""
+    return score(QRATIO, SIMILARITY, s1, s2, score_cutoff)
+
+
+__all__ += ["fuzz_token_sort_ratio", "fuzz_partial_token_sort_ratio", "fuzz_QRatio"]
 
 
 class _CachedBase:
@@ -100,6 +119,23 @@ class CachedPartialRatio:
 __all__.append("CachedPartialRatio")
 
 
+def _cached_fuzz(name, metric, doc):
+    def __init__(self, s1):
+        self._c = Cached(metric, s1)
+
+    def similarity(self, s2, score_cutoff=0.0, score_hint=0.0):
+        return self._c.score(SIMILARITY, s2, score_cutoff, score_hint)
+
+    globals()[name] = type(name, (), {"__init__": __init__, "similarity": similarity, "__doc__": doc})
+    __all__.append(name)
+
+
+_cached_fuzz("CachedTokenSortRatio", TOKEN_SORT_RATIO, "fuzz::CachedTokenSortRatio (fuzz_impl.hpp:313-328)")
+_cached_fuzz("CachedPartialTokenSortRatio", PARTIAL_TOKEN_SORT_RATIO,
+             "fuzz::CachedPartialTokenSortRatio (fuzz_impl.hpp:351-366)")
+_cached_fuzz("CachedQRatio", QRATIO, "fuzz::CachedQRatio (fuzz_impl.hpp:911-929)")
+
+
 class experimental:
     """experimental::Multi* (max_len = the MaxLen template argument)"""
 
@@ -139,6 +175,14 @@ class experimental:
 
         def similarity(self, s2, score_cutoff=0.0):
             return self._m.score(SIMILARITY, s2, score_cutoff)
+
+    class MultiTokenSortRatio(MultiRatio):
+        """fuzz::experimental::MultiTokenSortRatio (fuzz.hpp:236-278)"""
+        metric = TOKEN_SORT_RATIO
+
+    class MultiQRatio(MultiRatio):
+        """fuzz::experimental::MultiQRatio (fuzz.hpp:719-774)"""
+        metric = QRATIO
 
 
 __all__.append("experimental")

@@ -7,7 +7,9 @@ import numpy as np
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 lib_path = os.path.join(PKG_DIR, "lib", "librapidfuzz_gb300.so")
 
-LEVENSHTEIN, INDEL, LCSSEQ, OSA, JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO = range(8)
+(LEVENSHTEIN, INDEL, LCSSEQ, OSA, JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO, TOKEN_SORT_RATIO,
+ PARTIAL_TOKEN_SORT_RATIO, QRATIO) = range(11)
+FUZZ_METRICS = (RATIO, PARTIAL_RATIO, TOKEN_SORT_RATIO, PARTIAL_TOKEN_SORT_RATIO, QRATIO)
 DISTANCE, SIMILARITY, NORMALIZED_DISTANCE, NORMALIZED_SIMILARITY = range(4)
 FORM_FREE, FORM_CACHED, FORM_MULTI = range(3)
 I32, I64, F64 = range(3)
@@ -125,7 +127,7 @@ def check(status):
 
 
 def result_is_int(metric, op):
-    if metric in (JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO):
+    if metric in (JARO, JARO_WINKLER) or metric in FUZZ_METRICS:
         return False
     return op in (DISTANCE, SIMILARITY)
 
@@ -175,7 +177,7 @@ def make_params(weights=(1, 1, 1), prefix_weight=0.1):
 def _default_cutoff(metric, op):
     if result_is_int(metric, op):
         return (2**63 - 1) if op == DISTANCE else 0
-    return 1.0 if op in (DISTANCE, NORMALIZED_DISTANCE) and metric not in (RATIO, PARTIAL_RATIO) else 0.0
+    return 1.0 if op in (DISTANCE, NORMALIZED_DISTANCE) and metric not in FUZZ_METRICS else 0.0
 
 
 def score(metric, op, s1, s2, score_cutoff=None, score_hint=None, weights=(1, 1, 1), prefix_weight=0.1):

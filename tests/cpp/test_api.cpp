@@ -97,6 +97,38 @@ int main()
     CHECK(std::fabs(rapidfuzz::fuzz::partial_ratio(std::string("001"), std::string("220222")) - 33.3333333) < 1e-6);
     rapidfuzz::fuzz::CachedPartialRatio<char> cpr(std::string("physics 2 vid"));
     CHECK(cpr.similarity(std::string("study physics physics 2 video")) == 100.0);
+    // token scorers (tests-fuzz.cpp:82-86, 127-137)
+    CHECK(rapidfuzz::fuzz::token_sort_ratio(std::string("new york mets"), std::string("new york mets")) == 100.0);
+    CHECK(rapidfuzz::fuzz::token_sort_ratio(std::string("new york mets vs atlanta braves"),
+                                            std::string("atlanta braves vs new york mets")) == 100.0);
+    CHECK(rapidfuzz::fuzz::token_sort_ratio(std::string(""), std::string("")) == 100.0);
+    CHECK(rapidfuzz::fuzz::partial_token_sort_ratio(std::string(""), std::string("")) == 100.0);
+    CHECK(rapidfuzz::fuzz::QRatio(std::string(""), std::string("")) == 0.0);
+    CHECK(rapidfuzz::fuzz::QRatio(std::string("new york mets"), std::string("new york mets")) == 100.0);
+    rapidfuzz::fuzz::CachedTokenSortRatio<char> cts(std::string("mets new york"));
+    CHECK(cts.similarity(std::string("york  mets\tnew")) == 100.0);
+    rapidfuzz::fuzz::CachedPartialTokenSortRatio<char> cpts(std::string("york new"));
+    CHECK(cpts.similarity(std::string("mets new york")) == 100.0);
+    rapidfuzz::fuzz::CachedQRatio<char> cq(std::string(""));
+    CHECK(cq.similarity(std::string("")) == 0.0);
+    {
+        rapidfuzz::fuzz::experimental::MultiTokenSortRatio<16> mts(2);
+        mts.insert(std::string("  b a  "));
+        mts.insert(std::string("  c     b   a        "));  // 21 units; MaxLen applies to the join "a b c"
+        std::vector<double> r(mts.result_count());
+        mts.similarity(r.data(), r.size(), std::string("a b"));
+        CHECK(r[0] == 100.0 && r[1] == 75.0);
+    }
+    {
+        rapidfuzz::fuzz::experimental::MultiQRatio<8> mq(2);
+        mq.insert(std::string(""));
+        mq.insert(std::string("ab"));
+        std::vector<double> r(mq.result_count(), -1.0);
+        mq.similarity(r.data(), r.size(), std::string("ab"));
+        CHECK(r[0] == 0.0 && r[1] == 100.0);
+        mq.similarity(r.data(), r.size(), std::string(""));
+        CHECK(r[0] == 0.0 && r[1] == 0.0);
+    }
     // Multi* (Levenshtein.hpp:297-419) and its errors
     rapidfuzz::experimental::MultiLevenshtein<16> ml(3);
     ml.insert(std::string("kitten"));
@@ -155,6 +187,16 @@ int main()
         CHECK(same(rapidfuzz::fuzz::ratio(s1, s2, cf * 100), of(RFO_RATIO, RFO_SIMILARITY, 0, s1, s2, cf * 100)));
         CHECK(same(rapidfuzz::fuzz::partial_ratio(s1, s2, cf * 100),
                    of(RFO_PARTIAL_RATIO, RFO_SIMILARITY, 0, s1, s2, cf * 100)));
+        std::string t1, t2; /* whitespace-rich strings for the token scorers */
+        for (int i = 0; i < l1; ++i) t1 += " ab\tcd"[rng() % 6];
+        for (int i = 0; i < l2; ++i) t2 += " ab\tcd"[rng() % 6];
+        CHECK(same(rapidfuzz::fuzz::token_sort_ratio(t1, t2, cf * 100),
+                   of(RFO_TOKEN_SORT_RATIO, RFO_SIMILARITY, 0, t1, t2, cf * 100)));
+        CHECK(same(rapidfuzz::fuzz::partial_token_sort_ratio(t1, t2, cf * 100),
+                   of(RFO_PARTIAL_TOKEN_SORT_RATIO, RFO_SIMILARITY, 0, t1, t2, cf * 100)));
+        CHECK(same(rapidfuzz::fuzz::QRatio(t1, t2, cf * 100), of(RFO_QRATIO, RFO_SIMILARITY, 0, t1, t2, cf * 100)));
+        rapidfuzz::fuzz::CachedTokenSortRatio<char> cts2(t1);
+        CHECK(same(cts2.similarity(t2, cf * 100), of(RFO_TOKEN_SORT_RATIO, RFO_SIMILARITY, 1, t1, t2, cf * 100)));
         rapidfuzz::CachedOSA<char> co(s1);
         CHECK(same(co.normalized_similarity(s2, cf), of(RFO_OSA, RFO_NORM_SIMILARITY, 1, s1, s2, cf)));
     }

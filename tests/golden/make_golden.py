@@ -8,7 +8,8 @@ Three fixtures:
                 1/2/4/8, lengths 0..300 (word, multi-word, banded and any-length paths);
   multi.json    Multi* batches with several inserted strings;
   partial.json  fuzz::partial_ratio / CachedPartialRatio: the reference fuzz tests' inputs and
-                seeded random pairs.
+                seeded random pairs;
+  tokens.json   token_sort_ratio / partial_token_sort_ratio / QRatio (free and Cached forms).
 Doubles are stored with float.hex() so the comparison is bit-exact.
 
 Usage: python tests/golden/make_golden.py   (needs the reference checkout; run in the
@@ -25,7 +26,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 import numpy as np  # noqa: E402
 
 from oracle_lib import (DISTANCE, SIMILARITY, NORM_DISTANCE, NORM_SIMILARITY, LEVENSHTEIN, INDEL, LCSSEQ, OSA,  # noqa: E402
-                        JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO, FREE, CACHED, MULTI, as_units, reference, result_is_int,
+                        JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO, TOKEN_SORT_RATIO, PARTIAL_TOKEN_SORT_RATIO, QRATIO, FREE, CACHED, MULTI, as_units, reference, result_is_int,
                         score, make_params, pack_strings, strings_struct)
 
 OPS = (DISTANCE, SIMILARITY, NORM_DISTANCE, NORM_SIMILARITY)
@@ -258,7 +259,7 @@ def multi_cases(seed=3):
         p = make_params(weights, pw)
         is_int = result_is_int(metric, op)
         ci = (2**63 - 1 if op == DISTANCE else 0) if (cutoff is None or not is_int) else int(cutoff)
-        cf = (1.0 if op in (DISTANCE, NORM_DISTANCE) and metric != RATIO else 0.0) if (cutoff is None or is_int) \
+        cf = (1.0 if op in (DISTANCE, NORM_DISTANCE) and metric < RATIO else 0.0) if (cutoff is None or is_int) \
             else float(cutoff)
         r = ref.rfref_multi(metric, op, max_len, ctypes.byref(st), b.ctypes.data if b.size else None, b.size, 1,
                             ctypes.byref(p), ci, cf, oi.ctypes.data, of.ctypes.data, ctypes.byref(rc))
@@ -296,6 +297,17 @@ def multi_cases(seed=3):
             if metric == RATIO and cutoff is not None:
                 cutoff *= 100
         run(metric, op, max_len, strs, s2, cutoff, weights, rng.choice([0.1, 0.2]))
+    # MultiTokenSortRatio / MultiQRatio: whitespace-rich inserted strings (MaxLen bounds
+    # the raw string, so the join fits too), empty strings on both sides
+    trng = random.Random(seed + 100)
+    for _ in range(60):
+        metric = trng.choice([TOKEN_SORT_RATIO, QRATIO])
+        max_len = trng.choice([8, 16, 32, 64])
+        alpha = [97, 98, 99, 32, 32, 9]
+        strs = [bytes(rand_str(trng, alpha, 0, max_len)) for _ in range(trng.randint(1, 40))]
+        s2 = bytes(rand_str(trng, alpha, 0, 70)) if trng.random() < 0.85 else b""
+        cutoff = trng.choice([None, 0.0, 50.0, 80.0, 100.0])
+        run(metric, SIMILARITY, max_len, strs, s2, cutoff)
     return out
 
 
@@ -360,12 +372,50 @@ def partial_cases(seed=11):
     return [c for c in out if c is not None]
 
 
+def token_cases(seed=13):
+    """fuzz::token_sort_ratio / partial_token_sort_ratio / QRatio and their Cached forms:
+    the reference fuzz tests' inputs (test/tests-fuzz.cpp) paired with each other, then
+    seeded random token strings (every char width, ASCII and, for wider units, Unicode
+    whitespace between tokens, cutoffs 0..101)."""
+    T = "test/tests-fuzz.cpp"
+    metrics = (TOKEN_SORT_RATIO, PARTIAL_TOKEN_SORT_RATIO, QRATIO)
+    lits = fuzz_test_literals()
+    out = []
+    for i, a in enumerate(lits):
+        for b in (lits[i], lits[(i + 1) % len(lits)], lits[(i + 5) % len(lits)]):
+            for m in metrics:
+                out.append(case(m, SIMILARITY, FREE, a, b, cite=T))
+                out.append(case(m, SIMILARITY, CACHED, b, a, 50.0, cite=T))
+    rng = random.Random(seed)
+    spaces = [0x20, 0x09, 0x0A, 0x0D, 0x1F, 0x85, 0xA0, 0x2000, 0x2028, 0x3000]
+    while len(out) < 4000:
+        w = rng.choice([1, 2, 4, 8])
+        letters = [97, 98, 99, 100, 101, 0xC0, 0xFF] + ([300, 4000, 70000] if w == 4 else [300] if w == 2 else [])
+        sp = [c for c in spaces if w > 1 or c < 256]
+
+        def mk():
+            s = []
+            for _ in range(rng.randint(0, 7)):
+                s += [rng.choice(letters) for _ in range(rng.randint(0, 9))]
+                s += [rng.choice(sp) for _ in range(rng.randint(0, 2))]
+            return s
+        a, b = mk(), mk()
+        if rng.random() < 0.3:
+            b = list(a)
+            rng.shuffle(b)
+        cutoff = rng.choice([None, 0.0, 50.0, 80.0, 95.0, 100.0, 101.0])
+        c = case(rng.choice(metrics), SIMILARITY, rng.choice([FREE, CACHED]), a, b, cutoff, w1=w, w2=w)
+        if c is not None:
+            out.append(c)
+    return [c for c in out if c is not None]
+
+
 def main():
     if reference() is None:
         sys.exit("oracle/_ref/librfref.so is missing: run `make -C oracle ref` where the reference checkout exists")
-    which = sys.argv[1:] or ["kat.json", "random.json", "multi.json", "partial.json"]
+    which = sys.argv[1:] or ["kat.json", "random.json", "multi.json", "partial.json", "tokens.json"]
     gens = {"kat.json": kat_cases, "random.json": lambda: random_cases(4000), "multi.json": multi_cases,
-            "partial.json": partial_cases}
+            "partial.json": partial_cases, "tokens.json": token_cases}
     for name, cases in ((n, gens[n]()) for n in which):
         with open(os.path.join(HERE, name), "w") as f:
             json.dump(cases, f, separators=(",", ":"))

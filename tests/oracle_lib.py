@@ -11,6 +11,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 
 LEVENSHTEIN, INDEL, LCSSEQ, OSA, JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO = range(8)
+TOKEN_SORT_RATIO, PARTIAL_TOKEN_SORT_RATIO, QRATIO = 8, 9, 10
+FUZZ_METRICS = (RATIO, PARTIAL_RATIO, TOKEN_SORT_RATIO, PARTIAL_TOKEN_SORT_RATIO, QRATIO)
 DISTANCE, SIMILARITY, NORM_DISTANCE, NORM_SIMILARITY = range(4)
 FREE, CACHED, MULTI = range(3)
 METRIC_NAMES = ["levenshtein", "indel", "lcsseq", "osa", "jaro", "jaro_winkler", "ratio"]
@@ -27,7 +29,7 @@ class Strings(ctypes.Structure):
 
 
 def result_is_int(metric, op):
-    if metric in (JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO):
+    if metric in (JARO, JARO_WINKLER) + FUZZ_METRICS:
         return False
     return op in (DISTANCE, SIMILARITY)
 
@@ -129,7 +131,7 @@ def score(lib_fn, metric, op, form, s1, s2, cutoff=None, weights=(1, 1, 1), pref
     else:
         ci = 0
         if cutoff is None:
-            cf = 1.0 if op in (DISTANCE, NORM_DISTANCE) and metric not in (RATIO, PARTIAL_RATIO) else 0.0
+            cf = 1.0 if op in (DISTANCE, NORM_DISTANCE) and metric not in FUZZ_METRICS else 0.0
         else:
             cf = float(cutoff)
     oi = ctypes.c_int64(0)

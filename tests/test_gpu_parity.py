@@ -27,7 +27,7 @@ def gpu_score(c, a, b):
     return int(v) if R._lib.result_is_int(m, op) else float(v)
 
 
-@pytest.mark.parametrize("fixture", ["kat.json", "random.json", "partial.json"])
+@pytest.mark.parametrize("fixture", ["kat.json", "random.json", "partial.json", "tokens.json"])
 def test_fixtures_per_call(fixture):
     bad = []
     for c in G.load(fixture):
@@ -238,3 +238,112 @@ def test_partial_ratio_api_names():
         exp = oscore(o.rfo_score, R.PARTIAL_RATIO, R.SIMILARITY, FREE, a.encode(), b.encode(), 0.0)
         assert G.same(R.fuzz_partial_ratio(a, b), exp)
         assert G.same(R.CachedPartialRatio(a).similarity(b), exp)
+
+
+def _token_str(rng, w):
+    letters = [97, 98, 99, 100, 0xC0] + ([300, 70000] if w == 4 else [])
+    spaces = [0x20, 0x09, 0x0A] + ([0xA0, 0x2000, 0x3000] if w == 4 else [])
+    s = []
+    for _ in range(rng.randint(0, 6)):
+        s += [rng.choice(letters) for _ in range(rng.randint(0, 8))]
+        s += [rng.choice(spaces) for _ in range(rng.randint(0, 2))]
+    return s
+
+
+def _token_batches(seed, w):
+    """queries and choices for the token scorers: empty and all-whitespace strings,
+    choices that are the queries' tokens reordered with other whitespace"""
+    rng = random.Random(seed)
+    qs = [_token_str(rng, w) for _ in range(17)] + [[], [0x20, 0x09]]
+    cs = []
+    for _ in range(70):
+        if rng.random() < 0.35:
+            toks = [t for t in "".join(chr(x) for x in rng.choice(qs)).split() if t]
+            rng.shuffle(toks)
+            cs.append([ord(ch) for ch in rng.choice([" ", "  ", "\t"]).join(toks)])
+        else:
+            cs.append(_token_str(rng, w))
+    cs += [[], [0x20]]
+    dt = {1: np.uint8, 4: np.uint32}[w]
+    return (R.pack_strings([np.array(x, dtype=dt) for x in qs], w),
+            R.pack_strings([np.array(x, dtype=dt) for x in cs], w))
+
+
+@pytest.mark.parametrize("metric", ["TOKEN_SORT_RATIO", "PARTIAL_TOKEN_SORT_RATIO", "QRATIO"])
+@pytest.mark.parametrize("width", [1, 4])
+def test_cdist_token_scorers_match_oracle(metric, width):
+    """token_sort_ratio, partial_token_sort_ratio and QRatio over batches (host joins,
+    the ratio / partial_ratio kernels, QRatio's empty-string rule), free and cached forms"""
+    m = getattr(R, metric)
+    q, c = _token_batches(41 + width, width)
+    for cut in (0.0, 60.0, 100.0, 101.0):
+        exp = oracle_cdist(m, R.SIMILARITY, q, c, cut)
+        for form in (R.FORM_FREE, R.FORM_CACHED):
+            got = R.cdist(m, R.SIMILARITY, q, c, cut, form=form)
+            bad = np.argwhere(got.view(np.int64) != exp.view(np.int64))
+            assert bad.size == 0, "cut %r form %d mismatch at %r: got %r exp %r" % (
+                cut, form, bad[0], got[tuple(bad[0])], exp[tuple(bad[0])])
+    # CachedX.score_many (rfg_cached_score_many) for one query
+    data, off, w = q
+    s1 = data[off[3]:off[4]]
+    got = R.Cached(m, s1).score_many(R.SIMILARITY, c, 50.0)
+    exp = oracle_cdist(m, R.SIMILARITY, R.pack_strings([s1], w), c, 50.0)[0]
+    assert np.array_equal(got.view(np.int64), exp.view(np.int64))
+
+
+@pytest.mark.parametrize("metric", ["TOKEN_SORT_RATIO", "QRATIO"])
+def test_cdist_token_scorers_device_buffers(metric):
+    """device inputs (downloaded for the joins) and a device result with ld > choices
+    (QRatio's zero fix-up runs as a kernel there)"""
+    import ctypes
+    import torch
+    from rapidfuzz_gb300._lib import Cutoff, Strings, make_params, check
+    m = getattr(R, metric)
+    q, c = _token_batches(77, 1)
+    exp = oracle_cdist(m, R.SIMILARITY, q, c, 0.0)
+    dq = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in q[:2]]
+    dc = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in c[:2]]
+    nq, nc = q[1].size - 1, c[1].size - 1
+    ld = nc + 5
+    out = torch.full((nq, ld), -7.0, dtype=torch.float64, device="cuda")
+    qs = Strings(dq[0].data_ptr(), dq[1].data_ptr(), nq, 1)
+    cs = Strings(dc[0].data_ptr(), dc[1].data_ptr(), nc, 1)
+    p = make_params()
+    torch.cuda.synchronize()
+    check(R.lib().rfg_cdist(m, R.SIMILARITY, R.FORM_CACHED, ctypes.byref(qs), ctypes.byref(cs), ctypes.byref(p),
+                            Cutoff(0, 0.0, 0, 0.0), R.F64, out.data_ptr(), ld, R.DEVICE_INPUTS | R.DEVICE_OUTPUT))
+    check(R.lib().rfg_synchronize())
+    got = out.cpu().numpy()
+    assert np.array_equal(got[:, :nc].view(np.int64), exp.view(np.int64))
+    assert (got[:, nc:] == -7.0).all()
+
+
+def test_token_scorer_api_names():
+    """the reference's names (fuzz.hpp): token_sort_ratio, partial_token_sort_ratio,
+    QRatio, their Cached classes, MultiTokenSortRatio and MultiQRatio"""
+    o = oracle()
+    pairs = (("new york mets", "new york mets"), ("new york mets vs atlanta braves", "atlanta braves vs new york mets"),
+             ("", ""), ("abc", ""), ("  ", "a"), ("fuzzy wuzzy was a bear", "wuzzy fuzzy was a bear"))
+    for a, b in pairs:
+        for m, free, cached in ((R.TOKEN_SORT_RATIO, R.fuzz_token_sort_ratio, R.CachedTokenSortRatio),
+                                (R.PARTIAL_TOKEN_SORT_RATIO, R.fuzz_partial_token_sort_ratio,
+                                 R.CachedPartialTokenSortRatio),
+                                (R.QRATIO, R.fuzz_QRatio, R.CachedQRatio)):
+            exp = oscore(o.rfo_score, m, R.SIMILARITY, FREE, a.encode(), b.encode(), 0.0)
+            assert G.same(free(a, b), exp), (m, a, b)
+            assert G.same(cached(a).similarity(b), exp), (m, a, b)
+    assert R.fuzz_token_sort_ratio("", "") == 100.0 and R.fuzz_QRatio("", "") == 0.0
+    mt = R.experimental.MultiTokenSortRatio(16, 2)
+    mt.insert("  c     b   a        ")
+    mt.insert("b a")
+    r = mt.similarity("a b c")
+    assert r[0] == 100.0 and r[1] == 75.0
+    mq = R.experimental.MultiQRatio(8, 2)
+    mq.insert("")
+    mq.insert("ab")
+    assert list(mq.similarity("ab")[:2]) == [0.0, 100.0]
+    assert list(mq.similarity("")[:2]) == [0.0, 0.0]
+    with pytest.raises(ValueError):
+        R.Multi(R.PARTIAL_TOKEN_SORT_RATIO, 8, 1)
+    with pytest.raises(ValueError):
+        R.score(R.TOKEN_SORT_RATIO, R.DISTANCE, "a", "b")
