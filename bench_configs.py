@@ -12,6 +12,8 @@ cfg4  Jaro-Winkler (prefix_weight 0.1, cutoff 0.85) and fuzz::ratio (cutoff 85) 
       code-point token strings, 1,024 x 1,000,000, dense float64 outputs kept on the device.
 partial  fuzz::partial_ratio (cutoff 80) of 256 token queries against 200,000 token strings
       (uint32, as in cfg4), dense float64 out on the device (the first widening of the path).
+tokens   token_sort_ratio and QRatio (cutoff 80), 256 x 200,000 token strings, host inputs
+      and host results through rfg_cdist (the joins run on the host threads).
 cfg5  serving: device-resident corpora of 10,000,000 DNA strings (len U[10,200]) and
       1,000,000 uint32 token strings; Poisson arrivals (--rate req/s for --duration s), each
       an extractOne (limit 1) or top-10 extract of one query of length U[5,500] with a metric
@@ -166,6 +168,45 @@ def run(args, rank, world, local):
                      "e2e": None, "gpu_launches": steps, "clocks": clk})
     elif args.workload == "cfg5":
         return run_serving(args, R, WL)
+    elif args.workload == "tokens":
+        nq = 256
+        nc = args.nc if args.nc != 4096 else 200000
+        (q, ql) = WL.tokens_u32(seed=43, n=nq)
+        c = WL.tokens_u32_fast(seed=44, n=nc)
+        per = {}
+        clocks = B.ClockSampler()
+        clocks.start()
+        for name, m in (("token_sort_ratio", R.TOKEN_SORT_RATIO), ("QRatio", R.QRATIO)):
+            for _ in range(warmup):
+                out = R.cdist(m, R.SIMILARITY, q, c, 80.0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                out = R.cdist(m, R.SIMILARITY, q, c, 80.0)
+            per[name] = (time.perf_counter() - t0) / steps
+            rows = [0, 100, 255]
+            qrows = (np.concatenate([q[0][q[1][r]:q[1][r + 1]] for r in rows]),
+                     np.concatenate([[0], np.cumsum([q[1][r + 1] - q[1][r] for r in rows])]).astype(np.int64), 4)
+            exp = oracle_cdist(m, R.SIMILARITY, qrows, c, 80.0)
+            assert np.array_equal(out[rows].view(np.int64), exp.view(np.int64)), name + " parity"
+        clk = clocks.stop(torch.cuda.current_device())
+        sub = 8
+        qsub = (q[0][:q[1][sub]], q[1][:sub + 1].copy(), 4)
+        tc0 = time.perf_counter()
+        oracle_cdist(R.TOKEN_SORT_RATIO, R.SIMILARITY, qsub, c, 80.0)
+        tc = time.perf_counter() - tc0
+        t = per["token_sort_ratio"]
+        h2d = int(q[0].nbytes + q[1].nbytes + c[0].nbytes + c[1].nbytes)
+        line.update({"value": nq * nc / t, "unit": "pairs/s", "ms_per_step": t * 1e3, "dtype": "f64",
+                     "config": {"workload": "fuzz::token_sort_ratio cutoff 80 (and QRatio), 256 x %d uint32 token "
+                                            "strings (1-4 tokens of 3-12 units) from host buffers to a host float64 "
+                                            "matrix: host sorted-split joins, upload, ratio kernel, download" % nc,
+                                "ms_per_call": {k: v * 1e3 for k, v in per.items()}},
+                     "cpu_baseline": {"value": sub * nc / tc, "unit": "pairs/s", "cores": os.cpu_count(),
+                                      "kind": "port", "sample": "8 of the 256 queries x all %d choices" % nc},
+                     "e2e": {"value": nq * nc / t, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
+                             "d2h_bytes_per_step": nq * nc * 8},
+                     "gpu_launches": None, "clocks": clk})
     elif args.workload == "partial":
         nq = 256
         nc = args.nc if args.nc != 4096 else 200000

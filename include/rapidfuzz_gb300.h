@@ -63,7 +63,17 @@ typedef enum {
      * sort and QRatio) rfg_multi_*; not on a corpus, a batch or the no-allocation entry. */
     RFG_TOKEN_SORT_RATIO = 8,
     RFG_PARTIAL_TOKEN_SORT_RATIO = 9,
-    RFG_QRATIO = 10
+    RFG_QRATIO = 10,
+    /* the token_set_ratio family (fuzz.hpp:375-690, fuzz_impl.hpp:372-889): token_set_ratio,
+     * partial_token_set_ratio, token_ratio, partial_token_ratio and WRatio with their
+     * Cached forms, scored on the device from the strings, their sorted-split joins and
+     * the joins of their distinct tokens (made on the host).  Only RFG_SIMILARITY and
+     * RFG_F64, through rfg_score_f64, rfg_cached_* and rfg_cdist; no Multi form. */
+    RFG_TOKEN_SET_RATIO = 11,
+    RFG_PARTIAL_TOKEN_SET_RATIO = 12,
+    RFG_TOKEN_RATIO = 13,
+    RFG_PARTIAL_TOKEN_RATIO = 14,
+    RFG_WRATIO = 15
 } rfg_metric;
 
 /* the four result kinds of every metric (rapidfuzz/details/distance.hpp) */

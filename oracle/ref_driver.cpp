@@ -182,6 +182,26 @@ int score(int metric, int op, int form, const void* a, int64_t la, const void* b
             if (op != RFO_SIMILARITY) return -1;
             *of = fuzz::QRatio(s1, s2, cf);
             return 0;
+        case RFO_TOKEN_SET_RATIO:
+            if (op != RFO_SIMILARITY) return -1;
+            *of = fuzz::token_set_ratio(s1, s2, cf);
+            return 0;
+        case RFO_PARTIAL_TOKEN_SET_RATIO:
+            if (op != RFO_SIMILARITY) return -1;
+            *of = fuzz::partial_token_set_ratio(s1, s2, cf);
+            return 0;
+        case RFO_TOKEN_RATIO:
+            if (op != RFO_SIMILARITY) return -1;
+            *of = fuzz::token_ratio(s1, s2, cf);
+            return 0;
+        case RFO_PARTIAL_TOKEN_RATIO:
+            if (op != RFO_SIMILARITY) return -1;
+            *of = fuzz::partial_token_ratio(s1, s2, cf);
+            return 0;
+        case RFO_WRATIO:
+            if (op != RFO_SIMILARITY) return -1;
+            *of = fuzz::WRatio(s1, s2, cf);
+            return 0;
         }
         return -1;
     }
@@ -257,6 +277,36 @@ int score(int metric, int op, int form, const void* a, int64_t la, const void* b
     case RFO_QRATIO: {
         if (op != RFO_SIMILARITY) return -1;
         fuzz::CachedQRatio<C1> sc(s1);
+        *of = sc.similarity(s2, cf);
+        return 0;
+    }
+    case RFO_TOKEN_SET_RATIO: {
+        if (op != RFO_SIMILARITY) return -1;
+        fuzz::CachedTokenSetRatio<C1> sc(s1);
+        *of = sc.similarity(s2, cf);
+        return 0;
+    }
+    case RFO_PARTIAL_TOKEN_SET_RATIO: {
+        if (op != RFO_SIMILARITY) return -1;
+        fuzz::CachedPartialTokenSetRatio<C1> sc(s1);
+        *of = sc.similarity(s2, cf);
+        return 0;
+    }
+    case RFO_TOKEN_RATIO: {
+        if (op != RFO_SIMILARITY) return -1;
+        fuzz::CachedTokenRatio<C1> sc(s1);
+        *of = sc.similarity(s2, cf);
+        return 0;
+    }
+    case RFO_PARTIAL_TOKEN_RATIO: {
+        if (op != RFO_SIMILARITY) return -1;
+        fuzz::CachedPartialTokenRatio<C1> sc(s1);
+        *of = sc.similarity(s2, cf);
+        return 0;
+    }
+    case RFO_WRATIO: {
+        if (op != RFO_SIMILARITY) return -1;
+        fuzz::CachedWRatio<C1> sc(s1);
         *of = sc.similarity(s2, cf);
         return 0;
     }

@@ -953,6 +953,15 @@ int score_with_pm(int metric, int op, int form, const PM& pm, const S1& s1, cons
         *of = token_scorer(metric, s1, s2, cf);
         return 0;
     }
+    case RFO_TOKEN_SET_RATIO:
+    case RFO_PARTIAL_TOKEN_SET_RATIO:
+    case RFO_TOKEN_RATIO:
+    case RFO_PARTIAL_TOKEN_RATIO:
+    case RFO_WRATIO: {
+        if (op != RFO_SIMILARITY) return -1;
+        *of = token_set_family(metric, s1, s2, cf);
+        return 0;
+    }
     case RFO_RATIO: {
         if (op != RFO_SIMILARITY) return -1;
         auto dist = [&](u64 c) { return indel_cached(pm, s1, s2, c); };
@@ -1120,10 +1129,13 @@ bool unit_is_space(u64 c, bool one_byte)
     return false;
 }
 
+using Tokens = std::vector<std::vector<u64>>;
+
+/* sorted_split (common_impl.hpp:162-180): the tokens, sorted */
 template <typename S>
-std::vector<u64> sorted_join(const S& s, bool one_byte)
+Tokens sorted_tokens(const S& s, bool one_byte)
 {
-    std::vector<std::vector<u64>> toks;
+    Tokens toks;
     std::vector<u64> cur;
     for (i64 i = 0; i <= s.n; ++i) {
         if (i == s.n || unit_is_space(s[i], one_byte)) {
@@ -1133,12 +1145,24 @@ std::vector<u64> sorted_join(const S& s, bool one_byte)
         else cur.push_back(s[i]);
     }
     std::sort(toks.begin(), toks.end());
+    return toks;
+}
+
+/* SplittedSentenceView::join (SplittedSentenceView.hpp:71-85) */
+std::vector<u64> join_tokens(const Tokens& toks)
+{
     std::vector<u64> out;
     for (size_t k = 0; k < toks.size(); ++k) {
         if (k) out.push_back(0x20);
         out.insert(out.end(), toks[k].begin(), toks[k].end());
     }
     return out;
+}
+
+template <typename S>
+std::vector<u64> sorted_join(const S& s, bool one_byte)
+{
+    return join_tokens(sorted_tokens(s, one_byte));
 }
 
 /* fuzz::ratio (fuzz_impl.hpp:28-32) */
@@ -1187,6 +1211,155 @@ double token_multi(int metric, const S1& s1, const S2& s2, double cutoff)
     }
     const std::vector<u64> a = sorted_join(s1, sizeof(s1.p[0]) == 1), b = sorted_join(s2, sizeof(s2.p[0]) == 1);
     return multi_ratio(Str<u64>{a.data(), (i64)a.size()}, Str<u64>{b.data(), (i64)b.size()}, cutoff);
+}
+
+/* ------------------------------------------------ token_set_ratio, token_ratio, WRatio
+ * set_decomposition (common_impl.hpp:11-35): both sorted token lists lose adjacent
+ * duplicates, then each token of a is looked up in what is left of b: found tokens form
+ * the intersection (in a's order) and leave b, the others form diff_ab; the rest of b
+ * is diff_ba. */
+struct Decomp {
+    Tokens ab, ba, sect;
+};
+
+Decomp decompose(Tokens a, Tokens b)
+{
+    a.erase(std::unique(a.begin(), a.end()), a.end());
+    b.erase(std::unique(b.begin(), b.end()), b.end());
+    Decomp d;
+    d.ba = b;
+    for (const auto& t : a) {
+        auto it = std::find(d.ba.begin(), d.ba.end(), t);
+        if (it != d.ba.end()) {
+            d.ba.erase(it);
+            d.sect.push_back(t);
+        }
+        else d.ab.push_back(t);
+    }
+    return d;
+}
+
+/* SplittedSentenceView::size (SplittedSentenceView.hpp:56-69): the joined length */
+u64 joined_len(const Tokens& t)
+{
+    if (t.empty()) return 0;
+    u64 n = t.size() - 1;
+    for (const auto& x : t) n += x.size();
+    return n;
+}
+
+/* norm_distance, score_cutoff_to_distance (fuzz_impl.hpp:55-66) */
+double norm_distance_pct(u64 dist, u64 lensum, double cutoff)
+{
+    const double score = lensum > 0 ? 100.0 - 100.0 * (double)dist / (double)lensum : 100.0;
+    return score >= cutoff ? score : 0;
+}
+
+u64 cutoff_to_distance(double cutoff, u64 lensum)
+{
+    return (u64)std::ceil((double)lensum * (1.0 - cutoff / 100));
+}
+
+Str<u64> view(const std::vector<u64>& v) { return Str<u64>{v.data(), (i64)v.size()}; }
+
+/* indel_distance(a, b, cutoff): exact when <= cutoff, else cutoff + 1 */
+u64 indel_dist(const std::vector<u64>& a, const std::vector<u64>& b, u64 cutoff)
+{
+    PM pm;
+    pm.build(view(a));
+    return indel_cached(pm, view(a), view(b), cutoff);
+}
+
+/* the common part of token_set_ratio (fuzz_impl.hpp:372-420) and token_ratio
+ * (fuzz_impl.hpp:518-564); with_sorted adds ratio(tokens_a.join(), tokens_b.join()) */
+double token_set_tail(const Tokens& ta, const Tokens& tb, double cutoff, bool with_sorted)
+{
+    const Decomp d = decompose(ta, tb);
+    if (!d.sect.empty() && (d.ab.empty() || d.ba.empty())) return 100;
+    const std::vector<u64> ab = join_tokens(d.ab), ba = join_tokens(d.ba);
+    const u64 ab_len = ab.size(), ba_len = ba.size(), sect_len = joined_len(d.sect);
+    double result = 0;
+    if (with_sorted) {
+        const std::vector<u64> ja = join_tokens(ta), jb = join_tokens(tb);
+        result = ratio_plain(view(ja), view(jb), cutoff);
+    }
+    const u64 sect_ab_len = sect_len + (sect_len != 0) + ab_len, sect_ba_len = sect_len + (sect_len != 0) + ba_len;
+    const u64 cd = cutoff_to_distance(cutoff, sect_ab_len + sect_ba_len);
+    const u64 dist = indel_dist(ab, ba, cd);
+    if (dist <= cd) {
+        const double nd = norm_distance_pct(dist, sect_ab_len + sect_ba_len, cutoff);
+        result = with_sorted ? std::max(result, nd) : nd;
+    }
+    if (!sect_len) return result;
+    const double r_ab = norm_distance_pct((sect_len != 0) + ab_len, sect_len + sect_ab_len, cutoff);
+    const double r_ba = norm_distance_pct((sect_len != 0) + ba_len, sect_len + sect_ba_len, cutoff);
+    return std::max({result, r_ab, r_ba});
+}
+
+/* partial_token_ratio (fuzz_impl.hpp:704-731) */
+double partial_token_ratio_toks(const Tokens& ta, const Tokens& tb, double cutoff)
+{
+    if (cutoff > 100) return 0;
+    const Decomp d = decompose(ta, tb);
+    if (!d.sect.empty()) return 100;
+    const std::vector<u64> ja = join_tokens(ta), jb = join_tokens(tb);
+    const double result = partial_ratio_score(view(ja), view(jb), cutoff);
+    if (ta.size() == d.ab.size() && tb.size() == d.ba.size()) return result;
+    cutoff = std::max(cutoff, result);
+    const std::vector<u64> ab = join_tokens(d.ab), ba = join_tokens(d.ba);
+    return std::max(result, partial_ratio_score(view(ab), view(ba), cutoff));
+}
+
+/* token_ratio (fuzz_impl.hpp:518-564) */
+double token_ratio_toks(const Tokens& ta, const Tokens& tb, double cutoff)
+{
+    if (cutoff > 100) return 0;
+    return token_set_tail(ta, tb, cutoff, true);
+}
+
+/* token_set_ratio, partial_token_set_ratio, token_ratio, partial_token_ratio, WRatio
+ * (fuzz_impl.hpp:373-889); the Cached forms give the same values */
+template <typename S1, typename S2>
+double token_set_family(int metric, const S1& s1, const S2& s2, double cutoff)
+{
+    if (cutoff > 100) return 0;
+    const bool ob1 = sizeof(s1.p[0]) == 1, ob2 = sizeof(s2.p[0]) == 1;
+    switch (metric) {
+    case RFO_TOKEN_SET_RATIO: {
+        const Tokens ta = sorted_tokens(s1, ob1), tb = sorted_tokens(s2, ob2);
+        if (ta.empty() || tb.empty()) return 0;
+        return token_set_tail(ta, tb, cutoff, false);
+    }
+    case RFO_PARTIAL_TOKEN_SET_RATIO: {
+        const Tokens ta = sorted_tokens(s1, ob1), tb = sorted_tokens(s2, ob2);
+        if (ta.empty() || tb.empty()) return 0;
+        const Decomp d = decompose(ta, tb);
+        if (!d.sect.empty()) return 100;
+        const std::vector<u64> ab = join_tokens(d.ab), ba = join_tokens(d.ba);
+        return partial_ratio_score(view(ab), view(ba), cutoff);
+    }
+    case RFO_TOKEN_RATIO: return token_ratio_toks(sorted_tokens(s1, ob1), sorted_tokens(s2, ob2), cutoff);
+    case RFO_PARTIAL_TOKEN_RATIO:
+        return partial_token_ratio_toks(sorted_tokens(s1, ob1), sorted_tokens(s2, ob2), cutoff);
+    default: break;
+    }
+    /* WRatio (fuzz_impl.hpp:789-822) */
+    const double UNBASE_SCALE = 0.95;
+    const i64 len1 = s1.n, len2 = s2.n;
+    if (!len1 || !len2) return 0;
+    const double len_ratio = len1 > len2 ? (double)len1 / (double)len2 : (double)len2 / (double)len1;
+    double end_ratio = ratio_plain(s1, s2, cutoff);
+    if (len_ratio < 1.5) {
+        cutoff = std::max(cutoff, end_ratio) / UNBASE_SCALE;
+        return std::max(end_ratio, token_ratio_toks(sorted_tokens(s1, ob1), sorted_tokens(s2, ob2), cutoff) *
+                                       UNBASE_SCALE);
+    }
+    const double PARTIAL_SCALE = len_ratio <= 8.0 ? 0.9 : 0.6;
+    cutoff = std::max(cutoff, end_ratio) / PARTIAL_SCALE;
+    end_ratio = std::max(end_ratio, partial_ratio_score(s1, s2, cutoff) * PARTIAL_SCALE);
+    cutoff = std::max(cutoff, end_ratio) / UNBASE_SCALE;
+    return std::max(end_ratio, partial_token_ratio_toks(sorted_tokens(s1, ob1), sorted_tokens(s2, ob2), cutoff) *
+                                   UNBASE_SCALE * PARTIAL_SCALE);
 }
 
 template <typename T>

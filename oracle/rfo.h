@@ -35,7 +35,12 @@ enum {
     RFO_PARTIAL_RATIO = 7,
     RFO_TOKEN_SORT_RATIO = 8,
     RFO_PARTIAL_TOKEN_SORT_RATIO = 9,
-    RFO_QRATIO = 10
+    RFO_QRATIO = 10,
+    RFO_TOKEN_SET_RATIO = 11,
+    RFO_PARTIAL_TOKEN_SET_RATIO = 12,
+    RFO_TOKEN_RATIO = 13,
+    RFO_PARTIAL_TOKEN_RATIO = 14,
+    RFO_WRATIO = 15
 };
 
 /* operations */

@@ -213,7 +213,13 @@ rfg_status check_strings(const rfg_strings* s, const char* what)
 
 /* token_sort_ratio, partial_token_sort_ratio and QRatio: a host front end over the
  * ratio / partial_ratio engine */
-inline bool is_token_metric(int metric) { return metric >= RFG_TOKEN_SORT_RATIO && metric <= RFG_QRATIO; }
+inline bool is_token_metric(int metric)
+{
+    return (metric >= RFG_TOKEN_SORT_RATIO && metric <= RFG_QRATIO) ||
+           (metric >= RFG_TOKEN_SET_RATIO && metric <= RFG_WRATIO);
+}
+/* the family scored on the device from string parts (FAM_TOKEN) */
+inline bool is_token_set_metric(int metric) { return metric >= RFG_TOKEN_SET_RATIO && metric <= RFG_WRATIO; }
 inline int token_base(int metric) { return metric == RFG_PARTIAL_TOKEN_SORT_RATIO ? RFG_PARTIAL_RATIO : RFG_RATIO; }
 
 /* the metrics the engine scores directly (every entry point) */
@@ -244,8 +250,8 @@ rfg_status check_any_metric_op(int metric, int op, int form)
     if (form < RFG_FORM_FREE || form > RFG_FORM_MULTI) return fail(RFG_ERR_INVALID_ARGUMENT, "unknown form %d", form);
     if (op != RFG_SIMILARITY)
         return fail(RFG_ERR_INVALID_ARGUMENT, "token_sort_ratio, partial_token_sort_ratio and QRatio only have a similarity");
-    if (metric == RFG_PARTIAL_TOKEN_SORT_RATIO && form == RFG_FORM_MULTI)
-        return fail(RFG_ERR_INVALID_ARGUMENT, "fuzz::partial_token_sort_ratio has no experimental::Multi form");
+    if ((metric == RFG_PARTIAL_TOKEN_SORT_RATIO || is_token_set_metric(metric)) && form == RFG_FORM_MULTI)
+        return fail(RFG_ERR_INVALID_ARGUMENT, "this fuzz scorer has no experimental::Multi form");
     return RFG_OK;
 }
 
@@ -325,6 +331,9 @@ struct BatchSpec {
     int64_t fixed_maxlen = 0; /* the corpus's longest string */
     /* split the queries into this many contiguous row blocks (host-output pipelining) */
     int row_blocks = 1;
+    /* token_set_ratio family: device part-length arrays of the queries and the choices */
+    const int32_t* qparts = nullptr;
+    const int32_t* cparts = nullptr;
 };
 
 inline bool better_high_of(int op) { return op == RFG_SIMILARITY || op == RFG_NORMALIZED_SIMILARITY; }
@@ -471,7 +480,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
     for (int64_t b = 0; b < nblk; ++b)
         for (int64_t i = pb->rows[b].first; i < pb->rows[b].second; ++i) {
             int k;
-            if (fam == FAM_WF || fam == FAM_NONE || fam == FAM_PARTIAL) k = 4;
+            if (fam == FAM_WF || fam == FAM_NONE || fam == FAM_PARTIAL || fam == FAM_TOKEN) k = 4;
             else {
                 const int wc = word_class(q.len[i]);
                 k = wc == 1 ? 0 : wc == 2 ? 1 : wc == 4 ? 2 : wc == 8 ? 3 : 4;
@@ -586,6 +595,8 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         a.out = spec.out;
         a.out_dtype = spec.out_dtype;
         a.ld = spec.ld;
+        a.qparts = spec.qparts;
+        a.cparts = spec.cparts;
         const bool needs_table = fam != FAM_WF && fam != FAM_NONE;
         a.hcap = (needs_table && c.width > 1 && cls_wide[bk] > 0) ? next_pow2(2 * cls_wide[bk]) : 0;
 
@@ -714,6 +725,10 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
                 per_thread = partial_scratch_words(
                     wmax, std::max<int64_t>(cls_maxlen[bk], spec.fixed_perm ? spec.fixed_maxlen : max_choice_len));
                 break;
+            case FAM_TOKEN:
+                per_thread = tok_scratch_words(
+                    wmax, std::max<int64_t>(cls_maxlen[bk], spec.fixed_perm ? spec.fixed_maxlen : max_choice_len));
+                break;
             default: per_thread = cls_maxlen[bk] + 1;
             }
             a.wmax = wmax;
@@ -821,14 +836,16 @@ rfg_status check_dtype(int metric, int op, int dt)
 rfg_status token_cdist(int metric, int op, int form, const rfg_strings* Q, bool q_dev, const rfg_strings* C,
                        bool c_dev, const rfg_params* p, rfg_cutoff cut, int dt, void* out, int64_t ld, bool dev_out);
 
-/* cdist over host or device batches */
+/* cdist over host or device batches.  qparts / cparts: the device part-length arrays of
+ * the token_set_ratio family (Q and C are then the part concatenations) */
 rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const rfg_strings* C, const rfg_params* p,
-                      rfg_cutoff cut, int dt, void* out, int64_t ld, uint32_t flags)
+                      rfg_cutoff cut, int dt, void* out, int64_t ld, uint32_t flags, const int32_t* qparts = nullptr,
+                      const int32_t* cparts = nullptr)
 {
-    if (is_token_metric(metric))
+    if (is_token_metric(metric) && !qparts)
         return token_cdist(metric, op, form, Q, flags & RFG_DEVICE_INPUTS, C, flags & RFG_DEVICE_INPUTS, p, cut, dt, out,
                            ld, flags & RFG_DEVICE_OUTPUT);
-    RFG_TRY(check_metric_op(metric, op, form));
+    RFG_TRY(qparts ? check_any_metric_op(metric, op, form) : check_metric_op(metric, op, form));
     RFG_TRY(check_strings(Q, "queries"));
     RFG_TRY(check_strings(C, "choices"));
     RFG_TRY(check_dtype(metric, op, dt));
@@ -878,6 +895,8 @@ rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const 
     spec.cf = cut.cutoff_f;
     spec.out_dtype = dt;
     spec.ld = ld;
+    spec.qparts = qparts;
+    spec.cparts = cparts;
     const size_t esz = dtype_size(dt);
     if (flags & RFG_DEVICE_OUTPUT) {
         spec.out = out;
@@ -972,6 +991,26 @@ rfg_status token_cdist(int metric, int op, int form, const rfg_strings* Q, bool 
     RFG_TRY(check_offsets(c.offsets, nc, "choices"));
     if ((!q.data && nq && q.offsets[nq] > q.offsets[0]) || (!c.data && nc && c.offsets[nc] > c.offsets[0]))
         return fail(RFG_ERR_INVALID_ARGUMENT, "string data is NULL");
+    if (is_token_set_metric(metric)) {
+        /* the parts each metric reads: the string (WRatio), S (all but
+         * partial_token_set_ratio), J (the partial forms and WRatio) */
+        const bool orig = metric == RFG_WRATIO, srt = metric != RFG_PARTIAL_TOKEN_SET_RATIO;
+        const bool ddp = metric == RFG_PARTIAL_TOKEN_SET_RATIO || metric == RFG_PARTIAL_TOKEN_RATIO || metric == RFG_WRATIO;
+        std::vector<int32_t> qp, cp;
+        token_parts_set(q.data, q.offsets, nq, q.char_width, orig, srt, ddp, &jq.data, &jq.off, &qp);
+        token_parts_set(c.data, c.offsets, nc, c.char_width, orig, srt, ddp, &jc.data, &jc.off, &cp);
+        q.data = jq.data.data();
+        q.offsets = jq.off.data();
+        c.data = jc.data.data();
+        c.offsets = jc.off.data();
+        DBuf dqp, dcp;
+        RFG_TRY(dqp.alloc(qp.size() * 4));
+        RFG_TRY(dcp.alloc(cp.size() * 4));
+        if (!qp.empty()) RFG_CUDA(cudaMemcpyAsync(dqp.p, qp.data(), qp.size() * 4, cudaMemcpyHostToDevice, g.stream));
+        if (!cp.empty()) RFG_CUDA(cudaMemcpyAsync(dcp.p, cp.data(), cp.size() * 4, cudaMemcpyHostToDevice, g.stream));
+        return cdist_impl(metric, op, form, &q, &c, p, cut, dt, out, ld, dev_out ? RFG_DEVICE_OUTPUT : 0,
+                          dqp.as<int32_t>(), dcp.as<int32_t>());
+    }
     if (metric != RFG_QRATIO) {
         token_sort_join_set(q.data, q.offsets, nq, q.char_width, &jq.data, &jq.off);
         token_sort_join_set(c.data, c.offsets, nc, c.char_width, &jc.data, &jc.off);
@@ -1127,6 +1166,11 @@ rfg_status score_one(int metric, int op, int form, const void* s1, int64_t l1, i
     const ScoreParams sp = to_sp(p);
     RFG_TRY(check_params(metric, sp));
     RFG_TRY(ensure_ctx());
+    if (is_token_set_metric(metric)) { /* host parts, then one pair through the batch path */
+        int64_t o1[2] = {0, l1}, o2[2] = {0, l2};
+        rfg_strings q{s1, o1, 1, w1}, c{s2, o2, 1, w2};
+        return token_cdist(metric, op, form, &q, false, &c, false, p, cut, dt, result, 1, false);
+    }
     std::vector<unsigned char> j1, j2;
     if (is_token_metric(metric)) { /* the front end of token_cdist, for one pair */
         if (metric == RFG_QRATIO && (!l1 || !l2)) {
@@ -1266,7 +1310,8 @@ rfg_status rfg_cached_create(rfg_metric metric, const void* s1, int64_t len1, in
     h->width = width1;
     h->len = len1;
     h->host.assign((const unsigned char*)s1, (const unsigned char*)s1 + len1 * width1);
-    if (is_token_metric(metric) && metric != RFG_QRATIO) { /* the sorted-split join, as CachedTokenSortRatio keeps */
+    if (metric == RFG_TOKEN_SORT_RATIO || metric == RFG_PARTIAL_TOKEN_SORT_RATIO) { /* the sorted-split join, as
+                                                                                      CachedTokenSortRatio keeps */
         std::vector<unsigned char> j;
         len1 = h->len = token_sort_join(s1, len1, width1, &j);
         h->host.assign(j.begin(), j.begin() + len1 * width1);
@@ -1368,6 +1413,12 @@ rfg_status rfg_cached_score_f64(rfg_cached h, rfg_op op, const void* s2, int64_t
     const void* t2 = s2;
     int64_t n2 = len2;
     std::vector<unsigned char> j2;
+    if (is_token_set_metric(metric)) {
+        int64_t qo[2] = {0, h->len}, co[2] = {0, len2};
+        rfg_strings q{h->host.data(), qo, 1, h->width}, c{s2, co, 1, width2};
+        return token_cdist(metric, op, RFG_FORM_CACHED, &q, false, &c, false, &h->params,
+                           rfg_cutoff{0, score_cutoff, 0, score_hint}, RFG_F64, result, 1, false);
+    }
     if (is_token_metric(metric)) { /* CachedTokenSortRatio / CachedPartialTokenSortRatio / CachedQRatio */
         if (metric == RFG_QRATIO && (!h->len || !len2)) {
             *result = 0.0;

@@ -35,9 +35,12 @@
 /* double-precision tails of the chains: kept out of line so the integer launches never
  * evaluate them speculatively (the FP64 pipe is a small fraction of the INT32 rate) */
 #define RFG_COLD static __host__ __device__ __noinline__
+/* large device routines called from several places: one out-of-line copy each */
+#define RFG_NOINL __host__ __device__ __noinline__
 #else
 #define RFG_HD inline
 #define RFG_COLD static inline
+#define RFG_NOINL inline
 #endif
 
 namespace rfg {
@@ -167,12 +170,26 @@ RFG_HD double dmax(double a, double b) { return (a < b) ? b : a; }
 
 /* ----------------------------------------------------------- metric/op enums */
 
-enum Metric { LEVENSHTEIN = 0, INDEL = 1, LCSSEQ = 2, OSA = 3, JARO = 4, JARO_WINKLER = 5, RATIO = 6, PARTIAL_RATIO = 7 };
+enum Metric {
+    LEVENSHTEIN = 0,
+    INDEL = 1,
+    LCSSEQ = 2,
+    OSA = 3,
+    JARO = 4,
+    JARO_WINKLER = 5,
+    RATIO = 6,
+    PARTIAL_RATIO = 7,
+    TOKEN_SET_RATIO = 11,
+    PARTIAL_TOKEN_SET_RATIO = 12,
+    TOKEN_RATIO = 13,
+    PARTIAL_TOKEN_RATIO = 14,
+    WRATIO = 15
+};
 enum Op { DISTANCE = 0, SIMILARITY = 1, NORM_DISTANCE = 2, NORM_SIMILARITY = 3 };
 enum Form { FORM_FREE = 0, FORM_CACHED = 1, FORM_MULTI = 2 };
 
 /* bit-parallel core family a (metric, weights) pair runs on */
-enum Family { FAM_LEV = 0, FAM_LCS = 1, FAM_OSA = 2, FAM_JARO = 3, FAM_WF = 4, FAM_NONE = 5, FAM_PARTIAL = 6 };
+enum Family { FAM_LEV = 0, FAM_LCS = 1, FAM_OSA = 2, FAM_JARO = 3, FAM_WF = 4, FAM_NONE = 5, FAM_PARTIAL = 6, FAM_TOKEN = 7 };
 
 struct ScoreParams {
     i64 ins, del, rep;     /* Levenshtein weights */
@@ -1085,6 +1102,11 @@ RFG_HD int metric_family(int metric, int form, const ScoreParams& p)
     case RATIO: return FAM_LCS;
     case OSA: return FAM_OSA;
     case PARTIAL_RATIO: return FAM_PARTIAL;
+    case TOKEN_SET_RATIO:
+    case PARTIAL_TOKEN_SET_RATIO:
+    case TOKEN_RATIO:
+    case PARTIAL_TOKEN_RATIO:
+    case WRATIO: return FAM_TOKEN;
     default: return FAM_JARO;
     }
 }
@@ -1936,6 +1958,317 @@ RFG_HD double partial_ratio_dev(const PMW& pm, int W, int m, const TXT& c, int n
         if (score2 > score) return score2;
     }
     return score;
+}
+
+/* ------------------------------------------------ token_set_ratio family
+ * token_set_ratio, partial_token_set_ratio, token_ratio, partial_token_ratio and WRatio
+ * (fuzz_impl.hpp:372-889).  A string of these metrics arrives as the concatenation of up
+ * to three parts -- the string itself (WRatio), its sorted-split join S (tokens sorted,
+ * repeats kept) and the join J of its deduplicated tokens -- with the part lengths beside
+ * it; PMShift / TextSlice views give each part's pattern table and text, so the query's
+ * table is built once.  set_decomposition (common_impl.hpp:11-35) is a merge of the two
+ * sorted token streams of the S parts that skips repeats; the intersection and the
+ * differences are never written out:
+ *   - diff_ab.join() is a subsequence of q's S part (the kept tokens and one separator
+ *     before each kept token but the first), so its LCS with any text is the LCS of S
+ *     under a pattern table masked to those positions (a unit that matches nothing
+ *     changes no LCS);
+ *   - diff_ba.join() is the subsequence of c's S part walked with the kept-token bits,
+ *     the other units are left out of the recurrence.
+ * Tokens hold no U+0020 and the joins hold exactly one U+0020 between tokens. */
+
+/* the tokens of a join part [pos, end) of a unit accessor */
+template <typename R>
+struct TokWalk {
+    const R* r;
+    int pos, end;
+    int a, len, idx; /* current token [a, a + len), its index in the part */
+    RFG_HD bool next()
+    {
+        if (pos >= end) return false;
+        a = pos;
+        while (pos < end && (*r)[pos] != 0x20) ++pos;
+        len = pos - a;
+        ++pos;
+        ++idx;
+        return true;
+    }
+};
+
+/* lexicographic order of two tokens by code unit (unsigned) */
+template <typename R1, typename R2>
+RFG_HD int tok_cmp(const R1& x, int a, int la, const R2& y, int b, int lb)
+{
+    const int n = la < lb ? la : lb;
+    for (int k = 0; k < n; ++k) {
+        const u64 p = x[a + k], q = y[b + k];
+        if (p != q) return p < q ? -1 : 1;
+    }
+    return la < lb ? -1 : (la > lb ? 1 : 0);
+}
+
+/* the distinct tokens of a sorted join, in order (SplittedSentenceView::dedupe,
+ * SplittedSentenceView.hpp:48-54); total counts every token walked */
+template <typename R>
+struct UniqWalk {
+    TokWalk<R> w;
+    int pa, pl, total;
+    RFG_HD bool next()
+    {
+        while (w.next()) {
+            ++total;
+            if (total > 1 && tok_cmp(*w.r, pa, pl, *w.r, w.a, w.len) == 0) continue;
+            pa = w.a;
+            pl = w.len;
+            return true;
+        }
+        return false;
+    }
+};
+
+struct TokSplit {
+    int sect_len, ab_len, ba_len; /* joined lengths of the intersection and the differences */
+    int sect_n, ab_n, ba_n;       /* their token counts */
+    int na, nb;                   /* token counts before deduplication (word_count) */
+};
+
+RFG_HD void set_bits(u64* k, int lo, int hi)
+{
+    for (int i = lo; i < hi;) {
+        const int w = i >> 6, b = i & 63, n = (hi - i) < (64 - b) ? (hi - i) : (64 - b);
+        k[w] |= low_mask(n) << b;
+        i += n;
+    }
+}
+
+/* set_decomposition of q's part [qa, qa + qn) and c's part [ca, ca + cn) (S or J parts).
+ * kq (kqw words, may be null): bits of q's part in diff_ab.join(); kc (kcw words, may be
+ * null): one bit per token of c's part (repeats included) that is in diff_ba. */
+template <typename RQ, typename RC>
+RFG_HD TokSplit tok_split(const RQ& q, int qa, int qn, const RC& c, int ca, int cn, u64* kq, int kqw, u64* kc,
+                          int kcw)
+{
+    TokSplit r{0, 0, 0, 0, 0, 0, 0, 0};
+    for (int w = 0; kq && w < kqw; ++w) kq[w] = 0;
+    for (int w = 0; kc && w < kcw; ++w) kc[w] = 0;
+    UniqWalk<RQ> A{TokWalk<RQ>{&q, qa, qa + qn, 0, 0, -1}, 0, 0, 0};
+    UniqWalk<RC> B{TokWalk<RC>{&c, ca, ca + cn, 0, 0, -1}, 0, 0, 0};
+    bool ha = A.next(), hb = B.next();
+    while (ha || hb) {
+        const int cmp = !ha ? 1 : !hb ? -1 : tok_cmp(q, A.w.a, A.w.len, c, B.w.a, B.w.len);
+        if (cmp == 0) {
+            r.sect_len += A.w.len + (r.sect_n > 0);
+            ++r.sect_n;
+            ha = A.next();
+            hb = B.next();
+        }
+        else if (cmp < 0) {
+            if (kq) set_bits(kq, A.w.a - qa - (r.ab_n > 0), A.w.a - qa + A.w.len);
+            r.ab_len += A.w.len + (r.ab_n > 0);
+            ++r.ab_n;
+            ha = A.next();
+        }
+        else {
+            if (kc) kc[B.w.idx >> 6] |= 1ull << (B.w.idx & 63);
+            r.ba_len += B.w.len + (r.ba_n > 0);
+            ++r.ba_n;
+            hb = B.next();
+        }
+    }
+    r.na = A.total;
+    r.nb = B.total;
+    return r;
+}
+
+/* one step of Hyyro's LCS bit vector over W words */
+template <typename PMW>
+RFG_HD void lcs_step(const PMW& pm, int W, u64 c, u64* S)
+{
+    u32 carry = 0;
+    for (int w = 0; w < W; ++w) {
+        const u64 X = pm(c, w), sv = S[w], u = sv & X;
+        const u64 x = add_carry(sv, u, carry, &carry);
+        S[w] = x | (sv - u);
+    }
+}
+
+/* a pattern table restricted to the positions of a mask */
+template <typename PMW>
+struct PMMask {
+    const PMW* pm;
+    const u64* k;
+    RFG_HD u64 operator()(u64 c, int w) const { return (*pm)(c, w) & k[w]; }
+};
+
+/* One pass over c's S part (rows t[ca, ca + cn)): SA (may be null) runs the LCS of q's
+ * whole S part (table pms, W words), SB the LCS of diff_ab.join() (table pms masked by
+ * kq) with diff_ba.join() (the tokens whose kc bit is set, one separator between them). */
+template <typename PMW, typename TXT>
+RFG_HD void tok_lcs(const PMW& pms, int W, const u64* kq, const TXT& t, int ca, int cn, const u64* kc, u64* SA,
+                    u64* SB)
+{
+    for (int w = 0; w < W; ++w) {
+        if (SA) SA[w] = ~0ull;
+        if (SB) SB[w] = ~0ull;
+    }
+    const PMMask<PMW> pmk{&pms, kq};
+    int ti = 0;
+    bool kept = SB && (kc[0] & 1), seen = false;
+    for (int j = 0; j < cn; ++j) {
+        const u64 ch = t[ca + j];
+        if (SA) lcs_step(pms, W, ch, SA);
+        if (!SB) continue;
+        if (ch == 0x20) {
+            ++ti;
+            kept = (kc[ti >> 6] >> (ti & 63)) & 1;
+            if (kept && seen) lcs_step(pmk, W, 0x20, SB);
+            continue;
+        }
+        if (kept) {
+            lcs_step(pmk, W, ch, SB);
+            seen = true;
+        }
+    }
+}
+
+/* norm_distance, score_cutoff_to_distance (fuzz_impl.hpp:55-66) */
+RFG_HD double norm_distance_pct(u64 dist, u64 lensum, double cutoff)
+{
+    const double score = lensum > 0 ? dsub(100.0, ddiv(dmul(100.0, (double)dist), (double)lensum)) : 100.0;
+    return score >= cutoff ? score : 0.0;
+}
+
+RFG_HD u64 cutoff_to_distance(double cutoff, u64 lensum)
+{
+    return (u64)dceil(dmul((double)lensum, dsub(1.0, ddiv(cutoff, 100.0))));
+}
+
+/* one pair of the family: q's table over its whole concatenation (W words), q's units,
+ * c's rows (table keys) and units, and the part lengths (original, S, J) of both */
+template <typename PMW, typename RQ, typename TXT, typename RC>
+struct TokPair {
+    typedef PMW PMType;
+    typedef TXT TxtType;
+    const PMW* pm;
+    int W;
+    const RQ* q;
+    const TXT* t;
+    const RC* c;
+    int q0, qs, qj, c0, cs, cj;
+};
+
+RFG_HD int words_of(int L) { return (L + 63) >> 6; }
+
+/* per-thread scratch (words) of a pair whose concatenations are at most L units with a
+ * W-word table: kq, SA, SB (W each), kc (one bit per token), then partial_ratio's state
+ * words and window slots */
+RFG_HD i64 tok_scratch_words(int W, i64 L) { return 3 * (i64)W + (L + 1) / 128 + 1 + W + 1 + (5 * L + 3) / 2; }
+
+/* token_set_ratio (with_sorted = false; fuzz_impl.hpp:372-420, the empty-token exit in the
+ * caller) and token_ratio (with_sorted = true; fuzz_impl.hpp:518-564) over the S parts */
+template <typename P>
+RFG_NOINL double token_set_dev(const P& p, double cutoff, bool with_sorted, u64* st)
+{
+    if (cutoff > 100) return 0.0;
+    const int qa = p.q0, ca = p.c0, Ws = words_of(p.qs), kcw = (p.cs + 1) / 128 + 1;
+    u64* kq = st;
+    u64* kc = st + Ws;
+    u64* SA = kc + kcw;
+    u64* SB = SA + Ws;
+    const TokSplit r = tok_split(*p.q, qa, p.qs, *p.c, ca, p.cs, kq, Ws, kc, kcw);
+    if (r.sect_n > 0 && (r.ab_n == 0 || r.ba_n == 0)) return 100.0;
+    const bool needB = r.ab_n > 0 && r.ba_n > 0;
+    u64 lcsA = 0, lcsB = 0;
+    if (Ws && (with_sorted || needB)) {
+        const PMShift<typename P::PMType> pms{p.pm, p.W, qa, p.qs};
+        tok_lcs(pms, Ws, kq, *p.t, ca, p.cs, kc, with_sorted ? SA : nullptr, needB ? SB : nullptr);
+        if (with_sorted) lcsA = lcs_count(SA, Ws, p.qs);
+        if (needB) lcsB = lcs_count(SB, Ws, p.qs);
+    }
+    double result = with_sorted ? ratio_from_lcs((u64)p.qs, (u64)p.cs, lcsA, cutoff) : 0.0;
+    const u64 ab = (u64)r.ab_len, ba = (u64)r.ba_len, sect = (u64)r.sect_len;
+    const u64 sab = sect + (sect != 0) + ab, sba = sect + (sect != 0) + ba;
+    const u64 cd = cutoff_to_distance(cutoff, sab + sba);
+    const u64 dist = ab + ba - 2 * lcsB;
+    if (dist <= cd) {
+        const double nd = norm_distance_pct(dist, sab + sba, cutoff);
+        result = with_sorted ? dmax(result, nd) : nd;
+    }
+    if (!sect) return result;
+    const double r_ab = norm_distance_pct((sect != 0) + ab, sect + sab, cutoff);
+    const double r_ba = norm_distance_pct((sect != 0) + ba, sect + sba, cutoff);
+    return dmax(dmax(result, r_ab), r_ba);
+}
+
+/* partial_ratio of q's part [qa, qa + qm) with c's part [ca, ca + cn) */
+template <typename P>
+RFG_NOINL double tok_partial(const P& p, int qa, int qm, int ca, int cn, double cutoff, u64* st)
+{
+    const PMShift<typename P::PMType> pv{p.pm, p.W, qa, qm};
+    const TextSlice<typename P::TxtType> tv{p.t, ca};
+    return partial_ratio_dev(pv, words_of(qm), qm, tv, cn, cutoff, st, (u32*)(st + p.W + 1));
+}
+
+/* partial_token_ratio (fuzz_impl.hpp:704-731): partial_ratio of the S parts, then of the
+ * J parts (diff_ab / diff_ba are every distinct token when the intersection is empty)
+ * unless neither side had repeats */
+template <typename P>
+RFG_HD double partial_token_ratio_dev(const P& p, double cutoff, u64* st)
+{
+    if (cutoff > 100) return 0.0;
+    const TokSplit r = tok_split(*p.q, p.q0, p.qs, *p.c, p.c0, p.cs, (u64*)nullptr, 0, (u64*)nullptr, 0);
+    if (r.sect_n) return 100.0;
+    const double result = tok_partial(p, p.q0, p.qs, p.c0, p.cs, cutoff, st);
+    if (r.na == r.ab_n && r.nb == r.ba_n) return result;
+    return dmax(result, tok_partial(p, p.q0 + p.qs, p.qj, p.c0 + p.cs, p.cj, dmax(cutoff, result), st));
+}
+
+/* WRatio / CachedWRatio::similarity (fuzz_impl.hpp:789-822, 842-879) */
+template <typename P>
+RFG_HD double wratio_dev(const P& p, double cutoff, u64* st)
+{
+    const double UNBASE_SCALE = 0.95;
+    if (cutoff > 100) return 0.0;
+    const int len1 = p.q0, len2 = p.c0;
+    if (!len1 || !len2) return 0.0;
+    const double len_ratio = len1 > len2 ? ddiv((double)len1, (double)len2) : ddiv((double)len2, (double)len1);
+    /* ratio of the original strings */
+    const PMShift<typename P::PMType> pv{p.pm, p.W, 0, len1};
+    const TextSlice<typename P::TxtType> tv{p.t, 0};
+    lcs_stream(pv, words_of(len1), tv, len2, st, [](int) {});
+    double end_ratio = ratio_from_lcs((u64)len1, (u64)len2, lcs_count(st, words_of(len1), len1), cutoff);
+    if (len_ratio < 1.5) {
+        cutoff = ddiv(dmax(cutoff, end_ratio), UNBASE_SCALE);
+        return dmax(end_ratio, dmul(token_set_dev(p, cutoff, true, st), UNBASE_SCALE));
+    }
+    const double PARTIAL_SCALE = len_ratio <= 8.0 ? 0.9 : 0.6;
+    cutoff = ddiv(dmax(cutoff, end_ratio), PARTIAL_SCALE);
+    end_ratio = dmax(end_ratio, dmul(tok_partial(p, 0, len1, 0, len2, cutoff, st), PARTIAL_SCALE));
+    cutoff = ddiv(dmax(cutoff, end_ratio), UNBASE_SCALE);
+    return dmax(end_ratio, dmul(dmul(partial_token_ratio_dev(p, cutoff, st), UNBASE_SCALE), PARTIAL_SCALE));
+}
+
+/* one pair of token_set_ratio / partial_token_set_ratio / token_ratio /
+ * partial_token_ratio / WRatio (free and Cached forms give the same values) */
+template <typename P>
+RFG_HD double token_family_dev(int metric, const P& p, double cutoff, u64* st)
+{
+    if (cutoff > 100) return 0.0;
+    switch (metric) {
+    case TOKEN_SET_RATIO:
+        if (!p.qs || !p.cs) return 0.0; /* no tokens on a side (fuzz_impl.hpp:379) */
+        return token_set_dev(p, cutoff, false, st);
+    case PARTIAL_TOKEN_SET_RATIO: { /* fuzz_impl.hpp:460-477, on the J parts */
+        if (!p.qj || !p.cj) return 0.0;
+        const int qa = p.q0 + p.qs, ca = p.c0 + p.cs;
+        const TokSplit r = tok_split(*p.q, qa, p.qj, *p.c, ca, p.cj, (u64*)nullptr, 0, (u64*)nullptr, 0);
+        if (r.sect_n) return 100.0;
+        return tok_partial(p, qa, p.qj, ca, p.cj, cutoff, st);
+    }
+    case TOKEN_RATIO: return token_set_dev(p, cutoff, true, st);
+    case PARTIAL_TOKEN_RATIO: return partial_token_ratio_dev(p, cutoff, st);
+    default: return wratio_dev(p, cutoff, st);
+    }
 }
 
 /* Per-query tables of the Jaro chains (free / Cached forms): everything that depends

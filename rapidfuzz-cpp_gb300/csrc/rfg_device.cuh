@@ -82,6 +82,10 @@ struct KParams {
      * loads that do not wait for perm); null when the batch brings its own order */
     const int64_t* poff;
     const int32_t* plen;
+    /* token_set_ratio family: part lengths (original, sorted join, deduplicated join) of
+     * every query / choice string, three int32 each */
+    const int32_t* qparts;
+    const int32_t* cparts;
 };
 
 /* ----------------------------------------------------------------- helpers */
@@ -181,7 +185,7 @@ __device__ __forceinline__ void store_result(const KParams& a, int64_t q, int64_
 
 __device__ __forceinline__ bool result_is_int(int metric, int op)
 {
-    if (metric == JARO || metric == JARO_WINKLER || metric == RATIO || metric == PARTIAL_RATIO) return false;
+    if (metric == JARO || metric == JARO_WINKLER || metric >= RATIO) return false;
     return op == DISTANCE || op == SIMILARITY;
 }
 
@@ -774,6 +778,18 @@ __device__ __forceinline__ void score_pair_generic(const KParams& a, const u64* 
     if (FAM == FAM_PARTIAL) {
         /* fuzz::partial_ratio: W + 1 state words, then the window bookkeeping */
         vf = partial_ratio_dev(pm, W, m, txt, n, s.cf, st, (u32*)(st + W + 1));
+        emit(a, qi, ci, 0, vf, false, s.ci, s.cf, tl);
+        return;
+    }
+    if (FAM == FAM_TOKEN) {
+        /* the token_set_ratio family over the parts of both concatenations */
+        const int32_t* qp = a.qparts + 3 * qi;
+        const int32_t* cp = a.cparts + 3 * ci;
+        const RawQuery q{qb, a.q.width};
+        const RawText<CT> c{s2};
+        typedef TokPair<PMRowsRT, RawQuery, decltype(txt), RawText<CT>> Pair;
+        const Pair p{&pm, W, &q, &txt, &c, qp[0], qp[1], qp[2], __ldg(cp), __ldg(cp + 1), __ldg(cp + 2)};
+        vf = token_family_dev(a.metric, p, s.cf, st);
         emit(a, qi, ci, 0, vf, false, s.ci, s.cf, tl);
         return;
     }

@@ -90,6 +90,60 @@ void join_set(const T* data, const int64_t* off, int64_t n, std::vector<unsigned
     });
 }
 
+/* [s][S][J] parts of one string into out (room for 3 n units); lens gets the three lengths */
+template <typename T>
+int64_t parts_into(const T* s, int64_t n, bool orig, bool sorted, bool dedup, T* out, Tokens& tok, int32_t* lens)
+{
+    int64_t w = 0;
+    lens[0] = lens[1] = lens[2] = 0;
+    if (orig) {
+        for (int64_t i = 0; i < n; ++i) out[w++] = s[i];
+        lens[0] = (int32_t)n;
+    }
+    if (!sorted && !dedup) return w;
+    const int64_t ls = join_into(s, n, out + w, tok); /* tok: the sorted tokens */
+    if (sorted) {
+        lens[1] = (int32_t)ls;
+        w += ls;
+    }
+    if (dedup) {
+        int64_t wj = 0;
+        for (size_t k = 0; k < tok.size(); ++k) {
+            if (k && std::equal(s + tok[k].first, s + tok[k].second, s + tok[k - 1].first, s + tok[k - 1].second))
+                continue;
+            if (wj) out[w + wj++] = (T)0x20;
+            for (int64_t i = tok[k].first; i < tok[k].second; ++i) out[w + wj++] = s[i];
+        }
+        lens[2] = (int32_t)wj;
+        w += wj;
+    }
+    return w;
+}
+
+template <typename T>
+void parts_set(const T* data, const int64_t* off, int64_t n, bool orig, bool sorted, bool dedup,
+               std::vector<unsigned char>* od, std::vector<int64_t>* oo, std::vector<int32_t>* parts)
+{
+    const int64_t base = n ? off[0] : 0, total = n ? off[n] - base : 0;
+    std::vector<T> tmp((size_t)(3 * total));
+    std::vector<int64_t> jl((size_t)n);
+    parts->assign((size_t)(3 * n), 0);
+    parallel_ranges(n, 4096, [&](int64_t a, int64_t b) {
+        Tokens tok;
+        for (int64_t i = a; i < b; ++i)
+            jl[i] = parts_into(data + off[i], off[i + 1] - off[i], orig, sorted, dedup, tmp.data() + 3 * (off[i] - base),
+                               tok, parts->data() + 3 * i);
+    });
+    oo->assign((size_t)n + 1, 0);
+    for (int64_t i = 0; i < n; ++i) (*oo)[i + 1] = (*oo)[i] + jl[i];
+    od->assign((size_t)(*oo)[n] * sizeof(T) + 16, 0);
+    T* dst = (T*)od->data();
+    parallel_ranges(n, 16384, [&](int64_t a, int64_t b) {
+        for (int64_t i = a; i < b; ++i)
+            if (jl[i]) memcpy(dst + (*oo)[i], tmp.data() + 3 * (off[i] - base), (size_t)jl[i] * sizeof(T));
+    });
+}
+
 template <typename T>
 int64_t join_one(const void* s, int64_t len, std::vector<unsigned char>* out)
 {
@@ -99,6 +153,17 @@ int64_t join_one(const void* s, int64_t len, std::vector<unsigned char>* out)
 }
 
 } // namespace
+
+void token_parts_set(const void* data, const int64_t* off, int64_t n, int width, bool orig, bool sorted, bool dedup,
+                     std::vector<unsigned char>* out_data, std::vector<int64_t>* out_off, std::vector<int32_t>* parts)
+{
+    switch (width) {
+    case 1: parts_set((const uint8_t*)data, off, n, orig, sorted, dedup, out_data, out_off, parts); break;
+    case 2: parts_set((const uint16_t*)data, off, n, orig, sorted, dedup, out_data, out_off, parts); break;
+    case 4: parts_set((const uint32_t*)data, off, n, orig, sorted, dedup, out_data, out_off, parts); break;
+    default: parts_set((const uint64_t*)data, off, n, orig, sorted, dedup, out_data, out_off, parts); break;
+    }
+}
 
 int64_t token_sort_join(const void* s, int64_t len, int width, std::vector<unsigned char>* out)
 {

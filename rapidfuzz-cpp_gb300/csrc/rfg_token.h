@@ -20,4 +20,11 @@ int64_t token_sort_join(const void* s, int64_t len, int width, std::vector<unsig
 void token_sort_join_set(const void* data, const int64_t* off, int64_t n, int width,
                          std::vector<unsigned char>* out_data, std::vector<int64_t>* out_off);
 
+/* the token_set_ratio family: per string the concatenation of the parts asked for -- the
+ * string itself, its sorted-split join S, the join J of its deduplicated tokens
+ * (SplittedSentenceView::dedupe, SplittedSentenceView.hpp:48-54) -- and the three part
+ * lengths (0 for a part not asked for), three int32 per string */
+void token_parts_set(const void* data, const int64_t* off, int64_t n, int width, bool orig, bool sorted, bool dedup,
+                     std::vector<unsigned char>* out_data, std::vector<int64_t>* out_off, std::vector<int32_t>* parts);
+
 } // namespace rfg

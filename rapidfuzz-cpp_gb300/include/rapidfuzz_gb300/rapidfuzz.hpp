@@ -12,9 +12,9 @@
  *   Cached* scorers  same files (CachedLevenshtein Levenshtein.hpp:421-482, ...)
  *   Multi* scorers   experimental::Multi*<MaxLen> (Levenshtein.hpp:297-419, ...)
  *   fuzz::ratio      rapidfuzz/fuzz.hpp:44-126 (and CachedRatio, experimental::MultiRatio)
- *   fuzz::partial_ratio, token_sort_ratio, partial_token_sort_ratio, QRatio
- *                    rapidfuzz/fuzz.hpp:128-373, 692-804 (Cached*, MultiTokenSortRatio,
- *                    MultiQRatio)
+ *   fuzz::partial_ratio, token_sort_ratio, partial_token_sort_ratio, token_set_ratio,
+ *   partial_token_set_ratio, token_ratio, partial_token_ratio, WRatio, QRatio
+ *                    rapidfuzz/fuzz.hpp:128-804 (Cached*, MultiTokenSortRatio, MultiQRatio)
  * Exceptions: std::invalid_argument where the reference throws it; std::runtime_error
  * for device failures (the reference has none).
  */
@@ -542,6 +542,13 @@ struct CachedPartialRatio : rapidfuzz_gb300::detail::CachedScorer {
 RFG_FUZZ_FREE(token_sort_ratio, RFG_TOKEN_SORT_RATIO)
 RFG_FUZZ_FREE(partial_token_sort_ratio, RFG_PARTIAL_TOKEN_SORT_RATIO)
 RFG_FUZZ_FREE(QRatio, RFG_QRATIO)
+/* fuzz.hpp:375-690: token_set_ratio, partial_token_set_ratio, token_ratio,
+ * partial_token_ratio, WRatio */
+RFG_FUZZ_FREE(token_set_ratio, RFG_TOKEN_SET_RATIO)
+RFG_FUZZ_FREE(partial_token_set_ratio, RFG_PARTIAL_TOKEN_SET_RATIO)
+RFG_FUZZ_FREE(token_ratio, RFG_TOKEN_RATIO)
+RFG_FUZZ_FREE(partial_token_ratio, RFG_PARTIAL_TOKEN_RATIO)
+RFG_FUZZ_FREE(WRatio, RFG_WRATIO)
 #undef RFG_FUZZ_FREE
 
 /* CachedTokenSortRatio (fuzz.hpp:282-305), CachedPartialTokenSortRatio (fuzz.hpp:342-366),
@@ -574,6 +581,11 @@ RFG_FUZZ_FREE(QRatio, RFG_QRATIO)
 RFG_FUZZ_CACHED(CachedTokenSortRatio, RFG_TOKEN_SORT_RATIO)
 RFG_FUZZ_CACHED(CachedPartialTokenSortRatio, RFG_PARTIAL_TOKEN_SORT_RATIO)
 RFG_FUZZ_CACHED(CachedQRatio, RFG_QRATIO)
+RFG_FUZZ_CACHED(CachedTokenSetRatio, RFG_TOKEN_SET_RATIO)
+RFG_FUZZ_CACHED(CachedPartialTokenSetRatio, RFG_PARTIAL_TOKEN_SET_RATIO)
+RFG_FUZZ_CACHED(CachedTokenRatio, RFG_TOKEN_RATIO)
+RFG_FUZZ_CACHED(CachedPartialTokenRatio, RFG_PARTIAL_TOKEN_RATIO)
+RFG_FUZZ_CACHED(CachedWRatio, RFG_WRATIO)
 #undef RFG_FUZZ_CACHED
 
 #if __cplusplus >= 201703L
@@ -586,6 +598,15 @@ explicit CachedPartialTokenSortRatio(const Sentence1&)
 template <typename Sentence1>
 explicit CachedQRatio(const Sentence1&)
     -> CachedQRatio<typename std::decay<decltype(*std::begin(std::declval<Sentence1>()))>::type>;
+#define RFG_FUZZ_GUIDE(NAME)                                                                                       \
+    template <typename Sentence1>                                                                                  \
+    explicit NAME(const Sentence1&)->NAME<typename std::decay<decltype(*std::begin(std::declval<Sentence1>()))>::type>;
+RFG_FUZZ_GUIDE(CachedTokenSetRatio)
+RFG_FUZZ_GUIDE(CachedPartialTokenSetRatio)
+RFG_FUZZ_GUIDE(CachedTokenRatio)
+RFG_FUZZ_GUIDE(CachedPartialTokenRatio)
+RFG_FUZZ_GUIDE(CachedWRatio)
+#undef RFG_FUZZ_GUIDE
 #endif
 
 } // namespace fuzz

@@ -2,7 +2,8 @@
 (rapidfuzz/distance/*.hpp, rapidfuzz/fuzz.hpp)."""
 from ._lib import (DISTANCE, SIMILARITY, NORMALIZED_DISTANCE, NORMALIZED_SIMILARITY, LEVENSHTEIN, INDEL, LCSSEQ,
                    OSA, JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO, TOKEN_SORT_RATIO, PARTIAL_TOKEN_SORT_RATIO,
-                   QRATIO, Cached, Multi, score)
+                   QRATIO, TOKEN_SET_RATIO, PARTIAL_TOKEN_SET_RATIO, TOKEN_RATIO, PARTIAL_TOKEN_RATIO, WRATIO, Cached,
+                   Multi, score)
 
 __all__ = []
 
@@ -63,6 +64,23 @@ def fuzz_QRatio(s1, s2, score_cutoff=0.0):
 
 
 __all__ += ["fuzz_token_sort_ratio", "fuzz_partial_token_sort_ratio", "fuzz_QRatio"]
+
+
+def _fuzz_free(name, metric, doc):
+    def f(s1, s2, score_cutoff=0.0):
+        return score(metric, SIMILARITY, s1, s2, score_cutoff)
+    f.__name__ = name
+    f.__doc__ = doc
+    globals()[name] = f
+    __all__.append(name)
+
+
+_fuzz_free("fuzz_token_set_ratio", TOKEN_SET_RATIO, "fuzz::token_set_ratio (fuzz_impl.hpp:422-437)")
+_fuzz_free("fuzz_partial_token_set_ratio", PARTIAL_TOKEN_SET_RATIO,
+           "fuzz::partial_token_set_ratio (fuzz_impl.hpp:479-495)")
+_fuzz_free("fuzz_token_ratio", TOKEN_RATIO, "fuzz::token_ratio (fuzz_impl.hpp:517-571)")
+_fuzz_free("fuzz_partial_token_ratio", PARTIAL_TOKEN_RATIO, "fuzz::partial_token_ratio (fuzz_impl.hpp:703-737)")
+_fuzz_free("fuzz_WRatio", WRATIO, "fuzz::WRatio (fuzz_impl.hpp:788-829)")
 
 
 class _CachedBase:
@@ -134,6 +152,12 @@ _cached_fuzz("CachedTokenSortRatio", TOKEN_SORT_RATIO, "fuzz::CachedTokenSortRat
 _cached_fuzz("CachedPartialTokenSortRatio", PARTIAL_TOKEN_SORT_RATIO,
              "fuzz::CachedPartialTokenSortRatio (fuzz_impl.hpp:351-366)")
 _cached_fuzz("CachedQRatio", QRATIO, "fuzz::CachedQRatio (fuzz_impl.hpp:911-929)")
+_cached_fuzz("CachedTokenSetRatio", TOKEN_SET_RATIO, "fuzz::CachedTokenSetRatio (fuzz_impl.hpp:439-455)")
+_cached_fuzz("CachedPartialTokenSetRatio", PARTIAL_TOKEN_SET_RATIO,
+             "fuzz::CachedPartialTokenSetRatio (fuzz_impl.hpp:497-513)")
+_cached_fuzz("CachedTokenRatio", TOKEN_RATIO, "fuzz::CachedTokenRatio (fuzz_impl.hpp:685-699)")
+_cached_fuzz("CachedPartialTokenRatio", PARTIAL_TOKEN_RATIO, "fuzz::CachedPartialTokenRatio (fuzz_impl.hpp:770-784)")
+_cached_fuzz("CachedWRatio", WRATIO, "fuzz::CachedWRatio (fuzz_impl.hpp:831-886)")
 
 
 class experimental:

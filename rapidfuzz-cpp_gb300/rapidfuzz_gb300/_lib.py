@@ -9,7 +9,9 @@ lib_path = os.path.join(PKG_DIR, "lib", "librapidfuzz_gb300.so")
 
 (LEVENSHTEIN, INDEL, LCSSEQ, OSA, JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO, TOKEN_SORT_RATIO,
  PARTIAL_TOKEN_SORT_RATIO, QRATIO) = range(11)
-FUZZ_METRICS = (RATIO, PARTIAL_RATIO, TOKEN_SORT_RATIO, PARTIAL_TOKEN_SORT_RATIO, QRATIO)
+TOKEN_SET_RATIO, PARTIAL_TOKEN_SET_RATIO, TOKEN_RATIO, PARTIAL_TOKEN_RATIO, WRATIO = range(11, 16)
+FUZZ_METRICS = (RATIO, PARTIAL_RATIO, TOKEN_SORT_RATIO, PARTIAL_TOKEN_SORT_RATIO, QRATIO, TOKEN_SET_RATIO,
+                PARTIAL_TOKEN_SET_RATIO, TOKEN_RATIO, PARTIAL_TOKEN_RATIO, WRATIO)
 DISTANCE, SIMILARITY, NORMALIZED_DISTANCE, NORMALIZED_SIMILARITY = range(4)
 FORM_FREE, FORM_CACHED, FORM_MULTI = range(3)
 I32, I64, F64 = range(3)

@@ -129,6 +129,31 @@ int main()
         mq.similarity(r.data(), r.size(), std::string(""));
         CHECK(r[0] == 0.0 && r[1] == 0.0);
     }
+    // token_set_ratio family (tests-fuzz.cpp:48-137)
+    {
+        const std::string s1 = "new york mets", s3 = "the wonderful new york mets";
+        const std::string s4 = "new york mets vs atlanta braves", s5 = "atlanta braves vs new york mets";
+        const std::string s7 = "new york city mets - atlanta braves";
+        CHECK(rapidfuzz::fuzz::token_set_ratio(s4, s5) == 100.0);
+        CHECK(rapidfuzz::fuzz::token_set_ratio(std::string("a{"), std::string("{b")) == 50.0);
+        CHECK(rapidfuzz::fuzz::partial_token_set_ratio(s4, s7) == 100.0);
+        CHECK(rapidfuzz::fuzz::WRatio(s1, s1) == 100.0);
+        CHECK(std::fabs(rapidfuzz::fuzz::WRatio(s1, s3) - 90) < 1e-6);
+        CHECK(std::fabs(rapidfuzz::fuzz::WRatio(s4, s5) - 95) < 1e-6);
+        CHECK(rapidfuzz::fuzz::token_ratio(std::string(""), std::string("")) == 100.0);
+        CHECK(rapidfuzz::fuzz::partial_token_ratio(std::string(""), std::string("")) == 100.0);
+        CHECK(rapidfuzz::fuzz::WRatio(std::string(""), std::string("")) == 0.0);
+        rapidfuzz::fuzz::CachedWRatio<char> cw(s1);
+        CHECK(std::fabs(cw.similarity(s3) - 90) < 1e-6);
+        rapidfuzz::fuzz::CachedTokenSetRatio<char> cts3(s4);
+        CHECK(cts3.similarity(s5) == 100.0);
+        rapidfuzz::fuzz::CachedPartialTokenSetRatio<char> cpts3(s4);
+        CHECK(cpts3.similarity(s7) == 100.0);
+        rapidfuzz::fuzz::CachedTokenRatio<char> ctr(s4);
+        CHECK(ctr.similarity(s5) == 100.0);
+        rapidfuzz::fuzz::CachedPartialTokenRatio<char> cptr(s4);
+        CHECK(cptr.similarity(s7) == 100.0);
+    }
     // Multi* (Levenshtein.hpp:297-419) and its errors
     rapidfuzz::experimental::MultiLevenshtein<16> ml(3);
     ml.insert(std::string("kitten"));
@@ -195,6 +220,9 @@ int main()
         CHECK(same(rapidfuzz::fuzz::partial_token_sort_ratio(t1, t2, cf * 100),
                    of(RFO_PARTIAL_TOKEN_SORT_RATIO, RFO_SIMILARITY, 0, t1, t2, cf * 100)));
         CHECK(same(rapidfuzz::fuzz::QRatio(t1, t2, cf * 100), of(RFO_QRATIO, RFO_SIMILARITY, 0, t1, t2, cf * 100)));
+        CHECK(same(rapidfuzz::fuzz::token_set_ratio(t1, t2, cf * 100),
+                   of(RFO_TOKEN_SET_RATIO, RFO_SIMILARITY, 0, t1, t2, cf * 100)));
+        CHECK(same(rapidfuzz::fuzz::WRatio(t1, t2, cf * 100), of(RFO_WRATIO, RFO_SIMILARITY, 0, t1, t2, cf * 100)));
         rapidfuzz::fuzz::CachedTokenSortRatio<char> cts2(t1);
         CHECK(same(cts2.similarity(t2, cf * 100), of(RFO_TOKEN_SORT_RATIO, RFO_SIMILARITY, 1, t1, t2, cf * 100)));
         rapidfuzz::CachedOSA<char> co(s1);

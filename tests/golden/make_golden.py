@@ -1,7 +1,7 @@
 """Generate tests/golden/*.json from the UNMODIFIED reference (oracle/_ref/librfref.so,
 built by `make -C oracle ref` from the rapidfuzz-cpp v3.3.3 headers).
 
-Three fixtures:
+Fixtures:
   kat.json      the known-answer vectors of the reference's own test suite (each case cites
                 the test file:line it restates), with the value the reference computes here;
   random.json   seeded random cases over every metric x op x API form x cutoff, char widths
@@ -9,7 +9,9 @@ Three fixtures:
   multi.json    Multi* batches with several inserted strings;
   partial.json  fuzz::partial_ratio / CachedPartialRatio: the reference fuzz tests' inputs and
                 seeded random pairs;
-  tokens.json   token_sort_ratio / partial_token_sort_ratio / QRatio (free and Cached forms).
+  tokens.json   token_sort_ratio / partial_token_sort_ratio / QRatio (free and Cached forms);
+  tokenset.json token_set_ratio / partial_token_set_ratio / token_ratio / partial_token_ratio /
+                WRatio (free and Cached forms).
 Doubles are stored with float.hex() so the comparison is bit-exact.
 
 Usage: python tests/golden/make_golden.py   (needs the reference checkout; run in the
@@ -26,7 +28,8 @@ sys.path.insert(0, os.path.dirname(HERE))
 import numpy as np  # noqa: E402
 
 from oracle_lib import (DISTANCE, SIMILARITY, NORM_DISTANCE, NORM_SIMILARITY, LEVENSHTEIN, INDEL, LCSSEQ, OSA,  # noqa: E402
-                        JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO, TOKEN_SORT_RATIO, PARTIAL_TOKEN_SORT_RATIO, QRATIO, FREE, CACHED, MULTI, as_units, reference, result_is_int,
+                        JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO, TOKEN_SORT_RATIO, PARTIAL_TOKEN_SORT_RATIO, QRATIO,
+                        TOKEN_SET_RATIO, PARTIAL_TOKEN_SET_RATIO, TOKEN_RATIO, PARTIAL_TOKEN_RATIO, WRATIO, FREE, CACHED, MULTI, as_units, reference, result_is_int,
                         score, make_params, pack_strings, strings_struct)
 
 OPS = (DISTANCE, SIMILARITY, NORM_DISTANCE, NORM_SIMILARITY)
@@ -410,12 +413,56 @@ def token_cases(seed=13):
     return [c for c in out if c is not None]
 
 
+def tokenset_cases(seed=17):
+    """token_set_ratio / partial_token_set_ratio / token_ratio / partial_token_ratio / WRatio
+    and their Cached forms: the reference fuzz tests' inputs (test/tests-fuzz.cpp) paired
+    with each other, then seeded random strings drawn from small vocabularies (shared and
+    repeated tokens), every char width, ASCII and Unicode whitespace, length ratios on
+    both sides of WRatio's 1.5 and 8 thresholds, cutoffs 0..100.5."""
+    T = "test/tests-fuzz.cpp"
+    metrics = (TOKEN_SET_RATIO, PARTIAL_TOKEN_SET_RATIO, TOKEN_RATIO, PARTIAL_TOKEN_RATIO, WRATIO)
+    lits = fuzz_test_literals()
+    out = []
+    for i, a in enumerate(lits):
+        for b in (lits[i], lits[(i + 1) % len(lits)], lits[(i + 3) % len(lits)]):
+            for m in metrics:
+                out.append(case(m, SIMILARITY, FREE, a, b, cite=T))
+                out.append(case(m, SIMILARITY, CACHED, b, a, 50.0, cite=T))
+    rng = random.Random(seed)
+    spaces = [0x20, 0x09, 0x0A, 0x1C, 0x85, 0xA0, 0x2000, 0x3000]
+    while len(out) < 5000:
+        w = rng.choice([1, 2, 4, 8])
+        letters = [97, 98, 99, 100, 0xC0] + ([300, 4000, 70000] if w == 4 else [300] if w == 2 else [])
+        sp = [c for c in spaces if w > 1 or c < 256]
+        vocab = [[rng.choice(letters) for _ in range(rng.randint(1, 5))] for _ in range(rng.randint(1, 8))]
+
+        def mk(k):
+            s = []
+            for _ in range(k):
+                s += list(rng.choice(vocab)) if rng.random() < 0.7 else \
+                    [rng.choice(letters) for _ in range(rng.randint(0, 6))]
+                s += [rng.choice(sp) for _ in range(rng.randint(0, 2))]
+            return s
+        a = mk(rng.randint(0, 6))
+        b = mk(rng.choice([rng.randint(0, 6), rng.randint(0, 25)]))
+        if rng.random() < 0.2:
+            b = list(a)
+            rng.shuffle(b)
+        if rng.random() < 0.3:
+            a, b = b, a
+        cutoff = rng.choice([None, 0.0, 30.0, 50.0, 80.0, 90.0, 100.0, 100.5])
+        c = case(rng.choice(metrics), SIMILARITY, rng.choice([FREE, CACHED]), a, b, cutoff, w1=w, w2=w)
+        if c is not None:
+            out.append(c)
+    return [c for c in out if c is not None]
+
+
 def main():
     if reference() is None:
         sys.exit("oracle/_ref/librfref.so is missing: run `make -C oracle ref` where the reference checkout exists")
-    which = sys.argv[1:] or ["kat.json", "random.json", "multi.json", "partial.json", "tokens.json"]
+    which = sys.argv[1:] or ["kat.json", "random.json", "multi.json", "partial.json", "tokens.json", "tokenset.json"]
     gens = {"kat.json": kat_cases, "random.json": lambda: random_cases(4000), "multi.json": multi_cases,
-            "partial.json": partial_cases, "tokens.json": token_cases}
+            "partial.json": partial_cases, "tokens.json": token_cases, "tokenset.json": tokenset_cases}
     for name, cases in ((n, gens[n]()) for n in which):
         with open(os.path.join(HERE, name), "w") as f:
             json.dump(cases, f, separators=(",", ":"))

@@ -12,7 +12,9 @@ ORACLE_DIR = os.path.join(ROOT, "oracle")
 
 LEVENSHTEIN, INDEL, LCSSEQ, OSA, JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO = range(8)
 TOKEN_SORT_RATIO, PARTIAL_TOKEN_SORT_RATIO, QRATIO = 8, 9, 10
-FUZZ_METRICS = (RATIO, PARTIAL_RATIO, TOKEN_SORT_RATIO, PARTIAL_TOKEN_SORT_RATIO, QRATIO)
+TOKEN_SET_RATIO, PARTIAL_TOKEN_SET_RATIO, TOKEN_RATIO, PARTIAL_TOKEN_RATIO, WRATIO = 11, 12, 13, 14, 15
+FUZZ_METRICS = (RATIO, PARTIAL_RATIO, TOKEN_SORT_RATIO, PARTIAL_TOKEN_SORT_RATIO, QRATIO, TOKEN_SET_RATIO,
+                PARTIAL_TOKEN_SET_RATIO, TOKEN_RATIO, PARTIAL_TOKEN_RATIO, WRATIO)
 DISTANCE, SIMILARITY, NORM_DISTANCE, NORM_SIMILARITY = range(4)
 FREE, CACHED, MULTI = range(3)
 METRIC_NAMES = ["levenshtein", "indel", "lcsseq", "osa", "jaro", "jaro_winkler", "ratio"]

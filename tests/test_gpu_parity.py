@@ -27,7 +27,7 @@ def gpu_score(c, a, b):
     return int(v) if R._lib.result_is_int(m, op) else float(v)
 
 
-@pytest.mark.parametrize("fixture", ["kat.json", "random.json", "partial.json", "tokens.json"])
+@pytest.mark.parametrize("fixture", ["kat.json", "random.json", "partial.json", "tokens.json", "tokenset.json"])
 def test_fixtures_per_call(fixture):
     bad = []
     for c in G.load(fixture):
@@ -347,3 +347,102 @@ def test_token_scorer_api_names():
         R.Multi(R.PARTIAL_TOKEN_SORT_RATIO, 8, 1)
     with pytest.raises(ValueError):
         R.score(R.TOKEN_SORT_RATIO, R.DISTANCE, "a", "b")
+
+
+def _vocab_batches(seed, w, nq=23, nc=90):
+    """strings drawn from a small vocabulary (shared and repeated tokens), some long
+    choices, empty and all-whitespace strings"""
+    rng = random.Random(seed)
+    letters = [97, 98, 99, 100, 0xC0] + ([300, 70000] if w == 4 else [])
+    spaces = [0x20, 0x09, 0x0A] + ([0xA0, 0x3000] if w == 4 else [])
+    vocab = [[rng.choice(letters) for _ in range(rng.randint(1, 5))] for _ in range(10)]
+
+    def mk(k):
+        s = []
+        for _ in range(k):
+            s += list(rng.choice(vocab)) if rng.random() < 0.75 else [rng.choice(letters)
+                                                                       for _ in range(rng.randint(1, 6))]
+            s += [rng.choice(spaces) for _ in range(rng.randint(1, 2))]
+        return s
+    qs = [mk(rng.randint(0, 7)) for _ in range(nq - 2)] + [[], [0x20]]
+    cs = [mk(rng.choice([rng.randint(0, 7), rng.randint(0, 40)])) for _ in range(nc - 2)] + [[], [0x09, 0x20]]
+    dt = {1: np.uint8, 4: np.uint32}[w]
+    return (R.pack_strings([np.array(x, dtype=dt) for x in qs], w),
+            R.pack_strings([np.array(x, dtype=dt) for x in cs], w))
+
+
+@pytest.mark.parametrize("metric", ["TOKEN_SET_RATIO", "PARTIAL_TOKEN_SET_RATIO", "TOKEN_RATIO",
+                                    "PARTIAL_TOKEN_RATIO", "WRATIO"])
+@pytest.mark.parametrize("width", [1, 4])
+def test_cdist_token_set_family_matches_oracle(metric, width):
+    """token_set_ratio, partial_token_set_ratio, token_ratio, partial_token_ratio and WRatio
+    over batches (host parts, the FAM_TOKEN kernel), free and cached forms, several cutoffs"""
+    m = getattr(R, metric)
+    q, c = _vocab_batches(61 + width, width)
+    for cut in (0.0, 50.0, 85.0, 100.0, 100.5):
+        exp = oracle_cdist(m, R.SIMILARITY, q, c, cut)
+        for form in (R.FORM_FREE, R.FORM_CACHED):
+            got = R.cdist(m, R.SIMILARITY, q, c, cut, form=form)
+            bad = np.argwhere(got.view(np.int64) != exp.view(np.int64))
+            assert bad.size == 0, "cut %r form %d mismatch at %r: got %r exp %r" % (
+                cut, form, bad[0], got[tuple(bad[0])], exp[tuple(bad[0])])
+    data, off, w = q
+    s1 = data[off[2]:off[3]]
+    got = R.Cached(m, s1).score_many(R.SIMILARITY, c, 30.0)
+    exp = oracle_cdist(m, R.SIMILARITY, R.pack_strings([s1], w), c, 30.0)[0]
+    assert np.array_equal(got.view(np.int64), exp.view(np.int64))
+
+
+def test_cdist_wratio_device_buffers():
+    """WRatio with device inputs (downloaded for the parts) and a device result with ld"""
+    import ctypes
+    import torch
+    from rapidfuzz_gb300._lib import Cutoff, Strings, make_params, check
+    q, c = _vocab_batches(5, 1, 9, 40)
+    exp = oracle_cdist(R.WRATIO, R.SIMILARITY, q, c, 40.0)
+    dq = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in q[:2]]
+    dc = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in c[:2]]
+    nq, nc = q[1].size - 1, c[1].size - 1
+    ld = nc + 3
+    out = torch.full((nq, ld), -7.0, dtype=torch.float64, device="cuda")
+    qs = Strings(dq[0].data_ptr(), dq[1].data_ptr(), nq, 1)
+    cs = Strings(dc[0].data_ptr(), dc[1].data_ptr(), nc, 1)
+    torch.cuda.synchronize()
+    check(R.lib().rfg_cdist(R.WRATIO, R.SIMILARITY, R.FORM_CACHED, ctypes.byref(qs), ctypes.byref(cs),
+                            ctypes.byref(make_params()), Cutoff(0, 40.0, 0, 0.0), R.F64, out.data_ptr(), ld,
+                            R.DEVICE_INPUTS | R.DEVICE_OUTPUT))
+    check(R.lib().rfg_synchronize())
+    got = out.cpu().numpy()
+    assert np.array_equal(got[:, :nc].view(np.int64), exp.view(np.int64))
+    assert (got[:, nc:] == -7.0).all()
+
+
+def test_token_set_family_api_names():
+    """the reference's names and known answers (tests-fuzz.cpp:48-137)"""
+    s1, s3 = "new york mets", "the wonderful new york mets"
+    s4, s5 = "new york mets vs atlanta braves", "atlanta braves vs new york mets"
+    s7 = "new york city mets - atlanta braves"
+    assert R.fuzz_token_set_ratio(s4, s5) == 100.0
+    assert R.fuzz_token_set_ratio("{", "{") == 100.0 and R.fuzz_token_set_ratio("{a", "{a") == 100.0
+    assert R.fuzz_token_set_ratio("a{", "{b") == 50.0
+    assert R.fuzz_partial_token_set_ratio(s4, s7) == 100.0
+    assert R.fuzz_WRatio(s1, s1) == 100.0
+    assert abs(R.fuzz_WRatio(s1, s3) - 90.0) < 1e-6
+    assert abs(R.fuzz_WRatio(s4, s5) - 95.0) < 1e-6
+    assert abs(R.fuzz_WRatio("hello", "hello" + "abcde" * 7) - 90.0) < 1e-6
+    assert R.fuzz_token_set_ratio("", "") == 0.0 and R.fuzz_partial_token_set_ratio("", "") == 0.0
+    assert R.fuzz_token_ratio("", "") == 100.0 and R.fuzz_partial_token_ratio("", "") == 100.0
+    assert R.fuzz_WRatio("", "") == 0.0
+    o = oracle()
+    for a, b in ((s1, s3), (s4, s5), (s4, s7), ("", "a"), ("a a a", "a"), ("fuzzy was a bear", "fuzzy fuzzy was a bear")):
+        for m, free, cached in ((R.TOKEN_SET_RATIO, R.fuzz_token_set_ratio, R.CachedTokenSetRatio),
+                                (R.PARTIAL_TOKEN_SET_RATIO, R.fuzz_partial_token_set_ratio,
+                                 R.CachedPartialTokenSetRatio),
+                                (R.TOKEN_RATIO, R.fuzz_token_ratio, R.CachedTokenRatio),
+                                (R.PARTIAL_TOKEN_RATIO, R.fuzz_partial_token_ratio, R.CachedPartialTokenRatio),
+                                (R.WRATIO, R.fuzz_WRatio, R.CachedWRatio)):
+            exp = oscore(o.rfo_score, m, R.SIMILARITY, FREE, a.encode(), b.encode(), 0.0)
+            assert G.same(free(a, b), exp), (m, a, b)
+            assert G.same(cached(a).similarity(b), exp), (m, a, b)
+    with pytest.raises(ValueError):
+        R.Multi(R.WRATIO, 8, 1)

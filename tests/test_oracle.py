@@ -13,7 +13,7 @@ from oracle_lib import (CACHED, FREE, MULTI, LEVENSHTEIN, LCSSEQ, OSA, DISTANCE,
                         result_is_int, oracle_cdist, pack_strings)
 
 
-@pytest.mark.parametrize("fixture", ["kat.json", "random.json", "partial.json", "tokens.json"])
+@pytest.mark.parametrize("fixture", ["kat.json", "random.json", "partial.json", "tokens.json", "tokenset.json"])
 def test_oracle_matches_reference_fixtures(fixture):
     o = oracle()
     bad = []
