@@ -12,8 +12,8 @@ cfg4  Jaro-Winkler (prefix_weight 0.1, cutoff 0.85) and fuzz::ratio (cutoff 85) 
       code-point token strings, 1,024 x 1,000,000, dense float64 outputs kept on the device.
 partial  fuzz::partial_ratio (cutoff 80) of 256 token queries against 200,000 token strings
       (uint32, as in cfg4), dense float64 out on the device (the first widening of the path).
-tokens   token_sort_ratio and QRatio (cutoff 80), 256 x 200,000 token strings, host inputs
-      and host results through rfg_cdist (the joins run on the host threads).
+tokens   token_sort_ratio, QRatio, WRatio and token_set_ratio (cutoff 80), 256 x 200,000 token
+      strings, host inputs and host results through rfg_cdist (joins / parts on the host threads).
 cfg5  serving: device-resident corpora of 10,000,000 DNA strings (len U[10,200]) and
       1,000,000 uint32 token strings; Poisson arrivals (--rate req/s for --duration s), each
       an extractOne (limit 1) or top-10 extract of one query of length U[5,500] with a metric
@@ -176,7 +176,8 @@ def run(args, rank, world, local):
         per = {}
         clocks = B.ClockSampler()
         clocks.start()
-        for name, m in (("token_sort_ratio", R.TOKEN_SORT_RATIO), ("QRatio", R.QRATIO)):
+        for name, m in (("token_sort_ratio", R.TOKEN_SORT_RATIO), ("QRatio", R.QRATIO), ("WRatio", R.WRATIO),
+                        ("token_set_ratio", R.TOKEN_SET_RATIO)):
             for _ in range(warmup):
                 out = R.cdist(m, R.SIMILARITY, q, c, 80.0)
             torch.cuda.synchronize()
@@ -198,9 +199,10 @@ def run(args, rank, world, local):
         t = per["token_sort_ratio"]
         h2d = int(q[0].nbytes + q[1].nbytes + c[0].nbytes + c[1].nbytes)
         line.update({"value": nq * nc / t, "unit": "pairs/s", "ms_per_step": t * 1e3, "dtype": "f64",
-                     "config": {"workload": "fuzz::token_sort_ratio cutoff 80 (and QRatio), 256 x %d uint32 token "
-                                            "strings (1-4 tokens of 3-12 units) from host buffers to a host float64 "
-                                            "matrix: host sorted-split joins, upload, ratio kernel, download" % nc,
+                     "config": {"workload": "fuzz::token_sort_ratio cutoff 80 (and QRatio, WRatio, token_set_ratio), "
+                                            "256 x %d uint32 token strings (1-4 tokens of 3-12 units) from host "
+                                            "buffers to a host float64 matrix: host sorted-split joins / parts, "
+                                            "upload, device scorer, download" % nc,
                                 "ms_per_call": {k: v * 1e3 for k, v in per.items()}},
                      "cpu_baseline": {"value": sub * nc / tc, "unit": "pairs/s", "cores": os.cpu_count(),
                                       "kind": "port", "sample": "8 of the 256 queries x all %d choices" % nc},

@@ -59,8 +59,9 @@ typedef enum {
      * whitespace, the tokens sorted by code unit (compared unsigned) and joined with
      * U+0020 on the host (fuzz.hpp:203-373, fuzz_impl.hpp:297-366); QRatio is ratio with
      * 0 where either string is empty (fuzz.hpp:692-804, fuzz_impl.hpp:891-929).  Only
-     * RFG_SIMILARITY and RFG_F64, through rfg_score_f64, rfg_cached_*, rfg_cdist and (token
-     * sort and QRatio) rfg_multi_*; not on a corpus, a batch or the no-allocation entry. */
+     * RFG_SIMILARITY and RFG_F64, through rfg_score_f64, rfg_cached_*, rfg_cdist, rfg_extract
+     * and (token sort and QRatio) rfg_multi_*; not in a prepared batch, the server or the
+     * no-allocation entry. */
     RFG_TOKEN_SORT_RATIO = 8,
     RFG_PARTIAL_TOKEN_SORT_RATIO = 9,
     RFG_QRATIO = 10,
@@ -68,7 +69,7 @@ typedef enum {
      * partial_token_set_ratio, token_ratio, partial_token_ratio and WRatio with their
      * Cached forms, scored on the device from the strings, their sorted-split joins and
      * the joins of their distinct tokens (made on the host).  Only RFG_SIMILARITY and
-     * RFG_F64, through rfg_score_f64, rfg_cached_* and rfg_cdist; no Multi form. */
+     * RFG_F64, through rfg_score_f64, rfg_cached_*, rfg_cdist and rfg_extract; no Multi form. */
     RFG_TOKEN_SET_RATIO = 11,
     RFG_PARTIAL_TOKEN_SET_RATIO = 12,
     RFG_TOKEN_RATIO = 13,

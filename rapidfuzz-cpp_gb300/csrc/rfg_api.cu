@@ -1238,6 +1238,12 @@ struct rfg_corpus_s {
     int64_t chunk = 0;
     int64_t count = 0;
     int64_t maxlen = 0; /* longest string */
+    /* the token scorers' twin, built on first use: every string as [string][S][J] (its
+     * sorted-split join and the join of its distinct tokens) with the part lengths */
+    bool tok = false;
+    DBuf tdata, toff, tparts;
+    KStrings tdev{};
+    int64_t tmaxlen = 0;
 };
 
 struct rfg_multi_s {
@@ -1591,7 +1597,8 @@ struct ExtractJob {
 /* Enqueue extract/extractOne of the queries against a corpus on stream st: the tile
  * kernels keep each tile's best `k`, a merge kernel keeps each query's best `k`. */
 rfg_status extract_enqueue(rfg_corpus c, const QuerySet& q, int metric, int op, const ScoreParams& sp,
-                           rfg_cutoff cut, int k, int tie_last, cudaStream_t st, ExtractJob* job)
+                           rfg_cutoff cut, int k, int tie_last, cudaStream_t st, ExtractJob* job,
+                           const int32_t* qparts = nullptr)
 {
     const int64_t nq = q.dev.n;
     job->nq = nq;
@@ -1628,7 +1635,12 @@ rfg_status extract_enqueue(rfg_corpus c, const QuerySet& q, int metric, int op, 
     spec.chunk_lmin = c->lmin.as<int32_t>();
     spec.chunk_lmax = c->lmax.as<int32_t>();
     spec.fixed_maxlen = c->maxlen;
-    RFG_TRY(prepare_batch(q, c->dev, spec, &job->pb));
+    if (qparts) { /* token scorers: the parts of the queries and of the corpus twin */
+        spec.fixed_maxlen = c->tmaxlen;
+        spec.qparts = qparts;
+        spec.cparts = c->tparts.as<int32_t>();
+    }
+    RFG_TRY(prepare_batch(q, qparts ? c->tdev : c->dev, spec, &job->pb));
     if (st != g.stream) {
         /* uploads, resets and the tile lists were enqueued on the library stream */
         RFG_CUDA(cudaEventRecord(g.prep_ev, g.stream));
@@ -1771,13 +1783,36 @@ rfg_status rfg_corpus_destroy(rfg_corpus c)
     return RFG_OK;
 }
 
+/* the corpus's token twin (rfg_corpus_s::tok) */
+static rfg_status corpus_token_twin(rfg_corpus c)
+{
+    if (c->tok) return RFG_OK;
+    HostStrings h;
+    const rfg_strings dv{c->dev.data, c->dev.off, c->count, c->dev.width};
+    RFG_TRY(download_strings(&dv, &h, "corpus"));
+    std::vector<unsigned char> td;
+    std::vector<int64_t> to;
+    std::vector<int32_t> tp;
+    token_parts_set(h.data.data(), h.off.data(), c->count, c->dev.width, true, true, true, &td, &to, &tp);
+    const rfg_strings tv{td.data(), to.data(), c->count, c->dev.width};
+    RFG_TRY(upload_strings(&tv, &c->tdata, &c->toff, &c->tdev));
+    RFG_TRY(c->tparts.alloc(tp.size() * 4));
+    if (!tp.empty()) RFG_CUDA(cudaMemcpyAsync(c->tparts.p, tp.data(), tp.size() * 4, cudaMemcpyHostToDevice, g.stream));
+    RFG_CUDA(cudaStreamSynchronize(g.stream));
+    c->tmaxlen = 0;
+    for (int64_t i = 0; i < c->count; ++i) c->tmaxlen = std::max<int64_t>(c->tmaxlen, to[i + 1] - to[i]);
+    c->tok = true;
+    return RFG_OK;
+}
+
 rfg_status rfg_extract(rfg_corpus c, rfg_metric metric, rfg_op op, const rfg_strings* Q, const rfg_params* p,
                        rfg_cutoff cut, int32_t limit, int32_t tie_last_wins, int64_t* out_index, double* out_score,
                        int32_t* out_count, uint32_t flags)
 {
     std::lock_guard<std::recursive_mutex> lk(g.mu);
     if (!c) return fail(RFG_ERR_INVALID_ARGUMENT, "corpus is NULL");
-    RFG_TRY(check_metric_op(metric, op, RFG_FORM_CACHED));
+    const bool tok = is_token_metric(metric);
+    RFG_TRY(tok ? check_any_metric_op(metric, op, RFG_FORM_CACHED) : check_metric_op(metric, op, RFG_FORM_CACHED));
     RFG_TRY(check_strings(Q, "queries"));
     if (limit < 1 || limit > RFG_MAX_TOPK) return fail(RFG_ERR_INVALID_ARGUMENT, "limit must be in [1, 32]");
     if (!out_index || !out_score || !out_count) return fail(RFG_ERR_INVALID_ARGUMENT, "NULL output");
@@ -1785,9 +1820,29 @@ rfg_status rfg_extract(rfg_corpus c, rfg_metric metric, rfg_op op, const rfg_str
     RFG_TRY(check_params(metric, sp));
     RFG_TRY(ensure_ctx());
     QuerySet qs;
-    DBuf qd, qo;
+    DBuf qd, qo, qp;
     const int64_t nq = Q->count;
-    if (flags & RFG_DEVICE_INPUTS) {
+    if (tok) { /* the queries' parts on the host, then the corpus twin */
+        HostStrings hq, jq;
+        rfg_strings q = *Q;
+        if (flags & RFG_DEVICE_INPUTS) {
+            RFG_TRY(download_strings(Q, &hq, "queries"));
+            q.data = hq.data.data();
+            q.offsets = hq.off.data();
+        }
+        RFG_TRY(check_offsets(q.offsets, nq, "queries"));
+        if (!q.data && nq && q.offsets[nq] > q.offsets[0]) return fail(RFG_ERR_INVALID_ARGUMENT, "string data is NULL");
+        std::vector<int32_t> parts;
+        token_parts_set(q.data, q.offsets, nq, q.char_width, true, true, true, &jq.data, &jq.off, &parts);
+        const rfg_strings qt{jq.data.data(), jq.off.data(), nq, q.char_width};
+        RFG_TRY(query_info_from_host(qt.data, qt.offsets, nq, qt.char_width, &qs));
+        RFG_TRY(upload_strings(&qt, &qd, &qo, &qs.dev));
+        RFG_TRY(qp.alloc(parts.size() * 4));
+        if (!parts.empty())
+            RFG_CUDA(cudaMemcpyAsync(qp.p, parts.data(), parts.size() * 4, cudaMemcpyHostToDevice, g.stream));
+        RFG_TRY(corpus_token_twin(c));
+    }
+    else if (flags & RFG_DEVICE_INPUTS) {
         std::vector<int64_t> off(nq + 1);
         RFG_CUDA(cudaMemcpy(off.data(), Q->offsets, (nq + 1) * 8, cudaMemcpyDeviceToHost));
         std::vector<unsigned char> qh;
@@ -1803,7 +1858,8 @@ rfg_status rfg_extract(rfg_corpus c, rfg_metric metric, rfg_op op, const rfg_str
         RFG_TRY(upload_strings(Q, &qd, &qo, &qs.dev));
     }
     ExtractJob job;
-    RFG_TRY(extract_enqueue(c, qs, metric, op, sp, cut, limit, tie_last_wins ? 1 : 0, g.stream, &job));
+    RFG_TRY(extract_enqueue(c, qs, metric, op, sp, cut, limit, tie_last_wins ? 1 : 0, g.stream, &job,
+                            tok ? qp.as<int32_t>() : nullptr));
     job.free_on(nullptr);
     if (nq) {
         const cudaMemcpyKind kind = (flags & RFG_DEVICE_OUTPUT) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;

@@ -179,6 +179,9 @@ enum Metric {
     JARO_WINKLER = 5,
     RATIO = 6,
     PARTIAL_RATIO = 7,
+    TOKEN_SORT_RATIO = 8,
+    PARTIAL_TOKEN_SORT_RATIO = 9,
+    QRATIO = 10,
     TOKEN_SET_RATIO = 11,
     PARTIAL_TOKEN_SET_RATIO = 12,
     TOKEN_RATIO = 13,
@@ -1102,6 +1105,9 @@ RFG_HD int metric_family(int metric, int form, const ScoreParams& p)
     case RATIO: return FAM_LCS;
     case OSA: return FAM_OSA;
     case PARTIAL_RATIO: return FAM_PARTIAL;
+    case TOKEN_SORT_RATIO:
+    case PARTIAL_TOKEN_SORT_RATIO:
+    case QRATIO:
     case TOKEN_SET_RATIO:
     case PARTIAL_TOKEN_SET_RATIO:
     case TOKEN_RATIO:
@@ -2200,6 +2206,20 @@ RFG_NOINL double token_set_dev(const P& p, double cutoff, bool with_sorted, u64*
     return dmax(dmax(result, r_ab), r_ba);
 }
 
+/* ratio of q's part [qa, qa + qm) with c's part [ca, ca + cn) (fuzz_impl.hpp:22-32) */
+template <typename P>
+RFG_HD double tok_ratio(const P& p, int qa, int qm, int ca, int cn, double cutoff, u64* st)
+{
+    u64 lcs = 0;
+    if (qm && cn) {
+        const PMShift<typename P::PMType> pv{p.pm, p.W, qa, qm};
+        const TextSlice<typename P::TxtType> tv{p.t, ca};
+        lcs_stream(pv, words_of(qm), tv, cn, st, [](int) {});
+        lcs = lcs_count(st, words_of(qm), qm);
+    }
+    return ratio_from_lcs((u64)qm, (u64)cn, lcs, cutoff);
+}
+
 /* partial_ratio of q's part [qa, qa + qm) with c's part [ca, ca + cn) */
 template <typename P>
 RFG_NOINL double tok_partial(const P& p, int qa, int qm, int ca, int cn, double cutoff, u64* st)
@@ -2232,11 +2252,7 @@ RFG_HD double wratio_dev(const P& p, double cutoff, u64* st)
     const int len1 = p.q0, len2 = p.c0;
     if (!len1 || !len2) return 0.0;
     const double len_ratio = len1 > len2 ? ddiv((double)len1, (double)len2) : ddiv((double)len2, (double)len1);
-    /* ratio of the original strings */
-    const PMShift<typename P::PMType> pv{p.pm, p.W, 0, len1};
-    const TextSlice<typename P::TxtType> tv{p.t, 0};
-    lcs_stream(pv, words_of(len1), tv, len2, st, [](int) {});
-    double end_ratio = ratio_from_lcs((u64)len1, (u64)len2, lcs_count(st, words_of(len1), len1), cutoff);
+    double end_ratio = tok_ratio(p, 0, len1, 0, len2, cutoff, st);
     if (len_ratio < 1.5) {
         cutoff = ddiv(dmax(cutoff, end_ratio), UNBASE_SCALE);
         return dmax(end_ratio, dmul(token_set_dev(p, cutoff, true, st), UNBASE_SCALE));
@@ -2248,13 +2264,20 @@ RFG_HD double wratio_dev(const P& p, double cutoff, u64* st)
     return dmax(end_ratio, dmul(dmul(partial_token_ratio_dev(p, cutoff, st), UNBASE_SCALE), PARTIAL_SCALE));
 }
 
-/* one pair of token_set_ratio / partial_token_set_ratio / token_ratio /
- * partial_token_ratio / WRatio (free and Cached forms give the same values) */
+/* one pair of the token scorers (free and Cached forms give the same values):
+ * token_sort_ratio, partial_token_sort_ratio (fuzz_impl.hpp:297-349) and QRatio
+ * (fuzz_impl.hpp:891-909) on their parts here serve extract over a corpus; rfg_cdist
+ * scores them with the ratio kernels */
 template <typename P>
 RFG_HD double token_family_dev(int metric, const P& p, double cutoff, u64* st)
 {
     if (cutoff > 100) return 0.0;
     switch (metric) {
+    case TOKEN_SORT_RATIO: return tok_ratio(p, p.q0, p.qs, p.c0, p.cs, cutoff, st);
+    case PARTIAL_TOKEN_SORT_RATIO: return tok_partial(p, p.q0, p.qs, p.c0, p.cs, cutoff, st);
+    case QRATIO:
+        if (!p.q0 || !p.c0) return 0.0;
+        return tok_ratio(p, 0, p.q0, 0, p.c0, cutoff, st);
     case TOKEN_SET_RATIO:
         if (!p.qs || !p.cs) return 0.0; /* no tokens on a side (fuzz_impl.hpp:379) */
         return token_set_dev(p, cutoff, false, st);

@@ -789,7 +789,9 @@ __device__ __forceinline__ void score_pair_generic(const KParams& a, const u64* 
         const RawText<CT> c{s2};
         typedef TokPair<PMRowsRT, RawQuery, decltype(txt), RawText<CT>> Pair;
         const Pair p{&pm, W, &q, &txt, &c, qp[0], qp[1], qp[2], __ldg(cp), __ldg(cp + 1), __ldg(cp + 2)};
-        vf = token_family_dev(a.metric, p, s.cf, st);
+        /* extract: every pair is scored with the caller's cutoff (the running threshold
+         * only filters), so the lists equal a dense matrix filtered afterwards */
+        vf = token_family_dev(a.metric, p, a.cf, st);
         emit(a, qi, ci, 0, vf, false, s.ci, s.cf, tl);
         return;
     }

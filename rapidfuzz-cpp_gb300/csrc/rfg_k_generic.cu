@@ -20,7 +20,7 @@ static const void* pick_generic(int fam)
 
 const void* generic_kernel(int fam, int width, bool topk)
 {
-    if (fam == FAM_TOKEN) return topk ? nullptr : token_kernel(width);
+    if (fam == FAM_TOKEN) return token_kernel(width, topk);
     switch (width) {
     case 1: return topk ? pick_generic<uint8_t, true>(fam) : pick_generic<uint8_t, false>(fam);
     case 2: return topk ? pick_generic<uint16_t, true>(fam) : pick_generic<uint16_t, false>(fam);

@@ -22,8 +22,8 @@ const void* tiles_mq_kernel_jaro(int width);
 inline int mq_queries(int fam) { return fam == FAM_LCS ? 4 : 2; }
 /* k_generic<FAM, CT, TOPK> */
 const void* generic_kernel(int fam, int width, bool topk);
-/* k_generic<FAM_TOKEN, CT, false> (its own translation unit) */
-const void* token_kernel(int width);
+/* k_generic<FAM_TOKEN, CT, TOPK> (its own translation unit) */
+const void* token_kernel(int width, bool topk);
 /* k_topk_merge */
 const void* topk_merge_kernel();
 /* k_jaro_tables (per-query JaroTab pre-pass) */

@@ -51,3 +51,35 @@ def test_extract_matches_reference_loop(metric, op, cut, limit, tie_last):
         assert cnt[i] == len(ei), (i, cnt[i], len(ei))
         assert np.array_equal(idx[i, :cnt[i]], ei), (i, idx[i, :cnt[i]], ei)
         assert np.array_equal(sc[i, :cnt[i]].view(np.int64), es.view(np.int64))
+
+
+TOKEN_CASES = [(R.WRATIO, 0.0), (R.WRATIO, 70.0), (R.TOKEN_SET_RATIO, 50.0), (R.TOKEN_SORT_RATIO, 60.0),
+               (R.PARTIAL_TOKEN_SORT_RATIO, 0.0), (R.QRATIO, 0.0), (R.TOKEN_RATIO, 80.0),
+               (R.PARTIAL_TOKEN_SET_RATIO, 0.0), (R.PARTIAL_TOKEN_RATIO, 90.0)]
+
+
+@pytest.mark.parametrize("metric,cut", TOKEN_CASES)
+@pytest.mark.parametrize("limit,tie_last", [(1, True), (5, False)])
+def test_extract_token_scorers(metric, cut, limit, tie_last):
+    """extract / extractOne with the token scorers (WRatio is rapidfuzz's default scorer):
+    the corpus's token twin, the FAM_TOKEN extract kernel"""
+    rng = random.Random(hash((metric, limit)) & 0xffff)
+    vocab = [[rng.choice([97, 98, 99, 100]) for _ in range(rng.randint(1, 5))] for _ in range(12)]
+
+    def mk(k):
+        s = []
+        for _ in range(k):
+            s += list(rng.choice(vocab))
+            s += [32] * rng.randint(1, 2)
+        return s
+    qs = [mk(rng.randint(1, 5)) for _ in range(7)] + [[], [32]]
+    cs = [mk(rng.randint(0, 8)) for _ in range(3000)] + [[]]
+    q = R.pack_strings([np.array(x, dtype=np.uint8) for x in qs], 1)
+    c = R.pack_strings([np.array(x, dtype=np.uint8) for x in cs], 1)
+    corpus = R.Corpus(c)
+    idx, sc, cnt = corpus.extract(metric, R.SIMILARITY, q, limit, cut, tie_last)
+    exp = oracle_extract(metric, R.SIMILARITY, q, c, limit, cut, tie_last)
+    for i, (ei, es) in enumerate(exp):
+        assert cnt[i] == len(ei), (i, cnt[i], len(ei))
+        assert np.array_equal(idx[i, :cnt[i]], ei), (i, idx[i, :cnt[i]], ei)
+        assert np.array_equal(sc[i, :cnt[i]].view(np.int64), es.view(np.int64))
