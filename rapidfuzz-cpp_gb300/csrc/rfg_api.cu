@@ -23,6 +23,7 @@
 #include <mutex>
 #include <tuple>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -74,6 +75,11 @@ struct Ctx {
     cudaStream_t copy = nullptr; /* device-to-host result copies overlapping the next row block */
     cudaEvent_t blk_ev[RFG_MAX_ROW_BLOCKS] = {};
     cudaEvent_t prep_ev = nullptr; /* end of a preparation on `stream`, for launches on other streams */
+    /* pinned staging of host results bound for pageable memory: two slots, one copied out
+     * by the host threads while the other fills */
+    unsigned char* stage_h = nullptr;
+    size_t stage_slot = 0;
+    cudaEvent_t stage_ev[2] = {};
     std::recursive_mutex mu;
     std::unordered_map<const void*, int> occ; /* (kernel) -> CTAs per SM at the default smem */
 };
@@ -93,6 +99,7 @@ rfg_status ensure_ctx()
     RFG_CUDA(cudaStreamCreateWithFlags(&g.copy, cudaStreamNonBlocking));
     for (auto& e : g.blk_ev) RFG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     RFG_CUDA(cudaEventCreateWithFlags(&g.prep_ev, cudaEventDisableTiming));
+    for (auto& e : g.stage_ev) RFG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     cudaMemPool_t pool;
     RFG_CUDA(cudaDeviceGetDefaultMemPool(&pool, g.device));
     uint64_t thr = UINT64_MAX;
@@ -836,6 +843,56 @@ rfg_status check_dtype(int metric, int op, int dt)
 rfg_status token_cdist(int metric, int op, int form, const rfg_strings* Q, bool q_dev, const rfg_strings* C,
                        bool c_dev, const rfg_params* p, rfg_cutoff cut, int dt, void* out, int64_t ld, bool dev_out);
 
+/* host memory the driver has not pinned or registered */
+bool is_pageable(const void* p)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return true;
+    }
+    return at.type == cudaMemoryTypeUnregistered;
+}
+
+constexpr size_t kStageSlot = 32u << 20;
+
+rfg_status stage_reserve(size_t slot)
+{
+    if (g.stage_slot >= slot) return RFG_OK;
+    if (g.stage_h) cudaFreeHost(g.stage_h);
+    g.stage_h = nullptr;
+    g.stage_slot = 0;
+    RFG_CUDA(cudaHostAlloc((void**)&g.stage_h, 2 * slot, cudaHostAllocDefault));
+    g.stage_slot = slot;
+    return RFG_OK;
+}
+
+/* rows of row_bytes from a packed source to dst rows dpitch apart, over the host threads
+ * (the first touch of fresh pageable pages is the cost, and it spreads over cores) */
+void copy_rows_parallel(unsigned char* dst, size_t dpitch, const unsigned char* src, size_t row_bytes, int64_t rows)
+{
+    const size_t total = row_bytes * (size_t)rows;
+    const int64_t hw = std::max<int64_t>(1, (int64_t)std::thread::hardware_concurrency());
+    const int64_t nt = std::min<int64_t>({hw, 16, std::max<int64_t>(1, (int64_t)(total >> 22))});
+    auto part = [&](int64_t t) {
+        if (dpitch == row_bytes) { /* one contiguous range */
+            const size_t a = total * t / nt, b = total * (t + 1) / nt;
+            memcpy(dst + a, src + a, b - a);
+            return;
+        }
+        for (int64_t r = rows * t / nt; r < rows * (t + 1) / nt; ++r)
+            memcpy(dst + (size_t)r * dpitch, src + (size_t)r * row_bytes, row_bytes);
+    };
+    if (nt == 1) {
+        part(0);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int64_t t = 1; t < nt; ++t) th.emplace_back(part, t);
+    part(0);
+    for (auto& x : th) x.join();
+}
+
 /* cdist over host or device batches.  qparts / cparts: the device part-length arrays of
  * the token_set_ratio family (Q and C are then the part concatenations) */
 rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const rfg_strings* C, const rfg_params* p,
@@ -914,6 +971,42 @@ rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const 
     RFG_TRY(prepare_batch(qs, ck, spec, &pb, dev_in ? nullptr : C->offsets));
     RFG_CUDA(cudaMemsetAsync(pb.counters, 0, RFG_COUNTERS * sizeof(int), g.stream));
     RFG_TRY(enqueue_pre(pb, g.stream));
+    const size_t row_bytes = (size_t)nc * esz;
+    if (nc && bytes >= (8u << 20) && is_pageable(out)) {
+        /* pageable destination: row pieces of <= 32 MB go to pinned staging on the copy
+         * stream and on to `out` on the host threads, the next piece in flight meanwhile */
+        const int64_t prow = std::max<int64_t>(1, (int64_t)(kStageSlot / row_bytes));
+        RFG_TRY(stage_reserve((size_t)prow * row_bytes));
+        struct Piece {
+            int b;
+            int64_t r0, r1;
+        };
+        std::vector<Piece> pieces;
+        for (size_t b = 0; b < pb.rows.size(); ++b) {
+            RFG_TRY(enqueue_block(pb, (int)b, g.stream));
+            RFG_CUDA(cudaEventRecord(g.blk_ev[b], g.stream));
+            for (int64_t r = pb.rows[b].first; r < pb.rows[b].second; r += prow)
+                pieces.push_back(Piece{(int)b, r, std::min<int64_t>(pb.rows[b].second, r + prow)});
+        }
+        auto issue = [&](size_t i) -> rfg_status {
+            const Piece& P = pieces[i];
+            RFG_CUDA(cudaStreamWaitEvent(g.copy, g.blk_ev[P.b], 0));
+            RFG_CUDA(cudaMemcpy2DAsync(g.stage_h + (i & 1) * g.stage_slot, row_bytes,
+                                       (const char*)od.p + (size_t)P.r0 * ld * esz, ld * esz, row_bytes, P.r1 - P.r0,
+                                       cudaMemcpyDeviceToHost, g.copy));
+            RFG_CUDA(cudaEventRecord(g.stage_ev[i & 1], g.copy));
+            return RFG_OK;
+        };
+        if (!pieces.empty()) RFG_TRY(issue(0));
+        for (size_t i = 0; i < pieces.size(); ++i) {
+            if (i + 1 < pieces.size()) RFG_TRY(issue(i + 1));
+            RFG_CUDA(cudaEventSynchronize(g.stage_ev[i & 1]));
+            copy_rows_parallel((unsigned char*)out + (size_t)pieces[i].r0 * ld * esz, ld * esz,
+                               g.stage_h + (i & 1) * g.stage_slot, row_bytes, pieces[i].r1 - pieces[i].r0);
+        }
+        RFG_CUDA(cudaStreamSynchronize(g.copy));
+        return check_batch(pb, g.stream);
+    }
     for (size_t b = 0; b < pb.rows.size(); ++b) {
         RFG_TRY(enqueue_block(pb, (int)b, g.stream));
         const int64_t r0 = pb.rows[b].first, r1 = pb.rows[b].second;
