@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -80,6 +81,9 @@ struct Ctx {
     unsigned char* stage_h = nullptr;
     size_t stage_slot = 0;
     cudaEvent_t stage_ev[2] = {};
+    /* host results in pinned, mapped memory are stored by the kernels themselves over the
+     * host link (RFG_HOST_STORES=0 in the environment copies them from a device buffer) */
+    bool host_stores = true;
     std::recursive_mutex mu;
     std::unordered_map<const void*, int> occ; /* (kernel) -> CTAs per SM at the default smem */
 };
@@ -100,6 +104,7 @@ rfg_status ensure_ctx()
     for (auto& e : g.blk_ev) RFG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     RFG_CUDA(cudaEventCreateWithFlags(&g.prep_ev, cudaEventDisableTiming));
     for (auto& e : g.stage_ev) RFG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    if (const char* hs = getenv("RFG_HOST_STORES")) g.host_stores = atoi(hs) != 0;
     cudaMemPool_t pool;
     RFG_CUDA(cudaDeviceGetDefaultMemPool(&pool, g.device));
     uint64_t thr = UINT64_MAX;
@@ -958,6 +963,17 @@ rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const 
     if (flags & RFG_DEVICE_OUTPUT) {
         spec.out = out;
         return run_batch(qs, ck, spec, dev_in ? nullptr : C->offsets);
+    }
+    if (g.host_stores && nq * nc) {
+        /* pinned host memory mapped into the device's address space: the tiles' coalesced
+         * row segments cross the host link as they are written, no device buffer and no
+         * copy afterwards */
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, out) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer) {
+            spec.out = at.devicePointer;
+            return run_batch(qs, ck, spec, dev_in ? nullptr : C->offsets);
+        }
+        cudaGetLastError();
     }
     RFG_TRY(od.alloc((size_t)nq * ld * esz));
     spec.out = od.p;

@@ -446,3 +446,27 @@ def test_token_set_family_api_names():
             assert G.same(cached(a).similarity(b), exp), (m, a, b)
     with pytest.raises(ValueError):
         R.Multi(R.WRATIO, 8, 1)
+
+
+@pytest.mark.parametrize("metric,op,cut,dt", [("LEVENSHTEIN", "DISTANCE", 8, "I32"), ("INDEL", "NORMALIZED_SIMILARITY", 0.5, "F64"),
+                                              ("JARO_WINKLER", "SIMILARITY", 0.8, "F64"), ("WRATIO", "SIMILARITY", 50.0, "F64")])
+def test_cdist_into_pinned_host_memory(metric, op, cut, dt):
+    """results in pinned host memory: the kernels store them over the host link directly
+    (rows with ld > choices; the padding stays untouched)"""
+    import torch
+    m, o, d = getattr(R, metric), getattr(R, op), getattr(R, dt)
+    rng = random.Random(91)
+    qs = [bytes(_rand(rng, b"abcd ", 0, 70)) for _ in range(37)]
+    cs = [bytes(_rand(rng, b"abcd ", 0, 70)) for _ in range(1500)]
+    q, c = R.pack_strings(qs, 1), R.pack_strings(cs, 1)
+    nc = len(cs)
+    tdt = {R.I32: torch.int32, R.F64: torch.float64}[d]
+    ld = nc + 7
+    host = torch.full((len(qs), ld), -3, dtype=tdt).pin_memory()
+    got = R.cdist(m, o, q, c, cut, out_dtype=d, out=host.numpy(), ld=ld)
+    exp = oracle_cdist(m, o, q, c, cut, out_dtype=d)
+    a = got[:, :nc]
+    if a.dtype == np.float64:
+        a, exp = a.view(np.int64), exp.view(np.int64)
+    assert np.array_equal(a, exp)
+    assert (got[:, nc:] == -3).all()
