@@ -848,14 +848,21 @@ __global__ void __launch_bounds__(256) k_generic(const KParams a)
     u64* keys = rows + (int64_t)(256 + a.hcap + 1) * W;
     u64* st = region + (a.pm_smem ? 0 : table) + (int64_t)threadIdx.x * a.scratch_per_thread;
     __shared__ int64_t s_tile;
+    __shared__ int s_next;
     int64_t cur_q = -1;
     int m = 0;
     const unsigned char* qb = nullptr;
     TopList<TOPK> tl;
     tl.n = 0;
     const int64_t ntiles = (int64_t)a.nq * a.nchunks;
+    /* partial_ratio and the token scorers cost very different amounts per pair: the
+     * threads take the tile's choices one at a time instead of a fixed stride */
+    constexpr bool kDynamic = FAM == FAM_PARTIAL || FAM == FAM_TOKEN;
     for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(a.counter, 1);
+        if (threadIdx.x == 0) {
+            s_tile = atomicAdd(a.counter, 1);
+            s_next = 0;
+        }
         __syncthreads();
         const int64_t t = s_tile;
         if (t >= ntiles) break;
@@ -881,7 +888,11 @@ __global__ void __launch_bounds__(256) k_generic(const KParams a)
         const int64_t c0 = ch * a.chunk;
         const int64_t c1 = c0 + a.chunk < a.c.n ? c0 + a.chunk : a.c.n;
         const bool skip = TOPK && tile_hopeless(a, qi, m, ch);
-        if (!skip)
+        if (!skip && kDynamic)
+            for (int64_t p = c0 + atomicAdd(&s_next, 1); p < c1; p = c0 + atomicAdd(&s_next, 1))
+                score_pair_generic<FAM, CT, TOPK>(a, rows, keys, W, qi, m, qb,
+                                                  a.perm ? (int64_t)__ldg(a.perm + p) : p, st, &tl);
+        else if (!skip)
             for (int64_t p = c0 + threadIdx.x; p < c1; p += blockDim.x)
                 score_pair_generic<FAM, CT, TOPK>(a, rows, keys, W, qi, m, qb,
                                                   a.perm ? (int64_t)__ldg(a.perm + p) : p, st, &tl);
