@@ -284,6 +284,29 @@ rfg_status rfg_multi_score_i64(rfg_multi scorer, rfg_op op, int64_t* scores, siz
 rfg_status rfg_multi_score_f64(rfg_multi scorer, rfg_op op, double* scores, size_t score_count, const void* s2,
                                int64_t len2, int32_t width2, double score_cutoff);
 
+/* ------------------------------------------------------------------ editops
+ * levenshtein_editops (Levenshtein.hpp:282-295), indel_editops (Indel.hpp:65-75) and
+ * lcs_seq_editops (LCSseq.hpp:65-75) of many pairs (s1[i], s2[i]): the operations that
+ * turn s1[i] into s2[i], in the reference's order (EditOp, rapidfuzz/details/types.hpp:
+ * 28-56).  ops[offsets[i], offsets[i + 1]) are pair i's operations; the source / target
+ * lengths of pair i are the lengths of s1[i] / s2[i].  capacity >= sum over the pairs of
+ * max(len1, len2) (Levenshtein) or len1 + len2 (Indel, LCSseq) always suffices; with less,
+ * the call fills offsets and returns RFG_ERR_OUT_OF_RANGE.  score_hint is accepted and
+ * changes no result.  A Levenshtein pair whose strings, past their common prefix and
+ * suffix, are more than 64 x 10 units with 2 m n / 8 >= 1 MB (the reference aligns those
+ * with Hirschberg's algorithm) returns RFG_ERR_INVALID_ARGUMENT. */
+typedef enum { RFG_EDIT_NONE = 0, RFG_EDIT_REPLACE = 1, RFG_EDIT_INSERT = 2, RFG_EDIT_DELETE = 3 } rfg_edit_type;
+
+typedef struct {
+    int32_t type; /* rfg_edit_type */
+    int32_t reserved;
+    int64_t src_pos;
+    int64_t dest_pos;
+} rfg_editop;
+
+rfg_status rfg_editops(rfg_metric metric, const rfg_strings* s1, const rfg_strings* s2, uint64_t score_hint,
+                       rfg_editop* ops, int64_t capacity, int64_t* offsets, uint32_t flags);
+
 #ifdef __cplusplus
 }
 #endif

@@ -345,6 +345,47 @@ extern "C" int rfref_score(int metric, int op, int form, const void* a, int64_t 
     }
 }
 
+/* levenshtein_editops / indel_editops / lcs_seq_editops (Levenshtein.hpp:282-295,
+ * Indel.hpp:65-75, LCSseq.hpp:65-75) of the unmodified headers */
+template <typename C1, typename C2>
+int editops_pair(int metric, const void* a, int64_t la, const void* b, int64_t lb, uint64_t hint, rfo_editop* ops,
+                 int64_t cap, int64_t* count)
+{
+    std::vector<C1> s1((const C1*)a, (const C1*)a + la);
+    std::vector<C2> s2((const C2*)b, (const C2*)b + lb);
+    rapidfuzz::Editops e;
+    if (metric == RFO_LEVENSHTEIN) e = rapidfuzz::levenshtein_editops(s1, s2, (size_t)hint);
+    else if (metric == RFO_INDEL) e = rapidfuzz::indel_editops(s1, s2);
+    else e = rapidfuzz::lcs_seq_editops(s1, s2);
+    *count = (int64_t)e.size();
+    for (size_t k = 0; k < e.size() && (int64_t)k < cap; ++k)
+        ops[k] = rfo_editop{(int32_t)e[k].type, 0, (int64_t)e[k].src_pos, (int64_t)e[k].dest_pos};
+    return (e.get_src_len() == (size_t)la && e.get_dest_len() == (size_t)lb) ? 0 : -3;
+}
+
+template <typename C1>
+int editops_c2(int metric, const void* a, int64_t la, const void* b, int64_t lb, int cb, uint64_t hint,
+               rfo_editop* ops, int64_t cap, int64_t* count)
+{
+    switch (cb) {
+    case 1: return editops_pair<C1, uint8_t>(metric, a, la, b, lb, hint, ops, cap, count);
+    case 2: return editops_pair<C1, uint16_t>(metric, a, la, b, lb, hint, ops, cap, count);
+    case 4: return editops_pair<C1, uint32_t>(metric, a, la, b, lb, hint, ops, cap, count);
+    default: return editops_pair<C1, uint64_t>(metric, a, la, b, lb, hint, ops, cap, count);
+    }
+}
+
+extern "C" int rfref_editops(int metric, const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb,
+                             uint64_t hint, rfo_editop* ops, int64_t cap, int64_t* count)
+{
+    switch (ca) {
+    case 1: return editops_c2<uint8_t>(metric, a, la, b, lb, cb, hint, ops, cap, count);
+    case 2: return editops_c2<uint16_t>(metric, a, la, b, lb, cb, hint, ops, cap, count);
+    case 4: return editops_c2<uint32_t>(metric, a, la, b, lb, cb, hint, ops, cap, count);
+    default: return editops_c2<uint64_t>(metric, a, la, b, lb, cb, hint, ops, cap, count);
+    }
+}
+
 /* Multi* with several inserted strings (padding semantics, result order) */
 extern "C" int rfref_multi(int metric, int op, int max_len, const rfo_strings* inserted, const void* b, int64_t lb,
                            int cb, const rfo_params* p, uint64_t ci, double cf, int64_t* oi, double* of,

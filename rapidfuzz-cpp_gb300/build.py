@@ -16,7 +16,7 @@ PEAK_LIB = os.path.join(LIB_DIR, "librfg_peak.so")  # INT32 issue-rate microbenc
 COUNT_LIB = os.path.join(LIB_DIR, "librfg_count.so")  # executed word steps of the kernels (bench roofline)
 
 SOURCES = ["rfg_api.cu", "rfg_k_lev.cu", "rfg_k_lcs.cu", "rfg_k_osa.cu", "rfg_k_jaro.cu", "rfg_k_generic.cu", "rfg_noalloc.cu", "rfg_server.cu",
-           "rfg_k_token.cu", "rfg_token.cpp"]
+           "rfg_k_token.cu", "rfg_k_editops.cu", "rfg_token.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
          "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]

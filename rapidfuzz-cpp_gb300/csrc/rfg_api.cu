@@ -1979,6 +1979,120 @@ rfg_status rfg_extract(rfg_corpus c, rfg_metric metric, rfg_op op, const rfg_str
     return check_batch(job.pb, g.stream);
 }
 
+/* ----------------------------------------------------------------- editops */
+
+rfg_status rfg_editops(rfg_metric metric, const rfg_strings* S1, const rfg_strings* S2, uint64_t score_hint,
+                       rfg_editop* ops, int64_t capacity, int64_t* offsets, uint32_t flags)
+{
+    (void)score_hint; /* in the regime served here the reference's hint changes no result */
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    if (metric != RFG_LEVENSHTEIN && metric != RFG_INDEL && metric != RFG_LCSSEQ)
+        return fail(RFG_ERR_INVALID_ARGUMENT, "editops exist for Levenshtein, Indel and LCSseq");
+    RFG_TRY(check_strings(S1, "s1"));
+    RFG_TRY(check_strings(S2, "s2"));
+    if (S1->count != S2->count) return fail(RFG_ERR_INVALID_ARGUMENT, "s1 and s2 must hold the same number of strings");
+    if (!offsets) return fail(RFG_ERR_INVALID_ARGUMENT, "offsets is NULL");
+    if (capacity < 0 || (!ops && capacity)) return fail(RFG_ERR_INVALID_ARGUMENT, "invalid ops buffer");
+    RFG_TRY(ensure_ctx());
+    const int64_t np = S1->count;
+    HostStrings h1, h2;
+    rfg_strings a = *S1, b = *S2;
+    if (flags & RFG_DEVICE_INPUTS) {
+        RFG_TRY(download_strings(S1, &h1, "s1"));
+        RFG_TRY(download_strings(S2, &h2, "s2"));
+        a.data = h1.data.data();
+        a.offsets = h1.off.data();
+        b.data = h2.data.data();
+        b.offsets = h2.off.data();
+    }
+    RFG_TRY(check_offsets(a.offsets, np, "s1"));
+    RFG_TRY(check_offsets(b.offsets, np, "s2"));
+    if ((!a.data && np && a.offsets[np] > a.offsets[0]) || (!b.data && np && b.offsets[np] > b.offsets[0]))
+        return fail(RFG_ERR_INVALID_ARGUMENT, "string data is NULL");
+    const bool lev = metric == RFG_LEVENSHTEIN;
+    /* common affixes (remove_common_affix, common_impl.hpp:46-81) and region sizes */
+    std::vector<int64_t> pre(np), suf(np), moff(np + 1, 0), ooff(np + 1, 0);
+    for (int64_t i = 0; i < np; ++i) {
+        const int64_t a0 = a.offsets[i], la = a.offsets[i + 1] - a0, b0 = b.offsets[i], lb = b.offsets[i + 1] - b0;
+        int64_t p = 0;
+        while (p < la && p < lb && unit_at(a.data, a.char_width, a0 + p) == unit_at(b.data, b.char_width, b0 + p)) ++p;
+        int64_t q = 0;
+        while (q < la - p && q < lb - p &&
+               unit_at(a.data, a.char_width, a0 + la - 1 - q) == unit_at(b.data, b.char_width, b0 + lb - 1 - q))
+            ++q;
+        pre[i] = p;
+        suf[i] = q;
+        const int64_t m = la - p - q, n = lb - p - q, W = (m + 63) / 64;
+        if (lev && m >= 65 && n >= 10 && 2 * (uint64_t)m * (uint64_t)n / 8 >= (1u << 20))
+            return fail(RFG_ERR_INVALID_ARGUMENT,
+                        "pair %lld: the reference aligns strings of %lld x %lld units past their common affix with "
+                        "Hirschberg's algorithm, which this library does not run",
+                        (long long)i, (long long)m, (long long)n);
+        moff[i + 1] = moff[i] + (m && n ? (lev ? 2 : 1) * W * n : 0);
+        ooff[i + 1] = ooff[i] + (lev ? std::max(m, n) : m + n);
+    }
+    if (np == 0) {
+        offsets[0] = 0;
+        return RFG_OK;
+    }
+    DBuf da, dao, db, dbo, dpre, dsuf, dmo, doo, dcount, dops, derr;
+    KStrings ka, kb;
+    RFG_TRY(upload_strings(&a, &da, &dao, &ka));
+    RFG_TRY(upload_strings(&b, &db, &dbo, &kb));
+    RFG_TRY(dpre.alloc(np * 8));
+    RFG_TRY(dsuf.alloc(np * 8));
+    RFG_TRY(dmo.alloc((np + 1) * 8));
+    RFG_TRY(doo.alloc((np + 1) * 8));
+    RFG_TRY(dcount.alloc(np * 8));
+    RFG_TRY(dops.alloc((size_t)ooff[np] * sizeof(rfg_editop)));
+    RFG_TRY(derr.alloc(sizeof(int)));
+    RFG_CUDA(cudaMemsetAsync(derr.p, 0, sizeof(int), g.stream));
+    static_assert(sizeof(EditopDev) == sizeof(rfg_editop), "editop layouts");
+    RFG_CUDA(cudaMemcpyAsync(dpre.p, pre.data(), np * 8, cudaMemcpyHostToDevice, g.stream));
+    RFG_CUDA(cudaMemcpyAsync(dsuf.p, suf.data(), np * 8, cudaMemcpyHostToDevice, g.stream));
+    RFG_CUDA(cudaMemcpyAsync(doo.p, ooff.data(), (np + 1) * 8, cudaMemcpyHostToDevice, g.stream));
+    /* launches of pairs whose matrices fit 256M words of scratch together */
+    const int64_t budget = (int64_t)1 << 28;
+    int64_t maxw = 0;
+    for (int64_t i = 0; i < np; ++i) maxw = std::max(maxw, moff[i + 1] - moff[i]);
+    DBuf dmat;
+    RFG_TRY(dmat.alloc((size_t)std::max(maxw, std::min(budget, moff[np])) * 8 + 8));
+    std::vector<int64_t> lmo(np + 1);
+    for (int64_t p0 = 0; p0 < np;) {
+        int64_t p1 = p0 + 1;
+        while (p1 < np && moff[p1 + 1] - moff[p0] <= std::max(budget, maxw)) ++p1;
+        for (int64_t i = p0; i <= p1; ++i) lmo[i] = moff[i] - moff[p0]; /* offsets within this launch */
+        RFG_CUDA(cudaMemcpyAsync(dmo.as<int64_t>() + p0, lmo.data() + p0, (p1 - p0) * 8, cudaMemcpyHostToDevice,
+                                 g.stream));
+        EditopsParams prm{ka,           kb,          dpre.as<int64_t>(),     dsuf.as<int64_t>(),  dmo.as<int64_t>(),
+                          doo.as<int64_t>(), dmat.as<u64>(), dops.as<EditopDev>(), dcount.as<int64_t>(), derr.as<int>(),
+                          p0,           p1 - p0,     lev ? 1 : 0};
+        void* args[] = {&prm};
+        RFG_CUDA(cudaLaunchKernel(editops_kernel(), dim3((unsigned)((p1 - p0 + 127) / 128)), dim3(128), args, 0,
+                                  g.stream));
+        RFG_CUDA(cudaStreamSynchronize(g.stream)); /* the scratch is reused by the next launch */
+        p0 = p1;
+    }
+    std::vector<int64_t> cnt(np);
+    int h_err = 0;
+    RFG_CUDA(cudaMemcpyAsync(cnt.data(), dcount.p, np * 8, cudaMemcpyDeviceToHost, g.stream));
+    RFG_CUDA(cudaMemcpyAsync(&h_err, derr.p, sizeof(int), cudaMemcpyDeviceToHost, g.stream));
+    RFG_CUDA(cudaStreamSynchronize(g.stream));
+    if (h_err) return fail(RFG_ERR_DEVICE_CHECK, "device-side check failed (code %d)", h_err);
+    offsets[0] = 0;
+    for (int64_t i = 0; i < np; ++i) offsets[i + 1] = offsets[i] + cnt[i];
+    if (offsets[np] > capacity)
+        return fail(RFG_ERR_OUT_OF_RANGE, "the editops need %lld slots, capacity is %lld", (long long)offsets[np],
+                    (long long)capacity);
+    std::vector<rfg_editop> all((size_t)ooff[np]);
+    if (!all.empty())
+        RFG_CUDA(cudaMemcpyAsync(all.data(), dops.p, all.size() * sizeof(rfg_editop), cudaMemcpyDeviceToHost, g.stream));
+    RFG_CUDA(cudaStreamSynchronize(g.stream));
+    for (int64_t i = 0; i < np; ++i)
+        if (cnt[i]) memcpy(ops + offsets[i], all.data() + ooff[i], (size_t)cnt[i] * sizeof(rfg_editop));
+    return RFG_OK;
+}
+
 /* --------------------------------------------------------- prepared batches */
 
 static rfg_status batch_reprepare(rfg_batch b, int block, int64_t tiles, int stage = 1)

@@ -88,6 +88,28 @@ struct KParams {
     const int32_t* cparts;
 };
 
+/* editops of many pairs (k_editops): one operation, laid out as rfg_editop */
+struct EditopDev {
+    int32_t type;
+    int32_t reserved;
+    int64_t src_pos;
+    int64_t dest_pos;
+};
+
+struct EditopsParams {
+    KStrings a, b;       /* s1 and s2 of every pair */
+    const int64_t* pre;  /* common prefix length per pair */
+    const int64_t* suf;  /* common suffix length per pair */
+    const int64_t* moff; /* first scratch word of each pair's matrix (within the launch) */
+    const int64_t* ooff; /* first operation slot of each pair's output region */
+    u64* mat;
+    EditopDev* ops;
+    int64_t* count; /* operations per pair */
+    int* err;       /* device-side check flag */
+    int64_t p0, np; /* the pairs of this launch */
+    int lev;        /* 1: Levenshtein, 0: LCSseq / Indel */
+};
+
 /* ----------------------------------------------------------------- helpers */
 
 __device__ __forceinline__ u64 load_unit(const unsigned char* base, int width, int64_t i)

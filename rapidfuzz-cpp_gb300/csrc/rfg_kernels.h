@@ -28,6 +28,8 @@ const void* token_kernel(int width, bool topk);
 const void* topk_merge_kernel();
 /* k_jaro_tables (per-query JaroTab pre-pass) */
 const void* jaro_tables_kernel();
+/* k_editops (editops of many pairs, one thread per pair) */
+const void* editops_kernel();
 /* k_zero_pairs (QRatio's empty-string rule on a device result matrix) */
 const void* zero_pairs_kernel();
 } // namespace rfg

@@ -444,6 +444,88 @@ explicit CachedJaroWinkler(const Sentence1&, double = 0.1)
     -> CachedJaroWinkler<typename std::decay<decltype(*std::begin(std::declval<Sentence1>()))>::type>;
 #endif
 
+/* ------------------------------------------------------------------ editops */
+
+/* rapidfuzz/details/types.hpp:28-56 */
+enum class EditType { None = 0, Replace = 1, Insert = 2, Delete = 3 };
+
+struct EditOp {
+    EditType type = EditType::None;
+    size_t src_pos = 0;
+    size_t dest_pos = 0;
+    EditOp() = default;
+    EditOp(EditType t, size_t s, size_t d) : type(t), src_pos(s), dest_pos(d) {}
+    bool operator==(const EditOp& o) const { return type == o.type && src_pos == o.src_pos && dest_pos == o.dest_pos; }
+    bool operator!=(const EditOp& o) const { return !(*this == o); }
+};
+
+/* the operations plus the source and destination lengths (details/types.hpp:167-...) */
+class Editops : public std::vector<EditOp> {
+public:
+    Editops() = default;
+    size_t get_src_len() const { return src_len_; }
+    size_t get_dest_len() const { return dest_len_; }
+    void set_src_len(size_t n) { src_len_ = n; }
+    void set_dest_len(size_t n) { dest_len_ = n; }
+
+private:
+    size_t src_len_ = 0, dest_len_ = 0;
+};
+
+namespace detail {
+template <typename U1, typename U2>
+Editops editops(rfg_metric m, const U1& a, const U2& b, size_t score_hint)
+{
+    int64_t o1[2] = {0, a.len}, o2[2] = {0, b.len};
+    rfg_strings s1{a.data, o1, 1, a.width}, s2{b.data, o2, 1, b.width};
+    std::vector<rfg_editop> ops((size_t)(a.len + b.len) + 1);
+    int64_t off[2] = {0, 0};
+    throw_on(rfg_editops(m, &s1, &s2, (uint64_t)score_hint, ops.data(), (int64_t)ops.size(), off, 0));
+    Editops e;
+    for (int64_t k = off[0]; k < off[1]; ++k)
+        e.emplace_back((EditType)ops[(size_t)k].type, (size_t)ops[(size_t)k].src_pos, (size_t)ops[(size_t)k].dest_pos);
+    e.set_src_len((size_t)a.len);
+    e.set_dest_len((size_t)b.len);
+    return e;
+}
+} // namespace detail
+
+/* Levenshtein.hpp:282-295 */
+template <typename Sentence1, typename Sentence2>
+Editops levenshtein_editops(const Sentence1& s1, const Sentence2& s2,
+                            size_t score_hint = std::numeric_limits<size_t>::max())
+{
+    return detail::editops(RFG_LEVENSHTEIN, detail::units(s1), detail::units(s2), score_hint);
+}
+template <typename InputIt1, typename InputIt2, detail::if_iter<InputIt1> = 0>
+Editops levenshtein_editops(InputIt1 first1, InputIt1 last1, InputIt2 first2, InputIt2 last2,
+                            size_t score_hint = std::numeric_limits<size_t>::max())
+{
+    return detail::editops(RFG_LEVENSHTEIN, detail::units(first1, last1), detail::units(first2, last2), score_hint);
+}
+
+/* Indel.hpp:65-75, LCSseq.hpp:65-75 */
+template <typename Sentence1, typename Sentence2>
+Editops indel_editops(const Sentence1& s1, const Sentence2& s2)
+{
+    return detail::editops(RFG_INDEL, detail::units(s1), detail::units(s2), 0);
+}
+template <typename InputIt1, typename InputIt2, detail::if_iter<InputIt1> = 0>
+Editops indel_editops(InputIt1 first1, InputIt1 last1, InputIt2 first2, InputIt2 last2)
+{
+    return detail::editops(RFG_INDEL, detail::units(first1, last1), detail::units(first2, last2), 0);
+}
+template <typename Sentence1, typename Sentence2>
+Editops lcs_seq_editops(const Sentence1& s1, const Sentence2& s2)
+{
+    return detail::editops(RFG_LCSSEQ, detail::units(s1), detail::units(s2), 0);
+}
+template <typename InputIt1, typename InputIt2, detail::if_iter<InputIt1> = 0>
+Editops lcs_seq_editops(InputIt1 first1, InputIt1 last1, InputIt2 first2, InputIt2 last2)
+{
+    return detail::editops(RFG_LCSSEQ, detail::units(first1, last1), detail::units(first2, last2), 0);
+}
+
 /* --------------------------------------------------------------------- fuzz */
 
 namespace fuzz {

@@ -11,5 +11,6 @@ from ._lib import (DISTANCE, SIMILARITY, NORMALIZED_DISTANCE, NORMALIZED_SIMILAR
                    PARTIAL_TOKEN_SET_RATIO, TOKEN_RATIO, PARTIAL_TOKEN_RATIO, WRATIO,
                    FORM_FREE, FORM_CACHED, FORM_MULTI, I32, I64, F64,
                    DEVICE_INPUTS, DEVICE_OUTPUT, RapidfuzzError, lib, lib_path,
-                   as_units, pack_strings, score, Cached, Multi, cdist, Batch, library_stream, Corpus, Server)
+                   as_units, pack_strings, score, Cached, Multi, cdist, Batch, library_stream, Corpus, Server,
+                   editops_many, EDITOP_DTYPE)
 from ._api import *  # noqa: F401,F403

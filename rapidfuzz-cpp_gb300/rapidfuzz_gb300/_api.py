@@ -3,7 +3,7 @@
 from ._lib import (DISTANCE, SIMILARITY, NORMALIZED_DISTANCE, NORMALIZED_SIMILARITY, LEVENSHTEIN, INDEL, LCSSEQ,
                    OSA, JARO, JARO_WINKLER, RATIO, PARTIAL_RATIO, TOKEN_SORT_RATIO, PARTIAL_TOKEN_SORT_RATIO,
                    QRATIO, TOKEN_SET_RATIO, PARTIAL_TOKEN_SET_RATIO, TOKEN_RATIO, PARTIAL_TOKEN_RATIO, WRATIO, Cached,
-                   Multi, score)
+                   Multi, score, editops_many)
 
 __all__ = []
 
@@ -210,3 +210,59 @@ class experimental:
 
 
 __all__.append("experimental")
+
+
+
+class EditOp(tuple):
+    """rapidfuzz::EditOp (details/types.hpp:45-56): (type, src_pos, dest_pos), type one of
+    'none', 'replace', 'insert', 'delete'"""
+    __slots__ = ()
+    _names = ("none", "replace", "insert", "delete")
+
+    def __new__(cls, t, src, dest):
+        return tuple.__new__(cls, (cls._names[t], int(src), int(dest)))
+
+    type = property(lambda self: self[0])
+    src_pos = property(lambda self: self[1])
+    dest_pos = property(lambda self: self[2])
+
+
+class Editops(list):
+    """rapidfuzz::Editops (details/types.hpp:167-...): the operations plus the lengths of
+    the source and destination strings"""
+
+    def __init__(self, ops, src_len, dest_len):
+        super().__init__(ops)
+        self.src_len = src_len
+        self.dest_len = dest_len
+
+    def get_src_len(self):
+        return self.src_len
+
+    def get_dest_len(self):
+        return self.dest_len
+
+
+def _editops(metric, s1, s2, score_hint=None):
+    from ._lib import as_units
+    a, b = as_units(s1), as_units(s2)
+    e = editops_many(metric, [a], [b], score_hint)[0]
+    return Editops([EditOp(int(x["type"]), x["src_pos"], x["dest_pos"]) for x in e], a.size, b.size)
+
+
+def levenshtein_editops(s1, s2, score_hint=None):
+    """levenshtein_editops (Levenshtein.hpp:282-295)"""
+    return _editops(LEVENSHTEIN, s1, s2, score_hint)
+
+
+def indel_editops(s1, s2):
+    """indel_editops (Indel.hpp:65-75)"""
+    return _editops(INDEL, s1, s2)
+
+
+def lcs_seq_editops(s1, s2):
+    """lcs_seq_editops (LCSseq.hpp:65-75)"""
+    return _editops(LCSSEQ, s1, s2)
+
+
+__all__ += ["EditOp", "Editops", "levenshtein_editops", "indel_editops", "lcs_seq_editops"]

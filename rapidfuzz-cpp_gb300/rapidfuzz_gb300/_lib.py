@@ -111,6 +111,7 @@ def lib():
             "rfg_server_destroy": ([vp], ctypes.c_int),
             "rfg_cdist_noalloc": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, P(Strings), P(Strings), i64, P(Params),
                                    Cutoff, ctypes.c_int, vp, i64, vp], ctypes.c_int),
+            "rfg_editops": ([ctypes.c_int, P(Strings), P(Strings), u64, vp, i64, vp, ctypes.c_uint32], ctypes.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -443,3 +444,21 @@ class Server:
     def __del__(self):
         if _lib is not None:
             self.close()
+
+
+EDITOP_DTYPE = np.dtype([("type", np.int32), ("reserved", np.int32), ("src_pos", np.int64), ("dest_pos", np.int64)])
+
+
+def editops_many(metric, s1s, s2s, score_hint=None):
+    """rfg_editops: editops of the pairs (s1s[i], s2s[i]) -> list of structured arrays
+    (type, src_pos, dest_pos), one per pair"""
+    p1 = s1s if isinstance(s1s, tuple) else pack_strings(s1s)
+    p2 = s2s if isinstance(s2s, tuple) else pack_strings(s2s)
+    a, b = _batch(p1), _batch(p2)
+    cap = int(p1[1][-1] - p1[1][0] + p2[1][-1] - p2[1][0])
+    ops = np.zeros(max(cap, 1), dtype=EDITOP_DTYPE)
+    offsets = np.zeros(a.count + 1, dtype=np.int64)
+    hint = 2**64 - 1 if score_hint is None else int(score_hint)
+    check(lib().rfg_editops(metric, ctypes.byref(a), ctypes.byref(b), hint, ops.ctypes.data, cap,
+                            offsets.ctypes.data, 0))
+    return [ops[offsets[i]:offsets[i + 1]] for i in range(a.count)]

@@ -129,6 +129,25 @@ int main()
         mq.similarity(r.data(), r.size(), std::string(""));
         CHECK(r[0] == 0.0 && r[1] == 0.0);
     }
+    // editops (tests-Levenshtein.cpp:235-244): applying the operations turns s into d
+    {
+        const std::string s = "Lorem ipsum.", d = "XYZLorem ABC iPsum";
+        rapidfuzz::Editops ops = rapidfuzz::levenshtein_editops(s, d);
+        CHECK(ops.get_src_len() == s.size() && ops.get_dest_len() == d.size());
+        std::string r;
+        size_t sp = 0;
+        for (const auto& op : ops) { /* apply in order (editops_apply_str, distance.hpp:19-60) */
+            while (sp < op.src_pos) r += s[sp++];
+            if (op.type == rapidfuzz::EditType::Insert) r += d[op.dest_pos];
+            else if (op.type == rapidfuzz::EditType::Replace) { r += d[op.dest_pos]; ++sp; }
+            else if (op.type == rapidfuzz::EditType::Delete) ++sp;
+        }
+        while (sp < s.size()) r += s[sp++];
+        CHECK(r == d);
+        CHECK(rapidfuzz::indel_editops(std::string("kitten"), std::string("sitting")).size() == 5);
+        CHECK(rapidfuzz::lcs_seq_editops(std::string("kitten"), std::string("sitting")).size() == 5);
+        CHECK(rapidfuzz::levenshtein_editops(std::string("kitten"), std::string("sitting")).size() == 3);
+    }
     // token_set_ratio family (tests-fuzz.cpp:48-137)
     {
         const std::string s1 = "new york mets", s3 = "the wonderful new york mets";

@@ -11,7 +11,8 @@ Fixtures:
                 seeded random pairs;
   tokens.json   token_sort_ratio / partial_token_sort_ratio / QRatio (free and Cached forms);
   tokenset.json token_set_ratio / partial_token_set_ratio / token_ratio / partial_token_ratio /
-                WRatio (free and Cached forms).
+                WRatio (free and Cached forms);
+  editops.json  levenshtein_editops / indel_editops / lcs_seq_editops.
 Doubles are stored with float.hex() so the comparison is bit-exact.
 
 Usage: python tests/golden/make_golden.py   (needs the reference checkout; run in the
@@ -457,12 +458,67 @@ def tokenset_cases(seed=17):
     return [c for c in out if c is not None]
 
 
+def literals_in(path, first, last):
+    """the string literals of lines first..last of a reference test file"""
+    import re
+    lines = open(os.path.join(REF_ROOT, path), encoding="utf-8").read().split("\n")[first - 1:last]
+    return [bytes(m, "utf-8").decode("unicode_escape") for m in re.findall(r'"((?:[^"\\]|\\.)*)"', "\n".join(lines))]
+
+
+def editops_cases(seed=19):
+    """levenshtein_editops / indel_editops / lcs_seq_editops of the reference itself: the
+    string literals of its editops tests (test/distance/tests-Levenshtein.cpp:235-320)
+    paired with each other and repeated, then seeded random pairs (copies with edits,
+    unrelated strings; every char width; lengths 0..600; score hints none / 0 / 50)."""
+    from oracle_lib import editops as eops, oracle
+    ref, o = reference(), oracle()
+    T = "test/distance/tests-Levenshtein.cpp"
+    out = []
+
+    def add(metric, a, b, w, hint=None, cite=None):
+        a, b = as_units(a, w), as_units(b, w)
+        if eops(o.rfo_editops, metric, a, b) is None:
+            return  # the Hirschberg regime: not served
+        exp = eops(ref.rfref_editops, metric, a, b, hint)
+        d = {"metric": metric, "s1": [int(x) for x in a], "s2": [int(x) for x in b], "w": int(a.itemsize),
+             "hint": hint, "expected": [list(x) for x in exp]}
+        if cite:
+            d["cite"] = cite
+        out.append(d)
+    lits = literals_in(T, 235, 320)
+    for i, x in enumerate(lits):
+        for y in (lits[(i + 1) % len(lits)], x * 3, lits[(i + 2) % len(lits)] * 5):
+            for metric in (LEVENSHTEIN, INDEL, LCSSEQ):
+                add(metric, x, y, 1, cite=T + ":235-320")
+    rng = random.Random(seed)
+    while len(out) < 3000:
+        w = rng.choice([1, 2, 4])
+        alpha = rng.choice([[97, 98], [97, 98, 99, 100], list(range(97, 123))]) + ([300, 70000] if w == 4 else [])
+        la = rng.choice([0, 1, 5, 20, 63, 64, 65, 130, 300, 600])
+        a = [rng.choice(alpha) for _ in range(rng.randint(0, la))]
+        b = list(a)
+        for _ in range(rng.choice([rng.randint(0, 5), rng.randint(0, 80)])):
+            k = rng.random()
+            if k < 0.3 and b:
+                b[rng.randrange(len(b))] = rng.choice(alpha)
+            elif k < 0.6:
+                b.insert(rng.randint(0, len(b)), rng.choice(alpha))
+            elif b:
+                del b[rng.randrange(len(b))]
+        if rng.random() < 0.25:
+            b = [rng.choice(alpha) for _ in range(rng.randint(0, la + 10))]
+        add(rng.choice([LEVENSHTEIN, INDEL, LCSSEQ]), a, b, w, rng.choice([None, 0, 50]))
+    return out
+
+
 def main():
     if reference() is None:
         sys.exit("oracle/_ref/librfref.so is missing: run `make -C oracle ref` where the reference checkout exists")
-    which = sys.argv[1:] or ["kat.json", "random.json", "multi.json", "partial.json", "tokens.json", "tokenset.json"]
+    which = sys.argv[1:] or ["kat.json", "random.json", "multi.json", "partial.json", "tokens.json", "tokenset.json",
+                             "editops.json"]
     gens = {"kat.json": kat_cases, "random.json": lambda: random_cases(4000), "multi.json": multi_cases,
-            "partial.json": partial_cases, "tokens.json": token_cases, "tokenset.json": tokenset_cases}
+            "partial.json": partial_cases, "tokens.json": token_cases, "tokenset.json": tokenset_cases,
+            "editops.json": editops_cases}
     for name, cases in ((n, gens[n]()) for n in which):
         with open(os.path.join(HERE, name), "w") as f:
             json.dump(cases, f, separators=(",", ":"))

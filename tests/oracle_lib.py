@@ -73,12 +73,36 @@ def oracle():
             f = getattr(lib, name)
             f.restype = None
             f.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int] * 2 + [ctypes.POINTER(ctypes.c_int64)] * 2
+        lib.rfo_editops.restype = ctypes.c_int
         lib.rfo_cdist.restype = ctypes.c_int
         lib.rfo_cdist.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(Strings), ctypes.POINTER(Strings),
                                   ctypes.POINTER(Params), ctypes.c_uint64, ctypes.c_double, ctypes.c_int,
                                   ctypes.c_void_p, ctypes.c_int]
         _oracle = lib
     return _oracle
+
+
+class EditOp(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("reserved", ctypes.c_int32), ("src_pos", ctypes.c_int64),
+                ("dest_pos", ctypes.c_int64)]
+
+
+def editops(lib_fn, metric, s1, s2, score_hint=None):
+    """rfo_editops / rfref_editops of one pair -> [(type, src_pos, dest_pos), ...], or None
+    where the oracle leaves the pair out (the reference's Hirschberg regime)"""
+    a, b = as_units(s1), as_units(s2)
+    cap = a.size + b.size + 1
+    ops = (EditOp * cap)()
+    cnt = ctypes.c_int64()
+    args = [metric, _ptr(a), a.size, a.itemsize, _ptr(b), b.size, b.itemsize]
+    if lib_fn.__name__ == "rfref_editops":
+        args.append(ctypes.c_uint64(2**64 - 1 if score_hint is None else score_hint))
+    rc = lib_fn(*args, ops, cap, ctypes.byref(cnt))
+    if rc == -2:
+        return None
+    if rc != 0:
+        raise ValueError("editops rejected (%d)" % rc)
+    return [(ops[k].type, ops[k].src_pos, ops[k].dest_pos) for k in range(cnt.value)]
 
 
 def reference():
@@ -95,6 +119,7 @@ def reference():
                                     ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(Params),
                                     ctypes.c_uint64, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.POINTER(ctypes.c_int64)]
+        lib.rfref_editops.restype = ctypes.c_int
         _ref = lib
     return _ref
 

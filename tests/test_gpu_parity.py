@@ -470,3 +470,40 @@ def test_cdist_into_pinned_host_memory(metric, op, cut, dt):
         a, exp = a.view(np.int64), exp.view(np.int64)
     assert np.array_equal(a, exp)
     assert (got[:, nc:] == -3).all()
+
+
+
+def test_editops_fixture_batched():
+    """levenshtein_editops / indel_editops / lcs_seq_editops of every fixture pair, the
+    pairs of one metric and width in one rfg_editops call (one thread per pair)"""
+    cases = G.load("editops.json")
+    groups = {}
+    for c in cases:
+        groups.setdefault((c["metric"], c["w"]), []).append(c)
+    for (metric, w), cs in groups.items():
+        dt = {1: np.uint8, 2: np.uint16, 4: np.uint32}[w]
+        a = R.pack_strings([np.array(c["s1"], dtype=dt) for c in cs], w)
+        b = R.pack_strings([np.array(c["s2"], dtype=dt) for c in cs], w)
+        got = R.editops_many(metric, a, b)
+        for c, g in zip(cs, got):
+            assert [tuple(int(v) for v in x) for x in g[["type", "src_pos", "dest_pos"]].tolist()] == \
+                [tuple(x) for x in c["expected"]], (metric, w, c.get("cite"), len(c["s1"]), len(c["s2"]))
+
+
+def test_editops_api_names():
+    """levenshtein_editops (with a score hint), indel_editops, lcs_seq_editops; the
+    Hirschberg regime is refused"""
+    from oracle_lib import editops
+    o = oracle()
+    for a, b in (("Lorem ipsum.", "XYZLorem ABC iPsum"), ("", "abc"), ("abc", ""), ("", ""), ("aa", "abb"),
+                 ("kitten", "sitting"), ("a" * 70 + "xyz", "b" + "a" * 70 + "xz")):
+        for metric, fn in ((R.LEVENSHTEIN, R.levenshtein_editops), (R.INDEL, R.indel_editops),
+                           (R.LCSSEQ, R.lcs_seq_editops)):
+            exp = editops(o.rfo_editops, metric, a.encode(), b.encode())
+            e = fn(a, b)
+            assert [(["none", "replace", "insert", "delete"].index(x.type), x.src_pos, x.dest_pos) for x in e] == exp
+            assert e.get_src_len() == len(a) and e.get_dest_len() == len(b)
+    assert len(R.levenshtein_editops("kitten", "sitting", 5)) == 3
+    with pytest.raises(ValueError):
+        R.levenshtein_editops("ab" * 1100, "ba" * 1100)
+    assert len(R.indel_editops("ab" * 1100, "ba" * 1100)) == 2

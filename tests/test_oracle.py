@@ -25,6 +25,21 @@ def test_oracle_matches_reference_fixtures(fixture):
     assert not bad, "%d mismatches, first: %r" % (len(bad), bad[:2])
 
 
+def _eo_arrays(c):
+    dt = {1: np.uint8, 2: np.uint16, 4: np.uint32}[c["w"]]
+    return np.array(c["s1"], dtype=dt), np.array(c["s2"], dtype=dt)
+
+
+def test_oracle_editops_fixture():
+    """editops of the DP-table restatement equal the reference's (editops.json)"""
+    from oracle_lib import editops
+    o = oracle()
+    for c in G.load("editops.json"):
+        a, b = _eo_arrays(c)
+        got = editops(o.rfo_editops, c["metric"], a, b)
+        assert got == [tuple(x) for x in c["expected"]], (c.get("cite"), c["metric"], len(a), len(b))
+
+
 def test_oracle_multi_batches():
     """each element of a Multi* batch equals the single-pattern Multi chain"""
     o = oracle()
