@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape (fixed launch list)")
     ap.add_argument("--nq", type=int, default=4096)
     ap.add_argument("--nc", type=int, default=4096)
-    ap.add_argument("--workload", default="cdist", choices=["cdist", "cfg1", "cfg3", "cfg4", "cfg5", "partial", "tokens"],
+    ap.add_argument("--workload", default="cdist", choices=["cdist", "cfg1", "cfg3", "cfg4", "cfg5", "partial", "tokens", "editops"],
                     help="cdist: 4096x4096 Zipf a-z Lev/Indel/OSA (the headline); cfg1: 1 x 100k DNA per-call "
                          "vs batched; cfg3: 256 x 65536 long DNA banded; cfg4: 1024 x 1M uint32 JW + ratio; "
                          "cfg5: serving, Poisson extract/extractOne requests over 10M DNA + 1M token strings")

@@ -14,6 +14,7 @@ partial  fuzz::partial_ratio (cutoff 80) of 256 token queries against 200,000 to
       (uint32, as in cfg4), dense float64 out on the device (the first widening of the path).
 tokens   token_sort_ratio, QRatio, WRatio and token_set_ratio (cutoff 80), 256 x 200,000 token
       strings, host inputs and host results through rfg_cdist (joins / parts on the host threads).
+editops  levenshtein_editops of 200,000 DNA pairs (len U[8,64], 0-5 edits) through rfg_editops.
 cfg5  serving: device-resident corpora of 10,000,000 DNA strings (len U[10,200]) and
       1,000,000 uint32 token strings; Poisson arrivals (--rate req/s for --duration s), each
       an extractOne (limit 1) or top-10 extract of one query of length U[5,500] with a metric
@@ -209,6 +210,56 @@ def run(args, rank, world, local):
                      "e2e": {"value": nq * nc / t, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
                              "d2h_bytes_per_step": nq * nc * 8},
                      "gpu_launches": None, "clocks": clk})
+    elif args.workload == "editops":
+        from oracle_lib import editops as oracle_editops, oracle
+        npairs = args.nc if args.nc != 4096 else 200000
+        a = WL.dna_uniform(seed=51, n=npairs)
+        rng = np.random.default_rng(52)
+        b_strs = []
+        for i in range(npairs):
+            s = bytearray(a[0][a[1][i]:a[1][i + 1]].tobytes())
+            for _ in range(int(rng.integers(0, 6))):
+                k = int(rng.integers(0, 3))
+                pos = int(rng.integers(0, len(s) + 1))
+                if k == 0 and pos < len(s):
+                    s[pos] = b"ACGT"[int(rng.integers(0, 4))]
+                elif k == 1:
+                    s.insert(pos, b"ACGT"[int(rng.integers(0, 4))])
+                elif pos < len(s):
+                    del s[pos]
+            b_strs.append(bytes(s))
+        b = R.pack_strings(b_strs, 1)
+        clocks = B.ClockSampler()
+        clocks.start()
+        for _ in range(warmup):
+            got = R.editops_many(R.LEVENSHTEIN, a, b)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            got = R.editops_many(R.LEVENSHTEIN, a, b)
+        t = (time.perf_counter() - t0) / steps
+        clk = clocks.stop(torch.cuda.current_device())
+        o = oracle()
+        for i in (0, 1, npairs // 2, npairs - 1):
+            x = a[0][a[1][i]:a[1][i + 1]]
+            y = b[0][b[1][i]:b[1][i + 1]]
+            assert [tuple(int(v) for v in r) for r in got[i][["type", "src_pos", "dest_pos"]].tolist()] == \
+                oracle_editops(o.rfo_editops, R.LEVENSHTEIN, x, y), "editops parity"
+        sub = 2000
+        tc0 = time.perf_counter()
+        for i in range(sub):
+            oracle_editops(o.rfo_editops, R.LEVENSHTEIN, a[0][a[1][i]:a[1][i + 1]], b[0][b[1][i]:b[1][i + 1]])
+        tc = time.perf_counter() - tc0
+        nops = sum(len(g) for g in got)
+        line.update({"value": npairs / t, "unit": "pairs/s", "ms_per_step": t * 1e3, "dtype": "u64",
+                     "config": {"workload": "levenshtein_editops of %d DNA pairs, s1 len U[8,64], s2 = s1 with 0-5 "
+                                            "edits, host buffers in and out through rfg_editops" % npairs,
+                                "operations_per_step": nops},
+                     "cpu_baseline": {"value": sub / tc, "unit": "pairs/s", "cores": 1, "kind": "port",
+                                      "sample": "2,000 pairs through the oracle's DP restatement, one thread"},
+                     "e2e": {"value": npairs / t, "unit": "pairs/s",
+                             "h2d_bytes_per_step": int(a[0].nbytes + a[1].nbytes + b[0].nbytes + b[1].nbytes),
+                             "d2h_bytes_per_step": int(nops * 24 + npairs * 8)},
+                     "gpu_launches": 1, "clocks": clk})
     elif args.workload == "partial":
         nq = 256
         nc = args.nc if args.nc != 4096 else 200000
