@@ -249,7 +249,7 @@ def run(args, rank, world, local):
         for i in range(sub):
             oracle_editops(o.rfo_editops, R.LEVENSHTEIN, a[0][a[1][i]:a[1][i + 1]], b[0][b[1][i]:b[1][i + 1]])
         tc = time.perf_counter() - tc0
-        nops = sum(len(g) for g in got)
+        nops = int(got.offsets[-1])
         line.update({"value": npairs / t, "unit": "pairs/s", "ms_per_step": t * 1e3, "dtype": "u64",
                      "config": {"workload": "levenshtein_editops of %d DNA pairs, s1 len U[8,64], s2 = s1 with 0-5 "
                                             "edits, host buffers in and out through rfg_editops" % npairs,

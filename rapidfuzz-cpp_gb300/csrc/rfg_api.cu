@@ -2084,12 +2084,22 @@ rfg_status rfg_editops(rfg_metric metric, const rfg_strings* S1, const rfg_strin
     if (offsets[np] > capacity)
         return fail(RFG_ERR_OUT_OF_RANGE, "the editops need %lld slots, capacity is %lld", (long long)offsets[np],
                     (long long)capacity);
-    std::vector<rfg_editop> all((size_t)ooff[np]);
-    if (!all.empty())
-        RFG_CUDA(cudaMemcpyAsync(all.data(), dops.p, all.size() * sizeof(rfg_editop), cudaMemcpyDeviceToHost, g.stream));
+    if (offsets[np] == 0) return RFG_OK;
+    /* pack on the device, then one copy of exactly the operations */
+    DBuf doff, dpacked;
+    RFG_TRY(doff.alloc((np + 1) * 8));
+    RFG_TRY(dpacked.alloc((size_t)offsets[np] * sizeof(rfg_editop)));
+    RFG_CUDA(cudaMemcpyAsync(doff.p, offsets, (np + 1) * 8, cudaMemcpyHostToDevice, g.stream));
+    const EditopDev* src = dops.as<EditopDev>();
+    const int64_t* po = doo.as<int64_t>();
+    const int64_t* pf = doff.as<int64_t>();
+    EditopDev* dst = dpacked.as<EditopDev>();
+    void* pargs[] = {(void*)&src, (void*)&po, (void*)&pf, (void*)&dst, (void*)&np};
+    RFG_CUDA(cudaLaunchKernel(editops_pack_kernel(), dim3((unsigned)((np + 127) / 128)), dim3(128), pargs, 0,
+                              g.stream));
+    RFG_CUDA(cudaMemcpyAsync(ops, dpacked.p, (size_t)offsets[np] * sizeof(rfg_editop), cudaMemcpyDeviceToHost,
+                             g.stream));
     RFG_CUDA(cudaStreamSynchronize(g.stream));
-    for (int64_t i = 0; i < np; ++i)
-        if (cnt[i]) memcpy(ops + offsets[i], all.data() + ooff[i], (size_t)cnt[i] * sizeof(rfg_editop));
     return RFG_OK;
 }
 

@@ -122,6 +122,17 @@ __global__ void __launch_bounds__(128) k_editops(const EditopsParams P)
     }
 }
 
+/* pair i's operations from its region at ooff[i] to dst[off[i], off[i + 1]) */
+__global__ void __launch_bounds__(128) k_editops_pack(const EditopDev* src, const int64_t* ooff, const int64_t* off,
+                                                      EditopDev* dst, int64_t np)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    const int64_t n = off[i + 1] - off[i];
+    for (int64_t k = 0; k < n; ++k) dst[off[i] + k] = src[ooff[i] + k];
+}
+
 const void* editops_kernel() { return (const void*)&k_editops; }
+const void* editops_pack_kernel() { return (const void*)&k_editops_pack; }
 
 } // namespace rfg

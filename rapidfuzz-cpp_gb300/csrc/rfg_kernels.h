@@ -30,6 +30,8 @@ const void* topk_merge_kernel();
 const void* jaro_tables_kernel();
 /* k_editops (editops of many pairs, one thread per pair) */
 const void* editops_kernel();
+/* k_editops_pack (the pairs' operations, packed) */
+const void* editops_pack_kernel();
 /* k_zero_pairs (QRatio's empty-string rule on a device result matrix) */
 const void* zero_pairs_kernel();
 } // namespace rfg

@@ -449,9 +449,29 @@ class Server:
 EDITOP_DTYPE = np.dtype([("type", np.int32), ("reserved", np.int32), ("src_pos", np.int64), ("dest_pos", np.int64)])
 
 
+class EditopsBatch:
+    """the operations of many pairs: ops (structured array type / src_pos / dest_pos),
+    offsets (pair i owns ops[offsets[i]:offsets[i + 1]]); indexing gives one pair's slice"""
+
+    def __init__(self, ops, offsets):
+        self.ops = ops
+        self.offsets = offsets
+
+    def __len__(self):
+        return self.offsets.size - 1
+
+    def __getitem__(self, i):
+        if not -len(self) <= i < len(self):
+            raise IndexError(i)
+        i %= len(self)
+        return self.ops[self.offsets[i]:self.offsets[i + 1]]
+
+    def __iter__(self):
+        return (self[i] for i in range(len(self)))
+
+
 def editops_many(metric, s1s, s2s, score_hint=None):
-    """rfg_editops: editops of the pairs (s1s[i], s2s[i]) -> list of structured arrays
-    (type, src_pos, dest_pos), one per pair"""
+    """rfg_editops: editops of the pairs (s1s[i], s2s[i]) -> EditopsBatch"""
     p1 = s1s if isinstance(s1s, tuple) else pack_strings(s1s)
     p2 = s2s if isinstance(s2s, tuple) else pack_strings(s2s)
     a, b = _batch(p1), _batch(p2)
@@ -461,4 +481,4 @@ def editops_many(metric, s1s, s2s, score_hint=None):
     hint = 2**64 - 1 if score_hint is None else int(score_hint)
     check(lib().rfg_editops(metric, ctypes.byref(a), ctypes.byref(b), hint, ops.ctypes.data, cap,
                             offsets.ctypes.data, 0))
-    return [ops[offsets[i]:offsets[i + 1]] for i in range(a.count)]
+    return EditopsBatch(ops[:offsets[-1]], offsets)
