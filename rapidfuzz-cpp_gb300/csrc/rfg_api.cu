@@ -81,6 +81,11 @@ struct Ctx {
     unsigned char* stage_h = nullptr;
     size_t stage_slot = 0;
     cudaEvent_t stage_ev[2] = {};
+    /* pinned staging of a preparation's small host tables (one copy per preparation);
+     * up_ev marks the end of the last copy out of it */
+    unsigned char* up_h = nullptr;
+    size_t up_cap = 0;
+    cudaEvent_t up_ev = nullptr;
     /* host results in pinned, mapped memory are stored by the kernels themselves over the
      * host link (RFG_HOST_STORES=0 in the environment copies them from a device buffer) */
     bool host_stores = true;
@@ -104,12 +109,29 @@ rfg_status ensure_ctx()
     for (auto& e : g.blk_ev) RFG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     RFG_CUDA(cudaEventCreateWithFlags(&g.prep_ev, cudaEventDisableTiming));
     for (auto& e : g.stage_ev) RFG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    RFG_CUDA(cudaEventCreateWithFlags(&g.up_ev, cudaEventDisableTiming));
     if (const char* hs = getenv("RFG_HOST_STORES")) g.host_stores = atoi(hs) != 0;
     cudaMemPool_t pool;
     RFG_CUDA(cudaDeviceGetDefaultMemPool(&pool, g.device));
     uint64_t thr = UINT64_MAX;
     RFG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
     g.init = true;
+    return RFG_OK;
+}
+
+/* the pinned staging of small uploads, at least `bytes` long, free of in-flight copies */
+rfg_status upload_stage(size_t bytes, unsigned char** h)
+{
+    RFG_CUDA(cudaEventSynchronize(g.up_ev));
+    if (bytes > g.up_cap) {
+        if (g.up_h) cudaFreeHost(g.up_h);
+        g.up_h = nullptr;
+        g.up_cap = 0;
+        const size_t cap = std::max<size_t>(bytes, 1u << 20);
+        RFG_CUDA(cudaHostAlloc((void**)&g.up_h, cap, cudaHostAllocDefault));
+        g.up_cap = cap;
+    }
+    *h = g.up_h;
     return RFG_OK;
 }
 
@@ -369,7 +391,13 @@ struct LaunchRec {
 
 struct Prepared {
     std::vector<LaunchRec> launches;
-    DBuf qlist, small, scratch[1], perm, poff, plen, jtab;
+    DBuf packed, small, scratch[1], jtab;
+    /* in `packed` (one upload): the query lists of the classes, the choice visiting order
+     * and the choices' offsets and lengths in that order (these two: dense results only) */
+    const int32_t* qlist = nullptr;
+    const int32_t* perm = nullptr;
+    const int64_t* poff = nullptr;
+    const int32_t* plen = nullptr;
     bool has_pre = false; /* pre.a / grid: the per-query table pass before the row blocks */
     KParams pre;
     int* counters = nullptr;
@@ -394,8 +422,7 @@ struct Prepared {
     }
     void free_on(cudaStream_t st)
     {
-        qlist.free_on = small.free_on = scratch[0].free_on = perm.free_on = poff.free_on = plen.free_on =
-            jtab.free_on = st;
+        packed.free_on = small.free_on = scratch[0].free_on = jtab.free_on = st;
     }
 };
 
@@ -514,8 +541,6 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         cls_off[bk] = qall.size();
         qall.insert(qall.end(), cls[bk].begin(), cls[bk].end());
     }
-    RFG_TRY(pb->qlist.alloc(qall.size() * 4));
-    RFG_CUDA(cudaMemcpyAsync(pb->qlist.p, qall.data(), qall.size() * 4, cudaMemcpyHostToDevice, g.stream));
 
     /* one chunking of the choices for every class, each chunk visited in length order */
     int64_t chunk;
@@ -536,7 +561,9 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
     const bool jaro_ok = fam == FAM_JARO && spec.form != RFG_FORM_MULTI;
     const bool mq_ok = (fast_ok || norm_ok || jaro_ok) && spec.topk == 0 && !spec.fixed_perm && g_stage_mode != 0 &&
                        g_mq_mode != 0;
-    const int32_t* dperm;
+    const int32_t* dperm = nullptr;
+    std::vector<int32_t> perm, pl;
+    std::vector<int64_t> po;
     if (spec.fixed_perm) {
         chunk = spec.fixed_chunk;
         dperm = spec.fixed_perm;
@@ -555,30 +582,48 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             if (chunk > cap) chunk = (chunk + cap - 1) / cap * cap;
             stage = std::min(chunk, cap);
         }
-        std::vector<int32_t> clen, perm;
+        std::vector<int32_t> clen;
         std::vector<int64_t> off_tmp;
         RFG_TRY(choice_lengths(c, host_choice_off, &clen, &off_tmp));
         const int64_t* hoff = host_choice_off ? host_choice_off : off_tmp.data();
         for (int32_t l : clen) host_max_choice_len = std::max<int64_t>(host_max_choice_len, l);
         chunk_length_order(clen, stage ? stage : chunk, &perm);
-        RFG_TRY(pb->perm.alloc((size_t)nc * 4));
-        RFG_CUDA(cudaMemcpyAsync(pb->perm.p, perm.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, g.stream));
         if (spec.topk == 0) {
             /* offsets and lengths in visiting order */
-            std::vector<int64_t> po(nc);
-            std::vector<int32_t> pl(nc);
+            po.resize(nc);
+            pl.resize(nc);
             for (int64_t i = 0; i < nc; ++i) {
                 po[i] = hoff[perm[i]];
                 pl[i] = clen[perm[i]];
             }
-            RFG_TRY(pb->poff.alloc((size_t)nc * 8));
-            RFG_TRY(pb->plen.alloc((size_t)nc * 4));
-            RFG_CUDA(cudaMemcpyAsync(pb->poff.p, po.data(), (size_t)nc * 8, cudaMemcpyHostToDevice, g.stream));
-            RFG_CUDA(cudaMemcpyAsync(pb->plen.p, pl.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, g.stream));
         }
-        /* qall and perm are host temporaries: an asynchronous copy from pageable memory
-         * returns once the source has been staged, so they may go out of scope */
-        dperm = pb->perm.as<int32_t>();
+    }
+    {
+        /* the host tables leave in one copy from pinned staging */
+        size_t tot = 0;
+        auto reserve = [&](size_t bytes) {
+            const size_t o = tot;
+            tot += (bytes + 15) / 16 * 16;
+            return o;
+        };
+        const size_t oq = reserve(qall.size() * 4), operm = reserve(perm.size() * 4), opo = reserve(po.size() * 8),
+                     opl = reserve(pl.size() * 4);
+        unsigned char* h;
+        RFG_TRY(upload_stage(tot, &h));
+        memcpy(h + oq, qall.data(), qall.size() * 4);
+        if (!perm.empty()) memcpy(h + operm, perm.data(), perm.size() * 4);
+        if (!po.empty()) memcpy(h + opo, po.data(), po.size() * 8);
+        if (!pl.empty()) memcpy(h + opl, pl.data(), pl.size() * 4);
+        RFG_TRY(pb->packed.alloc(tot));
+        RFG_CUDA(cudaMemcpyAsync(pb->packed.p, h, tot, cudaMemcpyHostToDevice, g.stream));
+        RFG_CUDA(cudaEventRecord(g.up_ev, g.stream));
+        unsigned char* d = pb->packed.as<unsigned char>();
+        pb->qlist = (const int32_t*)(d + oq);
+        if (!perm.empty()) dperm = pb->perm = (const int32_t*)(d + operm);
+        if (!po.empty()) {
+            pb->poff = (const int64_t*)(d + opo);
+            pb->plen = (const int32_t*)(d + opl);
+        }
     }
     pb->chunk = chunk;
     pb->nchunks = (nc + chunk - 1) / chunk;
@@ -594,7 +639,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         memset(&a, 0, sizeof a);
         a.q = q.dev;
         a.c = c;
-        a.qlist = pb->qlist.as<int32_t>() + cls_off[bk];
+        a.qlist = pb->qlist + cls_off[bk];
         a.nq = (int32_t)cls[bk].size();
         a.counter = pb->counters + bk;
         a.err = pb->err;
@@ -711,9 +756,9 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             }
             a.jtab = pb->jtab.as<JaroTab>();
         }
-        if (pb->poff.p) {
-            a.poff = pb->poff.as<int64_t>();
-            a.plen = pb->plen.as<int32_t>();
+        if (pb->poff) {
+            a.poff = pb->poff;
+            a.plen = pb->plen;
         }
         if (fast_ok) {
             a.fast = 1;
