@@ -490,6 +490,115 @@ Editops editops(rfg_metric m, const U1& a, const U2& b, size_t score_hint)
 }
 } // namespace detail
 
+/* runs of operations (details/types.hpp:81-100): None runs are the unchanged stretches */
+struct Opcode {
+    EditType type = EditType::None;
+    size_t src_begin = 0, src_end = 0, dest_begin = 0, dest_end = 0;
+    Opcode() = default;
+    Opcode(EditType t, size_t sb, size_t se, size_t db, size_t de)
+        : type(t), src_begin(sb), src_end(se), dest_begin(db), dest_end(de)
+    {}
+    bool operator==(const Opcode& o) const
+    {
+        return type == o.type && src_begin == o.src_begin && src_end == o.src_end && dest_begin == o.dest_begin &&
+               dest_end == o.dest_end;
+    }
+};
+
+/* Opcodes(const Editops&) (details/types.hpp:526-569): gaps between operations become None
+ * runs, consecutive operations of one type that continue each other merge into one run */
+class Opcodes : public std::vector<Opcode> {
+public:
+    Opcodes() = default;
+    explicit Opcodes(const Editops& e) : src_len_(e.get_src_len()), dest_len_(e.get_dest_len())
+    {
+        size_t sp = 0, dp = 0;
+        for (size_t i = 0; i < e.size();) {
+            if (sp < e[i].src_pos || dp < e[i].dest_pos) {
+                emplace_back(EditType::None, sp, e[i].src_pos, dp, e[i].dest_pos);
+                sp = e[i].src_pos;
+                dp = e[i].dest_pos;
+            }
+            const size_t sb = sp, db = dp;
+            const EditType t = e[i].type;
+            do {
+                sp += (t == EditType::Replace || t == EditType::Delete);
+                dp += (t == EditType::Replace || t == EditType::Insert);
+                ++i;
+            } while (i < e.size() && e[i].type == t && e[i].src_pos == sp && e[i].dest_pos == dp);
+            emplace_back(t, sb, sp, db, dp);
+        }
+        if (sp < src_len_ || dp < dest_len_) emplace_back(EditType::None, sp, src_len_, dp, dest_len_);
+    }
+    size_t get_src_len() const { return src_len_; }
+    size_t get_dest_len() const { return dest_len_; }
+    /* Editops(const Opcodes&) (details/types.hpp:500-524) */
+    Editops as_editops() const
+    {
+        Editops e;
+        e.set_src_len(src_len_);
+        e.set_dest_len(dest_len_);
+        for (const Opcode& o : *this) {
+            if (o.type == EditType::Replace)
+                for (size_t j = 0; j < o.src_end - o.src_begin; ++j)
+                    e.emplace_back(EditType::Replace, o.src_begin + j, o.dest_begin + j);
+            else if (o.type == EditType::Insert)
+                for (size_t j = 0; j < o.dest_end - o.dest_begin; ++j)
+                    e.emplace_back(EditType::Insert, o.src_begin, o.dest_begin + j);
+            else if (o.type == EditType::Delete)
+                for (size_t j = 0; j < o.src_end - o.src_begin; ++j)
+                    e.emplace_back(EditType::Delete, o.src_begin + j, o.dest_begin);
+        }
+        return e;
+    }
+
+private:
+    size_t src_len_ = 0, dest_len_ = 0;
+};
+
+/* editops_apply_* / opcodes_apply_* (rapidfuzz/distance.hpp:19-160): s1 turned into s2 */
+template <typename CharT, typename Sentence1, typename Sentence2>
+std::vector<CharT> editops_apply_vec(const Editops& ops, const Sentence1& s1, const Sentence2& s2)
+{
+    std::vector<CharT> r;
+    size_t sp = 0;
+    for (const EditOp& op : ops) {
+        for (; sp < op.src_pos; ++sp) r.push_back((CharT)s1[sp]);
+        if (op.type == EditType::None || op.type == EditType::Replace) {
+            r.push_back((CharT)s2[op.dest_pos]);
+            ++sp;
+        }
+        else if (op.type == EditType::Insert) r.push_back((CharT)s2[op.dest_pos]);
+        else ++sp;
+    }
+    for (; sp < (size_t)std::distance(std::begin(s1), std::end(s1)); ++sp) r.push_back((CharT)s1[sp]);
+    return r;
+}
+template <typename CharT, typename Sentence1, typename Sentence2>
+std::basic_string<CharT> editops_apply_str(const Editops& ops, const Sentence1& s1, const Sentence2& s2)
+{
+    const std::vector<CharT> v = editops_apply_vec<CharT>(ops, s1, s2);
+    return std::basic_string<CharT>(v.begin(), v.end());
+}
+template <typename CharT, typename Sentence1, typename Sentence2>
+std::vector<CharT> opcodes_apply_vec(const Opcodes& ops, const Sentence1& s1, const Sentence2& s2)
+{
+    std::vector<CharT> r;
+    for (const Opcode& o : ops) {
+        if (o.type == EditType::None)
+            for (size_t i = o.src_begin; i < o.src_end; ++i) r.push_back((CharT)s1[i]);
+        else if (o.type != EditType::Delete)
+            for (size_t i = o.dest_begin; i < o.dest_end; ++i) r.push_back((CharT)s2[i]);
+    }
+    return r;
+}
+template <typename CharT, typename Sentence1, typename Sentence2>
+std::basic_string<CharT> opcodes_apply_str(const Opcodes& ops, const Sentence1& s1, const Sentence2& s2)
+{
+    const std::vector<CharT> v = opcodes_apply_vec<CharT>(ops, s1, s2);
+    return std::basic_string<CharT>(v.begin(), v.end());
+}
+
 /* Levenshtein.hpp:282-295 */
 template <typename Sentence1, typename Sentence2>
 Editops levenshtein_editops(const Sentence1& s1, const Sentence2& s2,

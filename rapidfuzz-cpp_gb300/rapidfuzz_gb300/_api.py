@@ -242,6 +242,91 @@ class Editops(list):
     def get_dest_len(self):
         return self.dest_len
 
+    def as_opcodes(self):
+        return Opcodes.from_editops(self)
+
+    def apply(self, s1, s2):
+        """editops_apply (rapidfuzz/distance.hpp:19-60): s1 turned into s2, as a list"""
+        out, sp = [], 0
+        for t, src, dest in self:
+            while sp < src:
+                out.append(s1[sp])
+                sp += 1
+            if t in ("none", "replace"):
+                out.append(s2[dest])
+                sp += 1
+            elif t == "insert":
+                out.append(s2[dest])
+            else:
+                sp += 1
+        out.extend(s1[sp:])
+        return out
+
+
+class Opcode(tuple):
+    """rapidfuzz::Opcode (details/types.hpp:81-100): (type, src_begin, src_end, dest_begin, dest_end)"""
+    __slots__ = ()
+
+    def __new__(cls, t, sb, se, db, de):
+        return tuple.__new__(cls, (t, int(sb), int(se), int(db), int(de)))
+
+    type = property(lambda self: self[0])
+    src_begin = property(lambda self: self[1])
+    src_end = property(lambda self: self[2])
+    dest_begin = property(lambda self: self[3])
+    dest_end = property(lambda self: self[4])
+
+
+class Opcodes(list):
+    """rapidfuzz::Opcodes: runs of operations, None runs for the unchanged stretches"""
+
+    def __init__(self, ops, src_len, dest_len):
+        super().__init__(ops)
+        self.src_len = src_len
+        self.dest_len = dest_len
+
+    @classmethod
+    def from_editops(cls, e):
+        """Opcodes(const Editops&) (details/types.hpp:526-569)"""
+        out, sp, dp, i = [], 0, 0, 0
+        while i < len(e):
+            if sp < e[i].src_pos or dp < e[i].dest_pos:
+                out.append(Opcode("none", sp, e[i].src_pos, dp, e[i].dest_pos))
+                sp, dp = e[i].src_pos, e[i].dest_pos
+            sb, db, t = sp, dp, e[i].type
+            while True:
+                sp += t in ("replace", "delete")
+                dp += t in ("replace", "insert")
+                i += 1
+                if not (i < len(e) and e[i].type == t and e[i].src_pos == sp and e[i].dest_pos == dp):
+                    break
+            out.append(Opcode(t, sb, sp, db, dp))
+        if sp < e.src_len or dp < e.dest_len:
+            out.append(Opcode("none", sp, e.src_len, dp, e.dest_len))
+        return cls(out, e.src_len, e.dest_len)
+
+    def as_editops(self):
+        """Editops(const Opcodes&) (details/types.hpp:500-524)"""
+        ops = []
+        for t, sb, se, db, de in self:
+            if t == "replace":
+                ops += [EditOp(1, sb + j, db + j) for j in range(se - sb)]
+            elif t == "insert":
+                ops += [EditOp(2, sb, db + j) for j in range(de - db)]
+            elif t == "delete":
+                ops += [EditOp(3, sb + j, db) for j in range(se - sb)]
+        return Editops(ops, self.src_len, self.dest_len)
+
+    def apply(self, s1, s2):
+        """opcodes_apply (rapidfuzz/distance.hpp:69-103)"""
+        out = []
+        for t, sb, se, db, de in self:
+            if t == "none":
+                out.extend(s1[sb:se])
+            elif t != "delete":
+                out.extend(s2[db:de])
+        return out
+
 
 def _editops(metric, s1, s2, score_hint=None):
     from ._lib import as_units
@@ -265,4 +350,4 @@ def lcs_seq_editops(s1, s2):
     return _editops(LCSSEQ, s1, s2)
 
 
-__all__ += ["EditOp", "Editops", "levenshtein_editops", "indel_editops", "lcs_seq_editops"]
+__all__ += ["EditOp", "Editops", "Opcode", "Opcodes", "levenshtein_editops", "indel_editops", "lcs_seq_editops"]

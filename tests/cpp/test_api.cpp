@@ -144,6 +144,11 @@ int main()
         }
         while (sp < s.size()) r += s[sp++];
         CHECK(r == d);
+        CHECK(rapidfuzz::editops_apply_str<char>(ops, s, d) == d);
+        rapidfuzz::Opcodes oc(ops);
+        CHECK(rapidfuzz::opcodes_apply_str<char>(oc, s, d) == d);
+        CHECK(oc.as_editops() == ops);
+        CHECK(oc.get_src_len() == s.size() && oc.get_dest_len() == d.size());
         CHECK(rapidfuzz::indel_editops(std::string("kitten"), std::string("sitting")).size() == 5);
         CHECK(rapidfuzz::lcs_seq_editops(std::string("kitten"), std::string("sitting")).size() == 5);
         CHECK(rapidfuzz::levenshtein_editops(std::string("kitten"), std::string("sitting")).size() == 3);

@@ -504,6 +504,11 @@ def test_editops_api_names():
             assert [(["none", "replace", "insert", "delete"].index(x.type), x.src_pos, x.dest_pos) for x in e] == exp
             assert e.get_src_len() == len(a) and e.get_dest_len() == len(b)
     assert len(R.levenshtein_editops("kitten", "sitting", 5)) == 3
+    for a, b in (("Lorem ipsum.", "XYZLorem ABC iPsum"), ("kitten", "sitting"), ("", "abc"), ("abc", "")):
+        e = R.levenshtein_editops(a, b)
+        assert "".join(e.apply(a, b)) == b
+        oc = e.as_opcodes()
+        assert "".join(oc.apply(a, b)) == b and list(oc.as_editops()) == list(e)
     with pytest.raises(ValueError):
         R.levenshtein_editops("ab" * 1100, "ba" * 1100)
     assert len(R.indel_editops("ab" * 1100, "ba" * 1100)) == 2
