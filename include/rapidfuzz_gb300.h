@@ -291,10 +291,9 @@ rfg_status rfg_multi_score_f64(rfg_multi scorer, rfg_op op, double* scores, size
  * 28-56).  ops[offsets[i], offsets[i + 1]) are pair i's operations; the source / target
  * lengths of pair i are the lengths of s1[i] / s2[i].  capacity >= sum over the pairs of
  * max(len1, len2) (Levenshtein) or len1 + len2 (Indel, LCSseq) always suffices; with less,
- * the call fills offsets and returns RFG_ERR_OUT_OF_RANGE.  score_hint is accepted and
- * changes no result.  A Levenshtein pair whose strings, past their common prefix and
- * suffix, are more than 64 x 10 units with 2 m n / 8 >= 1 MB (the reference aligns those
- * with Hirschberg's algorithm) returns RFG_ERR_INVALID_ARGUMENT. */
+ * the call fills offsets and returns RFG_ERR_OUT_OF_RANGE.  score_hint has the reference's
+ * meaning (a small hint makes the exact distance the first band); long Levenshtein pairs
+ * follow the reference's Hirschberg recursion (Levenshtein_impl.hpp:1184-1257). */
 typedef enum { RFG_EDIT_NONE = 0, RFG_EDIT_REPLACE = 1, RFG_EDIT_INSERT = 2, RFG_EDIT_DELETE = 3 } rfg_edit_type;
 
 typedef struct {

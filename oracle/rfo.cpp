@@ -1390,34 +1390,26 @@ bool result_is_int(int metric, int op)
  * NOT grow).  This restatement builds those bits from the full DP tables (not from bit
  * vectors) and walks back from the end as the reference does.  The reference's banded
  * Levenshtein matrices (a score_hint, or a source longer than 64 units) gave the same
- * walk as the full tables on every pair checked against it (4,000 pairs of 70-1,500
- * units, hints none / 0 / 50 / 200). */
-template <typename S1, typename S2>
-int editops_impl(int metric, const S1& a0, const S2& b0, std::vector<rfo_editop>* out)
+ * walk as the full tables on every pair checked against it.  Long Levenshtein pairs go
+ * through the reference's Hirschberg recursion (Levenshtein_impl.hpp:1090-1257): split s2
+ * in half, take the first s1 position minimising left + right distance, recurse. */
+using Units = std::vector<u64>;
+
+/* one segment's alignment from its DP table, written to out[pos, pos + dist) */
+void align_dp(bool lev, const u64* A, i64 m, const u64* B, i64 n, i64 src_pos, i64 dest_pos, i64 pos,
+              std::vector<rfo_editop>* out)
 {
-    i64 pre = 0;
-    while (pre < a0.n && pre < b0.n && (u64)a0[pre] == (u64)b0[pre]) ++pre;
-    i64 suf = 0;
-    while (suf < a0.n - pre && suf < b0.n - pre && (u64)a0[a0.n - 1 - suf] == (u64)b0[b0.n - 1 - suf]) ++suf;
-    const i64 m = a0.n - pre - suf, n = b0.n - pre - suf;
-    auto A = [&](i64 i) { return (u64)a0[pre + i]; };
-    auto B = [&](i64 j) { return (u64)b0[pre + j]; };
-    const bool lev = metric == RFO_LEVENSHTEIN;
-    /* the reference splits pairs whose full-band bit matrices pass 1 MB with Hirschberg's
-     * algorithm (Levenshtein_impl.hpp:1185-1213), which may pick another optimal path */
-    if (lev && m >= 65 && n >= 10 && 2 * (u64)m * (u64)n / 8 >= (1u << 20)) return -2;
-    /* T[i][j]: s1 prefix i (rows of the reference's bit columns), s2 prefix j */
     std::vector<i64> T((size_t)(m + 1) * (n + 1));
     auto at = [&](i64 i, i64 j) -> i64& { return T[(size_t)i * (n + 1) + j]; };
     for (i64 i = 0; i <= m; ++i)
         for (i64 j = 0; j <= n; ++j) {
             if (lev) {
                 if (!i || !j) at(i, j) = i + j;
-                else at(i, j) = std::min({at(i - 1, j) + 1, at(i, j - 1) + 1, at(i - 1, j - 1) + (A(i - 1) != B(j - 1))});
+                else at(i, j) = std::min({at(i - 1, j) + 1, at(i, j - 1) + 1, at(i - 1, j - 1) + (A[i - 1] != B[j - 1])});
             }
             else {
                 if (!i || !j) at(i, j) = 0;
-                else at(i, j) = A(i - 1) == B(j - 1) ? at(i - 1, j - 1) + 1 : std::max(at(i - 1, j), at(i, j - 1));
+                else at(i, j) = A[i - 1] == B[j - 1] ? at(i - 1, j - 1) + 1 : std::max(at(i - 1, j), at(i, j - 1));
             }
         }
     /* bit col of row r (s2 prefix r + 1) */
@@ -1425,13 +1417,13 @@ int editops_impl(int metric, const S1& a0, const S2& b0, std::vector<rfo_editop>
     auto vn = [&](i64 r, i64 col) { return at(col + 1, r + 1) - at(col, r + 1) == -1; };
     auto sbit = [&](i64 r, i64 col) { return at(col + 1, r + 1) - at(col, r + 1) == 0; };
     i64 dist = lev ? at(m, n) : m + n - 2 * at(m, n);
-    out->assign((size_t)dist, rfo_editop{0, 0, 0, 0});
+    if ((i64)out->size() < pos + dist) out->resize((size_t)(pos + dist), rfo_editop{0, 0, 0, 0});
     auto put = [&](int type, i64 col, i64 row) {
         --dist;
-        (*out)[(size_t)dist] = rfo_editop{type, 0, col + pre, row + pre};
+        (*out)[(size_t)(pos + dist)] = rfo_editop{type, 0, col + src_pos, row + dest_pos};
     };
     i64 col = m, row = n;
-    if (dist == 0) return 0;
+    if (dist == 0) return;
     while (row && col) {
         if (lev ? vp(row - 1, col - 1) : sbit(row - 1, col - 1)) {
             --col;
@@ -1443,7 +1435,7 @@ int editops_impl(int metric, const S1& a0, const S2& b0, std::vector<rfo_editop>
                 put(2, col, row);
             else {
                 --col;
-                if (lev && A(col) != B(row)) put(1, col, row);
+                if (lev && A[col] != B[row]) put(1, col, row);
             }
         }
     }
@@ -1455,6 +1447,85 @@ int editops_impl(int metric, const S1& a0, const S2& b0, std::vector<rfo_editop>
         --row;
         put(2, col, row);
     }
+}
+
+/* the Levenshtein DP row of A[0, m) against B[0, n): row[i] = D(A[0, i), B[0, n)) */
+std::vector<i64> lev_row(const u64* A, i64 m, const u64* B, i64 n)
+{
+    std::vector<i64> prev((size_t)m + 1), cur((size_t)m + 1);
+    for (i64 i = 0; i <= m; ++i) prev[i] = i;
+    for (i64 j = 1; j <= n; ++j) {
+        cur[0] = j;
+        for (i64 i = 1; i <= m; ++i)
+            cur[i] = std::min({prev[i] + 1, cur[i - 1] + 1, prev[i - 1] + (A[i - 1] != B[j - 1])});
+        std::swap(prev, cur);
+    }
+    return prev;
+}
+
+/* levenshtein_align_hirschberg (Levenshtein_impl.hpp:1184-1213) on A[0, m), B[0, n) */
+void align_hirschberg(const u64* A, i64 m, const u64* B, i64 n, i64 src_pos, i64 dest_pos, i64 pos, u64 max,
+                      std::vector<rfo_editop>* out)
+{
+    i64 pre = 0;
+    while (pre < m && pre < n && A[pre] == B[pre]) ++pre;
+    i64 suf = 0;
+    while (suf < m - pre && suf < n - pre && A[m - 1 - suf] == B[n - 1 - suf]) ++suf;
+    A += pre;
+    B += pre;
+    m -= pre + suf;
+    n -= pre + suf;
+    src_pos += pre;
+    dest_pos += pre;
+    max = std::min<u64>(max, (u64)std::max(m, n));
+    const u64 full_band = std::min<u64>((u64)m, 2 * max + 1);
+    const u64 matrix_size = 2 * full_band * (u64)n / 8;
+    if (matrix_size < 1024 * 1024 || m < 65 || n < 10) {
+        align_dp(true, A, m, B, n, src_pos, dest_pos, pos, out);
+        return;
+    }
+    /* find_hirschberg_pos (Levenshtein_impl.hpp:1096-1180) */
+    const i64 s2_mid = n / 2;
+    const std::vector<i64> left = lev_row(A, m, B, s2_mid);
+    Units ra(A, A + m), rb(B + s2_mid, B + n);
+    std::reverse(ra.begin(), ra.end());
+    std::reverse(rb.begin(), rb.end());
+    const std::vector<i64> right = lev_row(ra.data(), m, rb.data(), n - s2_mid);
+    i64 best = std::numeric_limits<i64>::max(), s1_mid = 0, ls = 0, rs = 0;
+    for (i64 i = 0; i <= m; ++i)
+        if (left[i] + right[m - i] < best) {
+            best = left[i] + right[m - i];
+            s1_mid = i;
+            ls = left[i];
+            rs = right[m - i];
+        }
+    align_hirschberg(A, s1_mid, B, s2_mid, src_pos, dest_pos, pos, (u64)ls, out);
+    align_hirschberg(A + s1_mid, m - s1_mid, B + s2_mid, n - s2_mid, src_pos + s1_mid, dest_pos + s2_mid, pos + ls,
+                     (u64)rs, out);
+}
+
+template <typename S1, typename S2>
+int editops_impl(int metric, const S1& a0, const S2& b0, u64 hint, std::vector<rfo_editop>* out)
+{
+    Units A((size_t)a0.n), B((size_t)b0.n);
+    for (i64 i = 0; i < a0.n; ++i) A[i] = (u64)a0[i];
+    for (i64 j = 0; j < b0.n; ++j) B[j] = (u64)b0[j];
+    out->clear();
+    if (metric != RFO_LEVENSHTEIN) { /* lcs_seq_editops: common affix, then one table */
+        i64 pre = 0;
+        while (pre < a0.n && pre < b0.n && A[pre] == B[pre]) ++pre;
+        i64 suf = 0;
+        while (suf < a0.n - pre && suf < b0.n - pre && A[a0.n - 1 - suf] == B[b0.n - 1 - suf]) ++suf;
+        align_dp(false, A.data() + pre, a0.n - pre - suf, B.data() + pre, b0.n - pre - suf, pre, pre, 0, out);
+        return 0;
+    }
+    /* levenshtein_editops (Levenshtein_impl.hpp:1234-1257): the exact distance becomes the
+     * band when a small hint makes that worth it */
+    if (hint < 31) hint = 31;
+    u64 cutoff = (u64)std::max(a0.n, b0.n);
+    if (std::numeric_limits<u64>::max() / 2 > hint && 2 * hint < cutoff)
+        cutoff = (u64)lev_row(A.data(), a0.n, B.data(), b0.n)[(size_t)a0.n];
+    align_hirschberg(A.data(), a0.n, B.data(), b0.n, 0, 0, 0, cutoff, out);
     return 0;
 }
 
@@ -1594,12 +1665,13 @@ void rfo_naive_jaro_counts(const void* a, int64_t la, int ca, const void* b, int
     });
 }
 
-int rfo_editops(int metric, const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb, rfo_editop* ops,
-                int64_t cap, int64_t* count)
+int rfo_editops(int metric, const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb, uint64_t hint,
+                rfo_editop* ops, int64_t cap, int64_t* count)
 {
     if (metric != RFO_LEVENSHTEIN && metric != RFO_INDEL && metric != RFO_LCSSEQ) return -1;
     std::vector<rfo_editop> v;
-    const int rc = with_strs(a, la, ca, b, lb, cb, [&](auto s1, auto s2) -> int { return editops_impl(metric, s1, s2, &v); });
+    const int rc = with_strs(a, la, ca, b, lb, cb,
+                             [&](auto s1, auto s2) -> int { return editops_impl(metric, s1, s2, hint, &v); });
     if (rc) return rc;
     *count = (int64_t)v.size();
     for (size_t k = 0; k < v.size() && (int64_t)k < cap; ++k) ops[k] = v[k];

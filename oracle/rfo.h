@@ -92,10 +92,10 @@ int rfo_cdist(int metric, int op, const rfo_strings* queries, const rfo_strings*
               uint64_t cutoff_i, double cutoff_f, int out_dtype, void* out, int nthreads);
 
 /* ---- editops (rapidfuzz/details/types.hpp:28-56 EditType / EditOp) ----
- * levenshtein_editops (any score_hint), indel_editops / lcs_seq_editops (metric RFO_INDEL
- * or RFO_LCSSEQ).  Writes up to cap operations, *count = the number of operations;
- * returns 0, -1 (invalid) or -2 (a Levenshtein pair in the reference's Hirschberg regime:
- * more than 64 x 10 units after the common affix and 2 m n / 8 >= 1 MB). */
+ * levenshtein_editops (with the reference's score_hint handling and its Hirschberg
+ * recursion for long pairs), indel_editops / lcs_seq_editops (metric RFO_INDEL or
+ * RFO_LCSSEQ; hint unused).  Writes up to cap operations, *count = the number of
+ * operations; returns 0 or -1 (invalid). */
 typedef struct {
     int32_t type; /* 0 none, 1 replace, 2 insert, 3 delete */
     int32_t reserved;
@@ -103,7 +103,7 @@ typedef struct {
     int64_t dest_pos;
 } rfo_editop;
 
-int rfo_editops(int metric, const void* s1, int64_t l1, int cw1, const void* s2, int64_t l2, int cw2,
+int rfo_editops(int metric, const void* s1, int64_t l1, int cw1, const void* s2, int64_t l2, int cw2, uint64_t hint,
                 rfo_editop* ops, int64_t cap, int64_t* count);
 
 #ifdef __cplusplus

@@ -2029,7 +2029,6 @@ rfg_status rfg_extract(rfg_corpus c, rfg_metric metric, rfg_op op, const rfg_str
 rfg_status rfg_editops(rfg_metric metric, const rfg_strings* S1, const rfg_strings* S2, uint64_t score_hint,
                        rfg_editop* ops, int64_t capacity, int64_t* offsets, uint32_t flags)
 {
-    (void)score_hint; /* in the regime served here the reference's hint changes no result */
     std::lock_guard<std::recursive_mutex> lk(g.mu);
     if (metric != RFG_LEVENSHTEIN && metric != RFG_INDEL && metric != RFG_LCSSEQ)
         return fail(RFG_ERR_INVALID_ARGUMENT, "editops exist for Levenshtein, Indel and LCSseq");
@@ -2057,6 +2056,8 @@ rfg_status rfg_editops(rfg_metric metric, const rfg_strings* S1, const rfg_strin
     const bool lev = metric == RFG_LEVENSHTEIN;
     /* common affixes (remove_common_affix, common_impl.hpp:46-81) and region sizes */
     std::vector<int64_t> pre(np), suf(np), moff(np + 1, 0), ooff(np + 1, 0);
+    std::vector<unsigned char> hb(np, 0);
+    bool any_hb = false;
     for (int64_t i = 0; i < np; ++i) {
         const int64_t a0 = a.offsets[i], la = a.offsets[i + 1] - a0, b0 = b.offsets[i], lb = b.offsets[i + 1] - b0;
         int64_t p = 0;
@@ -2068,19 +2069,23 @@ rfg_status rfg_editops(rfg_metric metric, const rfg_strings* S1, const rfg_strin
         pre[i] = p;
         suf[i] = q;
         const int64_t m = la - p - q, n = lb - p - q, W = (m + 63) / 64;
-        if (lev && m >= 65 && n >= 10 && 2 * (uint64_t)m * (uint64_t)n / 8 >= (1u << 20))
-            return fail(RFG_ERR_INVALID_ARGUMENT,
-                        "pair %lld: the reference aligns strings of %lld x %lld units past their common affix with "
-                        "Hirschberg's algorithm, which this library does not run",
-                        (long long)i, (long long)m, (long long)n);
-        moff[i + 1] = moff[i] + (m && n ? (lev ? 2 : 1) * W * n : 0);
+        if (lev && m >= 65 && n >= 10 && 2 * (uint64_t)m * (uint64_t)n / 8 >= (1u << 20)) {
+            /* the reference may split this pair with Hirschberg's algorithm: k_editops_hb's
+             * pattern table, row vectors, band row offsets and band (a bound of every leaf's) */
+            const int64_t Wa = std::max<int64_t>(1, (la + 63) / 64);
+            hb[i] = 1;
+            any_hb = true;
+            moff[i + 1] = moff[i] + (a.char_width == 1 && b.char_width == 1 ? 256 * Wa : 0) + 4 * Wa + (lb + 1) +
+                          (1 << 17) + 5 * lb + 20 * Wa + 64;
+        }
+        else moff[i + 1] = moff[i] + (m && n ? (lev ? 2 : 1) * W * n : 0);
         ooff[i + 1] = ooff[i] + (lev ? std::max(m, n) : m + n);
     }
     if (np == 0) {
         offsets[0] = 0;
         return RFG_OK;
     }
-    DBuf da, dao, db, dbo, dpre, dsuf, dmo, doo, dcount, dops, derr;
+    DBuf da, dao, db, dbo, dpre, dsuf, dmo, doo, dcount, dops, derr, dhb;
     KStrings ka, kb;
     RFG_TRY(upload_strings(&a, &da, &dao, &ka));
     RFG_TRY(upload_strings(&b, &db, &dbo, &kb));
@@ -2096,6 +2101,10 @@ rfg_status rfg_editops(rfg_metric metric, const rfg_strings* S1, const rfg_strin
     RFG_CUDA(cudaMemcpyAsync(dpre.p, pre.data(), np * 8, cudaMemcpyHostToDevice, g.stream));
     RFG_CUDA(cudaMemcpyAsync(dsuf.p, suf.data(), np * 8, cudaMemcpyHostToDevice, g.stream));
     RFG_CUDA(cudaMemcpyAsync(doo.p, ooff.data(), (np + 1) * 8, cudaMemcpyHostToDevice, g.stream));
+    if (any_hb) {
+        RFG_TRY(dhb.alloc(np));
+        RFG_CUDA(cudaMemcpyAsync(dhb.p, hb.data(), np, cudaMemcpyHostToDevice, g.stream));
+    }
     /* launches of pairs whose matrices fit 256M words of scratch together */
     const int64_t budget = (int64_t)1 << 28;
     int64_t maxw = 0;
@@ -2107,14 +2116,18 @@ rfg_status rfg_editops(rfg_metric metric, const rfg_strings* S1, const rfg_strin
         int64_t p1 = p0 + 1;
         while (p1 < np && moff[p1 + 1] - moff[p0] <= std::max(budget, maxw)) ++p1;
         for (int64_t i = p0; i <= p1; ++i) lmo[i] = moff[i] - moff[p0]; /* offsets within this launch */
-        RFG_CUDA(cudaMemcpyAsync(dmo.as<int64_t>() + p0, lmo.data() + p0, (p1 - p0) * 8, cudaMemcpyHostToDevice,
+        RFG_CUDA(cudaMemcpyAsync(dmo.as<int64_t>() + p0, lmo.data() + p0, (p1 - p0 + 1) * 8, cudaMemcpyHostToDevice,
                                  g.stream));
         EditopsParams prm{ka,           kb,          dpre.as<int64_t>(),     dsuf.as<int64_t>(),  dmo.as<int64_t>(),
                           doo.as<int64_t>(), dmat.as<u64>(), dops.as<EditopDev>(), dcount.as<int64_t>(), derr.as<int>(),
-                          p0,           p1 - p0,     lev ? 1 : 0};
+                          p0,           p1 - p0,     lev ? 1 : 0,          any_hb ? dhb.as<unsigned char>() : nullptr,
+                          score_hint};
         void* args[] = {&prm};
         RFG_CUDA(cudaLaunchKernel(editops_kernel(), dim3((unsigned)((p1 - p0 + 127) / 128)), dim3(128), args, 0,
                                   g.stream));
+        if (any_hb)
+            RFG_CUDA(cudaLaunchKernel(editops_hb_kernel(), dim3((unsigned)((p1 - p0 + 63) / 64)), dim3(64), args, 0,
+                                      g.stream));
         RFG_CUDA(cudaStreamSynchronize(g.stream)); /* the scratch is reused by the next launch */
         p0 = p1;
     }

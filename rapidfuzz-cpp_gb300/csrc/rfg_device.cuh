@@ -108,6 +108,10 @@ struct EditopsParams {
     int* err;       /* device-side check flag */
     int64_t p0, np; /* the pairs of this launch */
     int lev;        /* 1: Levenshtein, 0: LCSseq / Indel */
+    /* Levenshtein pairs that may need the reference's Hirschberg recursion (hb[i] = 1) run
+     * in k_editops_hb with the caller's score hint; the others in k_editops */
+    const unsigned char* hb;
+    uint64_t hint;
 };
 
 /* ----------------------------------------------------------------- helpers */

@@ -30,6 +30,8 @@ const void* topk_merge_kernel();
 const void* jaro_tables_kernel();
 /* k_editops (editops of many pairs, one thread per pair) */
 const void* editops_kernel();
+/* k_editops_hb (long Levenshtein pairs: the reference's Hirschberg recursion) */
+const void* editops_hb_kernel();
 /* k_editops_pack (the pairs' operations, packed) */
 const void* editops_pack_kernel();
 /* k_zero_pairs (QRatio's empty-string rule on a device result matrix) */

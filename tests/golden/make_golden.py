@@ -477,8 +477,6 @@ def editops_cases(seed=19):
 
     def add(metric, a, b, w, hint=None, cite=None):
         a, b = as_units(a, w), as_units(b, w)
-        if eops(o.rfo_editops, metric, a, b) is None:
-            return  # the Hirschberg regime: not served
         exp = eops(ref.rfref_editops, metric, a, b, hint)
         d = {"metric": metric, "s1": [int(x) for x in a], "s2": [int(x) for x in b], "w": int(a.itemsize),
              "hint": hint, "expected": [list(x) for x in exp]}
@@ -508,6 +506,20 @@ def editops_cases(seed=19):
         if rng.random() < 0.25:
             b = [rng.choice(alpha) for _ in range(rng.randint(0, la + 10))]
         add(rng.choice([LEVENSHTEIN, INDEL, LCSSEQ]), a, b, w, rng.choice([None, 0, 50]))
+    # long Levenshtein pairs: the reference's Hirschberg recursion (Levenshtein_impl.hpp:1184-1257)
+    for k in range(24):
+        alpha = rng.choice([[97, 98], [97, 98, 99, 100], list(range(97, 123))])
+        a = [rng.choice(alpha) for _ in range(rng.choice([1100, 1600, 2300]))]
+        b = list(a)
+        for _ in range(rng.choice([rng.randint(0, 20), rng.randint(0, 400)])):
+            k2 = rng.random()
+            if k2 < 0.3 and b:
+                b[rng.randrange(len(b))] = rng.choice(alpha)
+            elif k2 < 0.6:
+                b.insert(rng.randint(0, len(b)), rng.choice(alpha))
+            elif b:
+                del b[rng.randrange(len(b))]
+        add(LEVENSHTEIN, a, b, 1, [None, 0, 50][k % 3], cite="Levenshtein_impl.hpp:1184-1257 (Hirschberg)")
     return out
 
 

@@ -94,9 +94,8 @@ def editops(lib_fn, metric, s1, s2, score_hint=None):
     cap = a.size + b.size + 1
     ops = (EditOp * cap)()
     cnt = ctypes.c_int64()
-    args = [metric, _ptr(a), a.size, a.itemsize, _ptr(b), b.size, b.itemsize]
-    if lib_fn.__name__ == "rfref_editops":
-        args.append(ctypes.c_uint64(2**64 - 1 if score_hint is None else score_hint))
+    args = [metric, _ptr(a), a.size, a.itemsize, _ptr(b), b.size, b.itemsize,
+            ctypes.c_uint64(2**64 - 1 if score_hint is None else score_hint)]
     rc = lib_fn(*args, ops, cap, ctypes.byref(cnt))
     if rc == -2:
         return None

@@ -475,19 +475,19 @@ def test_cdist_into_pinned_host_memory(metric, op, cut, dt):
 
 def test_editops_fixture_batched():
     """levenshtein_editops / indel_editops / lcs_seq_editops of every fixture pair, the
-    pairs of one metric and width in one rfg_editops call (one thread per pair)"""
-    cases = G.load("editops.json")
+    pairs of one metric, width and score hint in one rfg_editops call (one thread per pair;
+    the long Levenshtein pairs through the Hirschberg kernel)"""
     groups = {}
-    for c in cases:
-        groups.setdefault((c["metric"], c["w"]), []).append(c)
-    for (metric, w), cs in groups.items():
+    for c in G.load("editops.json"):
+        groups.setdefault((c["metric"], c["w"], c["hint"]), []).append(c)
+    for (metric, w, hint), cs in groups.items():
         dt = {1: np.uint8, 2: np.uint16, 4: np.uint32}[w]
         a = R.pack_strings([np.array(c["s1"], dtype=dt) for c in cs], w)
         b = R.pack_strings([np.array(c["s2"], dtype=dt) for c in cs], w)
-        got = R.editops_many(metric, a, b)
+        got = R.editops_many(metric, a, b, hint)
         for c, g in zip(cs, got):
             assert [tuple(int(v) for v in x) for x in g[["type", "src_pos", "dest_pos"]].tolist()] == \
-                [tuple(x) for x in c["expected"]], (metric, w, c.get("cite"), len(c["s1"]), len(c["s2"]))
+                [tuple(x) for x in c["expected"]], (metric, w, hint, c.get("cite"), len(c["s1"]), len(c["s2"]))
 
 
 def test_editops_api_names():
@@ -509,6 +509,9 @@ def test_editops_api_names():
         assert "".join(e.apply(a, b)) == b
         oc = e.as_opcodes()
         assert "".join(oc.apply(a, b)) == b and list(oc.as_editops()) == list(e)
-    with pytest.raises(ValueError):
-        R.levenshtein_editops("ab" * 1100, "ba" * 1100)
-    assert len(R.indel_editops("ab" * 1100, "ba" * 1100)) == 2
+    a, b = "ab" * 1100, "ba" * 1100  # the reference's Hirschberg regime
+    e = R.levenshtein_editops(a, b)
+    assert [(["none", "replace", "insert", "delete"].index(x.type), x.src_pos, x.dest_pos) for x in e] == \
+        editops(o.rfo_editops, R.LEVENSHTEIN, a.encode(), b.encode())
+    assert "".join(e.apply(a, b)) == b
+    assert len(R.indel_editops(a, b)) == 2

@@ -36,7 +36,7 @@ def test_oracle_editops_fixture():
     o = oracle()
     for c in G.load("editops.json"):
         a, b = _eo_arrays(c)
-        got = editops(o.rfo_editops, c["metric"], a, b)
+        got = editops(o.rfo_editops, c["metric"], a, b, c["hint"])
         assert got == [tuple(x) for x in c["expected"]], (c.get("cite"), c["metric"], len(a), len(b))
 
 
