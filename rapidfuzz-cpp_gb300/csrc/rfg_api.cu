@@ -65,7 +65,7 @@ rfg_status fail(rfg_status s, const char* fmt, ...)
         if (s_ != RFG_OK) return s_;         \
     } while (0)
 
-#define RFG_COUNTERS 64
+#define RFG_COUNTERS 128
 #define RFG_MAX_ROW_BLOCKS 12
 
 struct Ctx {
@@ -86,6 +86,14 @@ struct Ctx {
     unsigned char* up_h = nullptr;
     size_t up_cap = 0;
     cudaEvent_t up_ev = nullptr;
+    /* the class launches of one batch are independent: launches 1.. run on side streams
+     * forked from and joined back into the caller's stream (graph capture records the
+     * same fork/join as parallel branches); each origin stream keeps its own set */
+    struct SideSet {
+        std::vector<cudaStream_t> side;
+        std::vector<cudaEvent_t> ev; /* [0] fork, [1..] joins */
+    };
+    std::unordered_map<cudaStream_t, SideSet> sides;
     /* host results in pinned, mapped memory are stored by the kernels themselves over the
      * host link (RFG_HOST_STORES=0 in the environment copies them from a device buffer) */
     bool host_stores = true;
@@ -375,6 +383,7 @@ inline bool better_high_of(int op) { return op == RFG_SIMILARITY || op == RFG_NO
 int64_t g_tiles_target = 0; /* override of the tile-count target (autotuning) */
 int g_stage_mode = 1;       /* dense tiles stage their results in shared memory (autotuning) */
 int g_mq_mode = 1;          /* one-word unit-weight distances take several queries per thread (autotuning) */
+int g_half_mode = 1;        /* queries of <= 32 units run on 32-bit recurrence words (autotuning) */
 int g_block_override = 0;   /* override of the tile kernels' block size (autotuning) */
 
 /* A prepared batch: everything a launch needs is on the device, so enqueue() only
@@ -407,19 +416,9 @@ struct Prepared {
     /* query rows of each row block; a host-output cdist copies block b while block b+1
      * computes */
     std::vector<std::pair<int64_t, int64_t>> rows;
-    /* the class launches of one batch are independent: launches 1.. run on side streams
-     * forked from and joined back into the caller's stream (graph capture records the
-     * same fork/join as parallel branches) */
-    std::vector<cudaStream_t> side;
-    std::vector<cudaEvent_t> ev; /* [0] fork, [1..] joins */
     Prepared() = default;
     Prepared(const Prepared&) = delete;
     Prepared& operator=(const Prepared&) = delete;
-    ~Prepared()
-    {
-        for (cudaEvent_t e : ev) cudaEventDestroy(e);
-        for (cudaStream_t s : side) cudaStreamDestroy(s);
-    }
     void free_on(cudaStream_t st)
     {
         packed.free_on = small.free_on = scratch[0].free_on = jtab.free_on = st;
@@ -677,9 +676,9 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         }
         else if (use_mq) {
             switch (fam) {
-            case FAM_LEV: fn = tiles_mq_kernel_lev(c.width, !fast_ok); break;
-            case FAM_LCS: fn = tiles_mq_kernel_lcs(c.width, !fast_ok); break;
-            default: fn = tiles_mq_kernel_osa(c.width, !fast_ok);
+            case FAM_LEV: fn = tiles_mq_kernel_lev(c.width, !fast_ok, false); break;
+            case FAM_LCS: fn = tiles_mq_kernel_lcs(c.width, !fast_ok, false); break;
+            default: fn = tiles_mq_kernel_osa(c.width, !fast_ok, false);
             }
             block = g_block_override > 0 ? g_block_override : 256;
             a.stage = stage;
@@ -796,6 +795,38 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             scratch_bytes = std::max(scratch_bytes, (size_t)grid * a.scratch_per_cta * 8);
             generic_recs.push_back(pb->launches.size());
         }
+        if (use_mq && fam != FAM_JARO && g_half_mode) {
+            /* the class is sorted longest first: its queries of at most 32 units are the
+             * tail, and run in their own launch on 32-bit recurrence words */
+            const std::vector<int32_t>& v = cls[bk];
+            int64_t nlong = 0;
+            while (nlong < (int64_t)v.size() && q.len[v[nlong]] > 32) ++nlong;
+            const int64_t nshort = (int64_t)v.size() - nlong;
+            if (nshort > 0) {
+                const void* fh = fam == FAM_LEV ? tiles_mq_kernel_lev(c.width, !fast_ok, true)
+                                 : fam == FAM_LCS ? tiles_mq_kernel_lcs(c.width, !fast_ok, true)
+                                                  : tiles_mq_kernel_osa(c.width, !fast_ok, true);
+                const int qh = mq_queries_half(fam);
+                const size_t smem_h =
+                    tiles_mq_smem_bytes(stage, spec.out_dtype,
+                                        fast_ok ? 0 : (int)std::min<int64_t>(RFG_JT_MAXT, max_choice_len) + 1, qh);
+                RFG_TRY(allow_dynamic_smem(fh, smem_h));
+                const int64_t slots_h = (int64_t)g.sms * occupancy(fh, block, smem_h);
+                KParams h = a;
+                h.qlist = a.qlist + nlong;
+                h.nq = (int32_t)nshort;
+                h.counter = pb->counters + nblk * 5 + bk / 5;
+                const int64_t tiles_h = (nshort + qh - 1) / qh * a.nchunks;
+                pb->launches.push_back(
+                    LaunchRec{fh, (unsigned)std::min<int64_t>(tiles_h, slots_h), block, smem_h, h, (int)(bk / 5)});
+                if (nlong == 0) continue;
+                a.nq = (int32_t)nlong;
+                const int64_t tiles_l = (nlong + mqq - 1) / mqq * a.nchunks;
+                pb->launches.push_back(
+                    LaunchRec{fn, (unsigned)std::min<int64_t>(tiles_l, slots), block, smem, a, (int)(bk / 5)});
+                continue;
+            }
+        }
         pb->launches.push_back(LaunchRec{fn, (unsigned)grid, block, smem, a, (int)(bk / 5)});
     }
     if (!generic_recs.empty()) {
@@ -813,32 +844,31 @@ rfg_status enqueue_block(Prepared& pb, int b, cudaStream_t st)
     for (const LaunchRec& L : pb.launches)
         if (L.rblock == b) ls.push_back(&L);
     const size_t nl = ls.size();
-    if (nl > 1 && pb.side.size() < nl - 1) {
-        while (pb.side.size() < nl - 1) {
-            cudaStream_t x;
-            RFG_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
-            pb.side.push_back(x);
-        }
-        while (pb.ev.size() < nl) {
-            cudaEvent_t e;
-            RFG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-            pb.ev.push_back(e);
-        }
+    Ctx::SideSet& ss = g.sides[st];
+    while (nl > 1 && ss.side.size() < nl - 1) {
+        cudaStream_t x;
+        RFG_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+        ss.side.push_back(x);
     }
-    if (nl > 1) RFG_CUDA(cudaEventRecord(pb.ev[0], st));
+    while (nl > 1 && ss.ev.size() < nl) {
+        cudaEvent_t e;
+        RFG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ss.ev.push_back(e);
+    }
+    if (nl > 1) RFG_CUDA(cudaEventRecord(ss.ev[0], st));
     for (size_t i = 0; i < nl; ++i) {
         const LaunchRec& L = *ls[i];
         cudaStream_t s = st;
         if (i > 0) {
-            s = pb.side[i - 1];
-            RFG_CUDA(cudaStreamWaitEvent(s, pb.ev[0], 0));
+            s = ss.side[i - 1];
+            RFG_CUDA(cudaStreamWaitEvent(s, ss.ev[0], 0));
         }
         KParams a = L.a;
         void* args[] = {&a};
         RFG_CUDA(cudaLaunchKernel(L.fn, dim3(L.grid), dim3(L.block), args, L.smem, s));
-        if (i > 0) RFG_CUDA(cudaEventRecord(pb.ev[i], s));
+        if (i > 0) RFG_CUDA(cudaEventRecord(ss.ev[i], s));
     }
-    for (size_t i = 1; i < nl; ++i) RFG_CUDA(cudaStreamWaitEvent(st, pb.ev[i], 0));
+    for (size_t i = 1; i < nl; ++i) RFG_CUDA(cudaStreamWaitEvent(st, ss.ev[i], 0));
     return RFG_OK;
 }
 

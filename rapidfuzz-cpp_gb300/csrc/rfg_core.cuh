@@ -326,14 +326,16 @@ RFG_HD i64 osa_word(const PMF& pm, int m, const TXT& t, int n, i64 K)
  * with the same length filter, empty-string rules and lower-bound exits as those cores
  * behind the tile kernel's fast path, so every d equals the single-pair result.
  * pm(q, c): pattern-match word of pattern q for text unit c; m[q] <= 64. */
-template <int FAM, int Q, typename PMQ, typename TXT>
+template <int FAM, int Q, typename PMQ, typename TXT, typename WT = u64>
 RFG_HD void group_word_dist(const PMQ& pm, const int* m, int qn, const TXT& t, int n, const i64* Kq, i64* d)
 {
-    u64 A[Q], B[Q], D0[Q], PO[Q]; /* Lev / OSA: VP, VN, D0, previous X; Indel: S in A */
+    /* WT: the recurrence word, 64 bits, or 32 when every pattern has at most 32 units (the
+     * GPU's ALU is 32 bits wide: half the instructions per step) */
+    WT A[Q], B[Q], D0[Q], PO[Q]; /* Lev / OSA: VP, VN, D0, previous X; Indel: S in A */
     unsigned live = 0, chk = 0;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-        A[q] = ~0ull;
+        A[q] = (WT)~(WT)0;
         B[q] = D0[q] = PO[q] = 0;
         d[q] = 0;
         if (q >= qn) continue;
@@ -370,24 +372,24 @@ RFG_HD void group_word_dist(const PMQ& pm, const int* m, int qn, const TXT& t, i
 #pragma unroll
             for (int k = 0; k < RFG_FETCH; ++k) {
                 if (k < kn) {
-                    const u64 X = pm(q, c[k]);
+                    const WT X = (WT)pm(q, c[k]);
                     if (FAM == FAM_LCS) {
-                        const u64 u = A[q] & X;
-                        A[q] = (A[q] + u) | (A[q] - u);
+                        const WT u = A[q] & X;
+                        A[q] = (WT)(A[q] + u) | (WT)(A[q] - u);
                     }
                     else {
-                        const u64 VP = A[q], VN = B[q];
-                        u64 D = (((X & VP) + VP) ^ VP) | X | VN;
+                        const WT VP = A[q], VN = B[q];
+                        WT D = (WT)((WT)((X & VP) + VP) ^ VP) | X | VN;
                         if (FAM == FAM_OSA) {
-                            D |= (((~D0[q]) & X) << 1) & PO[q];
+                            D |= (WT)(((WT)~D0[q] & X) << 1) & PO[q];
                             D0[q] = D;
                             PO[q] = X;
                         }
-                        u64 HP = VN | ~(D | VP);
-                        u64 HN = D & VP;
-                        HP = (HP << 1) | 1;
-                        HN = HN << 1;
-                        A[q] = HN | ~(D | HP);
+                        WT HP = VN | (WT)~(D | VP);
+                        WT HN = D & VP;
+                        HP = (WT)(HP << 1) | (WT)1;
+                        HN = (WT)(HN << 1);
+                        A[q] = HN | (WT)~(D | HP);
                         B[q] = HP & D;
                     }
                 }
@@ -396,10 +398,10 @@ RFG_HD void group_word_dist(const PMQ& pm, const int* m, int qn, const TXT& t, i
                 const i64 K = Kq[q];
                 const int jj = j0 + RFG_FETCH, is = m[q] - n + jj;
                 if (is >= 0) {
-                    const u64 lm = low_mask(is);
+                    const WT lm = (WT)low_mask(is);
                     const bool out = FAM == FAM_LCS
-                                         ? (i64)is + jj - 2 * (i64)popc64(~A[q] & lm) > K
-                                         : (i64)jj + popc64(A[q] & lm) - popc64(B[q] & lm) > K;
+                                         ? (i64)is + jj - 2 * (i64)popc64((u64)(WT)(~A[q] & lm)) > K
+                                         : (i64)jj + popc64((u64)(A[q] & lm)) - popc64((u64)(B[q] & lm)) > K;
                     if (out) {
                         d[q] = K + 1;
                         live &= ~(1u << q);
@@ -411,9 +413,9 @@ RFG_HD void group_word_dist(const PMQ& pm, const int* m, int qn, const TXT& t, i
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         if ((live >> q) & 1u) {
-            const u64 mm = low_mask(m[q]);
-            d[q] = FAM == FAM_LCS ? (i64)m[q] + n - 2 * (i64)popc64(~A[q] & mm)
-                                  : (i64)n + popc64(A[q] & mm) - popc64(B[q] & mm);
+            const WT mm = (WT)low_mask(m[q]);
+            d[q] = FAM == FAM_LCS ? (i64)m[q] + n - 2 * (i64)popc64((u64)(WT)(~A[q] & mm))
+                                  : (i64)n + popc64((u64)(A[q] & mm)) - popc64((u64)(B[q] & mm));
         }
         d[q] = d[q] <= Kq[q] ? d[q] : Kq[q] + 1;
     }

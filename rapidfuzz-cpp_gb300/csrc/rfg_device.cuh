@@ -13,6 +13,7 @@
  * once; the cores then read `rows[r * W + w]`.
  */
 #pragma once
+#include <type_traits>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -948,6 +949,12 @@ struct MQRows {
     __device__ __forceinline__ u64 operator()(int q, u64 c) const { return rows[q * 257 + c]; }
 };
 
+/* the low 32 bits of the rows (patterns of at most 32 units) */
+struct MQRows32 {
+    const uint32_t* rows;
+    __device__ __forceinline__ uint32_t operator()(int q, u64 c) const { return rows[2 * (q * 257 + c)]; }
+};
+
 template <typename CT>
 struct MQText {
     const CT* p;
@@ -958,7 +965,7 @@ struct MQText {
     }
 };
 
-template <int FAM, typename CT, bool NORM, int Q>
+template <int FAM, typename CT, bool NORM, int Q, bool HALF = false>
 __global__ void __launch_bounds__(256, FAM == FAM_OSA ? RFG_MINB_MQ_OSA : RFG_MINB_MQ) k_tiles_mq(const KParams a)
 {
     extern __shared__ u64 smem[];
@@ -989,9 +996,9 @@ __global__ void __launch_bounds__(256, FAM == FAM_OSA ? RFG_MINB_MQ_OSA : RFG_MI
                 if (k < a.nq) {
                     qi = a.qlist[k];
                     m = (int)(a.q.off[qi + 1] - a.q.off[qi]);
-                    if (m > 64) { /* the host classified this query into a smaller class */
+                    if (m > (HALF ? 32 : 64)) { /* the host classified this query into a smaller class */
                         atomicExch(a.err, 2);
-                        m = 64;
+                        m = HALF ? 32 : 64;
                     }
                 }
                 s_q[threadIdx.x] = qi;
@@ -1031,7 +1038,9 @@ __global__ void __launch_bounds__(256, FAM == FAM_OSA ? RFG_MINB_MQ_OSA : RFG_MI
             m[q] = s_m[q];
             if (s_q[q] >= 0) qn = q + 1;
         }
-        const MQRows pm{rows};
+        typedef typename std::conditional<HALF, MQRows32, MQRows>::type Rows;
+        typedef typename std::conditional<HALF, uint32_t, u64>::type Word;
+        const Rows pm{(decltype(Rows::rows))rows};
         const int64_t c0 = ch * a.chunk;
         const int64_t c1 = c0 + a.chunk < a.c.n ? c0 + a.chunk : a.c.n;
         for (int64_t s0 = c0; s0 < c1; s0 += a.stage) {
@@ -1075,7 +1084,8 @@ __global__ void __launch_bounds__(256, FAM == FAM_OSA ? RFG_MINB_MQ_OSA : RFG_MI
                         Kq[q] = clamp_bound(kd);
                     }
                 }
-                group_word_dist<FAM, Q>(pm, m, qn, MQText<CT>{(const CT*)a.c.data + o0}, n, Kq, d);
+                group_word_dist<FAM, Q, Rows, MQText<CT>, Word>(pm, m, qn, MQText<CT>{(const CT*)a.c.data + o0}, n, Kq,
+                                                                d);
                 const int64_t i = ci - s0;
 #pragma unroll
                 for (int q = 0; q < Q; ++q) {

@@ -27,21 +27,22 @@ const void* tiles_kernel_lcs(int width, int W, bool topk)
     return nullptr;
 }
 
-const void* tiles_mq_kernel_lcs(int width, bool norm)
+template <typename CT>
+static const void* pick_mq_lcs(bool norm, bool half)
+{
+    if (half)
+        return norm ? (const void*)&k_tiles_mq<FAM_LCS, CT, true, 4, true>
+                    : (const void*)&k_tiles_mq<FAM_LCS, CT, false, 4, true>;
+    return norm ? (const void*)&k_tiles_mq<FAM_LCS, CT, true, 4> : (const void*)&k_tiles_mq<FAM_LCS, CT, false, 4>;
+}
+
+const void* tiles_mq_kernel_lcs(int width, bool norm, bool half)
 {
     switch (width) {
-    case 1:
-        return norm ? (const void*)&k_tiles_mq<FAM_LCS, uint8_t, true, 4>
-                    : (const void*)&k_tiles_mq<FAM_LCS, uint8_t, false, 4>;
-    case 2:
-        return norm ? (const void*)&k_tiles_mq<FAM_LCS, uint16_t, true, 4>
-                    : (const void*)&k_tiles_mq<FAM_LCS, uint16_t, false, 4>;
-    case 4:
-        return norm ? (const void*)&k_tiles_mq<FAM_LCS, uint32_t, true, 4>
-                    : (const void*)&k_tiles_mq<FAM_LCS, uint32_t, false, 4>;
-    case 8:
-        return norm ? (const void*)&k_tiles_mq<FAM_LCS, unsigned long long, true, 4>
-                    : (const void*)&k_tiles_mq<FAM_LCS, unsigned long long, false, 4>;
+    case 1: return pick_mq_lcs<uint8_t>(norm, half);
+    case 2: return pick_mq_lcs<uint16_t>(norm, half);
+    case 4: return pick_mq_lcs<uint32_t>(norm, half);
+    case 8: return pick_mq_lcs<unsigned long long>(norm, half);
     }
     return nullptr;
 }

@@ -27,21 +27,22 @@ const void* tiles_kernel_osa(int width, int W, bool topk)
     return nullptr;
 }
 
-const void* tiles_mq_kernel_osa(int width, bool norm)
+template <typename CT>
+static const void* pick_mq_osa(bool norm, bool half)
+{
+    if (half)
+        return norm ? (const void*)&k_tiles_mq<FAM_OSA, CT, true, 2, true>
+                    : (const void*)&k_tiles_mq<FAM_OSA, CT, false, 2, true>;
+    return norm ? (const void*)&k_tiles_mq<FAM_OSA, CT, true, 2> : (const void*)&k_tiles_mq<FAM_OSA, CT, false, 2>;
+}
+
+const void* tiles_mq_kernel_osa(int width, bool norm, bool half)
 {
     switch (width) {
-    case 1:
-        return norm ? (const void*)&k_tiles_mq<FAM_OSA, uint8_t, true, 2>
-                    : (const void*)&k_tiles_mq<FAM_OSA, uint8_t, false, 2>;
-    case 2:
-        return norm ? (const void*)&k_tiles_mq<FAM_OSA, uint16_t, true, 2>
-                    : (const void*)&k_tiles_mq<FAM_OSA, uint16_t, false, 2>;
-    case 4:
-        return norm ? (const void*)&k_tiles_mq<FAM_OSA, uint32_t, true, 2>
-                    : (const void*)&k_tiles_mq<FAM_OSA, uint32_t, false, 2>;
-    case 8:
-        return norm ? (const void*)&k_tiles_mq<FAM_OSA, unsigned long long, true, 2>
-                    : (const void*)&k_tiles_mq<FAM_OSA, unsigned long long, false, 2>;
+    case 1: return pick_mq_osa<uint8_t>(norm, half);
+    case 2: return pick_mq_osa<uint16_t>(norm, half);
+    case 4: return pick_mq_osa<uint32_t>(norm, half);
+    case 8: return pick_mq_osa<unsigned long long>(norm, half);
     }
     return nullptr;
 }

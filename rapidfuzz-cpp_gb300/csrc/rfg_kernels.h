@@ -9,17 +9,20 @@ const void* tiles_kernel_lev(int width, int W, bool topk);
 const void* tiles_kernel_lcs(int width, int W, bool topk);
 const void* tiles_kernel_osa(int width, int W, bool topk);
 const void* tiles_kernel_jaro(int width, int W, bool topk);
-/* k_tiles_mq<FAM, CT, NORM, Q> (unit-weight distances or their normalized chains, several
- * queries per thread) */
-const void* tiles_mq_kernel_lev(int width, bool norm);
-const void* tiles_mq_kernel_lcs(int width, bool norm);
-const void* tiles_mq_kernel_osa(int width, bool norm);
+/* k_tiles_mq<FAM, CT, NORM, Q, HALF> (unit-weight distances or their normalized chains,
+ * several queries per thread; HALF: 32-bit recurrence words for patterns of <= 32 units) */
+const void* tiles_mq_kernel_lev(int width, bool norm, bool half);
+const void* tiles_mq_kernel_lcs(int width, bool norm, bool half);
+const void* tiles_mq_kernel_osa(int width, bool norm, bool half);
 /* k_tiles_mq_jaro<CT, Q> (Jaro / Jaro-Winkler, several queries per thread) */
 const void* tiles_mq_kernel_jaro(int width);
 /* queries per thread of the several-queries kernels of a family (measured on GB300:
  * two keep Levenshtein / OSA / Jaro state in registers with room for latency hiding,
  * the two-register LCS state takes four) */
 inline int mq_queries(int fam) { return fam == FAM_LCS ? 4 : 2; }
+/* ... and of the 32-bit-word kernels (measured: twice the queries per thread was slower
+ * for Indel and OSA and level for Levenshtein, so the same counts) */
+inline int mq_queries_half(int fam) { return mq_queries(fam); }
 /* k_generic<FAM, CT, TOPK> */
 const void* generic_kernel(int fam, int width, bool topk);
 /* k_generic<FAM_TOKEN, CT, TOPK> (its own translation unit) */

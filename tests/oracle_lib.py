@@ -74,6 +74,7 @@ def oracle():
             f.restype = None
             f.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int] * 2 + [ctypes.POINTER(ctypes.c_int64)] * 2
         lib.rfo_editops.restype = ctypes.c_int
+        lib.rfo_editops.argtypes = _EDITOPS_ARGS
         lib.rfo_cdist.restype = ctypes.c_int
         lib.rfo_cdist.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(Strings), ctypes.POINTER(Strings),
                                   ctypes.POINTER(Params), ctypes.c_uint64, ctypes.c_double, ctypes.c_int,
@@ -85,6 +86,10 @@ def oracle():
 class EditOp(ctypes.Structure):
     _fields_ = [("type", ctypes.c_int32), ("reserved", ctypes.c_int32), ("src_pos", ctypes.c_int64),
                 ("dest_pos", ctypes.c_int64)]
+
+
+_EDITOPS_ARGS = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64,
+                 ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(EditOp), ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
 
 
 def editops(lib_fn, metric, s1, s2, score_hint=None):
@@ -119,6 +124,7 @@ def reference():
                                     ctypes.c_uint64, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.POINTER(ctypes.c_int64)]
         lib.rfref_editops.restype = ctypes.c_int
+        lib.rfref_editops.argtypes = _EDITOPS_ARGS
         _ref = lib
     return _ref
 
