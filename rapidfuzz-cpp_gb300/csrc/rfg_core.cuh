@@ -30,6 +30,8 @@
 #pragma once
 #include <stdint.h>
 
+#include <type_traits>
+
 #ifdef __CUDACC__
 #define RFG_HD __host__ __device__ __forceinline__
 /* double-precision tails of the chains: kept out of line so the integer launches never
@@ -360,18 +362,20 @@ RFG_HD void group_word_dist(const PMQ& pm, const int* m, int qn, const TXT& t, i
             }
         }
     }
-    for (int j0 = 0; j0 < n && live; j0 += RFG_FETCH) {
+    /* blocks of RFG_FETCH units: full blocks without per-unit bounds tests, then the tail */
+    auto block = [&](int j0, auto full) {
+        constexpr bool FULL = decltype(full)::value;
         u64 c[RFG_FETCH];
 #pragma unroll
-        for (int k = 0; k < RFG_FETCH; ++k) c[k] = j0 + k < n ? t[j0 + k] : 0;
-        const int kn = n - j0 < RFG_FETCH ? n - j0 : RFG_FETCH;
-        const bool at_check = kn == RFG_FETCH && ((j0 + RFG_FETCH) & 7) == 0;
+        for (int k = 0; k < RFG_FETCH; ++k) c[k] = (FULL || j0 + k < n) ? t[j0 + k] : 0;
+        const int kn = FULL ? RFG_FETCH : n - j0;
+        const bool at_check = FULL && ((j0 + RFG_FETCH) & 7) == 0;
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             if (!((live >> q) & 1u)) continue;
 #pragma unroll
             for (int k = 0; k < RFG_FETCH; ++k) {
-                if (k < kn) {
+                if (FULL || k < kn) {
                     const WT X = (WT)pm(q, c[k]);
                     if (FAM == FAM_LCS) {
                         const WT u = A[q] & X;
@@ -409,7 +413,10 @@ RFG_HD void group_word_dist(const PMQ& pm, const int* m, int qn, const TXT& t, i
                 }
             }
         }
-    }
+    };
+    int j0 = 0;
+    for (; j0 + RFG_FETCH <= n && live; j0 += RFG_FETCH) block(j0, std::integral_constant<bool, true>());
+    if (j0 < n && live) block(j0, std::integral_constant<bool, false>());
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         if ((live >> q) & 1u) {
