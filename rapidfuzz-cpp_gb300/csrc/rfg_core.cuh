@@ -327,7 +327,8 @@ RFG_HD i64 osa_word(const PMF& pm, int m, const TXT& t, int n, i64 K)
  * Levenshtein / OSA (lev_word / osa_word) or Indel (lcs_word, d = m + n - 2 LCS),
  * with the same length filter, empty-string rules and lower-bound exits as those cores
  * behind the tile kernel's fast path, so every d equals the single-pair result.
- * pm(q, c): pattern-match word of pattern q for text unit c; m[q] <= 64. */
+ * pm(q, c): pattern-match word of pattern q for the table row c of a text unit (t[j]
+ * gives rows, at most 256); m[q] <= 64. */
 template <int FAM, int Q, typename PMQ, typename TXT, typename WT = u64>
 RFG_HD void group_word_dist(const PMQ& pm, const int* m, int qn, const TXT& t, int n, const i64* Kq, i64* d)
 {
@@ -365,9 +366,9 @@ RFG_HD void group_word_dist(const PMQ& pm, const int* m, int qn, const TXT& t, i
     /* blocks of RFG_FETCH units: full blocks without per-unit bounds tests, then the tail */
     auto block = [&](int j0, auto full) {
         constexpr bool FULL = decltype(full)::value;
-        u64 c[RFG_FETCH];
+        unsigned c[RFG_FETCH]; /* the table row of each unit (at most 256) */
 #pragma unroll
-        for (int k = 0; k < RFG_FETCH; ++k) c[k] = (FULL || j0 + k < n) ? t[j0 + k] : 0;
+        for (int k = 0; k < RFG_FETCH; ++k) c[k] = (FULL || j0 + k < n) ? (unsigned)t[j0 + k] : 0u;
         const int kn = FULL ? RFG_FETCH : n - j0;
         const bool at_check = FULL && ((j0 + RFG_FETCH) & 7) == 0;
 #pragma unroll

@@ -946,13 +946,13 @@ __global__ void __launch_bounds__(256) k_generic(const KParams a)
 
 struct MQRows {
     const u64* rows;
-    __device__ __forceinline__ u64 operator()(int q, u64 c) const { return rows[q * 257 + c]; }
+    __device__ __forceinline__ u64 operator()(int q, unsigned c) const { return rows[q * 257 + c]; }
 };
 
 /* the low 32 bits of the rows (patterns of at most 32 units) */
 struct MQRows32 {
     const uint32_t* rows;
-    __device__ __forceinline__ uint32_t operator()(int q, u64 c) const { return rows[2 * (q * 257 + c)]; }
+    __device__ __forceinline__ uint32_t operator()(int q, unsigned c) const { return rows[2 * (q * 257 + c)]; }
 };
 
 template <typename CT>
