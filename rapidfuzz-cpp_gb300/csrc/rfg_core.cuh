@@ -212,26 +212,23 @@ struct ScoreParams {
 #define RFG_FETCH 8
 #endif
 
-template <typename PMF, typename TXT>
-RFG_HD void fetch_block(const PMF& pm, const TXT& t, int j0, int n, u64 (&X)[RFG_FETCH])
-{
-#pragma unroll
-    for (int k = 0; k < RFG_FETCH; ++k) X[k] = j0 + k < n ? pm(t[j0 + k]) : 0;
-}
-
 /* Hyyro 2003 (Levenshtein_impl.hpp:259-322) */
 template <typename PMF, typename TXT>
 RFG_HD i64 lev_word(const PMF& pm, int m, const TXT& t, int n, i64 K)
 {
     u64 VP = ~0ull, VN = 0;
     const bool check = K < (i64)(m > n ? m : n);
-    for (int j0 = 0; j0 < n; j0 += RFG_FETCH) {
+    /* full blocks of RFG_FETCH units without per-unit bounds tests, then the tail;
+     * returns true once the bound is passed */
+    auto block = [&](int j0, auto full) -> bool {
+        constexpr bool FULL = decltype(full)::value;
         u64 Xb[RFG_FETCH];
-        fetch_block(pm, t, j0, n, Xb);
-        const int kn = n - j0 < RFG_FETCH ? n - j0 : RFG_FETCH;
+#pragma unroll
+        for (int k = 0; k < RFG_FETCH; ++k) Xb[k] = (FULL || j0 + k < n) ? pm(t[j0 + k]) : 0;
+        const int kn = FULL ? RFG_FETCH : n - j0;
 #pragma unroll
         for (int k = 0; k < RFG_FETCH; ++k) {
-            if (k < kn) {
+            if (FULL || k < kn) {
                 const u64 X = Xb[k];
                 const u64 D0 = (((X & VP) + VP) ^ VP) | X | VN;
                 u64 HP = VN | ~(D0 | VP);
@@ -242,15 +239,20 @@ RFG_HD i64 lev_word(const PMF& pm, int m, const TXT& t, int n, i64 K)
                 VN = HP & D0;
             }
         }
-        if (check && kn == RFG_FETCH && ((j0 + RFG_FETCH) & 7) == 0) {
+        if (FULL && check && ((j0 + RFG_FETCH) & 7) == 0) {
             const int jj = j0 + RFG_FETCH, is = m - n + jj;
             if (is >= 0) {
                 const u64 lm = low_mask(is);
                 const i64 lb = (i64)jj + popc64(VP & lm) - popc64(VN & lm);
-                if (lb > K) return K + 1;
+                if (lb > K) return true;
             }
         }
-    }
+        return false;
+    };
+    int j0 = 0;
+    for (; j0 + RFG_FETCH <= n; j0 += RFG_FETCH)
+        if (block(j0, std::integral_constant<bool, true>())) return K + 1;
+    if (j0 < n) block(j0, std::integral_constant<bool, false>());
     const u64 mm = low_mask(m);
     return (i64)n + popc64(VP & mm) - popc64(VN & mm);
 }
@@ -262,25 +264,34 @@ RFG_HD i64 lcs_word(const PMF& pm, int m, const TXT& t, int n, i64 Kd)
 {
     u64 S = ~0ull;
     const bool check = Kd < (i64)(m + n);
-    for (int j0 = 0; j0 < n; j0 += RFG_FETCH) {
+    /* full blocks of RFG_FETCH units without per-unit bounds tests, then the tail;
+     * returns true once the bound is passed */
+    auto block = [&](int j0, auto full) -> bool {
+        constexpr bool FULL = decltype(full)::value;
         u64 Xb[RFG_FETCH];
-        fetch_block(pm, t, j0, n, Xb);
-        const int kn = n - j0 < RFG_FETCH ? n - j0 : RFG_FETCH;
+#pragma unroll
+        for (int k = 0; k < RFG_FETCH; ++k) Xb[k] = (FULL || j0 + k < n) ? pm(t[j0 + k]) : 0;
+        const int kn = FULL ? RFG_FETCH : n - j0;
 #pragma unroll
         for (int k = 0; k < RFG_FETCH; ++k) {
-            if (k < kn) {
+            if (FULL || k < kn) {
                 const u64 u = S & Xb[k];
                 S = (S + u) | (S - u);
             }
         }
-        if (check && kn == RFG_FETCH && ((j0 + RFG_FETCH) & 7) == 0) {
+        if (FULL && check && ((j0 + RFG_FETCH) & 7) == 0) {
             const int jj = j0 + RFG_FETCH, is = m - n + jj;
             if (is >= 0) {
                 const i64 lcs_is = popc64(~S & low_mask(is));
-                if ((i64)is + jj - 2 * lcs_is > Kd) return -1;
+                if ((i64)is + jj - 2 * lcs_is > Kd) return true;
             }
         }
-    }
+        return false;
+    };
+    int j0 = 0;
+    for (; j0 + RFG_FETCH <= n; j0 += RFG_FETCH)
+        if (block(j0, std::integral_constant<bool, true>())) return -1;
+    if (j0 < n) block(j0, std::integral_constant<bool, false>());
     return popc64(~S & low_mask(m));
 }
 
@@ -290,13 +301,17 @@ RFG_HD i64 osa_word(const PMF& pm, int m, const TXT& t, int n, i64 K)
 {
     u64 VP = ~0ull, VN = 0, D0 = 0, PMold = 0;
     const bool check = K < (i64)(m > n ? m : n);
-    for (int j0 = 0; j0 < n; j0 += RFG_FETCH) {
+    /* full blocks of RFG_FETCH units without per-unit bounds tests, then the tail;
+     * returns true once the bound is passed */
+    auto block = [&](int j0, auto full) -> bool {
+        constexpr bool FULL = decltype(full)::value;
         u64 Xb[RFG_FETCH];
-        fetch_block(pm, t, j0, n, Xb);
-        const int kn = n - j0 < RFG_FETCH ? n - j0 : RFG_FETCH;
+#pragma unroll
+        for (int k = 0; k < RFG_FETCH; ++k) Xb[k] = (FULL || j0 + k < n) ? pm(t[j0 + k]) : 0;
+        const int kn = FULL ? RFG_FETCH : n - j0;
 #pragma unroll
         for (int k = 0; k < RFG_FETCH; ++k) {
-            if (k < kn) {
+            if (FULL || k < kn) {
                 const u64 X = Xb[k];
                 const u64 TR = (((~D0) & X) << 1) & PMold;
                 D0 = (((X & VP) + VP) ^ VP) | X | VN | TR;
@@ -309,15 +324,20 @@ RFG_HD i64 osa_word(const PMF& pm, int m, const TXT& t, int n, i64 K)
                 PMold = X;
             }
         }
-        if (check && kn == RFG_FETCH && ((j0 + RFG_FETCH) & 7) == 0) {
+        if (FULL && check && ((j0 + RFG_FETCH) & 7) == 0) {
             const int jj = j0 + RFG_FETCH, is = m - n + jj;
             if (is >= 0) {
                 const u64 lm = low_mask(is);
                 const i64 lb = (i64)jj + popc64(VP & lm) - popc64(VN & lm);
-                if (lb > K) return K + 1;
+                if (lb > K) return true;
             }
         }
-    }
+        return false;
+    };
+    int j0 = 0;
+    for (; j0 + RFG_FETCH <= n; j0 += RFG_FETCH)
+        if (block(j0, std::integral_constant<bool, true>())) return K + 1;
+    if (j0 < n) block(j0, std::integral_constant<bool, false>());
     const u64 mm = low_mask(m);
     return (i64)n + popc64(VP & mm) - popc64(VN & mm);
 }
