@@ -533,6 +533,20 @@ RFG_HD void group_jaro_word(const PMQ& pm, const int* pl, unsigned active, const
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             if (!((live >> q) & 1u)) continue;
+            if (j0 + RFG_FETCH <= te[q]) {
+                /* a full block for this pattern: no per-unit bounds tests, the exit test at
+                 * units 3 and 7 of the block (j0 is a multiple of RFG_FETCH) */
+#pragma unroll
+                for (int k = 0; k < RFG_FETCH; ++k) {
+                    const int j = j0 + k;
+                    const u64 x = pm(q, c[k]) & bmask[q] & ~pflag[q];
+                    pflag[q] |= blsi(x);
+                    tflag[q] |= (u64)(x != 0) << j;
+                    bmask[q] = j < lead[q] ? (bmask[q] << 1) | 1 : bmask[q] << 1;
+                    if ((k & 3) == 3 && popc64(pflag[q]) + (te[q] - 1 - j) < need[q]) live &= ~(1u << q);
+                }
+                continue;
+            }
 #pragma unroll
             for (int k = 0; k < RFG_FETCH; ++k) {
                 const int j = j0 + k;
