@@ -592,8 +592,10 @@ RFG_HD i64 lev_multi(const PMW& pm, int m, const TXT& t, int n, i64 K)
         VN[w] = 0;
     }
     const bool check = K < (i64)(m > n ? m : n);
+    u64 c_next = n > 0 ? t[0] : 0; /* the next unit, loaded one step ahead */
     for (int j = 0; j < n; ++j) {
-        const u64 c = t[j];
+        const u64 c = c_next;
+        if (j + 1 < n) c_next = t[j + 1];
         u64 hp_c = 1, hn_c = 0;
 #pragma unroll
         for (int w = 0; w < W; ++w) {
@@ -642,8 +644,10 @@ RFG_HD i64 lcs_multi(const PMW& pm, int m, const TXT& t, int n, i64 Kd)
 #pragma unroll
     for (int w = 0; w < W; ++w) S[w] = ~0ull;
     const bool check = Kd < (i64)(m + n);
+    u64 c_next = n > 0 ? t[0] : 0; /* the next unit, loaded one step ahead */
     for (int j = 0; j < n; ++j) {
-        const u64 c = t[j];
+        const u64 c = c_next;
+        if (j + 1 < n) c_next = t[j + 1];
         u32 carry = 0;
 #pragma unroll
         for (int w = 0; w < W; ++w) {
@@ -689,8 +693,10 @@ RFG_HD i64 osa_multi(const PMW& pm, int m, const TXT& t, int n, i64 K)
         PMo[w] = 0;
     }
     const bool check = K < (i64)(m > n ? m : n);
+    u64 c_next = n > 0 ? t[0] : 0; /* the next unit, loaded one step ahead */
     for (int j = 0; j < n; ++j) {
-        const u64 c = t[j];
+        const u64 c = c_next;
+        if (j + 1 < n) c_next = t[j + 1];
         u64 hp_c = 1, hn_c = 0;
         u64 d0_prev_word = 0; /* previous column's D0 of word w-1 */
         u64 pm_prev_word = 0; /* this column's match vector of word w-1 */
@@ -761,8 +767,10 @@ RFG_HD i64 lev_band(const PMW& pm, int pw, int m, const TXT& t, int n, int K)
     }
     i64 diag = K;
     int start = K + 1 - NB; /* pattern index of window bit 0 */
+    u64 c_next = n > 0 ? t[0] : 0; /* the next unit, loaded one step ahead */
     for (int j = 0; j < n; ++j, ++start) {
-        const u64 c = t[j];
+        const u64 c = c_next;
+        if (j + 1 < n) c_next = t[j + 1];
         /* window of match bits: pattern indices [start, start + NB) */
         u64 X[B];
         {
