@@ -58,13 +58,13 @@ def parse():
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape (fixed launch list)")
     ap.add_argument("--nq", type=int, default=4096)
     ap.add_argument("--nc", type=int, default=4096)
-    ap.add_argument("--workload", default="cdist", choices=["cdist", "cfg1", "cfg3", "cfg4", "cfg5", "partial", "tokens", "editops"],
-                    help="cdist: 4096x4096 Zipf a-z Lev/Indel/OSA (the headline); cfg1: 1 x 100k DNA per-call "
-                         "vs batched; cfg3: 256 x 65536 long DNA banded; cfg4: 1024 x 1M uint32 JW + ratio; "
-                         "cfg5: serving, Poisson extract/extractOne requests over 10M DNA + 1M token strings")
-    ap.add_argument("--rate", type=float, default=2000.0, help="cfg5: request arrival rate (req/s)")
-    ap.add_argument("--duration", type=float, default=2.0, help="cfg5: seconds of arrivals")
-    ap.add_argument("--corpus", type=int, default=10_000_000, help="cfg5: DNA corpus size")
+    ap.add_argument("--workload", default="cdist", choices=["cdist", "dna1x100k", "dna256x65536", "tokens1024x1m", "serving", "partial", "tokens", "editops"],
+                    help="cdist: 4096x4096 Zipf a-z Lev/Indel/OSA (the headline); dna1x100k: 1 x 100k DNA per-call "
+                         "vs batched; dna256x65536: 256 x 65536 long DNA banded; tokens1024x1m: 1024 x 1M uint32 JW + ratio; "
+                         "serving: serving, Poisson extract/extractOne requests over 10M DNA + 1M token strings")
+    ap.add_argument("--rate", type=float, default=2000.0, help="serving: request arrival rate (req/s)")
+    ap.add_argument("--duration", type=float, default=2.0, help="serving: seconds of arrivals")
+    ap.add_argument("--corpus", type=int, default=10_000_000, help="serving: DNA corpus size")
     return ap.parse_args()
 
 

@@ -1,21 +1,21 @@
-"""The other benchmark configurations of bench.py (--workload cfg1 | cfg3 | cfg4); each
+"""The other benchmark configurations of bench.py (--workload dna1x100k | dna256x65536 | tokens1024x1m); each
 prints one JSON line like the headline workload.
 
-cfg1  Levenshtein (no cutoff), 1 query x 100,000 DNA choices len U[8,64], int64: the
+dna1x100k  Levenshtein (no cutoff), 1 query x 100,000 DNA choices len U[8,64], int64: the
       batched launch (prepared batch, device-resident) against the plain per-call path
       (rfg_cached_score_i64, one H2D + launch + D2H per choice, timed on a sample) and the
       CPU port (Cached* loop, all host threads).
-cfg3  Levenshtein normalized_distance with score_cutoff 0.1 (cutoff = 10 % of the longer
+dna256x65536  Levenshtein normalized_distance with score_cutoff 0.1 (cutoff = 10 % of the longer
       string), 256 x 65,536 DNA strings, lengths log-normal(300, 0.6) in [100, 2000], each
       choice unrelated or a query mutated at 1-15 %: multi-word and banded kernels.
-cfg4  Jaro-Winkler (prefix_weight 0.1, cutoff 0.85) and fuzz::ratio (cutoff 85) over uint32
+tokens1024x1m  Jaro-Winkler (prefix_weight 0.1, cutoff 0.85) and fuzz::ratio (cutoff 85) over uint32
       code-point token strings, 1,024 x 1,000,000, dense float64 outputs kept on the device.
 partial  fuzz::partial_ratio (cutoff 80) of 256 token queries against 200,000 token strings
-      (uint32, as in cfg4), dense float64 out on the device (the first widening of the path).
+      (uint32, as in tokens1024x1m), dense float64 out on the device (the first widening of the path).
 tokens   token_sort_ratio, QRatio, WRatio and token_set_ratio (cutoff 80), 256 x 200,000 token
       strings, host inputs and host results through rfg_cdist (joins / parts on the host threads).
 editops  levenshtein_editops of 200,000 DNA pairs (len U[8,64], 0-5 edits) through rfg_editops.
-cfg5  serving: device-resident corpora of 10,000,000 DNA strings (len U[10,200]) and
+serving  serving: device-resident corpora of 10,000,000 DNA strings (len U[10,200]) and
       1,000,000 uint32 token strings; Poisson arrivals (--rate req/s for --duration s), each
       an extractOne (limit 1) or top-10 extract of one query of length U[5,500] with a metric
       drawn from {Levenshtein, Indel, OSA} (DNA corpus) or Jaro-Winkler (token corpus);
@@ -87,7 +87,7 @@ def run(args, rank, world, local):
     steps, warmup = args.steps, args.warmup
     line = {"metric": METRIC, "unit": "GCUPS", "n_gpus": 1, "steps": steps, "warmup": warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic (seeded)"}
-    if args.workload == "cfg1":
+    if args.workload == "dna1x100k":
         q = WL.dna_uniform(seed=11, n=1)
         c = WL.dna_uniform(seed=12, n=100000)
         nq, nc = 1, 100000
@@ -100,7 +100,7 @@ def run(args, rank, world, local):
         t, per, clk = _timed_batches(torch, [b], stream, steps, warmup, flush)
         batched_pairs = nc * steps / t
         exp = oracle_cdist(R.LEVENSHTEIN, R.DISTANCE, q, c)
-        assert np.array_equal(out.cpu().numpy(), exp), "cfg1 parity"
+        assert np.array_equal(out.cpu().numpy(), exp), "dna1x100k parity"
         # plain per-call GPU path: one Cached* call per choice
         qs = q[0][:q[1][1]]
         sc = R.Cached(R.LEVENSHTEIN, qs)
@@ -126,7 +126,7 @@ def run(args, rank, world, local):
         oracle_cdist(R.LEVENSHTEIN, R.DISTANCE, q, c, nthreads=1)
         tc1 = time.perf_counter() - tc1
         line.update({"value": cells * steps / t / 1e9, "ms_per_step": t / steps * 1e3, "dtype": "u64",
-                     "config": {"workload": "cfg1: Levenshtein, 1 query x 100,000 DNA len U[8,64], no cutoff, int64",
+                     "config": {"workload": "dna1x100k: Levenshtein, 1 query x 100,000 DNA len U[8,64], no cutoff, int64",
                                 "pairs_per_s_batched": batched_pairs, "pairs_per_s_per_call_gpu": percall_pairs,
                                 "batched_over_per_call": batched_pairs / percall_pairs,
                                 "per_call_us": tp / len(strs) * 1e6,
@@ -137,7 +137,7 @@ def run(args, rank, world, local):
                      "cpu_baseline": {"value": cells / tc / 1e9, "unit": "GCUPS", "cores": os.cpu_count(),
                                       "kind": "port", "sample": "the full 1 x 100k workload"},
                      "gpu_launches": steps, "clocks": clk})
-    elif args.workload == "cfg3":
+    elif args.workload == "dna256x65536":
         q, c = WL.dna_lognormal(seed=13, nq=256, nc=65536)
         nq, nc = 256, 65536
         cells = _cells(q, c)
@@ -154,20 +154,20 @@ def run(args, rank, world, local):
                            (np.concatenate([q[0][q[1][r]:q[1][r + 1]] for r in rows]),
                             np.concatenate([[0], np.cumsum([q[1][r + 1] - q[1][r] for r in rows])]).astype(np.int64),
                             1), c, 0.1)
-        assert np.array_equal(out[rows].cpu().numpy().view(np.int64), exp.view(np.int64)), "cfg3 parity"
+        assert np.array_equal(out[rows].cpu().numpy().view(np.int64), exp.view(np.int64)), "dna256x65536 parity"
         tc0 = time.perf_counter()
         sub = 16
         qsub = (q[0][:q[1][sub]], q[1][:sub + 1].copy(), 1)
         oracle_cdist(R.LEVENSHTEIN, R.NORMALIZED_DISTANCE, qsub, c, 0.1)
         tc = time.perf_counter() - tc0
         line.update({"value": cells * steps / t / 1e9, "ms_per_step": t / steps * 1e3, "dtype": "u64",
-                     "config": {"workload": "cfg3: Levenshtein normalized_distance cutoff 0.1, 256 x 65,536 DNA "
+                     "config": {"workload": "dna256x65536: Levenshtein normalized_distance cutoff 0.1, 256 x 65,536 DNA "
                                             "lognormal(300,0.6) in [100,2000], half mutated 1-15%",
                                 "pairs_per_s": nq * nc * steps / t},
                      "cpu_baseline": {"value": _cells(qsub, c) / tc / 1e9, "unit": "GCUPS", "cores": os.cpu_count(),
                                       "kind": "port", "sample": "16 of the 256 queries x all 65,536 choices"},
                      "e2e": None, "gpu_launches": steps, "clocks": clk})
-    elif args.workload == "cfg5":
+    elif args.workload == "serving":
         return run_serving(args, R, WL)
     elif args.workload == "tokens":
         nq = 256
@@ -313,7 +313,7 @@ def run(args, rank, world, local):
                  np.concatenate([[0], np.cumsum([q[1][r + 1] - q[1][r] for r in rows])]).astype(np.int64), 4)
         for m, cut, o in ((R.JARO_WINKLER, 0.85, outs[0]), (R.RATIO, 85.0, outs[1])):
             exp = oracle_cdist(m, R.SIMILARITY, qrows, c, cut)
-            assert np.array_equal(o[rows].cpu().numpy().view(np.int64), exp.view(np.int64)), "cfg4 parity"
+            assert np.array_equal(o[rows].cpu().numpy().view(np.int64), exp.view(np.int64)), "tokens1024x1m parity"
         tc0 = time.perf_counter()
         sub = 4
         qsub = (q[0][:q[1][sub]], q[1][:sub + 1].copy(), 4)
@@ -321,7 +321,7 @@ def run(args, rank, world, local):
             oracle_cdist(m, R.SIMILARITY, qsub, c, cut)
         tc = time.perf_counter() - tc0
         line.update({"value": 2 * cells * steps / t / 1e9, "ms_per_step": t / steps * 1e3, "dtype": "u64+f64",
-                     "config": {"workload": "cfg4: Jaro-Winkler 0.85 + fuzz::ratio 85, 1,024 x %d uint32 "
+                     "config": {"workload": "tokens1024x1m: Jaro-Winkler 0.85 + fuzz::ratio 85, 1,024 x %d uint32 "
                                             "token strings, dense float64 out (on device)" % nc,
                                 "pairs_per_s": 2 * nq * nc * steps / t,
                                 "per_kernel_ms": {"jaro_winkler": per[0], "ratio": per[1]},
@@ -403,7 +403,7 @@ def run_serving(args, R, WL):
     line = {"metric": METRIC, "value": pairs / wall, "unit": "pairs/s", "n_gpus": 1, "steps": n_req, "warmup": 0,
             "ms_per_step": wall / n_req * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "u64+f64", "data": "synthetic (seeded dna_corpus_fast, tokens_u32_fast)",
-            "config": {"workload": "cfg5: serving, %d DNA (len U[10,200]) + 1,000,000 uint32 token strings, "
+            "config": {"workload": "serving: serving, %d DNA (len U[10,200]) + 1,000,000 uint32 token strings, "
                                    "Poisson %.0f req/s for %.1f s, extractOne/top-10, Lev/Indel/OSA/JW, "
                                    "query len U[5,500]" % (args.corpus, args.rate, args.duration),
                        "requests": n_req, "p50_ms": float(np.percentile(lat, 50)),
