@@ -1259,7 +1259,7 @@ rfg_status pair_path_init()
  * the batch path) */
 rfg_status score_pair_trip(int metric, int op, int form, const void* s1, int64_t l1, int w1, const void* s2,
                            int64_t l2, int w2, const ScoreParams& sp, rfg_cutoff cut, int dt, void* result,
-                           bool* done)
+                           bool* done, const int32_t* qparts = nullptr, const int32_t* cparts = nullptr)
 {
     *done = false;
     const size_t b1 = (size_t)l1 * w1, b2 = (size_t)l2 * w2;
@@ -1278,8 +1278,10 @@ rfg_status score_pair_trip(int metric, int op, int form, const void* s1, int64_t
     case FAM_OSA: per_thread = 4 * (int64_t)wmax; break;
     case FAM_JARO: per_thread = 2 * (int64_t)wmax; break;
     case FAM_PARTIAL: per_thread = partial_scratch_words(wmax, std::max(l1, l2)); break;
+    case FAM_TOKEN: per_thread = tok_scratch_words(wmax, std::max(l1, l2)); break;
     default: per_thread = l1 + 1;
     }
+    if (fam == FAM_TOKEN && (!qparts || !cparts)) return RFG_OK;
     const int block = 128;
     const int64_t table = wmax ? (int64_t)(256 + hcap + 1) * wmax + hcap : 0;
     if (table + block * per_thread > (int64_t)kPairScratchWords) return RFG_OK;
@@ -1295,6 +1297,10 @@ rfg_status score_pair_trip(int metric, int op, int form, const void* s1, int64_t
     ((int32_t*)(h + 32))[0] = 0; /* qlist */
     ((int32_t*)(h + 36))[0] = 0; /* tile counter */
     ((int32_t*)(h + 40))[0] = 0; /* check flag */
+    if (qparts) { /* the part lengths of the token_set_ratio family */
+        memcpy(h + 64, qparts, 12);
+        memcpy(h + 80, cparts, 12);
+    }
     if (b1) memcpy(h + o1, s1, b1);
     if (b2) memcpy(h + o2, s2, b2);
     RFG_CUDA(cudaMemcpyAsync(d, h, o2 + b2, cudaMemcpyHostToDevice, g.stream));
@@ -1323,6 +1329,10 @@ rfg_status score_pair_trip(int metric, int op, int form, const void* s1, int64_t
     a.better_high = better_high_of(op);
     a.wmax = wmax;
     a.scratch = g_pair.scratch;
+    if (qparts) {
+        a.qparts = (const int32_t*)(d + 64);
+        a.cparts = (const int32_t*)(d + 80);
+    }
     a.scratch_per_thread = per_thread;
     a.scratch_per_cta = table + block * per_thread;
     const void* fn = generic_kernel(fam == FAM_NONE ? FAM_WF : fam, w2, false);
@@ -1335,6 +1345,28 @@ rfg_status score_pair_trip(int metric, int op, int form, const void* s1, int64_t
     memcpy(result, h + 48, 8);
     *done = true;
     return RFG_OK;
+}
+
+/* one pair of the token_set_ratio family: host parts, then the one-trip path (or the batch
+ * path for pairs too long for its staging) */
+rfg_status token_set_one(int metric, int op, int form, const void* s1, int64_t l1, int w1, const void* s2, int64_t l2,
+                         int w2, const rfg_params* p, rfg_cutoff cut, int dt, void* result)
+{
+    const bool orig = metric == RFG_WRATIO, srt = metric != RFG_PARTIAL_TOKEN_SET_RATIO;
+    const bool ddp = metric == RFG_PARTIAL_TOKEN_SET_RATIO || metric == RFG_PARTIAL_TOKEN_RATIO || metric == RFG_WRATIO;
+    const int64_t o1[2] = {0, l1}, o2[2] = {0, l2};
+    std::vector<unsigned char> d1, d2;
+    std::vector<int64_t> f1, f2;
+    std::vector<int32_t> p1, p2;
+    token_parts_set(s1, o1, 1, w1, orig, srt, ddp, &d1, &f1, &p1);
+    token_parts_set(s2, o2, 1, w2, orig, srt, ddp, &d2, &f2, &p2);
+    bool done = false;
+    RFG_TRY(score_pair_trip(metric, op, form, d1.data(), f1[1], w1, d2.data(), f2[1], w2, to_sp(p), cut, dt, result,
+                            &done, p1.data(), p2.data()));
+    if (done) return RFG_OK;
+    int64_t q1[2] = {0, l1}, q2[2] = {0, l2};
+    rfg_strings q{s1, q1, 1, w1}, c{s2, q2, 1, w2};
+    return token_cdist(metric, op, form, &q, false, &c, false, p, cut, dt, result, 1, false);
 }
 
 /* one pair through the engine */
@@ -1350,11 +1382,7 @@ rfg_status score_one(int metric, int op, int form, const void* s1, int64_t l1, i
     const ScoreParams sp = to_sp(p);
     RFG_TRY(check_params(metric, sp));
     RFG_TRY(ensure_ctx());
-    if (is_token_set_metric(metric)) { /* host parts, then one pair through the batch path */
-        int64_t o1[2] = {0, l1}, o2[2] = {0, l2};
-        rfg_strings q{s1, o1, 1, w1}, c{s2, o2, 1, w2};
-        return token_cdist(metric, op, form, &q, false, &c, false, p, cut, dt, result, 1, false);
-    }
+    if (is_token_set_metric(metric)) return token_set_one(metric, op, form, s1, l1, w1, s2, l2, w2, p, cut, dt, result);
     std::vector<unsigned char> j1, j2;
     if (is_token_metric(metric)) { /* the front end of token_cdist, for one pair */
         if (metric == RFG_QRATIO && (!l1 || !l2)) {
@@ -1603,12 +1631,9 @@ rfg_status rfg_cached_score_f64(rfg_cached h, rfg_op op, const void* s2, int64_t
     const void* t2 = s2;
     int64_t n2 = len2;
     std::vector<unsigned char> j2;
-    if (is_token_set_metric(metric)) {
-        int64_t qo[2] = {0, h->len}, co[2] = {0, len2};
-        rfg_strings q{h->host.data(), qo, 1, h->width}, c{s2, co, 1, width2};
-        return token_cdist(metric, op, RFG_FORM_CACHED, &q, false, &c, false, &h->params,
-                           rfg_cutoff{0, score_cutoff, 0, score_hint}, RFG_F64, result, 1, false);
-    }
+    if (is_token_set_metric(metric))
+        return token_set_one(metric, op, RFG_FORM_CACHED, h->host.data(), h->len, h->width, s2, len2, width2,
+                             &h->params, rfg_cutoff{0, score_cutoff, 0, score_hint}, RFG_F64, result);
     if (is_token_metric(metric)) { /* CachedTokenSortRatio / CachedPartialTokenSortRatio / CachedQRatio */
         if (metric == RFG_QRATIO && (!h->len || !len2)) {
             *result = 0.0;
