@@ -361,7 +361,8 @@ def main():
                              "frac": achieved / peak, "traffic": traffic, "kernel": dom_kernel,
                              "peak_source": "measured: LOP3/IADD3/SHF issue-rate microbenchmark (librfg_peak.so)",
                              "ops_per_word_step": OPS_PER_WORD_STEP[dom]},
-                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * args.steps, "clocks": clk}
+                "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": sum(len(k) for k in kern.values()) * args.steps, "clocks": clk}
         print(json.dumps(line), flush=True)
     for _, b in batches:
         b.close()
