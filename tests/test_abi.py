@@ -102,3 +102,43 @@ def test_no_cpu_fallback_without_a_device():
     with pytest.raises(R.RapidfuzzError) as e:
         R.levenshtein_distance("abc", "abd")
     assert e.value.status == 5
+
+
+def test_reference_names_are_mirrored():
+    """every scorer name of the reference's public API has its mirror in the Python package
+    (rapidfuzz/distance/*.hpp, rapidfuzz/fuzz.hpp, rapidfuzz/details/types.hpp); no call"""
+    import rapidfuzz_gb300 as R
+    for prefix in ("levenshtein", "indel", "lcs_seq", "osa", "jaro", "jaro_winkler"):
+        for op in ("distance", "similarity", "normalized_distance", "normalized_similarity"):
+            assert callable(getattr(R, "%s_%s" % (prefix, op)))
+    for name in ("ratio", "partial_ratio", "token_sort_ratio", "partial_token_sort_ratio", "token_set_ratio",
+                 "partial_token_set_ratio", "token_ratio", "partial_token_ratio", "WRatio", "QRatio"):
+        assert callable(getattr(R, "fuzz_" + name))
+    for name in ("CachedLevenshtein", "CachedIndel", "CachedLCSseq", "CachedOSA", "CachedJaro", "CachedJaroWinkler",
+                 "CachedRatio", "CachedPartialRatio", "CachedTokenSortRatio", "CachedPartialTokenSortRatio",
+                 "CachedTokenSetRatio", "CachedPartialTokenSetRatio", "CachedTokenRatio", "CachedPartialTokenRatio",
+                 "CachedWRatio", "CachedQRatio"):
+        assert isinstance(getattr(R, name), type)
+    for name in ("MultiLevenshtein", "MultiIndel", "MultiLCSseq", "MultiOSA", "MultiJaro", "MultiJaroWinkler",
+                 "MultiRatio", "MultiTokenSortRatio", "MultiQRatio"):
+        assert isinstance(getattr(R.experimental, name), type)
+    for name in ("levenshtein_editops", "indel_editops", "lcs_seq_editops"):
+        assert callable(getattr(R, name))
+    e = R.Editops([R.EditOp(2, 0, 0), R.EditOp(1, 3, 4)], 5, 6)
+    oc = e.as_opcodes()
+    assert list(oc.as_editops()) == list(e) and oc.src_len == 5 and oc.dest_len == 6
+    assert "".join(e.apply("abcde", "xabcyz")[:1]) == "x"
+
+
+@pytest.mark.parametrize("std", ["c++11", "c++17"])
+def test_cpp_dropin_compiles(std):
+    """the C++ drop-in header and its caller compile (run on the GPU in test_gpu_cpp_api.py)"""
+    import shutil
+    import subprocess
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    cmd = ["g++", "-std=" + std, "-fsyntax-only", "-Wall", "-I", os.path.join(ROOT, "include"),
+           "-I", os.path.join(ROOT, "rapidfuzz-cpp_gb300", "include"), "-I", os.path.join(ROOT, "oracle"),
+           os.path.join(ROOT, "tests", "cpp", "test_api.cpp")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
