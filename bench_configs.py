@@ -259,7 +259,9 @@ def run(args, rank, world, local):
                      "e2e": {"value": npairs / t, "unit": "pairs/s",
                              "h2d_bytes_per_step": int(a[0].nbytes + a[1].nbytes + b[0].nbytes + b[1].nbytes),
                              "d2h_bytes_per_step": int(nops * 24 + npairs * 8)},
-                     "gpu_launches": 1, "clocks": clk})
+                     # per call: one k_editops launch (the pairs' matrices fit one scratch
+                     # budget of 256M words at this size) and one k_editops_pack
+                     "gpu_launches": 2 * steps, "clocks": clk})
     elif args.workload == "partial":
         nq = 256
         nc = args.nc if args.nc != 4096 else 200000

@@ -1911,6 +1911,58 @@ void server_extract_free(void* job)
     std::lock_guard<std::recursive_mutex> lk(g.mu);
     delete (ServerJob*)job;
 }
+
+/* the two code-unit types of a pair set: f(TA(), TB()) */
+template <typename F>
+void with_unit_types(int wa, int wb, F f)
+{
+    auto second = [&](auto ta) {
+        switch (wb) {
+        case 1: f(ta, uint8_t()); break;
+        case 2: f(ta, uint16_t()); break;
+        case 4: f(ta, uint32_t()); break;
+        default: f(ta, uint64_t()); break;
+        }
+    };
+    switch (wa) {
+    case 1: second(uint8_t()); break;
+    case 2: second(uint16_t()); break;
+    case 4: second(uint32_t()); break;
+    default: second(uint64_t()); break;
+    }
+}
+
+/* pairs [i0, i1): common prefix and suffix lengths, the Hirschberg-regime mark and the
+ * sizes of each pair's matrix region (words) and operation slots */
+template <typename TA, typename TB>
+void editops_sizes(const TA* ad, const int64_t* ao, const TB* bd, const int64_t* bo, bool lev, bool one_byte,
+                   int64_t i0, int64_t i1, int64_t* pre, int64_t* suf, int64_t* msize, int64_t* osize,
+                   unsigned char* hb)
+{
+    for (int64_t i = i0; i < i1; ++i) {
+        const int64_t la = ao[i + 1] - ao[i], lb = bo[i + 1] - bo[i];
+        int64_t p = 0, q = 0;
+        if (la && lb) {
+            const TA* s1 = ad + ao[i];
+            const TB* s2 = bd + bo[i];
+            while (p < la && p < lb && (u64)s1[p] == (u64)s2[p]) ++p;
+            while (q < la - p && q < lb - p && (u64)s1[la - 1 - q] == (u64)s2[lb - 1 - q]) ++q;
+        }
+        pre[i] = p;
+        suf[i] = q;
+        const int64_t m = la - p - q, n = lb - p - q, W = (m + 63) / 64;
+        if (lev && m >= 65 && n >= 10 && 2 * (uint64_t)m * (uint64_t)n / 8 >= (1u << 20)) {
+            /* the reference may split this pair with Hirschberg's algorithm: k_editops_hb's
+             * pattern table, row vectors, band row offsets and band (a bound of every leaf's) */
+            const int64_t Wa = std::max<int64_t>(1, (la + 63) / 64);
+            hb[i] = 1;
+            msize[i] = (one_byte ? 256 * Wa : 0) + 4 * Wa + (lb + 1) + (1 << 17) + 5 * lb + 20 * Wa + 64;
+        }
+        else msize[i] = m && n ? (lev ? 2 : 1) * W * n : 0;
+        osize[i] = lev ? std::max(m, n) : m + n;
+    }
+}
+
 } // namespace rfg
 
 extern "C" {
@@ -2109,33 +2161,32 @@ rfg_status rfg_editops(rfg_metric metric, const rfg_strings* S1, const rfg_strin
     if ((!a.data && np && a.offsets[np] > a.offsets[0]) || (!b.data && np && b.offsets[np] > b.offsets[0]))
         return fail(RFG_ERR_INVALID_ARGUMENT, "string data is NULL");
     const bool lev = metric == RFG_LEVENSHTEIN;
-    /* common affixes (remove_common_affix, common_impl.hpp:46-81) and region sizes */
+    /* common affixes (remove_common_affix, common_impl.hpp:46-81) and region sizes, over
+     * the host threads; the sizes become offsets afterwards */
     std::vector<int64_t> pre(np), suf(np), moff(np + 1, 0), ooff(np + 1, 0);
     std::vector<unsigned char> hb(np, 0);
-    bool any_hb = false;
-    for (int64_t i = 0; i < np; ++i) {
-        const int64_t a0 = a.offsets[i], la = a.offsets[i + 1] - a0, b0 = b.offsets[i], lb = b.offsets[i + 1] - b0;
-        int64_t p = 0;
-        while (p < la && p < lb && unit_at(a.data, a.char_width, a0 + p) == unit_at(b.data, b.char_width, b0 + p)) ++p;
-        int64_t q = 0;
-        while (q < la - p && q < lb - p &&
-               unit_at(a.data, a.char_width, a0 + la - 1 - q) == unit_at(b.data, b.char_width, b0 + lb - 1 - q))
-            ++q;
-        pre[i] = p;
-        suf[i] = q;
-        const int64_t m = la - p - q, n = lb - p - q, W = (m + 63) / 64;
-        if (lev && m >= 65 && n >= 10 && 2 * (uint64_t)m * (uint64_t)n / 8 >= (1u << 20)) {
-            /* the reference may split this pair with Hirschberg's algorithm: k_editops_hb's
-             * pattern table, row vectors, band row offsets and band (a bound of every leaf's) */
-            const int64_t Wa = std::max<int64_t>(1, (la + 63) / 64);
-            hb[i] = 1;
-            any_hb = true;
-            moff[i + 1] = moff[i] + (a.char_width == 1 && b.char_width == 1 ? 256 * Wa : 0) + 4 * Wa + (lb + 1) +
-                          (1 << 17) + 5 * lb + 20 * Wa + 64;
-        }
-        else moff[i + 1] = moff[i] + (m && n ? (lev ? 2 : 1) * W * n : 0);
-        ooff[i + 1] = ooff[i] + (lev ? std::max(m, n) : m + n);
+    const bool one_byte = a.char_width == 1 && b.char_width == 1;
+    const int64_t hw = std::max<int64_t>(1, (int64_t)std::thread::hardware_concurrency());
+    const int64_t nt = std::min<int64_t>({hw, 16, std::max<int64_t>(1, np / 16384)});
+    auto range = [&](int64_t t) {
+        with_unit_types(a.char_width, b.char_width, [&](auto ta, auto tb) {
+            editops_sizes((const decltype(ta)*)a.data, a.offsets, (const decltype(tb)*)b.data, b.offsets, lev,
+                          one_byte, np * t / nt, np * (t + 1) / nt, pre.data(), suf.data(), moff.data() + 1,
+                          ooff.data() + 1, hb.data());
+        });
+    };
+    if (nt == 1) range(0);
+    else {
+        std::vector<std::thread> th;
+        for (int64_t t = 1; t < nt; ++t) th.emplace_back(range, t);
+        range(0);
+        for (auto& x : th) x.join();
     }
+    for (int64_t i = 0; i < np; ++i) {
+        moff[i + 1] += moff[i];
+        ooff[i + 1] += ooff[i];
+    }
+    const bool any_hb = np && memchr(hb.data(), 1, (size_t)np) != nullptr;
     if (np == 0) {
         offsets[0] = 0;
         return RFG_OK;
