@@ -1678,6 +1678,18 @@ int rfo_editops(int metric, const void* a, int64_t la, int ca, const void* b, in
     return 0;
 }
 
+int rfo_token_join(const void* s, int64_t len, int cw, int dedup, uint64_t* out, int64_t cap, int64_t* out_len)
+{
+    return with_strs(s, len, cw, s, len, cw, [&](auto a, auto) -> int {
+        Tokens t = sorted_tokens(a, cw == 1);
+        if (dedup) t.erase(std::unique(t.begin(), t.end()), t.end()); /* SplittedSentenceView::dedupe */
+        const std::vector<u64> j = join_tokens(t);
+        *out_len = (int64_t)j.size();
+        for (size_t k = 0; k < j.size() && (int64_t)k < cap; ++k) out[k] = j[k];
+        return 0;
+    });
+}
+
 int rfo_score(int metric, int op, int form, const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb,
               const rfo_params* p, uint64_t ci, double cf, int64_t* oi, double* of)
 {

@@ -106,6 +106,13 @@ typedef struct {
 int rfo_editops(int metric, const void* s1, int64_t l1, int cw1, const void* s2, int64_t l2, int cw2, uint64_t hint,
                 rfo_editop* ops, int64_t cap, int64_t* count);
 
+/* the joins the token scorers score: sorted_split(s).join() (dedup = 0; common_impl.hpp
+ * 162-180, SplittedSentenceView.hpp:71-85) or the join of the sorted tokens without
+ * adjacent duplicates (dedup = 1; SplittedSentenceView::dedupe, SplittedSentenceView.hpp
+ * 48-54).  Code units are widened to uint64; writes up to cap units, *out_len = the
+ * join's length; returns 0. */
+int rfo_token_join(const void* s, int64_t len, int cw, int dedup, uint64_t* out, int64_t cap, int64_t* out_len);
+
 #ifdef __cplusplus
 }
 #endif
