@@ -386,6 +386,46 @@ extern "C" int rfref_editops(int metric, const void* a, int64_t la, int ca, cons
     }
 }
 
+/* Opcodes(const Editops&), Editops(const Opcodes&) (details/types.hpp:500-569) and
+ * editops_apply_vec / opcodes_apply_vec (distance.hpp:19-103, 134-165) of the unmodified
+ * headers on one pair's operations: opc gets 5 int64 per opcode (type, src_begin, src_end,
+ * dest_begin, dest_end), back the editops of those opcodes, ea / oa (room for la + lb
+ * units) the two applies of s1 (a, la units) and s2 (b, lb units), one-byte strings.
+ * Counts are always written; entries up to the capacities. */
+extern "C" int rfref_opcodes(const rfo_editop* ops, int64_t n, const void* a, int64_t la, const void* b, int64_t lb,
+                             int64_t* opc, int64_t cap, int64_t* count, rfo_editop* back, int64_t bcap,
+                             int64_t* bcount, uint8_t* ea, int64_t* ea_len, uint8_t* oa, int64_t* oa_len)
+{
+    rapidfuzz::Editops e((size_t)n);
+    for (int64_t k = 0; k < n; ++k)
+        e[(size_t)k] = rapidfuzz::EditOp((rapidfuzz::EditType)ops[k].type, (size_t)ops[k].src_pos,
+                                         (size_t)ops[k].dest_pos);
+    e.set_src_len((size_t)la);
+    e.set_dest_len((size_t)lb);
+    const rapidfuzz::Opcodes o(e);
+    *count = (int64_t)o.size();
+    for (size_t k = 0; k < o.size() && (int64_t)k < cap; ++k) {
+        int64_t* r = opc + 5 * k;
+        r[0] = (int64_t)o[k].type;
+        r[1] = (int64_t)o[k].src_begin;
+        r[2] = (int64_t)o[k].src_end;
+        r[3] = (int64_t)o[k].dest_begin;
+        r[4] = (int64_t)o[k].dest_end;
+    }
+    const rapidfuzz::Editops bk(o);
+    *bcount = (int64_t)bk.size();
+    for (size_t k = 0; k < bk.size() && (int64_t)k < bcap; ++k)
+        back[k] = rfo_editop{(int32_t)bk[k].type, 0, (int64_t)bk[k].src_pos, (int64_t)bk[k].dest_pos};
+    const std::vector<uint8_t> s1((const uint8_t*)a, (const uint8_t*)a + la), s2((const uint8_t*)b, (const uint8_t*)b + lb);
+    const std::vector<uint8_t> x = rapidfuzz::editops_apply_vec<uint8_t>(e, s1, s2);
+    const std::vector<uint8_t> y = rapidfuzz::opcodes_apply_vec<uint8_t>(o, s1, s2);
+    *ea_len = (int64_t)x.size();
+    *oa_len = (int64_t)y.size();
+    std::copy(x.begin(), x.end(), ea);
+    std::copy(y.begin(), y.end(), oa);
+    return 0;
+}
+
 /* Multi* with several inserted strings (padding semantics, result order) */
 extern "C" int rfref_multi(int metric, int op, int max_len, const rfo_strings* inserted, const void* b, int64_t lb,
                            int cb, const rfo_params* p, uint64_t ci, double cf, int64_t* oi, double* of,

@@ -12,7 +12,9 @@ Fixtures:
   tokens.json   token_sort_ratio / partial_token_sort_ratio / QRatio (free and Cached forms);
   tokenset.json token_set_ratio / partial_token_set_ratio / token_ratio / partial_token_ratio /
                 WRatio (free and Cached forms);
-  editops.json  levenshtein_editops / indel_editops / lcs_seq_editops.
+  editops.json  levenshtein_editops / indel_editops / lcs_seq_editops;
+  opcodes.json  the reference's Opcodes / Editops conversions and applies of editops.json's
+                one-byte pairs.
 Doubles are stored with float.hex() so the comparison is bit-exact.
 
 Usage: python tests/golden/make_golden.py   (needs the reference checkout; run in the
@@ -523,14 +525,54 @@ def editops_cases(seed=19):
     return out
 
 
+def opcodes_cases(limit=600):
+    """Opcodes(Editops), Editops(Opcodes) and the two applies (details/types.hpp:500-569,
+    distance.hpp:19-165) of the reference on the one-byte pairs of editops.json whose
+    strings hold at most 300 units together; each case names its editops.json index."""
+    ref = reference()
+    P, I64 = ctypes.c_void_p, ctypes.c_int64
+    fn = ref.rfref_opcodes
+    fn.restype = ctypes.c_int
+    fn.argtypes = [P, I64, P, I64, P, I64, P, I64, P, P, I64, P, P, P, P, P]
+    with open(os.path.join(HERE, "editops.json")) as f:
+        eops = json.load(f)
+    out = []
+    for i, c in enumerate(eops):
+        if len(out) >= limit:
+            break
+        if c["w"] != 1 or len(c["s1"]) + len(c["s2"]) > 300:
+            continue
+        a = np.array(c["s1"], dtype=np.uint8)
+        b = np.array(c["s2"], dtype=np.uint8)
+        n = len(c["expected"])
+        ops = np.zeros(max(n, 1), dtype=[("type", "<i4"), ("reserved", "<i4"), ("src_pos", "<i8"), ("dest_pos", "<i8")])
+        for k, (t, sp, dp) in enumerate(c["expected"]):
+            ops[k] = (t, 0, sp, dp)
+        cap = 2 * (len(a) + len(b)) + 2
+        opc = np.zeros(5 * cap, dtype=np.int64)
+        back = np.zeros(cap, dtype=ops.dtype)
+        ea = np.zeros(len(a) + len(b) + 1, dtype=np.uint8)
+        oa = np.zeros(len(a) + len(b) + 1, dtype=np.uint8)
+        cnt, bcnt, eal, oal = (ctypes.c_int64() for _ in range(4))
+        assert fn(ops.ctypes.data, n, a.ctypes.data, len(a), b.ctypes.data, len(b), opc.ctypes.data, cap,
+                  ctypes.byref(cnt), back.ctypes.data, cap, ctypes.byref(bcnt), ea.ctypes.data, ctypes.byref(eal),
+                  oa.ctypes.data, ctypes.byref(oal)) == 0
+        assert cnt.value <= cap and bcnt.value <= cap
+        out.append({"case": i,
+                    "opcodes": opc[:5 * cnt.value].reshape(-1, 5).tolist(),
+                    "back": [[int(x["type"]), int(x["src_pos"]), int(x["dest_pos"])] for x in back[:bcnt.value]],
+                    "editops_apply": ea[:eal.value].tolist(), "opcodes_apply": oa[:oal.value].tolist()})
+    return out
+
+
 def main():
     if reference() is None:
         sys.exit("oracle/_ref/librfref.so is missing: run `make -C oracle ref` where the reference checkout exists")
     which = sys.argv[1:] or ["kat.json", "random.json", "multi.json", "partial.json", "tokens.json", "tokenset.json",
-                             "editops.json"]
+                             "editops.json", "opcodes.json"]
     gens = {"kat.json": kat_cases, "random.json": lambda: random_cases(4000), "multi.json": multi_cases,
             "partial.json": partial_cases, "tokens.json": token_cases, "tokenset.json": tokenset_cases,
-            "editops.json": editops_cases}
+            "editops.json": editops_cases, "opcodes.json": opcodes_cases}
     for name, cases in ((n, gens[n]()) for n in which):
         with open(os.path.join(HERE, name), "w") as f:
             json.dump(cases, f, separators=(",", ":"))
