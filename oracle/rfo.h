@@ -4,7 +4,7 @@
  * This is a restatement, in plain C-style C++, of rapidfuzz-cpp v3.3.3's scorers
  * (Levenshtein / Indel / LCSseq / OSA / Jaro / Jaro-Winkler / fuzz::ratio) and of
  * the formula chains of its metric bases (rapidfuzz/details/distance.hpp).  It is
- * the checker for the CUDA path and the CPU baseline timed beside it.  Only the
+ * what the CUDA path is compared with, and the CPU baseline timed beside it.  Only the
  * tests, the smoke check and the CPU-baseline leg of the benchmark may load it;
  * the product library never links or calls it.
  *

@@ -1,6 +1,6 @@
 """ctypes access to the CPU oracle (oracle/librfo.so) and, where it was built, to the
-reference driver (oracle/_ref/librfref.so).  Test infrastructure: the checker side of
-the parity tests, never the thing measured."""
+reference driver (oracle/_ref/librfref.so).  Test infrastructure: the side of
+the parity tests the CUDA path is compared with, never the thing measured."""
 import ctypes
 import os
 import subprocess
