@@ -1,0 +1,213 @@
+/* The library's scorer cores (rfg_core.cuh: the same templates the kernels instantiate)
+ * compiled for the host, behind C entry points for the CPU tests, which compare them with
+ * the oracle's exact values.  The dispatch restates the kernels' callers: the length
+ * filter and empty-string rules first, then the core the kernel would pick.  One-byte
+ * strings; patterns of any length (the table holds 256 rows of W words, plus one zero row
+ * per query for the several-queries cores). */
+#include <stdint.h>
+
+#include <vector>
+
+#include "rfg_core.cuh"
+
+using namespace rfg;
+
+namespace {
+
+struct PM1 { /* one-word table */
+    const u64* rows;
+    u64 operator()(u64 c) const { return rows[c]; }
+};
+struct PMW { /* W-word table */
+    const u64* rows;
+    int W;
+    u64 operator()(u64 c, int w) const { return rows[c * (u64)W + w]; }
+};
+struct PMQ { /* several one-word patterns: 257 rows each (row 256 is zero) */
+    const u64* rows;
+    u64 operator()(int q, unsigned c) const { return rows[q * 257 + c]; }
+};
+struct Txt {
+    const uint8_t* p;
+    u64 operator[](int j) const { return p[j]; }
+};
+
+std::vector<u64> table(const uint8_t* a, int m, int W)
+{
+    std::vector<u64> rows((size_t)256 * W, 0);
+    for (int k = 0; k < m; ++k) rows[(size_t)a[k] * W + k / 64] |= 1ull << (k % 64);
+    return rows;
+}
+
+/* fam 0 Levenshtein, 1 Indel (via LCS), 2 OSA: the raw core value with the callers'
+ * shortcuts (LCS: the length, or -1 when pruned; distances: d or any value > K) */
+template <int W>
+i64 reg_core(int fam, const PMW& pm, const PM1& pm1, int m, const Txt& t, int n, i64 K)
+{
+    const i64 diff = m > n ? m - n : n - m;
+    if (fam == 1) {
+        if (m == 0 || n == 0) return 0;
+        if (K < diff) return -1;
+        return W == 1 ? lcs_word(pm1, m, t, n, K) : lcs_multi<W>(pm, m, t, n, K);
+    }
+    if (m == 0) return n;
+    if (K < diff) return K + 1;
+    if (n == 0) return m;
+    if (fam == 2) return W == 1 ? osa_word(pm1, m, t, n, K) : osa_multi<W>(pm, m, t, n, K);
+    if (W == 1) return lev_word(pm1, m, t, n, K);
+    if (K < m) {
+        const i64 band = 2 * K + 1;
+        if (W > 1 && band <= 64) return lev_band<1>(pm, W, m, t, n, (int)K);
+        if (W > 2 && band <= 128) return lev_band<2>(pm, W, m, t, n, (int)K);
+        if (W > 4 && band <= 256) return lev_band<4>(pm, W, m, t, n, (int)K);
+    }
+    return lev_multi<W>(pm, m, t, n, K);
+}
+
+i64 rt_core(int fam, const PMW& pm, int W, int m, const Txt& t, int n, i64 K)
+{
+    std::vector<u64> st((size_t)4 * W + 4);
+    const i64 diff = m > n ? m - n : n - m;
+    if (fam == 1) {
+        if (m == 0 || n == 0) return 0;
+        if (K < diff) return -1;
+        return lcs_multi_rt(pm, W, m, t, n, K, st.data());
+    }
+    if (m == 0) return n;
+    if (K < diff) return K + 1;
+    if (n == 0) return m;
+    if (fam == 2) return osa_multi_rt(pm, W, m, t, n, K, st.data(), st.data() + W, st.data() + 2 * W, st.data() + 3 * W);
+    if (K < m && 2 * K + 1 <= 64) return lev_band<1>(pm, W, m, t, n, (int)K);
+    if (K < m && 2 * K + 1 <= 128) return lev_band<2>(pm, W, m, t, n, (int)K);
+    if (K < m && 2 * K + 1 <= 256) return lev_band<4>(pm, W, m, t, n, (int)K);
+    if (K < m && 2 * K + 1 <= 512) return lev_band<8>(pm, W, m, t, n, (int)K);
+    return lev_multi_rt(pm, W, m, t, n, K, st.data(), st.data() + W);
+}
+
+/* the distance chain d <= K ? d : K + 1 of a raw core value */
+int64_t chain(int fam, int m, int n, i64 raw, i64 K)
+{
+    i64 d = raw;
+    if (fam == 1) d = raw < 0 ? K + 1 : (i64)m + n - 2 * raw;
+    return d <= K ? d : K + 1;
+}
+
+} // namespace
+
+extern "C" {
+
+/* variant 0: the register-resident cores of the tile kernel (W = 1, 2, 4, 8 by the
+ * pattern length, at most 512 units); variant 1: the any-length kernel's cores (runtime
+ * W, bands up to 8 words).  Returns the distance chain, or -2 for a shape the variant
+ * does not take. */
+int64_t hc_distance(int fam, int variant, const uint8_t* a, int m, const uint8_t* b, int n, int64_t K)
+{
+    const int W = m > 0 ? (m + 63) / 64 : 1;
+    const Txt t{b};
+    if (variant == 0) {
+        const int Wr = W <= 1 ? 1 : W <= 2 ? 2 : W <= 4 ? 4 : W <= 8 ? 8 : 0;
+        if (!Wr) return -2;
+        const std::vector<u64> rows = table(a, m, Wr);
+        const std::vector<u64> rows1 = table(a, m < 64 ? m : 64, 1);
+        const PMW pm{rows.data(), Wr};
+        const PM1 pm1{rows1.data()};
+        i64 raw = 0;
+        switch (Wr) {
+        case 1: raw = reg_core<1>(fam, pm, pm1, m, t, n, K); break;
+        case 2: raw = reg_core<2>(fam, pm, pm1, m, t, n, K); break;
+        case 4: raw = reg_core<4>(fam, pm, pm1, m, t, n, K); break;
+        default: raw = reg_core<8>(fam, pm, pm1, m, t, n, K); break;
+        }
+        return chain(fam, m, n, raw, K);
+    }
+    const std::vector<u64> rows = table(a, m, W);
+    return chain(fam, m, n, rt_core(fam, PMW{rows.data(), W}, W, m, t, n, K), K);
+}
+
+/* the several-queries core (group_word_dist) on two patterns of at most 64 units (32
+ * with word32) against one text; out[q] = the distance chain of pattern q */
+int hc_group(int fam, int word32, const uint8_t* a1, int m1, const uint8_t* a2, int m2, const uint8_t* b, int n,
+             int64_t K1, int64_t K2, int64_t* out)
+{
+    if (m1 > 64 || m2 > 64 || (word32 && (m1 > 32 || m2 > 32))) return -2;
+    std::vector<u64> rows(2 * 257, 0);
+    for (int k = 0; k < m1; ++k) rows[a1[k]] |= 1ull << k;
+    for (int k = 0; k < m2; ++k) rows[257 + a2[k]] |= 1ull << k;
+    const int m[2] = {m1, m2};
+    const i64 Kq[2] = {K1, K2};
+    i64 d[2] = {0, 0};
+    const PMQ pm{rows.data()};
+    const int F = fam == 0 ? FAM_LEV : fam == 1 ? FAM_LCS : FAM_OSA;
+    const Txt t{b};
+    if (F == FAM_LEV) {
+        if (word32) group_word_dist<FAM_LEV, 2, PMQ, Txt, u32>(pm, m, 2, t, n, Kq, d);
+        else group_word_dist<FAM_LEV, 2, PMQ, Txt, u64>(pm, m, 2, t, n, Kq, d);
+    }
+    else if (F == FAM_LCS) {
+        if (word32) group_word_dist<FAM_LCS, 2, PMQ, Txt, u32>(pm, m, 2, t, n, Kq, d);
+        else group_word_dist<FAM_LCS, 2, PMQ, Txt, u64>(pm, m, 2, t, n, Kq, d);
+    }
+    else {
+        if (word32) group_word_dist<FAM_OSA, 2, PMQ, Txt, u32>(pm, m, 2, t, n, Kq, d);
+        else group_word_dist<FAM_OSA, 2, PMQ, Txt, u64>(pm, m, 2, t, n, Kq, d);
+    }
+    out[0] = d[0];
+    out[1] = d[1];
+    return 0;
+}
+
+/* Jaro common characters and (unhalved) transpositions, m, n > 0.  variant 0: jaro_word
+ * (pattern <= 64 units, effective text end <= 64); 1: jaro_multi<W> (W = 1, 2, 4, 8);
+ * 2: jaro_multi_rt; 3: group_jaro_word with the pattern in both slots (as variant 0).
+ * Returns -2 for a shape the variant does not take. */
+int hc_jaro(int variant, const uint8_t* a, int m, const uint8_t* b, int n, int64_t* common, int64_t* transp)
+{
+    int bound = (m > n ? m : n) / 2;
+    if (bound > 0) --bound;
+    const int te = n < m + bound ? n : m + bound;
+    const Txt t{b};
+    int c = 0, tr = 0;
+    const int W = (m + 63) / 64;
+    if (variant == 0 || variant == 3) {
+        if (m > 64 || te > 64) return -2;
+        if (variant == 0) {
+            const std::vector<u64> rows = table(a, m, 1);
+            jaro_word(PM1{rows.data()}, m, t, n, &c, &tr);
+        }
+        else {
+            std::vector<u64> rows(2 * 257, 0);
+            for (int k = 0; k < m; ++k) {
+                rows[a[k]] |= 1ull << k;
+                rows[257 + a[k]] |= 1ull << k;
+            }
+            const int pl[2] = {m, m}, need[2] = {0, 0};
+            int C[2] = {0, 0}, T[2] = {0, 0};
+            group_jaro_word<2>(PMQ{rows.data()}, pl, 3u, t, n, need, C, T);
+            if (C[0] != C[1] || T[0] != T[1]) return -3;
+            c = C[0];
+            tr = T[0];
+        }
+    }
+    else if (variant == 1) {
+        const int Wr = W <= 1 ? 1 : W <= 2 ? 2 : W <= 4 ? 4 : W <= 8 ? 8 : 0;
+        if (!Wr) return -2;
+        const std::vector<u64> rows = table(a, m, Wr);
+        const PMW pm{rows.data(), Wr};
+        switch (Wr) {
+        case 1: jaro_multi<1>(pm, m, t, n, &c, &tr); break;
+        case 2: jaro_multi<2>(pm, m, t, n, &c, &tr); break;
+        case 4: jaro_multi<4>(pm, m, t, n, &c, &tr); break;
+        default: jaro_multi<8>(pm, m, t, n, &c, &tr); break;
+        }
+    }
+    else {
+        const std::vector<u64> rows = table(a, m, W);
+        std::vector<u64> f1((size_t)W), f2((size_t)W);
+        jaro_multi_rt(PMW{rows.data(), W}, W, m, t, n, &c, &tr, f1.data(), f2.data());
+    }
+    *common = c;
+    *transp = tr;
+    return 0;
+}
+
+} /* extern "C" */

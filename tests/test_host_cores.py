@@ -1,0 +1,135 @@
+"""CPU tests of the scorer cores themselves: rfg_core.cuh (the templates the kernels
+instantiate) compiled for the host behind tests/cpp/host_cores.cpp, against the oracle's
+exact values on seeded pairs -- every core the kernels pick (one-word, W-word, banded,
+runtime-W and several-queries recurrences on 64- and 32-bit words; the Jaro flagging
+cores), patterns of 1..700 units, cutoffs from 0 to unbounded, with the distance chain
+d <= K ? d : K + 1.  No GPU."""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle_lib import ROOT, oracle
+
+CSRC = os.path.join(ROOT, "rapidfuzz-cpp_gb300", "csrc")
+BIG = 2**62
+
+
+@pytest.fixture(scope="module")
+def libs():
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    out = os.path.join(ROOT, "tests", "cpp", "_build")
+    os.makedirs(out, exist_ok=True)
+    so = os.path.join(out, "libhost_cores.so")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-shared", "-fPIC", "-I" + CSRC, "-o", so,
+                    os.path.join(ROOT, "tests", "cpp", "host_cores.cpp")], check=True)
+    lib = ctypes.CDLL(so)
+    P, I64, I = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+    lib.hc_distance.restype = I64
+    lib.hc_distance.argtypes = [I, I, P, I, P, I, I64]
+    lib.hc_group.restype = I
+    lib.hc_group.argtypes = [I, I, P, I, P, I, P, I, I64, I64, P]
+    lib.hc_jaro.restype = I
+    lib.hc_jaro.argtypes = [I, P, I, P, I, P, P]
+    o = oracle()
+    for f in (o.rfo_lcs_exact, o.rfo_osa_exact):
+        f.restype = I64
+        f.argtypes = [P, I64, I, P, I64, I]
+    o.rfo_levenshtein_exact.restype = I64
+    o.rfo_levenshtein_exact.argtypes = [P, I64, I, P, I64, I, I64, I64, I64]
+    o.rfo_jaro_counts.restype = None
+    o.rfo_jaro_counts.argtypes = [P, I64, I, P, I64, I, P, P]
+    return lib, o
+
+
+def pairs(seed, n, lens):
+    """(a, b): b is a with edits (substitutions, insertions, deletions, adjacent swaps) or
+    an unrelated string; alphabets of 2, 4 and 26 letters"""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        alpha = [b"ab", b"ACGT", b"abcdefghijklmnopqrstuvwxyz"][int(rng.integers(0, 3))]
+        la = int(rng.choice(lens))
+        a = bytearray(alpha[int(rng.integers(0, len(alpha)))] for _ in range(la))
+        if rng.random() < 0.25:
+            b = bytearray(alpha[int(rng.integers(0, len(alpha)))] for _ in range(int(rng.integers(0, la + 10))))
+        else:
+            b = bytearray(a)
+            for _ in range(int(rng.integers(0, max(2, la // 6)))):
+                k, pos = rng.random(), int(rng.integers(0, len(b) + 1))
+                if k < 0.3 and pos < len(b):
+                    b[pos] = alpha[int(rng.integers(0, len(alpha)))]
+                elif k < 0.55:
+                    b.insert(pos, alpha[int(rng.integers(0, len(alpha)))])
+                elif k < 0.8 and pos < len(b):
+                    del b[pos]
+                elif pos + 1 < len(b):
+                    b[pos], b[pos + 1] = b[pos + 1], b[pos]
+        out.append((bytes(a), bytes(b)))
+    return out
+
+
+def exact(o, fam, a, b):
+    if fam == 0:
+        return o.rfo_levenshtein_exact(a, len(a), 1, b, len(b), 1, 1, 1, 1)
+    if fam == 1:
+        return len(a) + len(b) - 2 * o.rfo_lcs_exact(a, len(a), 1, b, len(b), 1)
+    return o.rfo_osa_exact(a, len(a), 1, b, len(b), 1)
+
+
+def cutoffs(rng, d):
+    return sorted({0, 1, 3, 8, max(0, d - 1), d, d + 1, int(rng.integers(0, 2 * d + 2)), 31, 64, 200, BIG})
+
+
+@pytest.mark.parametrize("fam", [0, 1, 2], ids=["levenshtein", "indel", "osa"])
+def test_cores_match_oracle(libs, fam):
+    lib, o = libs
+    rng = np.random.default_rng(10 + fam)
+    lens = [0, 1, 2, 5, 20, 31, 32, 33, 63, 64, 65, 100, 128, 129, 200, 256, 300, 512, 513, 700]
+    for a, b in pairs(20 + fam, 900, lens):
+        d = exact(o, fam, a, b)
+        for K in cutoffs(rng, d):
+            want = d if d <= K else K + 1
+            for variant in (0, 1):
+                got = lib.hc_distance(fam, variant, a, len(a), b, len(b), K)
+                if got == -2:
+                    continue
+                assert got == want, (fam, variant, a, b, K)
+
+
+@pytest.mark.parametrize("fam", [0, 1, 2], ids=["levenshtein", "indel", "osa"])
+@pytest.mark.parametrize("word32", [0, 1], ids=["64bit", "32bit"])
+def test_several_queries_core_matches_oracle(libs, fam, word32):
+    lib, o = libs
+    rng = np.random.default_rng(30 + fam + 3 * word32)
+    lens = [0, 1, 2, 7, 8, 9, 16, 31, 32] + ([] if word32 else [33, 48, 63, 64])
+    ps = pairs(40 + fam + 3 * word32, 1200, lens)
+    out = (ctypes.c_int64 * 2)()
+    for k in range(0, len(ps) - 1, 2):
+        (a1, b), (a2, _) = ps[k], ps[k + 1]
+        d1, d2 = exact(o, fam, a1, b), exact(o, fam, a2, b)
+        for K1, K2 in zip(cutoffs(rng, d1), reversed(cutoffs(rng, d2))):
+            assert lib.hc_group(fam, word32, a1, len(a1), a2, len(a2), b, len(b), K1, K2, out) == 0
+            assert list(out) == [d1 if d1 <= K1 else K1 + 1, d2 if d2 <= K2 else K2 + 1], (a1, a2, b, K1, K2)
+
+
+def test_jaro_cores_match_oracle(libs):
+    lib, o = libs
+    c, t, ec, et = (ctypes.c_int64() for _ in range(4))
+    lens = [1, 2, 3, 5, 10, 20, 40, 63, 64, 65, 100, 200, 300]
+    seen = set()
+    for a, b in pairs(50, 1500, lens):
+        if not a or not b:
+            continue
+        o.rfo_jaro_counts(a, len(a), 1, b, len(b), 1, ctypes.byref(ec), ctypes.byref(et))
+        for variant in (0, 1, 2, 3):
+            rc = lib.hc_jaro(variant, a, len(a), b, len(b), ctypes.byref(c), ctypes.byref(t))
+            if rc == -2:
+                continue
+            assert rc == 0 and (c.value, t.value) == (ec.value, et.value), (variant, a, b)
+            seen.add(variant)
+    assert seen == {0, 1, 2, 3}
