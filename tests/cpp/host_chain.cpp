@@ -1,0 +1,123 @@
+/* One scorer call the way the any-length kernel makes it (score_pair_generic): the pair's
+ * plan and formula chains (plan_int / finish_int / finish_jaro in rfg_core.cuh) around
+ * the runtime-W cores, compiled for the host behind the oracle's rfo_score signature, so
+ * the CPU tests can run the reference-made fixtures through the device code's chains.
+ * Code units of any width: units below 256 index the table directly, wider ones get a row
+ * each (a text unit the pattern lacks reads a zero row), as the kernels' hashed rows do. */
+#include <stdint.h>
+#include <string.h>
+
+#include <map>
+#include <vector>
+
+#include "rfg_core.cuh"
+
+using namespace rfg;
+
+namespace {
+
+struct Params {
+    int64_t ins, del, rep;
+    double prefix_weight;
+};
+struct PMRows {
+    const u64* rows;
+    int W;
+    u64 operator()(u64 r, int w) const { return rows[r * (u64)W + w]; }
+};
+struct Seq {
+    const u64* p;
+    u64 operator[](int j) const { return p[j]; }
+};
+
+std::vector<u64> widen(const void* s, int64_t n, int w)
+{
+    std::vector<u64> v((size_t)n);
+    for (int64_t i = 0; i < n; ++i) {
+        switch (w) {
+        case 1: v[i] = ((const uint8_t*)s)[i]; break;
+        case 2: v[i] = ((const uint16_t*)s)[i]; break;
+        case 4: v[i] = ((const uint32_t*)s)[i]; break;
+        default: v[i] = ((const uint64_t*)s)[i]; break;
+        }
+    }
+    return v;
+}
+
+} // namespace
+
+extern "C" {
+
+/* rfo_score's arguments; free and Cached forms of Levenshtein .. ratio (metrics 0..6).
+ * Returns 0, or -1 for a form or metric outside that set. */
+int hc_score(int metric, int op, int form, const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb,
+             const Params* p, uint64_t ci, double cf, int64_t* oi, double* of)
+{
+    if (form == FORM_MULTI || metric < 0 || metric > RATIO) return -1;
+    const std::vector<u64> A = widen(a, la, ca), B = widen(b, lb, cb);
+    std::map<u64, u64> wide;
+    for (u64 x : A)
+        if (x >= 256 && !wide.count(x)) wide.emplace(x, 256 + wide.size());
+    const u64 zero_row = 256 + wide.size();
+    std::vector<u64> rb((size_t)lb);
+    for (int64_t j = 0; j < lb; ++j) {
+        const u64 x = B[j];
+        rb[j] = x < 256 ? x : (wide.count(x) ? wide[x] : zero_row);
+    }
+    const int m = (int)la, n = (int)lb, W = m > 0 ? (m + 63) / 64 : 1;
+    std::vector<u64> table((size_t)(zero_row + 1) * W, 0);
+    for (int k = 0; k < m; ++k) table[(A[k] < 256 ? A[k] : wide[A[k]]) * W + k / 64] |= 1ull << (k % 64);
+    const PMRows pm{table.data(), W};
+    const Seq txt{rb.data()}, q{A.data()}, t2{B.data()};
+    std::vector<u64> st((size_t)(4 * W + m + 8));
+
+    PairSpec s;
+    s.metric = metric;
+    s.op = op;
+    s.form = form;
+    s.l1 = (u64)m;
+    s.l2 = (u64)n;
+    s.ci = ci;
+    s.cf = cf;
+    s.p = ScoreParams{p->ins, p->del, p->rep, p->prefix_weight};
+    const int fam = metric_family(metric, form, s.p);
+    *oi = 0;
+    *of = 0.0;
+    if (fam == FAM_JARO) {
+        i64 prefix = 0;
+        const int mx = (m < n ? m : n) < 4 ? (m < n ? m : n) : 4;
+        for (; prefix < mx; ++prefix)
+            if (B[prefix] != A[prefix]) break;
+        int common = 0, transp = 0;
+        if (m > 0 && n > 0 && jaro_pair_needs_counts(s, prefix))
+            jaro_multi_rt(pm, W, m, txt, n, &common, &transp, st.data(), st.data() + W);
+        *of = finish_jaro(s, prefix, common, transp);
+        return 0;
+    }
+    const Plan pl = plan_int(s);
+    i64 raw = 0;
+    if (pl.run) {
+        const i64 K = pl.K;
+        const i64 diff = m > n ? m - n : n - m;
+        if (fam == FAM_WF) raw = (i64)wf_distance(q, m, t2, n, s.p, (u64)K, st.data());
+        else if (fam == FAM_LCS) {
+            if (m == 0 || n == 0) raw = 0;
+            else if (K < diff) raw = -1;
+            else raw = lcs_multi_rt(pm, W, m, txt, n, K, st.data());
+        }
+        else if (m == 0) raw = n;
+        else if (K < diff) raw = K + 1;
+        else if (n == 0) raw = m;
+        else if (fam == FAM_OSA)
+            raw = osa_multi_rt(pm, W, m, txt, n, K, st.data(), st.data() + W, st.data() + 2 * W, st.data() + 3 * W);
+        else if (K < m && 2 * K + 1 <= 64) raw = lev_band<1>(pm, W, m, txt, n, (int)K);
+        else if (K < m && 2 * K + 1 <= 128) raw = lev_band<2>(pm, W, m, txt, n, (int)K);
+        else if (K < m && 2 * K + 1 <= 256) raw = lev_band<4>(pm, W, m, txt, n, (int)K);
+        else if (K < m && 2 * K + 1 <= 512) raw = lev_band<8>(pm, W, m, txt, n, (int)K);
+        else raw = lev_multi_rt(pm, W, m, txt, n, K, st.data(), st.data() + W);
+    }
+    finish_int(s, pl, raw, oi, of);
+    return 0;
+}
+
+} /* extern "C" */
