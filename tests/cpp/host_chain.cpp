@@ -1,7 +1,8 @@
-/* One scorer call the way the any-length kernel makes it (score_pair_generic): the pair's
- * plan and formula chains (plan_int / finish_int / finish_jaro in rfg_core.cuh) around
- * the runtime-W cores, compiled for the host behind the oracle's rfo_score signature, so
- * the CPU tests can run the reference-made fixtures through the device code's chains.
+/* One scorer call the way the kernels make it: the pair's plan and formula chains
+ * (plan_int / finish_int / finish_jaro in rfg_core.cuh) around the runtime-W cores, as the
+ * any-length kernel runs them (score_pair_generic), or with the tile kernels' per-query
+ * length tables; compiled for the host behind the oracle's rfo_score signature, so the
+ * CPU tests can run the reference-made fixtures through the device code's chains.
  * Code units of any width: units below 256 index the table directly, wider ones get a row
  * each (a text unit the pattern lacks reads a zero row), as the kernels' hashed rows do. */
 #include <stdint.h>
@@ -44,14 +45,11 @@ std::vector<u64> widen(const void* s, int64_t n, int w)
     return v;
 }
 
-} // namespace
-
-extern "C" {
-
-/* rfo_score's arguments; free and Cached forms of Levenshtein .. ratio (metrics 0..6).
- * Returns 0, or -1 for a form or metric outside that set. */
-int hc_score(int metric, int op, int form, const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb,
-             const Params* p, uint64_t ci, double cf, int64_t* oi, double* of)
+/* tables: the per-query length tables of the tile kernels (text lengths up to
+ * RFG_JT_MAXT): the Jaro table (jaro_tab_head / jaro_tab_minc, finish_jaro_tab or the
+ * failing value) and the normalized chains' integer cutoff (chain_kd as kd_pre) */
+int score(int metric, int op, int form, const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb,
+          const Params* p, uint64_t ci, double cf, int64_t* oi, double* of, bool tables)
 {
     if (form == FORM_MULTI || metric < 0 || metric > RATIO) return -1;
     const std::vector<u64> A = widen(a, la, ca), B = widen(b, lb, cb);
@@ -83,17 +81,35 @@ int hc_score(int metric, int op, int form, const void* a, int64_t la, int ca, co
     const int fam = metric_family(metric, form, s.p);
     *oi = 0;
     *of = 0.0;
+    const bool tab = tables && n <= RFG_JT_MAXT;
     if (fam == FAM_JARO) {
         i64 prefix = 0;
         const int mx = (m < n ? m : n) < 4 ? (m < n ? m : n) : 4;
         for (; prefix < mx; ++prefix)
             if (B[prefix] != A[prefix]) break;
         int common = 0, transp = 0;
+        if (tab) {
+            JaroTab jt;
+            jaro_tab_head(jt, s);
+            const unsigned short mc = jaro_tab_minc(s, m, (int)prefix, n);
+            jt.minc[prefix][n] = mc;
+            const int cmax = m < n ? m : n;
+            const bool one = m == 1 && n == 1;
+            bool fail = mc != 0 && !one && (mc == 0xffff || cmax < (int)mc);
+            if (mc != 0 && !fail) {
+                jaro_multi_rt(pm, W, m, txt, n, &common, &transp, st.data(), st.data() + W);
+                fail = common < (one ? 0 : (int)mc);
+            }
+            if (mc == 0 && !(m == 0 && n == 0)) fail = true;
+            *of = fail ? jt.vfail[prefix] : finish_jaro_tab(s, jt, prefix, common, transp);
+            return 0;
+        }
         if (m > 0 && n > 0 && jaro_pair_needs_counts(s, prefix))
             jaro_multi_rt(pm, W, m, txt, n, &common, &transp, st.data(), st.data() + W);
         *of = finish_jaro(s, prefix, common, transp);
         return 0;
     }
+    if (tab && (metric == RATIO || op >= NORM_DISTANCE)) s.kd_pre = chain_kd(s);
     const Plan pl = plan_int(s);
     i64 raw = 0;
     if (pl.run) {
@@ -118,6 +134,25 @@ int hc_score(int metric, int op, int form, const void* a, int64_t la, int ca, co
     }
     finish_int(s, pl, raw, oi, of);
     return 0;
+}
+
+} // namespace
+
+extern "C" {
+
+/* rfo_score's arguments; free and Cached forms of Levenshtein .. ratio (metrics 0..6):
+ * the any-length kernel's path (hc_score) and the tile kernels' table path
+ * (hc_score_tab).  Return 0, or -1 for a form or metric outside that set. */
+int hc_score(int metric, int op, int form, const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb,
+             const Params* p, uint64_t ci, double cf, int64_t* oi, double* of)
+{
+    return score(metric, op, form, a, la, ca, b, lb, cb, p, ci, cf, oi, of, false);
+}
+
+int hc_score_tab(int metric, int op, int form, const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb,
+                 const Params* p, uint64_t ci, double cf, int64_t* oi, double* of)
+{
+    return score(metric, op, form, a, la, ca, b, lb, cb, p, ci, cf, oi, of, true);
 }
 
 } /* extern "C" */

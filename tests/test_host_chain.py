@@ -1,6 +1,7 @@
 """CPU tests of the device code's formula chains: the pair plan and chains of the
 any-length kernel (plan_int / finish_int / finish_jaro around the runtime-W cores,
-rfg_core.cuh) compiled for the host behind tests/cpp/host_chain.cpp, run on the
+rfg_core.cuh) and the tile kernels' per-query length tables (Jaro table, normalized
+chains' integer cutoff) compiled for the host behind tests/cpp/host_chain.cpp, run on the
 reference-made fixtures kat.json and random.json (free and Cached forms of Levenshtein
 with every weight set, Indel, LCSseq, OSA, Jaro, Jaro-Winkler and ratio, all four ops,
 every code-unit width, default and explicit cutoffs), ints equal and doubles bit for bit.
@@ -34,20 +35,23 @@ def _build(name, sources, extra=()):
 def chain():
     lib = _build("libhost_chain.so", [os.path.join(ROOT, "tests", "cpp", "host_chain.cpp")])
     P, I64, I = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
-    lib.hc_score.restype = I
-    lib.hc_score.argtypes = [I, I, I, P, I64, I, P, I64, I, ctypes.POINTER(Params), ctypes.c_uint64,
-                             ctypes.c_double, ctypes.POINTER(I64), ctypes.POINTER(ctypes.c_double)]
+    for f in (lib.hc_score, lib.hc_score_tab):
+        f.restype = I
+        f.argtypes = [I, I, I, P, I64, I, P, I64, I, ctypes.POINTER(Params), ctypes.c_uint64, ctypes.c_double,
+                      ctypes.POINTER(I64), ctypes.POINTER(ctypes.c_double)]
     return lib
 
 
 @pytest.mark.parametrize("fixture", ["kat.json", "random.json"])
-def test_chains_match_reference_fixtures(chain, fixture):
+@pytest.mark.parametrize("entry", ["hc_score", "hc_score_tab"], ids=["any_length_path", "length_tables"])
+def test_chains_match_reference_fixtures(chain, fixture, entry):
+    fn = getattr(chain, entry)
     n, bad = 0, []
     for c in G.load(fixture):
         if c["form"] == MULTI or c["metric"] > 6:
             continue
         a, b = G.arrays(c)
-        v = score(chain.hc_score, c["metric"], c["op"], c["form"], a, b, c["cutoff"], tuple(c["weights"]), c["pw"])
+        v = score(fn, c["metric"], c["op"], c["form"], a, b, c["cutoff"], tuple(c["weights"]), c["pw"])
         n += 1
         if not G.same(v, G.dec(c["expected"])):
             bad.append((c, v))
