@@ -51,7 +51,7 @@ std::vector<u64> widen(const void* s, int64_t n, int w)
 int score(int metric, int op, int form, const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb,
           const Params* p, uint64_t ci, double cf, int64_t* oi, double* of, bool tables)
 {
-    if (form == FORM_MULTI || metric < 0 || metric > RATIO) return -1;
+    if (metric < 0 || metric > RATIO) return -1;
     const std::vector<u64> A = widen(a, la, ca), B = widen(b, lb, cb);
     std::map<u64, u64> wide;
     for (u64 x : A)
@@ -81,7 +81,7 @@ int score(int metric, int op, int form, const void* a, int64_t la, int ca, const
     const int fam = metric_family(metric, form, s.p);
     *oi = 0;
     *of = 0.0;
-    const bool tab = tables && n <= RFG_JT_MAXT;
+    const bool tab = tables && n <= RFG_JT_MAXT && form != FORM_MULTI; /* the kernels: no tables for Multi */
     if (fam == FAM_JARO) {
         i64 prefix = 0;
         const int mx = (m < n ? m : n) < 4 ? (m < n ? m : n) : 4;
@@ -140,9 +140,9 @@ int score(int metric, int op, int form, const void* a, int64_t la, int ca, const
 
 extern "C" {
 
-/* rfo_score's arguments; free and Cached forms of Levenshtein .. ratio (metrics 0..6):
+/* rfo_score's arguments; free, Cached and Multi forms of Levenshtein .. ratio (metrics 0..6):
  * the any-length kernel's path (hc_score) and the tile kernels' table path
- * (hc_score_tab).  Return 0, or -1 for a form or metric outside that set. */
+ * (hc_score_tab).  Return 0, or -1 for a metric outside that set. */
 int hc_score(int metric, int op, int form, const void* a, int64_t la, int ca, const void* b, int64_t lb, int cb,
              const Params* p, uint64_t ci, double cf, int64_t* oi, double* of)
 {
