@@ -426,6 +426,64 @@ extern "C" int rfref_opcodes(const rfo_editop* ops, int64_t n, const void* a, in
     return 0;
 }
 
+/* the list operations of Editops / Opcodes (details/types.hpp:109-161, 240-320, 420-475)
+ * of the unmodified headers on one operation list: which 0 Editops::slice, 1
+ * remove_slice, 2 reverse, 3 inverse, 4 remove_subsequence(slice(start, stop, step)); 10
+ * Opcodes(ops).slice, 12 reverse, 13 inverse.  out gets 3
+ * int64 per edit operation or 5 per opcode (up to cap records), lens the result's
+ * src_len / dest_len.  Returns 0, or -1 where the reference throws invalid_argument. */
+extern "C" int rfref_list_op(int which, const rfo_editop* ops, int64_t n, int64_t src_len, int64_t dest_len, int start,
+                             int stop, int step, int64_t* out, int64_t cap, int64_t* count, int64_t* lens)
+{
+    rapidfuzz::Editops e((size_t)n);
+    for (int64_t k = 0; k < n; ++k)
+        e[(size_t)k] = rapidfuzz::EditOp((rapidfuzz::EditType)ops[k].type, (size_t)ops[k].src_pos,
+                                         (size_t)ops[k].dest_pos);
+    e.set_src_len((size_t)src_len);
+    e.set_dest_len((size_t)dest_len);
+    try {
+        if (which < 10) {
+            rapidfuzz::Editops r;
+            if (which == 0) r = e.slice(start, stop, step);
+            else if (which == 1) {
+                r = e;
+                r.remove_slice(start, stop, step);
+            }
+            else if (which == 2) r = e.reverse();
+            else if (which == 3) r = e.inverse();
+            else r = e.remove_subsequence(e.slice(start, stop, step));
+            *count = (int64_t)r.size();
+            for (size_t k = 0; k < r.size() && (int64_t)k < cap; ++k) {
+                out[3 * k] = (int64_t)r[k].type;
+                out[3 * k + 1] = (int64_t)r[k].src_pos;
+                out[3 * k + 2] = (int64_t)r[k].dest_pos;
+            }
+            lens[0] = (int64_t)r.get_src_len();
+            lens[1] = (int64_t)r.get_dest_len();
+            return 0;
+        }
+        const rapidfuzz::Opcodes o(e);
+        rapidfuzz::Opcodes r;
+        if (which == 10) r = o.slice(start, stop, step);
+        else if (which == 12) r = o.reverse();
+        else r = o.inverse();
+        *count = (int64_t)r.size();
+        for (size_t k = 0; k < r.size() && (int64_t)k < cap; ++k) {
+            out[5 * k] = (int64_t)r[k].type;
+            out[5 * k + 1] = (int64_t)r[k].src_begin;
+            out[5 * k + 2] = (int64_t)r[k].src_end;
+            out[5 * k + 3] = (int64_t)r[k].dest_begin;
+            out[5 * k + 4] = (int64_t)r[k].dest_end;
+        }
+        lens[0] = (int64_t)r.get_src_len();
+        lens[1] = (int64_t)r.get_dest_len();
+        return 0;
+    }
+    catch (const std::invalid_argument&) {
+        return -1;
+    }
+}
+
 /* Multi* with several inserted strings (padding semantics, result order) */
 extern "C" int rfref_multi(int metric, int op, int max_len, const rfo_strings* inserted, const void* b, int64_t lb,
                            int cb, const rfo_params* p, uint64_t ci, double cf, int64_t* oi, double* of,

@@ -20,6 +20,7 @@
  */
 #pragma once
 
+#include <algorithm>
 #include <cstddef>
 #include <cstdint>
 #include <iterator>
@@ -459,7 +460,27 @@ struct EditOp {
     bool operator!=(const EditOp& o) const { return !(*this == o); }
 };
 
-/* the operations plus the source and destination lengths (details/types.hpp:167-...) */
+namespace detail {
+/* the positions a slice takes (details/types.hpp:109-161): a positive step; negative
+ * bounds count from the end and clamp at 0, bounds past the end clamp to the size */
+inline std::vector<size_t> slice_positions(size_t size, int start, int stop, int step)
+{
+    if (step == 0) throw std::invalid_argument("slice step cannot be zero");
+    if (step < 0) throw std::invalid_argument("step sizes below 0 lead to an invalid order of editops");
+    const int n = (int)size;
+    start = start < 0 ? std::max(start + n, 0) : std::min(start, n);
+    stop = stop < 0 ? std::max(stop + n, 0) : std::min(stop, n);
+    std::vector<size_t> pos;
+    for (int i = start; i < stop; i += step) pos.push_back((size_t)i);
+    return pos;
+}
+inline EditType swapped(EditType t)
+{
+    return t == EditType::Insert ? EditType::Delete : t == EditType::Delete ? EditType::Insert : t;
+}
+} // namespace detail
+
+/* the operations plus the source and destination lengths (details/types.hpp:167-356) */
 class Editops : public std::vector<EditOp> {
 public:
     Editops() = default;
@@ -468,7 +489,67 @@ public:
     void set_src_len(size_t n) { src_len_ = n; }
     void set_dest_len(size_t n) { dest_len_ = n; }
 
+    Editops slice(int start, int stop, int step = 1) const
+    {
+        Editops r = empty_like();
+        for (size_t i : detail::slice_positions(size(), start, stop, step)) r.push_back((*this)[i]);
+        return r;
+    }
+    void remove_slice(int start, int stop, int step = 1)
+    {
+        const std::vector<size_t> drop = detail::slice_positions(size(), start, stop, step);
+        std::vector<EditOp> keep;
+        size_t d = 0;
+        for (size_t i = 0; i < size(); ++i) {
+            if (d < drop.size() && drop[d] == i) ++d;
+            else keep.push_back((*this)[i]);
+        }
+        std::vector<EditOp>::operator=(keep);
+    }
+    Editops reverse() const
+    {
+        Editops r(*this);
+        std::reverse(r.begin(), r.end());
+        return r;
+    }
+    /* the operations turning the destination into the source */
+    Editops inverse() const
+    {
+        Editops r;
+        r.src_len_ = dest_len_;
+        r.dest_len_ = src_len_;
+        for (const EditOp& op : *this) r.emplace_back(detail::swapped(op.type), op.dest_pos, op.src_pos);
+        return r;
+    }
+    /* the operations left once those of sub (in order) are taken out; source positions
+     * shift by the removed insertions and deletions */
+    Editops remove_subsequence(const Editops& sub) const
+    {
+        if (sub.size() > size()) throw std::invalid_argument("subsequence is not a subsequence");
+        Editops r = empty_like();
+        long long offset = 0;
+        size_t it = 0;
+        auto keep = [&](const EditOp& op) {
+            r.emplace_back(op.type, (size_t)((long long)op.src_pos + offset), op.dest_pos);
+        };
+        for (const EditOp& sop : sub) {
+            for (; it < size() && (*this)[it] != sop; ++it) keep((*this)[it]);
+            if (it == size()) throw std::invalid_argument("subsequence is not a subsequence");
+            offset += sop.type == EditType::Insert ? 1 : sop.type == EditType::Delete ? -1 : 0;
+            ++it;
+        }
+        for (; it < size(); ++it) keep((*this)[it]);
+        return r;
+    }
+
 private:
+    Editops empty_like() const
+    {
+        Editops r;
+        r.src_len_ = src_len_;
+        r.dest_len_ = dest_len_;
+        return r;
+    }
     size_t src_len_ = 0, dest_len_ = 0;
 };
 
@@ -532,6 +613,27 @@ public:
     }
     size_t get_src_len() const { return src_len_; }
     size_t get_dest_len() const { return dest_len_; }
+    Opcodes slice(int start, int stop, int step = 1) const
+    {
+        Opcodes r = empty_like();
+        for (size_t i : detail::slice_positions(size(), start, stop, step)) r.push_back((*this)[i]);
+        return r;
+    }
+    Opcodes reverse() const
+    {
+        Opcodes r(*this);
+        std::reverse(r.begin(), r.end());
+        return r;
+    }
+    Opcodes inverse() const
+    {
+        Opcodes r;
+        r.src_len_ = dest_len_;
+        r.dest_len_ = src_len_;
+        for (const Opcode& o : *this)
+            r.emplace_back(detail::swapped(o.type), o.dest_begin, o.dest_end, o.src_begin, o.src_end);
+        return r;
+    }
     /* Editops(const Opcodes&) (details/types.hpp:500-524) */
     Editops as_editops() const
     {
@@ -553,6 +655,13 @@ public:
     }
 
 private:
+    Opcodes empty_like() const
+    {
+        Opcodes r;
+        r.src_len_ = src_len_;
+        r.dest_len_ = dest_len_;
+        return r;
+    }
     size_t src_len_ = 0, dest_len_ = 0;
 };
 

@@ -213,6 +213,21 @@ __all__.append("experimental")
 
 
 
+def _slice_indices(n, start, stop, step):
+    """the positions a slice takes (details/types.hpp:109-135): step must be positive;
+    negative bounds count from the end and clamp at 0, bounds past the end clamp to n"""
+    if step == 0:
+        raise ValueError("slice step cannot be zero")
+    if step < 0:
+        raise ValueError("step sizes below 0 lead to an invalid order of editops")
+    start = max(start + n, 0) if start < 0 else min(start, n)
+    stop = max(stop + n, 0) if stop < 0 else min(stop, n)
+    return range(start, stop, step) if start < stop else range(0)
+
+
+_SWAP = {"insert": "delete", "delete": "insert"}
+
+
 class EditOp(tuple):
     """rapidfuzz::EditOp (details/types.hpp:45-56): (type, src_pos, dest_pos), type one of
     'none', 'replace', 'insert', 'delete'"""
@@ -244,6 +259,45 @@ class Editops(list):
 
     def as_opcodes(self):
         return Opcodes.from_editops(self)
+
+    def slice(self, start, stop, step=1):
+        """Editops::slice (details/types.hpp:240-245): the lengths are kept"""
+        return Editops([self[i] for i in _slice_indices(len(self), start, stop, step)], self.src_len, self.dest_len)
+
+    def remove_slice(self, start, stop, step=1):
+        """Editops::remove_slice (details/types.hpp:247-250, 137-161), in place"""
+        drop = set(_slice_indices(len(self), start, stop, step))
+        self[:] = [op for i, op in enumerate(self) if i not in drop]
+
+    def reverse(self):
+        """Editops::reverse: the operations in reverse order (a new list)"""
+        return Editops(self[::-1], self.src_len, self.dest_len)
+
+    def inverse(self):
+        """Editops::inverse (details/types.hpp:276-288): the operations turning the
+        destination into the source"""
+        return Editops([tuple.__new__(EditOp, (_SWAP.get(t, t), d, s)) for t, s, d in self], self.dest_len,
+                       self.src_len)
+
+    def remove_subsequence(self, subsequence):
+        """Editops::remove_subsequence (details/types.hpp:290-320): the operations left
+        once those of subsequence (in order) are taken out, source positions shifted by the
+        removed insertions and deletions"""
+        if len(subsequence) > len(self):
+            raise ValueError("subsequence is not a subsequence")
+        out, offset, it = [], 0, 0
+        for sop in subsequence:
+            while it < len(self) and tuple(self[it]) != tuple(sop):
+                t, sp, dp = self[it]
+                out.append(tuple.__new__(EditOp, (t, sp + offset, dp)))
+                it += 1
+            if it == len(self):
+                raise ValueError("subsequence is not a subsequence")
+            offset += 1 if sop[0] == "insert" else -1 if sop[0] == "delete" else 0
+            it += 1
+        for t, sp, dp in self[it:]:
+            out.append(tuple.__new__(EditOp, (t, sp + offset, dp)))
+        return Editops(out, self.src_len, self.dest_len)
 
     def apply(self, s1, s2):
         """editops_apply (rapidfuzz/distance.hpp:19-60): s1 turned into s2, as a list"""
@@ -304,6 +358,19 @@ class Opcodes(list):
         if sp < e.src_len or dp < e.dest_len:
             out.append(Opcode("none", sp, e.src_len, dp, e.dest_len))
         return cls(out, e.src_len, e.dest_len)
+
+    def slice(self, start, stop, step=1):
+        """Opcodes::slice (details/types.hpp:429-435): the lengths are kept"""
+        return Opcodes([self[i] for i in _slice_indices(len(self), start, stop, step)], self.src_len, self.dest_len)
+
+    def reverse(self):
+        """Opcodes::reverse: the runs in reverse order (a new list)"""
+        return Opcodes(self[::-1], self.src_len, self.dest_len)
+
+    def inverse(self):
+        """Opcodes::inverse (details/types.hpp:461-474)"""
+        return Opcodes([Opcode(_SWAP.get(t, t), db, de, sb, se) for t, sb, se, db, de in self], self.dest_len,
+                       self.src_len)
 
     def as_editops(self):
         """Editops(const Opcodes&) (details/types.hpp:500-524)"""

@@ -14,7 +14,9 @@ Fixtures:
                 WRatio (free and Cached forms);
   editops.json  levenshtein_editops / indel_editops / lcs_seq_editops;
   opcodes.json  the reference's Opcodes / Editops conversions and applies of editops.json's
-                one-byte pairs.
+                one-byte pairs;
+  listops.json  the list operations of Editops / Opcodes (slice, remove_slice, reverse,
+                inverse, remove_subsequence) on editops.json's operation lists.
 Doubles are stored with float.hex() so the comparison is bit-exact.
 
 Usage: python tests/golden/make_golden.py   (needs the reference checkout; run in the
@@ -565,14 +567,54 @@ def opcodes_cases(limit=600):
     return out
 
 
+def listops_cases(limit=300, seed=23):
+    """Editops slice / remove_slice / reverse / inverse / remove_subsequence and Opcodes
+    slice / reverse / inverse (details/types.hpp:109-161, 240-320, 420-475) of the
+    reference on operation lists of editops.json, with seeded slice bounds (negative,
+    past the end, empty) and steps 1..3 (step 0 and negative steps: the reference's
+    invalid_argument, recorded as null)."""
+    ref = reference()
+    P, I64, I = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+    fn = ref.rfref_list_op
+    fn.restype = I
+    fn.argtypes = [I, P, I64, I64, I64, I, I, I, P, I64, P, P]
+    with open(os.path.join(HERE, "editops.json")) as f:
+        eops = json.load(f)
+    rng = random.Random(seed)
+    picks = [i for i, c in enumerate(eops) if len(c["expected"]) <= 60]
+    rng.shuffle(picks)
+    out = []
+    for i in picks[:limit]:
+        c = eops[i]
+        n = len(c["expected"])
+        ops = np.zeros(max(n, 1), dtype=[("type", "<i4"), ("reserved", "<i4"), ("src_pos", "<i8"), ("dest_pos", "<i8")])
+        for k, (t, sp, dp) in enumerate(c["expected"]):
+            ops[k] = (t, 0, sp, dp)
+        for which in (0, 1, 2, 3, 4, 10, 12, 13):
+            start = rng.choice([0, 1, 2, -1, -3, n // 2, n, n + 5, -n - 5])
+            stop = rng.choice([n, n - 1, 1, -1, -2, n // 2, n + 5, 0])
+            step = rng.choice([1, 1, 2, 3, 0, -1]) if which in (0, 1, 4, 10) else 1
+            cap = 2 * (len(c["s1"]) + len(c["s2"])) + 4
+            res = np.zeros(5 * cap, dtype=np.int64)
+            cnt = ctypes.c_int64()
+            lens = np.zeros(2, dtype=np.int64)
+            rc = fn(which, ops.ctypes.data, n, len(c["s1"]), len(c["s2"]), start, stop, step, res.ctypes.data, cap,
+                    ctypes.byref(cnt), lens.ctypes.data)
+            rec = 3 if which < 10 else 5
+            out.append({"case": i, "which": which, "start": start, "stop": stop, "step": step,
+                        "result": None if rc else res[:rec * cnt.value].reshape(-1, rec).tolist(),
+                        "lens": None if rc else lens.tolist()})
+    return out
+
+
 def main():
     if reference() is None:
         sys.exit("oracle/_ref/librfref.so is missing: run `make -C oracle ref` where the reference checkout exists")
     which = sys.argv[1:] or ["kat.json", "random.json", "multi.json", "partial.json", "tokens.json", "tokenset.json",
-                             "editops.json", "opcodes.json"]
+                             "editops.json", "opcodes.json", "listops.json"]
     gens = {"kat.json": kat_cases, "random.json": lambda: random_cases(4000), "multi.json": multi_cases,
             "partial.json": partial_cases, "tokens.json": token_cases, "tokenset.json": tokenset_cases,
-            "editops.json": editops_cases, "opcodes.json": opcodes_cases}
+            "editops.json": editops_cases, "opcodes.json": opcodes_cases, "listops.json": listops_cases}
     for name, cases in ((n, gens[n]()) for n in which):
         with open(os.path.join(HERE, name), "w") as f:
             json.dump(cases, f, separators=(",", ":"))
