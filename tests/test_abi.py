@@ -128,6 +128,11 @@ def test_reference_names_are_mirrored():
     oc = e.as_opcodes()
     assert list(oc.as_editops()) == list(e) and oc.src_len == 5 and oc.dest_len == 6
     assert "".join(e.apply("abcde", "xabcyz")[:1]) == "x"
+    for name in ("slice", "remove_slice", "reverse", "inverse", "remove_subsequence"):
+        assert callable(getattr(e, name))
+    for name in ("slice", "reverse", "inverse"):
+        assert callable(getattr(oc, name))
+    assert e.inverse().inverse() == e and e.reverse().reverse() == e
 
 
 @pytest.mark.parametrize("std", ["c++11", "c++17"])
