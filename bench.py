@@ -76,7 +76,7 @@ def dist_env():
 
 
 def workload(rank, nq, nc):
-    from rapidfuzz_gb300.workloads import cdist_zipf
+    from workloads import cdist_zipf
     return cdist_zipf(seed=1234 + rank, nq=nq, nc=nc)
 
 

@@ -78,7 +78,7 @@ def _cells(q, c):
 def run(args, rank, world, local):
     import torch
     import rapidfuzz_gb300 as R
-    from rapidfuzz_gb300 import workloads as WL
+    import workloads as WL
     from oracle_lib import oracle_cdist
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)

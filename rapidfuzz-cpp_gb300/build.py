@@ -2,6 +2,7 @@
 translation unit compiled in parallel, linked into lib/librapidfuzz_gb300.so."""
 import concurrent.futures
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -14,6 +15,9 @@ LIB_DIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIB_DIR, "librapidfuzz_gb300.so")
 PEAK_LIB = os.path.join(LIB_DIR, "librfg_peak.so")  # INT32 issue-rate microbenchmark (bench roofline)
 COUNT_LIB = os.path.join(LIB_DIR, "librfg_count.so")  # executed word steps of the kernels (bench roofline)
+# the machine the libraries in lib/ were built on: a tree copied to another machine
+# (an x86-64 build container, an aarch64 GPU host) rebuilds instead of reusing them
+STAMP = os.path.join(LIB_DIR, "build_machine.txt")
 
 SOURCES = ["rfg_api.cu", "rfg_k_lev.cu", "rfg_k_lcs.cu", "rfg_k_osa.cu", "rfg_k_jaro.cu", "rfg_k_generic.cu", "rfg_noalloc.cu", "rfg_server.cu",
            "rfg_k_token.cu", "rfg_k_editops.cu", "rfg_token.cpp"]
@@ -42,9 +46,18 @@ def _compile(src):
     return obj
 
 
+def _stamp_matches():
+    try:
+        with open(STAMP) as f:
+            return f.read().strip() == platform.machine()
+    except OSError:
+        return False
+
+
 def build(force=False, verbose=False):
-    """Compile the library if any source is newer than it; returns the .so path."""
-    if not force and all(os.path.exists(x) for x in (LIB, PEAK_LIB, COUNT_LIB)):
+    """Compile the library if any source is newer than it, or if it was built on another
+    kind of machine; returns the .so path."""
+    if not force and _stamp_matches() and all(os.path.exists(x) for x in (LIB, PEAK_LIB, COUNT_LIB)):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in _deps()):
             return LIB
@@ -67,8 +80,10 @@ def build(force=False, verbose=False):
                         "-o", COUNT_LIB, os.path.join(CSRC, "rfg_count.cpp")], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("work counter build failed:\n%s%s" % (r.stdout, r.stderr))
+    with open(STAMP, "w") as f:
+        f.write(platform.machine() + "\n")
     if verbose:
-        print("built", LIB)
+        print("built", LIB, "on", platform.machine())
     return LIB
 
 

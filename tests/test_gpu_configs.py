@@ -9,7 +9,7 @@ from oracle_lib import oracle_cdist
 pytestmark = pytest.mark.gpu
 
 import rapidfuzz_gb300 as R  # noqa: E402
-from rapidfuzz_gb300 import workloads as WL  # noqa: E402
+import workloads as WL  # noqa: E402
 
 
 def _same(a, b):

@@ -12,7 +12,7 @@ from extract_lib import oracle_extract
 pytestmark = pytest.mark.gpu
 
 import rapidfuzz_gb300 as R  # noqa: E402
-from rapidfuzz_gb300 import workloads as WL  # noqa: E402
+import workloads as WL  # noqa: E402
 
 
 def _dna(rng, n):

@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 import rapidfuzz_gb300 as R  # noqa: E402
 from rapidfuzz_gb300._lib import Cutoff, Strings, make_params, check  # noqa: E402
-from rapidfuzz_gb300.workloads import dna_lognormal, tokens_u32  # noqa: E402
+from workloads import dna_lognormal, tokens_u32  # noqa: E402
 
 
 def _device_batch(torch, data, offsets, width):
