@@ -158,3 +158,22 @@ def tokens_u32_fast(seed=0, n=1_000_000):
     sep_pos = off[owner] + (tok_end - str_start_all)
     data[sep_pos[~is_last]] = 0x20
     return data, off, 4
+
+
+def tokens_u32_mixed(seed=0, n=1_000_000, derive_from=None, derive_count=0):
+    """tokens_u32_fast strings with derive_count of them (at seeded positions) replaced by
+    copies of derive_from strings with 0-3 random edits, so that hits above a cutoff exist"""
+    data, off, w = tokens_u32_fast(seed=seed, n=n)
+    if not derive_from or derive_count <= 0:
+        return data, off, w
+    rng = np.random.default_rng(seed + 7919)
+    pos = set(int(x) for x in rng.choice(n, size=derive_count, replace=False))
+    out = []
+    for i in range(n):
+        if i in pos:
+            base = derive_from[int(rng.integers(0, len(derive_from)))]
+            out.append(np.asarray(mutate(rng, list(base), TOKEN_ALPHABET, int(rng.integers(0, 4))), dtype=np.uint32))
+        else:
+            out.append(data[off[i]:off[i + 1]])
+    d, o = _pack(out, np.uint32)
+    return d, o, 4
