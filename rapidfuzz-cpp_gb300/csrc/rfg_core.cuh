@@ -449,6 +449,122 @@ RFG_HD void group_word_dist(const PMQ& pm, const int* m, int qn, const TXT& t, i
     }
 }
 
+/* popcount of a recurrence word (one POPC for 32-bit words) */
+RFG_HD int popc_w(u64 x) { return popc64(x); }
+RFG_HD int popc_w(u32 x)
+{
+#ifdef __CUDA_ARCH__
+    return __popc(x);
+#else
+    return __builtin_popcount(x);
+#endif
+}
+
+/* The unit-weight distance chain d <= K ? d : K + 1 of Q one-word patterns against one
+ * text, for the warp tiles of the distance fast path: Levenshtein 1/1/1 (Hyyro 2003,
+ * Levenshtein_impl.hpp:259-322), OSA (OSA_impl.hpp:34-74) or Indel (d = m + n - 2 LCS,
+ * LCSseq_impl.hpp:205-260), with the length filter and empty-string rules of those
+ * functions (Levenshtein_impl.hpp:863, LCSseq_impl.hpp:389) and the diagonal lower-bound
+ * exit every 8 text units, so every d equals the single-pair result.  Lengths and K are
+ * below 2^31 (int bookkeeping: every 64-bit integer operation costs two ALU instructions
+ * on the GPU).  pm(q, c): pattern word of pattern q for table row c (t[j] gives rows);
+ * m[q] <= bits of WT.  The LCS step S' = (S + u) | (S - u) with u = S & X is written as
+ * (S + u) | (S & ~X): u is a subset of S, so S - u = S & ~X, which a single three-input
+ * logic instruction merges with the OR. */
+template <int FAM, int Q, typename PMQ, typename TXT, typename WT>
+RFG_HD void fast_group(const PMQ& pm, const int* m, int qn, const TXT& t, int n, int K, int* d)
+{
+    WT A[Q], B[Q], D0[Q], PO[Q]; /* Lev / OSA: VP, VN, D0, previous X; Indel: S in A */
+    unsigned live = 0, chk = 0; /* chk: the cutoff is below the largest possible distance */
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        A[q] = (WT)~(WT)0;
+        B[q] = D0[q] = PO[q] = 0;
+        d[q] = 0;
+        if (q >= qn) continue;
+        const int mq = m[q];
+        const int diff = mq > n ? mq - n : n - mq;
+        if (FAM == FAM_LCS) {
+            if (mq == 0 || n == 0) d[q] = mq + n;
+            else if (K < diff) d[q] = K + 1;
+            else {
+                live |= 1u << q;
+                if (K < mq + n) chk |= 1u << q;
+            }
+        }
+        else {
+            if (mq == 0) d[q] = n;
+            else if (K < diff) d[q] = K + 1;
+            else if (n == 0) d[q] = mq;
+            else {
+                live |= 1u << q;
+                if (K < (mq > n ? mq : n)) chk |= 1u << q;
+            }
+        }
+    }
+    auto block = [&](int j0, auto full) {
+        constexpr bool FULL = decltype(full)::value;
+        unsigned c[RFG_FETCH];
+#pragma unroll
+        for (int k = 0; k < RFG_FETCH; ++k) c[k] = (FULL || j0 + k < n) ? (unsigned)t[j0 + k] : 0u;
+        const int kn = FULL ? RFG_FETCH : n - j0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            if (!((live >> q) & 1u)) continue;
+#pragma unroll
+            for (int k = 0; k < RFG_FETCH; ++k) {
+                if (FULL || k < kn) {
+                    const WT X = (WT)pm(q, c[k]);
+                    if (FAM == FAM_LCS) {
+                        const WT S = A[q];
+                        A[q] = (WT)(S + (WT)(S & X)) | (WT)(S & (WT)~X);
+                    }
+                    else {
+                        const WT VP = A[q], VN = B[q];
+                        WT D = (WT)((WT)((X & VP) + VP) ^ VP) | X | VN;
+                        if (FAM == FAM_OSA) {
+                            D |= (WT)(((WT)~D0[q] & X) << 1) & PO[q];
+                            D0[q] = D;
+                            PO[q] = X;
+                        }
+                        WT HP = VN | (WT)~(D | VP);
+                        const WT HN = D & VP;
+                        HP = (WT)(HP << 1) | (WT)1;
+                        const WT HNs = (WT)(HN << 1);
+                        A[q] = HNs | (WT)~(D | HP);
+                        B[q] = HP & D;
+                    }
+                }
+            }
+            if (FULL && ((chk >> q) & 1u)) {
+                /* lower bound at column jj on the diagonal through (m, n) */
+                const int jj = j0 + RFG_FETCH, is = m[q] - n + jj;
+                if (is >= 0) {
+                    const WT lm = (WT)low_mask(is);
+                    const int lb = FAM == FAM_LCS ? is + jj - 2 * popc_w((WT)(~A[q] & lm))
+                                                  : jj + popc_w((WT)(A[q] & lm)) - popc_w((WT)(B[q] & lm));
+                    if (lb > K) {
+                        d[q] = K + 1;
+                        live &= ~(1u << q);
+                    }
+                }
+            }
+        }
+    };
+    int j0 = 0;
+    for (; j0 + RFG_FETCH <= n && live; j0 += RFG_FETCH) block(j0, std::integral_constant<bool, true>());
+    if (j0 < n && live) block(j0, std::integral_constant<bool, false>());
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if ((live >> q) & 1u) {
+            const WT mm = (WT)low_mask(m[q]);
+            d[q] = FAM == FAM_LCS ? m[q] + n - 2 * popc_w((WT)(~A[q] & mm))
+                                  : n + popc_w((WT)(A[q] & mm)) - popc_w((WT)(B[q] & mm));
+        }
+        d[q] = d[q] <= K ? d[q] : K + 1;
+    }
+}
+
 /* Jaro flagging, P (= s1) 1..64 chars, effective text length <= 64
  * (Jaro_impl.hpp:94-132, 258-276).  Returns common chars, transpositions (unhalved). */
 template <typename PMF, typename TXT>

@@ -156,6 +156,38 @@ int hc_group(int fam, int word32, const uint8_t* a1, int m1, const uint8_t* a2, 
     return 0;
 }
 
+/* the warp tiles' core (fast_group, int bookkeeping, one cutoff K for every pattern) on
+ * four patterns (packed, offsets off[0..4]) of at most 64 units (32 with word32) against
+ * one text; qn of the four slots are used; out[q] = the distance chain of pattern q */
+int hc_fast(int fam, int word32, const uint8_t* pats, const int64_t* off, int qn, const uint8_t* b, int n, int K,
+            int* out)
+{
+    std::vector<u64> rows(4 * 257, 0);
+    int m[4] = {0, 0, 0, 0};
+    for (int q = 0; q < qn; ++q) {
+        m[q] = (int)(off[q + 1] - off[q]);
+        if (m[q] > (word32 ? 32 : 64)) return -2;
+        for (int k = 0; k < m[q]; ++k) rows[q * 257 + pats[off[q] + k]] |= 1ull << k;
+    }
+    const PMQ pm{rows.data()};
+    const Txt t{b};
+    int d[4] = {0, 0, 0, 0};
+    if (fam == 0) {
+        if (word32) fast_group<FAM_LEV, 4, PMQ, Txt, u32>(pm, m, qn, t, n, K, d);
+        else fast_group<FAM_LEV, 4, PMQ, Txt, u64>(pm, m, qn, t, n, K, d);
+    }
+    else if (fam == 1) {
+        if (word32) fast_group<FAM_LCS, 4, PMQ, Txt, u32>(pm, m, qn, t, n, K, d);
+        else fast_group<FAM_LCS, 4, PMQ, Txt, u64>(pm, m, qn, t, n, K, d);
+    }
+    else {
+        if (word32) fast_group<FAM_OSA, 4, PMQ, Txt, u32>(pm, m, qn, t, n, K, d);
+        else fast_group<FAM_OSA, 4, PMQ, Txt, u64>(pm, m, qn, t, n, K, d);
+    }
+    for (int q = 0; q < qn; ++q) out[q] = d[q];
+    return 0;
+}
+
 /* Jaro common characters and (unhalved) transpositions, m, n > 0.  variant 0: jaro_word
  * (pattern <= 64 units, effective text end <= 64); 1: jaro_multi<W> (W = 1, 2, 4, 8);
  * 2: jaro_multi_rt; 3: group_jaro_word with the pattern in both slots (as variant 0).

@@ -33,6 +33,8 @@ def libs():
     lib.hc_distance.argtypes = [I, I, P, I, P, I, I64]
     lib.hc_group.restype = I
     lib.hc_group.argtypes = [I, I, P, I, P, I, P, I, I64, I64, P]
+    lib.hc_fast.restype = I
+    lib.hc_fast.argtypes = [I, I, P, P, I, P, I, I, P]
     lib.hc_jaro.restype = I
     lib.hc_jaro.argtypes = [I, P, I, P, I, P, P]
     o = oracle()
@@ -115,6 +117,29 @@ def test_several_queries_core_matches_oracle(libs, fam, word32):
         for K1, K2 in zip(cutoffs(rng, d1), reversed(cutoffs(rng, d2))):
             assert lib.hc_group(fam, word32, a1, len(a1), a2, len(a2), b, len(b), K1, K2, out) == 0
             assert list(out) == [d1 if d1 <= K1 else K1 + 1, d2 if d2 <= K2 else K2 + 1], (a1, a2, b, K1, K2)
+
+
+@pytest.mark.parametrize("fam", [0, 1, 2], ids=["levenshtein", "indel", "osa"])
+@pytest.mark.parametrize("word32", [0, 1], ids=["64bit", "32bit"])
+def test_warp_tile_core_matches_oracle(libs, fam, word32):
+    """fast_group: one to four patterns per text, one cutoff, int bookkeeping"""
+    lib, o = libs
+    rng = np.random.default_rng(50 + fam + 3 * word32)
+    lens = [0, 1, 2, 7, 8, 9, 15, 16, 17, 24, 31, 32] + ([] if word32 else [33, 40, 48, 63, 64])
+    ps = pairs(60 + fam + 3 * word32, 2000, lens)
+    out = (ctypes.c_int * 4)()
+    for k in range(0, len(ps) - 3, 4):
+        qn = int(rng.integers(1, 5))
+        pats = [ps[k + j][0] for j in range(qn)]
+        b = ps[k][1]
+        off = np.zeros(5, dtype=np.int64)
+        off[1:qn + 1] = np.cumsum([len(x) for x in pats])
+        packed = b"".join(pats) or b"\0"
+        ds = [exact(o, fam, x, b) for x in pats]
+        for K in cutoffs(rng, ds[0]):
+            K = min(K, 2**31 - 1)
+            assert lib.hc_fast(fam, word32, packed, off.ctypes.data, qn, b, len(b), K, out) == 0
+            assert list(out)[:qn] == [d if d <= K else K + 1 for d in ds], (pats, b, K)
 
 
 def test_jaro_cores_match_oracle(libs):
