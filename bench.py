@@ -38,13 +38,20 @@ sys.path.insert(0, os.path.join(ROOT, "rapidfuzz-cpp_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 METRIC_NAME = "GCUPS & pairs/s, batched vs per-call, 1 GB300, bit-exact; extract p50/p99 ms"
-# dram__bytes_read.sum + dram__bytes_write.sum of one metric's launches of the several-queries
-# kernels (k_tiles_mq, 64-bit and 32-bit words) on this workload, averaged over four steps of
-# one `ncu --metrics` capture: the strings are read once, the 67 MB of results stay in the
-# 129 MB L2 when the launch ends (written back later)
-DRAM_BYTES_PER_LAUNCH = {"levenshtein": 1117056, "indel": 1151168, "osa": 1015104}
+# dram__bytes_read.sum + dram__bytes_write.sum of one metric's k_fast launches (64-bit and
+# 32-bit words) on this workload from one `ncu --metrics` capture, per step (filled in from
+# the capture summarised under profiles/; empty: not measured for this build)
+DRAM_BYTES_PER_LAUNCH = {}
+# algorithmic INT32 operations per word step (minimal 32-bit ALU form of the reference's
+# step): 64-bit words (Levenshtein_impl.hpp:285-302, LCSseq_impl.hpp:226-229,
+# OSA_impl.hpp:52-54) and the same model for a 32-bit word (patterns of <= 32 units, which
+# run on 32-bit recurrence words): every two-instruction 64-bit term is one instruction,
+# the three score-tracking instructions of the Levenshtein step stay three
 OPS_PER_WORD_STEP = {"levenshtein": 23, "indel": 8, "osa": 29}
+OPS_PER_WORD_STEP_32 = {"levenshtein": 13, "indel": 4, "osa": 16}
 CUTOFF = 8
+WORKLOAD = ("cdist %dx%d a-z Zipf(1.1) len U[16,64], 20%% mutated copies; "
+            "Levenshtein+Indel+OSA score_cutoff=8, int32 out")
 
 
 def parse():
@@ -65,6 +72,11 @@ def parse():
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: request arrival rate (req/s)")
     ap.add_argument("--duration", type=float, default=2.0, help="serving: seconds of arrivals")
     ap.add_argument("--corpus", type=int, default=10_000_000, help="serving: DNA corpus size")
+    ap.add_argument("--no-per-call", action="store_true", help="cdist: skip the per-call (one pair per call) leg")
+    ap.add_argument("--no-serving", action="store_true", help="cdist: skip the short serving leg")
+    ap.add_argument("--serving-duration", type=float, default=2.0, help="cdist: seconds of arrivals of the serving leg")
+    ap.add_argument("--load-s", type=float, default=1.5,
+                    help="seconds of untimed steps, with the clock sampler running, right before the timed region")
     return ap.parse_args()
 
 
@@ -148,12 +160,22 @@ class ClockSampler:
 
 
 def cpu_cdist(q, c, nthreads=0):
-    """the three metrics on the CPU restatement; returns seconds"""
+    """the three metrics on the CPU restatement (the reference's Cached* loop); returns
+    (seconds, the three int32 matrices)"""
     from oracle_lib import oracle_cdist, LEVENSHTEIN, INDEL, OSA, DISTANCE
     t0 = time.perf_counter()
-    for m in (LEVENSHTEIN, INDEL, OSA):
-        oracle_cdist(m, DISTANCE, q, c, CUTOFF, out_dtype=0, nthreads=nthreads)
-    return time.perf_counter() - t0
+    outs = [oracle_cdist(m, DISTANCE, q, c, CUTOFF, out_dtype=0, nthreads=nthreads) for m in (LEVENSHTEIN, INDEL, OSA)]
+    return time.perf_counter() - t0, outs
+
+
+def cpu_one_core(q, c, rows=64):
+    """the same three metrics on one host thread over the first `rows` queries x all
+    choices; returns GCUPS"""
+    sub = (q[0][:q[1][rows]], q[1][:rows + 1].copy(), 1)
+    t, _ = cpu_cdist(sub, c, nthreads=1)
+    ql = np.diff(sub[1]).astype(np.float64)
+    cl = np.diff(c[1]).astype(np.float64)
+    return float(ql.sum()) * float(cl.sum()) * 3 / t / 1e9
 
 
 def run_reference(args, rank, world):
@@ -165,33 +187,38 @@ def run_reference(args, rank, world):
     cores = os.cpu_count() or 1
     for _ in range(min(args.warmup, 1)):
         cpu_cdist(q, c)
-    times = [cpu_cdist(q, c) for _ in range(args.steps)]
+    times = [cpu_cdist(q, c)[0] for _ in range(args.steps)]
     t = float(np.sum(times))
     value = cells * 3 * args.steps / t / 1e9
+    one = cpu_one_core(q, c)
     line = {"impl": "reference", "metric": METRIC_NAME, "value": value, "unit": "GCUPS", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
             "data": "synthetic (seeded cdist_zipf)",
-            "config": {"workload": "cdist 4096x4096 a-z Zipf(1.1) len U[16,64], 20% mutated copies; "
-                                   "Levenshtein+Indel+OSA score_cutoff=8, int32 out",
-                       "global_batch": int(npairs), "pairs_per_s": npairs * args.steps / t},
+            "config": {"workload": WORKLOAD % (args.nq, args.nc), "global_batch": int(npairs * world)},
+            "detail": {"pairs_per_s": npairs * args.steps / t, "one_core_gcups": one,
+                       "what": "the CPU restatement of the reference's Cached* loop (a query's pattern table "
+                               "built once, then every choice), all host threads; the reference's AVX2 "
+                               "experimental::Multi* scorers do not exist on this aarch64 host"},
             "cpu_baseline": {"value": value, "unit": "GCUPS", "cores": cores, "kind": "port",
-                             "sample": "the full workload, every step"},
+                             "sample": "the full workload, every step", "one_core_value": one},
             "e2e": {"value": value, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
 def executed_word_steps(metric, q, c):
-    """word steps the single-word kernels execute on this workload (early exits and the
-    length filter included), counted on the host by the same cores (librfg_count.so)"""
+    """word steps the one-word kernels execute on this workload (early exits and the
+    length filter included), counted on the host by the same core (librfg_count.so):
+    (steps on 64-bit words, steps on 32-bit words)"""
     lib = ctypes.CDLL(os.path.join(ROOT, "rapidfuzz-cpp_gb300", "lib", "librfg_count.so"))
-    lib.rfg_count_word_steps.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
-                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint64,
-                                         ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
-    out = ctypes.c_uint64()
-    rc = lib.rfg_count_word_steps(metric, q[0].ctypes.data, q[1].ctypes.data, len(q[1]) - 1, c[0].ctypes.data,
-                                  c[1].ctypes.data, len(c[1]) - 1, CUTOFF, 0, ctypes.byref(out))
-    return float(out.value) if rc == 0 else None
+    lib.rfg_count_word_steps2.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint64,
+                                          ctypes.c_int, ctypes.POINTER(ctypes.c_uint64),
+                                          ctypes.POINTER(ctypes.c_uint64)]
+    s64, s32 = ctypes.c_uint64(), ctypes.c_uint64()
+    rc = lib.rfg_count_word_steps2(metric, q[0].ctypes.data, q[1].ctypes.data, len(q[1]) - 1, c[0].ctypes.data,
+                                   c[1].ctypes.data, len(c[1]) - 1, CUTOFF, 0, ctypes.byref(s64), ctypes.byref(s32))
+    return (float(s64.value), float(s32.value)) if rc == 0 else None
 
 
 def int_peak_ops():
@@ -262,24 +289,21 @@ def main():
             b.check(stream.cuda_stream)
     torch.cuda.synchronize()
 
-    # parity spot check of the timed path (rows of each matrix against the oracle)
-    from oracle_lib import oracle_cdist
-    rows = [0, nq // 2, nq - 1]
-    qsub_list = [q[0][q[1][r]:q[1][r + 1]] for r in rows]
-    qs_off = np.zeros(len(rows) + 1, dtype=np.int64)
-    qs_off[1:] = np.cumsum([len(x) for x in qsub_list])
-    qsub = (np.concatenate(qsub_list), qs_off, 1)
-    for (name, m), o in zip(metrics, outs):
-        exp = oracle_cdist(m, R.DISTANCE, qsub, c, CUTOFF, out_dtype=0)
-        got = o[rows].cpu().numpy()
-        if not np.array_equal(got, exp):
-            raise SystemExit("bench: %s result differs from the oracle" % name)
-
     if dist is not None:
         dist.barrier()
     clocks = ClockSampler()
     clocks.start()
-    time.sleep(0.3)
+    # untimed load with the sampler running, so that the clock record covers the GPU under
+    # this work even when the timed region is only a few milliseconds long
+    t_load = time.perf_counter()
+    with torch.cuda.stream(stream):
+        while time.perf_counter() - t_load < args.load_s:
+            for _ in range(50):
+                flush.zero_()
+                step()
+            stream.synchronize()
+    if dist is not None:
+        dist.barrier()
     per_kernel = {name: 0.0 for name, _ in batches}
     total_ms = 0.0
     with torch.cuda.stream(stream):
@@ -301,18 +325,42 @@ def main():
     value = cells * 3 * args.steps * world / t_max / 1e9
     pairs_per_s = npairs * 3 * args.steps * world / t_max
 
-    # roofline of the dominant kernel
-    dom = max(per_kernel, key=per_kernel.get)
-    dom_ms = per_kernel[dom] / args.steps
-    metric_ids = {"levenshtein": 0, "indel": 1, "osa": 3}
-    exec_steps = {name: executed_word_steps(metric_ids[name], q, c) for name, _ in batches}
-    alg_ops = (exec_steps[dom] if exec_steps[dom] is not None else req_steps) * OPS_PER_WORD_STEP[dom]
+    # roofline of every metric: executed word steps x algorithmic ops (64-bit and 32-bit
+    # words credited at their own counts) / the metric's CUDA-event time
     peak = int_peak_ops()
-    achieved = alg_ops / (dom_ms * 1e-3)
+    metric_ids = {"levenshtein": 0, "indel": 1, "osa": 3}
     kern = dict((name, b.kernels()) for name, b in batches)
+    per_metric = {}
+    for name, _ in batches:
+        ms = per_kernel[name] / args.steps
+        ex = executed_word_steps(metric_ids[name], q, c)
+        if ex is None:
+            alg = req_steps * OPS_PER_WORD_STEP[name]
+            ex = (req_steps, 0.0)
+        else:
+            alg = ex[0] * OPS_PER_WORD_STEP[name] + ex[1] * OPS_PER_WORD_STEP_32[name]
+        ach = alg / (ms * 1e-3)
+        per_metric[name] = {"ms": ms, "achieved": ach / 1e12, "frac": ach / peak, "word_steps_64": ex[0],
+                            "word_steps_32": ex[1], "kernels": kern[name]}
+    dom = max(per_kernel, key=per_kernel.get)
     dom_kernel = ";".join(kern[dom])
-    traffic = (DRAM_BYTES_PER_LAUNCH.get(dom) if args.nq == 4096 and args.nc == 4096 and "k_tiles_mq" in dom_kernel
+    traffic = (DRAM_BYTES_PER_LAUNCH.get(dom) if args.nq == 4096 and args.nc == 4096 and "k_fast" in dom_kernel
                else None)
+
+    # parity of the timed path: every element of the three matrices against the oracle
+    # (the CPU restatement of the reference's Cached* loop), which is also the CPU baseline
+    cpu = None
+    if rank == 0:
+        tc, exp = cpu_cdist(q, c)
+        for (name, _), o, e in zip(metrics, outs, exp):
+            got = o.cpu().numpy()
+            if not np.array_equal(got, e):
+                raise SystemExit("bench: %s result differs from the oracle in %d elements" % (name, int((got != e).sum())))
+        if not args.no_cpu_baseline:
+            one = cpu_one_core(q, c)
+            cpu = {"value": cells * 3 / tc / 1e9, "unit": "GCUPS", "cores": os.cpu_count() or 1, "kind": "port",
+                   "sample": "the full 4096x4096 x3-metric workload, one pass", "seconds": tc,
+                   "one_core_value": one, "one_core_sample": "64 queries x 4096 choices x3 metrics, one thread"}
 
     # e2e through the public C ABI with pinned host buffers
     e2e = None
@@ -339,35 +387,89 @@ def main():
                "d2h_bytes_per_step": d2h, "ms_per_step": te / args.steps * 1e3,
                "pairs_per_s": npairs * 3 * args.steps * world / te}
 
-    cpu = None
-    if not args.no_cpu_baseline and rank == 0:
-        tc = cpu_cdist(q, c)
-        cpu = {"value": cells * 3 / tc / 1e9, "unit": "GCUPS", "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": "the full 4096x4096 x3-metric workload, one pass", "seconds": tc}
+    # the plain per-call drop-in: one Cached scorer per query, one call per pair (host
+    # strings in, one result out), on a fixed sample of this workload's pairs
+    per_call = None
+    if not args.no_per_call and rank == 0:
+        per_call = per_call_leg(R, q, c, metrics)
+        per_call["batched_over_per_call"] = pairs_per_s / world / per_call["pairs_per_s"]
+
+    serving = None
+    if not args.no_serving and rank == 0:
+        import bench_configs
+        serving = bench_configs.serving_leg(R, args.serving_duration)
 
     if rank == 0:
         line = {"metric": METRIC_NAME, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded cdist_zipf)",
-                "config": {"workload": "cdist %dx%d a-z Zipf(1.1) len U[16,64], 20%% mutated copies; "
-                                       "Levenshtein+Indel+OSA score_cutoff=8, int32 out" % (nq, nc),
-                           "global_batch": int(npairs * 3 * world), "pairs_per_s": pairs_per_s,
+                "config": {"workload": WORKLOAD % (nq, nc), "global_batch": int(npairs * 3 * world)},
+                "detail": {"pairs_per_s": pairs_per_s,
                            "l2": "flushed between steps (256 MB write); strings are L2-resident within a step",
                            "launch": "prepared batches replayed as CUDA graphs",
                            "per_kernel_ms": {k: v / args.steps for k, v in per_kernel.items()},
-                           "required_word_steps_per_metric": req_steps,
-                           "executed_word_steps": exec_steps, "pairs_passing_length_filter": pairs_pass},
-                "roofline": {"bound": "int32", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "Tops/s",
-                             "frac": achieved / peak, "traffic": traffic, "kernel": dom_kernel,
+                           "required_word_steps_per_metric": req_steps, "pairs_passing_length_filter": pairs_pass,
+                           "parity": "every element of the three timed matrices equals the oracle"},
+                "roofline": {"bound": "int32", "achieved": per_metric[dom]["achieved"], "peak": peak / 1e12,
+                             "unit": "Tops/s", "frac": per_metric[dom]["frac"], "traffic": traffic,
+                             "kernel": dom_kernel, "metric": dom,
                              "peak_source": "measured: LOP3/IADD3/SHF issue-rate microbenchmark (librfg_peak.so)",
-                             "ops_per_word_step": OPS_PER_WORD_STEP[dom]},
-                "cpu_baseline": cpu, "e2e": e2e,
+                             "ops_per_word_step": {"64bit": OPS_PER_WORD_STEP, "32bit": OPS_PER_WORD_STEP_32},
+                             "per_metric": per_metric,
+                             "min_frac": min(v["frac"] for v in per_metric.values())},
+                "cpu_baseline": cpu, "e2e": e2e, "per_call": per_call, "serving": serving,
                 "gpu_launches": sum(len(k) for k in kern.values()) * args.steps, "clocks": clk}
         print(json.dumps(line), flush=True)
     for _, b in batches:
         b.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def per_call_leg(R, q, c, metrics, npairs=1500, threads=(1, 16)):
+    """pairs/s of the per-pair drop-in (CachedX::distance with score_cutoff 8 through
+    rfg_cached_score_i64): 1,500 fixed (query, choice) pairs of the workload per metric,
+    from one host thread and from several at once; every result checked with the oracle"""
+    import concurrent.futures
+    from oracle_lib import oracle_cdist
+    rng = np.random.default_rng(77)
+    qi = rng.integers(0, len(q[1]) - 1, size=npairs)
+    ci = rng.integers(0, len(c[1]) - 1, size=npairs)
+    uq = sorted(set(qi.tolist()))
+    row = {k: i for i, k in enumerate(uq)}
+    qsub = (np.concatenate([q[0][q[1][k]:q[1][k + 1]] for k in uq]),
+            np.concatenate([[0], np.cumsum([q[1][k + 1] - q[1][k] for k in uq])]).astype(np.int64), 1)
+    out = {"pairs": npairs, "what": "rfg_cached_score_i64: one pair per call, host strings, one result back"}
+    best = None
+    for nth in threads:
+        total_t = 0.0
+        for name, m in metrics:
+            scorers = {k: R.Cached(m, q[0][q[1][k]:q[1][k + 1]]) for k in uq}
+            s2 = [c[0][c[1][k]:c[1][k + 1]] for k in ci]
+            for k in range(20):
+                scorers[int(qi[k])].score(R.DISTANCE, s2[k], CUTOFF)
+            got = np.zeros(npairs, dtype=np.int64)
+
+            def run(lo, hi):
+                for k in range(lo, hi):
+                    got[k] = scorers[int(qi[k])].score(R.DISTANCE, s2[k], CUTOFF)
+            bounds = np.linspace(0, npairs, nth + 1).astype(int)
+            t0 = time.perf_counter()
+            if nth == 1:
+                run(0, npairs)
+            else:
+                with concurrent.futures.ThreadPoolExecutor(nth) as ex:
+                    list(ex.map(lambda i: run(bounds[i], bounds[i + 1]), range(nth)))
+            total_t += time.perf_counter() - t0
+            exp = oracle_cdist(m, R.DISTANCE, qsub, c, CUTOFF)
+            want = np.array([exp[row[int(a)], int(b)] for a, b in zip(qi, ci)])
+            if not np.array_equal(got, want):
+                raise SystemExit("bench: per-call %s results differ from the oracle" % name)
+        pps = npairs * len(metrics) / total_t
+        out["threads_%d" % nth] = {"pairs_per_s": pps, "us_per_call": total_t / (npairs * len(metrics)) * 1e6 * nth}
+        best = pps if best is None else max(best, pps)
+    out["pairs_per_s"] = best
+    return out
 
 
 if __name__ == "__main__":

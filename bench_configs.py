@@ -350,14 +350,21 @@ def run(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
-def run_serving(args, R, WL):
+def serving_leg(R, duration, rate=2000.0, corpus=10_000_000, max_inflight=4, max_batch=64, seed=33):
+    """Config 5 in short: device-resident corpora of `corpus` DNA strings (len U[10,200]) and
+    1,000,000 uint32 token strings; Poisson arrivals at `rate` req/s for `duration` s, each
+    an extractOne (limit 1) or top-10 extract of one query of length U[5,500] with a metric
+    drawn from {Levenshtein, Indel, OSA} (DNA) or Jaro-Winkler (tokens), through the
+    continuous-batching server; returns latency percentiles, completed and offered req/s,
+    and the same kinds of requests one at a time (rfg_extract)"""
     import threading
+    import workloads as WL
     t0 = time.perf_counter()
-    dna = WL.dna_corpus_fast(seed=31, n=args.corpus)
+    dna = WL.dna_corpus_fast(seed=31, n=corpus)
     tok = WL.tokens_u32_fast(seed=32, n=1_000_000)
     corpora = [R.Corpus(dna), R.Corpus(tok)]
     t_setup = time.perf_counter() - t0
-    rng = np.random.default_rng(33)
+    rng = np.random.default_rng(seed)
     acgt = np.frombuffer(b"ACGT", dtype=np.uint8)
     alpha = np.array(WL.TOKEN_ALPHABET + [0x20], dtype=np.uint32)
     kinds = [(0, R.LEVENSHTEIN, R.DISTANCE), (0, R.INDEL, R.DISTANCE), (0, R.OSA, R.DISTANCE),
@@ -385,11 +392,11 @@ def run_serving(args, R, WL):
         alone[kind] = float(np.median(ts[1:]))
     sizes = [corpora[0].count, corpora[1].count]
 
-    n_req = int(args.rate * args.duration)
-    gaps = rng.exponential(1.0 / args.rate, size=n_req)
+    n_req = int(rate * duration)
+    gaps = rng.exponential(1.0 / rate, size=n_req)
     arrivals = np.cumsum(gaps)
     reqs = [make_request() for _ in range(n_req)]
-    server = R.Server(corpora, max_inflight=4, max_batch=64)
+    server = R.Server(corpora, max_inflight=max_inflight, max_batch=max_batch)
     tickets = [None] * n_req
     clocks = B.ClockSampler()
     clocks.start()
@@ -417,19 +424,24 @@ def run_serving(args, R, WL):
     lat = np.array(lat)
     pairs = float(sum(sizes[c] for c, *_ in reqs))
     pairs_alone = float(np.mean([sizes[kinds[k][0]] / alone[k] for k in range(4)]))
-    line = {"metric": METRIC, "value": pairs / wall, "unit": "pairs/s", "n_gpus": 1, "steps": n_req, "warmup": 0,
-            "ms_per_step": wall / n_req * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "u64+f64", "data": "synthetic (seeded dna_corpus_fast, tokens_u32_fast)",
-            "config": {"workload": "serving: serving, %d DNA (len U[10,200]) + 1,000,000 uint32 token strings, "
-                                   "Poisson %.0f req/s for %.1f s, extractOne/top-10, Lev/Indel/OSA/JW, "
-                                   "query len U[5,500]" % (args.corpus, args.rate, args.duration),
-                       "requests": n_req, "p50_ms": float(np.percentile(lat, 50)),
-                       "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
-                       "completed_per_s": n_req / wall, "offered_per_s": args.rate,
-                       "arrivals_span_s": float(arrivals[-1]), "submit_span_s": t_submitted,
-                       "batches": st["batches"], "mean_batch": st["batched_requests"] / max(st["batches"], 1),
-                       "alone_ms": {"levenshtein": alone[0] * 1e3, "indel": alone[1] * 1e3, "osa": alone[2] * 1e3,
-                                    "jaro_winkler": alone[3] * 1e3},
-                       "pairs_per_s_one_at_a_time": pairs_alone, "setup_s": t_setup},
-            "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": clk}
+    return {"workload": "serving: %d DNA (len U[10,200]) + 1,000,000 uint32 token strings, Poisson %.0f req/s "
+                        "for %.1f s, extractOne/top-10, Lev/Indel/OSA/JW, query len U[5,500]" % (corpus, rate, duration),
+            "requests": n_req, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "max_ms": float(lat.max()), "completed_per_s": n_req / wall, "offered_per_s": rate,
+            "pairs_per_s": pairs / wall, "wall_s": wall,
+            "arrivals_span_s": float(arrivals[-1]), "submit_span_s": t_submitted,
+            "batches": st["batches"], "mean_batch": st["batched_requests"] / max(st["batches"], 1),
+            "alone_ms": {"levenshtein": alone[0] * 1e3, "indel": alone[1] * 1e3, "osa": alone[2] * 1e3,
+                         "jaro_winkler": alone[3] * 1e3},
+            "pairs_per_s_one_at_a_time": pairs_alone, "setup_s": t_setup, "clocks": clk}
+
+
+def run_serving(args, R, WL):
+    leg = serving_leg(R, args.duration, rate=args.rate, corpus=args.corpus)
+    n_req = leg["requests"]
+    line = {"metric": METRIC, "value": leg["pairs_per_s"], "unit": "pairs/s", "n_gpus": 1, "steps": n_req,
+            "warmup": 0, "ms_per_step": leg["wall_s"] / n_req * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64+f64", "data": "synthetic (seeded dna_corpus_fast, tokens_u32_fast)",
+            "config": {"workload": leg["workload"]}, "detail": leg,
+            "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": leg["clocks"]}
     print(json.dumps(line), flush=True)

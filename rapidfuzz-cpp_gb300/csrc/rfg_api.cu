@@ -30,6 +30,7 @@
 
 #include "rapidfuzz_gb300.h"
 #include "rfg_device.cuh"
+#include "rfg_fast.cuh"
 #include "rfg_kernels.h"
 #include "rfg_token.h"
 
@@ -385,6 +386,8 @@ int g_stage_mode = 1;       /* dense tiles stage their results in shared memory 
 int g_mq_mode = 1;          /* one-word unit-weight distances take several queries per thread (autotuning) */
 int g_half_mode = 1;        /* queries of <= 32 units run on 32-bit recurrence words (autotuning) */
 int g_block_override = 0;   /* override of the tile kernels' block size (autotuning) */
+int g_fast_mode = 1;        /* unit-weight one-word distances run on the warp tiles (k_fast) */
+int64_t g_fast_window = 256; /* choice positions per warp window of k_fast (autotuning) */
 
 /* A prepared batch: everything a launch needs is on the device, so enqueue() only
  * resets the tile counters and launches the kernels (no host work, no allocation,
@@ -407,6 +410,7 @@ struct Prepared {
     const int32_t* perm = nullptr;
     const int64_t* poff = nullptr;
     const int32_t* plen = nullptr;
+    const int4* prec = nullptr; /* k_fast visiting records */
     bool has_pre = false; /* pre.a / grid: the per-query table pass before the row blocks */
     KParams pre;
     int* counters = nullptr;
@@ -563,6 +567,15 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
     const int32_t* dperm = nullptr;
     std::vector<int32_t> perm, pl;
     std::vector<int64_t> po;
+    /* the warp tiles (k_fast) take the one-word class of a unit-weight distance whose
+     * pattern tables need no hash rows; they visit the choices in windows of their own,
+     * each sorted by length, through 16-byte records */
+    bool fast_any = false;
+    for (int64_t b = 0; b < nblk; ++b)
+        if (!cls[b * 5].empty() && (c.width == 1 || cls_wide[b * 5] == 0)) fast_any = true;
+    fast_any = fast_any && fast_ok && spec.topk == 0 && !spec.fixed_perm && g_fast_mode != 0;
+    const int64_t fwin = std::max<int64_t>(32, std::min<int64_t>(1024, g_fast_window / 4 * 4));
+    std::vector<int32_t> frec;
     if (spec.fixed_perm) {
         chunk = spec.fixed_chunk;
         dperm = spec.fixed_perm;
@@ -596,6 +609,19 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
                 pl[i] = clen[perm[i]];
             }
         }
+        if (fast_any) {
+            std::vector<int32_t> fperm;
+            chunk_length_order(clen, fwin, &fperm);
+            frec.resize((size_t)nc * 4);
+            for (int64_t i = 0; i < nc; ++i) {
+                const int32_t ci = fperm[i];
+                const uint64_t o = (uint64_t)hoff[ci];
+                frec[4 * i] = (int32_t)(uint32_t)o;
+                frec[4 * i + 1] = (int32_t)(uint32_t)(o >> 32);
+                frec[4 * i + 2] = clen[ci];
+                frec[4 * i + 3] = (int32_t)(ci - i / fwin * fwin);
+            }
+        }
     }
     {
         /* the host tables leave in one copy from pinned staging */
@@ -606,13 +632,14 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             return o;
         };
         const size_t oq = reserve(qall.size() * 4), operm = reserve(perm.size() * 4), opo = reserve(po.size() * 8),
-                     opl = reserve(pl.size() * 4);
+                     opl = reserve(pl.size() * 4), ofr = reserve(frec.size() * 4);
         unsigned char* h;
         RFG_TRY(upload_stage(tot, &h));
         memcpy(h + oq, qall.data(), qall.size() * 4);
         if (!perm.empty()) memcpy(h + operm, perm.data(), perm.size() * 4);
         if (!po.empty()) memcpy(h + opo, po.data(), po.size() * 8);
         if (!pl.empty()) memcpy(h + opl, pl.data(), pl.size() * 4);
+        if (!frec.empty()) memcpy(h + ofr, frec.data(), frec.size() * 4);
         RFG_TRY(pb->packed.alloc(tot));
         RFG_CUDA(cudaMemcpyAsync(pb->packed.p, h, tot, cudaMemcpyHostToDevice, g.stream));
         RFG_CUDA(cudaEventRecord(g.up_ev, g.stream));
@@ -623,6 +650,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             pb->poff = (const int64_t*)(d + opo);
             pb->plen = (const int32_t*)(d + opl);
         }
+        if (!frec.empty()) pb->prec = (const int4*)(d + ofr);
     }
     pb->chunk = chunk;
     pb->nchunks = (nc + chunk - 1) / chunk;
@@ -665,7 +693,44 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         const int64_t nchunks_full = (nc + chunk - 1) / chunk;
         const bool small_class =
             k < 4 && !topk && (int64_t)cls[bk].size() * nchunks_full < (int64_t)g.sms * 8 && chunk > 256;
-        const bool use_mq = k == 0 && mq_ok && a.hcap == 0 && stage > 0 && !small_class;
+        const bool use_fast = k == 0 && fast_any && a.hcap == 0 && pb->prec;
+        const bool use_mq = !use_fast && k == 0 && mq_ok && a.hcap == 0 && stage > 0 && !small_class;
+        if (use_fast) {
+            /* warp tiles: one task = (Q queries, one window); queries of at most 32 units
+             * (the tail of the longest-first class) in their own launch on 32-bit words */
+            const int Qf = fast_queries(fam);
+            const int fblock = RFG_FAST_WARPS * 32;
+            a.prec = pb->prec;
+            a.stage = fwin;
+            a.nchunks = (nc + fwin - 1) / fwin;
+            a.chunk = 1;
+            a.fast = 1;
+            a.fast_k = clamp_bound(spec.ci);
+            const size_t esz = spec.out_dtype == RFG_I32 ? 4 : 8;
+            a.vec = ((uintptr_t)spec.out % 16 == 0) && ((spec.ld * (int64_t)esz) % 16 == 0) && (fwin * (int64_t)esz) % 16 == 0;
+            const std::vector<int32_t>& v = cls[bk];
+            int64_t nlong = 0;
+            while (nlong < (int64_t)v.size() && q.len[v[nlong]] > 32) ++nlong;
+            for (int half = 0; half < 2; ++half) {
+                const int64_t n0 = half ? nlong : 0, n1 = half ? (int64_t)v.size() : nlong;
+                if (n1 <= n0) continue;
+                const void* ff = fam == FAM_LEV ? fast_kernel_lev(c.width, half) : fam == FAM_LCS ? fast_kernel_lcs(c.width, half)
+                                                                                              : fast_kernel_osa(c.width, half);
+                const size_t fsm = fast_smem_bytes(Qf, half, fwin, spec.out_dtype);
+                RFG_TRY(allow_dynamic_smem(ff, fsm));
+                const int64_t fslots = (int64_t)g.sms * occupancy(ff, fblock, fsm);
+                KParams h = a;
+                h.qlist = a.qlist + n0;
+                h.nq = (int32_t)(n1 - n0);
+                h.counter = pb->counters + (half ? nblk * 5 + bk / 5 : bk);
+                const int64_t tasks = (h.nq + Qf - 1) / Qf * h.nchunks;
+                if (tasks > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "batch too large for one launch");
+                const int64_t warps = std::max<int64_t>(1, std::min<int64_t>(tasks, fslots * RFG_FAST_WARPS));
+                pb->launches.push_back(
+                    LaunchRec{ff, (unsigned)((warps + RFG_FAST_WARPS - 1) / RFG_FAST_WARPS), fblock, fsm, h, (int)(bk / 5)});
+            }
+            continue;
+        }
         if (use_mq && fam == FAM_JARO) {
             fn = tiles_mq_kernel_jaro(c.width);
             block = g_block_override > 0 ? g_block_override : 256;

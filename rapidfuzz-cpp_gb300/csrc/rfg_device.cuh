@@ -87,6 +87,12 @@ struct KParams {
      * every query / choice string, three int32 each */
     const int32_t* qparts;
     const int32_t* cparts;
+    /* warp tiles of the distance fast path (k_fast): per visiting position {offset (low,
+     * high 32 bits), length, index within its window}, windows of `stage` positions each
+     * sorted by length; vec = 1 when every result row segment of a window starts on a
+     * 16-byte boundary */
+    const int4* prec;
+    int vec;
 };
 
 /* editops of many pairs (k_editops): one operation, laid out as rfg_editop */

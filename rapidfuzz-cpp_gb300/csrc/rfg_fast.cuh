@@ -1,0 +1,214 @@
+/*
+ * rfg_fast.cuh -- warp tiles for the unit-weight distances of one-word patterns:
+ * Levenshtein 1/1/1, Indel and OSA with the chain d <= K ? d : K + 1 (cdist with a
+ * distance cutoff, the reference's Cached*::distance over many choices,
+ * Levenshtein.hpp:421-482, Indel.hpp:148-183, OSA.hpp:232-271).
+ *
+ * Every warp is its own worker: it pulls a task (a group of Q queries, one window of
+ * choices) from the launch's counter, builds the group's pattern tables in its own
+ * slice of shared memory, and for the window
+ *   1. fills its result stage with K + 1, the value of every pair that fails the length
+ *      filter |m - n| <= K (Levenshtein_impl.hpp:863, LCSseq_impl.hpp:389);
+ *   2. finds, with two warp-wide votes, the visiting positions whose lengths can pass for
+ *      some query of the group -- windows are sorted by choice length, so they form one
+ *      run -- and scores only those, one choice per lane against the Q queries
+ *      (fast_group);
+ *   3. writes the window's Q result rows with 16-byte stores.
+ * No barrier of the whole CTA is ever taken (only __syncwarp), so a warp that meets
+ * short or quickly pruned choices moves on to the next task at once.
+ *
+ * Layout (per warp, in dynamic shared memory): Q pattern tables of 257 rows (code units
+ * 0..255, then an all-zero row for units the patterns lack), 64-bit rows for patterns
+ * of up to 64 units or 32-bit rows for patterns of up to 32 units (whose recurrence runs
+ * on 32-bit words, the ALU width); then Q x window results.
+ */
+#pragma once
+#include "rfg_device.cuh"
+
+namespace rfg {
+
+#ifndef RFG_FAST_WARPS
+#define RFG_FAST_WARPS 4 /* warps per CTA (the CTA only packs independent warps) */
+#endif
+#ifndef RFG_FAST_MINB
+#define RFG_FAST_MINB 8 /* CTAs per SM the register budget is sized for (64 registers) */
+#endif
+
+/* bytes of one warp's slice: tables, then the result stage */
+__host__ __device__ inline size_t fast_pm_bytes(int Q, bool half) { return ((size_t)Q * 257 * (half ? 4 : 8) + 15) / 16 * 16; }
+__host__ __device__ inline size_t fast_stage_bytes(int Q, int64_t window, int out_dtype)
+{
+    return (size_t)Q * window * (out_dtype == 0 ? 4 : 8);
+}
+inline size_t fast_smem_bytes(int Q, bool half, int64_t window, int out_dtype)
+{
+    return (size_t)RFG_FAST_WARPS * (fast_pm_bytes(Q, half) + fast_stage_bytes(Q, window, out_dtype));
+}
+
+template <typename WT>
+struct FastRows {
+    const WT* rows;
+    __device__ __forceinline__ WT operator()(int q, unsigned c) const { return rows[q * 257 + c]; }
+};
+
+/* first position p of [0, nn) with lens[4 p] >= L (lens ascending; nn <= 1024), by the
+ * whole warp: one sampled length per lane, then the 32-position run the answer lies in */
+__device__ __forceinline__ int first_at_least(const int* lens, int nn, int64_t L, int lane)
+{
+    const int S = (nn + 31) >> 5; /* sample stride, at most 32 */
+    const int ps = lane * S;
+    const unsigned below = __ballot_sync(0xffffffffu, ps < nn && (int64_t)__ldg(lens + 4 * ps) < L);
+    const int c = __popc(below); /* samples 0..c-1 lie below L */
+    if (c == 0) return 0;
+    const int base = (c - 1) * S + 1; /* the answer is in [base, min(c * S, nn)] */
+    const int pq = base + lane;
+    const unsigned b2 = __ballot_sync(0xffffffffu, lane < S - 1 && pq < nn && (int64_t)__ldg(lens + 4 * pq) < L);
+    return base + __popc(b2);
+}
+
+/* set (SET) or clear the table rows of pattern q: lane l holds units l and l + 32;
+ * lanes holding one code unit find each other by match and the lowest of them writes
+ * that 32-bit half of the row */
+template <typename WT, bool SET>
+__device__ __forceinline__ void fast_rows(WT* rows, int q, const KParams& a, int qi, int m, int lane)
+{
+    const unsigned char* qb = a.q.data + a.q.off[qi] * a.q.width;
+#pragma unroll
+    for (int h = 0; h < (sizeof(WT) == 4 ? 1 : 2); ++h) {
+        const int i = lane + 32 * h;
+        int r = 256;
+        if (i < m) {
+            const u64 c = load_unit(qb, a.q.width, i);
+            if (c < 256) r = (int)c; /* a wider unit never occurs in one-byte choices */
+        }
+        if (SET) {
+            const unsigned same = __match_any_sync(0xffffffffu, r);
+            if (r < 256 && lane == __ffs(same) - 1) ((uint32_t*)&rows[q * 257 + r])[h] = same;
+        }
+        else if (r < 256)
+            rows[q * 257 + r] = 0;
+    }
+}
+
+template <int FAM, typename CT, int Q, bool HALF>
+__global__ void __launch_bounds__(RFG_FAST_WARPS * 32, RFG_FAST_MINB) k_fast(const KParams a)
+{
+    typedef typename std::conditional<HALF, uint32_t, u64>::type WT;
+    extern __shared__ u64 smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int win = (int)a.stage; /* positions per window (a multiple of 4, at most 1024) */
+    const size_t pmb = fast_pm_bytes(Q, HALF);
+    unsigned char* slice = (unsigned char*)smem + (size_t)warp * (pmb + fast_stage_bytes(Q, win, a.out_dtype));
+    WT* rows = (WT*)slice;
+    unsigned char* stage = slice + pmb;
+    const int K = (int)(a.fast_k < 0x7fffffff ? a.fast_k : 0x7fffffff);
+    /* the host keeps tasks and windows below 2^31 */
+    const int nwin = (int)a.nchunks;
+    const int ntasks = (int)(((int64_t)a.nq + Q - 1) / Q * nwin);
+    const int maxm = HALF ? 32 : 64;
+
+    for (int i = lane; i < Q * 257; i += 32) rows[i] = 0;
+    int cur_g = -1;
+    int m[Q], qi[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) m[q] = qi[q] = 0;
+    int qn = 0, mmin = 0, mmax = 0;
+    __syncwarp();
+
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(a.counter, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= ntasks) break;
+        const int g = t / nwin, w = t - g * nwin;
+        if (g != cur_g) {
+            /* clear the previous group's rows (its units are read again), then set the new */
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+                if (q < qn) fast_rows<WT, false>(rows, q, a, qi[q], m[q], lane);
+            __syncwarp();
+            qn = 0;
+            mmin = 0x7fffffff;
+            mmax = 0;
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const int kq = g * Q + q;
+                m[q] = 0;
+                if (kq < a.nq) {
+                    qi[q] = a.qlist[kq];
+                    int mq = (int)(a.q.off[qi[q] + 1] - a.q.off[qi[q]]);
+                    if (mq > maxm) { /* the host classified this query into a smaller class */
+                        if (lane == 0) atomicExch(a.err, 2);
+                        mq = maxm;
+                    }
+                    m[q] = mq;
+                    qn = q + 1;
+                    mmin = mq < mmin ? mq : mmin;
+                    mmax = mq > mmax ? mq : mmax;
+                    fast_rows<WT, true>(rows, q, a, qi[q], mq, lane);
+                }
+            }
+            __syncwarp();
+            cur_g = g;
+        }
+        const int64_t p0 = (int64_t)w * win;
+        const int nn = (int)(p0 + win < a.c.n ? win : a.c.n - p0);
+        /* visiting positions [lo, hi) of the window whose lengths lie in
+         * [mmin - K, mmax + K] (lengths ascend within a window) */
+        const int* lens = (const int*)(a.prec + p0) + 2;
+        const int lo = first_at_least(lens, nn, (int64_t)mmin - K, lane);
+        const int hi = first_at_least(lens, nn, (int64_t)mmax + K + 1, lane);
+        /* the stage holds K + 1 for every pair the filter rejects */
+        if (a.out_dtype == 0) {
+            const int v = K < 0x7fffffff ? K + 1 : K;
+            const int4 f = make_int4(v, v, v, v);
+            for (int i = lane * 4; i < Q * win; i += 128) *(int4*)((int*)stage + i) = f;
+        }
+        else {
+            const long long v = a.out_dtype == 1 ? (long long)K + 1
+                                                 : (long long)__double_as_longlong(int_result_as_double((i64)K + 1));
+            const longlong2 f = make_longlong2(v, v);
+            for (int i = lane * 2; i < Q * win; i += 64) *(longlong2*)((long long*)stage + i) = f;
+        }
+        __syncwarp();
+        for (int p = lo + lane; p < hi; p += 32) {
+            const int4 r = __ldg(a.prec + p0 + p);
+            const int64_t o0 = (int64_t)(((uint64_t)(uint32_t)r.y << 32) | (uint32_t)r.x);
+            int d[Q];
+            fast_group<FAM, Q, FastRows<WT>, MQText<CT>, WT>(FastRows<WT>{rows}, m, qn,
+                                                             MQText<CT>{(const CT*)a.c.data + o0}, r.z, K, d);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                if (q >= qn) break;
+                const int at = q * win + r.w;
+                if (a.out_dtype == 0) ((int*)stage)[at] = d[q];
+                else if (a.out_dtype == 1) ((long long*)stage)[at] = d[q];
+                else ((double*)stage)[at] = int_result_as_double(d[q]);
+            }
+        }
+        __syncwarp();
+        /* the window's rows: 16-byte stores where the row segment is aligned */
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            if (q >= qn) break;
+            const int64_t base = (int64_t)qi[q] * a.ld + p0;
+            if (a.out_dtype == 0) {
+                const int* src = (const int*)stage + q * win;
+                int* dst = (int*)a.out + base;
+                const int nv = a.vec ? nn & ~3 : 0;
+                for (int i = lane * 4; i < nv; i += 128) *(int4*)(dst + i) = *(const int4*)(src + i);
+                for (int i = nv + lane; i < nn; i += 32) dst[i] = src[i];
+            }
+            else {
+                const long long* src = (const long long*)stage + q * win;
+                long long* dst = (long long*)a.out + base;
+                const int nv = a.vec ? nn & ~1 : 0;
+                for (int i = lane * 2; i < nv; i += 64) *(longlong2*)(dst + i) = *(const longlong2*)(src + i);
+                for (int i = nv + lane; i < nn; i += 32) dst[i] = src[i];
+            }
+        }
+        __syncwarp();
+    }
+}
+
+} // namespace rfg

@@ -1,5 +1,6 @@
 /* k_tiles instantiations of the LCS core family */
 #include "rfg_device.cuh"
+#include "rfg_fast.cuh"
 #include "rfg_kernels.h"
 
 namespace rfg {
@@ -43,6 +44,23 @@ const void* tiles_mq_kernel_lcs(int width, bool norm, bool half)
     case 2: return pick_mq_lcs<uint16_t>(norm, half);
     case 4: return pick_mq_lcs<uint32_t>(norm, half);
     case 8: return pick_mq_lcs<unsigned long long>(norm, half);
+    }
+    return nullptr;
+}
+
+template <typename CT>
+static const void* pick_fast_lcs(bool half)
+{
+    return half ? (const void*)&k_fast<FAM_LCS, CT, 4, true> : (const void*)&k_fast<FAM_LCS, CT, 4, false>;
+}
+
+const void* fast_kernel_lcs(int width, bool half)
+{
+    switch (width) {
+    case 1: return pick_fast_lcs<uint8_t>(half);
+    case 2: return pick_fast_lcs<uint16_t>(half);
+    case 4: return pick_fast_lcs<uint32_t>(half);
+    case 8: return pick_fast_lcs<unsigned long long>(half);
     }
     return nullptr;
 }

@@ -1,5 +1,6 @@
 /* k_tiles instantiations of the LEV core family */
 #include "rfg_device.cuh"
+#include "rfg_fast.cuh"
 #include "rfg_kernels.h"
 
 namespace rfg {
@@ -43,6 +44,23 @@ const void* tiles_mq_kernel_lev(int width, bool norm, bool half)
     case 2: return pick_mq_lev<uint16_t>(norm, half);
     case 4: return pick_mq_lev<uint32_t>(norm, half);
     case 8: return pick_mq_lev<unsigned long long>(norm, half);
+    }
+    return nullptr;
+}
+
+template <typename CT>
+static const void* pick_fast_lev(bool half)
+{
+    return half ? (const void*)&k_fast<FAM_LEV, CT, 2, true> : (const void*)&k_fast<FAM_LEV, CT, 2, false>;
+}
+
+const void* fast_kernel_lev(int width, bool half)
+{
+    switch (width) {
+    case 1: return pick_fast_lev<uint8_t>(half);
+    case 2: return pick_fast_lev<uint16_t>(half);
+    case 4: return pick_fast_lev<uint32_t>(half);
+    case 8: return pick_fast_lev<unsigned long long>(half);
     }
     return nullptr;
 }

@@ -1,5 +1,6 @@
 /* k_tiles instantiations of the OSA core family */
 #include "rfg_device.cuh"
+#include "rfg_fast.cuh"
 #include "rfg_kernels.h"
 
 namespace rfg {
@@ -43,6 +44,23 @@ const void* tiles_mq_kernel_osa(int width, bool norm, bool half)
     case 2: return pick_mq_osa<uint16_t>(norm, half);
     case 4: return pick_mq_osa<uint32_t>(norm, half);
     case 8: return pick_mq_osa<unsigned long long>(norm, half);
+    }
+    return nullptr;
+}
+
+template <typename CT>
+static const void* pick_fast_osa(bool half)
+{
+    return half ? (const void*)&k_fast<FAM_OSA, CT, 2, true> : (const void*)&k_fast<FAM_OSA, CT, 2, false>;
+}
+
+const void* fast_kernel_osa(int width, bool half)
+{
+    switch (width) {
+    case 1: return pick_fast_osa<uint8_t>(half);
+    case 2: return pick_fast_osa<uint16_t>(half);
+    case 4: return pick_fast_osa<uint32_t>(half);
+    case 8: return pick_fast_osa<unsigned long long>(half);
     }
     return nullptr;
 }

@@ -14,6 +14,13 @@ const void* tiles_kernel_jaro(int width, int W, bool topk);
 const void* tiles_mq_kernel_lev(int width, bool norm, bool half);
 const void* tiles_mq_kernel_lcs(int width, bool norm, bool half);
 const void* tiles_mq_kernel_osa(int width, bool norm, bool half);
+/* k_fast<FAM, CT, Q, HALF> (unit-weight distances of one-word patterns, warp tiles over
+ * the length-filter range of each window; HALF: 32-bit words for patterns of <= 32 units) */
+const void* fast_kernel_lev(int width, bool half);
+const void* fast_kernel_lcs(int width, bool half);
+const void* fast_kernel_osa(int width, bool half);
+/* queries per lane of k_fast */
+inline int fast_queries(int fam) { return fam == FAM_LCS ? 4 : 2; }
 /* k_tiles_mq_jaro<CT, Q> (Jaro / Jaro-Winkler, several queries per thread) */
 const void* tiles_mq_kernel_jaro(int width);
 /* queries per thread of the several-queries kernels of a family (measured on GB300:
