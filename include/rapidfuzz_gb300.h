@@ -264,7 +264,9 @@ rfg_status rfg_server_destroy(rfg_server server);
  * looks up that array's address (make it before any stream capture); calls that
  * overlap on the GPU race on the array and must be serialised.  max_query_len bounds
  * the query lengths (at most 4096 code units); larger values, or a query longer than
- * the bound, return RFG_ERR_INVALID_ARGUMENT.  Runs on cuda_stream and waits for it. */
+ * the bound, return RFG_ERR_INVALID_ARGUMENT (in the second case after the kernel ran:
+ * the rows of the other queries are written, that query's row is left as it was).
+ * Runs on cuda_stream and waits for it. */
 rfg_status rfg_cdist_noalloc(rfg_metric metric, rfg_op op, rfg_form form, const rfg_strings* queries,
                              const rfg_strings* choices, int64_t max_query_len, const rfg_params* params,
                              rfg_cutoff cutoff, rfg_dtype out_dtype, void* out, int64_t ld, void* cuda_stream);

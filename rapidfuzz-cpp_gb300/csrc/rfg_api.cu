@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -70,7 +71,7 @@ rfg_status fail(rfg_status s, const char* fmt, ...)
 #define RFG_MAX_ROW_BLOCKS 12
 
 struct Ctx {
-    bool init = false;
+    std::atomic<bool> init{false};
     int device = 0;
     int sms = 0;
     cudaStream_t stream = nullptr;
@@ -103,9 +104,28 @@ struct Ctx {
 };
 Ctx g;
 
+thread_local int t_device = -1; /* the device this host thread has made current */
+
+rfg_status ensure_ctx_locked();
+
+/* The library's context, created once (thread-safe); every host thread that calls in has
+ * the library's device made current for it. */
 rfg_status ensure_ctx()
 {
-    if (g.init) return RFG_OK;
+    if (!g.init.load(std::memory_order_acquire)) {
+        std::lock_guard<std::recursive_mutex> lk(g.mu);
+        RFG_TRY(ensure_ctx_locked());
+    }
+    if (t_device != g.device) {
+        RFG_CUDA(cudaSetDevice(g.device));
+        t_device = g.device;
+    }
+    return RFG_OK;
+}
+
+rfg_status ensure_ctx_locked()
+{
+    if (g.init.load(std::memory_order_relaxed)) return RFG_OK;
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0)
@@ -124,7 +144,7 @@ rfg_status ensure_ctx()
     RFG_CUDA(cudaDeviceGetDefaultMemPool(&pool, g.device));
     uint64_t thr = UINT64_MAX;
     RFG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
-    g.init = true;
+    g.init.store(true, std::memory_order_release);
     return RFG_OK;
 }
 
@@ -1298,25 +1318,57 @@ rfg_status token_cdist(int metric, int op, int form, const rfg_strings* Q, bool 
 /* One pair in one round trip (the per-call path of the free functions and the cached
  * scorers): both strings, their offsets, the tile list and the zeroed counter and check
  * flag leave in one copy from pinned staging memory, one CTA of the any-length kernel
- * scores the pair, and the check flag and the result return in one copy.  Staging and
- * scratch are allocated once per context; calls are serialised by the library lock. */
-struct PairPath {
-    bool init = false;
+ * scores the pair, and the check flag and the result return in one copy.
+ *
+ * The reference's Cached* scorers are const and are called from many host threads at
+ * once (its README's OpenMP loop over choices), so this path takes no library-wide
+ * lock: every host thread gets a slot of its own -- pinned staging, device staging and
+ * scratch, and a stream -- on its first call, and its calls run on that stream while
+ * other threads' calls run on theirs.  Past kPairMaxSlots threads, slots are shared
+ * (each slot's mutex serialises its users). */
+struct PairSlot {
+    std::mutex mu;
+    cudaStream_t stream = nullptr;
     unsigned char* h = nullptr; /* pinned */
     unsigned char* d = nullptr;
     u64* scratch = nullptr;
 };
-PairPath g_pair;
 constexpr size_t kPairStage = 64 * 1024, kPairHead = 128, kPairScratchWords = 128 * 1024;
 constexpr int64_t kPairMaxLen1 = 1024;
+constexpr size_t kPairMaxSlots = 64;
+std::mutex g_slot_mu;
+std::vector<PairSlot*> g_slots; /* never freed: streams and staging live as long as the process */
+size_t g_slot_next = 0;
+thread_local PairSlot* t_slot = nullptr;
 
-rfg_status pair_path_init()
+rfg_status pair_slot(PairSlot** out)
 {
-    if (g_pair.init) return RFG_OK;
-    RFG_CUDA(cudaHostAlloc((void**)&g_pair.h, kPairStage, cudaHostAllocDefault));
-    RFG_CUDA(cudaMalloc((void**)&g_pair.d, kPairStage));
-    RFG_CUDA(cudaMalloc((void**)&g_pair.scratch, kPairScratchWords * 8));
-    g_pair.init = true;
+    if (t_slot) {
+        *out = t_slot;
+        return RFG_OK;
+    }
+    std::lock_guard<std::mutex> lk(g_slot_mu);
+    if (g_slots.size() >= kPairMaxSlots) {
+        t_slot = g_slots[g_slot_next++ % g_slots.size()];
+        *out = t_slot;
+        return RFG_OK;
+    }
+    PairSlot* s = new PairSlot();
+    cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaHostAlloc((void**)&s->h, kPairStage, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&s->d, kPairStage);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&s->scratch, kPairScratchWords * 8);
+    if (e != cudaSuccess) {
+        if (s->scratch) cudaFree(s->scratch);
+        if (s->d) cudaFree(s->d);
+        if (s->h) cudaFreeHost(s->h);
+        if (s->stream) cudaStreamDestroy(s->stream);
+        delete s;
+        return fail(RFG_ERR_OUT_OF_MEMORY, "per-thread staging of the per-call path: %s", cudaGetErrorString(e));
+    }
+    g_slots.push_back(s);
+    t_slot = s;
+    *out = s;
     return RFG_OK;
 }
 
@@ -1350,10 +1402,13 @@ rfg_status score_pair_trip(int metric, int op, int form, const void* s1, int64_t
     const int block = 128;
     const int64_t table = wmax ? (int64_t)(256 + hcap + 1) * wmax + hcap : 0;
     if (table + block * per_thread > (int64_t)kPairScratchWords) return RFG_OK;
-    RFG_TRY(pair_path_init());
+    PairSlot* slot;
+    RFG_TRY(pair_slot(&slot));
+    std::lock_guard<std::mutex> slot_lk(slot->mu);
+    const cudaStream_t st = slot->stream;
 
-    unsigned char* h = g_pair.h;
-    unsigned char* d = g_pair.d;
+    unsigned char* h = slot->h;
+    unsigned char* d = slot->d;
     int64_t* hoff = (int64_t*)h;
     hoff[0] = 0;
     hoff[1] = l1;
@@ -1368,7 +1423,7 @@ rfg_status score_pair_trip(int metric, int op, int form, const void* s1, int64_t
     }
     if (b1) memcpy(h + o1, s1, b1);
     if (b2) memcpy(h + o2, s2, b2);
-    RFG_CUDA(cudaMemcpyAsync(d, h, o2 + b2, cudaMemcpyHostToDevice, g.stream));
+    RFG_CUDA(cudaMemcpyAsync(d, h, o2 + b2, cudaMemcpyHostToDevice, st));
 
     KParams a;
     memset(&a, 0, sizeof a);
@@ -1393,7 +1448,7 @@ rfg_status score_pair_trip(int metric, int op, int form, const void* s1, int64_t
     a.tab_t = -1;
     a.better_high = better_high_of(op);
     a.wmax = wmax;
-    a.scratch = g_pair.scratch;
+    a.scratch = slot->scratch;
     if (qparts) {
         a.qparts = (const int32_t*)(d + 64);
         a.cparts = (const int32_t*)(d + 80);
@@ -1402,9 +1457,9 @@ rfg_status score_pair_trip(int metric, int op, int form, const void* s1, int64_t
     a.scratch_per_cta = table + block * per_thread;
     const void* fn = generic_kernel(fam == FAM_NONE ? FAM_WF : fam, w2, false);
     void* args[] = {&a};
-    RFG_CUDA(cudaLaunchKernel(fn, dim3(1), dim3(block), args, 0, g.stream));
-    RFG_CUDA(cudaMemcpyAsync(h + 40, d + 40, 16, cudaMemcpyDeviceToHost, g.stream));
-    RFG_CUDA(cudaStreamSynchronize(g.stream));
+    RFG_CUDA(cudaLaunchKernel(fn, dim3(1), dim3(block), args, 0, st));
+    RFG_CUDA(cudaMemcpyAsync(h + 40, d + 40, 16, cudaMemcpyDeviceToHost, st));
+    RFG_CUDA(cudaStreamSynchronize(st));
     const int err = ((int32_t*)(h + 40))[0];
     if (err) return fail(RFG_ERR_DEVICE_CHECK, "device-side check failed (code %d)", err);
     memcpy(result, h + 48, 8);
@@ -1431,6 +1486,7 @@ rfg_status token_set_one(int metric, int op, int form, const void* s1, int64_t l
     if (done) return RFG_OK;
     int64_t q1[2] = {0, l1}, q2[2] = {0, l2};
     rfg_strings q{s1, q1, 1, w1}, c{s2, q2, 1, w2};
+    std::lock_guard<std::recursive_mutex> lk(g.mu); /* the batch path shares the library's stream */
     return token_cdist(metric, op, form, &q, false, &c, false, p, cut, dt, result, 1, false);
 }
 
@@ -1467,6 +1523,7 @@ rfg_status score_one(int metric, int op, int form, const void* s1, int64_t l1, i
     if (done) return RFG_OK;
     int64_t o1[2] = {0, l1}, o2[2] = {0, l2};
     rfg_strings q{s1, o1, 1, w1}, c{s2, o2, 1, w2};
+    std::lock_guard<std::recursive_mutex> lk(g.mu); /* the batch path shares the library's stream */
     return cdist_impl(metric, op, form, &q, &c, p, cut, dt, result, 1, 0);
 }
 
@@ -1558,7 +1615,7 @@ rfg_status rfg_score_i64(rfg_metric metric, rfg_op op, const void* s1, int64_t l
                          int64_t len2, int32_t width2, const rfg_params* params, uint64_t score_cutoff,
                          uint64_t score_hint, int64_t* result)
 {
-    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    /* no library-wide lock: the per-pair path runs on this thread's own slot */
     if (!is_int_result(metric, op)) return fail(RFG_ERR_INVALID_ARGUMENT, "this metric/op returns a double");
     rfg_cutoff cut{score_cutoff, 0.0, score_hint, 0.0};
     return score_one(metric, op, RFG_FORM_FREE, s1, len1, width1, s2, len2, width2, params, cut, RFG_I64, result);
@@ -1568,7 +1625,6 @@ rfg_status rfg_score_f64(rfg_metric metric, rfg_op op, const void* s1, int64_t l
                          int64_t len2, int32_t width2, const rfg_params* params, double score_cutoff, double score_hint,
                          double* result)
 {
-    std::lock_guard<std::recursive_mutex> lk(g.mu);
     if (is_int_result(metric, op)) return fail(RFG_ERR_INVALID_ARGUMENT, "this metric/op returns an integer");
     rfg_cutoff cut{0, score_cutoff, 0, score_hint};
     return score_one(metric, op, RFG_FORM_FREE, s1, len1, width1, s2, len2, width2, params, cut, RFG_F64, result);
@@ -1668,7 +1724,7 @@ static rfg_status cached_many(rfg_cached h, int op, const rfg_strings* C, rfg_cu
 rfg_status rfg_cached_score_i64(rfg_cached h, rfg_op op, const void* s2, int64_t len2, int32_t width2,
                                 uint64_t score_cutoff, uint64_t score_hint, int64_t* result)
 {
-    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    /* const and reentrant like CachedX::distance: no library-wide lock on the per-pair path */
     if (!h) return fail(RFG_ERR_INVALID_ARGUMENT, "scorer is NULL");
     if (!is_int_result(h->metric, op)) return fail(RFG_ERR_INVALID_ARGUMENT, "this metric/op returns a double");
     if (!valid_width(width2) || len2 < 0 || (!s2 && len2) || !result) return fail(RFG_ERR_INVALID_ARGUMENT, "invalid s2");
@@ -1680,13 +1736,13 @@ rfg_status rfg_cached_score_i64(rfg_cached h, rfg_op op, const void* s2, int64_t
     if (done) return RFG_OK;
     int64_t off[2] = {0, len2};
     rfg_strings c{s2, off, 1, width2};
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
     return cached_many(h, op, &c, rfg_cutoff{score_cutoff, 0.0, score_hint, 0.0}, RFG_I64, result, 0);
 }
 
 rfg_status rfg_cached_score_f64(rfg_cached h, rfg_op op, const void* s2, int64_t len2, int32_t width2,
                                 double score_cutoff, double score_hint, double* result)
 {
-    std::lock_guard<std::recursive_mutex> lk(g.mu);
     if (!h) return fail(RFG_ERR_INVALID_ARGUMENT, "scorer is NULL");
     if (is_int_result(h->metric, op)) return fail(RFG_ERR_INVALID_ARGUMENT, "this metric/op returns an integer");
     if (!valid_width(width2) || len2 < 0 || (!s2 && len2) || !result) return fail(RFG_ERR_INVALID_ARGUMENT, "invalid s2");
@@ -1716,6 +1772,7 @@ rfg_status rfg_cached_score_f64(rfg_cached h, rfg_op op, const void* s2, int64_t
     if (done) return RFG_OK;
     int64_t off[2] = {0, len2};
     rfg_strings c{s2, off, 1, width2};
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
     return cached_many(h, op, &c, rfg_cutoff{0, score_cutoff, 0, score_hint}, RFG_F64, result, 0);
 }
 

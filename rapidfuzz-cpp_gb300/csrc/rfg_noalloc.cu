@@ -22,9 +22,13 @@
  *    the array: serialise them.
  *  - Limits: query lengths up to RFG_NOALLOC_MAX_QUERY_LEN (4096) code units; larger
  *    arguments are rejected with RFG_ERR_INVALID_ARGUMENT before anything is launched.
+ *    A query longer than the caller's max_query_len is found on the device: its row of
+ *    `out` is left as it was, every other row is written, and the call returns
+ *    RFG_ERR_INVALID_ARGUMENT -- so after that error `out` is partly written.
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 
@@ -173,7 +177,9 @@ extern "C" rfg_status rfg_cdist_noalloc(rfg_metric metric, rfg_op op, rfg_form f
 
     int fam = metric_family(metric, form, sp);
     if (fam == FAM_NONE) fam = FAM_WF;
-    const int wmax = fam == FAM_WF ? 0 : (int)((max_query_len + 63) / 64);
+    /* at least one word: a bound of 0 (only empty queries) still gets a table of its own
+     * per block */
+    const int wmax = fam == FAM_WF ? 0 : (int)std::max<int64_t>(1, (max_query_len + 63) / 64);
     int hcap = 0;
     if (fam != FAM_WF && choices->char_width > 1 && queries->char_width > 1) {
         hcap = 8;
