@@ -221,9 +221,12 @@ rfg_status rfg_extract(rfg_corpus corpus, rfg_metric metric, rfg_op op, const rf
  * with the same spec (corpus, metric, op, params, cutoff, limit, tie rule, width) into
  * batches of up to max_batch and admits a batch whenever one of max_inflight stream
  * slots is free and its device-memory estimate fits max_device_bytes (0: 80 % of the
- * free device memory at create); batches run concurrently.  wait() blocks until the
- * request's result is in its out_* buffers (limit entries; out_count set) and reports
- * the submit-to-completion latency.  Results equal rfg_extract of the request alone. */
+ * free device memory at create); batches run concurrently.  A request that alone needs
+ * more than max_device_bytes is refused at submit with RFG_ERR_BUSY.  wait() blocks until
+ * the request's result is in its out_* buffers (limit entries; out_count set) and reports
+ * the submit-to-completion latency, or returns RFG_ERR_BUSY once timeout_s (> 0) has
+ * passed without a result (the request stays queued; wait again).  Results equal
+ * rfg_extract of the request alone. */
 typedef struct {
     int32_t max_inflight;
     int32_t max_batch;
@@ -252,6 +255,13 @@ rfg_status rfg_server_submit(rfg_server server, const rfg_request* request, uint
 rfg_status rfg_server_wait(rfg_server server, uint64_t ticket, double timeout_s, double* latency_ms);
 rfg_status rfg_server_stats(rfg_server server, int64_t* completed, int64_t* batches, int64_t* batched_requests);
 rfg_status rfg_server_destroy(rfg_server server);
+
+/* ------------------------------------------------------------------ testing
+ * Fault injection on the host for the library's own failure tests (no reference
+ * counterpart): after `after` more successful device allocations of the batch engine,
+ * every further one fails as if the device were out of memory, so that callers see
+ * RFG_ERR_OUT_OF_MEMORY; a negative value switches the injection off. */
+rfg_status rfg_testing_fail_device_allocs(int64_t after);
 
 /* ------------------------------------------------------ no-allocation cdist
  * rfg_cdist_noalloc has no counterpart in the reference.  It is for callers that may

@@ -164,6 +164,10 @@ rfg_status upload_stage(size_t bytes, unsigned char** h)
     return RFG_OK;
 }
 
+/* allocations left before the injected failures of rfg_testing_fail_device_allocs
+ * (negative: no injection) */
+std::atomic<int64_t> g_fail_allocs_after{-1};
+
 /* stream-ordered device allocation freed at scope exit */
 struct DBuf {
     void* p = nullptr;
@@ -178,6 +182,11 @@ struct DBuf {
     rfg_status alloc(size_t bytes)
     {
         if (bytes == 0) bytes = 16;
+        if (g_fail_allocs_after.load(std::memory_order_relaxed) >= 0 && g_fail_allocs_after.fetch_sub(1) <= 0) {
+            g_fail_allocs_after.store(0);
+            p = nullptr;
+            return fail(RFG_ERR_OUT_OF_MEMORY, "device allocation of %zu bytes failed (injected)", bytes);
+        }
         cudaError_t e = cudaMallocAsync(&p, bytes, g.stream);
         if (e != cudaSuccess) {
             p = nullptr;
@@ -271,6 +280,15 @@ rfg_status check_strings(const rfg_strings* s, const char* what)
     if (s->count < 0) return fail(RFG_ERR_INVALID_ARGUMENT, "%s: negative count", what);
     if (!valid_width(s->char_width)) return fail(RFG_ERR_INVALID_ARGUMENT, "%s: char_width must be 1, 2, 4 or 8", what);
     if (!s->offsets) return fail(RFG_ERR_INVALID_ARGUMENT, "%s: offsets is NULL", what);
+    return RFG_OK;
+}
+
+/* offsets of a host batch: non-decreasing from 0 up, strings shorter than 2^31 units */
+rfg_status check_offsets(const int64_t* off, int64_t n, const char* what)
+{
+    for (int64_t i = 0; i < n; ++i)
+        if (off[i] < 0 || off[i + 1] < off[i] || off[i + 1] - off[i] > INT32_MAX)
+            return fail(RFG_ERR_INVALID_ARGUMENT, "%s: offsets must be non-decreasing and >= 0", what);
     return RFG_OK;
 }
 
@@ -461,11 +479,11 @@ rfg_status choice_lengths(const KStrings& c, const int64_t* host_off, std::vecto
         RFG_CUDA(cudaStreamSynchronize(g.stream));
         host_off = tmp->data();
     }
+    /* device-resident offsets are seen here first: a batch with broken offsets is
+     * refused before any kernel reads strings through them */
+    RFG_TRY(check_offsets(host_off, nc, "choices"));
     len->resize(nc);
-    for (int64_t i = 0; i < nc; ++i) {
-        const int64_t l = host_off[i + 1] - host_off[i];
-        (*len)[i] = (int32_t)(l < 0 ? 0 : l > INT32_MAX ? INT32_MAX : l);
-    }
+    for (int64_t i = 0; i < nc; ++i) (*len)[i] = (int32_t)(host_off[i + 1] - host_off[i]);
     return RFG_OK;
 }
 
@@ -1077,9 +1095,13 @@ rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const 
     if (ld == 0) ld = nc;
     if (ld < nc) return fail(RFG_ERR_INVALID_ARGUMENT, "ld must be >= the number of choices");
     if (!out && nq * nc) return fail(RFG_ERR_INVALID_ARGUMENT, "out is NULL");
+    const bool dev_in = flags & RFG_DEVICE_INPUTS;
+    if (!dev_in) { /* host offsets are checked before the device is touched */
+        RFG_TRY(check_offsets(Q->offsets, nq, "queries"));
+        RFG_TRY(check_offsets(C->offsets, nc, "choices"));
+    }
     RFG_TRY(ensure_ctx());
 
-    const bool dev_in = flags & RFG_DEVICE_INPUTS;
     QuerySet qs;
     DBuf qd, qo, cd, co, od;
     KStrings ck;
@@ -1088,6 +1110,7 @@ rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const 
         std::vector<int64_t> off(nq + 1);
         RFG_CUDA(cudaMemcpyAsync(off.data(), Q->offsets, (nq + 1) * 8, cudaMemcpyDeviceToHost, g.stream));
         RFG_CUDA(cudaStreamSynchronize(g.stream));
+        RFG_TRY(check_offsets(off.data(), nq, "queries")); /* before anything is read through them */
         std::vector<unsigned char> qh;
         if (Q->char_width > 1 && nq) {
             qh.resize((size_t)off[nq] * Q->char_width);
@@ -1203,13 +1226,6 @@ struct HostStrings {
     std::vector<int64_t> off;
 };
 
-rfg_status check_offsets(const int64_t* off, int64_t n, const char* what)
-{
-    for (int64_t i = 0; i < n; ++i)
-        if (off[i] < 0 || off[i + 1] < off[i] || off[i + 1] - off[i] > INT32_MAX)
-            return fail(RFG_ERR_INVALID_ARGUMENT, "%s: offsets must be non-decreasing and >= 0", what);
-    return RFG_OK;
-}
 
 rfg_status download_strings(const rfg_strings* s, HostStrings* h, const char* what)
 {
@@ -1601,6 +1617,12 @@ rfg_status rfg_set_device(int device)
     if (g.init && device != g.device) return fail(RFG_ERR_INVALID_ARGUMENT, "device already selected");
     g.device = device;
     return ensure_ctx();
+}
+
+rfg_status rfg_testing_fail_device_allocs(int64_t after)
+{
+    g_fail_allocs_after.store(after < 0 ? -1 : after);
+    return RFG_OK;
 }
 
 rfg_status rfg_synchronize(void)
@@ -2095,6 +2117,7 @@ rfg_status rfg_corpus_create(const rfg_strings* C, uint32_t flags, rfg_corpus* o
     if (!out) return fail(RFG_ERR_INVALID_ARGUMENT, "out is NULL");
     *out = nullptr;
     RFG_TRY(check_strings(C, "choices"));
+    if (!(flags & RFG_DEVICE_INPUTS)) RFG_TRY(check_offsets(C->offsets, C->count, "choices"));
     RFG_TRY(ensure_ctx());
     rfg_corpus c = new rfg_corpus_s();
     const int64_t nc = C->count;
@@ -2106,6 +2129,7 @@ rfg_status rfg_corpus_create(const rfg_strings* C, uint32_t flags, rfg_corpus* o
         if (cudaMemcpy(hoff.data(), C->offsets, (nc + 1) * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
             st = fail(RFG_ERR_CUDA, "reading choice offsets failed");
         off = hoff.data();
+        if (st == RFG_OK) st = check_offsets(off, nc, "choices");
         /* the corpus keeps its own copy: callers may free theirs */
         if (st == RFG_OK) st = c->data.alloc((size_t)off[nc] * C->char_width + 16);
         if (st == RFG_OK) st = c->off.alloc((size_t)(nc + 1) * 8);
@@ -2437,6 +2461,10 @@ rfg_status rfg_batch_create(rfg_metric metric, rfg_op op, rfg_form form, const r
     const int64_t nq = Q->count, nc = C->count;
     if (ld == 0) ld = nc;
     if (ld < nc) return fail(RFG_ERR_INVALID_ARGUMENT, "ld must be >= the number of choices");
+    if (!(flags & RFG_DEVICE_INPUTS)) { /* host offsets are checked before the device is touched */
+        RFG_TRY(check_offsets(Q->offsets, nq, "queries"));
+        RFG_TRY(check_offsets(C->offsets, nc, "choices"));
+    }
     RFG_TRY(ensure_ctx());
     rfg_batch b = new rfg_batch_s();
     rfg_status st = RFG_OK;
@@ -2445,6 +2473,7 @@ rfg_status rfg_batch_create(rfg_metric metric, rfg_op op, rfg_form form, const r
         std::vector<unsigned char> qh;
         if (cudaMemcpy(off.data(), Q->offsets, (nq + 1) * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
             st = fail(RFG_ERR_CUDA, "reading query offsets failed");
+        if (st == RFG_OK) st = check_offsets(off.data(), nq, "queries"); /* before anything is read through them */
         if (st == RFG_OK && Q->char_width > 1 && nq) {
             qh.resize((size_t)off[nq] * Q->char_width);
             if (cudaMemcpy(qh.data(), Q->data, qh.size(), cudaMemcpyDeviceToHost) != cudaSuccess)

@@ -37,6 +37,13 @@ rfg_status server_extract_enqueue(rfg_corpus c, const unsigned char* qdata, cons
 rfg_status server_extract_results(void* job, int64_t* idx, double* score, int32_t* count, cudaStream_t st);
 void server_extract_free(void* job);
 int64_t corpus_chunks(rfg_corpus c);
+
+/* device bytes one batch holds while it runs: its packed queries, offsets, per-query
+ * thresholds and results, and the per-(query, chunk) candidate lists of the extract */
+inline int64_t batch_bytes(int64_t query_bytes, int64_t nq, int64_t k, int64_t chunks)
+{
+    return query_bytes + 8 * (nq + 1) + nq * (8 + 4 + 16 * k) + nq * chunks * k * 16 + (1 << 20);
+}
 } // namespace rfg
 
 using namespace rfg;
@@ -117,8 +124,7 @@ bool rfg_server_s::admit(Slot& s, std::unique_lock<std::mutex>& lk)
     /* device memory estimate: queries, thresholds, candidates, results */
     const int64_t k = head->r.limit;
     const int64_t nq = (int64_t)batch.size();
-    const int64_t est = (int64_t)data.size() + 8 * (nq + 1) + nq * (8 + 4 + 16 * k) +
-                        nq * corpus_chunks(corpora[head->r.corpus]) * k * 16 + (1 << 20);
+    const int64_t est = batch_bytes((int64_t)data.size(), nq, k, corpus_chunks(corpora[head->r.corpus]));
     if (bytes_in_use + est > cfg.max_device_bytes && bytes_in_use > 0) {
         /* not admitted: back to the front of the queue, in order */
         for (auto it = batch.rbegin(); it != batch.rend(); ++it) queue.push_front(*it);
@@ -266,6 +272,12 @@ rfg_status rfg_server_submit(rfg_server s, const rfg_request* r, uint64_t* ticke
     if (r->metric < RFG_LEVENSHTEIN || r->metric > RFG_RATIO || r->op < RFG_DISTANCE ||
         r->op > RFG_NORMALIZED_SIMILARITY || (r->metric == RFG_RATIO && r->op != RFG_SIMILARITY))
         return set_last_error(RFG_ERR_INVALID_ARGUMENT, "invalid metric/op");
+    /* memory-bounded admission: a request that alone needs more device memory than the
+     * server's budget can never run -- refused at once instead of queued */
+    const int64_t need = batch_bytes(r->query_len * r->query_width + 16, 1, r->limit, corpus_chunks(s->corpora[r->corpus]));
+    if (need > s->cfg.max_device_bytes)
+        return set_last_error(RFG_ERR_BUSY, "admission refused: the request needs more device memory than the "
+                                            "server's max_device_bytes");
     Req* q = new Req();
     q->r = *r;
     q->query.assign((const unsigned char*)r->query, (const unsigned char*)r->query + r->query_len * r->query_width);

@@ -107,6 +107,7 @@ def lib():
             "rfg_server_create": ([P(vp), i32, P(ServerConfig), P(vp)], ctypes.c_int),
             "rfg_server_submit": ([vp, P(Request), P(ctypes.c_uint64)], ctypes.c_int),
             "rfg_server_wait": ([vp, ctypes.c_uint64, ctypes.c_double, P(ctypes.c_double)], ctypes.c_int),
+            "rfg_testing_fail_device_allocs": ([i64], ctypes.c_int),
             "rfg_server_stats": ([vp, P(i64), P(i64), P(i64)], ctypes.c_int),
             "rfg_server_destroy": ([vp], ctypes.c_int),
             "rfg_cdist_noalloc": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, P(Strings), P(Strings), i64, P(Params),
