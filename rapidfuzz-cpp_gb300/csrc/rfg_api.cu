@@ -425,7 +425,7 @@ int g_mq_mode = 1;          /* one-word unit-weight distances take several queri
 int g_half_mode = 1;        /* queries of <= 32 units run on 32-bit recurrence words (autotuning) */
 int g_block_override = 0;   /* override of the tile kernels' block size (autotuning) */
 int g_fast_mode = 1;        /* unit-weight one-word distances run on the warp tiles (k_fast) */
-int64_t g_fast_window = 256; /* choice positions per warp window of k_fast (autotuning) */
+int64_t g_fast_window = 512; /* choice positions per warp window of k_fast (autotuning) */
 
 /* A prepared batch: everything a launch needs is on the device, so enqueue() only
  * resets the tile counters and launches the kernels (no host work, no allocation,
@@ -612,7 +612,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
     for (int64_t b = 0; b < nblk; ++b)
         if (!cls[b * 5].empty() && (c.width == 1 || cls_wide[b * 5] == 0)) fast_any = true;
     fast_any = fast_any && fast_ok && spec.topk == 0 && !spec.fixed_perm && g_fast_mode != 0;
-    const int64_t fwin = std::max<int64_t>(32, std::min<int64_t>(1024, g_fast_window / 4 * 4));
+    const int64_t fwin = std::max<int64_t>(32, std::min<int64_t>(1024, g_fast_window / 8 * 8));
     std::vector<int32_t> frec;
     if (spec.fixed_perm) {
         chunk = spec.fixed_chunk;
@@ -754,7 +754,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
                 if (n1 <= n0) continue;
                 const void* ff = fam == FAM_LEV ? fast_kernel_lev(c.width, half) : fam == FAM_LCS ? fast_kernel_lcs(c.width, half)
                                                                                               : fast_kernel_osa(c.width, half);
-                const size_t fsm = fast_smem_bytes(Qf, half, fwin, spec.out_dtype);
+                const size_t fsm = fast_smem_bytes(Qf, half, fwin, a.fast_k < 0xffff);
                 RFG_TRY(allow_dynamic_smem(ff, fsm));
                 const int64_t fslots = (int64_t)g.sms * occupancy(ff, fblock, fsm);
                 KParams h = a;

@@ -20,7 +20,9 @@
  * Layout (per warp, in dynamic shared memory): Q pattern tables of 257 rows (code units
  * 0..255, then an all-zero row for units the patterns lack), 64-bit rows for patterns
  * of up to 64 units or 32-bit rows for patterns of up to 32 units (whose recurrence runs
- * on 32-bit words, the ALU width); then Q x window results.
+ * on 32-bit words, the ALU width); then Q x window results, 16 bits wide when the cutoff
+ * allows (every value of the chain is at most K + 1), converted to the output type when
+ * the window's rows are written.
  */
 #pragma once
 #include "rfg_device.cuh"
@@ -34,15 +36,13 @@ namespace rfg {
 #define RFG_FAST_MINB 8 /* CTAs per SM the register budget is sized for (64 registers) */
 #endif
 
-/* bytes of one warp's slice: tables, then the result stage */
+/* bytes of one warp's slice: tables, then the result stage (16-bit results when every
+ * value the chain can give, at most K + 1, fits in 16 bits; else 32-bit) */
 __host__ __device__ inline size_t fast_pm_bytes(int Q, bool half) { return ((size_t)Q * 257 * (half ? 4 : 8) + 15) / 16 * 16; }
-__host__ __device__ inline size_t fast_stage_bytes(int Q, int64_t window, int out_dtype)
+__host__ __device__ inline size_t fast_stage_bytes(int Q, int64_t window, bool s16) { return (size_t)Q * window * (s16 ? 2 : 4); }
+inline size_t fast_smem_bytes(int Q, bool half, int64_t window, bool s16)
 {
-    return (size_t)Q * window * (out_dtype == 0 ? 4 : 8);
-}
-inline size_t fast_smem_bytes(int Q, bool half, int64_t window, int out_dtype)
-{
-    return (size_t)RFG_FAST_WARPS * (fast_pm_bytes(Q, half) + fast_stage_bytes(Q, window, out_dtype));
+    return (size_t)RFG_FAST_WARPS * (fast_pm_bytes(Q, half) + fast_stage_bytes(Q, window, s16));
 }
 
 template <typename WT>
@@ -96,12 +96,13 @@ __global__ void __launch_bounds__(RFG_FAST_WARPS * 32, RFG_FAST_MINB) k_fast(con
     typedef typename std::conditional<HALF, uint32_t, u64>::type WT;
     extern __shared__ u64 smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int win = (int)a.stage; /* positions per window (a multiple of 4, at most 1024) */
+    const int win = (int)a.stage; /* positions per window (a multiple of 8, at most 1024) */
+    const int K = (int)(a.fast_k < 0x7fffffff ? a.fast_k : 0x7fffffff);
+    const bool s16 = K < 0xffff;
     const size_t pmb = fast_pm_bytes(Q, HALF);
-    unsigned char* slice = (unsigned char*)smem + (size_t)warp * (pmb + fast_stage_bytes(Q, win, a.out_dtype));
+    unsigned char* slice = (unsigned char*)smem + (size_t)warp * (pmb + fast_stage_bytes(Q, win, s16));
     WT* rows = (WT*)slice;
     unsigned char* stage = slice + pmb;
-    const int K = (int)(a.fast_k < 0x7fffffff ? a.fast_k : 0x7fffffff);
     /* the host keeps tasks and windows below 2^31 */
     const int nwin = (int)a.nchunks;
     const int ntasks = (int)(((int64_t)a.nq + Q - 1) / Q * nwin);
@@ -159,20 +160,20 @@ __global__ void __launch_bounds__(RFG_FAST_WARPS * 32, RFG_FAST_MINB) k_fast(con
         const int lo = first_at_least(lens, nn, (int64_t)mmin - K, lane);
         const int hi = first_at_least(lens, nn, (int64_t)mmax + K + 1, lane);
         /* the stage holds K + 1 for every pair the filter rejects */
-        if (a.out_dtype == 0) {
-            const int v = K < 0x7fffffff ? K + 1 : K;
-            const int4 f = make_int4(v, v, v, v);
-            for (int i = lane * 4; i < Q * win; i += 128) *(int4*)((int*)stage + i) = f;
-        }
-        else {
-            const long long v = a.out_dtype == 1 ? (long long)K + 1
-                                                 : (long long)__double_as_longlong(int_result_as_double((i64)K + 1));
-            const longlong2 f = make_longlong2(v, v);
-            for (int i = lane * 2; i < Q * win; i += 64) *(longlong2*)((long long*)stage + i) = f;
+        {
+            const unsigned v = K < 0x7fffffff ? (unsigned)K + 1 : (unsigned)K;
+            const unsigned w2 = s16 ? v * 0x10001u : v;
+            const int4 f = make_int4((int)w2, (int)w2, (int)w2, (int)w2);
+            const int words = Q * win / (s16 ? 2 : 1); /* 32-bit words of the stage */
+            for (int i = lane * 4; i < words; i += 128) *(int4*)((unsigned*)stage + i) = f;
         }
         __syncwarp();
+        /* the next position's record is loaded while the current one is scored */
+        int4 rn = make_int4(0, 0, 0, 0);
+        if (lo + lane < hi) rn = __ldg(a.prec + p0 + lo + lane);
         for (int p = lo + lane; p < hi; p += 32) {
-            const int4 r = __ldg(a.prec + p0 + p);
+            const int4 r = rn;
+            if (p + 32 < hi) rn = __ldg(a.prec + p0 + p + 32);
             const int64_t o0 = (int64_t)(((uint64_t)(uint32_t)r.y << 32) | (uint32_t)r.x);
             int d[Q];
             fast_group<FAM, Q, FastRows<WT>, MQText<CT>, WT>(FastRows<WT>{rows}, m, qn,
@@ -181,30 +182,46 @@ __global__ void __launch_bounds__(RFG_FAST_WARPS * 32, RFG_FAST_MINB) k_fast(con
             for (int q = 0; q < Q; ++q) {
                 if (q >= qn) break;
                 const int at = q * win + r.w;
-                if (a.out_dtype == 0) ((int*)stage)[at] = d[q];
-                else if (a.out_dtype == 1) ((long long*)stage)[at] = d[q];
-                else ((double*)stage)[at] = int_result_as_double(d[q]);
+                if (s16) ((unsigned short*)stage)[at] = (unsigned short)d[q];
+                else ((unsigned*)stage)[at] = (unsigned)d[q];
             }
         }
         __syncwarp();
-        /* the window's rows: 16-byte stores where the row segment is aligned */
+        /* the window's rows, converted to the output type: 16-byte stores where the row
+         * segment is aligned */
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             if (q >= qn) break;
             const int64_t base = (int64_t)qi[q] * a.ld + p0;
+            const unsigned short* s1 = (const unsigned short*)stage + q * win;
+            const unsigned* s2 = (const unsigned*)stage + q * win;
             if (a.out_dtype == 0) {
-                const int* src = (const int*)stage + q * win;
                 int* dst = (int*)a.out + base;
                 const int nv = a.vec ? nn & ~3 : 0;
-                for (int i = lane * 4; i < nv; i += 128) *(int4*)(dst + i) = *(const int4*)(src + i);
-                for (int i = nv + lane; i < nn; i += 32) dst[i] = src[i];
+                for (int i = lane * 4; i < nv; i += 128) {
+                    int4 o;
+                    if (s16) {
+                        const uint2 u = *(const uint2*)(s1 + i);
+                        o = make_int4((int)(u.x & 0xffff), (int)(u.x >> 16), (int)(u.y & 0xffff), (int)(u.y >> 16));
+                    }
+                    else
+                        o = *(const int4*)(s2 + i);
+                    *(int4*)(dst + i) = o;
+                }
+                for (int i = nv + lane; i < nn; i += 32) dst[i] = s16 ? (int)s1[i] : (int)s2[i];
             }
             else {
-                const long long* src = (const long long*)stage + q * win;
                 long long* dst = (long long*)a.out + base;
+                const bool dbl = a.out_dtype == 2;
+                auto conv = [&](unsigned x) -> long long {
+                    return dbl ? (long long)__double_as_longlong(int_result_as_double((i64)x)) : (long long)x;
+                };
                 const int nv = a.vec ? nn & ~1 : 0;
-                for (int i = lane * 2; i < nv; i += 64) *(longlong2*)(dst + i) = *(const longlong2*)(src + i);
-                for (int i = nv + lane; i < nn; i += 32) dst[i] = src[i];
+                for (int i = lane * 2; i < nv; i += 64) {
+                    const unsigned x0 = s16 ? s1[i] : s2[i], x1 = s16 ? s1[i + 1] : s2[i + 1];
+                    *(longlong2*)(dst + i) = make_longlong2(conv(x0), conv(x1));
+                }
+                for (int i = nv + lane; i < nn; i += 32) dst[i] = conv(s16 ? s1[i] : s2[i]);
             }
         }
         __syncwarp();
