@@ -39,9 +39,10 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 METRIC_NAME = "GCUPS & pairs/s, batched vs per-call, 1 GB300, bit-exact; extract p50/p99 ms"
 # dram__bytes_read.sum + dram__bytes_write.sum of one metric's k_fast launches (64-bit and
-# 32-bit words) on this workload from one `ncu --metrics` capture, per step (filled in from
-# the capture summarised under profiles/; empty: not measured for this build)
-DRAM_BYTES_PER_LAUNCH = {}
+# 32-bit words) on this workload, averaged over the four steps of one `ncu --metrics`
+# capture (profiles/cdist4096_launch_list.md): the strings are read once, the 67 MB of
+# results stay in the 129 MB L2 when the launches end and are written back later
+DRAM_BYTES_PER_LAUNCH = {"levenshtein": 1170048, "indel": 1166336, "osa": 1027264}
 # algorithmic INT32 operations per word step (minimal 32-bit ALU form of the reference's
 # step): 64-bit words (Levenshtein_impl.hpp:285-302, LCSseq_impl.hpp:226-229,
 # OSA_impl.hpp:52-54) and the same model for a 32-bit word (patterns of <= 32 units, which
