@@ -929,6 +929,88 @@ RFG_HD i64 lev_band(const PMW& pm, int pw, int m, const TXT& t, int n, int K)
     return (i64)n; /* n == 0; callers never ask (|m-n| <= K < m) */
 }
 
+/* bits [a, b] of a 32-bit word, clipped to [0, 31]; empty when b < a */
+RFG_HD u32 range_mask32(int a, int b)
+{
+    if (a < 0) a = 0;
+    if (b > 31) b = 31;
+    if (b < a) return 0;
+    return (b >= 31 ? ~0u : ((1u << (b + 1)) - 1)) & ~(a >= 32 ? ~0u : ((1u << a) - 1));
+}
+
+/* bits [sh, sh + 32) of the 64-bit value hi:lo, sh in [0, 31] (one funnel shift) */
+RFG_HD u32 funnel32(u32 lo, u32 hi, int sh)
+{
+#ifdef __CUDA_ARCH__
+    return __funnelshift_r(lo, hi, sh);
+#else
+    return (u32)((((u64)hi << 32) | lo) >> sh);
+#endif
+}
+
+/* The banded Levenshtein of lev_band over B 32-bit words (a window of 32*B bits), for
+ * a pattern table of 32-bit words: pm(c) gives the row of text unit c as a pointer to
+ * its words, with at least B + 1 zero words before word 0 and B + 1 after the last, so
+ * the window's words are loaded without range tests.  Window bit b of step j is pattern
+ * index K+1-32B+j+b; extracting it takes one funnel shift per word (the GPU's native
+ * width), and the carry of (X & VP) + VP runs through the words.  Requires
+ * 2K+1 <= 32*B, |m-n| <= K < m, n > 0.  Same result as lev_band (levenshtein_hyrroe2003
+ * _small_band, Levenshtein_impl.hpp:419-505): d, or K + 1 once the diagonal lower bound
+ * passes K (checked every 8 text units). */
+template <int B, typename PM32, typename TXT>
+RFG_HD i64 lev_band32(const PM32& pm, int m, const TXT& t, int n, int K)
+{
+    const int NB = 32 * B;
+    u32 VP[B], VN[B], rmask[B];
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        VP[b] = range_mask32(NB - 1 - K - 32 * b, NB - 1 - 32 * b);
+        VN[b] = 0;
+        rmask[b] = range_mask32(NB - 1 - K + (m - n) - 32 * b, NB - 2 - 32 * b);
+    }
+    int diag = K;
+    int start = K + 1 - NB; /* pattern index of window bit 0 */
+    for (int j = 0; j < n; ++j, ++start) {
+        const u32* row = pm(t[j]);
+        const int w0 = start >> 5; /* floor division (arithmetic shift) */
+        const int sh = start & 31;
+        u32 X[B];
+        u32 prev = row[w0];
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const u32 next = row[w0 + b + 1];
+            X[b] = funnel32(prev, next, sh);
+            prev = next;
+        }
+        u32 D0[B];
+        u32 carry = 0;
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const u32 u = X[b] & VP[b];
+            const u64 s = (u64)u + VP[b] + carry;
+            carry = (u32)(s >> 32);
+            D0[b] = ((u32)s ^ VP[b]) | X[b] | VN[b];
+        }
+        diag += (D0[B - 1] >> 31) == 0;
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const u32 HP = VN[b] | ~(D0[b] | VP[b]);
+            const u32 HN = D0[b] & VP[b];
+            const u32 D0s = b + 1 < B ? funnel32(D0[b], D0[b + 1 < B ? b + 1 : b], 1) : (D0[b] >> 1);
+            VP[b] = HN | ~(D0s | HP);
+            VN[b] = D0s & HP;
+        }
+        if ((j & 7) == 7 || j == n - 1) {
+            int v = diag;
+#pragma unroll
+            for (int b = 0; b < B; ++b) v -= popc_w(VP[b] & rmask[b]) - popc_w(VN[b] & rmask[b]);
+            if (j == n - 1) return v;
+            if (v > K) return (i64)K + 1;
+        }
+    }
+    return (i64)n;
+}
+
 /* Jaro with P (= s1) of up to 64*W chars and a text of any length: the greedy
  * flagging of flag_similar_characters_block (Jaro_impl.hpp:134-256), with the window
  * masks built per word, and the transposition count of count_transpositions_block

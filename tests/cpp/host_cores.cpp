@@ -156,6 +156,38 @@ int hc_group(int fam, int word32, const uint8_t* a1, int m1, const uint8_t* a2, 
     return 0;
 }
 
+/* the 32-bit banded core (lev_band32<B>) with the compact padded table of the band
+ * kernel; B = 32-bit words of the window.  Returns -2 where the shape does not apply
+ * (2K+1 > 32B, K >= m, |m-n| > K, or an empty string). */
+struct PM32 {
+    const uint32_t* base;
+    const int32_t* rmap;
+    const uint32_t* operator()(uint64_t c) const { return base + rmap[c & 255]; }
+};
+
+int64_t hc_band32(int B, const uint8_t* a, int m, const uint8_t* b, int n, int64_t K)
+{
+    if (m == 0 || n == 0 || K >= m || 2 * K + 1 > 32 * B || (m > n ? m - n : n - m) > K) return -2;
+    const int W32 = (m + 31) / 32, pad = B + 1, S = W32 + 2 * pad;
+    std::vector<int32_t> rmap(256, 0);
+    int R = 1; /* row 0: the zero row */
+    for (int k = 0; k < m; ++k)
+        if (!rmap[a[k]]) rmap[a[k]] = R++;
+    std::vector<uint32_t> rows((size_t)R * S, 0);
+    for (int k = 0; k < m; ++k) rows[(size_t)rmap[a[k]] * S + pad + k / 32] |= 1u << (k % 32);
+    for (int c = 0; c < 256; ++c) rmap[c] = rmap[c] * S + pad;
+    const PM32 pm{rows.data(), rmap.data()};
+    const Txt t{b};
+    switch (B) {
+    case 1: return lev_band32<1>(pm, m, t, n, (int)K);
+    case 2: return lev_band32<2>(pm, m, t, n, (int)K);
+    case 4: return lev_band32<4>(pm, m, t, n, (int)K);
+    case 8: return lev_band32<8>(pm, m, t, n, (int)K);
+    case 16: return lev_band32<16>(pm, m, t, n, (int)K);
+    }
+    return -2;
+}
+
 /* the warp tiles' core (fast_group, int bookkeeping, one cutoff K for every pattern) on
  * four patterns (packed, offsets off[0..4]) of at most 64 units (32 with word32) against
  * one text; qn of the four slots are used; out[q] = the distance chain of pattern q */

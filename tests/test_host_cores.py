@@ -33,6 +33,8 @@ def libs():
     lib.hc_distance.argtypes = [I, I, P, I, P, I, I64]
     lib.hc_group.restype = I
     lib.hc_group.argtypes = [I, I, P, I, P, I, P, I, I64, I64, P]
+    lib.hc_band32.restype = I64
+    lib.hc_band32.argtypes = [I, P, I, P, I, I64]
     lib.hc_fast.restype = I
     lib.hc_fast.argtypes = [I, I, P, P, I, P, I, I, P]
     lib.hc_jaro.restype = I
@@ -140,6 +142,26 @@ def test_warp_tile_core_matches_oracle(libs, fam, word32):
             K = min(K, 2**31 - 1)
             assert lib.hc_fast(fam, word32, packed, off.ctypes.data, qn, b, len(b), K, out) == 0
             assert list(out)[:qn] == [d if d <= K else K + 1 for d in ds], (pats, b, K)
+
+
+def test_band32_core_matches_oracle(libs):
+    """lev_band32<B>: the 32-bit banded Levenshtein of the band kernel, every window size,
+    against the exact distance with the distance chain"""
+    lib, o = libs
+    rng = np.random.default_rng(77)
+    lens = [40, 63, 64, 65, 100, 127, 128, 129, 200, 300, 513, 700]
+    checked = 0
+    for a, b in pairs(78, 700, lens):
+        d = exact(o, 0, a, b)
+        for B in (1, 2, 4, 8, 16):
+            for K in sorted({int(rng.integers(0, 16 * B)), 16 * B - 1, max(0, d - 1), d, d + 1, abs(len(a) - len(b))}):
+                got = lib.hc_band32(B, a, len(a), b, len(b), K)
+                if got == -2:
+                    continue
+                # the core gives d, or any value above K once d > K (the chain maps it to K + 1)
+                assert (got == d) if d <= K else (got > K), (B, K, len(a), len(b), got, d)
+                checked += 1
+    assert checked > 2000
 
 
 def test_jaro_cores_match_oracle(libs):
