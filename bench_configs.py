@@ -163,7 +163,7 @@ def run(args, rank, world, local):
         line.update({"value": cells * steps / t / 1e9, "ms_per_step": t / steps * 1e3, "dtype": "u64",
                      "config": {"workload": "dna256x65536: Levenshtein normalized_distance cutoff 0.1, 256 x 65,536 DNA "
                                             "lognormal(300,0.6) in [100,2000], half mutated 1-15%",
-                                "pairs_per_s": nq * nc * steps / t},
+                                "pairs_per_s": nq * nc * steps / t, "kernels": b.kernels()},
                      "cpu_baseline": {"value": _cells(qsub, c) / tc / 1e9, "unit": "GCUPS", "cores": os.cpu_count(),
                                       "kind": "port", "sample": "16 of the 256 queries x all 65,536 choices"},
                      "e2e": None, "gpu_launches": steps, "clocks": clk})

@@ -32,6 +32,7 @@
 #include "rapidfuzz_gb300.h"
 #include "rfg_device.cuh"
 #include "rfg_fast.cuh"
+#include "rfg_band.cuh"
 #include "rfg_kernels.h"
 #include "rfg_token.h"
 
@@ -67,7 +68,7 @@ rfg_status fail(rfg_status s, const char* fmt, ...)
         if (s_ != RFG_OK) return s_;         \
     } while (0)
 
-#define RFG_COUNTERS 128
+#define RFG_COUNTERS 256
 #define RFG_MAX_ROW_BLOCKS 12
 
 struct Ctx {
@@ -237,22 +238,31 @@ struct QuerySet {
     KStrings dev{};
     std::vector<int64_t> len;
     std::vector<int32_t> wide;
+    /* distinct code units below 256 per query (the rows of the band kernel's compact
+     * table), or -1 where the query's units were not seen on the host */
+    std::vector<int32_t> distinct;
 };
 
 rfg_status query_info_from_host(const void* data, const int64_t* off, int64_t n, int width, QuerySet* qs)
 {
     qs->len.resize(n);
     qs->wide.assign(n, 0);
+    qs->distinct.assign(n, -1);
     for (int64_t i = 0; i < n; ++i) {
         const int64_t a = off[i], b = off[i + 1];
         if (a < 0 || b < a) return fail(RFG_ERR_INVALID_ARGUMENT, "offsets must be non-decreasing and >= 0");
         if (b - a > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "strings longer than 2^31-1 code units");
         qs->len[i] = b - a;
-        if (width > 1) {
-            int32_t w = 0;
-            for (int64_t k = a; k < b; ++k) w += unit_at(data, width, k) >= 256;
-            qs->wide[i] = w;
+        if (!data && b > a) continue;
+        u64 seen[4] = {0, 0, 0, 0};
+        int32_t w = 0;
+        for (int64_t k = a; k < b; ++k) {
+            const u64 c = unit_at(data, width, k);
+            if (c >= 256) ++w;
+            else seen[c >> 6] |= 1ull << (c & 63);
         }
+        qs->wide[i] = width > 1 ? w : 0;
+        qs->distinct[i] = popc64(seen[0]) + popc64(seen[1]) + popc64(seen[2]) + popc64(seen[3]);
     }
     return RFG_OK;
 }
@@ -425,6 +435,67 @@ int g_mq_mode = 1;          /* one-word unit-weight distances take several queri
 int g_half_mode = 1;        /* queries of <= 32 units run on 32-bit recurrence words (autotuning) */
 int g_block_override = 0;   /* override of the tile kernels' block size (autotuning) */
 int g_fast_mode = 1;        /* unit-weight one-word distances run on the warp tiles (k_fast) */
+int g_band_mode = 1;        /* unit-weight Levenshtein with a band narrower than the pattern runs on k_band */
+
+/* query classes per row block: 0..3 = 1, 2, 4, 8 register words, 4 = any length, 5.. =
+ * the band classes (BAND_WORDS 32-bit words of band) */
+constexpr int NCLS = 13;
+constexpr int BAND_WORDS[8] = {1, 2, 3, 4, 6, 8, 12, 16};
+inline int band_class_index(int words)
+{
+    int i = 0;
+    while (i < 7 && BAND_WORDS[i] < words) ++i;
+    return i;
+}
+
+/* 32-bit words of the widest diagonal band any pair of a query of m units can need
+ * under the batch's chain (the bound K of plan_int, capped by the length filter
+ * |m - n| <= K over choice lengths up to maxlen), or 0 when that band is not narrower
+ * than the pattern (or wider than 512 bits).  For n <= m the bound is K(m) (the
+ * maximum is m); for n >= m, K grows by at most one per unit of n, so the pairs that
+ * pass form one run [m, n_last], found by binary search, and K(n_last) is the widest. */
+int band_words_for(const BatchSpec& spec, int64_t m, int64_t maxlen)
+{
+    if (m < 2) return 0;
+    const bool norm = spec.op == RFG_NORMALIZED_DISTANCE || spec.op == RFG_NORMALIZED_SIMILARITY;
+    if (norm && !(spec.cf >= 0.0 && spec.cf <= 1.0)) return 0;
+    PairSpec s;
+    s.metric = spec.metric;
+    s.op = spec.op;
+    s.form = spec.form;
+    s.ci = spec.ci;
+    s.cf = spec.cf;
+    s.p = spec.sp;
+    s.l1 = (u64)m;
+    auto bound = [&](int64_t n, bool* pass) -> int64_t {
+        s.l2 = (u64)n;
+        const Plan pl = plan_int(s);
+        if (!pl.run) {
+            *pass = false;
+            return -1;
+        }
+        *pass = pl.K >= (n > m ? n - m : m - n);
+        return pl.K;
+    };
+    bool pass = false;
+    int64_t Kmax = bound(m, &pass);
+    if (!pass) return 0;
+    if (maxlen > m) {
+        int64_t lo = m, hi = maxlen; /* lo passes; find the last passing n */
+        while (lo < hi) {
+            const int64_t mid = lo + (hi - lo + 1) / 2;
+            bool p;
+            bound(mid, &p);
+            if (p) lo = mid;
+            else hi = mid - 1;
+        }
+        bool p;
+        Kmax = std::max(Kmax, bound(lo, &p));
+    }
+    const int64_t band = 2 * Kmax + 1;
+    if (Kmax < 0 || band >= m || band > 512) return 0;
+    return (int)((band + 31) / 32);
+}
 int64_t g_fast_window = 512; /* choice positions per warp window of k_fast (autotuning) */
 
 /* A prepared batch: everything a launch needs is on the device, so enqueue() only
@@ -553,10 +624,23 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
     for (int64_t b = 0; b < R; ++b) pb->rows.emplace_back(b * rb, std::min(nq, (b + 1) * rb));
     const int64_t nblk = (int64_t)pb->rows.size();
 
-    /* classes: 1, 2, 4, 8 register words; index 4 = any length; one set per row block */
-    std::vector<std::vector<int32_t>> cls(nblk * 5);
-    std::vector<int64_t> cls_maxlen(nblk * 5, 0);
-    std::vector<int32_t> cls_wide(nblk * 5, 0);
+    /* the choices' lengths (for the band classes and the length order below) */
+    std::vector<int32_t> clen;
+    std::vector<int64_t> off_tmp;
+    int64_t host_max_choice_len = 0;
+    if (!spec.fixed_perm) {
+        RFG_TRY(choice_lengths(c, host_choice_off, &clen, &off_tmp));
+        for (int32_t l : clen) host_max_choice_len = std::max<int64_t>(host_max_choice_len, l);
+    }
+    /* classes: 1, 2, 4, 8 register words; index 4 = any length; 5.. = the band classes of
+     * unit-weight Levenshtein (BAND_WORDS[k - 5] 32-bit words); one set per row block */
+    const bool band_ok = g_band_mode != 0 && fam == FAM_LEV && spec.metric == RFG_LEVENSHTEIN && spec.sp.ins == 1 &&
+                         spec.sp.del == 1 && spec.sp.rep == 1 && spec.form != RFG_FORM_MULTI && spec.topk == 0 &&
+                         !spec.fixed_perm && c.width == 1;
+    std::vector<std::vector<int32_t>> cls(nblk * NCLS);
+    std::vector<int64_t> cls_maxlen(nblk * NCLS, 0);
+    std::vector<int32_t> cls_wide(nblk * NCLS, 0);
+    std::vector<int32_t> cls_distinct(nblk * NCLS, 0);
     for (int64_t b = 0; b < nblk; ++b)
         for (int64_t i = pb->rows[b].first; i < pb->rows[b].second; ++i) {
             int k;
@@ -565,10 +649,15 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
                 const int wc = word_class(q.len[i]);
                 k = wc == 1 ? 0 : wc == 2 ? 1 : wc == 4 ? 2 : wc == 8 ? 3 : 4;
             }
-            const int64_t bk = b * 5 + k;
+            if (band_ok && k > 0 && q.distinct[i] >= 0) {
+                const int bw = band_words_for(spec, q.len[i], host_max_choice_len);
+                if (bw > 0) k = 5 + band_class_index(bw);
+            }
+            const int64_t bk = b * NCLS + k;
             cls[bk].push_back((int32_t)i);
             cls_maxlen[bk] = std::max(cls_maxlen[bk], q.len[i]);
             cls_wide[bk] = std::max(cls_wide[bk], q.wide[i]);
+            cls_distinct[bk] = std::max(cls_distinct[bk], q.distinct[i]);
         }
     size_t total = 0;
     for (auto& v : cls) {
@@ -577,15 +666,14 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
     }
     std::vector<int32_t> qall;
     qall.reserve(total);
-    std::vector<size_t> cls_off(nblk * 5);
-    for (int64_t bk = 0; bk < nblk * 5; ++bk) {
+    std::vector<size_t> cls_off(nblk * NCLS);
+    for (int64_t bk = 0; bk < nblk * NCLS; ++bk) {
         cls_off[bk] = qall.size();
         qall.insert(qall.end(), cls[bk].begin(), cls[bk].end());
     }
 
     /* one chunking of the choices for every class, each chunk visited in length order */
     int64_t chunk;
-    int64_t host_max_choice_len = 0;
     int64_t stage = 0; /* staged window of the dense tiles (elements), 0 = direct stores */
     /* unit-weight distance: the chain is d <= K ? d : K + 1 (fast path of the tile kernels) */
     const bool fast_ok = spec.form != RFG_FORM_MULTI && spec.op == RFG_DISTANCE &&
@@ -610,7 +698,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
      * each sorted by length, through 16-byte records */
     bool fast_any = false;
     for (int64_t b = 0; b < nblk; ++b)
-        if (!cls[b * 5].empty() && (c.width == 1 || cls_wide[b * 5] == 0)) fast_any = true;
+        if (!cls[b * NCLS].empty() && (c.width == 1 || cls_wide[b * NCLS] == 0)) fast_any = true;
     fast_any = fast_any && fast_ok && spec.topk == 0 && !spec.fixed_perm && g_fast_mode != 0;
     const int64_t fwin = std::max<int64_t>(32, std::min<int64_t>(1024, g_fast_window / 8 * 8));
     std::vector<int32_t> frec;
@@ -632,11 +720,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             if (chunk > cap) chunk = (chunk + cap - 1) / cap * cap;
             stage = std::min(chunk, cap);
         }
-        std::vector<int32_t> clen;
-        std::vector<int64_t> off_tmp;
-        RFG_TRY(choice_lengths(c, host_choice_off, &clen, &off_tmp));
         const int64_t* hoff = host_choice_off ? host_choice_off : off_tmp.data();
-        for (int32_t l : clen) host_max_choice_len = std::max<int64_t>(host_max_choice_len, l);
         chunk_length_order(clen, stage ? stage : chunk, &perm);
         if (spec.topk == 0) {
             /* offsets and lengths in visiting order */
@@ -697,8 +781,8 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
 
     std::vector<size_t> generic_recs;
     size_t scratch_bytes = 0;
-    for (int64_t bk = 0; bk < nblk * 5; ++bk) {
-        const int k = (int)(bk % 5);
+    for (int64_t bk = 0; bk < nblk * NCLS; ++bk) {
+        const int k = (int)(bk % NCLS);
         if (cls[bk].empty()) continue;
         KParams a;
         memset(&a, 0, sizeof a);
@@ -731,6 +815,46 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         const int64_t nchunks_full = (nc + chunk - 1) / chunk;
         const bool small_class =
             k < 4 && !topk && (int64_t)cls[bk].size() * nchunks_full < (int64_t)g.sms * 8 && chunk > 256;
+        if (k >= 5) {
+            /* banded Levenshtein, one pair per thread, table and cutoffs per query in
+             * shared memory */
+            const int B = BAND_WORDS[k - 5];
+            const void* fb = band_kernel(c.width, B);
+            if (!fb) return fail(RFG_ERR_INVALID_ARGUMENT, "no band kernel for this code-unit width");
+            const int bblock = 256;
+            a.wmax = band_row_stride((int)cls_maxlen[bk], B);
+            a.scratch_per_thread = cls_distinct[bk] + 1; /* table rows: the units below 256, the zero row */
+            a.tab_t = (spec.op == RFG_NORMALIZED_DISTANCE || spec.op == RFG_NORMALIZED_SIMILARITY)
+                          ? (int)std::min<int64_t>(host_max_choice_len, 4095)
+                          : -1;
+            if (fast_ok) {
+                a.fast = 1;
+                a.fast_k = clamp_bound(spec.ci);
+            }
+            a.perm = dperm;
+            a.poff = pb->poff;
+            a.plen = pb->plen;
+            const int64_t nchunks_full = (nc + chunk - 1) / chunk;
+            const bool small = (int64_t)cls[bk].size() * nchunks_full < (int64_t)g.sms * 8 && chunk > 256;
+            a.stage = (stage && !small) ? stage : 0;
+            size_t bsm = band_smem_bytes(a.tab_t, (int)a.scratch_per_thread, a.wmax, a.stage, spec.out_dtype);
+            RFG_TRY(allow_dynamic_smem(fb, bsm));
+            const int64_t bslots = (int64_t)g.sms * std::max(1, occupancy(fb, bblock, bsm));
+            int64_t cchunk = chunk;
+            if (small) {
+                const int64_t want = bslots * 4;
+                int64_t cc = ((int64_t)cls[bk].size() * nc + want - 1) / want;
+                cc = std::max<int64_t>(cc, bblock);
+                cchunk = std::min(chunk, (cc + bblock - 1) / bblock * bblock);
+            }
+            a.chunk = cchunk;
+            a.nchunks = (nc + cchunk - 1) / cchunk;
+            const int64_t btiles = (int64_t)a.nq * a.nchunks;
+            if (btiles > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "batch too large for one launch");
+            pb->launches.push_back(
+                LaunchRec{fb, (unsigned)std::min<int64_t>(btiles, bslots), bblock, bsm, a, (int)(bk / NCLS)});
+            continue;
+        }
         const bool use_fast = k == 0 && fast_any && a.hcap == 0 && pb->prec;
         const bool use_mq = !use_fast && k == 0 && mq_ok && a.hcap == 0 && stage > 0 && !small_class;
         if (use_fast) {
@@ -760,12 +884,12 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
                 KParams h = a;
                 h.qlist = a.qlist + n0;
                 h.nq = (int32_t)(n1 - n0);
-                h.counter = pb->counters + (half ? nblk * 5 + bk / 5 : bk);
+                h.counter = pb->counters + (half ? nblk * NCLS + bk / NCLS : bk);
                 const int64_t tasks = (h.nq + Qf - 1) / Qf * h.nchunks;
                 if (tasks > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "batch too large for one launch");
                 const int64_t warps = std::max<int64_t>(1, std::min<int64_t>(tasks, fslots * RFG_FAST_WARPS));
                 pb->launches.push_back(
-                    LaunchRec{ff, (unsigned)((warps + RFG_FAST_WARPS - 1) / RFG_FAST_WARPS), fblock, fsm, h, (int)(bk / 5)});
+                    LaunchRec{ff, (unsigned)((warps + RFG_FAST_WARPS - 1) / RFG_FAST_WARPS), fblock, fsm, h, (int)(bk / NCLS)});
             }
             continue;
         }
@@ -918,19 +1042,19 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
                 KParams h = a;
                 h.qlist = a.qlist + nlong;
                 h.nq = (int32_t)nshort;
-                h.counter = pb->counters + nblk * 5 + bk / 5;
+                h.counter = pb->counters + nblk * NCLS + bk / NCLS;
                 const int64_t tiles_h = (nshort + qh - 1) / qh * a.nchunks;
                 pb->launches.push_back(
-                    LaunchRec{fh, (unsigned)std::min<int64_t>(tiles_h, slots_h), block, smem_h, h, (int)(bk / 5)});
+                    LaunchRec{fh, (unsigned)std::min<int64_t>(tiles_h, slots_h), block, smem_h, h, (int)(bk / NCLS)});
                 if (nlong == 0) continue;
                 a.nq = (int32_t)nlong;
                 const int64_t tiles_l = (nlong + mqq - 1) / mqq * a.nchunks;
                 pb->launches.push_back(
-                    LaunchRec{fn, (unsigned)std::min<int64_t>(tiles_l, slots), block, smem, a, (int)(bk / 5)});
+                    LaunchRec{fn, (unsigned)std::min<int64_t>(tiles_l, slots), block, smem, a, (int)(bk / NCLS)});
                 continue;
             }
         }
-        pb->launches.push_back(LaunchRec{fn, (unsigned)grid, block, smem, a, (int)(bk / 5)});
+        pb->launches.push_back(LaunchRec{fn, (unsigned)grid, block, smem, a, (int)(bk / NCLS)});
     }
     if (!generic_recs.empty()) {
         RFG_TRY(pb->scratch[0].alloc(scratch_bytes));
@@ -1112,7 +1236,7 @@ rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const 
         RFG_CUDA(cudaStreamSynchronize(g.stream));
         RFG_TRY(check_offsets(off.data(), nq, "queries")); /* before anything is read through them */
         std::vector<unsigned char> qh;
-        if (Q->char_width > 1 && nq) {
+        if (nq && off[nq] > off[0]) {
             qh.resize((size_t)off[nq] * Q->char_width);
             RFG_CUDA(cudaMemcpyAsync(qh.data(), Q->data, qh.size(), cudaMemcpyDeviceToHost, g.stream));
             RFG_CUDA(cudaStreamSynchronize(g.stream));
@@ -2474,7 +2598,7 @@ rfg_status rfg_batch_create(rfg_metric metric, rfg_op op, rfg_form form, const r
         if (cudaMemcpy(off.data(), Q->offsets, (nq + 1) * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
             st = fail(RFG_ERR_CUDA, "reading query offsets failed");
         if (st == RFG_OK) st = check_offsets(off.data(), nq, "queries"); /* before anything is read through them */
-        if (st == RFG_OK && Q->char_width > 1 && nq) {
+        if (st == RFG_OK && nq && off[nq] > off[0]) {
             qh.resize((size_t)off[nq] * Q->char_width);
             if (cudaMemcpy(qh.data(), Q->data, qh.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
                 st = fail(RFG_ERR_CUDA, "reading queries failed");

@@ -19,6 +19,9 @@ const void* tiles_mq_kernel_osa(int width, bool norm, bool half);
 const void* fast_kernel_lev(int width, bool half);
 const void* fast_kernel_lcs(int width, bool half);
 const void* fast_kernel_osa(int width, bool half);
+/* k_band<CT, B> (banded unit-weight Levenshtein, B 32-bit words of band in
+ * {1, 2, 3, 4, 6, 8, 12, 16}); one-byte choices only, nullptr otherwise */
+const void* band_kernel(int width, int B);
 /* queries per lane of k_fast */
 inline int fast_queries(int fam) { return fam == FAM_LCS ? 4 : 2; }
 /* k_tiles_mq_jaro<CT, Q> (Jaro / Jaro-Winkler, several queries per thread) */
