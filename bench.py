@@ -398,7 +398,7 @@ def main():
     serving = None
     if not args.no_serving and rank == 0:
         import bench_configs
-        serving = bench_configs.serving_leg(R, args.serving_duration)
+        serving = bench_configs.serving_capacity(R, args.serving_duration)
 
     if rank == 0:
         line = {"metric": METRIC_NAME, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,

@@ -350,7 +350,28 @@ def run(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
-def serving_leg(R, duration, rate=2000.0, corpus=10_000_000, max_inflight=4, max_batch=64, seed=33):
+def serving_corpora(R, corpus=10_000_000):
+    """the two device-resident corpora of config 5 and the seconds it took to build them"""
+    import workloads as WL
+    t0 = time.perf_counter()
+    dna = WL.dna_corpus_fast(seed=31, n=corpus)
+    tok = WL.tokens_u32_fast(seed=32, n=1_000_000)
+    corpora = [R.Corpus(dna), R.Corpus(tok)]
+    return corpora, time.perf_counter() - t0
+
+
+def serving_capacity(R, duration, rate=2000.0, corpus=10_000_000):
+    """config 5 at the offered rate, then at 80 % of the completed rate that run measured
+    (a load the server sustains without its queue growing): both legs' results"""
+    corpora, setup = serving_corpora(R, corpus)
+    over = serving_leg(R, duration, rate=rate, corpus=corpus, corpora=corpora)
+    over["setup_s"] = setup
+    sustained = serving_leg(R, duration, rate=0.8 * min(rate, over["completed_per_s"]), corpus=corpus,
+                            corpora=corpora, seed=34)
+    return {"at_offered_rate": over, "at_sustained_rate": sustained}
+
+
+def serving_leg(R, duration, rate=2000.0, corpus=10_000_000, max_inflight=4, max_batch=64, seed=33, corpora=None):
     """Config 5 in short: device-resident corpora of `corpus` DNA strings (len U[10,200]) and
     1,000,000 uint32 token strings; Poisson arrivals at `rate` req/s for `duration` s, each
     an extractOne (limit 1) or top-10 extract of one query of length U[5,500] with a metric
@@ -359,11 +380,9 @@ def serving_leg(R, duration, rate=2000.0, corpus=10_000_000, max_inflight=4, max
     and the same kinds of requests one at a time (rfg_extract)"""
     import threading
     import workloads as WL
-    t0 = time.perf_counter()
-    dna = WL.dna_corpus_fast(seed=31, n=corpus)
-    tok = WL.tokens_u32_fast(seed=32, n=1_000_000)
-    corpora = [R.Corpus(dna), R.Corpus(tok)]
-    t_setup = time.perf_counter() - t0
+    t_setup = 0.0
+    if corpora is None:
+        corpora, t_setup = serving_corpora(R, corpus)
     rng = np.random.default_rng(seed)
     acgt = np.frombuffer(b"ACGT", dtype=np.uint8)
     alpha = np.array(WL.TOKEN_ALPHABET + [0x20], dtype=np.uint32)
