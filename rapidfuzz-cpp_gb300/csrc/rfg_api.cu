@@ -520,6 +520,8 @@ struct Prepared {
     const int64_t* poff = nullptr;
     const int32_t* plen = nullptr;
     const int4* prec = nullptr; /* k_fast visiting records */
+    /* which kinds of launches the preparation holds (what the tuner has to sweep) */
+    bool has_fast = false, has_band = false, has_tiles = false;
     bool has_pre = false; /* pre.a / grid: the per-query table pass before the row blocks */
     KParams pre;
     int* counters = nullptr;
@@ -853,10 +855,12 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             if (btiles > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "batch too large for one launch");
             pb->launches.push_back(
                 LaunchRec{fb, (unsigned)std::min<int64_t>(btiles, bslots), bblock, bsm, a, (int)(bk / NCLS)});
+            pb->has_band = true;
             continue;
         }
         const bool use_fast = k == 0 && fast_any && a.hcap == 0 && pb->prec;
         const bool use_mq = !use_fast && k == 0 && mq_ok && a.hcap == 0 && stage > 0 && !small_class;
+        if (!use_fast) pb->has_tiles = true;
         if (use_fast) {
             /* warp tiles: one task = (Q queries, one window); queries of at most 32 units
              * (the tail of the longest-first class) in their own launch on 32-bit words */
@@ -891,6 +895,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
                 pb->launches.push_back(
                     LaunchRec{ff, (unsigned)((warps + RFG_FAST_WARPS - 1) / RFG_FAST_WARPS), fblock, fsm, h, (int)(bk / NCLS)});
             }
+            pb->has_fast = true;
             continue;
         }
         if (use_mq && fam == FAM_JARO) {
@@ -2539,19 +2544,31 @@ rfg_status rfg_editops(rfg_metric metric, const rfg_strings* S1, const rfg_strin
 
 /* --------------------------------------------------------- prepared batches */
 
-static rfg_status batch_reprepare(rfg_batch b, int block, int64_t tiles, int stage = 1)
+/* the launch-shape knobs of a preparation (what rfg_batch_tune chooses) */
+struct TuneChoice {
+    int block = 0;        /* tile kernels' block size (0: default) */
+    int64_t tiles = 0;    /* tile-count target (0: default) */
+    int stage = 1;        /* dense tiles stage results in shared memory */
+    int64_t window = 512; /* warp tiles: choice positions per window */
+    int band = 1;         /* band classes on (k_band) or off (the general kernels) */
+};
+
+static rfg_status batch_reprepare(rfg_batch b, const TuneChoice& c)
 {
-    const int ob = g_block_override;
-    const int64_t ot = g_tiles_target;
-    const int os = g_stage_mode;
-    g_block_override = block;
-    g_tiles_target = tiles;
-    g_stage_mode = stage;
+    const int ob = g_block_override, os = g_stage_mode, obd = g_band_mode;
+    const int64_t ot = g_tiles_target, ow = g_fast_window;
+    g_block_override = c.block;
+    g_tiles_target = c.tiles;
+    g_stage_mode = c.stage;
+    g_fast_window = c.window;
+    g_band_mode = c.band;
     Prepared* np = new Prepared();
     rfg_status st = prepare_batch(b->qs, b->ck, b->spec, np);
     g_block_override = ob;
     g_tiles_target = ot;
     g_stage_mode = os;
+    g_fast_window = ow;
+    g_band_mode = obd;
     if (st == RFG_OK && cudaStreamSynchronize(g.stream) != cudaSuccess) st = fail(RFG_ERR_CUDA, "prepare failed");
     if (st != RFG_OK) {
         delete np;
@@ -2563,9 +2580,20 @@ static rfg_status batch_reprepare(rfg_batch b, int block, int64_t tiles, int sta
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
     }
-    b->block = block;
-    b->tiles = tiles;
+    b->block = c.block;
+    b->tiles = c.tiles;
     return RFG_OK;
+}
+
+static rfg_status batch_reprepare_shape(rfg_batch b, int block, int64_t tiles, int stage = 1)
+{
+    TuneChoice c;
+    c.block = block;
+    c.tiles = tiles;
+    c.stage = stage;
+    c.window = g_fast_window;
+    c.band = g_band_mode;
+    return batch_reprepare(b, c);
 }
 
 rfg_status rfg_batch_create(rfg_metric metric, rfg_op op, rfg_form form, const rfg_strings* Q, const rfg_strings* C,
@@ -2621,7 +2649,7 @@ rfg_status rfg_batch_create(rfg_metric metric, rfg_op op, rfg_form form, const r
     b->spec.out_dtype = dt;
     b->spec.out = out;
     b->spec.ld = ld;
-    if (st == RFG_OK) st = batch_reprepare(b, 0, 0);
+    if (st == RFG_OK) st = batch_reprepare_shape(b, 0, 0);
     if (st != RFG_OK) {
         delete b;
         return st;
@@ -2661,47 +2689,102 @@ rfg_status rfg_batch_check(rfg_batch b, void* stream)
     return check_batch(*b->pb, stream ? (cudaStream_t)stream : g.stream);
 }
 
+/* tuned shapes, kept per (metric, op, form, output type, code-unit widths, and power-of-two
+ * buckets of the longest query, the query count and the choice count): a later batch of
+ * the same kind takes the stored choice without sweeping */
+typedef std::tuple<int, int, int, int, int, int, int, int, int> TuneKey;
+std::map<TuneKey, TuneChoice> g_tune_cache;
+
+static int log2_bucket(int64_t x)
+{
+    int b = 0;
+    while (x > 1) {
+        x >>= 1;
+        ++b;
+    }
+    return b;
+}
+
 rfg_status rfg_batch_tune(rfg_batch b, void* stream, int32_t* best_block, int64_t* best_tiles)
 {
     std::lock_guard<std::recursive_mutex> lk(g.mu);
     if (!b) return fail(RFG_ERR_INVALID_ARGUMENT, "batch is NULL");
     cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+    int64_t maxq = 0;
+    for (int64_t l : b->qs.len) maxq = std::max(maxq, l);
+    const TuneKey key{b->spec.metric, b->spec.op, b->spec.form, b->spec.out_dtype, b->qs.dev.width, b->ck.width,
+                      log2_bucket(maxq), log2_bucket(b->qs.dev.n), log2_bucket(b->ck.n)};
+    auto hit = g_tune_cache.find(key);
+    if (hit != g_tune_cache.end()) {
+        RFG_TRY(batch_reprepare(b, hit->second));
+        RFG_TRY(check_batch(*b->pb, st));
+        if (best_block) *best_block = hit->second.block;
+        if (best_tiles) *best_tiles = hit->second.tiles;
+        return RFG_OK;
+    }
     cudaEvent_t e0, e1;
     RFG_CUDA(cudaEventCreate(&e0));
     RFG_CUDA(cudaEventCreate(&e1));
-    float best = 1e30f;
-    int bb = 256, bs = 1;
-    int64_t bt = 0;
-    const int blocks[] = {128, 256};
-    const int mults[] = {2, 4, 8, 16, 32};
-    for (int stage = 1; stage >= 0; --stage)
-    for (int blk : blocks) {
-        for (int mu : mults) {
-            const int64_t tiles = (int64_t)g.sms * mu * (256 / blk) * 2;
-            RFG_TRY(batch_reprepare(b, blk, tiles, stage));
-            float times[3];
-            for (int r = 0; r < 3; ++r) {
-                RFG_CUDA(cudaEventRecord(e0, st));
-                RFG_TRY(enqueue_batch(*b->pb, st));
-                RFG_CUDA(cudaEventRecord(e1, st));
-                RFG_CUDA(cudaEventSynchronize(e1));
-                RFG_CUDA(cudaEventElapsedTime(&times[r], e0, e1));
-            }
-            std::sort(times, times + 3);
-            if (times[1] < best) {
-                best = times[1];
-                bb = blk;
-                bt = tiles;
-                bs = stage;
-            }
+    float best_t = 1e30f;
+    TuneChoice best;
+    best.window = g_fast_window;
+    best.band = g_band_mode;
+    auto trial = [&](const TuneChoice& c) -> rfg_status {
+        RFG_TRY(batch_reprepare(b, c));
+        float times[3];
+        for (int r = 0; r < 3; ++r) {
+            RFG_CUDA(cudaEventRecord(e0, st));
+            RFG_TRY(enqueue_batch(*b->pb, st));
+            RFG_CUDA(cudaEventRecord(e1, st));
+            RFG_CUDA(cudaEventSynchronize(e1));
+            RFG_CUDA(cudaEventElapsedTime(&times[r], e0, e1));
         }
+        std::sort(times, times + 3);
+        if (times[1] < best_t) {
+            best_t = times[1];
+            best = c;
+        }
+        return RFG_OK;
+    };
+    /* the default shape first; then the knobs of the launch kinds the batch holds, one
+     * at a time from the best so far: the band classes on or off (words per thread sized
+     * by the band, or by the pattern), the warp tiles' window, and the tile kernels'
+     * block size, tile count and staging */
+    RFG_TRY(trial(best));
+    const bool fast = b->pb->has_fast, band = b->pb->has_band;
+    if (band) {
+        TuneChoice c = best;
+        c.band = 0;
+        RFG_TRY(trial(c));
+    }
+    if (fast)
+        for (int64_t w : {256, 1024}) {
+            TuneChoice c = best;
+            c.window = w;
+            RFG_TRY(trial(c));
+        }
+    RFG_TRY(batch_reprepare(b, best));
+    if (b->pb->has_tiles) {
+        const TuneChoice base = best;
+        const int blocks[] = {128, 256};
+        const int mults[] = {2, 4, 8, 16, 32};
+        for (int stage = 1; stage >= 0; --stage)
+            for (int blk : blocks)
+                for (int mu : mults) {
+                    TuneChoice c = base;
+                    c.block = blk;
+                    c.tiles = (int64_t)g.sms * mu * (256 / blk) * 2;
+                    c.stage = stage;
+                    RFG_TRY(trial(c));
+                }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    RFG_TRY(batch_reprepare(b, bb, bt, bs));
+    RFG_TRY(batch_reprepare(b, best));
     RFG_TRY(check_batch(*b->pb, st));
-    if (best_block) *best_block = bb;
-    if (best_tiles) *best_tiles = bt;
+    g_tune_cache[key] = best;
+    if (best_block) *best_block = best.block;
+    if (best_tiles) *best_tiles = best.tiles;
     return RFG_OK;
 }
 
