@@ -448,7 +448,7 @@ inline int band_class_index(int words)
     return i;
 }
 
-/* 32-bit words of the widest diagonal band any pair of a query of m units can need
+/* 32-bit words of the widest (Ukkonen) band any pair of a query of m units can need
  * under the batch's chain (the bound K of plan_int, capped by the length filter
  * |m - n| <= K over choice lengths up to maxlen), or 0 when that band is not narrower
  * than the pattern (or wider than 512 bits).  For n <= m the bound is K(m) (the
@@ -492,7 +492,8 @@ int band_words_for(const BatchSpec& spec, int64_t m, int64_t maxlen)
         bool p;
         Kmax = std::max(Kmax, bound(lo, &p));
     }
-    const int64_t band = 2 * Kmax + 1;
+    /* Ukkonen's band of a pair with bound K spans at most K + 2 diagonals */
+    const int64_t band = Kmax + 2;
     if (Kmax < 0 || band >= m || band > 512) return 0;
     return (int)((band + 31) / 32);
 }

@@ -2,17 +2,18 @@
  * rfg_band.cuh -- banded Levenshtein (weights 1/1/1) for queries whose every passing pair
  * needs a diagonal band narrower than the pattern: the reference's
  * levenshtein_hyrroe2003_small_band / the band of levenshtein_hyrroe2003_block
- * (Levenshtein_impl.hpp:419-505, 641-850), chosen when 2K+1 < m for the largest bound K
- * any pair of the query can reach (the length filter Levenshtein_impl.hpp:863 caps it).
+ * (Levenshtein_impl.hpp:419-505, 641-850), on Ukkonen's band of about K + 2 diagonals
+ * (lev_band32), chosen when that band is narrower than the pattern for the largest bound
+ * K any pair of the query can reach (the length filter Levenshtein_impl.hpp:863 caps it).
  *
  * A CTA takes (query, chunk of choices) tiles from the launch's counter, like the tile
  * kernel, and scores one pair per thread with lev_band32<B> on B 32-bit words; the
  * kernel's registers are sized by the band, not by the pattern's length.  Per query the
  * CTA builds in shared memory
  *   - a compact pattern table: one row of ceil(m/32) 32-bit words for each code unit
- *     the query holds (plus the all-zero row), each row with B + 1 zero words on either
- *     side so the band's window is loaded without range tests, and rmap[c] = the word
- *     offset of unit c's row;
+ *     the query holds (plus the all-zero row), each row with zero words on either side
+ *     so the band's window is loaded without range tests, and rmap[c] = the word offset
+ *     of unit c's row;
  *   - for the normalized ops, the integer cutoff chain_kd of every choice length up to
  *     tab_t (32-bit; 0xffffffff: none), so no pair evaluates the double-precision chain
  *     to find its bound.
@@ -24,8 +25,10 @@
 
 namespace rfg {
 
-/* words of one compact row for a class of queries of at most m units and band B */
-__host__ __device__ inline int band_row_stride(int m, int B) { return (m + 31) / 32 + 2 * (B + 1); }
+/* words of one compact row for a class of queries of at most m units and band B: the
+ * pattern's words, B + 1 zero words before and 2B + 2 after (the window of a pair with
+ * n up to m + K reads that far past the pattern's last word) */
+__host__ __device__ inline int band_row_stride(int m, int B) { return (m + 31) / 32 + 3 * (B + 1); }
 
 struct BandRows {
     const u32* base;
@@ -161,7 +164,7 @@ __global__ void __launch_bounds__(256, B <= 4 ? 4 : B <= 8 ? 2 : 1) k_band(const
                     if (m == 0) raw = n;
                     else if (K < diff) raw = K + 1;
                     else if (n == 0) raw = m;
-                    else if (2 * K + 1 > 32 * B || K >= m) { /* outside the class the host computed */
+                    else if (K >= m || band_bits((int)K, m - n) > 32 * B) { /* outside the class the host computed */
                         atomicExch(a.err, 6);
                         raw = K + 1;
                     }

@@ -948,28 +948,41 @@ RFG_HD u32 funnel32(u32 lo, u32 hi, int sh)
 #endif
 }
 
-/* The banded Levenshtein of lev_band over B 32-bit words (a window of 32*B bits), for
- * a pattern table of 32-bit words: pm(c) gives the row of text unit c as a pointer to
- * its words, with at least B + 1 zero words before word 0 and B + 1 after the last, so
- * the window's words are loaded without range tests.  Window bit b of step j is pattern
- * index K+1-32B+j+b; extracting it takes one funnel shift per word (the GPU's native
- * width), and the carry of (X & VP) + VP runs through the words.  Requires
- * 2K+1 <= 32*B, |m-n| <= K < m, n > 0.  Same result as lev_band (levenshtein_hyrroe2003
- * _small_band, Levenshtein_impl.hpp:419-505): d, or K + 1 once the diagonal lower bound
- * passes K (checked every 8 text units). */
+/* Ukkonen's band of a pair (m, n) with bound K: a path of cost <= K to (m, n) only visits
+ * diagonals d = i - j with |d| + |(m - n) - d| <= K (it needs |d| indels to reach d and
+ * |(m - n) - d| to leave it), i.e. d in [band_lo, band_hi] =
+ * [-ceil((K - (m-n)) / 2), ceil((K + (m-n)) / 2)]: at most K + 2 diagonals, about half of
+ * the 2K + 1 of the symmetric band.  |m - n| <= K. */
+RFG_HD int band_lo(int K, int delta) { return -((K - delta + 1) >> 1); }
+RFG_HD int band_hi(int K, int delta) { return (K + delta + 1) >> 1; }
+RFG_HD int band_bits(int K, int delta) { return band_hi(K, delta) - band_lo(K, delta) + 1; }
+
+/* Banded Levenshtein on B 32-bit words (a window of 32*B bits) over a pattern table of
+ * 32-bit words: pm(c) gives the row of text unit c as a pointer to its words, with at
+ * least B + 1 zero words before word 0 and 2B + 2 after the last, so the window's words
+ * are loaded without range tests.  Window bit b covers diagonal dlo + b (pattern index
+ * dlo + j + b at step j); dlo = band_lo(K, m - n) and band_bits(K, m - n) <= 32*B.
+ * Extracting the window takes one funnel shift per word (the GPU's native width); the
+ * carry of (X & VP) + VP runs through the words; the frame moves down one row per text
+ * unit (D0 >> 1), as in levenshtein_hyrroe2003_small_band (Levenshtein_impl.hpp:419-505).
+ * The band computes the distance over paths inside it -- exact for every pair whose
+ * distance is at most K, since those paths never leave Ukkonen's band -- and the lower
+ * bound on the diagonal through (m, n) stops it every 8 text units once it passes K.
+ * Requires |m-n| <= K < m, n > 0.  Returns d, or any value > K. */
 template <int B, typename PM32, typename TXT>
 RFG_HD i64 lev_band32(const PM32& pm, int m, const TXT& t, int n, int K)
 {
     const int NB = 32 * B;
+    const int dlo = band_lo(K, m - n);
     u32 VP[B], VN[B], rmask[B];
 #pragma unroll
     for (int b = 0; b < B; ++b) {
-        VP[b] = range_mask32(NB - 1 - K - 32 * b, NB - 1 - 32 * b);
+        VP[b] = range_mask32(-dlo - 32 * b, NB - 1 - 32 * b); /* rows 1.. of column 0: delta +1 */
         VN[b] = 0;
-        rmask[b] = range_mask32(NB - 1 - K + (m - n) - 32 * b, NB - 2 - 32 * b);
+        rmask[b] = range_mask32((m - n) - dlo - 32 * b, NB - 2 - 32 * b);
     }
-    int diag = K;
-    int start = K + 1 - NB; /* pattern index of window bit 0 */
+    int diag = dlo + NB - 1; /* D on the window's bottom diagonal, column 0 */
+    int start = dlo;         /* pattern index of window bit 0 */
     for (int j = 0; j < n; ++j, ++start) {
         const u32* row = pm(t[j]);
         const int w0 = start >> 5; /* floor division (arithmetic shift) */

@@ -167,8 +167,8 @@ struct PM32 {
 
 int64_t hc_band32(int B, const uint8_t* a, int m, const uint8_t* b, int n, int64_t K)
 {
-    if (m == 0 || n == 0 || K >= m || 2 * K + 1 > 32 * B || (m > n ? m - n : n - m) > K) return -2;
-    const int W32 = (m + 31) / 32, pad = B + 1, S = W32 + 2 * pad;
+    if (m == 0 || n == 0 || K >= m || (m > n ? m - n : n - m) > K || band_bits((int)K, m - n) > 32 * B) return -2;
+    const int W32 = (m + 31) / 32, pad = B + 1, S = W32 + 3 * pad;
     std::vector<int32_t> rmap(256, 0);
     int R = 1; /* row 0: the zero row */
     for (int k = 0; k < m; ++k)

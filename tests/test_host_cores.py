@@ -145,8 +145,8 @@ def test_warp_tile_core_matches_oracle(libs, fam, word32):
 
 
 def test_band32_core_matches_oracle(libs):
-    """lev_band32<B>: the 32-bit banded Levenshtein of the band kernel, every window size,
-    against the exact distance with the distance chain"""
+    """lev_band32<B>: the 32-bit banded Levenshtein of the band kernel on Ukkonen's band
+    (about K + 2 diagonals), every window size, against the exact distance"""
     lib, o = libs
     rng = np.random.default_rng(77)
     lens = [40, 63, 64, 65, 100, 127, 128, 129, 200, 300, 513, 700]
@@ -154,7 +154,8 @@ def test_band32_core_matches_oracle(libs):
     for a, b in pairs(78, 700, lens):
         d = exact(o, 0, a, b)
         for B in (1, 2, 4, 8, 16):
-            for K in sorted({int(rng.integers(0, 16 * B)), 16 * B - 1, max(0, d - 1), d, d + 1, abs(len(a) - len(b))}):
+            for K in sorted({int(rng.integers(0, 32 * B)), 32 * B - 2, 32 * B - 1, max(0, d - 1), d, d + 1,
+                             abs(len(a) - len(b))}):
                 got = lib.hc_band32(B, a, len(a), b, len(b), K)
                 if got == -2:
                     continue
