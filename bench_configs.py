@@ -69,6 +69,21 @@ def _dev(torch, batch, dev):
     return (td.data_ptr(), to.data_ptr(), w, o.size - 1), (td, to)
 
 
+def band_steps(q, c, op, ci, cf):
+    """word steps of the band kernels on one-byte strings (librfg_count.so)"""
+    import ctypes
+    lib = ctypes.CDLL(os.path.join(B.ROOT, "rapidfuzz-cpp_gb300", "lib", "librfg_count.so"))
+    vp, u64p = ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)
+    lib.rfg_count_band_steps.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_double, vp, vp, ctypes.c_int64, vp,
+                                         vp, ctypes.c_int64, ctypes.c_int, u64p, u64p, u64p]
+    e, a, p = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+    rc = lib.rfg_count_band_steps(op, ci, cf, q[0].ctypes.data, q[1].ctypes.data, len(q[1]) - 1, c[0].ctypes.data,
+                                  c[1].ctypes.data, len(c[1]) - 1, 0, ctypes.byref(e), ctypes.byref(a), ctypes.byref(p))
+    if rc != 0:
+        raise RuntimeError("band step count failed")
+    return {"exec_words": float(e.value), "alg_words": float(a.value), "pairs": int(p.value)}
+
+
 def _cells(q, c):
     ql = np.diff(q[1]).astype(np.float64)
     cl = np.diff(c[1]).astype(np.float64)
@@ -160,13 +175,24 @@ def run(args, rank, world, local):
         qsub = (q[0][:q[1][sub]], q[1][:sub + 1].copy(), 1)
         oracle_cdist(R.LEVENSHTEIN, R.NORMALIZED_DISTANCE, qsub, c, 0.1)
         tc = time.perf_counter() - tc0
+        # roofline of the band kernels: the 32-bit word steps Ukkonen's band of every pair
+        # needs (counted on the host by the same core), 13 INT32 operations each (the
+        # 32-bit-word form of the Levenshtein step: Levenshtein_impl.hpp:285-302)
+        band = band_steps(q, c, 2, 0, 0.1)
+        peak = B.int_peak_ops()
+        ach = band["alg_words"] * 13 / (t / steps)
+        roofline = {"bound": "int32", "achieved": ach / 1e12, "peak": peak / 1e12, "unit": "Tops/s",
+                    "frac": ach / peak, "traffic": None, "kernel": ";".join(b.kernels()),
+                    "peak_source": "measured: LOP3/IADD3/SHF issue-rate microbenchmark (librfg_peak.so)",
+                    "ops_per_word_step_32": 13, "band_pairs": band["pairs"],
+                    "alg_word_steps_32": band["alg_words"], "exec_word_steps_32": band["exec_words"]}
         line.update({"value": cells * steps / t / 1e9, "ms_per_step": t / steps * 1e3, "dtype": "u64",
                      "config": {"workload": "dna256x65536: Levenshtein normalized_distance cutoff 0.1, 256 x 65,536 DNA "
                                             "lognormal(300,0.6) in [100,2000], half mutated 1-15%",
                                 "pairs_per_s": nq * nc * steps / t, "kernels": b.kernels()},
                      "cpu_baseline": {"value": _cells(qsub, c) / tc / 1e9, "unit": "GCUPS", "cores": os.cpu_count(),
                                       "kind": "port", "sample": "16 of the 256 queries x all 65,536 choices"},
-                     "e2e": None, "gpu_launches": steps, "clocks": clk})
+                     "roofline": roofline, "e2e": None, "gpu_launches": steps * len(b.kernels()), "clocks": clk})
     elif args.workload == "serving":
         return run_serving(args, R, WL)
     elif args.workload == "tokens":

@@ -243,7 +243,11 @@ struct QuerySet {
     std::vector<int32_t> distinct;
 };
 
-rfg_status query_info_from_host(const void* data, const int64_t* off, int64_t n, int width, QuerySet* qs)
+/* lengths and wide-unit counts of a host batch; with want_distinct, the distinct units
+ * below 256 of every query longer than 64 units (the band-class candidates of
+ * Levenshtein) */
+rfg_status query_info_from_host(const void* data, const int64_t* off, int64_t n, int width, QuerySet* qs,
+                                bool want_distinct = false)
 {
     qs->len.resize(n);
     qs->wide.assign(n, 0);
@@ -254,6 +258,8 @@ rfg_status query_info_from_host(const void* data, const int64_t* off, int64_t n,
         if (b - a > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "strings longer than 2^31-1 code units");
         qs->len[i] = b - a;
         if (!data && b > a) continue;
+        const bool dist = want_distinct && b - a > 64;
+        if (width == 1 && !dist) continue;
         u64 seen[4] = {0, 0, 0, 0};
         int32_t w = 0;
         for (int64_t k = a; k < b; ++k) {
@@ -262,9 +268,17 @@ rfg_status query_info_from_host(const void* data, const int64_t* off, int64_t n,
             else seen[c >> 6] |= 1ull << (c & 63);
         }
         qs->wide[i] = width > 1 ? w : 0;
-        qs->distinct[i] = popc64(seen[0]) + popc64(seen[1]) + popc64(seen[2]) + popc64(seen[3]);
+        if (dist) qs->distinct[i] = popc64(seen[0]) + popc64(seen[1]) + popc64(seen[2]) + popc64(seen[3]);
     }
     return RFG_OK;
+}
+
+/* some query is longer than 64 units (a band-class candidate) */
+inline bool has_long_query(const int64_t* off, int64_t n)
+{
+    for (int64_t i = 0; i < n; ++i)
+        if (off[i + 1] - off[i] > 64) return true;
+    return false;
 }
 
 /* copy a host batch to the device (data padded to 16 bytes) */
@@ -436,68 +450,18 @@ int g_half_mode = 1;        /* queries of <= 32 units run on 32-bit recurrence w
 int g_block_override = 0;   /* override of the tile kernels' block size (autotuning) */
 int g_fast_mode = 1;        /* unit-weight one-word distances run on the warp tiles (k_fast) */
 int g_band_mode = 1;        /* unit-weight Levenshtein with a band narrower than the pattern runs on k_band */
+int64_t g_fast_window = 512; /* choice positions per warp window of k_fast (autotuning) */
 
 /* query classes per row block: 0..3 = 1, 2, 4, 8 register words, 4 = any length, 5.. =
- * the band classes (BAND_WORDS 32-bit words of band) */
-constexpr int NCLS = 13;
-constexpr int BAND_WORDS[8] = {1, 2, 3, 4, 6, 8, 12, 16};
-inline int band_class_index(int words)
-{
-    int i = 0;
-    while (i < 7 && BAND_WORDS[i] < words) ++i;
-    return i;
-}
+ * the band classes (band_class_words(k - 5) 32-bit words of band, rfg_core.cuh) */
+constexpr int NCLS = 5 + BAND_CLASSES;
 
-/* 32-bit words of the widest (Ukkonen) band any pair of a query of m units can need
- * under the batch's chain (the bound K of plan_int, capped by the length filter
- * |m - n| <= K over choice lengths up to maxlen), or 0 when that band is not narrower
- * than the pattern (or wider than 512 bits).  For n <= m the bound is K(m) (the
- * maximum is m); for n >= m, K grows by at most one per unit of n, so the pairs that
- * pass form one run [m, n_last], found by binary search, and K(n_last) is the widest. */
-int band_words_for(const BatchSpec& spec, int64_t m, int64_t maxlen)
+/* the band class of a query of m units (band_class_words index), or -1 (band_class in
+ * rfg_core.cuh, shared with the host work counter) */
+int band_class_of(const BatchSpec& spec, int64_t m, int64_t maxlen)
 {
-    if (m < 2) return 0;
-    const bool norm = spec.op == RFG_NORMALIZED_DISTANCE || spec.op == RFG_NORMALIZED_SIMILARITY;
-    if (norm && !(spec.cf >= 0.0 && spec.cf <= 1.0)) return 0;
-    PairSpec s;
-    s.metric = spec.metric;
-    s.op = spec.op;
-    s.form = spec.form;
-    s.ci = spec.ci;
-    s.cf = spec.cf;
-    s.p = spec.sp;
-    s.l1 = (u64)m;
-    auto bound = [&](int64_t n, bool* pass) -> int64_t {
-        s.l2 = (u64)n;
-        const Plan pl = plan_int(s);
-        if (!pl.run) {
-            *pass = false;
-            return -1;
-        }
-        *pass = pl.K >= (n > m ? n - m : m - n);
-        return pl.K;
-    };
-    bool pass = false;
-    int64_t Kmax = bound(m, &pass);
-    if (!pass) return 0;
-    if (maxlen > m) {
-        int64_t lo = m, hi = maxlen; /* lo passes; find the last passing n */
-        while (lo < hi) {
-            const int64_t mid = lo + (hi - lo + 1) / 2;
-            bool p;
-            bound(mid, &p);
-            if (p) lo = mid;
-            else hi = mid - 1;
-        }
-        bool p;
-        Kmax = std::max(Kmax, bound(lo, &p));
-    }
-    /* Ukkonen's band of a pair with bound K spans at most K + 2 diagonals */
-    const int64_t band = Kmax + 2;
-    if (Kmax < 0 || band >= m || band > 512) return 0;
-    return (int)((band + 31) / 32);
+    return band_class(spec.metric, spec.op, spec.form, spec.sp, spec.ci, spec.cf, m, maxlen);
 }
-int64_t g_fast_window = 512; /* choice positions per warp window of k_fast (autotuning) */
 
 /* A prepared batch: everything a launch needs is on the device, so enqueue() only
  * resets the tile counters and launches the kernels (no host work, no allocation,
@@ -636,7 +600,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         for (int32_t l : clen) host_max_choice_len = std::max<int64_t>(host_max_choice_len, l);
     }
     /* classes: 1, 2, 4, 8 register words; index 4 = any length; 5.. = the band classes of
-     * unit-weight Levenshtein (BAND_WORDS[k - 5] 32-bit words); one set per row block */
+     * unit-weight Levenshtein (band_class_words(k - 5) 32-bit words); one set per row block */
     const bool band_ok = g_band_mode != 0 && fam == FAM_LEV && spec.metric == RFG_LEVENSHTEIN && spec.sp.ins == 1 &&
                          spec.sp.del == 1 && spec.sp.rep == 1 && spec.form != RFG_FORM_MULTI && spec.topk == 0 &&
                          !spec.fixed_perm && c.width == 1;
@@ -653,8 +617,8 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
                 k = wc == 1 ? 0 : wc == 2 ? 1 : wc == 4 ? 2 : wc == 8 ? 3 : 4;
             }
             if (band_ok && k > 0 && q.distinct[i] >= 0) {
-                const int bw = band_words_for(spec, q.len[i], host_max_choice_len);
-                if (bw > 0) k = 5 + band_class_index(bw);
+                const int bc = band_class_of(spec, q.len[i], host_max_choice_len);
+                if (bc >= 0) k = 5 + bc;
             }
             const int64_t bk = b * NCLS + k;
             cls[bk].push_back((int32_t)i);
@@ -821,7 +785,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         if (k >= 5) {
             /* banded Levenshtein, one pair per thread, table and cutoffs per query in
              * shared memory */
-            const int B = BAND_WORDS[k - 5];
+            const int B = band_class_words(k - 5);
             const void* fb = band_kernel(c.width, B);
             if (!fb) return fail(RFG_ERR_INVALID_ARGUMENT, "no band kernel for this code-unit width");
             const int bblock = 256;
@@ -1241,20 +1205,21 @@ rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const 
         RFG_CUDA(cudaMemcpyAsync(off.data(), Q->offsets, (nq + 1) * 8, cudaMemcpyDeviceToHost, g.stream));
         RFG_CUDA(cudaStreamSynchronize(g.stream));
         RFG_TRY(check_offsets(off.data(), nq, "queries")); /* before anything is read through them */
+        const bool want = metric == RFG_LEVENSHTEIN && has_long_query(off.data(), nq);
         std::vector<unsigned char> qh;
-        if (nq && off[nq] > off[0]) {
+        if ((Q->char_width > 1 || want) && nq && off[nq] > off[0]) {
             qh.resize((size_t)off[nq] * Q->char_width);
             RFG_CUDA(cudaMemcpyAsync(qh.data(), Q->data, qh.size(), cudaMemcpyDeviceToHost, g.stream));
             RFG_CUDA(cudaStreamSynchronize(g.stream));
         }
-        RFG_TRY(query_info_from_host(qh.data(), off.data(), nq, Q->char_width, &qs));
+        RFG_TRY(query_info_from_host(qh.data(), off.data(), nq, Q->char_width, &qs, want));
         qs.dev = KStrings{(const unsigned char*)Q->data, Q->offsets, nq, Q->char_width};
         ck = KStrings{(const unsigned char*)C->data, C->offsets, nc, C->char_width};
     }
     else {
         if ((!Q->data && nq && Q->offsets[nq]) || (!C->data && nc && C->offsets[nc]))
             return fail(RFG_ERR_INVALID_ARGUMENT, "string data is NULL");
-        RFG_TRY(query_info_from_host(Q->data, Q->offsets, nq, Q->char_width, &qs));
+        RFG_TRY(query_info_from_host(Q->data, Q->offsets, nq, Q->char_width, &qs, metric == RFG_LEVENSHTEIN));
         for (int64_t i = 0; i < nc; ++i)
             if (C->offsets[i] < 0 || C->offsets[i + 1] < C->offsets[i] || C->offsets[i + 1] - C->offsets[i] > INT32_MAX)
                 return fail(RFG_ERR_INVALID_ARGUMENT, "choice offsets must be non-decreasing and >= 0");
@@ -1809,7 +1774,7 @@ rfg_status rfg_cached_create(rfg_metric metric, const void* s1, int64_t len1, in
     }
     int64_t off[2] = {0, len1};
     rfg_strings q{h->host.data(), off, 1, width1};
-    rfg_status st = query_info_from_host(h->host.data(), off, 1, width1, &h->qs);
+    rfg_status st = query_info_from_host(h->host.data(), off, 1, width1, &h->qs, metric == RFG_LEVENSHTEIN);
     if (st == RFG_OK) st = upload_strings(&q, &h->data, &h->off, &h->qs.dev);
     if (st == RFG_OK && cudaStreamSynchronize(g.stream) != cudaSuccess) st = fail(RFG_ERR_CUDA, "upload failed");
     if (st != RFG_OK) {
@@ -2627,17 +2592,18 @@ rfg_status rfg_batch_create(rfg_metric metric, rfg_op op, rfg_form form, const r
         if (cudaMemcpy(off.data(), Q->offsets, (nq + 1) * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
             st = fail(RFG_ERR_CUDA, "reading query offsets failed");
         if (st == RFG_OK) st = check_offsets(off.data(), nq, "queries"); /* before anything is read through them */
-        if (st == RFG_OK && nq && off[nq] > off[0]) {
+        const bool want = metric == RFG_LEVENSHTEIN && st == RFG_OK && has_long_query(off.data(), nq);
+        if (st == RFG_OK && (Q->char_width > 1 || want) && nq && off[nq] > off[0]) {
             qh.resize((size_t)off[nq] * Q->char_width);
             if (cudaMemcpy(qh.data(), Q->data, qh.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
                 st = fail(RFG_ERR_CUDA, "reading queries failed");
         }
-        if (st == RFG_OK) st = query_info_from_host(qh.data(), off.data(), nq, Q->char_width, &b->qs);
+        if (st == RFG_OK) st = query_info_from_host(qh.data(), off.data(), nq, Q->char_width, &b->qs, want);
         b->qs.dev = KStrings{(const unsigned char*)Q->data, Q->offsets, nq, Q->char_width};
         b->ck = KStrings{(const unsigned char*)C->data, C->offsets, nc, C->char_width};
     }
     else {
-        st = query_info_from_host(Q->data, Q->offsets, nq, Q->char_width, &b->qs);
+        st = query_info_from_host(Q->data, Q->offsets, nq, Q->char_width, &b->qs, metric == RFG_LEVENSHTEIN);
         if (st == RFG_OK) st = upload_strings(Q, &b->qd, &b->qo, &b->qs.dev);
         if (st == RFG_OK) st = upload_strings(C, &b->cd, &b->co, &b->ck);
     }
@@ -2765,7 +2731,7 @@ rfg_status rfg_batch_tune(rfg_batch b, void* stream, int32_t* best_block, int64_
             RFG_TRY(trial(c));
         }
     RFG_TRY(batch_reprepare(b, best));
-    if (b->pb->has_tiles) {
+    if (b->pb->has_tiles || b->pb->has_band) { /* chunk size and staging shape the band launches too */
         const TuneChoice base = best;
         const int blocks[] = {128, 256};
         const int mults[] = {2, 4, 8, 16, 32};

@@ -1915,6 +1915,68 @@ RFG_HD void finish_int(const PairSpec& s, const Plan& pl, i64 raw, i64* oi, doub
 }
 
 /* Jaro families.  prefix: common prefix (<= 4) of the two strings. */
+/* The band classes of the band kernel: 32-bit words of window, and the class of a query
+ * of m units under a unit-weight Levenshtein chain: the widest Ukkonen band (K + 2
+ * diagonals) any pair with a choice of length up to maxlen can need, rounded up to a
+ * class, or -1 when that band is not narrower than the pattern (or wider than 512 bits).
+ * K comes from plan_int; for n <= m it is K(m) (the maximum is m), and for n >= m it
+ * grows by at most one per unit of n (cutoffs in [0, 1] for the normalized ops), so the
+ * choices that pass the length filter |m - n| <= K form one run [.., n_last], found by
+ * binary search, and K(n_last) is the widest. */
+#define BAND_CLASSES 8
+RFG_HD int band_class_words(int i)
+{
+    const int w[BAND_CLASSES] = {1, 2, 3, 4, 6, 8, 12, 16};
+    return w[i];
+}
+
+RFG_HD int band_class(int metric, int op, int form, const ScoreParams& sp, u64 ci, double cf, i64 m, i64 maxlen)
+{
+    if (m < 2 || metric != LEVENSHTEIN || sp.ins != 1 || sp.del != 1 || sp.rep != 1 || form == FORM_MULTI) return -1;
+    if ((op == NORM_DISTANCE || op == NORM_SIMILARITY) && !(cf >= 0.0 && cf <= 1.0)) return -1;
+    PairSpec s;
+    s.metric = metric;
+    s.op = op;
+    s.form = form;
+    s.ci = ci;
+    s.cf = cf;
+    s.p = sp;
+    s.l1 = (u64)m;
+    s.kd_pre = ~0ull;
+    auto bound = [&](i64 n, bool* pass) -> i64 {
+        s.l2 = (u64)n;
+        const Plan pl = plan_int(s);
+        if (!pl.run) {
+            *pass = false;
+            return -1;
+        }
+        *pass = pl.K >= (n > m ? n - m : m - n);
+        return pl.K;
+    };
+    bool pass = false;
+    i64 Kmax = bound(m, &pass);
+    if (!pass) return -1;
+    if (maxlen > m) {
+        i64 lo = m, hi = maxlen; /* lo passes; find the last passing n */
+        while (lo < hi) {
+            const i64 mid = lo + (hi - lo + 1) / 2;
+            bool p;
+            bound(mid, &p);
+            if (p) lo = mid;
+            else hi = mid - 1;
+        }
+        bool p;
+        const i64 k2 = bound(lo, &p);
+        if (k2 > Kmax) Kmax = k2;
+    }
+    const i64 bits = Kmax + 2;
+    if (Kmax < 0 || bits >= m || bits > 512) return -1;
+    const int words = (int)((bits + 31) / 32);
+    for (int i = 0; i < BAND_CLASSES; ++i)
+        if (band_class_words(i) >= words) return i;
+    return -1;
+}
+
 RFG_HD double jaro_cutoff_for(const PairSpec& s, i64 prefix)
 {
     if (s.form == FORM_MULTI) return 0.0; /* Multi: counts are always read */

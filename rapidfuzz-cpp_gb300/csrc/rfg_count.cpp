@@ -110,4 +110,91 @@ int rfg_count_word_steps2(int metric, const uint8_t* qd, const int64_t* qo, int6
     return 0;
 }
 
+/* Band classes of unit-weight Levenshtein (the band kernel, lev_band32) on one-byte
+ * strings under the chain of `op` (rfg_op numbering) with the cutoff ci / cf: for every
+ * pair of a band-class query that passes the length filter, the text units the core
+ * fetches (steps) times the class's window words (*exec_words, what the kernel runs) and
+ * times the words Ukkonen's band of the pair needs (*alg_words); *pairs counts those
+ * pairs.  Queries outside the band classes are not counted. */
+int rfg_count_band_steps(int op, uint64_t ci, double cf, const uint8_t* qd, const int64_t* qo, int64_t nq,
+                         const uint8_t* cd, const int64_t* co, int64_t nc, int nthreads, uint64_t* exec_words,
+                         uint64_t* alg_words, uint64_t* pairs)
+{
+    if (!exec_words || !alg_words || !pairs) return -1;
+    int64_t maxlen = 0;
+    for (int64_t c = 0; c < nc; ++c) maxlen = std::max<int64_t>(maxlen, co[c + 1] - co[c]);
+    if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+    ScoreParams sp;
+    sp.ins = sp.del = sp.rep = 1;
+    sp.prefix_weight = 0.1;
+    std::atomic<int64_t> next(0);
+    std::vector<uint64_t> pe(nthreads, 0), pa(nthreads, 0), pp(nthreads, 0);
+    std::vector<std::thread> th;
+    for (int w = 0; w < nthreads; ++w)
+        th.emplace_back([&, w]() {
+            for (;;) {
+                const int64_t qi = next.fetch_add(1);
+                if (qi >= nq) break;
+                const int m = (int)(qo[qi + 1] - qo[qi]);
+                const int bc = band_class(LEVENSHTEIN, op, FORM_CACHED, sp, ci, cf, m, maxlen);
+                if (bc < 0) continue;
+                const int B = band_class_words(bc);
+                const uint8_t* a = qd + qo[qi];
+                const int W32 = (m + 31) / 32, pad = B + 1, S = W32 + 3 * pad;
+                std::vector<int32_t> rmap(256, 0);
+                int R = 1;
+                for (int k = 0; k < m; ++k)
+                    if (!rmap[a[k]]) rmap[a[k]] = R++;
+                std::vector<uint32_t> rows((size_t)R * S, 0);
+                for (int k = 0; k < m; ++k) rows[(size_t)rmap[a[k]] * S + pad + k / 32] |= 1u << (k % 32);
+                for (int c = 0; c < 256; ++c) rmap[c] = rmap[c] * S + pad;
+                struct PM {
+                    const uint32_t* base;
+                    const int32_t* rmap;
+                    const uint32_t* operator()(u64 c) const { return base + rmap[c & 255]; }
+                } pm{rows.data(), rmap.data()};
+                PairSpec s;
+                s.metric = LEVENSHTEIN;
+                s.op = op;
+                s.form = FORM_CACHED;
+                s.ci = ci;
+                s.cf = cf;
+                s.p = sp;
+                s.l1 = (u64)m;
+                for (int64_t c = 0; c < nc; ++c) {
+                    const int n = (int)(co[c + 1] - co[c]);
+                    s.l2 = (u64)n;
+                    s.kd_pre = ~0ull;
+                    const Plan pl = plan_int(s);
+                    if (!pl.run || n == 0) continue;
+                    const i64 K = pl.K, diff = m > n ? m - n : n - m;
+                    if (K < diff || K >= m) continue;
+                    uint64_t f = 0;
+                    const CountingText txt{cd + co[c], &f};
+                    switch (B) {
+                    case 1: lev_band32<1>(pm, m, txt, n, (int)K); break;
+                    case 2: lev_band32<2>(pm, m, txt, n, (int)K); break;
+                    case 3: lev_band32<3>(pm, m, txt, n, (int)K); break;
+                    case 4: lev_band32<4>(pm, m, txt, n, (int)K); break;
+                    case 6: lev_band32<6>(pm, m, txt, n, (int)K); break;
+                    case 8: lev_band32<8>(pm, m, txt, n, (int)K); break;
+                    case 12: lev_band32<12>(pm, m, txt, n, (int)K); break;
+                    default: lev_band32<16>(pm, m, txt, n, (int)K); break;
+                    }
+                    pe[w] += f * (uint64_t)B;
+                    pa[w] += f * (uint64_t)((band_bits((int)K, m - n) + 31) / 32);
+                    ++pp[w];
+                }
+            }
+        });
+    for (auto& t : th) t.join();
+    *exec_words = *alg_words = *pairs = 0;
+    for (int w = 0; w < nthreads; ++w) {
+        *exec_words += pe[w];
+        *alg_words += pa[w];
+        *pairs += pp[w];
+    }
+    return 0;
+}
+
 } // extern "C"
