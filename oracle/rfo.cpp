@@ -325,6 +325,14 @@ template <typename S2>
 i64 lcs_full(const PM& pm, const S2& t)
 {
     const i64 words = pm.words;
+    if (words == 1) { /* one word in a register, as lcs_unroll<1> (LCSseq_impl.hpp:205-260) */
+        u64 S = ~0ull;
+        for (i64 j = 0; j < t.n; ++j) {
+            const u64 u = S & pm.get(0, t[j]);
+            S = (S + u) | (S - u);
+        }
+        return popc(~S);
+    }
     std::vector<u64> S(words, ~0ull);
     for (i64 j = 0; j < t.n; ++j) {
         const u64 c = t[j];
