@@ -801,19 +801,16 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             a.perm = dperm;
             a.poff = pb->poff;
             a.plen = pb->plen;
-            const int64_t nchunks_full = (nc + chunk - 1) / chunk;
-            const bool small = (int64_t)cls[bk].size() * nchunks_full < (int64_t)g.sms * 8 && chunk > 256;
-            a.stage = (stage && !small) ? stage : 0;
-            size_t bsm = band_smem_bytes(a.tab_t, (int)a.scratch_per_thread, a.wmax, a.stage, spec.out_dtype);
+            /* results go straight out (no staged window); tiles sized for about four per
+             * resident CTA, in whole 32-position runs */
+            a.stage = 0;
+            size_t bsm = band_smem_bytes(a.tab_t, (int)a.scratch_per_thread, a.wmax);
             RFG_TRY(allow_dynamic_smem(fb, bsm));
             const int64_t bslots = (int64_t)g.sms * std::max(1, occupancy(fb, bblock, bsm));
-            int64_t cchunk = chunk;
-            if (small) {
-                const int64_t want = bslots * 4;
-                int64_t cc = ((int64_t)cls[bk].size() * nc + want - 1) / want;
-                cc = std::max<int64_t>(cc, bblock);
-                cchunk = std::min(chunk, (cc + bblock - 1) / bblock * bblock);
-            }
+            const int64_t want = (g_tiles_target > 0 ? g_tiles_target : bslots * 4);
+            int64_t cchunk = ((int64_t)cls[bk].size() * nc + want - 1) / want;
+            cchunk = std::max<int64_t>(cchunk, 1024);
+            cchunk = std::min<int64_t>((cchunk + 31) / 32 * 32, std::max<int64_t>(32, (nc + 31) / 32 * 32));
             a.chunk = cchunk;
             a.nchunks = (nc + cchunk - 1) / cchunk;
             const int64_t btiles = (int64_t)a.nq * a.nchunks;

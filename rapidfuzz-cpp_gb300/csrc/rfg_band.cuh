@@ -6,10 +6,13 @@
  * (lev_band32), chosen when that band is narrower than the pattern for the largest bound
  * K any pair of the query can reach (the length filter Levenshtein_impl.hpp:863 caps it).
  *
- * A CTA takes (query, chunk of choices) tiles from the launch's counter, like the tile
- * kernel, and scores one pair per thread with lev_band32<B> on B 32-bit words; the
- * kernel's registers are sized by the band, not by the pattern's length.  Per query the
- * CTA builds in shared memory
+ * A CTA takes (query, chunk of choices) tiles from the launch's counter; its warps take
+ * runs of 32 length-ordered positions of the tile from a counter of the CTA and score one
+ * pair per lane with lev_band32<B> on B 32-bit words (the kernel's registers are sized by
+ * the band, not by the pattern's length).  Only a few pairs of a chunk pass the length
+ * filter and those run hundreds of steps, so no barrier is taken between runs: a warp
+ * whose pairs were rejected takes the next run at once.  Results are stored where they
+ * belong.  Per query the CTA builds in shared memory
  *   - a compact pattern table: one row of ceil(m/32) 32-bit words for each code unit
  *     the query holds (plus the all-zero row), each row with zero words on either side
  *     so the band's window is loaded without range tests, and rmap[c] = the word offset
@@ -42,13 +45,12 @@ struct BandText {
     __device__ __forceinline__ u64 operator[](int j) const { return (u64)__ldg(p + j); }
 };
 
-/* shared-memory bytes of a band launch: kd table, rmap, rows, stage */
-inline size_t band_smem_bytes(int tab_t, int rows, int stride, int64_t stage, int out_dtype)
+/* shared-memory bytes of a band launch: kd table, rmap, rows */
+inline size_t band_smem_bytes(int tab_t, int rows, int stride)
 {
     const size_t kd = tab_t >= 0 ? ((size_t)tab_t + 1) * 4 : 0;
     const size_t head = (kd + 1024 + 15) / 16 * 16;
-    const size_t tab = ((size_t)rows * stride * 4 + 15) / 16 * 16;
-    return head + tab + (size_t)stage * (out_dtype == 0 ? 4 : 8);
+    return head + ((size_t)rows * stride * 4 + 15) / 16 * 16;
 }
 
 template <typename CT, int B>
@@ -62,8 +64,8 @@ __global__ void __launch_bounds__(256, B <= 4 ? 4 : B <= 8 ? 2 : 1) k_band(const
     const size_t kdb = tab_t >= 0 ? ((size_t)tab_t + 1) * 4 : 0;
     int* rmap = (int*)((unsigned char*)smem + kdb);
     u32* rows = (u32*)((unsigned char*)smem + (kdb + 1024 + 15) / 16 * 16);
-    unsigned char* stage = a.stage ? (unsigned char*)rows + ((size_t)R * S * 4 + 15) / 16 * 16 : nullptr;
     __shared__ int64_t s_tile;
+    __shared__ int s_sub;
     __shared__ int s_warp_cnt[8];
     int64_t cur_q = -1;
     int m = 0;
@@ -71,7 +73,10 @@ __global__ void __launch_bounds__(256, B <= 4 ? 4 : B <= 8 ? 2 : 1) k_band(const
     const bool is_int = result_is_int(a.metric, a.op);
     const bool use_kd = tab_t >= 0;
     for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(a.counter, 1);
+        if (threadIdx.x == 0) {
+            s_tile = atomicAdd(a.counter, 1);
+            s_sub = 0;
+        }
         __syncthreads();
         const int64_t t = s_tile;
         if (t >= ntiles) break;
@@ -129,13 +134,21 @@ __global__ void __launch_bounds__(256, B <= 4 ? 4 : B <= 8 ? 2 : 1) k_band(const
             __syncthreads();
             cur_q = qi;
         }
+        /* the tile's positions go out in runs of 32 that warps take from a counter of
+         * the CTA: a warp that meets pairs the length filter rejects moves on at once,
+         * and the CTA waits for its slowest warp only at the end of the tile */
         const int64_t c0 = ch * a.chunk;
         const int64_t c1 = c0 + a.chunk < a.c.n ? c0 + a.chunk : a.c.n;
-        const int64_t win = stage ? a.stage : c1 - c0;
+        const int nsub = (int)((c1 - c0 + 31) / 32);
         const BandRows pm{rows, rmap};
-        for (int64_t s0 = c0; s0 < c1; s0 += win) {
-            const int64_t s1 = s0 + win < c1 ? s0 + win : c1;
-            for (int64_t p = s0 + threadIdx.x; p < s1; p += blockDim.x) {
+        const int lane = threadIdx.x & 31;
+        for (;;) {
+            int sub = 0;
+            if (lane == 0) sub = atomicAdd(&s_sub, 1);
+            sub = __shfl_sync(0xffffffffu, sub, 0);
+            if (sub >= nsub) break;
+            const int64_t p = c0 + (int64_t)sub * 32 + lane;
+            if (p < c1) {
                 const int64_t ci = __ldg(a.perm + p);
                 const int64_t o0 = __ldg(a.poff + p);
                 const int n = __ldg(a.plen + p);
@@ -177,12 +190,7 @@ __global__ void __launch_bounds__(256, B <= 4 ? 4 : B <= 8 ? 2 : 1) k_band(const
                 }
                 else
                     finish_int(s, pl, raw, &vi, &vf);
-                emit(a, qi, ci, vi, vf, is_int, s.ci, s.cf, (TopList<false>*)nullptr, stage, s0);
-            }
-            if (stage) {
-                __syncthreads();
-                flush_stage(a, stage, qi, s0, s1);
-                __syncthreads();
+                store_result(a, qi, ci, vi, vf, is_int);
             }
         }
         __syncthreads();
