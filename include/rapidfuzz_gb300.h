@@ -263,6 +263,11 @@ rfg_status rfg_server_destroy(rfg_server server);
  * RFG_ERR_OUT_OF_MEMORY; a negative value switches the injection off. */
 rfg_status rfg_testing_fail_device_allocs(int64_t after);
 
+/* Launch-shape override for measurements: the band kernels' work units of 32 x rounds
+ * pairs of one query (1..64; 0 restores the default, sized by the class).  Batches
+ * prepared afterwards use it, until rfg_batch_tune chooses its own. */
+rfg_status rfg_testing_band_rounds(int32_t rounds);
+
 /* ------------------------------------------------------ no-allocation cdist
  * rfg_cdist_noalloc has no counterpart in the reference.  It is for callers that may
  * not allocate device memory (inside another framework's memory manager, in a process

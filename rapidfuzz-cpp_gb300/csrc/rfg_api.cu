@@ -75,6 +75,7 @@ struct Ctx {
     std::atomic<bool> init{false};
     int device = 0;
     int sms = 0;
+    int prio_high = 0; /* the device's highest stream priority (urgent launches) */
     cudaStream_t stream = nullptr;
     cudaStream_t copy = nullptr; /* device-to-host result copies overlapping the next row block */
     cudaEvent_t blk_ev[RFG_MAX_ROW_BLOCKS] = {};
@@ -134,6 +135,11 @@ rfg_status ensure_ctx_locked()
                     cudaGetErrorString(e));
     RFG_CUDA(cudaSetDevice(g.device));
     RFG_CUDA(cudaDeviceGetAttribute(&g.sms, cudaDevAttrMultiProcessorCount, g.device));
+    {
+        int least = 0, greatest = 0;
+        RFG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        g.prio_high = greatest;
+    }
     RFG_CUDA(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
     RFG_CUDA(cudaStreamCreateWithFlags(&g.copy, cudaStreamNonBlocking));
     for (auto& e : g.blk_ev) RFG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -449,6 +455,11 @@ int g_mq_mode = 1;          /* one-word unit-weight distances take several queri
 int g_half_mode = 1;        /* queries of <= 32 units run on 32-bit recurrence words (autotuning) */
 int g_block_override = 0;   /* override of the tile kernels' block size (autotuning) */
 int g_fast_mode = 1;        /* unit-weight one-word distances run on the warp tiles (k_fast) */
+/* band launches: the largest pattern table of a band query (bytes), and the shared
+ * memory a band CTA takes at most (warps x slice) */
+#define RFG_BAND_MAX_TABLE (48 * 1024)
+#define RFG_BAND_MAX_SMEM (96 * 1024)
+int g_band_rounds = 0; /* band units of 32 x this many pairs (0: sized by the class; autotuning) */
 int g_band_mode = 1;        /* unit-weight Levenshtein with a band narrower than the pattern runs on k_band */
 int64_t g_fast_window = 512; /* choice positions per warp window of k_fast (autotuning) */
 
@@ -473,6 +484,7 @@ struct LaunchRec {
     size_t smem;
     KParams a;
     int rblock; /* row block (a contiguous range of queries) the launch belongs to */
+    int urgent = 0; /* 1: launched at the device's highest priority (the block's critical path) */
 };
 
 struct Prepared {
@@ -485,6 +497,8 @@ struct Prepared {
     const int64_t* poff = nullptr;
     const int32_t* plen = nullptr;
     const int4* prec = nullptr; /* k_fast visiting records */
+    const int4* brec = nullptr; /* band launches: the choices' records in length order */
+    const BandQuery* bq = nullptr; /* band launches: per-query records, each class's in a run */
     /* which kinds of launches the preparation holds (what the tuner has to sweep) */
     bool has_fast = false, has_band = false, has_tiles = false;
     bool has_pre = false; /* pre.a / grid: the per-query table pass before the row blocks */
@@ -603,11 +617,11 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
      * unit-weight Levenshtein (band_class_words(k - 5) 32-bit words); one set per row block */
     const bool band_ok = g_band_mode != 0 && fam == FAM_LEV && spec.metric == RFG_LEVENSHTEIN && spec.sp.ins == 1 &&
                          spec.sp.del == 1 && spec.sp.rep == 1 && spec.form != RFG_FORM_MULTI && spec.topk == 0 &&
-                         !spec.fixed_perm && c.width == 1;
+                         !spec.fixed_perm && c.width == 1 && nc < INT32_MAX;
     std::vector<std::vector<int32_t>> cls(nblk * NCLS);
     std::vector<int64_t> cls_maxlen(nblk * NCLS, 0);
     std::vector<int32_t> cls_wide(nblk * NCLS, 0);
-    std::vector<int32_t> cls_distinct(nblk * NCLS, 0);
+    std::vector<int64_t> cls_bwords(nblk * NCLS, 0); /* band classes: row words of the largest table */
     for (int64_t b = 0; b < nblk; ++b)
         for (int64_t i = pb->rows[b].first; i < pb->rows[b].second; ++i) {
             int k;
@@ -616,15 +630,18 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
                 const int wc = word_class(q.len[i]);
                 k = wc == 1 ? 0 : wc == 2 ? 1 : wc == 4 ? 2 : wc == 8 ? 3 : 4;
             }
+            int64_t bwords = 0;
             if (band_ok && k > 0 && q.distinct[i] >= 0) {
                 const int bc = band_class_of(spec, q.len[i], host_max_choice_len);
-                if (bc >= 0) k = 5 + bc;
+                /* the query's table (distinct units + the zero row) must fit a warp's slice */
+                if (bc >= 0) bwords = (int64_t)(q.distinct[i] + 1) * band_row_stride((int)q.len[i], band_class_words(bc));
+                if (bc >= 0 && bwords * 4 <= RFG_BAND_MAX_TABLE) k = 5 + bc;
             }
             const int64_t bk = b * NCLS + k;
             cls[bk].push_back((int32_t)i);
             cls_maxlen[bk] = std::max(cls_maxlen[bk], q.len[i]);
             cls_wide[bk] = std::max(cls_wide[bk], q.wide[i]);
-            cls_distinct[bk] = std::max(cls_distinct[bk], q.distinct[i]);
+            if (k >= 5) cls_bwords[bk] = std::max(cls_bwords[bk], bwords);
         }
     size_t total = 0;
     for (auto& v : cls) {
@@ -712,6 +729,68 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             }
         }
     }
+    /* band classes: the choices in one length order ({offset low, high, length, index}),
+     * and per query its passing run of that order (band_range) cut into units */
+    std::vector<int32_t> brec;
+    std::vector<BandQuery> bqv;
+    std::vector<size_t> cls_bq(nblk * NCLS, 0);
+    std::vector<int64_t> cls_units(nblk * NCLS, 0), cls_rounds(nblk * NCLS, 1);
+    bool any_band = false;
+    for (int64_t bk = 0; bk < nblk * NCLS; ++bk)
+        if (bk % NCLS >= 5 && !cls[bk].empty()) any_band = true;
+    if (any_band) {
+        const int64_t* hoff = host_choice_off ? host_choice_off : off_tmp.data();
+        std::vector<int32_t> gperm;
+        chunk_length_order(clen, std::max<int64_t>(nc, 1), &gperm);
+        std::vector<int32_t> slen(nc);
+        brec.resize((size_t)nc * 4);
+        for (int64_t i = 0; i < nc; ++i) {
+            const int32_t ci = gperm[i];
+            const uint64_t o = (uint64_t)hoff[ci];
+            brec[4 * i] = (int32_t)(uint32_t)o;
+            brec[4 * i + 1] = (int32_t)(uint32_t)(o >> 32);
+            brec[4 * i + 2] = slen[i] = clen[ci];
+            brec[4 * i + 3] = ci;
+        }
+        for (int64_t bk = 0; bk < nblk * NCLS; ++bk) {
+            if (bk % NCLS < 5 || cls[bk].empty()) continue;
+            const size_t first = bqv.size();
+            int64_t npass = 0;
+            for (int32_t qi : cls[bk]) {
+                i64 nlo = 1, nhi = 0, Kmax = 0;
+                BandQuery r{};
+                r.qi = qi;
+                if (band_range(spec.metric, spec.op, spec.form, spec.sp, spec.ci, spec.cf, q.len[qi], host_max_choice_len,
+                               &nlo, &nhi, &Kmax)) {
+                    r.nlo = (int32_t)nlo;
+                    r.nhi = (int32_t)nhi;
+                    r.plo = (int32_t)(std::lower_bound(slen.begin(), slen.end(), r.nlo) - slen.begin());
+                    r.phi = (int32_t)(std::upper_bound(slen.begin(), slen.end(), r.nhi) - slen.begin());
+                }
+                else { /* nothing passes: every pair is filled */
+                    r.nlo = 1;
+                    r.nhi = 0;
+                }
+                npass += r.phi - r.plo;
+                bqv.push_back(r);
+            }
+            /* units of `rounds` groups of 32 pairs (one table build each): as many
+             * groups as keep about two units per resident warp */
+            const int64_t rounds = g_band_rounds > 0 ? g_band_rounds
+                                                     : std::min<int64_t>(8, std::max<int64_t>(1, npass / ((int64_t)g.sms * 2048)));
+            int64_t ustart = 0;
+            for (size_t i = first; i < bqv.size(); ++i) {
+                bqv[i].ustart = (int32_t)std::min<int64_t>(ustart, INT32_MAX);
+                ustart += (bqv[i].phi - bqv[i].plo + 32 * rounds - 1) / (32 * rounds);
+            }
+            BandQuery end{};
+            end.ustart = (int32_t)std::min<int64_t>(ustart, INT32_MAX);
+            bqv.push_back(end);
+            cls_bq[bk] = first;
+            cls_units[bk] = ustart;
+            cls_rounds[bk] = rounds;
+        }
+    }
     {
         /* the host tables leave in one copy from pinned staging */
         size_t tot = 0;
@@ -721,7 +800,8 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             return o;
         };
         const size_t oq = reserve(qall.size() * 4), operm = reserve(perm.size() * 4), opo = reserve(po.size() * 8),
-                     opl = reserve(pl.size() * 4), ofr = reserve(frec.size() * 4);
+                     opl = reserve(pl.size() * 4), ofr = reserve(frec.size() * 4), obr = reserve(brec.size() * 4),
+                     obq = reserve(bqv.size() * sizeof(BandQuery));
         unsigned char* h;
         RFG_TRY(upload_stage(tot, &h));
         memcpy(h + oq, qall.data(), qall.size() * 4);
@@ -729,6 +809,8 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         if (!po.empty()) memcpy(h + opo, po.data(), po.size() * 8);
         if (!pl.empty()) memcpy(h + opl, pl.data(), pl.size() * 4);
         if (!frec.empty()) memcpy(h + ofr, frec.data(), frec.size() * 4);
+        if (!brec.empty()) memcpy(h + obr, brec.data(), brec.size() * 4);
+        if (!bqv.empty()) memcpy(h + obq, bqv.data(), bqv.size() * sizeof(BandQuery));
         RFG_TRY(pb->packed.alloc(tot));
         RFG_CUDA(cudaMemcpyAsync(pb->packed.p, h, tot, cudaMemcpyHostToDevice, g.stream));
         RFG_CUDA(cudaEventRecord(g.up_ev, g.stream));
@@ -740,6 +822,8 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             pb->plen = (const int32_t*)(d + opl);
         }
         if (!frec.empty()) pb->prec = (const int4*)(d + ofr);
+        if (!brec.empty()) pb->brec = (const int4*)(d + obr);
+        if (!bqv.empty()) pb->bq = (const BandQuery*)(d + obq);
     }
     pb->chunk = chunk;
     pb->nchunks = (nc + chunk - 1) / chunk;
@@ -748,8 +832,12 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
 
     std::vector<size_t> generic_recs;
     size_t scratch_bytes = 0;
-    for (int64_t bk = 0; bk < nblk * NCLS; ++bk) {
-        const int k = (int)(bk % NCLS);
+    /* within a row block the band classes go first, widest first: their few long pairs
+     * set the block's critical path, and the block scheduler serves launches in order */
+    for (int64_t kb = 0; kb < nblk * NCLS; ++kb) {
+        const int kk = (int)(kb % NCLS);
+        const int k = kk < BAND_CLASSES ? NCLS - 1 - kk : kk - BAND_CLASSES;
+        const int64_t bk = kb - kk + k;
         if (cls[bk].empty()) continue;
         KParams a;
         memset(&a, 0, sizeof a);
@@ -783,40 +871,34 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         const bool small_class =
             k < 4 && !topk && (int64_t)cls[bk].size() * nchunks_full < (int64_t)g.sms * 8 && chunk > 256;
         if (k >= 5) {
-            /* banded Levenshtein, one pair per thread, table and cutoffs per query in
-             * shared memory */
+            /* banded Levenshtein: warp tasks of passing pairs and of row fills, each warp
+             * with its own table in shared memory */
             const int B = band_class_words(k - 5);
             const void* fb = band_kernel(c.width, B);
             if (!fb) return fail(RFG_ERR_INVALID_ARGUMENT, "no band kernel for this code-unit width");
-            const int bblock = 256;
-            a.wmax = band_row_stride((int)cls_maxlen[bk], B);
-            a.scratch_per_thread = cls_distinct[bk] + 1; /* table rows: the units below 256, the zero row */
-            a.tab_t = (spec.op == RFG_NORMALIZED_DISTANCE || spec.op == RFG_NORMALIZED_SIMILARITY)
-                          ? (int)std::min<int64_t>(host_max_choice_len, 4095)
-                          : -1;
+            a.scratch_per_thread = cls_bwords[bk];
+            a.tab_t = (spec.op == RFG_NORMALIZED_DISTANCE || spec.op == RFG_NORMALIZED_SIMILARITY) ? 32 * B : -1;
             if (fast_ok) {
                 a.fast = 1;
                 a.fast_k = clamp_bound(spec.ci);
             }
-            a.perm = dperm;
-            a.poff = pb->poff;
-            a.plen = pb->plen;
-            /* results go straight out (no staged window); tiles sized for about four per
-             * resident CTA, in whole 32-position runs */
-            a.stage = 0;
-            size_t bsm = band_smem_bytes(a.tab_t, (int)a.scratch_per_thread, a.wmax);
+            a.prec = pb->brec;
+            a.band_q = pb->bq + cls_bq[bk];
+            a.chunk = cls_rounds[bk];
+            a.nchunks = cls_units[bk];
+            const int64_t fills = (int64_t)a.nq * ((nc + RFG_BAND_FILL - 1) / RFG_BAND_FILL);
+            if (cls_units[bk] + fills > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "batch too large for one launch");
+            const size_t per = band_warp_bytes(a.tab_t, a.scratch_per_thread);
+            const int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (size_t)RFG_BAND_MAX_SMEM / per));
+            const int bblock = 32 * warps;
+            const size_t bsm = per * warps;
             RFG_TRY(allow_dynamic_smem(fb, bsm));
             const int64_t bslots = (int64_t)g.sms * std::max(1, occupancy(fb, bblock, bsm));
-            const int64_t want = (g_tiles_target > 0 ? g_tiles_target : bslots * 4);
-            int64_t cchunk = ((int64_t)cls[bk].size() * nc + want - 1) / want;
-            cchunk = std::max<int64_t>(cchunk, 1024);
-            cchunk = std::min<int64_t>((cchunk + 31) / 32 * 32, std::max<int64_t>(32, (nc + 31) / 32 * 32));
-            a.chunk = cchunk;
-            a.nchunks = (nc + cchunk - 1) / cchunk;
-            const int64_t btiles = (int64_t)a.nq * a.nchunks;
-            if (btiles > INT32_MAX) return fail(RFG_ERR_INVALID_ARGUMENT, "batch too large for one launch");
-            pb->launches.push_back(
-                LaunchRec{fb, (unsigned)std::min<int64_t>(btiles, bslots), bblock, bsm, a, (int)(bk / NCLS)});
+            const int64_t tasks = cls_units[bk] + fills;
+            /* the widest bands hold the longest pairs and few of them: their CTAs are
+             * served first, ahead of the classes that fill the GPU */
+            pb->launches.push_back(LaunchRec{fb, (unsigned)std::min<int64_t>((tasks + warps - 1) / warps, bslots), bblock,
+                                             bsm, a, (int)(bk / NCLS), B >= 4 ? 1 : 0});
             pb->has_band = true;
             continue;
         }
@@ -1059,7 +1141,21 @@ rfg_status enqueue_block(Prepared& pb, int b, cudaStream_t st)
         }
         KParams a = L.a;
         void* args[] = {&a};
-        RFG_CUDA(cudaLaunchKernel(L.fn, dim3(L.grid), dim3(L.block), args, L.smem, s));
+        if (L.urgent) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(L.grid);
+            cfg.blockDim = dim3(L.block);
+            cfg.dynamicSmemBytes = L.smem;
+            cfg.stream = s;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributePriority;
+            attr[0].val.priority = g.prio_high;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            RFG_CUDA(cudaLaunchKernelExC(&cfg, L.fn, args));
+        }
+        else
+            RFG_CUDA(cudaLaunchKernel(L.fn, dim3(L.grid), dim3(L.block), args, L.smem, s));
         if (i > 0) RFG_CUDA(cudaEventRecord(ss.ev[i], s));
     }
     for (size_t i = 1; i < nl; ++i) RFG_CUDA(cudaStreamWaitEvent(st, ss.ev[i], 0));
@@ -1714,6 +1810,13 @@ rfg_status rfg_set_device(int device)
 rfg_status rfg_testing_fail_device_allocs(int64_t after)
 {
     g_fail_allocs_after.store(after < 0 ? -1 : after);
+    return RFG_OK;
+}
+
+rfg_status rfg_testing_band_rounds(int32_t rounds)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    g_band_rounds = rounds > 0 ? std::min(rounds, 64) : 0;
     return RFG_OK;
 }
 
@@ -2514,12 +2617,14 @@ struct TuneChoice {
     int stage = 1;        /* dense tiles stage results in shared memory */
     int64_t window = 512; /* warp tiles: choice positions per window */
     int band = 1;         /* band classes on (k_band) or off (the general kernels) */
+    int rounds = 0;       /* band units: 32 x rounds pairs (0: sized by the class) */
 };
 
 static rfg_status batch_reprepare(rfg_batch b, const TuneChoice& c)
 {
-    const int ob = g_block_override, os = g_stage_mode, obd = g_band_mode;
+    const int ob = g_block_override, os = g_stage_mode, obd = g_band_mode, orr = g_band_rounds;
     const int64_t ot = g_tiles_target, ow = g_fast_window;
+    g_band_rounds = c.rounds;
     g_block_override = c.block;
     g_tiles_target = c.tiles;
     g_stage_mode = c.stage;
@@ -2532,6 +2637,7 @@ static rfg_status batch_reprepare(rfg_batch b, const TuneChoice& c)
     g_stage_mode = os;
     g_fast_window = ow;
     g_band_mode = obd;
+    g_band_rounds = orr;
     if (st == RFG_OK && cudaStreamSynchronize(g.stream) != cudaSuccess) st = fail(RFG_ERR_CUDA, "prepare failed");
     if (st != RFG_OK) {
         delete np;
@@ -2556,6 +2662,7 @@ static rfg_status batch_reprepare_shape(rfg_batch b, int block, int64_t tiles, i
     c.stage = stage;
     c.window = g_fast_window;
     c.band = g_band_mode;
+    c.rounds = g_band_rounds;
     return batch_reprepare(b, c);
 }
 
@@ -2728,7 +2835,7 @@ rfg_status rfg_batch_tune(rfg_batch b, void* stream, int32_t* best_block, int64_
             RFG_TRY(trial(c));
         }
     RFG_TRY(batch_reprepare(b, best));
-    if (b->pb->has_tiles || b->pb->has_band) { /* chunk size and staging shape the band launches too */
+    if (b->pb->has_tiles) {
         const TuneChoice base = best;
         const int blocks[] = {128, 256};
         const int mults[] = {2, 4, 8, 16, 32};

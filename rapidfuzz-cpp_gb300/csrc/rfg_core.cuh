@@ -957,71 +957,198 @@ RFG_HD int band_lo(int K, int delta) { return -((K - delta + 1) >> 1); }
 RFG_HD int band_hi(int K, int delta) { return (K + delta + 1) >> 1; }
 RFG_HD int band_bits(int K, int delta) { return band_hi(K, delta) - band_lo(K, delta) + 1; }
 
+/* s = a + b over B 32-bit words, the carry out of the top word dropped: on the GPU one
+ * add.cc / addc chain (the carry passes in the condition code, one instruction a word) */
+template <int B>
+RFG_HD void add_chain(const u32* a, const u32* b, u32* s)
+{
+#ifdef __CUDA_ARCH__
+    if constexpr (B == 1)
+        s[0] = a[0] + b[0];
+    else if constexpr (B == 2)
+        asm("add.cc.u32 %0, %2, %4; addc.u32 %1, %3, %5;"
+            : "=r"(s[0]), "=r"(s[1])
+            : "r"(a[0]), "r"(a[1]), "r"(b[0]), "r"(b[1]));
+    else if constexpr (B == 3)
+        asm("add.cc.u32 %0, %3, %6; addc.cc.u32 %1, %4, %7; addc.u32 %2, %5, %8;"
+            : "=r"(s[0]), "=r"(s[1]), "=r"(s[2])
+            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(b[0]), "r"(b[1]), "r"(b[2]));
+    else if constexpr (B == 4)
+        asm("add.cc.u32 %0, %4, %8; addc.cc.u32 %1, %5, %9; addc.cc.u32 %2, %6, %10; addc.u32 %3, %7, %11;"
+            : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3])
+            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]));
+    else if constexpr (B == 6)
+        asm("add.cc.u32 %0, %6, %12; addc.cc.u32 %1, %7, %13; addc.cc.u32 %2, %8, %14; addc.cc.u32 %3, %9, %15; addc.cc.u32 %4, %10, %16; addc.u32 %5, %11, %17;"
+            : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5])
+            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]));
+    else if constexpr (B == 8)
+        asm("add.cc.u32 %0, %8, %16; addc.cc.u32 %1, %9, %17; addc.cc.u32 %2, %10, %18; addc.cc.u32 %3, %11, %19; addc.cc.u32 %4, %12, %20; addc.cc.u32 %5, %13, %21; addc.cc.u32 %6, %14, %22; addc.u32 %7, %15, %23;"
+            : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6]), "=r"(s[7])
+            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]));
+    else if constexpr (B == 12)
+        asm("add.cc.u32 %0, %12, %24; addc.cc.u32 %1, %13, %25; addc.cc.u32 %2, %14, %26; addc.cc.u32 %3, %15, %27; addc.cc.u32 %4, %16, %28; addc.cc.u32 %5, %17, %29; addc.cc.u32 %6, %18, %30; addc.cc.u32 %7, %19, %31; addc.cc.u32 %8, %20, %32; addc.cc.u32 %9, %21, %33; addc.cc.u32 %10, %22, %34; addc.u32 %11, %23, %35;"
+            : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6]), "=r"(s[7]), "=r"(s[8]), "=r"(s[9]), "=r"(s[10]), "=r"(s[11])
+            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(a[8]), "r"(a[9]), "r"(a[10]), "r"(a[11]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]), "r"(b[8]), "r"(b[9]), "r"(b[10]), "r"(b[11]));
+    else if constexpr (B == 16)
+        asm("add.cc.u32 %0, %16, %32; addc.cc.u32 %1, %17, %33; addc.cc.u32 %2, %18, %34; addc.cc.u32 %3, %19, %35; addc.cc.u32 %4, %20, %36; addc.cc.u32 %5, %21, %37; addc.cc.u32 %6, %22, %38; addc.cc.u32 %7, %23, %39; addc.cc.u32 %8, %24, %40; addc.cc.u32 %9, %25, %41; addc.cc.u32 %10, %26, %42; addc.cc.u32 %11, %27, %43; addc.cc.u32 %12, %28, %44; addc.cc.u32 %13, %29, %45; addc.cc.u32 %14, %30, %46; addc.u32 %15, %31, %47;"
+            : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6]), "=r"(s[7]), "=r"(s[8]), "=r"(s[9]), "=r"(s[10]), "=r"(s[11]), "=r"(s[12]), "=r"(s[13]), "=r"(s[14]), "=r"(s[15])
+            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(a[8]), "r"(a[9]), "r"(a[10]), "r"(a[11]), "r"(a[12]), "r"(a[13]), "r"(a[14]), "r"(a[15]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]), "r"(b[8]), "r"(b[9]), "r"(b[10]), "r"(b[11]), "r"(b[12]), "r"(b[13]), "r"(b[14]), "r"(b[15]));
+    else
+        static_assert(B == 1, "no add chain for this width");
+#else
+    u32 carry = 0;
+    for (int i = 0; i < B; ++i) {
+        const u64 t = (u64)a[i] + b[i] + carry;
+        s[i] = (u32)t;
+        carry = (u32)(t >> 32);
+    }
+#endif
+}
+
+/* the B-word window of a pattern row from pattern index `start` (any sign; the row has
+ * B + 1 zero words before word 0): one funnel shift per word */
+template <int B>
+RFG_HD void band_window(const u32* row, int start, u32* X)
+{
+    const int w0 = start >> 5; /* floor division (arithmetic shift) */
+    const int sh = start & 31;
+    u32 prev = row[w0];
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        const u32 next = row[w0 + b + 1];
+        X[b] = funnel32(prev, next, sh);
+        prev = next;
+    }
+}
+
 /* Banded Levenshtein on B 32-bit words (a window of 32*B bits) over a pattern table of
- * 32-bit words: pm(c) gives the row of text unit c as a pointer to its words, with at
- * least B + 1 zero words before word 0 and 2B + 2 after the last, so the window's words
- * are loaded without range tests.  Window bit b covers diagonal dlo + b (pattern index
- * dlo + j + b at step j); dlo = band_lo(K, m - n) and band_bits(K, m - n) <= 32*B.
- * Extracting the window takes one funnel shift per word (the GPU's native width); the
- * carry of (X & VP) + VP runs through the words; the frame moves down one row per text
- * unit (D0 >> 1), as in levenshtein_hyrroe2003_small_band (Levenshtein_impl.hpp:419-505).
- * The band computes the distance over paths inside it -- exact for every pair whose
- * distance is at most K, since those paths never leave Ukkonen's band -- and the lower
- * bound on the diagonal through (m, n) stops it every 8 text units once it passes K.
- * Requires |m-n| <= K < m, n > 0.  Returns d, or any value > K. */
-template <int B, typename PM32, typename TXT>
-RFG_HD i64 lev_band32(const PM32& pm, int m, const TXT& t, int n, int K)
+ * 32-bit words, for one-byte texts: pm(c) gives the row of text unit c as a pointer to
+ * its words, with at least B + 1 zero words before word 0 and 2B + 2 after the last, so
+ * the window's words are loaded without range tests.  Window bit b covers diagonal
+ * dlo + b (pattern index dlo + j + b at step j); dlo = band_lo(K, m - n) and
+ * band_bits(K, m - n) <= 32*B.  The carry of (X & VP) + VP runs through the words; the
+ * frame moves down one row per text unit (D0 >> 1), as in
+ * levenshtein_hyrroe2003_small_band (Levenshtein_impl.hpp:419-505).  The band computes
+ * the distance over paths inside it -- exact for every pair whose distance is at most K,
+ * since those paths never leave Ukkonen's band -- and the lower bound on the diagonal
+ * through (m, n) stops it after every 8 text units once it passes K.
+ * A pair is a lane's state (BandLane) that band_run8 advances 8 text units at a time:
+ * the band kernel gives a lane whose pair ended the next pair, and the text of the next
+ * 8 units is loaded while the current 8 run.  Requires |m-n| <= K < m, n > 0. */
+template <int B>
+struct BandLane {
+    u32 VP[B], VN[B], rmask[B];
+    u32 cur[2]; /* the block's 8 text units, 4 to a word */
+    int diag;   /* D on the window's bottom diagonal */
+    int start;  /* pattern index of window bit 0 at the block's first unit */
+    int j, n, K;
+};
+
+template <int B, typename TXT>
+RFG_HD void band_init(BandLane<B>& L, int m, const TXT& t, int n, int K)
 {
     const int NB = 32 * B;
     const int dlo = band_lo(K, m - n);
-    u32 VP[B], VN[B], rmask[B];
 #pragma unroll
     for (int b = 0; b < B; ++b) {
-        VP[b] = range_mask32(-dlo - 32 * b, NB - 1 - 32 * b); /* rows 1.. of column 0: delta +1 */
-        VN[b] = 0;
-        rmask[b] = range_mask32((m - n) - dlo - 32 * b, NB - 2 - 32 * b);
+        L.VP[b] = range_mask32(-dlo - 32 * b, NB - 1 - 32 * b); /* rows 1.. of column 0: delta +1 */
+        L.VN[b] = 0;
+        L.rmask[b] = range_mask32((m - n) - dlo - 32 * b, NB - 2 - 32 * b);
     }
-    int diag = dlo + NB - 1; /* D on the window's bottom diagonal, column 0 */
-    int start = dlo;         /* pattern index of window bit 0 */
-    for (int j = 0; j < n; ++j, ++start) {
-        const u32* row = pm(t[j]);
-        const int w0 = start >> 5; /* floor division (arithmetic shift) */
-        const int sh = start & 31;
-        u32 X[B];
-        u32 prev = row[w0];
+    L.diag = dlo + NB - 1;
+    L.start = dlo;
+    L.j = 0;
+    L.n = n;
+    L.K = K;
+    u32 u[8];
 #pragma unroll
-        for (int b = 0; b < B; ++b) {
-            const u32 next = row[w0 + b + 1];
-            X[b] = funnel32(prev, next, sh);
-            prev = next;
-        }
-        u32 D0[B];
-        u32 carry = 0;
+    for (int s = 0; s < 8; ++s) u[s] = (u32)t[s < n - 1 ? s : n - 1];
+    L.cur[0] = u[0] | u[1] << 8 | u[2] << 16 | u[3] << 24;
+    L.cur[1] = u[4] | u[5] << 8 | u[6] << 16 | u[7] << 24;
+}
+
+/* one text unit whose window X is loaded */
+template <int B>
+RFG_HD void band_step(BandLane<B>& L, const u32* X)
+{
+    u32 U[B], S[B], D0[B];
 #pragma unroll
-        for (int b = 0; b < B; ++b) {
-            const u32 u = X[b] & VP[b];
-            const u64 s = (u64)u + VP[b] + carry;
-            carry = (u32)(s >> 32);
-            D0[b] = ((u32)s ^ VP[b]) | X[b] | VN[b];
-        }
-        diag += (D0[B - 1] >> 31) == 0;
+    for (int b = 0; b < B; ++b) U[b] = X[b] & L.VP[b];
+    add_chain<B>(U, L.VP, S);
 #pragma unroll
-        for (int b = 0; b < B; ++b) {
-            const u32 HP = VN[b] | ~(D0[b] | VP[b]);
-            const u32 HN = D0[b] & VP[b];
-            const u32 D0s = b + 1 < B ? funnel32(D0[b], D0[b + 1 < B ? b + 1 : b], 1) : (D0[b] >> 1);
-            VP[b] = HN | ~(D0s | HP);
-            VN[b] = D0s & HP;
-        }
-        if ((j & 7) == 7 || j == n - 1) {
-            int v = diag;
+    for (int b = 0; b < B; ++b) D0[b] = (S[b] ^ L.VP[b]) | X[b] | L.VN[b];
+    L.diag += 1 - (int)(D0[B - 1] >> 31);
 #pragma unroll
-            for (int b = 0; b < B; ++b) v -= popc_w(VP[b] & rmask[b]) - popc_w(VN[b] & rmask[b]);
-            if (j == n - 1) return v;
-            if (v > K) return (i64)K + 1;
+    for (int b = 0; b < B; ++b) {
+        const u32 HP = L.VN[b] | ~(D0[b] | L.VP[b]);
+        const u32 HN = D0[b] & L.VP[b];
+        const u32 D0s = b + 1 < B ? funnel32(D0[b], D0[b + 1 < B ? b + 1 : b], 1) : (D0[b] >> 1);
+        L.VP[b] = HN | ~(D0s | HP);
+        L.VN[b] = D0s & HP;
+    }
+}
+
+/* the next 8 text units (fewer at the end); true when the pair is done, with *out = d,
+ * or any value > K */
+template <int B, typename PM32, typename TXT>
+RFG_HD bool band_run8(BandLane<B>& L, const PM32& pm, const TXT& t, i64* out)
+{
+    const int last = L.n - 1;
+    u32 nx[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int k = L.j + 8 + s;
+        nx[s] = (u32)t[k < last ? k : last];
+    }
+    const int rem = L.n - L.j;
+    if (rem >= 8) { /* a whole block: straight-line code, the loads of later units run ahead */
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            const u32 c = (L.cur[s >> 2] >> (8 * (s & 3))) & 0xffu;
+            u32 X[B];
+            band_window<B>(pm(c), L.start + s, X);
+            band_step<B>(L, X);
         }
     }
-    return (i64)n;
+    else {
+#pragma unroll
+        for (int s = 0; s < 8; ++s)
+            if (s < rem) {
+                const u32 c = (L.cur[s >> 2] >> (8 * (s & 3))) & 0xffu;
+                u32 X[B];
+                band_window<B>(pm(c), L.start + s, X);
+                band_step<B>(L, X);
+            }
+    }
+    L.j += 8;
+    L.start += 8;
+    int v = L.diag;
+#pragma unroll
+    for (int b = 0; b < B; ++b) v -= popc_w(L.VP[b] & L.rmask[b]) - popc_w(L.VN[b] & L.rmask[b]);
+    if (L.j >= L.n) {
+        *out = v;
+        return true;
+    }
+    if (v > L.K) {
+        *out = (i64)L.K + 1;
+        return true;
+    }
+    L.cur[0] = nx[0] | nx[1] << 8 | nx[2] << 16 | nx[3] << 24;
+    L.cur[1] = nx[4] | nx[5] << 8 | nx[6] << 16 | nx[7] << 24;
+    return false;
+}
+
+/* one pair start to end; *steps (if given) = the text units run */
+template <int B, typename PM32, typename TXT>
+RFG_HD i64 lev_band32(const PM32& pm, int m, const TXT& t, int n, int K, int* steps = nullptr)
+{
+    BandLane<B> L;
+    band_init<B>(L, m, t, n, K);
+    i64 v = 0;
+    while (!band_run8<B>(L, pm, t, &v)) {
+    }
+    if (steps) *steps = L.j < n ? L.j : n;
+    return v;
 }
 
 /* Jaro with P (= s1) of up to 64*W chars and a text of any length: the greedy
@@ -1915,14 +2042,7 @@ RFG_HD void finish_int(const PairSpec& s, const Plan& pl, i64 raw, i64* oi, doub
 }
 
 /* Jaro families.  prefix: common prefix (<= 4) of the two strings. */
-/* The band classes of the band kernel: 32-bit words of window, and the class of a query
- * of m units under a unit-weight Levenshtein chain: the widest Ukkonen band (K + 2
- * diagonals) any pair with a choice of length up to maxlen can need, rounded up to a
- * class, or -1 when that band is not narrower than the pattern (or wider than 512 bits).
- * K comes from plan_int; for n <= m it is K(m) (the maximum is m), and for n >= m it
- * grows by at most one per unit of n (cutoffs in [0, 1] for the normalized ops), so the
- * choices that pass the length filter |m - n| <= K form one run [.., n_last], found by
- * binary search, and K(n_last) is the widest. */
+/* The band classes of the band kernel: 32-bit words of window */
 #define BAND_CLASSES 8
 RFG_HD int band_class_words(int i)
 {
@@ -1930,10 +2050,20 @@ RFG_HD int band_class_words(int i)
     return w[i];
 }
 
-RFG_HD int band_class(int metric, int op, int form, const ScoreParams& sp, u64 ci, double cf, i64 m, i64 maxlen)
+/* The choice lengths whose pairs with a pattern of m units pass the length filter
+ * |m - n| <= K(n) (Levenshtein_impl.hpp:863) for unit-weight Levenshtein: [*nlo, *nhi]
+ * within [1, max(m, maxlen)], and the largest bound *Kmax such a pair gets.  With unit
+ * weights the maximum is max(m, n), so K is one value for every n <= m; for n > m,
+ * K(n) - (n - m) does not grow with n (the distance ops: K(n) = ci or n - ci; the
+ * normalized ops, cutoff c in [0, 1]: K(n) = ceil(fl(n c)) rises by at most 1 per unit
+ * of n, fl being monotone and exact at integers), so the passing n > m form one run
+ * that a binary search ends.  n = 0 never reaches the core.  Returns false when no
+ * pair passes (or the cutoff is outside the range the argument covers). */
+RFG_HD bool band_range(int metric, int op, int form, const ScoreParams& sp, u64 ci, double cf, i64 m, i64 maxlen,
+                       i64* nlo, i64* nhi, i64* Kmax)
 {
-    if (m < 2 || metric != LEVENSHTEIN || sp.ins != 1 || sp.del != 1 || sp.rep != 1 || form == FORM_MULTI) return -1;
-    if ((op == NORM_DISTANCE || op == NORM_SIMILARITY) && !(cf >= 0.0 && cf <= 1.0)) return -1;
+    if (m < 1 || metric != LEVENSHTEIN || sp.ins != 1 || sp.del != 1 || sp.rep != 1 || form == FORM_MULTI) return false;
+    if ((op == NORM_DISTANCE || op == NORM_SIMILARITY) && !(cf >= 0.0 && cf <= 1.0)) return false;
     PairSpec s;
     s.metric = metric;
     s.op = op;
@@ -1954,10 +2084,11 @@ RFG_HD int band_class(int metric, int op, int form, const ScoreParams& sp, u64 c
         return pl.K;
     };
     bool pass = false;
-    i64 Kmax = bound(m, &pass);
-    if (!pass) return -1;
+    const i64 Km = bound(m, &pass);
+    if (!pass) return false;
+    i64 lo = m;
     if (maxlen > m) {
-        i64 lo = m, hi = maxlen; /* lo passes; find the last passing n */
+        i64 hi = maxlen; /* lo passes; find the last passing n */
         while (lo < hi) {
             const i64 mid = lo + (hi - lo + 1) / 2;
             bool p;
@@ -1965,16 +2096,46 @@ RFG_HD int band_class(int metric, int op, int form, const ScoreParams& sp, u64 c
             if (p) lo = mid;
             else hi = mid - 1;
         }
-        bool p;
-        const i64 k2 = bound(lo, &p);
-        if (k2 > Kmax) Kmax = k2;
     }
+    bool p;
+    const i64 Khi = bound(lo, &p);
+    *nlo = m - Km > 1 ? m - Km : 1;
+    *nhi = lo;
+    *Kmax = Khi > Km ? Khi : Km;
+    return true;
+}
+
+/* The band class of a pattern of m units against choices of at most maxlen units: the
+ * index of the narrowest band_class_words width holding Ukkonen's band (about K + 2
+ * diagonals) of every pair that passes the length filter, or -1 when the band is not
+ * narrower than the pattern (or wider than 512 bits). */
+RFG_HD int band_class(int metric, int op, int form, const ScoreParams& sp, u64 ci, double cf, i64 m, i64 maxlen)
+{
+    i64 nlo, nhi, Kmax;
+    if (m < 2 || !band_range(metric, op, form, sp, ci, cf, m, maxlen, &nlo, &nhi, &Kmax)) return -1;
     const i64 bits = Kmax + 2;
     if (Kmax < 0 || bits >= m || bits > 512) return -1;
     const int words = (int)((bits + 31) / 32);
     for (int i = 0; i < BAND_CLASSES; ++i)
         if (band_class_words(i) >= words) return i;
     return -1;
+}
+
+/* The result of every pair of a band-class pattern that fails the length filter (the
+ * chain's value for the pruned distance K + 1, which depends on neither length):
+ * distance K + 1 with K the cutoff (fast: fast_k), similarity 0, normalized distance
+ * 1.0, normalized similarity 0.0 -- the pruned-pair shortcut of dist_chain_finish,
+ * which holds for cutoffs in [0, 1] (band_range refuses others). */
+RFG_HD void band_reject_value(int op, u64 ci, int fast, i64 fast_k, i64* vi, double* vf)
+{
+    *vi = 0;
+    *vf = 0.0;
+    switch (op) {
+    case DISTANCE: *vi = (fast ? fast_k : clamp_bound(ci)) + 1; break;
+    case SIMILARITY: break;
+    case NORM_DISTANCE: *vf = 1.0; break;
+    default: break;
+    }
 }
 
 RFG_HD double jaro_cutoff_for(const PairSpec& s, i64 prefix)

@@ -27,6 +27,11 @@ struct HostPM {
     u64 operator()(u64 c) const { return row[c & 255]; }
 };
 
+struct Txt8 {
+    const uint8_t* p;
+    u64 operator[](int j) const { return p[j]; }
+};
+
 struct CountingText {
     const uint8_t* p;
     uint64_t* fetched;
@@ -169,20 +174,22 @@ int rfg_count_band_steps(int op, uint64_t ci, double cf, const uint8_t* qd, cons
                     if (!pl.run || n == 0) continue;
                     const i64 K = pl.K, diff = m > n ? m - n : n - m;
                     if (K < diff || K >= m) continue;
-                    uint64_t f = 0;
-                    const CountingText txt{cd + co[c], &f};
+                    int st = 0;
+                    const Txt8 txt{cd + co[c]};
                     switch (B) {
-                    case 1: lev_band32<1>(pm, m, txt, n, (int)K); break;
-                    case 2: lev_band32<2>(pm, m, txt, n, (int)K); break;
-                    case 3: lev_band32<3>(pm, m, txt, n, (int)K); break;
-                    case 4: lev_band32<4>(pm, m, txt, n, (int)K); break;
-                    case 6: lev_band32<6>(pm, m, txt, n, (int)K); break;
-                    case 8: lev_band32<8>(pm, m, txt, n, (int)K); break;
-                    case 12: lev_band32<12>(pm, m, txt, n, (int)K); break;
-                    default: lev_band32<16>(pm, m, txt, n, (int)K); break;
+                    case 1: lev_band32<1>(pm, m, txt, n, (int)K, &st); break;
+                    case 2: lev_band32<2>(pm, m, txt, n, (int)K, &st); break;
+                    case 3: lev_band32<3>(pm, m, txt, n, (int)K, &st); break;
+                    case 4: lev_band32<4>(pm, m, txt, n, (int)K, &st); break;
+                    case 6: lev_band32<6>(pm, m, txt, n, (int)K, &st); break;
+                    case 8: lev_band32<8>(pm, m, txt, n, (int)K, &st); break;
+                    case 12: lev_band32<12>(pm, m, txt, n, (int)K, &st); break;
+                    default: lev_band32<16>(pm, m, txt, n, (int)K, &st); break;
                     }
-                    pe[w] += f * (uint64_t)B;
-                    pa[w] += f * (uint64_t)((band_bits((int)K, m - n) + 31) / 32);
+                    /* the steps the kernel runs: every unit up to the end of the 8-unit
+                     * block at which the pair ends */
+                    pe[w] += (uint64_t)st * (uint64_t)B;
+                    pa[w] += (uint64_t)st * (uint64_t)((band_bits((int)K, m - n) + 31) / 32);
                     ++pp[w];
                 }
             }

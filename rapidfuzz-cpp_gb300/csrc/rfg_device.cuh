@@ -28,6 +28,13 @@ struct KStrings {
     int width;
 };
 
+/* one query of a band launch: its first work unit, its passing choices [plo, phi) in
+ * the length order of the choices (the lengths [nlo, nhi]), its index; the record after
+ * a launch's last query holds the launch's unit count in ustart */
+struct BandQuery {
+    int32_t ustart, plo, phi, nlo, nhi, qi, pad0, pad1;
+};
+
 struct KParams {
     KStrings q, c;
     const int32_t* qlist; /* queries of this launch (size class), longest first */
@@ -93,6 +100,8 @@ struct KParams {
      * 16-byte boundary */
     const int4* prec;
     int vec;
+    /* band launches: the queries' records (BandQuery) */
+    const BandQuery* band_q;
 };
 
 /* editops of many pairs (k_editops): one operation, laid out as rfg_editop */

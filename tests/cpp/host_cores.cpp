@@ -188,6 +188,49 @@ int64_t hc_band32(int B, const uint8_t* a, int m, const uint8_t* b, int n, int64
     return -2;
 }
 
+/* band launches' host logic: band_range (the passing choice lengths of a pattern of m
+ * units, unit-weight Levenshtein, op / ci / cf the chain) and band_reject_value; and one
+ * pair's plan as the band kernel makes it: *pass = the pair reaches the core, else
+ * (vi, vf) = the chain's value of the pruned pair */
+int hc_band_range(int op, uint64_t ci, double cf, int64_t m, int64_t maxlen, int64_t* nlo, int64_t* nhi,
+                  int64_t* kmax)
+{
+    ScoreParams sp;
+    sp.ins = sp.del = sp.rep = 1;
+    sp.prefix_weight = 0.1;
+    return band_range(LEVENSHTEIN, op, FORM_CACHED, sp, ci, cf, m, maxlen, nlo, nhi, kmax) ? 1 : 0;
+}
+
+void hc_band_reject(int op, uint64_t ci, int64_t* vi, double* vf)
+{
+    const int fast = op == DISTANCE;
+    band_reject_value(op, ci, fast, clamp_bound(ci), vi, vf);
+}
+
+void hc_band_pair(int op, uint64_t ci, double cf, int64_t m, int64_t n, int* pass, int64_t* vi, double* vf)
+{
+    PairSpec s;
+    s.metric = LEVENSHTEIN;
+    s.op = op;
+    s.form = FORM_CACHED;
+    s.ci = ci;
+    s.cf = cf;
+    s.p.ins = s.p.del = s.p.rep = 1;
+    s.p.prefix_weight = 0.1;
+    s.l1 = (u64)m;
+    s.l2 = (u64)n;
+    const Plan pl = plan_int(s);
+    const i64 K = pl.run ? pl.K : -1;
+    const i64 diff = m > n ? m - n : n - m;
+    *pass = K >= 0 && m > 0 && n > 0 && K >= diff;
+    i64 raw = 0;
+    if (K >= 0) raw = m == 0 ? n : n == 0 ? m : K + 1;
+    *vi = 0;
+    *vf = 0.0;
+    if (op == DISTANCE) *vi = raw <= (i64)clamp_bound(ci) ? raw : clamp_bound(ci) + 1;
+    else finish_int(s, pl, raw, vi, vf);
+}
+
 /* the warp tiles' core (fast_group, int bookkeeping, one cutoff K for every pattern) on
  * four patterns (packed, offsets off[0..4]) of at most 64 units (32 with word32) against
  * one text; qn of the four slots are used; out[q] = the distance chain of pattern q */

@@ -35,6 +35,12 @@ def libs():
     lib.hc_group.argtypes = [I, I, P, I, P, I, P, I, I64, I64, P]
     lib.hc_band32.restype = I64
     lib.hc_band32.argtypes = [I, P, I, P, I, I64]
+    lib.hc_band_range.restype = I
+    lib.hc_band_range.argtypes = [I, ctypes.c_uint64, ctypes.c_double, I64, I64, P, P, P]
+    lib.hc_band_reject.restype = None
+    lib.hc_band_reject.argtypes = [I, ctypes.c_uint64, P, P]
+    lib.hc_band_pair.restype = None
+    lib.hc_band_pair.argtypes = [I, ctypes.c_uint64, ctypes.c_double, I64, I64, P, P, P]
     lib.hc_fast.restype = I
     lib.hc_fast.argtypes = [I, I, P, P, I, P, I, I, P]
     lib.hc_jaro.restype = I
@@ -163,6 +169,53 @@ def test_band32_core_matches_oracle(libs):
                 assert (got == d) if d <= K else (got > K), (B, K, len(a), len(b), got, d)
                 checked += 1
     assert checked > 2000
+
+
+def test_band_ranges_and_rejected_values(libs):
+    """the band launches' split of a query's pairs: the choice lengths that pass the
+    length filter are exactly band_range's [nlo, nhi] (so a query's passing pairs are one
+    run of the length-sorted choices), and every other pair's value is band_reject_value,
+    for all four ops and cutoffs from 0 to 1 (checked against the per-pair plan at every
+    length up to maxlen)"""
+    lib, _ = libs
+    rng = np.random.default_rng(91)
+    D, S, ND, NS = 0, 1, 2, 3
+    lo, hi, km = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    ps, vi, vf = ctypes.c_int(), ctypes.c_int64(), ctypes.c_double()
+    rvi, rvf = ctypes.c_int64(), ctypes.c_double()
+    cases = 0
+    for _ in range(400):
+        op = int(rng.integers(0, 4))
+        m = int(rng.choice([1, 2, 65, 100, 257, 300, 1000, 2000]))
+        maxlen = int(rng.choice([0, 1, m // 2, m, m + 5, 2 * m, 3000]))
+        if op in (ND, NS):
+            cf = float(rng.choice([0.0, 0.01, 0.05, 0.1, 0.1 + 1e-9, 0.18, 0.3, 0.5, 0.9, 0.99, 1.0]))
+            ci = 0
+        else:
+            ci = int(rng.choice([0, 1, 5, 30, m // 2, m, m + 3, 2**40]))
+            cf = 0.0
+        ok = lib.hc_band_range(op, ci, cf, m, maxlen, ctypes.byref(lo), ctypes.byref(hi), ctypes.byref(km))
+        lib.hc_band_reject(op, ci, ctypes.byref(rvi), ctypes.byref(rvf))
+        # the band classes take patterns whose band (Kmax + 2 bits) is narrower than m
+        band = ok and km.value + 2 < m
+        passing = []
+        for n in range(0, max(m, maxlen) + 1):
+            lib.hc_band_pair(op, ci, cf, m, n, ctypes.byref(ps), ctypes.byref(vi), ctypes.byref(vf))
+            if ps.value:
+                passing.append(n)
+            elif not band:
+                continue
+            elif op in (D, S):
+                assert vi.value == rvi.value, (op, ci, m, n, vi.value, rvi.value)
+            else:
+                assert vf.value == rvf.value, (op, cf, m, n, vf.value, rvf.value)
+        if not ok:
+            assert not passing, (op, ci, cf, m, maxlen)
+            continue
+        expect = [n for n in range(0, max(m, maxlen) + 1) if lo.value <= n <= hi.value]
+        assert passing == expect, (op, ci, cf, m, maxlen, lo.value, hi.value)
+        cases += band
+    assert cases > 100
 
 
 def test_jaro_cores_match_oracle(libs):
