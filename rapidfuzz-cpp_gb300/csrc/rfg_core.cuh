@@ -957,6 +957,17 @@ RFG_HD int band_lo(int K, int delta) { return -((K - delta + 1) >> 1); }
 RFG_HD int band_hi(int K, int delta) { return (K + delta + 1) >> 1; }
 RFG_HD int band_bits(int K, int delta) { return band_hi(K, delta) - band_lo(K, delta) + 1; }
 
+/* units of window loads run ahead of the band recurrence in a whole block (about 32
+ * registers of windows) */
+#define BAND_AHEAD(B) ((B) <= 4 ? 8 / ((B) + 1 >> 1) : (B) <= 8 ? 4 : 2)
+
+/* a hint that text unit j will be read soon (the band kernel's texts override it with a
+ * cache prefetch); j is a valid index */
+template <typename TXT>
+RFG_HD void text_prefetch(const TXT&, int)
+{
+}
+
 /* s = a + b over B 32-bit words, the carry out of the top word dropped: on the GPU one
  * add.cc / addc chain (the carry passes in the condition code, one instruction a word) */
 template <int B>
@@ -1095,19 +1106,32 @@ RFG_HD bool band_run8(BandLane<B>& L, const PM32& pm, const TXT& t, i64* out)
 {
     const int last = L.n - 1;
     u32 nx[8];
+    if (L.j + 16 <= L.n) {
 #pragma unroll
-    for (int s = 0; s < 8; ++s) {
-        const int k = L.j + 8 + s;
-        nx[s] = (u32)t[k < last ? k : last];
+        for (int s = 0; s < 8; ++s) nx[s] = (u32)t[L.j + 8 + s];
     }
-    const int rem = L.n - L.j;
-    if (rem >= 8) { /* a whole block: straight-line code, the loads of later units run ahead */
+    else {
 #pragma unroll
         for (int s = 0; s < 8; ++s) {
-            const u32 c = (L.cur[s >> 2] >> (8 * (s & 3))) & 0xffu;
-            u32 X[B];
-            band_window<B>(pm(c), L.start + s, X);
-            band_step<B>(L, X);
+            const int k = L.j + 8 + s;
+            nx[s] = (u32)t[k < last ? k : last];
+        }
+    }
+    text_prefetch(t, L.j + 64 < last ? L.j + 64 : last);
+    const int rem = L.n - L.j;
+    if (rem >= 8) {
+        /* a whole block: straight-line code whose windows are loaded BAND_AHEAD units
+         * before their step (they depend on the text alone, not on the recurrence) */
+        constexpr int AH = BAND_AHEAD(B);
+        u32 X[8][B];
+#pragma unroll
+        for (int s = 0; s < AH; ++s) band_window<B>(pm((L.cur[s >> 2] >> (8 * (s & 3))) & 0xffu), L.start + s, X[s]);
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            if (s + AH < 8)
+                band_window<B>(pm((L.cur[(s + AH) >> 2] >> (8 * ((s + AH) & 3))) & 0xffu), L.start + s + AH,
+                               X[s + AH < 8 ? s + AH : 0]);
+            band_step<B>(L, X[s]);
         }
     }
     else {
