@@ -459,6 +459,7 @@ int g_fast_mode = 1;        /* unit-weight one-word distances run on the warp ti
  * memory a band CTA takes at most (warps x slice) */
 #define RFG_BAND_MAX_TABLE (48 * 1024)
 #define RFG_BAND_MAX_SMEM (96 * 1024)
+int g_count_filter = 1; /* the warp tiles' count filter (hist_lower_bound) */
 int g_band_rounds = 0; /* band units of 32 x this many pairs (0: sized by the class; autotuning) */
 int g_band_mode = 1;        /* unit-weight Levenshtein with a band narrower than the pattern runs on k_band */
 int64_t g_fast_window = 512; /* choice positions per warp window of k_fast (autotuning) */
@@ -489,7 +490,7 @@ struct LaunchRec {
 
 struct Prepared {
     std::vector<LaunchRec> launches;
-    DBuf packed, small, scratch[1], jtab;
+    DBuf packed, small, scratch[1], jtab, chist;
     /* in `packed` (one upload): the query lists of the classes, the choice visiting order
      * and the choices' offsets and lengths in that order (these two: dense results only) */
     const int32_t* qlist = nullptr;
@@ -502,6 +503,8 @@ struct Prepared {
     /* which kinds of launches the preparation holds (what the tuner has to sweep) */
     bool has_fast = false, has_band = false, has_tiles = false;
     bool has_pre = false; /* pre.a / grid: the per-query table pass before the row blocks */
+    bool has_hist = false; /* hist: the choices' count histograms before the warp tiles */
+    KParams hist{};
     KParams pre;
     int* counters = nullptr;
     int* err = nullptr;
@@ -515,7 +518,7 @@ struct Prepared {
     Prepared& operator=(const Prepared&) = delete;
     void free_on(cudaStream_t st)
     {
-        packed.free_on = small.free_on = scratch[0].free_on = jtab.free_on = st;
+        packed.free_on = small.free_on = scratch[0].free_on = jtab.free_on = chist.free_on = st;
     }
 };
 
@@ -918,6 +921,17 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
             a.fast_k = clamp_bound(spec.ci);
             const size_t esz = spec.out_dtype == RFG_I32 ? 4 : 8;
             a.vec = ((uintptr_t)spec.out % 16 == 0) && ((spec.ld * (int64_t)esz) % 16 == 0) && (fwin * (int64_t)esz) % 16 == 0;
+            /* the count filter, below cutoffs at which a 64-unit pattern's bound can
+             * still exceed K (its histograms, one pass over the choices, run first) */
+            if (g_count_filter && a.fast_k < 2 * RFG_HIST_MAXLEN) {
+                if (!pb->chist.p) {
+                    RFG_TRY(pb->chist.alloc((size_t)std::max<int64_t>(nc, 1) * 32));
+                    pb->hist = a;
+                    pb->has_hist = true;
+                }
+                a.chist = pb->chist.as<uint4>();
+                a.cfilter = 1;
+            }
             const std::vector<int32_t>& v = cls[bk];
             int64_t nlong = 0;
             while (nlong < (int64_t)v.size() && q.len[v[nlong]] > 32) ++nlong;
@@ -1165,6 +1179,13 @@ rfg_status enqueue_block(Prepared& pb, int b, cudaStream_t st)
 /* the per-query table pass that the row blocks read */
 rfg_status enqueue_pre(Prepared& pb, cudaStream_t st)
 {
+    if (pb.has_hist && pb.hist.c.n > 0) {
+        KParams h = pb.hist;
+        uint4* out = pb.chist.as<uint4>();
+        void* hargs[] = {&h, &out};
+        const unsigned hgrid = (unsigned)std::min<int64_t>((h.c.n + RFG_HIST_WARPS - 1) / RFG_HIST_WARPS, (int64_t)g.sms * 8);
+        RFG_CUDA(cudaLaunchKernel(fast_hist_kernel(), dim3(hgrid), dim3(RFG_HIST_WARPS * 32), hargs, 0, st));
+    }
     if (!pb.has_pre || pb.pre.q.n == 0) return RFG_OK;
     KParams a = pb.pre;
     JaroTab* out = pb.jtab.as<JaroTab>();
@@ -2880,6 +2901,7 @@ rfg_status rfg_batch_kernels(rfg_batch b, char* names, size_t cap)
         all += nm;
     };
     if (b->pb->has_pre) add(jaro_tables_kernel());
+    if (b->pb->has_hist) add(fast_hist_kernel());
     for (const LaunchRec& L : b->pb->launches) add(L.fn);
     if (all.size() + 1 > cap) return fail(RFG_ERR_INVALID_ARGUMENT, "buffer too small (%zu bytes needed)", all.size() + 1);
     memcpy(names, all.c_str(), all.size() + 1);

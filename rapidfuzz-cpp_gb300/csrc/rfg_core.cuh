@@ -460,19 +460,53 @@ RFG_HD int popc_w(u32 x)
 #endif
 }
 
+/* Count filter of the distance fast path.  A string's code units counted in 32 buckets
+ * (unit & 31), one byte each, four to a 32-bit word (strings of at most 255 units).
+ * Indel distance >= sum_b |cnt_a(b) - cnt_b(b)| (an insertion or a deletion changes one
+ * count by one); Levenshtein and OSA distance >= (that sum + |m - n|) / 2 (a substitution
+ * moves one unit between two counts, an insertion or deletion changes one count, a
+ * transposition none: the units a must lose and gain are each at most d).  Merging units
+ * into buckets only lowers the sum, so the bound holds for any code units.  A pair whose
+ * bound exceeds the cutoff K has distance > K: the chain's value is K + 1, as the
+ * recurrence would give. */
+#define RFG_HIST_MAXLEN 255
+
+RFG_HD u32 sad4(u32 a, u32 b)
+{
+#ifdef __CUDA_ARCH__
+    return __vsadu4(a, b);
+#else
+    u32 s = 0;
+    for (int k = 0; k < 4; ++k) {
+        const int x = (int)((a >> (8 * k)) & 0xffu), y = (int)((b >> (8 * k)) & 0xffu);
+        s += (u32)(x > y ? x - y : y - x);
+    }
+    return s;
+#endif
+}
+
+RFG_HD int hist_lower_bound(int fam, const u32* ha, const u32* hb, int m, int n)
+{
+    int s = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) s += (int)sad4(ha[w], hb[w]);
+    return fam == FAM_LCS ? s : (s + (m > n ? m - n : n - m)) >> 1;
+}
+
 /* The unit-weight distance chain d <= K ? d : K + 1 of Q one-word patterns against one
  * text, for the warp tiles of the distance fast path: Levenshtein 1/1/1 (Hyyro 2003,
  * Levenshtein_impl.hpp:259-322), OSA (OSA_impl.hpp:34-74) or Indel (d = m + n - 2 LCS,
  * LCSseq_impl.hpp:205-260), with the length filter and empty-string rules of those
  * functions (Levenshtein_impl.hpp:863, LCSseq_impl.hpp:389) and the diagonal lower-bound
- * exit every 8 text units, so every d equals the single-pair result.  Lengths and K are
+ * exit every 8 text units, so every d equals the single-pair result; patterns in `skip`
+ * (their count bound exceeds K: hist_lower_bound) take K + 1 without running.  Lengths and K are
  * below 2^31 (int bookkeeping: every 64-bit integer operation costs two ALU instructions
  * on the GPU).  pm(q, c): pattern word of pattern q for table row c (t[j] gives rows);
  * m[q] <= bits of WT.  The LCS step S' = (S + u) | (S - u) with u = S & X is written as
  * (S + u) | (S & ~X): u is a subset of S, so S - u = S & ~X, which a single three-input
  * logic instruction merges with the OR. */
 template <int FAM, int Q, typename PMQ, typename TXT, typename WT>
-RFG_HD void fast_group(const PMQ& pm, const int* m, int qn, const TXT& t, int n, int K, int* d)
+RFG_HD void fast_group(const PMQ& pm, const int* m, int qn, const TXT& t, int n, int K, int* d, unsigned skip = 0)
 {
     WT A[Q], B[Q], D0[Q], PO[Q]; /* Lev / OSA: VP, VN, D0, previous X; Indel: S in A */
     unsigned live = 0, chk = 0; /* chk: the cutoff is below the largest possible distance */
@@ -486,7 +520,7 @@ RFG_HD void fast_group(const PMQ& pm, const int* m, int qn, const TXT& t, int n,
         const int diff = mq > n ? mq - n : n - mq;
         if (FAM == FAM_LCS) {
             if (mq == 0 || n == 0) d[q] = mq + n;
-            else if (K < diff) d[q] = K + 1;
+            else if (K < diff || ((skip >> q) & 1u)) d[q] = K + 1;
             else {
                 live |= 1u << q;
                 if (K < mq + n) chk |= 1u << q;
@@ -496,6 +530,7 @@ RFG_HD void fast_group(const PMQ& pm, const int* m, int qn, const TXT& t, int n,
             if (mq == 0) d[q] = n;
             else if (K < diff) d[q] = K + 1;
             else if (n == 0) d[q] = mq;
+            else if ((skip >> q) & 1u) d[q] = K + 1;
             else {
                 live |= 1u << q;
                 if (K < (mq > n ? mq : n)) chk |= 1u << q;

@@ -47,15 +47,32 @@ struct HostPMQ {
     u64 operator()(int, unsigned c) const { return row[c]; }
 };
 
+/* a string's count histogram (hist_lower_bound), for strings of at most
+ * RFG_HIST_MAXLEN units */
+void host_hist(const uint8_t* s, int n, u32* h)
+{
+    unsigned char b[32] = {0};
+    if (n <= RFG_HIST_MAXLEN)
+        for (int i = 0; i < n; ++i) ++b[s[i] & 31];
+    for (int w = 0; w < 8; ++w) h[w] = (u32)b[4 * w] | (u32)b[4 * w + 1] << 8 | (u32)b[4 * w + 2] << 16 | (u32)b[4 * w + 3] << 24;
+}
+
 /* the unit-weight distance fast path of the warp tiles (fast_group, one query, the word
- * width of the query's launch: 32 bits for patterns of at most 32 units) */
-uint64_t pair_steps(int metric, const HostPM& pm, int m, const uint8_t* t, int n, int K)
+ * width of the query's launch: 32 bits for patterns of at most 32 units), with the count
+ * filter the tiles apply below cutoffs of 2 * RFG_HIST_MAXLEN */
+uint64_t pair_steps(int metric, const HostPM& pm, int m, const uint8_t* t, int n, int K, const u32* hq)
 {
     uint64_t f = 0;
     const CountingText txt{t, &f};
     const HostPMQ pq{pm.row};
     const int mm[1] = {m};
     int d[1];
+    if (K < 2 * RFG_HIST_MAXLEN && n <= RFG_HIST_MAXLEN) {
+        u32 hc[8];
+        host_hist(t, n, hc);
+        const int diff = m > n ? m - n : n - m;
+        if (m > 0 && n > 0 && K >= diff && hist_lower_bound(metric == 1 ? FAM_LCS : FAM_LEV, hq, hc, m, n) > K) return 0;
+    }
     if (m <= 32) {
         if (metric == 1) fast_group<FAM_LCS, 1, HostPMQ, CountingText, u32>(pq, mm, 1, txt, n, K, d);
         else if (metric == 3) fast_group<FAM_OSA, 1, HostPMQ, CountingText, u32>(pq, mm, 1, txt, n, K, d);
@@ -98,9 +115,11 @@ int rfg_count_word_steps2(int metric, const uint8_t* qd, const int64_t* qo, int6
                 const int m = (int)(qo[qi + 1] - qo[qi]);
                 std::fill(pm.row, pm.row + 256, 0ull);
                 for (int k = 0; k < m; ++k) pm.row[qd[qo[qi] + k]] |= 1ull << k;
+                u32 hq[8];
+                host_hist(qd + qo[qi], m, hq);
                 uint64_t acc = 0;
                 for (int64_t c = 0; c < nc; ++c)
-                    acc += pair_steps(metric, pm, m, cd + co[c], (int)(co[c + 1] - co[c]), K);
+                    acc += pair_steps(metric, pm, m, cd + co[c], (int)(co[c + 1] - co[c]), K, hq);
                 (m <= 32 ? a32 : a64) += acc;
             }
             p64[w] = a64;

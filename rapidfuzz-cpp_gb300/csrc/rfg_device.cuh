@@ -100,6 +100,10 @@ struct KParams {
      * 16-byte boundary */
     const int4* prec;
     int vec;
+    /* warp tiles: per visiting position the choice's count histogram (two uint4,
+     * hist_lower_bound), and whether the count filter runs (cfilter) */
+    const uint4* chist;
+    int cfilter;
     /* band launches: the queries' records (BandQuery) */
     const BandQuery* band_q;
 };

@@ -11,8 +11,9 @@
  *      filter |m - n| <= K (Levenshtein_impl.hpp:863, LCSseq_impl.hpp:389);
  *   2. finds, with two warp-wide votes, the visiting positions whose lengths can pass for
  *      some query of the group -- windows are sorted by choice length, so they form one
- *      run -- and scores only those, one choice per lane against the Q queries
- *      (fast_group);
+ *      run -- puts them through the length filter and the count filter
+ *      (hist_lower_bound, below cutoffs where it can prune), and scores the survivors
+ *      gathered 32 at a time, one choice per lane against the Q queries (fast_group);
  *   3. writes the window's Q result rows with 16-byte stores.
  * No barrier of the whole CTA is ever taken (only __syncwarp), so a warp that meets
  * short or quickly pruned choices moves on to the next task at once.
@@ -36,13 +37,47 @@ namespace rfg {
 #define RFG_FAST_MINB 8 /* CTAs per SM the register budget is sized for (64 registers) */
 #endif
 
-/* bytes of one warp's slice: tables, then the result stage (16-bit results when every
- * value the chain can give, at most K + 1, fits in 16 bits; else 32-bit) */
+/* bytes of one warp's slice: tables, the patterns' count histograms (32 bytes each),
+ * then the result stage (16-bit results when every value the chain can give, at most
+ * K + 1, fits in 16 bits; else 32-bit) */
 __host__ __device__ inline size_t fast_pm_bytes(int Q, bool half) { return ((size_t)Q * 257 * (half ? 4 : 8) + 15) / 16 * 16; }
+__host__ __device__ inline size_t fast_hist_bytes(int Q) { return (size_t)Q * 32; }
 __host__ __device__ inline size_t fast_stage_bytes(int Q, int64_t window, bool s16) { return (size_t)Q * window * (s16 ? 2 : 4); }
 inline size_t fast_smem_bytes(int Q, bool half, int64_t window, bool s16)
 {
-    return (size_t)RFG_FAST_WARPS * (fast_pm_bytes(Q, half) + fast_stage_bytes(Q, window, s16));
+    return (size_t)RFG_FAST_WARPS * (fast_pm_bytes(Q, half) + fast_hist_bytes(Q) + fast_stage_bytes(Q, window, s16));
+}
+
+/* the count histograms of the choices in visiting order, before the warp tiles of a
+ * launch: 32 buckets of one byte, for choices of at most RFG_HIST_MAXLEN units (longer
+ * choices get zeros and are never filtered).  One warp a choice: lanes holding units of
+ * one bucket find each other and the lowest adds their number to the bucket's byte. */
+#define RFG_HIST_WARPS 8
+static __global__ void __launch_bounds__(RFG_HIST_WARPS * 32) k_fast_hist(const KParams a, uint4* out)
+{
+    __shared__ u32 cnt[RFG_HIST_WARPS][8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned char* b = (unsigned char*)cnt[warp];
+    for (int64_t p = (int64_t)blockIdx.x * RFG_HIST_WARPS + warp; p < a.c.n; p += (int64_t)gridDim.x * RFG_HIST_WARPS) {
+        if (lane < 8) cnt[warp][lane] = 0;
+        __syncwarp();
+        const int4 r = __ldg(a.prec + p);
+        const int64_t o0 = (int64_t)(((uint64_t)(uint32_t)r.y << 32) | (uint32_t)r.x);
+        if (r.z <= RFG_HIST_MAXLEN) {
+            const unsigned char* cb = a.c.data + o0 * a.c.width;
+            for (int i0 = 0; i0 < r.z; i0 += 32) {
+                const int i = i0 + lane;
+                const int bkt = i < r.z ? (int)(load_unit(cb, a.c.width, i) & 31) : -1;
+                const unsigned same = __match_any_sync(0xffffffffu, bkt);
+                if (bkt >= 0 && lane == __ffs(same) - 1) b[bkt] += (unsigned char)__popc(same);
+                __syncwarp();
+            }
+        }
+        if (lane < 2)
+            out[2 * p + lane] = make_uint4(cnt[warp][4 * lane], cnt[warp][4 * lane + 1], cnt[warp][4 * lane + 2],
+                                           cnt[warp][4 * lane + 3]);
+        __syncwarp();
+    }
 }
 
 template <typename WT>
@@ -50,6 +85,22 @@ struct FastRows {
     const WT* rows;
     __device__ __forceinline__ WT operator()(int q, unsigned c) const { return rows[q * 257 + c]; }
 };
+
+/* the position of the n-th (from 0) set bit of m (n < popc(m)) */
+__device__ __forceinline__ int select_bit(unsigned m, int n)
+{
+    int pos = 0;
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+        const int c = __popc(m & ((1u << w) - 1u));
+        if (n >= c) {
+            n -= c;
+            m >>= w;
+            pos += w;
+        }
+    }
+    return pos;
+}
 
 /* first position p of [0, nn) with lens[4 p] >= L (lens ascending; nn <= 1024), by the
  * whole warp: one sampled length per lane, then the 32-position run the answer lies in */
@@ -100,9 +151,10 @@ __global__ void __launch_bounds__(RFG_FAST_WARPS * 32, RFG_FAST_MINB) k_fast(con
     const int K = (int)(a.fast_k < 0x7fffffff ? a.fast_k : 0x7fffffff);
     const bool s16 = K < 0xffff;
     const size_t pmb = fast_pm_bytes(Q, HALF);
-    unsigned char* slice = (unsigned char*)smem + (size_t)warp * (pmb + fast_stage_bytes(Q, win, s16));
+    unsigned char* slice = (unsigned char*)smem + (size_t)warp * (pmb + fast_hist_bytes(Q) + fast_stage_bytes(Q, win, s16));
     WT* rows = (WT*)slice;
-    unsigned char* stage = slice + pmb;
+    u32* qh = (u32*)(slice + pmb); /* pattern q's histogram: words 8q .. 8q + 7 */
+    unsigned char* stage = slice + pmb + fast_hist_bytes(Q);
     /* the host keeps tasks and windows below 2^31 */
     const int nwin = (int)a.nchunks;
     const int ntasks = (int)(((int64_t)a.nq + Q - 1) / Q * nwin);
@@ -149,6 +201,25 @@ __global__ void __launch_bounds__(RFG_FAST_WARPS * 32, RFG_FAST_MINB) k_fast(con
                     fast_rows<WT, true>(rows, q, a, qi[q], mq, lane);
                 }
             }
+            if (a.cfilter) {
+                /* the group's count histograms: lanes holding units of one bucket find
+                 * each other; the lowest adds their number to the bucket's byte */
+                for (int i = lane; i < Q * 8; i += 32) qh[i] = 0;
+                __syncwarp();
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    if (q >= qn) break;
+                    const unsigned char* qb = a.q.data + a.q.off[qi[q]] * a.q.width;
+#pragma unroll
+                    for (int h = 0; h < (HALF ? 1 : 2); ++h) {
+                        const int i = lane + 32 * h;
+                        const int bkt = i < m[q] ? (int)(load_unit(qb, a.q.width, i) & 31) : -1;
+                        const unsigned same = __match_any_sync(0xffffffffu, bkt);
+                        if (bkt >= 0 && lane == __ffs(same) - 1) ((unsigned char*)qh)[32 * q + bkt] += (unsigned char)__popc(same);
+                        __syncwarp();
+                    }
+                }
+            }
             __syncwarp();
             cur_g = g;
         }
@@ -168,24 +239,82 @@ __global__ void __launch_bounds__(RFG_FAST_WARPS * 32, RFG_FAST_MINB) k_fast(con
             for (int i = lane * 4; i < words; i += 128) *(int4*)((unsigned*)stage + i) = f;
         }
         __syncwarp();
-        /* the next position's record is loaded while the current one is scored */
+        /* every visiting position goes through the length and count filters; the pairs
+         * that survive wait in a lane each (position and skip mask) and are scored
+         * together once up to 32 wait, so the recurrence runs with full warps rather
+         * than for the one or two survivors of each 32 positions.  The next position's
+         * record is loaded while the current one is filtered. */
+        int pend = -1;          /* this lane's waiting position, or -1 */
+        unsigned pend_skip = 0; /* its patterns whose bound exceeds K */
+        auto run_pending = [&]() {
+            if (!__any_sync(0xffffffffu, pend >= 0)) return;
+            if (pend >= 0) {
+                const int4 r = __ldg(a.prec + p0 + pend);
+                const int64_t o0 = (int64_t)(((uint64_t)(uint32_t)r.y << 32) | (uint32_t)r.x);
+                int d[Q];
+                fast_group<FAM, Q, FastRows<WT>, MQText<CT>, WT>(FastRows<WT>{rows}, m, qn,
+                                                                 MQText<CT>{(const CT*)a.c.data + o0}, r.z, K, d,
+                                                                 pend_skip);
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    if (q >= qn) break;
+                    const int at = q * win + r.w;
+                    if (s16) ((unsigned short*)stage)[at] = (unsigned short)d[q];
+                    else ((unsigned*)stage)[at] = (unsigned)d[q];
+                }
+            }
+            pend = -1;
+        };
         int4 rn = make_int4(0, 0, 0, 0);
         if (lo + lane < hi) rn = __ldg(a.prec + p0 + lo + lane);
-        for (int p = lo + lane; p < hi; p += 32) {
+        for (int b0 = lo; b0 < hi; b0 += 32) {
+            const int p = b0 + lane;
             const int4 r = rn;
             if (p + 32 < hi) rn = __ldg(a.prec + p0 + p + 32);
-            const int64_t o0 = (int64_t)(((uint64_t)(uint32_t)r.y << 32) | (uint32_t)r.x);
-            int d[Q];
-            fast_group<FAM, Q, FastRows<WT>, MQText<CT>, WT>(FastRows<WT>{rows}, m, qn,
-                                                             MQText<CT>{(const CT*)a.c.data + o0}, r.z, K, d);
+            bool surv = false;
+            unsigned skip = 0;
+            if (p < hi) {
+                /* patterns the length filter lets through, less those whose count bound
+                 * exceeds K (they keep the stage's K + 1) */
+                unsigned live = 0;
 #pragma unroll
-            for (int q = 0; q < Q; ++q) {
-                if (q >= qn) break;
-                const int at = q * win + r.w;
-                if (s16) ((unsigned short*)stage)[at] = (unsigned short)d[q];
-                else ((unsigned*)stage)[at] = (unsigned)d[q];
+                for (int q = 0; q < Q; ++q) {
+                    const int diff = m[q] > r.z ? m[q] - r.z : r.z - m[q];
+                    if (q < qn && diff <= K) live |= 1u << q;
+                }
+                if (a.cfilter && live && r.z <= RFG_HIST_MAXLEN) {
+                    const int64_t vp = p0 + p;
+                    const uint4 h0 = __ldg(a.chist + 2 * vp), h1 = __ldg(a.chist + 2 * vp + 1);
+                    const u32 hc[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+#pragma unroll
+                    for (int q = 0; q < Q; ++q) {
+                        if (!((live >> q) & 1u)) continue;
+                        const uint4 g0 = *(const uint4*)(qh + 8 * q), g1 = *(const uint4*)(qh + 8 * q + 4);
+                        const u32 hq[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
+                        if (hist_lower_bound(FAM, hq, hc, m[q], r.z) > K) skip |= 1u << q;
+                    }
+                }
+                surv = (live & ~skip) != 0;
+            }
+            const unsigned sm = __ballot_sync(0xffffffffu, surv);
+            if (!sm) continue;
+            unsigned idle = __ballot_sync(0xffffffffu, pend < 0);
+            if (__popc(sm) > __popc(idle)) {
+                run_pending();
+                idle = 0xffffffffu;
+            }
+            /* the k-th survivor waits in the k-th idle lane */
+            const int rank = __popc(idle & ((1u << lane) - 1));
+            const bool take = ((idle >> lane) & 1u) && rank < __popc(sm);
+            const int src = take ? select_bit(sm, rank) : lane;
+            const int sp = __shfl_sync(0xffffffffu, p, src);
+            const unsigned ss = __shfl_sync(0xffffffffu, skip, src);
+            if (take) {
+                pend = sp;
+                pend_skip = ss;
             }
         }
+        run_pending();
         __syncwarp();
         /* the window's rows, converted to the output type: 16-byte stores where the row
          * segment is aligned */

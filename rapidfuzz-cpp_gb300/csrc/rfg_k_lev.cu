@@ -54,6 +54,8 @@ static const void* pick_fast_lev(bool half)
     return half ? (const void*)&k_fast<FAM_LEV, CT, 2, true> : (const void*)&k_fast<FAM_LEV, CT, 2, false>;
 }
 
+const void* fast_hist_kernel() { return (const void*)&k_fast_hist; }
+
 const void* fast_kernel_lev(int width, bool half)
 {
     switch (width) {

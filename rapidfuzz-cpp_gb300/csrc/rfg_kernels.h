@@ -17,6 +17,8 @@ const void* tiles_mq_kernel_osa(int width, bool norm, bool half);
 /* k_fast<FAM, CT, Q, HALF> (unit-weight distances of one-word patterns, warp tiles over
  * the length-filter range of each window; HALF: 32-bit words for patterns of <= 32 units) */
 const void* fast_kernel_lev(int width, bool half);
+/* k_fast_hist: the choices' count histograms of the warp tiles' filter */
+const void* fast_hist_kernel();
 const void* fast_kernel_lcs(int width, bool half);
 const void* fast_kernel_osa(int width, bool half);
 /* k_band<CT, B> (banded unit-weight Levenshtein, B 32-bit words of band in

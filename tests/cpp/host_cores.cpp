@@ -188,6 +188,21 @@ int64_t hc_band32(int B, const uint8_t* a, int m, const uint8_t* b, int n, int64
     return -2;
 }
 
+/* the count bound of the warp tiles' filter (hist_lower_bound) for a pair of one-byte
+ * strings of at most RFG_HIST_MAXLEN units; fam 0 Levenshtein / OSA, 1 Indel */
+int hc_hist_bound(int fam, const uint8_t* a, int m, const uint8_t* b, int n)
+{
+    unsigned char ca[32] = {0}, cb[32] = {0};
+    for (int i = 0; i < m; ++i) ++ca[a[i] & 31];
+    for (int i = 0; i < n; ++i) ++cb[b[i] & 31];
+    u32 ha[8], hb[8];
+    for (int w = 0; w < 8; ++w) {
+        ha[w] = (u32)ca[4 * w] | (u32)ca[4 * w + 1] << 8 | (u32)ca[4 * w + 2] << 16 | (u32)ca[4 * w + 3] << 24;
+        hb[w] = (u32)cb[4 * w] | (u32)cb[4 * w + 1] << 8 | (u32)cb[4 * w + 2] << 16 | (u32)cb[4 * w + 3] << 24;
+    }
+    return hist_lower_bound(fam == 1 ? FAM_LCS : FAM_LEV, ha, hb, m, n);
+}
+
 /* band launches' host logic: band_range (the passing choice lengths of a pattern of m
  * units, unit-weight Levenshtein, op / ci / cf the chain) and band_reject_value; and one
  * pair's plan as the band kernel makes it: *pass = the pair reaches the core, else

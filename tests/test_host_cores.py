@@ -35,6 +35,8 @@ def libs():
     lib.hc_group.argtypes = [I, I, P, I, P, I, P, I, I64, I64, P]
     lib.hc_band32.restype = I64
     lib.hc_band32.argtypes = [I, P, I, P, I, I64]
+    lib.hc_hist_bound.restype = I
+    lib.hc_hist_bound.argtypes = [I, P, I, P, I]
     lib.hc_band_range.restype = I
     lib.hc_band_range.argtypes = [I, ctypes.c_uint64, ctypes.c_double, I64, I64, P, P, P]
     lib.hc_band_reject.restype = None
@@ -169,6 +171,26 @@ def test_band32_core_matches_oracle(libs):
                 assert (got == d) if d <= K else (got > K), (B, K, len(a), len(b), got, d)
                 checked += 1
     assert checked > 2000
+
+
+def test_count_filter_bound_never_exceeds_distance(libs):
+    """the warp tiles' count filter skips a pair only when its bound exceeds the cutoff:
+    the bound (hist_lower_bound) is at most the exact Levenshtein, OSA and Indel distance
+    on every pair (so a skipped pair's distance exceeds K and its chain value is K + 1),
+    and it is tight for anagrams-free cases such as pure insertions"""
+    lib, o = libs
+    checked = 0
+    tight = 0
+    for a, b in pairs(81, 3000, [0, 1, 2, 5, 16, 31, 32, 33, 63, 64, 100, 200, 255]):
+        if len(a) > 255 or len(b) > 255:
+            continue
+        for fam, exact_fam in ((0, 0), (0, 2), (1, 1)):
+            lb = lib.hc_hist_bound(fam, a, len(a), b, len(b))
+            d = exact(o, exact_fam, a, b)
+            assert 0 <= lb <= d, (fam, exact_fam, a, b, lb, d)
+            tight += lb == d
+            checked += 1
+    assert checked > 5000 and tight > 100
 
 
 def test_band_ranges_and_rejected_values(libs):
