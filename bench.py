@@ -11,10 +11,11 @@ One step = the three cdists over the whole batch.
   e2e   : the same metric through the public C ABI (rfg_cdist) with pinned host buffers:
           host->device copies of the strings and the device->host copy of the three
           int32 matrices inside the timed region.
-  roofline : the dominant kernel against the measured INT32 issue rate (LOP3/IADD3/SHF
-          microbenchmark): algorithmic integer ops = required word-steps (pairs that pass
-          the length filter |l1-l2| <= 8, ceil(l1/64)*l2 each) x ops per word-step
-          (Levenshtein 23, Indel/LCS 8, OSA 29).
+  roofline : the dominant metric's launches against the measured HBM copy rate: their
+          algorithmic bytes are the int32 result matrix they must write (nq x nc x 4) and
+          the strings and records they read.  Per metric also the INT32 view against the
+          measured LOP3/IADD3/SHF issue rate: count-filter checks x their ops plus the
+          recurrence word steps executed by the pairs that survive x ops per word step.
   cpu_baseline : the CPU restatement of the reference's Cached* path (oracle/librfo.so),
           all host threads, on the same workload.
 
@@ -38,11 +39,9 @@ sys.path.insert(0, os.path.join(ROOT, "rapidfuzz-cpp_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 METRIC_NAME = "GCUPS & pairs/s, batched vs per-call, 1 GB300, bit-exact; extract p50/p99 ms"
-# dram__bytes_read.sum + dram__bytes_write.sum of one metric's k_fast launches (64-bit and
-# 32-bit words) on this workload, averaged over the four steps of one `ncu --metrics`
-# capture (profiles/cdist4096_launch_list.md): the strings are read once, the 67 MB of
-# results stay in the 129 MB L2 when the launches end and are written back later
-DRAM_BYTES_PER_LAUNCH = {"levenshtein": 1170048, "indel": 1166336, "osa": 1027264}
+# integer operations of one count-filter check (hist_lower_bound): 8 byte-SAD, 7 adds,
+# the compare; Levenshtein / OSA add the length difference and the halving (3)
+OPS_PER_FILTER_CHECK = {"levenshtein": 19, "indel": 16, "osa": 19}
 # algorithmic INT32 operations per word step (minimal 32-bit ALU form of the reference's
 # step): 64-bit words (Levenshtein_impl.hpp:285-302, LCSseq_impl.hpp:226-229,
 # OSA_impl.hpp:52-54) and the same model for a 32-bit word (patterns of <= 32 units, which
@@ -222,6 +221,29 @@ def executed_word_steps(metric, q, c):
     return (float(s64.value), float(s32.value)) if rc == 0 else None
 
 
+def filter_checks(metric, q, c):
+    """(pairs the count filter examines, pairs that survive it) on this workload, counted
+    on the host with the kernels' bound (librfg_count.so)"""
+    lib = ctypes.CDLL(os.path.join(ROOT, "rapidfuzz-cpp_gb300", "lib", "librfg_count.so"))
+    lib.rfg_count_filter.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64),
+                                     ctypes.POINTER(ctypes.c_uint64)]
+    ck, sv = ctypes.c_uint64(), ctypes.c_uint64()
+    rc = lib.rfg_count_filter(metric, q[0].ctypes.data, q[1].ctypes.data, len(q[1]) - 1, c[0].ctypes.data,
+                              c[1].ctypes.data, len(c[1]) - 1, CUTOFF, ctypes.byref(ck), ctypes.byref(sv))
+    return (float(ck.value), float(sv.value)) if rc == 0 else (0.0, 0.0)
+
+
+def hbm_peak_gbs():
+    """the measured HBM copy rate of the GB300s (MEASURED_PEAKS.json), else the
+    earlier measurement the profiling notes give"""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback 6.8 TB/s"
+
+
 def int_peak_ops():
     lib = ctypes.CDLL(os.path.join(ROOT, "rapidfuzz-cpp_gb300", "lib", "librfg_peak.so"))
     lib.rfg_peak_int_ops.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
@@ -326,27 +348,31 @@ def main():
     value = cells * 3 * args.steps * world / t_max / 1e9
     pairs_per_s = npairs * 3 * args.steps * world / t_max
 
-    # roofline of every metric: executed word steps x algorithmic ops (64-bit and 32-bit
-    # words credited at their own counts) / the metric's CUDA-event time
+    # roofline of every metric: the bytes its launches must move (the int32 result matrix
+    # written, the strings and visiting records read) against the measured HBM rate, and
+    # the INT32 view: count-filter checks x their ops + the recurrence word steps the
+    # survivors execute x ops per word step (64- and 32-bit words at their own counts)
     peak = int_peak_ops()
+    hbm, hbm_src = hbm_peak_gbs()
     metric_ids = {"levenshtein": 0, "indel": 1, "osa": 3}
     kern = dict((name, b.kernels()) for name, b in batches)
+    moved = nq * nc * 4 + q[0].nbytes + c[0].nbytes + (nq + 1 + nc + 1) * 8
     per_metric = {}
     for name, _ in batches:
         ms = per_kernel[name] / args.steps
         ex = executed_word_steps(metric_ids[name], q, c)
         if ex is None:
-            alg = req_steps * OPS_PER_WORD_STEP[name]
             ex = (req_steps, 0.0)
-        else:
-            alg = ex[0] * OPS_PER_WORD_STEP[name] + ex[1] * OPS_PER_WORD_STEP_32[name]
+        ck, sv = filter_checks(metric_ids[name], q, c)
+        alg = ex[0] * OPS_PER_WORD_STEP[name] + ex[1] * OPS_PER_WORD_STEP_32[name] + ck * OPS_PER_FILTER_CHECK[name]
         ach = alg / (ms * 1e-3)
-        per_metric[name] = {"ms": ms, "achieved": ach / 1e12, "frac": ach / peak, "word_steps_64": ex[0],
-                            "word_steps_32": ex[1], "kernels": kern[name]}
+        gbs = moved / (ms * 1e-3) / 1e9
+        per_metric[name] = {"ms": ms, "achieved_gbs": gbs, "frac_hbm": gbs / hbm,
+                            "int32": {"achieved": ach / 1e12, "frac": ach / peak, "word_steps_64": ex[0],
+                                      "word_steps_32": ex[1], "filter_checks": ck, "filter_survivors": sv},
+                            "kernels": kern[name]}
     dom = max(per_kernel, key=per_kernel.get)
     dom_kernel = ";".join(kern[dom])
-    traffic = (DRAM_BYTES_PER_LAUNCH.get(dom) if args.nq == 4096 and args.nc == 4096 and "k_fast" in dom_kernel
-               else None)
 
     # parity of the timed path: every element of the three matrices against the oracle
     # (the CPU restatement of the reference's Cached* loop), which is also the CPU baseline
@@ -411,13 +437,13 @@ def main():
                            "per_kernel_ms": {k: v / args.steps for k, v in per_kernel.items()},
                            "required_word_steps_per_metric": req_steps, "pairs_passing_length_filter": pairs_pass,
                            "parity": "every element of the three timed matrices equals the oracle"},
-                "roofline": {"bound": "int32", "achieved": per_metric[dom]["achieved"], "peak": peak / 1e12,
-                             "unit": "Tops/s", "frac": per_metric[dom]["frac"], "traffic": traffic,
-                             "kernel": dom_kernel, "metric": dom,
-                             "peak_source": "measured: LOP3/IADD3/SHF issue-rate microbenchmark (librfg_peak.so)",
+                "roofline": {"bound": "hbm", "achieved": per_metric[dom]["achieved_gbs"], "peak": hbm, "unit": "GB/s",
+                             "frac": per_metric[dom]["frac_hbm"], "traffic": None, "kernel": dom_kernel,
+                             "metric": dom, "algorithmic_bytes_per_metric": moved, "peak_source": hbm_src,
+                             "int32_peak_tops": peak / 1e12,
+                             "int32_peak_source": "measured: LOP3/IADD3/SHF issue-rate microbenchmark (librfg_peak.so)",
                              "ops_per_word_step": {"64bit": OPS_PER_WORD_STEP, "32bit": OPS_PER_WORD_STEP_32},
-                             "per_metric": per_metric,
-                             "min_frac": min(v["frac"] for v in per_metric.values())},
+                             "ops_per_filter_check": OPS_PER_FILTER_CHECK, "per_metric": per_metric},
                 "cpu_baseline": cpu, "e2e": e2e, "per_call": per_call, "serving": serving,
                 "gpu_launches": sum(len(k) for k in kern.values()) * args.steps, "clocks": clk}
         print(json.dumps(line), flush=True)

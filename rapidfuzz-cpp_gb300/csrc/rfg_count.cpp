@@ -89,6 +89,34 @@ uint64_t pair_steps(int metric, const HostPM& pm, int m, const uint8_t* t, int n
 
 extern "C" {
 
+/* the warp tiles' count filter on the same inputs as rfg_count_word_steps2: *checks =
+ * (query, choice) pairs it examines (both lengths at most RFG_HIST_MAXLEN, the length
+ * filter passed, a cutoff below 2 * RFG_HIST_MAXLEN), *survivors = those whose bound
+ * does not exceed the cutoff (they run the recurrence) */
+int rfg_count_filter(int metric, const uint8_t* qd, const int64_t* qo, int64_t nq, const uint8_t* cd,
+                     const int64_t* co, int64_t nc, uint64_t cutoff, uint64_t* checks, uint64_t* survivors)
+{
+    if (!checks || !survivors || (metric != 0 && metric != 1 && metric != 3)) return -1;
+    *checks = *survivors = 0;
+    const int K = (int)std::min<uint64_t>(cutoff, 0x7fffffffull);
+    if (K >= 2 * RFG_HIST_MAXLEN) return 0;
+    std::vector<u32> hc((size_t)nc * 8);
+    for (int64_t c = 0; c < nc; ++c) host_hist(cd + co[c], (int)(co[c + 1] - co[c]), &hc[(size_t)c * 8]);
+    for (int64_t i = 0; i < nq; ++i) {
+        const int m = (int)(qo[i + 1] - qo[i]);
+        if (m == 0 || m > RFG_HIST_MAXLEN) continue;
+        u32 hq[8];
+        host_hist(qd + qo[i], m, hq);
+        for (int64_t c = 0; c < nc; ++c) {
+            const int n = (int)(co[c + 1] - co[c]);
+            if (n == 0 || n > RFG_HIST_MAXLEN || (m > n ? m - n : n - m) > K) continue;
+            ++*checks;
+            if (hist_lower_bound(metric == 1 ? FAM_LCS : FAM_LEV, hq, &hc[(size_t)c * 8], m, n) <= K) ++*survivors;
+        }
+    }
+    return 0;
+}
+
 /* metric: 0 Levenshtein (1/1/1), 1 Indel, 3 OSA; uint8 strings, every query <= 64
  * code units; distance cutoff.  Returns 0 and the executed word steps of queries of
  * 33..64 units (64-bit words) in *steps64 and of queries of at most 32 units (32-bit

@@ -33,9 +33,17 @@ namespace rfg {
 #ifndef RFG_FAST_WARPS
 #define RFG_FAST_WARPS 4 /* warps per CTA (the CTA only packs independent warps) */
 #endif
-#ifndef RFG_FAST_MINB
-#define RFG_FAST_MINB 8 /* CTAs per SM the register budget is sized for (64 registers) */
-#endif
+/* CTAs per SM the register budget is sized for: as many as the shared memory of the
+ * default 512-position window lets reside, at most 8 (64 registers; 7 for OSA on 64-bit
+ * words, whose recurrence holds two more words a pattern) */
+template <int FAM, int Q, bool HALF>
+constexpr int fast_min_blocks()
+{
+    return (227 * 1024) / (RFG_FAST_WARPS * (Q * 257 * (HALF ? 4 : 8) + Q * 32 + Q * 512 * 2)) <
+                   (FAM == FAM_OSA && !HALF ? 7 : 8)
+               ? (227 * 1024) / (RFG_FAST_WARPS * (Q * 257 * (HALF ? 4 : 8) + Q * 32 + Q * 512 * 2))
+               : (FAM == FAM_OSA && !HALF ? 7 : 8);
+}
 
 /* bytes of one warp's slice: tables, the patterns' count histograms (32 bytes each),
  * then the result stage (16-bit results when every value the chain can give, at most
@@ -142,7 +150,7 @@ __device__ __forceinline__ void fast_rows(WT* rows, int q, const KParams& a, int
 }
 
 template <int FAM, typename CT, int Q, bool HALF>
-__global__ void __launch_bounds__(RFG_FAST_WARPS * 32, RFG_FAST_MINB) k_fast(const KParams a)
+__global__ void __launch_bounds__(RFG_FAST_WARPS * 32, (fast_min_blocks<FAM, Q, HALF>())) k_fast(const KParams a)
 {
     typedef typename std::conditional<HALF, uint32_t, u64>::type WT;
     extern __shared__ u64 smem[];
@@ -242,8 +250,7 @@ __global__ void __launch_bounds__(RFG_FAST_WARPS * 32, RFG_FAST_MINB) k_fast(con
         /* every visiting position goes through the length and count filters; the pairs
          * that survive wait in a lane each (position and skip mask) and are scored
          * together once up to 32 wait, so the recurrence runs with full warps rather
-         * than for the one or two survivors of each 32 positions.  The next position's
-         * record is loaded while the current one is filtered. */
+         * than for the one or two survivors of each 32 positions. */
         int pend = -1;          /* this lane's waiting position, or -1 */
         unsigned pend_skip = 0; /* its patterns whose bound exceeds K */
         auto run_pending = [&]() {
@@ -265,12 +272,29 @@ __global__ void __launch_bounds__(RFG_FAST_WARPS * 32, RFG_FAST_MINB) k_fast(con
             }
             pend = -1;
         };
-        int4 rn = make_int4(0, 0, 0, 0);
-        if (lo + lane < hi) rn = __ldg(a.prec + p0 + lo + lane);
+        /* the filter needs a position's length and histogram only; the next iteration's
+         * are loaded before this one is filtered */
+        const bool hf = a.cfilter != 0;
+        int zn = 0;
+        uint4 hn0 = make_uint4(0, 0, 0, 0), hn1 = hn0;
+        if (lo + lane < hi) {
+            zn = __ldg(&a.prec[p0 + lo + lane].z);
+            if (hf) {
+                hn0 = __ldg(a.chist + 2 * (p0 + lo + lane));
+                hn1 = __ldg(a.chist + 2 * (p0 + lo + lane) + 1);
+            }
+        }
         for (int b0 = lo; b0 < hi; b0 += 32) {
             const int p = b0 + lane;
-            const int4 r = rn;
-            if (p + 32 < hi) rn = __ldg(a.prec + p0 + p + 32);
+            const int z = zn;
+            const uint4 h0 = hn0, h1 = hn1;
+            if (p + 32 < hi) {
+                zn = __ldg(&a.prec[p0 + p + 32].z);
+                if (hf) {
+                    hn0 = __ldg(a.chist + 2 * (p0 + p + 32));
+                    hn1 = __ldg(a.chist + 2 * (p0 + p + 32) + 1);
+                }
+            }
             bool surv = false;
             unsigned skip = 0;
             if (p < hi) {
@@ -279,19 +303,17 @@ __global__ void __launch_bounds__(RFG_FAST_WARPS * 32, RFG_FAST_MINB) k_fast(con
                 unsigned live = 0;
 #pragma unroll
                 for (int q = 0; q < Q; ++q) {
-                    const int diff = m[q] > r.z ? m[q] - r.z : r.z - m[q];
+                    const int diff = m[q] > z ? m[q] - z : z - m[q];
                     if (q < qn && diff <= K) live |= 1u << q;
                 }
-                if (a.cfilter && live && r.z <= RFG_HIST_MAXLEN) {
-                    const int64_t vp = p0 + p;
-                    const uint4 h0 = __ldg(a.chist + 2 * vp), h1 = __ldg(a.chist + 2 * vp + 1);
+                if (hf && live && z <= RFG_HIST_MAXLEN) {
                     const u32 hc[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
 #pragma unroll
                     for (int q = 0; q < Q; ++q) {
                         if (!((live >> q) & 1u)) continue;
                         const uint4 g0 = *(const uint4*)(qh + 8 * q), g1 = *(const uint4*)(qh + 8 * q + 4);
                         const u32 hq[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
-                        if (hist_lower_bound(FAM, hq, hc, m[q], r.z) > K) skip |= 1u << q;
+                        if (hist_lower_bound(FAM, hq, hc, m[q], z) > K) skip |= 1u << q;
                     }
                 }
                 surv = (live & ~skip) != 0;
