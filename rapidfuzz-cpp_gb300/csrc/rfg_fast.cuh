@@ -168,8 +168,8 @@ __global__ void __launch_bounds__(RFG_FAST_WARPS * 32, (fast_min_blocks<FAM, Q, 
     const int ntasks = (int)(((int64_t)a.nq + Q - 1) / Q * nwin);
     const int maxm = HALF ? 32 : 64;
 
-    for (int i = lane; i < Q * 257; i += 32) rows[i] = 0;
     int cur_g = -1;
+    bool tab_ok = false; /* the rows hold the current group's patterns */
     int m[Q], qi[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) m[q] = qi[q] = 0;
@@ -183,11 +183,9 @@ __global__ void __launch_bounds__(RFG_FAST_WARPS * 32, (fast_min_blocks<FAM, Q, 
         if (t >= ntasks) break;
         const int g = t / nwin, w = t - g * nwin;
         if (g != cur_g) {
-            /* clear the previous group's rows (its units are read again), then set the new */
-#pragma unroll
-            for (int q = 0; q < Q; ++q)
-                if (q < qn) fast_rows<WT, false>(rows, q, a, qi[q], m[q], lane);
-            __syncwarp();
+            /* the group's pattern tables are built when its first survivors are scored
+             * (most tasks of a pruning cutoff have none) */
+            tab_ok = false;
             qn = 0;
             mmin = 0x7fffffff;
             mmax = 0;
@@ -206,7 +204,6 @@ __global__ void __launch_bounds__(RFG_FAST_WARPS * 32, (fast_min_blocks<FAM, Q, 
                     qn = q + 1;
                     mmin = mq < mmin ? mq : mmin;
                     mmax = mq > mmax ? mq : mmax;
-                    fast_rows<WT, true>(rows, q, a, qi[q], mq, lane);
                 }
             }
             if (a.cfilter) {
@@ -255,6 +252,18 @@ __global__ void __launch_bounds__(RFG_FAST_WARPS * 32, (fast_min_blocks<FAM, Q, 
         unsigned pend_skip = 0; /* its patterns whose bound exceeds K */
         auto run_pending = [&]() {
             if (!__any_sync(0xffffffffu, pend >= 0)) return;
+            if (!tab_ok) {
+                /* all rows zeroed (the previous group's units among them), then the
+                 * group's patterns set */
+                u64* z = (u64*)rows;
+                for (int i = lane; i < (int)(Q * 257 * sizeof(WT) / 8); i += 32) z[i] = 0;
+                __syncwarp();
+#pragma unroll
+                for (int q = 0; q < Q; ++q)
+                    if (q < qn) fast_rows<WT, true>(rows, q, a, qi[q], m[q], lane);
+                __syncwarp();
+                tab_ok = true;
+            }
             if (pend >= 0) {
                 const int4 r = __ldg(a.prec + p0 + pend);
                 const int64_t o0 = (int64_t)(((uint64_t)(uint32_t)r.y << 32) | (uint32_t)r.x);

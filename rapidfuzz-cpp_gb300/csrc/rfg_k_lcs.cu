@@ -51,7 +51,7 @@ const void* tiles_mq_kernel_lcs(int width, bool norm, bool half)
 template <typename CT>
 static const void* pick_fast_lcs(bool half)
 {
-    return half ? (const void*)&k_fast<FAM_LCS, CT, 4, true> : (const void*)&k_fast<FAM_LCS, CT, 4, false>;
+    return half ? (const void*)&k_fast<FAM_LCS, CT, RFG_FAST_LCS_Q, true> : (const void*)&k_fast<FAM_LCS, CT, RFG_FAST_LCS_Q, false>;
 }
 
 const void* fast_kernel_lcs(int width, bool half)

@@ -25,7 +25,10 @@ const void* fast_kernel_osa(int width, bool half);
  * {1, 2, 3, 4, 6, 8, 12, 16}); one-byte choices only, nullptr otherwise */
 const void* band_kernel(int width, int B);
 /* queries per lane of k_fast */
-inline int fast_queries(int fam) { return fam == FAM_LCS ? 4 : 2; }
+#ifndef RFG_FAST_LCS_Q
+#define RFG_FAST_LCS_Q 2 /* queries a lane scores for Indel (2 since the count filter makes the recurrence rare) */
+#endif
+inline int fast_queries(int fam) { return fam == FAM_LCS ? RFG_FAST_LCS_Q : 2; }
 /* k_tiles_mq_jaro<CT, Q> (Jaro / Jaro-Winkler, several queries per thread) */
 const void* tiles_mq_kernel_jaro(int width);
 /* queries per thread of the several-queries kernels of a family (measured on GB300:
