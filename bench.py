@@ -34,6 +34,12 @@ import time
 
 import numpy as np
 
+# a prepared batch runs its length classes as parallel branches of one CUDA graph; with
+# the default 8 hardware connections two branches can share a work queue and serialise
+# (the band classes of dna256x65536 then vary 0.51-0.73 ms by batch; with 32,
+# 0.51-0.54), so the process asks for 32 before CUDA starts (a caller's setting stands)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "rapidfuzz-cpp_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "tests"))
