@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape (fixed launch list)")
+    ap.add_argument("--serial-metrics", action="store_true",
+                    help="cdist: the three metrics one after another on one stream (default: parallel branches)")
     ap.add_argument("--nq", type=int, default=4096)
     ap.add_argument("--nc", type=int, default=4096)
     ap.add_argument("--workload", default="cdist", choices=["cdist", "dna1x100k", "dna256x65536", "tokens1024x1m", "serving", "partial", "tokens", "editops"],
@@ -303,13 +305,43 @@ def main():
         batches.append((name, b))
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
 
-    def step(events=None):
+    # the three cdists are independent: by default they run as parallel branches (one
+    # side stream each, forked from and joined back into the step's stream)
+    side = [torch.cuda.Stream(device=dev) for _ in batches]
+
+    def step(events=None, span=None):
+        if args.serial_metrics:
+            if span is not None:
+                span[0].record(stream)
+            for i, (name, b) in enumerate(batches):
+                if events is not None:
+                    events[i][0].record(stream)
+                b.launch(stream.cuda_stream, graph=True)
+                if events is not None:
+                    events[i][1].record(stream)
+            if span is not None:
+                span[1].record(stream)
+            return
+        fork = torch.cuda.Event()
+        if span is not None:
+            span[0].record(stream)
+        fork.record(stream)
+        joins = []
         for i, (name, b) in enumerate(batches):
+            s = side[i]
+            s.wait_event(fork)
             if events is not None:
-                events[i][0].record(stream)
-            b.launch(stream.cuda_stream, graph=True)
+                events[i][0].record(s)
+            b.launch(s.cuda_stream, graph=True)
+            j = torch.cuda.Event(enable_timing=events is not None)
             if events is not None:
-                events[i][1].record(stream)
+                events[i][1].record(s)
+            j.record(s)
+            joins.append(j)
+        for j in joins:
+            stream.wait_event(j)
+        if span is not None:
+            span[1].record(stream)
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -339,12 +371,13 @@ def main():
         for _ in range(args.steps):
             flush.zero_()
             ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in batches]
-            step(ev)
-            stream.synchronize()
+            span = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            step(ev, span)
+            torch.cuda.synchronize()
             for (name, _), (e0, e1) in zip(batches, ev):
                 t = e0.elapsed_time(e1)
                 per_kernel[name] += t
-            total_ms += ev[0][0].elapsed_time(ev[-1][1])
+            total_ms += span[0].elapsed_time(span[1])
     torch.cuda.synchronize()
     clk = clocks.stop(local)
     t_max = sharding.max_over_ranks(total_ms / 1e3, device=dev)
@@ -439,7 +472,9 @@ def main():
                 "config": {"workload": WORKLOAD % (nq, nc), "global_batch": int(npairs * 3 * world)},
                 "detail": {"pairs_per_s": pairs_per_s,
                            "l2": "flushed between steps (256 MB write); strings are L2-resident within a step",
-                           "launch": "prepared batches replayed as CUDA graphs",
+                           "launch": ("prepared batches replayed as CUDA graphs, one after another" if args.serial_metrics
+                                      else "prepared batches replayed as CUDA graphs, the three metrics as parallel "
+                                           "branches (per_kernel_ms: each metric's own span)"),
                            "per_kernel_ms": {k: v / args.steps for k, v in per_kernel.items()},
                            "required_word_steps_per_metric": req_steps, "pairs_passing_length_filter": pairs_pass,
                            "parity": "every element of the three timed matrices equals the oracle"},
