@@ -412,6 +412,12 @@ def main():
                             "kernels": kern[name]}
     dom = max(per_kernel, key=per_kernel.get)
     dom_kernel = ";".join(kern[dom])
+    if args.serial_metrics:  # the dominant metric's launches alone
+        roof_gbs, roof_kernel, roof_metric = per_metric[dom]["achieved_gbs"], dom_kernel, dom
+    else:  # the metrics overlap: the step's launches together against the step's time
+        roof_gbs = moved * len(batches) / (t_max / args.steps) / 1e9
+        roof_kernel = ";".join(";".join(kern[n]) for n, _ in batches)
+        roof_metric = "all three metrics (parallel branches of the step)"
 
     # parity of the timed path: every element of the three matrices against the oracle
     # (the CPU restatement of the reference's Cached* loop), which is also the CPU baseline
@@ -478,9 +484,9 @@ def main():
                            "per_kernel_ms": {k: v / args.steps for k, v in per_kernel.items()},
                            "required_word_steps_per_metric": req_steps, "pairs_passing_length_filter": pairs_pass,
                            "parity": "every element of the three timed matrices equals the oracle"},
-                "roofline": {"bound": "hbm", "achieved": per_metric[dom]["achieved_gbs"], "peak": hbm, "unit": "GB/s",
-                             "frac": per_metric[dom]["frac_hbm"], "traffic": None, "kernel": dom_kernel,
-                             "metric": dom, "algorithmic_bytes_per_metric": moved, "peak_source": hbm_src,
+                "roofline": {"bound": "hbm", "achieved": roof_gbs, "peak": hbm, "unit": "GB/s",
+                             "frac": roof_gbs / hbm, "traffic": None, "kernel": roof_kernel, "metric": roof_metric,
+                             "algorithmic_bytes_per_metric": moved, "peak_source": hbm_src,
                              "int32_peak_tops": peak / 1e12,
                              "int32_peak_source": "measured: LOP3/IADD3/SHF issue-rate microbenchmark (librfg_peak.so)",
                              "ops_per_word_step": {"64bit": OPS_PER_WORD_STEP, "32bit": OPS_PER_WORD_STEP_32},
