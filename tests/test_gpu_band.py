@@ -56,3 +56,23 @@ def test_band_classes_match_oracle(alphabet):
             got = R.cdist(R.LEVENSHTEIN, op, q, c, cut, out_dtype=dt)
             exp = oracle_cdist(R.LEVENSHTEIN, op, q, c, cut, out_dtype={None: None, R.I32: 0, R.I64: 1, R.F64: 2}[dt])
             assert _same(got, exp), (op, cut, dt)
+
+
+@pytest.mark.parametrize("rounds", [2, 5])
+def test_band_units_of_several_rounds_match_oracle(rounds):
+    """band units of several 32-pair groups (the size the host picks for large classes),
+    forced through the launch-shape hook on a batch small enough for the oracle"""
+    lib = R.lib()
+    rng = np.random.default_rng(95 + rounds)
+    alpha = list(b"ACGT")
+    qs = _batch(rng, rng.integers(150, 900, size=12), alpha)
+    cs = _batch(rng, rng.integers(100, 1000, size=1500), alpha, base=qs, rate=0.1)
+    q, c = R.pack_strings(qs, 1), R.pack_strings(cs, 1)
+    try:
+        assert lib.rfg_testing_band_rounds(rounds) == 0
+        for op, cut in ((R.NORMALIZED_DISTANCE, 0.1), (R.DISTANCE, 40), (R.SIMILARITY, 600)):
+            got = R.cdist(R.LEVENSHTEIN, op, q, c, cut)
+            exp = oracle_cdist(R.LEVENSHTEIN, op, q, c, cut)
+            assert _same(got, exp), (rounds, op, cut)
+    finally:
+        lib.rfg_testing_band_rounds(0)
