@@ -687,7 +687,7 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
     for (int64_t b = 0; b < nblk; ++b)
         if (!cls[b * NCLS].empty() && (c.width == 1 || cls_wide[b * NCLS] == 0)) fast_any = true;
     fast_any = fast_any && fast_ok && spec.topk == 0 && !spec.fixed_perm && g_fast_mode != 0;
-    const int64_t fwin = std::max<int64_t>(32, std::min<int64_t>(1024, g_fast_window / 8 * 8));
+    const int64_t fwin = std::max<int64_t>(32, std::min<int64_t>(2048, g_fast_window / 8 * 8));
     std::vector<int32_t> frec;
     if (spec.fixed_perm) {
         chunk = spec.fixed_chunk;
@@ -2850,7 +2850,7 @@ rfg_status rfg_batch_tune(rfg_batch b, void* stream, int32_t* best_block, int64_
         RFG_TRY(trial(c));
     }
     if (fast)
-        for (int64_t w : {256, 1024}) {
+        for (int64_t w : {256, 1024, 2048}) {
             TuneChoice c = best;
             c.window = w;
             RFG_TRY(trial(c));

@@ -110,19 +110,24 @@ __device__ __forceinline__ int select_bit(unsigned m, int n)
     return pos;
 }
 
-/* first position p of [0, nn) with lens[4 p] >= L (lens ascending; nn <= 1024), by the
- * whole warp: one sampled length per lane, then the 32-position run the answer lies in */
+/* first position p of [0, nn) with lens[4 p] >= L (lens ascending; nn <= 4096), by the
+ * whole warp: one sampled length per lane narrows the answer to one run of
+ * S = ceil(nn / 32) positions, which 32-position votes then search */
 __device__ __forceinline__ int first_at_least(const int* lens, int nn, int64_t L, int lane)
 {
-    const int S = (nn + 31) >> 5; /* sample stride, at most 32 */
+    const int S = (nn + 31) >> 5; /* sample stride */
     const int ps = lane * S;
     const unsigned below = __ballot_sync(0xffffffffu, ps < nn && (int64_t)__ldg(lens + 4 * ps) < L);
     const int c = __popc(below); /* samples 0..c-1 lie below L */
     if (c == 0) return 0;
-    const int base = (c - 1) * S + 1; /* the answer is in [base, min(c * S, nn)] */
-    const int pq = base + lane;
-    const unsigned b2 = __ballot_sync(0xffffffffu, lane < S - 1 && pq < nn && (int64_t)__ldg(lens + 4 * pq) < L);
-    return base + __popc(b2);
+    const int base = (c - 1) * S + 1;              /* the answer is in [base, end] */
+    const int end = c * S < nn ? c * S : nn;       /* sample c (if any) is not below L */
+    for (int b = base; b < end; b += 32) {
+        const int pq = b + lane;
+        const unsigned b2 = __ballot_sync(0xffffffffu, pq < end && (int64_t)__ldg(lens + 4 * pq) < L);
+        if (b2 != 0xffffffffu) return b + __popc(b2); /* the lengths below L are a prefix */
+    }
+    return end;
 }
 
 /* set (SET) or clear the table rows of pattern q: lane l holds units l and l + 32;
@@ -155,7 +160,7 @@ __global__ void __launch_bounds__(RFG_FAST_WARPS * 32, (fast_min_blocks<FAM, Q, 
     typedef typename std::conditional<HALF, uint32_t, u64>::type WT;
     extern __shared__ u64 smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int win = (int)a.stage; /* positions per window (a multiple of 8, at most 1024) */
+    const int win = (int)a.stage; /* positions per window (a multiple of 8, at most 2048) */
     const int K = (int)(a.fast_k < 0x7fffffff ? a.fast_k : 0x7fffffff);
     const bool s16 = K < 0xffff;
     const size_t pmb = fast_pm_bytes(Q, HALF);
