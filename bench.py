@@ -45,6 +45,12 @@ sys.path.insert(0, os.path.join(ROOT, "rapidfuzz-cpp_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 METRIC_NAME = "GCUPS & pairs/s, batched vs per-call, 1 GB300, bit-exact; extract p50/p99 ms"
+# dram__bytes_read.sum + dram__bytes_write.sum of one step's launches (three k_fast_hist,
+# six k_fast) on this workload, from one `ncu --metrics` capture of four steps
+# (profiles/cdist4096_launch_list.md): the strings and records are read once; the 201 MB of
+# int32 results land in the 129 MB L2 and are written back after the launches (by the next
+# launches or the flush), so the traffic inside the launches is far below the result bytes
+DRAM_BYTES_PER_STEP = 4370000
 # integer operations of one count-filter check (hist_lower_bound): 8 byte-SAD, 7 adds,
 # the compare; Levenshtein / OSA add the length difference and the halving (3)
 OPS_PER_FILTER_CHECK = {"levenshtein": 19, "indel": 16, "osa": 19}
@@ -485,7 +491,12 @@ def main():
                            "required_word_steps_per_metric": req_steps, "pairs_passing_length_filter": pairs_pass,
                            "parity": "every element of the three timed matrices equals the oracle"},
                 "roofline": {"bound": "hbm", "achieved": roof_gbs, "peak": hbm, "unit": "GB/s",
-                             "frac": roof_gbs / hbm, "traffic": None, "kernel": roof_kernel, "metric": roof_metric,
+                             "frac": roof_gbs / hbm,
+                             "traffic": (DRAM_BYTES_PER_STEP if args.nq == 4096 and args.nc == 4096
+                                         and not args.serial_metrics else None),
+                             "traffic_note": "DRAM bytes inside one step's launches (ncu); the results are "
+                                             "written back from L2 after the launches",
+                             "kernel": roof_kernel, "metric": roof_metric,
                              "algorithmic_bytes_per_metric": moved, "peak_source": hbm_src,
                              "int32_peak_tops": peak / 1e12,
                              "int32_peak_source": "measured: LOP3/IADD3/SHF issue-rate microbenchmark (librfg_peak.so)",
