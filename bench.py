@@ -79,9 +79,10 @@ def parse():
                     help="cdist: the three metrics one after another on one stream (default: parallel branches)")
     ap.add_argument("--nq", type=int, default=4096)
     ap.add_argument("--nc", type=int, default=4096)
-    ap.add_argument("--workload", default="cdist", choices=["cdist", "dna1x100k", "dna256x65536", "tokens1024x1m", "serving", "partial", "tokens", "editops"],
+    ap.add_argument("--workload", default="cdist", choices=["cdist", "dna1x100k", "dna256x65536", "dna256x65536_indel", "tokens1024x1m", "serving",
+                             "partial", "tokens", "editops"],
                     help="cdist: 4096x4096 Zipf a-z Lev/Indel/OSA (the headline); dna1x100k: 1 x 100k DNA per-call "
-                         "vs batched; dna256x65536: 256 x 65536 long DNA banded; tokens1024x1m: 1024 x 1M uint32 JW + ratio; "
+                         "vs batched; dna256x65536: 256 x 65536 long DNA banded (_indel: Indel on the LCS band); tokens1024x1m: 1024 x 1M uint32 JW + ratio; "
                          "serving: serving, Poisson extract/extractOne requests over 10M DNA + 1M token strings")
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: request arrival rate (req/s)")
     ap.add_argument("--duration", type=float, default=2.0, help="serving: seconds of arrivals")

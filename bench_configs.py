@@ -8,6 +8,8 @@ dna1x100k  Levenshtein (no cutoff), 1 query x 100,000 DNA choices len U[8,64], i
 dna256x65536  Levenshtein normalized_distance with score_cutoff 0.1 (cutoff = 10 % of the longer
       string), 256 x 65,536 DNA strings, lengths log-normal(300, 0.6) in [100, 2000], each
       choice unrelated or a query mutated at 1-15 %: multi-word and banded kernels.
+dna256x65536_indel  the same strings under Indel normalized_distance with score_cutoff 0.1
+      (10 % of m + n): the banded LCS kernels, timed beside the unbanded multi-word cores.
 tokens1024x1m  Jaro-Winkler (prefix_weight 0.1, cutoff 0.85) and fuzz::ratio (cutoff 85) over uint32
       code-point token strings, 1,024 x 1,000,000, dense float64 outputs kept on the device.
 partial  fuzz::partial_ratio (cutoff 80) of 256 token queries against 200,000 token strings
@@ -69,15 +71,16 @@ def _dev(torch, batch, dev):
     return (td.data_ptr(), to.data_ptr(), w, o.size - 1), (td, to)
 
 
-def band_steps(q, c, op, ci, cf):
-    """word steps of the band kernels on one-byte strings (librfg_count.so)"""
+def band_steps(q, c, op, ci, cf, metric=0):
+    """word steps of the band kernels on one-byte strings (librfg_count.so); metric in the
+    scorer enum (0 Levenshtein, 1 Indel, 2 LCSseq, 6 ratio)"""
     import ctypes
     lib = ctypes.CDLL(os.path.join(B.ROOT, "rapidfuzz-cpp_gb300", "lib", "librfg_count.so"))
     vp, u64p = ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)
-    lib.rfg_count_band_steps.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_double, vp, vp, ctypes.c_int64, vp,
+    lib.rfg_count_band_steps.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_double, vp, vp, ctypes.c_int64, vp,
                                          vp, ctypes.c_int64, ctypes.c_int, u64p, u64p, u64p]
     e, a, p = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
-    rc = lib.rfg_count_band_steps(op, ci, cf, q[0].ctypes.data, q[1].ctypes.data, len(q[1]) - 1, c[0].ctypes.data,
+    rc = lib.rfg_count_band_steps(metric, op, ci, cf, q[0].ctypes.data, q[1].ctypes.data, len(q[1]) - 1, c[0].ctypes.data,
                                   c[1].ctypes.data, len(c[1]) - 1, 0, ctypes.byref(e), ctypes.byref(a), ctypes.byref(p))
     if rc != 0:
         raise RuntimeError("band step count failed")
@@ -193,6 +196,61 @@ def run(args, rank, world, local):
                      "cpu_baseline": {"value": _cells(qsub, c) / tc / 1e9, "unit": "GCUPS", "cores": os.cpu_count(),
                                       "kind": "port", "sample": "16 of the 256 queries x all 65,536 choices"},
                      "roofline": roofline, "e2e": None, "gpu_launches": steps * len(b.kernels()), "clocks": clk})
+    elif args.workload == "dna256x65536_indel":
+        q, c = WL.dna_lognormal(seed=13, nq=256, nc=65536)
+        nq, nc = 256, 65536
+        cells = _cells(q, c)
+        qd, kq = _dev(torch, q, dev)
+        cd, kc = _dev(torch, c, dev)
+        out = torch.empty((nq, nc), dtype=torch.float64, device=dev)
+        lib = R.lib()
+        times = {}
+        try:
+            # the same batch with the band kernels and on the unbanded multi-word cores
+            for mode in (0, 1):
+                assert lib.rfg_testing_band_mode(mode) == 0
+                b = R.Batch(R.INDEL, R.NORMALIZED_DISTANCE, qd, cd, out.data_ptr(), 0.1, out_dtype=R.F64,
+                            flags=R.DEVICE_INPUTS)
+                t, per, clk = _timed_batches(torch, [b], stream, steps, warmup, flush)
+                times[mode] = (t, b.kernels(), clk)
+                if mode == 0:
+                    b.close()
+        finally:
+            lib.rfg_testing_band_mode(1)
+        t, kernels, clk = times[1]
+        rows = [0, 100, 255]
+        exp = oracle_cdist(R.INDEL, R.NORMALIZED_DISTANCE,
+                           (np.concatenate([q[0][q[1][r]:q[1][r + 1]] for r in rows]),
+                            np.concatenate([[0], np.cumsum([q[1][r + 1] - q[1][r] for r in rows])]).astype(np.int64),
+                            1), c, 0.1)
+        assert np.array_equal(out[rows].cpu().numpy().view(np.int64), exp.view(np.int64)), "dna256x65536 Indel parity"
+        b.close()
+        tc0 = time.perf_counter()
+        sub = 16
+        qsub = (q[0][:q[1][sub]], q[1][:sub + 1].copy(), 1)
+        oracle_cdist(R.INDEL, R.NORMALIZED_DISTANCE, qsub, c, 0.1)
+        tc = time.perf_counter() - tc0
+        # roofline of the LCS band kernels: the 32-bit word steps Ukkonen's band of every
+        # pair needs (counted on the host by the same core), 4 INT32 operations each (the
+        # 32-bit-word form of the LCS step: LCSseq_impl.hpp:226-229)
+        band = band_steps(q, c, 2, 0, 0.1, metric=1)
+        peak = B.int_peak_ops()
+        ach = band["alg_words"] * 4 / (t / steps)
+        roofline = {"bound": "int32", "achieved": ach / 1e12, "peak": peak / 1e12, "unit": "Tops/s",
+                    "frac": ach / peak, "traffic": None, "kernel": ";".join(kernels),
+                    "peak_source": "measured: LOP3/IADD3/SHF issue-rate microbenchmark (librfg_peak.so)",
+                    "ops_per_word_step_32": 4, "band_pairs": band["pairs"],
+                    "alg_word_steps_32": band["alg_words"], "exec_word_steps_32": band["exec_words"]}
+        line.update({"value": cells * steps / t / 1e9, "ms_per_step": t / steps * 1e3, "dtype": "u64",
+                     "config": {"workload": "dna256x65536: Indel normalized_distance cutoff 0.1, 256 x 65,536 DNA "
+                                            "lognormal(300,0.6) in [100,2000], half mutated 1-15%",
+                                "pairs_per_s": nq * nc * steps / t, "kernels": kernels,
+                                "ms_per_step_unbanded": times[0][0] / steps * 1e3,
+                                "kernels_unbanded": times[0][1],
+                                "band_speedup": times[0][0] / t},
+                     "cpu_baseline": {"value": _cells(qsub, c) / tc / 1e9, "unit": "GCUPS", "cores": os.cpu_count(),
+                                      "kind": "port", "sample": "16 of the 256 queries x all 65,536 choices"},
+                     "roofline": roofline, "e2e": None, "gpu_launches": steps * len(kernels), "clocks": clk})
     elif args.workload == "serving":
         return run_serving(args, R, WL)
     elif args.workload == "tokens":

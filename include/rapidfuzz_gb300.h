@@ -268,6 +268,11 @@ rfg_status rfg_testing_fail_device_allocs(int64_t after);
  * prepared afterwards use it, until rfg_batch_tune chooses its own. */
 rfg_status rfg_testing_band_rounds(int32_t rounds);
 
+/* Kernel-choice override for measurements: 0 keeps every query off the band kernels
+ * (the unbanded multi-word cores score them), 1 restores the default.  Batches prepared
+ * afterwards use it, until rfg_batch_tune chooses its own. */
+rfg_status rfg_testing_band_mode(int32_t on);
+
 /* ------------------------------------------------------ no-allocation cdist
  * rfg_cdist_noalloc has no counterpart in the reference.  It is for callers that may
  * not allocate device memory (inside another framework's memory manager, in a process

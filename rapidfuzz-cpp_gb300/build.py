@@ -19,7 +19,7 @@ COUNT_LIB = os.path.join(LIB_DIR, "librfg_count.so")  # executed word steps of t
 # (an x86-64 build container, an aarch64 GPU host) rebuilds instead of reusing them
 STAMP = os.path.join(LIB_DIR, "build_machine.txt")
 
-SOURCES = ["rfg_api.cu", "rfg_k_band.cu", "rfg_k_lev.cu", "rfg_k_lcs.cu", "rfg_k_osa.cu", "rfg_k_jaro.cu", "rfg_k_generic.cu", "rfg_noalloc.cu", "rfg_server.cu",
+SOURCES = ["rfg_api.cu", "rfg_k_band.cu", "rfg_k_band_lcs.cu", "rfg_k_lev.cu", "rfg_k_lcs.cu", "rfg_k_osa.cu", "rfg_k_jaro.cu", "rfg_k_generic.cu", "rfg_noalloc.cu", "rfg_server.cu",
            "rfg_k_token.cu", "rfg_k_editops.cu", "rfg_token.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",

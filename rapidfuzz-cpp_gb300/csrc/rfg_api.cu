@@ -249,9 +249,15 @@ struct QuerySet {
     std::vector<int32_t> distinct;
 };
 
+/* the metrics whose long queries may take the band kernels (their tables need the
+ * distinct code units of the query) */
+bool band_candidate(int metric)
+{
+    return metric == RFG_LEVENSHTEIN || metric == RFG_INDEL || metric == RFG_LCSSEQ || metric == RFG_RATIO;
+}
+
 /* lengths and wide-unit counts of a host batch; with want_distinct, the distinct units
- * below 256 of every query longer than 64 units (the band-class candidates of
- * Levenshtein) */
+ * below 256 of every query longer than 64 units (the band-class candidates) */
 rfg_status query_info_from_host(const void* data, const int64_t* off, int64_t n, int width, QuerySet* qs,
                                 bool want_distinct = false)
 {
@@ -461,7 +467,7 @@ int g_fast_mode = 1;        /* unit-weight one-word distances run on the warp ti
 #define RFG_BAND_MAX_SMEM (96 * 1024)
 int g_count_filter = 1; /* the warp tiles' count filter (hist_lower_bound) */
 int g_band_rounds = 0; /* band units of 32 x this many pairs (0: sized by the class; autotuning) */
-int g_band_mode = 1;        /* unit-weight Levenshtein with a band narrower than the pattern runs on k_band */
+int g_band_mode = 1;        /* unit-weight Levenshtein and the LCS families with a band narrower than the pattern run on k_band */
 int64_t g_fast_window = 512; /* choice positions per warp window of k_fast (autotuning) */
 
 /* query classes per row block: 0..3 = 1, 2, 4, 8 register words, 4 = any length, 5.. =
@@ -617,10 +623,12 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         for (int32_t l : clen) host_max_choice_len = std::max<int64_t>(host_max_choice_len, l);
     }
     /* classes: 1, 2, 4, 8 register words; index 4 = any length; 5.. = the band classes of
-     * unit-weight Levenshtein (band_class_words(k - 5) 32-bit words); one set per row block */
-    const bool band_ok = g_band_mode != 0 && fam == FAM_LEV && spec.metric == RFG_LEVENSHTEIN && spec.sp.ins == 1 &&
-                         spec.sp.del == 1 && spec.sp.rep == 1 && spec.form != RFG_FORM_MULTI && spec.topk == 0 &&
-                         !spec.fixed_perm && c.width == 1 && nc < INT32_MAX;
+     * unit-weight Levenshtein and of the LCS families (band_class_words(k - 5) 32-bit
+     * words); one set per row block */
+    const bool band_fam = (fam == FAM_LEV && spec.metric == RFG_LEVENSHTEIN) ||
+                          (fam == FAM_LCS && (spec.metric == RFG_INDEL || spec.metric == RFG_LCSSEQ || spec.metric == RFG_RATIO));
+    const bool band_ok = g_band_mode != 0 && band_fam && band_metric(spec.metric, spec.sp) && spec.form != RFG_FORM_MULTI &&
+                         spec.topk == 0 && !spec.fixed_perm && c.width == 1 && nc < INT32_MAX;
     std::vector<std::vector<int32_t>> cls(nblk * NCLS);
     std::vector<int64_t> cls_maxlen(nblk * NCLS, 0);
     std::vector<int32_t> cls_wide(nblk * NCLS, 0);
@@ -874,13 +882,17 @@ rfg_status prepare_batch(const QuerySet& q, const KStrings& c, const BatchSpec& 
         const bool small_class =
             k < 4 && !topk && (int64_t)cls[bk].size() * nchunks_full < (int64_t)g.sms * 8 && chunk > 256;
         if (k >= 5) {
-            /* banded Levenshtein: warp tasks of passing pairs and of row fills, each warp
-             * with its own table in shared memory */
+            /* banded Levenshtein / LCS: warp tasks of passing pairs and of row fills, each
+             * warp with its own table in shared memory */
             const int B = band_class_words(k - 5);
-            const void* fb = band_kernel(c.width, B);
+            const bool lcs = fam == FAM_LCS;
+            const void* fb = band_kernel(c.width, B, lcs);
             if (!fb) return fail(RFG_ERR_INVALID_ARGUMENT, "no band kernel for this code-unit width");
             a.scratch_per_thread = cls_bwords[bk];
-            a.tab_t = (spec.op == RFG_NORMALIZED_DISTANCE || spec.op == RFG_NORMALIZED_SIMILARITY) ? 32 * B : -1;
+            /* normalized chains: the cutoff table (the LCS families' spans n - m in [-32B, 32B]) */
+            const bool norm = spec.op == RFG_NORMALIZED_DISTANCE || spec.op == RFG_NORMALIZED_SIMILARITY ||
+                              spec.metric == RFG_RATIO;
+            a.tab_t = norm ? (lcs ? 64 * B : 32 * B) : -1;
             if (fast_ok) {
                 a.fast = 1;
                 a.fast_k = clamp_bound(spec.ci);
@@ -1319,7 +1331,7 @@ rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const 
         RFG_CUDA(cudaMemcpyAsync(off.data(), Q->offsets, (nq + 1) * 8, cudaMemcpyDeviceToHost, g.stream));
         RFG_CUDA(cudaStreamSynchronize(g.stream));
         RFG_TRY(check_offsets(off.data(), nq, "queries")); /* before anything is read through them */
-        const bool want = metric == RFG_LEVENSHTEIN && has_long_query(off.data(), nq);
+        const bool want = band_candidate(metric) && has_long_query(off.data(), nq);
         std::vector<unsigned char> qh;
         if ((Q->char_width > 1 || want) && nq && off[nq] > off[0]) {
             qh.resize((size_t)off[nq] * Q->char_width);
@@ -1333,7 +1345,7 @@ rfg_status cdist_impl(int metric, int op, int form, const rfg_strings* Q, const 
     else {
         if ((!Q->data && nq && Q->offsets[nq]) || (!C->data && nc && C->offsets[nc]))
             return fail(RFG_ERR_INVALID_ARGUMENT, "string data is NULL");
-        RFG_TRY(query_info_from_host(Q->data, Q->offsets, nq, Q->char_width, &qs, metric == RFG_LEVENSHTEIN));
+        RFG_TRY(query_info_from_host(Q->data, Q->offsets, nq, Q->char_width, &qs, band_candidate(metric)));
         for (int64_t i = 0; i < nc; ++i)
             if (C->offsets[i] < 0 || C->offsets[i + 1] < C->offsets[i] || C->offsets[i + 1] - C->offsets[i] > INT32_MAX)
                 return fail(RFG_ERR_INVALID_ARGUMENT, "choice offsets must be non-decreasing and >= 0");
@@ -1841,6 +1853,13 @@ rfg_status rfg_testing_band_rounds(int32_t rounds)
     return RFG_OK;
 }
 
+rfg_status rfg_testing_band_mode(int32_t on)
+{
+    std::lock_guard<std::recursive_mutex> lk(g.mu);
+    g_band_mode = on ? 1 : 0;
+    return RFG_OK;
+}
+
 rfg_status rfg_synchronize(void)
 {
     std::lock_guard<std::recursive_mutex> lk(g.mu);
@@ -1895,7 +1914,7 @@ rfg_status rfg_cached_create(rfg_metric metric, const void* s1, int64_t len1, in
     }
     int64_t off[2] = {0, len1};
     rfg_strings q{h->host.data(), off, 1, width1};
-    rfg_status st = query_info_from_host(h->host.data(), off, 1, width1, &h->qs, metric == RFG_LEVENSHTEIN);
+    rfg_status st = query_info_from_host(h->host.data(), off, 1, width1, &h->qs, band_candidate(metric));
     if (st == RFG_OK) st = upload_strings(&q, &h->data, &h->off, &h->qs.dev);
     if (st == RFG_OK && cudaStreamSynchronize(g.stream) != cudaSuccess) st = fail(RFG_ERR_CUDA, "upload failed");
     if (st != RFG_OK) {
@@ -2717,7 +2736,7 @@ rfg_status rfg_batch_create(rfg_metric metric, rfg_op op, rfg_form form, const r
         if (cudaMemcpy(off.data(), Q->offsets, (nq + 1) * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
             st = fail(RFG_ERR_CUDA, "reading query offsets failed");
         if (st == RFG_OK) st = check_offsets(off.data(), nq, "queries"); /* before anything is read through them */
-        const bool want = metric == RFG_LEVENSHTEIN && st == RFG_OK && has_long_query(off.data(), nq);
+        const bool want = band_candidate(metric) && st == RFG_OK && has_long_query(off.data(), nq);
         if (st == RFG_OK && (Q->char_width > 1 || want) && nq && off[nq] > off[0]) {
             qh.resize((size_t)off[nq] * Q->char_width);
             if (cudaMemcpy(qh.data(), Q->data, qh.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
@@ -2728,7 +2747,7 @@ rfg_status rfg_batch_create(rfg_metric metric, rfg_op op, rfg_form form, const r
         b->ck = KStrings{(const unsigned char*)C->data, C->offsets, nc, C->char_width};
     }
     else {
-        st = query_info_from_host(Q->data, Q->offsets, nq, Q->char_width, &b->qs, metric == RFG_LEVENSHTEIN);
+        st = query_info_from_host(Q->data, Q->offsets, nq, Q->char_width, &b->qs, band_candidate(metric));
         if (st == RFG_OK) st = upload_strings(Q, &b->qd, &b->qo, &b->qs.dev);
         if (st == RFG_OK) st = upload_strings(C, &b->cd, &b->co, &b->ck);
     }

@@ -1,10 +1,13 @@
 /*
- * rfg_band.cuh -- banded Levenshtein (weights 1/1/1) for queries whose every passing pair
- * needs a diagonal band narrower than the pattern: the reference's
- * levenshtein_hyrroe2003_small_band / the band of levenshtein_hyrroe2003_block
- * (Levenshtein_impl.hpp:419-505, 641-850), on Ukkonen's band of about K + 2 diagonals
- * (lev_band32), chosen when that band is narrower than the pattern for the largest bound
- * K any pair of the query can reach (the length filter Levenshtein_impl.hpp:863 caps it).
+ * rfg_band.cuh -- banded Levenshtein (weights 1/1/1) and banded LCS (Indel, LCSseq,
+ * ratio) for queries whose every passing pair needs a diagonal band narrower than the
+ * pattern: the reference's levenshtein_hyrroe2003_small_band / the band of
+ * levenshtein_hyrroe2003_block (Levenshtein_impl.hpp:419-505, 641-850) and the band of
+ * lcs_blockwise (LCSseq_impl.hpp:262-333, chosen at :349), on Ukkonen's band of about
+ * K + 2 diagonals (lev_band32, lcs_band32; K the Levenshtein bound, or for the LCS
+ * families the Indel-distance bound their plans carry), chosen when that band is
+ * narrower than the pattern for the largest bound K any pair of the query can reach (the
+ * length filters Levenshtein_impl.hpp:863, LCSseq_impl.hpp:389 cap it).
  *
  * Whether a pair passes the length filter depends on its two lengths alone, and the
  * passing choice lengths of a query form one interval [nlo, nhi] (band_range).  With the
@@ -24,9 +27,11 @@
  *     the query holds (plus the all-zero row), each row with zero words on either side
  *     so the band's window is loaded without range tests; rmap[c] = the word offset of
  *     unit c's row;
- *   - for the normalized ops, the integer cutoff chain_kd(m, m + j) for j = 0..32B (the
- *     cutoff depends on max(m, n) only, so j = 0 serves every n <= m, and no passing
- *     pair has n > m + 32B), so no pair evaluates the double-precision chain.
+ *   - for the normalized ops, the integer cutoff chain_kd(m, m + j) so that no pair
+ *     evaluates the double-precision chain: Levenshtein j = 0..32B (the cutoff depends
+ *     on max(m, n) only, so j = 0 serves every n <= m); the LCS families, whose Indel
+ *     maximum m + n depends on n on both sides, j = -32B..32B (no passing pair has
+ *     |n - m| > K, and K < 32B).
  * One-byte choices only (a wider unit has no row: the zero row would do, but the host
  * keeps wide alphabets on the general kernels).
  */
@@ -80,7 +85,9 @@ __device__ __forceinline__ int band_query_of(const BandQuery* bq, int nq, int t,
 }
 
 /* a pair's chain as the band kernel plans it: the cutoff of a normalized op from the
- * warp's table (kd[n - m], kd[0] for every n <= m), else from the double chain */
+ * warp's table (Levenshtein: kd[n - m], kd[0] for every n <= m; the LCS families:
+ * kd[n - m + tab_t / 2]), else from the double chain */
+template <bool LCS>
 __device__ __forceinline__ PairSpec band_pair_spec(const KParams& a, const u32* kd, int tab_t, int m, int n)
 {
     PairSpec s;
@@ -93,22 +100,34 @@ __device__ __forceinline__ PairSpec band_pair_spec(const KParams& a, const u32* 
     s.cf = a.cf;
     s.p = a.sp;
     if (tab_t >= 0) {
-        const int jj = n - m;
-        if (jj <= tab_t) {
-            const u32 v = kd[jj > 0 ? jj : 0];
-            s.kd_pre = v == 0xffffffffu ? ~0ull : (u64)v;
+        if constexpr (LCS) {
+            const int h = tab_t >> 1, jj = n - m + h;
+            if (jj >= 0 && jj <= tab_t) {
+                const u32 v = kd[jj];
+                s.kd_pre = v == 0xffffffffu ? ~0ull : (u64)v;
+            }
+        }
+        else {
+            const int jj = n - m;
+            if (jj <= tab_t) {
+                const u32 v = kd[jj > 0 ? jj : 0];
+                s.kd_pre = v == 0xffffffffu ? ~0ull : (u64)v;
+            }
         }
     }
     return s;
 }
 
-/* a pair's result from the core's raw distance */
+/* a pair's result from the core's raw distance (Levenshtein, or for the LCS families
+ * the Indel distance m + n - 2 LCS; any value > K when pruned) */
+template <bool LCS>
 __device__ __forceinline__ void band_store(const KParams& a, const PairSpec& s, const Plan& pl, i64 K, i64 raw,
-                                           int64_t qi, int64_t ci, bool is_int)
+                                           int m, int n, int64_t qi, int64_t ci, bool is_int)
 {
     i64 vi = 0;
     double vf = 0.0;
     if (a.fast) vi = raw <= K ? raw : K + 1;
+    else if constexpr (LCS) finish_int(s, pl, raw <= K ? ((i64)m + n - raw) >> 1 : -1, &vi, &vf); /* the LCS length, or -1 */
     else finish_int(s, pl, raw, &vi, &vf);
     store_result(a, qi, ci, vi, vf, is_int);
 }
@@ -117,12 +136,12 @@ __device__ __forceinline__ void band_store(const KParams& a, const PairSpec& s, 
 #define RFG_BAND_MINB 3 /* CTAs of 256 threads per SM the register budget of bands up to 4 words is sized for (85 registers) */
 #endif
 
-template <typename CT, int B>
+template <typename CT, int B, bool LCS>
 __global__ void __launch_bounds__(256, B <= 4 ? RFG_BAND_MINB : B <= 8 ? 2 : 1) k_band(const KParams a)
 {
     extern __shared__ u64 smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int tab_t = a.tab_t; /* cutoffs of n = m .. m + tab_t (-1: not used) */
+    const int tab_t = a.tab_t; /* cutoffs of n = m .. m + tab_t (LCS: m - tab_t/2 .. m + tab_t/2; -1: not used) */
     const int64_t words = a.scratch_per_thread; /* row words a slice holds */
     unsigned char* slice = (unsigned char*)smem + (size_t)warp * band_warp_bytes(tab_t, words);
     int* rmap = (int*)slice;
@@ -139,7 +158,7 @@ __global__ void __launch_bounds__(256, B <= 4 ? RFG_BAND_MINB : B <= 8 ? 2 : 1) 
     const bool use_kd = tab_t >= 0;
     i64 rej_i;
     double rej_f;
-    band_reject_value(a.op, a.ci, a.fast, a.fast_k, &rej_i, &rej_f);
+    band_reject_value(a.metric, a.op, a.ci, a.fast, a.fast_k, &rej_i, &rej_f);
     int cur = -1, m = 0, S = 0;
     int64_t qi = 0;
     for (;;) {
@@ -214,8 +233,9 @@ __global__ void __launch_bounds__(256, B <= 4 ? RFG_BAND_MINB : B <= 8 ? 2 : 1) 
                 s.ci = a.ci;
                 s.cf = a.cf;
                 s.p = a.sp;
+                const int j0 = LCS ? -(tab_t >> 1) : 0;
                 for (int jj = lane; jj <= tab_t; jj += 32) {
-                    s.l2 = (u64)(m + jj);
+                    s.l2 = (u64)(m + j0 + jj > 0 ? m + j0 + jj : 0);
                     const u64 v = chain_kd(s);
                     kd[jj] = v >= 0xffffffffull ? 0xffffffffu : (u32)v;
                 }
@@ -239,7 +259,7 @@ __global__ void __launch_bounds__(256, B <= 4 ? RFG_BAND_MINB : B <= 8 ? 2 : 1) 
             if (mine) rec = __ldg(a.prec + p);
             const int n = rec.z;
             const BandText<CT> tx{(const CT*)a.c.data + (int64_t)(((uint64_t)(uint32_t)rec.y << 32) | (uint32_t)rec.x)};
-            const PairSpec s = band_pair_spec(a, kd, tab_t, m, n);
+            const PairSpec s = band_pair_spec<LCS>(a, kd, tab_t, m, n);
             Plan pl;
             i64 K;
             if (a.fast) K = a.fast_k;
@@ -257,12 +277,20 @@ __global__ void __launch_bounds__(256, B <= 4 ? RFG_BAND_MINB : B <= 8 ? 2 : 1) 
             }
             else if (!passes && K >= 0)
                 raw = m == 0 ? n : n == 0 ? m : K + 1;
-            BandLane<B> L;
-            if (run) band_init<B>(L, m, tx, n, (int)K);
             bool act = run;
-            while (__any_sync(0xffffffffu, act))
-                if (act && band_run8<B>(L, pm, tx, &raw)) act = false;
-            if (mine) band_store(a, s, pl, K, raw, qi, rec.w, is_int);
+            if constexpr (LCS) {
+                LcsBandLane<B> L;
+                if (run) lcs_band_init<B>(L, m, tx, n, (int)K);
+                while (__any_sync(0xffffffffu, act))
+                    if (act && lcs_band_run8<B>(L, pm, tx, &raw)) act = false;
+            }
+            else {
+                BandLane<B> L;
+                if (run) band_init<B>(L, m, tx, n, (int)K);
+                while (__any_sync(0xffffffffu, act))
+                    if (act && band_run8<B>(L, pm, tx, &raw)) act = false;
+            }
+            if (mine) band_store<LCS>(a, s, pl, K, raw, m, n, qi, rec.w, is_int);
         }
     }
 }

@@ -1210,6 +1210,152 @@ RFG_HD i64 lev_band32(const PM32& pm, int m, const TXT& t, int n, int K, int* st
     return v;
 }
 
+/* Banded LCS on B 32-bit words, the band of lcs_blockwise (LCSseq_impl.hpp:262-333)
+ * moved one row per text unit like the Levenshtein band above.  The LCS families reach
+ * the core with an Indel-distance bound K (an LCS of at least (m + n - K) / 2), and a path
+ * with at most K indels visits only the diagonals of Ukkonen's band for K -- the window
+ * of band_lo / band_bits: bit b of the window is the difference bit (Hyyro's S, 0 = the
+ * LCS rises at that pattern unit) of pattern index start + b.  Each text unit runs the
+ * step S' = (S + (S & X)) | (S & ~X) (LCSseq_impl.hpp:226-229) over the window with no
+ * carry into its bottom word, then moves the frame: the bottom bit leaves (a 0 adds one
+ * to `base`, the LCS of the units below the window), and a 1 enters at the top.  Every
+ * value the window then holds is the LCS of some real alignment (a pattern unit below
+ * the window keeps its last value, one above it adds nothing), so the result never
+ * exceeds the true LCS, and it equals it when the LCS is at least (m + n - K) / 2, since
+ * those alignments never leave the band.  Indel distances along a diagonal never fall,
+ * so after every 8 text units the cell on the diagonal of (m, n) (pattern index j + m - n
+ * after j units: the window bits below m - n - dlo) gives a lower bound that stops the
+ * pair once it passes K.  The lane reports the Indel distance m + n - 2 LCS, or any
+ * value > K.  Requires |m - n| <= K, n > 0. */
+template <int B>
+struct LcsBandLane {
+    u32 S[B], dmask[B];
+    u32 cur[2]; /* the block's 8 text units, 4 to a word */
+    u32 gone;   /* the bits that left the window in this block, the latest at bit 31 */
+    int base;   /* LCS of the pattern units below the window */
+    int start;  /* pattern index of window bit 0 at the block's first unit */
+    int j, n, K, mn;
+};
+
+template <int B, typename TXT>
+RFG_HD void lcs_band_init(LcsBandLane<B>& L, int m, const TXT& t, int n, int K)
+{
+    const int dlo = band_lo(K, m - n);
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        L.S[b] = ~0u;
+        L.dmask[b] = range_mask32(-32 * b, (m - n) - dlo - 1 - 32 * b);
+    }
+    L.gone = ~0u;
+    L.base = 0;
+    L.start = dlo;
+    L.j = 0;
+    L.n = n;
+    L.K = K;
+    L.mn = m + n;
+    u32 u[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) u[s] = (u32)t[s < n - 1 ? s : n - 1];
+    L.cur[0] = u[0] | u[1] << 8 | u[2] << 16 | u[3] << 24;
+    L.cur[1] = u[4] | u[5] << 8 | u[6] << 16 | u[7] << 24;
+}
+
+/* one text unit whose window X is loaded */
+template <int B>
+RFG_HD void lcs_band_step(LcsBandLane<B>& L, const u32* X)
+{
+    u32 U[B], T[B];
+#pragma unroll
+    for (int b = 0; b < B; ++b) U[b] = L.S[b] & X[b];
+    add_chain<B>(L.S, U, T);
+#pragma unroll
+    for (int b = 0; b < B; ++b) T[b] = T[b] | (L.S[b] & ~X[b]);
+    L.gone = funnel32(L.gone, T[0], 1);
+#pragma unroll
+    for (int b = 0; b < B; ++b) L.S[b] = funnel32(T[b], b + 1 < B ? T[b + 1 < B ? b + 1 : b] : ~0u, 1);
+}
+
+/* the next 8 text units (fewer at the end); true when the pair is done, with *out = the
+ * Indel distance, or any value > K */
+template <int B, typename PM32, typename TXT>
+RFG_HD bool lcs_band_run8(LcsBandLane<B>& L, const PM32& pm, const TXT& t, i64* out)
+{
+    const int last = L.n - 1;
+    u32 nx[8];
+    if (L.j + 16 <= L.n) {
+#pragma unroll
+        for (int s = 0; s < 8; ++s) nx[s] = (u32)t[L.j + 8 + s];
+    }
+    else {
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            const int k = L.j + 8 + s;
+            nx[s] = (u32)t[k < last ? k : last];
+        }
+    }
+    text_prefetch(t, L.j + 64 < last ? L.j + 64 : last);
+    const int rem = L.n - L.j;
+    if (rem >= 8) {
+        constexpr int AH = BAND_AHEAD(B);
+        u32 X[8][B];
+#pragma unroll
+        for (int s = 0; s < AH; ++s) band_window<B>(pm((L.cur[s >> 2] >> (8 * (s & 3))) & 0xffu), L.start + s, X[s]);
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            if (s + AH < 8)
+                band_window<B>(pm((L.cur[(s + AH) >> 2] >> (8 * ((s + AH) & 3))) & 0xffu), L.start + s + AH,
+                               X[s + AH < 8 ? s + AH : 0]);
+            lcs_band_step<B>(L, X[s]);
+        }
+    }
+    else {
+#pragma unroll
+        for (int s = 0; s < 8; ++s)
+            if (s < rem) {
+                const u32 c = (L.cur[s >> 2] >> (8 * (s & 3))) & 0xffu;
+                u32 X[B];
+                band_window<B>(pm(c), L.start + s, X);
+                lcs_band_step<B>(L, X);
+            }
+            else L.gone = funnel32(L.gone, ~0u, 1);
+    }
+    /* the block's 8 leaving bits are the top byte of `gone` */
+    L.base += 8 - popc_w(L.gone >> 24);
+    L.j += 8;
+    L.start += 8;
+    if (L.j >= L.n) {
+        int lcs = L.base;
+#pragma unroll
+        for (int b = 0; b < B; ++b) lcs += popc_w(~L.S[b]);
+        *out = L.mn - 2 * lcs;
+        return true;
+    }
+    int v = L.base;
+#pragma unroll
+    for (int b = 0; b < B; ++b) v += popc_w(~L.S[b] & L.dmask[b]);
+    /* the cell (j + m - n, j): (j + m - n) + j - 2 v */
+    if (2 * L.j + (L.mn - 2 * L.n) - 2 * v > L.K) {
+        *out = (i64)L.K + 1;
+        return true;
+    }
+    L.cur[0] = nx[0] | nx[1] << 8 | nx[2] << 16 | nx[3] << 24;
+    L.cur[1] = nx[4] | nx[5] << 8 | nx[6] << 16 | nx[7] << 24;
+    return false;
+}
+
+/* one pair start to end; *steps (if given) = the text units run */
+template <int B, typename PM32, typename TXT>
+RFG_HD i64 lcs_band32(const PM32& pm, int m, const TXT& t, int n, int K, int* steps = nullptr)
+{
+    LcsBandLane<B> L;
+    lcs_band_init<B>(L, m, t, n, K);
+    i64 v = 0;
+    while (!lcs_band_run8<B>(L, pm, t, &v)) {
+    }
+    if (steps) *steps = L.j < n ? L.j : n;
+    return v;
+}
+
 /* Jaro with P (= s1) of up to 64*W chars and a text of any length: the greedy
  * flagging of flag_similar_characters_block (Jaro_impl.hpp:134-256), with the window
  * masks built per word, and the transposition count of count_transpositions_block
@@ -2109,20 +2255,38 @@ RFG_HD int band_class_words(int i)
     return w[i];
 }
 
+/* The metrics the band kernel takes: unit-weight Levenshtein, and the LCS families
+ * (Indel, LCSseq, ratio), whose plans carry an Indel-distance bound K (plan_int) */
+RFG_HD bool band_metric(int metric, const ScoreParams& sp)
+{
+    if (metric == LEVENSHTEIN) return sp.ins == 1 && sp.del == 1 && sp.rep == 1;
+    return metric == INDEL || metric == LCSSEQ || metric == RATIO;
+}
+
 /* The choice lengths whose pairs with a pattern of m units pass the length filter
- * |m - n| <= K(n) (Levenshtein_impl.hpp:863) for unit-weight Levenshtein: [*nlo, *nhi]
- * within [1, max(m, maxlen)], and the largest bound *Kmax such a pair gets.  With unit
- * weights the maximum is max(m, n), so K is one value for every n <= m; for n > m,
- * K(n) - (n - m) does not grow with n (the distance ops: K(n) = ci or n - ci; the
- * normalized ops, cutoff c in [0, 1]: K(n) = ceil(fl(n c)) rises by at most 1 per unit
- * of n, fl being monotone and exact at integers), so the passing n > m form one run
- * that a binary search ends.  n = 0 never reaches the core.  Returns false when no
- * pair passes (or the cutoff is outside the range the argument covers). */
+ * |m - n| <= K(n) (Levenshtein_impl.hpp:863, LCSseq_impl.hpp:389) for a band metric:
+ * [*nlo, *nhi] within [1, max(m, maxlen)], holding every passing length (the rest of
+ * the interval may hold lengths that fail), and an upper bound *Kmax of the bound K any
+ * passing pair gets.
+ *   - n <= m: K(n) <= K(m) (Levenshtein, LCSseq distance and similarity: one value or
+ *     falling with m - n; Indel and ratio: K rises with n), so every passing n is at
+ *     least m - K(m);
+ *   - n > m: K(n) - (n - m) does not grow with n (the distance ops: K(n) = ci, n - ci,
+ *     m + n - ci, min(m + n, 2 ci - (n - m)) or m + n - 2 ci; the normalized ops, cutoff c in [0, 1]:
+ *     K(n) = ceil(fl(M c)) (LCSseq: twice that less n - m) rises by at most 1 per unit of
+ *     the maximum M, fl being monotone and exact at integers), so the passing n > m form
+ *     one run that a binary search ends.  K(n) there is largest at the run's end except
+ *     for LCSseq (normalized: K moves by +1 or -1 per unit of n; distance: K = m + n
+ *     while max(m, n) < ci, 2 ci - (n - m) after), whose run is scanned.
+ * n = 0 never reaches the core.  Returns false when no pair passes (or the cutoff is
+ * outside the range the argument covers). */
 RFG_HD bool band_range(int metric, int op, int form, const ScoreParams& sp, u64 ci, double cf, i64 m, i64 maxlen,
                        i64* nlo, i64* nhi, i64* Kmax)
 {
-    if (m < 1 || metric != LEVENSHTEIN || sp.ins != 1 || sp.del != 1 || sp.rep != 1 || form == FORM_MULTI) return false;
-    if ((op == NORM_DISTANCE || op == NORM_SIMILARITY) && !(cf >= 0.0 && cf <= 1.0)) return false;
+    if (m < 1 || !band_metric(metric, sp) || form == FORM_MULTI) return false;
+    if (metric == RATIO ? !(cf >= 0.0 && cf <= 100.0)
+                        : (op == NORM_DISTANCE || op == NORM_SIMILARITY) && !(cf >= 0.0 && cf <= 1.0))
+        return false;
     PairSpec s;
     s.metric = metric;
     s.op = op;
@@ -2157,7 +2321,16 @@ RFG_HD bool band_range(int metric, int op, int form, const ScoreParams& sp, u64 
         }
     }
     bool p;
-    const i64 Khi = bound(lo, &p);
+    i64 Khi = bound(lo, &p);
+    if (metric == LCSSEQ)
+        for (i64 n = m + 1; n < lo; ++n) {
+            const i64 k = bound(n, &p);
+            Khi = k > Khi ? k : Khi;
+            if (Khi > 1024) { /* no band class holds it: K <= m + n bounds the rest */
+                Khi = m + lo;
+                break;
+            }
+        }
     *nlo = m - Km > 1 ? m - Km : 1;
     *nhi = lo;
     *Kmax = Khi > Km ? Khi : Km;
@@ -2182,13 +2355,16 @@ RFG_HD int band_class(int metric, int op, int form, const ScoreParams& sp, u64 c
 
 /* The result of every pair of a band-class pattern that fails the length filter (the
  * chain's value for the pruned distance K + 1, which depends on neither length):
- * distance K + 1 with K the cutoff (fast: fast_k), similarity 0, normalized distance
- * 1.0, normalized similarity 0.0 -- the pruned-pair shortcut of dist_chain_finish,
- * which holds for cutoffs in [0, 1] (band_range refuses others). */
-RFG_HD void band_reject_value(int op, u64 ci, int fast, i64 fast_k, i64* vi, double* vf)
+ * distance K + 1 with K the cutoff (fast: fast_k; LCSseq: the LCS is 0, the distance the
+ * maximum, which exceeds the cutoff), similarity 0, normalized distance 1.0, normalized
+ * similarity and ratio 0.0 -- the pruned-pair shortcuts of dist_chain_finish and
+ * ratio_finish, which hold for cutoffs in [0, 1] (ratio: [0, 100]; band_range refuses
+ * others). */
+RFG_HD void band_reject_value(int metric, int op, u64 ci, int fast, i64 fast_k, i64* vi, double* vf)
 {
     *vi = 0;
     *vf = 0.0;
+    if (metric == RATIO) return;
     switch (op) {
     case DISTANCE: *vi = (fast ? fast_k : clamp_bound(ci)) + 1; break;
     case SIMILARITY: break;

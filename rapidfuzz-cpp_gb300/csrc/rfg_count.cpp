@@ -162,13 +162,14 @@ int rfg_count_word_steps2(int metric, const uint8_t* qd, const int64_t* qo, int6
     return 0;
 }
 
-/* Band classes of unit-weight Levenshtein (the band kernel, lev_band32) on one-byte
- * strings under the chain of `op` (rfg_op numbering) with the cutoff ci / cf: for every
+/* Band classes of unit-weight Levenshtein or of an LCS family (metric in rfg_metric
+ * numbering; the band kernel, lev_band32 / lcs_band32) on one-byte strings under the
+ * chain of `op` (rfg_op numbering) with the cutoff ci / cf: for every
  * pair of a band-class query that passes the length filter, the text units the core
  * fetches (steps) times the class's window words (*exec_words, what the kernel runs) and
  * times the words Ukkonen's band of the pair needs (*alg_words); *pairs counts those
  * pairs.  Queries outside the band classes are not counted. */
-int rfg_count_band_steps(int op, uint64_t ci, double cf, const uint8_t* qd, const int64_t* qo, int64_t nq,
+int rfg_count_band_steps(int metric, int op, uint64_t ci, double cf, const uint8_t* qd, const int64_t* qo, int64_t nq,
                          const uint8_t* cd, const int64_t* co, int64_t nc, int nthreads, uint64_t* exec_words,
                          uint64_t* alg_words, uint64_t* pairs)
 {
@@ -188,7 +189,7 @@ int rfg_count_band_steps(int op, uint64_t ci, double cf, const uint8_t* qd, cons
                 const int64_t qi = next.fetch_add(1);
                 if (qi >= nq) break;
                 const int m = (int)(qo[qi + 1] - qo[qi]);
-                const int bc = band_class(LEVENSHTEIN, op, FORM_CACHED, sp, ci, cf, m, maxlen);
+                const int bc = band_class(metric, op, FORM_CACHED, sp, ci, cf, m, maxlen);
                 if (bc < 0) continue;
                 const int B = band_class_words(bc);
                 const uint8_t* a = qd + qo[qi];
@@ -206,7 +207,7 @@ int rfg_count_band_steps(int op, uint64_t ci, double cf, const uint8_t* qd, cons
                     const uint32_t* operator()(u64 c) const { return base + rmap[c & 255]; }
                 } pm{rows.data(), rmap.data()};
                 PairSpec s;
-                s.metric = LEVENSHTEIN;
+                s.metric = metric;
                 s.op = op;
                 s.form = FORM_CACHED;
                 s.ci = ci;
@@ -223,7 +224,17 @@ int rfg_count_band_steps(int op, uint64_t ci, double cf, const uint8_t* qd, cons
                     if (K < diff || K >= m) continue;
                     int st = 0;
                     const Txt8 txt{cd + co[c]};
-                    switch (B) {
+                    if (metric != LEVENSHTEIN) switch (B) {
+                        case 1: lcs_band32<1>(pm, m, txt, n, (int)K, &st); break;
+                        case 2: lcs_band32<2>(pm, m, txt, n, (int)K, &st); break;
+                        case 3: lcs_band32<3>(pm, m, txt, n, (int)K, &st); break;
+                        case 4: lcs_band32<4>(pm, m, txt, n, (int)K, &st); break;
+                        case 6: lcs_band32<6>(pm, m, txt, n, (int)K, &st); break;
+                        case 8: lcs_band32<8>(pm, m, txt, n, (int)K, &st); break;
+                        case 12: lcs_band32<12>(pm, m, txt, n, (int)K, &st); break;
+                        default: lcs_band32<16>(pm, m, txt, n, (int)K, &st); break;
+                        }
+                    else switch (B) {
                     case 1: lev_band32<1>(pm, m, txt, n, (int)K, &st); break;
                     case 2: lev_band32<2>(pm, m, txt, n, (int)K, &st); break;
                     case 3: lev_band32<3>(pm, m, txt, n, (int)K, &st); break;

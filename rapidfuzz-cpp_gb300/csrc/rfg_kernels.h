@@ -21,9 +21,11 @@ const void* fast_kernel_lev(int width, bool half);
 const void* fast_hist_kernel();
 const void* fast_kernel_lcs(int width, bool half);
 const void* fast_kernel_osa(int width, bool half);
-/* k_band<CT, B> (banded unit-weight Levenshtein, B 32-bit words of band in
- * {1, 2, 3, 4, 6, 8, 12, 16}); one-byte choices only, nullptr otherwise */
-const void* band_kernel(int width, int B);
+/* k_band<CT, B, LCS> (banded unit-weight Levenshtein, or with lcs the banded LCS
+ * families; B 32-bit words of band in {1, 2, 3, 4, 6, 8, 12, 16}); one-byte choices only,
+ * nullptr otherwise */
+const void* band_kernel(int width, int B, bool lcs);
+const void* band_lcs_kernel(int B);
 /* queries per lane of k_fast */
 #ifndef RFG_FAST_LCS_Q
 #define RFG_FAST_LCS_Q 2 /* queries a lane scores for Indel (2 since the count filter makes the recurrence rare) */

@@ -109,6 +109,7 @@ def lib():
             "rfg_server_wait": ([vp, ctypes.c_uint64, ctypes.c_double, P(ctypes.c_double)], ctypes.c_int),
             "rfg_testing_fail_device_allocs": ([i64], ctypes.c_int),
             "rfg_testing_band_rounds": ([ctypes.c_int32], ctypes.c_int),
+            "rfg_testing_band_mode": ([ctypes.c_int32], ctypes.c_int),
             "rfg_server_stats": ([vp, P(i64), P(i64), P(i64)], ctypes.c_int),
             "rfg_server_destroy": ([vp], ctypes.c_int),
             "rfg_cdist_noalloc": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, P(Strings), P(Strings), i64, P(Params),

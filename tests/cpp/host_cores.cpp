@@ -156,16 +156,17 @@ int hc_group(int fam, int word32, const uint8_t* a1, int m1, const uint8_t* a2, 
     return 0;
 }
 
-/* the 32-bit banded core (lev_band32<B>) with the compact padded table of the band
- * kernel; B = 32-bit words of the window.  Returns -2 where the shape does not apply
- * (2K+1 > 32B, K >= m, |m-n| > K, or an empty string). */
+/* the 32-bit banded cores (lev_band32<B>, or with lcs lcs_band32<B>: the Indel distance)
+ * with the compact padded table of the band kernel; B = 32-bit words of the window.
+ * Returns -2 where the shape does not apply (band_bits > 32B, K >= m, |m-n| > K, or an
+ * empty string). */
 struct PM32 {
     const uint32_t* base;
     const int32_t* rmap;
     const uint32_t* operator()(uint64_t c) const { return base + rmap[c & 255]; }
 };
 
-int64_t hc_band32(int B, const uint8_t* a, int m, const uint8_t* b, int n, int64_t K)
+int64_t hc_band32(int lcs, int B, const uint8_t* a, int m, const uint8_t* b, int n, int64_t K)
 {
     if (m == 0 || n == 0 || K >= m || (m > n ? m - n : n - m) > K || band_bits((int)K, m - n) > 32 * B) return -2;
     const int W32 = (m + 31) / 32, pad = B + 1, S = W32 + 3 * pad;
@@ -178,6 +179,14 @@ int64_t hc_band32(int B, const uint8_t* a, int m, const uint8_t* b, int n, int64
     for (int c = 0; c < 256; ++c) rmap[c] = rmap[c] * S + pad;
     const PM32 pm{rows.data(), rmap.data()};
     const Txt t{b};
+    if (lcs) switch (B) {
+        case 1: return lcs_band32<1>(pm, m, t, n, (int)K);
+        case 2: return lcs_band32<2>(pm, m, t, n, (int)K);
+        case 3: return lcs_band32<3>(pm, m, t, n, (int)K);
+        case 4: return lcs_band32<4>(pm, m, t, n, (int)K);
+        case 8: return lcs_band32<8>(pm, m, t, n, (int)K);
+        case 16: return lcs_band32<16>(pm, m, t, n, (int)K);
+        }
     switch (B) {
     case 1: return lev_band32<1>(pm, m, t, n, (int)K);
     case 2: return lev_band32<2>(pm, m, t, n, (int)K);
@@ -207,25 +216,31 @@ int hc_hist_bound(int fam, const uint8_t* a, int m, const uint8_t* b, int n)
  * units, unit-weight Levenshtein, op / ci / cf the chain) and band_reject_value; and one
  * pair's plan as the band kernel makes it: *pass = the pair reaches the core, else
  * (vi, vf) = the chain's value of the pruned pair */
-int hc_band_range(int op, uint64_t ci, double cf, int64_t m, int64_t maxlen, int64_t* nlo, int64_t* nhi,
+int hc_band_range(int metric, int op, uint64_t ci, double cf, int64_t m, int64_t maxlen, int64_t* nlo, int64_t* nhi,
                   int64_t* kmax)
 {
     ScoreParams sp;
     sp.ins = sp.del = sp.rep = 1;
     sp.prefix_weight = 0.1;
-    return band_range(LEVENSHTEIN, op, FORM_CACHED, sp, ci, cf, m, maxlen, nlo, nhi, kmax) ? 1 : 0;
+    return band_range(metric, op, FORM_CACHED, sp, ci, cf, m, maxlen, nlo, nhi, kmax) ? 1 : 0;
 }
 
-void hc_band_reject(int op, uint64_t ci, int64_t* vi, double* vf)
+/* the kernels' fast chain (d <= K ? d : K + 1) serves the unit-weight distances:
+ * Levenshtein and Indel */
+void hc_band_reject(int metric, int op, uint64_t ci, int64_t* vi, double* vf)
 {
-    const int fast = op == DISTANCE;
-    band_reject_value(op, ci, fast, clamp_bound(ci), vi, vf);
+    const int fast = op == DISTANCE && (metric == LEVENSHTEIN || metric == INDEL);
+    band_reject_value(metric, op, ci, fast, clamp_bound(ci), vi, vf);
 }
 
-void hc_band_pair(int op, uint64_t ci, double cf, int64_t m, int64_t n, int* pass, int64_t* vi, double* vf)
+/* one pair as the band kernel stores it when the pair never reaches the core (raw: the
+ * pruned distance K + 1; the LCS families: the LCS -1) and whether it passes the length
+ * filter; K the plan's bound */
+void hc_band_pair(int metric, int op, uint64_t ci, double cf, int64_t m, int64_t n, int* pass, int64_t* vi, double* vf,
+                  int64_t* kout)
 {
     PairSpec s;
-    s.metric = LEVENSHTEIN;
+    s.metric = metric;
     s.op = op;
     s.form = FORM_CACHED;
     s.ci = ci;
@@ -238,11 +253,15 @@ void hc_band_pair(int op, uint64_t ci, double cf, int64_t m, int64_t n, int* pas
     const i64 K = pl.run ? pl.K : -1;
     const i64 diff = m > n ? m - n : n - m;
     *pass = K >= 0 && m > 0 && n > 0 && K >= diff;
+    *kout = K;
     i64 raw = 0;
     if (K >= 0) raw = m == 0 ? n : n == 0 ? m : K + 1;
     *vi = 0;
     *vf = 0.0;
-    if (op == DISTANCE) *vi = raw <= (i64)clamp_bound(ci) ? raw : clamp_bound(ci) + 1;
+    const bool lcs = metric != LEVENSHTEIN;
+    if (op == DISTANCE && (metric == LEVENSHTEIN || metric == INDEL))
+        *vi = raw <= (i64)clamp_bound(ci) ? raw : clamp_bound(ci) + 1;
+    else if (lcs) finish_int(s, pl, raw <= K ? (m + n - raw) >> 1 : -1, vi, vf);
     else finish_int(s, pl, raw, vi, vf);
 }
 

@@ -34,15 +34,15 @@ def libs():
     lib.hc_group.restype = I
     lib.hc_group.argtypes = [I, I, P, I, P, I, P, I, I64, I64, P]
     lib.hc_band32.restype = I64
-    lib.hc_band32.argtypes = [I, P, I, P, I, I64]
+    lib.hc_band32.argtypes = [I, I, P, I, P, I, I64]
     lib.hc_hist_bound.restype = I
     lib.hc_hist_bound.argtypes = [I, P, I, P, I]
     lib.hc_band_range.restype = I
-    lib.hc_band_range.argtypes = [I, ctypes.c_uint64, ctypes.c_double, I64, I64, P, P, P]
+    lib.hc_band_range.argtypes = [I, I, ctypes.c_uint64, ctypes.c_double, I64, I64, P, P, P]
     lib.hc_band_reject.restype = None
-    lib.hc_band_reject.argtypes = [I, ctypes.c_uint64, P, P]
+    lib.hc_band_reject.argtypes = [I, I, ctypes.c_uint64, P, P]
     lib.hc_band_pair.restype = None
-    lib.hc_band_pair.argtypes = [I, ctypes.c_uint64, ctypes.c_double, I64, I64, P, P, P]
+    lib.hc_band_pair.argtypes = [I, I, ctypes.c_uint64, ctypes.c_double, I64, I64, P, P, P, P]
     lib.hc_fast.restype = I
     lib.hc_fast.argtypes = [I, I, P, P, I, P, I, I, P]
     lib.hc_jaro.restype = I
@@ -152,19 +152,21 @@ def test_warp_tile_core_matches_oracle(libs, fam, word32):
             assert list(out)[:qn] == [d if d <= K else K + 1 for d in ds], (pats, b, K)
 
 
-def test_band32_core_matches_oracle(libs):
-    """lev_band32<B>: the 32-bit banded Levenshtein of the band kernel on Ukkonen's band
-    (about K + 2 diagonals), every window size, against the exact distance"""
+@pytest.mark.parametrize("lcs", [0, 1], ids=["levenshtein", "indel"])
+def test_band32_core_matches_oracle(libs, lcs):
+    """lev_band32<B> / lcs_band32<B>: the 32-bit banded Levenshtein and LCS (as the Indel
+    distance) of the band kernel on Ukkonen's band (about K + 2 diagonals), every window
+    size, against the exact distance"""
     lib, o = libs
-    rng = np.random.default_rng(77)
+    rng = np.random.default_rng(77 + lcs)
     lens = [40, 63, 64, 65, 100, 127, 128, 129, 200, 300, 513, 700]
     checked = 0
-    for a, b in pairs(78, 700, lens):
-        d = exact(o, 0, a, b)
-        for B in (1, 2, 4, 8, 16):
+    for a, b in pairs(78 + lcs, 700, lens):
+        d = exact(o, lcs, a, b)
+        for B in ((1, 2, 3, 4, 8, 16) if lcs else (1, 2, 4, 8, 16)):
             for K in sorted({int(rng.integers(0, 32 * B)), 32 * B - 2, 32 * B - 1, max(0, d - 1), d, d + 1,
                              abs(len(a) - len(b))}):
-                got = lib.hc_band32(B, a, len(a), b, len(b), K)
+                got = lib.hc_band32(lcs, B, a, len(a), b, len(b), K)
                 if got == -2:
                     continue
                 # the core gives d, or any value above K once d > K (the chain maps it to K + 1)
@@ -193,51 +195,68 @@ def test_count_filter_bound_never_exceeds_distance(libs):
     assert checked > 5000 and tight > 100
 
 
-def test_band_ranges_and_rejected_values(libs):
-    """the band launches' split of a query's pairs: the choice lengths that pass the
-    length filter are exactly band_range's [nlo, nhi] (so a query's passing pairs are one
-    run of the length-sorted choices), and every other pair's value is band_reject_value,
-    for all four ops and cutoffs from 0 to 1 (checked against the per-pair plan at every
-    length up to maxlen)"""
+# metric ids of the scorer enum (rfg_core.cuh)
+LEV_M, INDEL_M, LCSSEQ_M, RATIO_M = 0, 1, 2, 6
+
+
+@pytest.mark.parametrize("metric", [LEV_M, INDEL_M, LCSSEQ_M, RATIO_M], ids=["levenshtein", "indel", "lcsseq", "ratio"])
+def test_band_ranges_and_rejected_values(libs, metric):
+    """the band launches' split of a query's pairs: every choice length that passes the
+    length filter lies in band_range's [nlo, nhi] (so a query's passing pairs are one
+    run of the length-sorted choices; for unit-weight Levenshtein, whose bound is one
+    value for n <= m, the interval is exactly the passing lengths), Kmax bounds every
+    passing pair's K, and every pair outside the interval gets band_reject_value, for all
+    four ops (ratio: its one chain) and cutoffs across their range (checked against the
+    per-pair plan at every length up to maxlen)"""
     lib, _ = libs
-    rng = np.random.default_rng(91)
+    rng = np.random.default_rng(91 + metric)
     D, S, ND, NS = 0, 1, 2, 3
     lo, hi, km = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
-    ps, vi, vf = ctypes.c_int(), ctypes.c_int64(), ctypes.c_double()
+    ps, vi, vf, kk = ctypes.c_int(), ctypes.c_int64(), ctypes.c_double(), ctypes.c_int64()
     rvi, rvf = ctypes.c_int64(), ctypes.c_double()
     cases = 0
     for _ in range(400):
-        op = int(rng.integers(0, 4))
+        op = NS if metric == RATIO_M else int(rng.integers(0, 4))
         m = int(rng.choice([1, 2, 65, 100, 257, 300, 1000, 2000]))
         maxlen = int(rng.choice([0, 1, m // 2, m, m + 5, 2 * m, 3000]))
-        if op in (ND, NS):
+        if metric == RATIO_M:
+            cf = float(rng.choice([0.0, 1.0, 50.0, 80.0, 85.0, 90.0, 95.0 + 1e-9, 99.0, 100.0]))
+            ci = 0
+        elif op in (ND, NS):
             cf = float(rng.choice([0.0, 0.01, 0.05, 0.1, 0.1 + 1e-9, 0.18, 0.3, 0.5, 0.9, 0.99, 1.0]))
             ci = 0
         else:
-            ci = int(rng.choice([0, 1, 5, 30, m // 2, m, m + 3, 2**40]))
+            ci = int(rng.choice([0, 1, 5, 30, m // 2, m, m + 3, 2 * m - 1, 2**40]))
             cf = 0.0
-        ok = lib.hc_band_range(op, ci, cf, m, maxlen, ctypes.byref(lo), ctypes.byref(hi), ctypes.byref(km))
-        lib.hc_band_reject(op, ci, ctypes.byref(rvi), ctypes.byref(rvf))
+        ok = lib.hc_band_range(metric, op, ci, cf, m, maxlen, ctypes.byref(lo), ctypes.byref(hi), ctypes.byref(km))
+        lib.hc_band_reject(metric, op, ci, ctypes.byref(rvi), ctypes.byref(rvf))
         # the band classes take patterns whose band (Kmax + 2 bits) is narrower than m
         band = ok and km.value + 2 < m
         passing = []
         for n in range(0, max(m, maxlen) + 1):
-            lib.hc_band_pair(op, ci, cf, m, n, ctypes.byref(ps), ctypes.byref(vi), ctypes.byref(vf))
+            lib.hc_band_pair(metric, op, ci, cf, m, n, ctypes.byref(ps), ctypes.byref(vi), ctypes.byref(vf),
+                             ctypes.byref(kk))
             if ps.value:
                 passing.append(n)
-            elif not band:
+                if ok:
+                    assert kk.value <= km.value, (metric, op, ci, cf, m, n, kk.value, km.value)
+            elif not band or (lo.value <= n <= hi.value):
                 continue
-            elif op in (D, S):
-                assert vi.value == rvi.value, (op, ci, m, n, vi.value, rvi.value)
+            elif metric == RATIO_M or op in (ND, NS):
+                assert vf.value == rvf.value, (metric, op, cf, m, n, vf.value, rvf.value)
             else:
-                assert vf.value == rvf.value, (op, cf, m, n, vf.value, rvf.value)
+                assert vi.value == rvi.value, (metric, op, ci, m, n, vi.value, rvi.value)
         if not ok:
-            assert not passing, (op, ci, cf, m, maxlen)
+            assert not passing, (metric, op, ci, cf, m, maxlen)
             continue
-        expect = [n for n in range(0, max(m, maxlen) + 1) if lo.value <= n <= hi.value]
-        assert passing == expect, (op, ci, cf, m, maxlen, lo.value, hi.value)
+        assert all(lo.value <= n <= hi.value for n in passing), (metric, op, ci, cf, m, maxlen, lo.value, hi.value)
+        if metric == LEV_M:
+            expect = [n for n in range(0, max(m, maxlen) + 1) if lo.value <= n <= hi.value]
+            assert passing == expect, (op, ci, cf, m, maxlen, lo.value, hi.value)
+        else:
+            assert passing and passing[-1] == hi.value, (metric, op, ci, cf, m, maxlen, hi.value)
         cases += band
-    assert cases > 100
+    assert cases > 60
 
 
 def test_jaro_cores_match_oracle(libs):
