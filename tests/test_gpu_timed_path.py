@@ -117,3 +117,29 @@ def test_config4_all_choices():
         exp = oracle_cdist(m, R.SIMILARITY, q, c, cut)
         assert _same(got, exp), m
         assert (got > 0).sum() > 1000  # the derived choices give hits above the cutoff
+
+
+def test_long_dna_band_workloads_full_matrix():
+    """the long-DNA band workloads exactly as the bench times them (256 x 65,536 DNA,
+    seed 13): prepared batches over device strings, replayed as graphs, every element
+    against the oracle -- Levenshtein (k_band) and Indel / ratio (the LCS band classes)"""
+    torch = pytest.importorskip("torch")
+    q, c = WL.dna_lognormal(seed=13, nq=256, nc=65536)
+    dev = torch.device("cuda", 0)
+    td = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (q[0], q[1], c[0], c[1])]
+    qd = (td[0].data_ptr(), td[1].data_ptr(), 1, 256)
+    cd = (td[2].data_ptr(), td[3].data_ptr(), 1, 65536)
+    stream = torch.cuda.Stream(device=dev)
+    out = torch.empty((256, 65536), dtype=torch.float64, device=dev)
+    for metric, op, cut in ((R.LEVENSHTEIN, R.NORMALIZED_DISTANCE, 0.1), (R.INDEL, R.NORMALIZED_DISTANCE, 0.1),
+                            (R.RATIO, R.SIMILARITY, 90.0)):
+        b = R.Batch(metric, op, qd, cd, out.data_ptr(), cut, out_dtype=R.F64, flags=R.DEVICE_INPUTS)
+        assert any("k_band" in k for k in b.kernels()), b.kernels()
+        exp = oracle_cdist(metric, op, q, c, cut)
+        for _ in range(2):
+            out.fill_(-1.0)
+            b.launch(stream.cuda_stream, graph=True)
+            b.check(stream.cuda_stream)
+            got = out.cpu().numpy()
+            assert _same(got, exp), (metric, _mismatch(got, exp))
+        b.close()
