@@ -1678,6 +1678,10 @@ rfg_status score_pair_trip(int metric, int op, int form, const void* s1, int64_t
     a.sp = sp;
     a.ci = cut.cutoff_i;
     a.cf = cut.cutoff_f;
+    /* the one-pair calls carry the reference's score_hint (the batch calls have none) */
+    a.hint_i = cut.hint_i;
+    a.hint_f = cut.hint_f;
+    a.has_hint = 1;
     a.out = d + 48;
     a.out_dtype = dt;
     a.ld = 1;

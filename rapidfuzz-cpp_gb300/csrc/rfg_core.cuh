@@ -2116,6 +2116,27 @@ RFG_HD Plan plan_int(const PairSpec& s)
     return pl;
 }
 
+/* The first band of the score-hint doubling for a unit-weight Levenshtein pair: the
+ * caller's score_hint as a distance bound, converted by the op's chain the way the
+ * reference's wrappers convert it (distance.hpp: similarity hint -> maximum - hint,
+ * normalized hints -> ceil(maximum * hint) of the distance form).  Any value gives the
+ * same results (a band whose distance exceeds its bound is discarded); the hint only
+ * sets how much work the first band does. */
+RFG_HD i64 lev_hint_bound(const PairSpec& s, u64 hint_i, double hint_f)
+{
+    const u64 M = lev_maximum(s.l1, s.l2, s.p);
+    double c;
+    switch (s.op) {
+    case DISTANCE: return clamp_bound(hint_i);
+    case SIMILARITY: return hint_i >= M ? 0 : (i64)(M - hint_i);
+    case NORM_DISTANCE: c = hint_f; break;
+    default: c = dsub(1.0, hint_f);
+    }
+    if (!(c >= 0.0)) return 0;
+    if (!(c < 1.0)) return (i64)M;
+    return (i64)ceil_cut(M, c);
+}
+
 /* Finish for integer families.  raw: LEV/OSA/WF -> distance (> K when pruned);
  * LCS -> LCS length, or -1 when pruned.  Ignored when plan.run == 0. */
 RFG_HD void finish_int(const PairSpec& s, const Plan& pl, i64 raw, i64* oi, double* of)

@@ -47,6 +47,11 @@ struct KParams {
     ScoreParams sp;
     u64 ci;
     double cf;
+    /* the caller's score_hint (has_hint: given; the integer ops read hint_i, the
+     * normalized ones hint_f): the first band of the score-hint doubling */
+    u64 hint_i;
+    double hint_f;
+    int has_hint;
     void* out;
     int out_dtype; /* 0 i32, 1 i64, 2 f64 */
     int64_t ld;
@@ -475,6 +480,19 @@ __device__ __forceinline__ i64 run_int_core(const PMF& pm, int m, const TXT& t, 
     return lev_multi<W>(pm, m, t, n, K);
 }
 
+/* unit-weight Levenshtein of a pattern of W > 1 words with bound K (|m - n| <= K, n > 0):
+ * the 64-bit diagonal band of 2K + 1 bits when it is narrower than the pattern and at
+ * most 512 bits, else every word; the distance, or any value > K */
+template <typename PMW, typename TXT>
+__device__ __forceinline__ i64 lev_long_core(const PMW& pm, int W, int m, const TXT& txt, int n, i64 K, u64* st)
+{
+    if (K < m && 2 * K + 1 <= 64) return lev_band<1>(pm, W, m, txt, n, (int)K);
+    if (K < m && 2 * K + 1 <= 128) return lev_band<2>(pm, W, m, txt, n, (int)K);
+    if (K < m && 2 * K + 1 <= 256) return lev_band<4>(pm, W, m, txt, n, (int)K);
+    if (K < m && 2 * K + 1 <= 512) return lev_band<8>(pm, W, m, txt, n, (int)K);
+    return lev_multi_rt(pm, W, m, txt, n, K, st, st + W);
+}
+
 /* one (query, choice) pair of an integer-valued or Jaro family */
 /* per-query length tables (see JaroTab / chain_kd) */
 union LenTab {
@@ -873,11 +891,26 @@ __device__ __forceinline__ void score_pair_generic(const KParams& a, const u64* 
         else if (K < diff) raw = K + 1;
         else if (n == 0) raw = m;
         else if (FAM == FAM_OSA) raw = osa_multi_rt(pm, W, m, txt, n, K, st, st + W, st + 2 * W, st + 3 * W);
-        else if (K < m && 2 * K + 1 <= 64) raw = lev_band<1>(pm, W, m, txt, n, (int)K);
-        else if (K < m && 2 * K + 1 <= 128) raw = lev_band<2>(pm, W, m, txt, n, (int)K);
-        else if (K < m && 2 * K + 1 <= 256) raw = lev_band<4>(pm, W, m, txt, n, (int)K);
-        else if (K < m && 2 * K + 1 <= 512) raw = lev_band<8>(pm, W, m, txt, n, (int)K);
-        else raw = lev_multi_rt(pm, W, m, txt, n, K, st, st + W);
+        else {
+            /* the score-hint doubling of uniform_levenshtein_distance
+             * (Levenshtein_impl.hpp:876-897): bands of bound h, 2h, 4h ... below K first;
+             * the first whose distance fits its bound is exact */
+            i64 h = a.has_hint && m > 64 && K >= 4 && lev_mode(s.p) == LEV_UNIFORM && s.p.ins == 1
+                        ? lev_hint_bound(s, a.hint_i, a.hint_f)
+                        : K;
+            h = h > diff ? h : diff;
+            bool done = false;
+            while (h < K) {
+                const i64 d = lev_long_core(pm, W, m, txt, n, h, st);
+                if (d <= h) {
+                    raw = d;
+                    done = true;
+                    break;
+                }
+                h = h > K / 2 ? K : (h > 0 ? 2 * h : 1);
+            }
+            if (!done) raw = lev_long_core(pm, W, m, txt, n, K, st);
+        }
     }
     finish_int(s, pl, raw, &vi, &vf);
     emit(a, qi, ci, vi, vf, is_int, s.ci, s.cf, tl);
