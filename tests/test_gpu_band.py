@@ -70,10 +70,12 @@ def test_band_units_of_several_rounds_match_oracle(rounds):
     q, c = R.pack_strings(qs, 1), R.pack_strings(cs, 1)
     try:
         assert lib.rfg_testing_band_rounds(rounds) == 0
-        for op, cut in ((R.NORMALIZED_DISTANCE, 0.1), (R.DISTANCE, 40), (R.SIMILARITY, 600)):
-            got = R.cdist(R.LEVENSHTEIN, op, q, c, cut)
-            exp = oracle_cdist(R.LEVENSHTEIN, op, q, c, cut)
-            assert _same(got, exp), (rounds, op, cut)
+        for metric, op, cut in ((R.LEVENSHTEIN, R.NORMALIZED_DISTANCE, 0.1), (R.LEVENSHTEIN, R.DISTANCE, 40),
+                                (R.LEVENSHTEIN, R.SIMILARITY, 600), (R.INDEL, R.NORMALIZED_DISTANCE, 0.1),
+                                (R.LCSSEQ, R.DISTANCE, 40), (R.RATIO, R.SIMILARITY, 92.0)):
+            got = R.cdist(metric, op, q, c, cut)
+            exp = oracle_cdist(metric, op, q, c, cut)
+            assert _same(got, exp), (rounds, metric, op, cut)
     finally:
         lib.rfg_testing_band_rounds(0)
 
